@@ -1,0 +1,366 @@
+"""Benchmark: FP64 RK3 HLLC-MUSCL step throughput (cell-updates/s) on GB300.
+
+Workload (default): the isentropic vortex on a periodic [0,10]^2 box of
+1024x1024 quads with a seed-chosen half split into triangles (1,572,864 mixed
+cells), HLLC flux, MUSCL-linear reconstruction with the Venkatakrishnan
+limiter, SSP-RK3, CFL 0.8, global adaptive time step.  One "step" is one full
+reference time step: the stable time step (min over cells) and the three RK3
+stages (reconstruct, face flux, cell gather + stage update), all on the
+device.  Inputs are synthetic (seeded); the working set (~1.2 GB) is far
+larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+``--impl reference`` times the oracle (the C restatement of the reference's
+single-threaded CPU path) on the host cores for the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RK3 HLLC-MUSCL cell-updates/s"
+UNIT = "cell-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gpu", "reference"), default="gpu")
+    ap.add_argument("--workload", default="vortex1024", choices=("vortex1024", "vortex1024all", "vortex512", "vortex256"))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=5, help="RK3 steps of the CPU baseline sample")
+    ap.add_argument("--profile-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+WORKLOADS = {
+    "vortex1024": dict(n=1024, split="half"),
+    "vortex1024all": dict(n=1024, split="all"),
+    "vortex512": dict(n=512, split="half"),
+    "vortex256": dict(n=256, split="half"),
+}
+
+
+def make_workload(name):
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import cell_centroids, vortex_case, vortex_primitive
+
+    w = WORKLOADS[name]
+    case, _ = vortex_case(w["n"], split=w["split"])
+    settings = case.numerics
+    g = build_geometry(case.mesh, case)
+    P0 = vortex_primitive(cell_centroids(case.mesh))
+    config = {
+        "workload": f"isentropic vortex, periodic [0,10]^2, {w['n']}x{w['n']} quads, "
+                    f"{'half' if w['split'] == 'half' else 'all'} split to triangles, jitter 0.15h, seed 0",
+        "cells": int(len(g.areas)),
+        "faces": int(len(g.face_lengths)),
+        "interior_faces": int(len(g.interior_faces)),
+        "periodic_pairs": int(len(g.periodic_faces_a)),
+        "flux": settings.flux, "reconstruction": settings.reconstruction, "limiter": settings.limiter,
+        "time_integration": settings.time_integration, "cfl": settings.cfl,
+        "time_step_mode": settings.time_step_mode, "precision": "fp64, reference operation order (no FMA)",
+        "l2": "inputs larger than L2 (working set > 1 GB), no flush",
+        "parallelism": "replicas",
+    }
+    return case, settings, g, P0, config
+
+
+def model_bytes(g):
+    """Algorithmic bytes per launch group of each kernel class (the
+    reference 3-pass model: every array the reference algorithm produces or
+    consumes moves once).  C cells, F flux faces, E gradient entries, L
+    limiter entries."""
+    C = len(g.areas)
+    F = len(g.interior_faces) + len(g.periodic_faces_a) + len(g.wall_faces) + len(g.velocity_inlet_faces) \
+        + len(g.pressure_outlet_faces) + len(g.far_field_faces)
+    E = len(g.gradient_sources)
+    L = len(g.limiter_cells)
+    return {
+        "reconstruct": C * (32 + 64 + 32) + E * (4 + 16) + L * 16,
+        "flux": C * (32 + 64 + 32) + F * (8 + 16 + 8 + 32 + 32),
+        "gather": C * (32 + 32 + 32 + 8) + F * 32,
+        "time_step": C * (32 + 8) + F * (8 + 16 + 8),
+        "primitive": C * 64,
+    }, dict(C=C, F=F, E=E, L=L)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None}
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(g, settings, P0, steps):
+    """The oracle (C restatement of the reference path, one thread) on the same
+    mesh: ``steps`` full RK3 steps including the stable time step."""
+    from oracle.oracle import Oracle
+
+    orc = Oracle(g)
+    U = orc.conservative(P0, settings.gamma)
+    orc.solve(U, settings, 1)  # warm caches / page-in
+    t0 = time.perf_counter()
+    orc.solve(U, settings, steps)
+    dt = time.perf_counter() - t0
+    return len(g.areas) * steps / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    case, settings, g, P0, config = make_workload(args.workload)
+    steps, warm = args.steps, args.warmup
+    from oracle.oracle import Oracle
+
+    orc = Oracle(g)
+    U = orc.conservative(P0, settings.gamma)
+    U, _ = orc.solve(U, settings, warm)
+    t0 = time.perf_counter()
+    orc.solve(U, settings, steps)
+    elapsed = time.perf_counter() - t0
+    value = len(g.areas) * steps / elapsed
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * elapsed / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded vortex)",
+        "config": config,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{steps} RK3 steps of the full {len(g.areas)}-cell workload "
+                                   "(oracle: single-threaded C restatement of the reference path; "
+                                   "the reference itself is single-threaded NumPy/Numba)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    from meshcfd_gb300 import _lib
+    from meshcfd_gb300.device import DeviceGeometry, make_config
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+
+    case, settings, g, P0, config = make_workload(args.workload)
+    config["parallelism"] = f"replicas x{world}"
+    cfg = make_config(settings)
+    native = _lib.native()
+    dg = DeviceGeometry(g, device)
+    C = dg.n_cells
+    from oracle.oracle import Oracle  # only to build the seeded initial conservative state
+
+    U_init = Oracle(g).conservative(P0, settings.gamma)
+    U = torch.as_tensor(U_init, device=device)
+    dt = torch.empty(1, dtype=torch.float64, device=device)
+    P = dg.primitive_buffer()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        dg.time_steps(P, cfg, out_min=dt)
+        dg.explicit_step(U, cfg, 2, dt)
+
+    dg.primitive(U, cfg, out=P)
+    for _ in range(args.warmup):
+        step()
+    dg.check_status()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    launches0 = native.mcfd_launch_count()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(device.index) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        stop.record(stream)
+        barrier()
+    launches = native.mcfd_launch_count() - launches0
+    ms = start.elapsed_time(stop)
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    dg.check_status()
+    ms_per_step = ms / args.steps
+    value = world * C * args.steps / (ms * 1e-3)
+
+    # per-kernel breakdown (CUDA events on the launching stream)
+    import ctypes as Cc
+
+    native.mcfd_profile_enable(dg.handle, 1)
+    for _ in range(args.profile_steps):
+        step()
+    tot = (Cc.c_double * 6)()
+    grp = (Cc.c_int64 * 6)()
+    native.mcfd_profile_read(dg.handle, tot, grp)
+    native.mcfd_profile_enable(dg.handle, 0)
+    names = ("primitive", "reconstruct", "flux", "gather", "time_step", "other")
+    kernels = {names[k]: {"ms_total": tot[k], "groups": int(grp[k]),
+                          "ms_per_group": tot[k] / grp[k] if grp[k] else None} for k in range(6) if grp[k]}
+    total_ms = sum(v["ms_total"] for v in kernels.values())
+    for v in kernels.values():
+        v["share"] = v["ms_total"] / total_ms
+    mbytes, counts = model_bytes(g)
+    dominant = max(kernels, key=lambda k: kernels[k]["ms_total"])
+    peak, peak_kind = measured_peaks()
+    achieved = mbytes[dominant] / (kernels[dominant]["ms_per_group"] * 1e-3) / 1e9
+    traffic = None
+    tpath = ROOT / "profiles" / "ncu_traffic.json"
+    if tpath.exists():
+        per_cell = json.loads(tpath.read_text()).get("dram_bytes_per_cell", {}).get(dominant)
+        if per_cell:
+            traffic = per_cell * C
+    step_bytes = 3 * (mbytes["reconstruct"] + mbytes["flux"] + mbytes["gather"]) - 32 * C + mbytes["time_step"]
+    roofline = {
+        "bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+        "algorithmic_bytes_per_launch": mbytes[dominant],
+        "step_algorithmic_bytes_per_cell": step_bytes / C,
+        "step_achieved_gbs": step_bytes / (ms_per_step * 1e-3) / 1e9,
+        "step_frac": step_bytes / (ms_per_step * 1e-3) / 1e9 / peak,
+        "note": "FP64-ALU bound: GB300 FP64 ~0.5 T instr/s (measured), the step is far from the HBM roof",
+    }
+
+    # end to end: state in pinned host memory, H2D + step + D2H every step
+    e2e = None
+    if not args.no_e2e:
+        host = torch.as_tensor(U_init).pin_memory()
+        out = torch.empty_like(host).pin_memory()
+
+        def e2e_step():
+            U.copy_(host, non_blocking=True)
+            dg.primitive(U, cfg, out=P)
+            step()
+            out.copy_(U, non_blocking=True)
+
+        for _ in range(2):
+            e2e_step()
+        barrier()
+        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s2.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e2.record(stream)
+        barrier()
+        ms2 = s2.elapsed_time(e2)
+        dg.check_status()
+        e2e = {"value": world * C * args.steps / (ms2 * 1e-3), "unit": UNIT,
+               "h2d_bytes_per_step": int(host.numel() * 8), "d2h_bytes_per_step": int(out.numel() * 8),
+               "ms_per_step": ms2 / args.steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, secs = cpu_oracle_rate(g, settings, P0, args.cpu_steps)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_steps} RK3 steps of the same {C}-cell workload in {secs:.1f} s "
+                         "(oracle: single-threaded C restatement of the reference path)"}
+    clock = clocks.summary()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded vortex mesh and state)",
+            "config": config, "gpu_launches": int(launches), "roofline": roofline, "kernels": kernels,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clock,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,258 @@
+/*
+ * meshcfd_gb300 — C ABI of the GB300 (sm_103a) residual / time-step path.
+ *
+ * Every entry point takes plain pointers and sizes.  Device arrays are
+ * caller-owned CUDA device pointers; host arrays are ordinary host memory.
+ * Streams are passed as `void*` holding a `cudaStream_t` (NULL = legacy
+ * default stream).  Functions return 0 on success or an MCFD_E_* code; none of
+ * them traps or aborts.  Errors the numerics detect on the device (the
+ * reference's ValueError/SolverError cases) are accumulated in a per-geometry
+ * status word and returned by mcfd_status_fetch().
+ *
+ * State layout: conservative U and primitive P are (n_cells, 4) row-major
+ * float64 arrays — (rho, rho*u, rho*v, E) and (rho, u, v, p) — in the
+ * reference cell order (src/meshcfd/core/solver.py:2437-2442 takes and
+ * returns exactly this shape).  Cell, face and entry ids are never renumbered
+ * on output.
+ *
+ * The reference is a Python package whose hot path is the set of module
+ * functions cited below; a Python caller binds these entry points with
+ * ctypes.
+ */
+#ifndef MESHCFD_GB300_H
+#define MESHCFD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCFD_ABI_VERSION 1
+
+/* ---- return codes (host-side failures) ---- */
+#define MCFD_OK 0
+#define MCFD_E_ARG 1         /* invalid argument (null pointer, bad size or code) */
+#define MCFD_E_CUDA 2        /* a CUDA runtime call failed */
+#define MCFD_E_UNSUPPORTED 3 /* option outside what the GPU path implements */
+#define MCFD_E_GEOMETRY 4    /* geometry description inconsistent */
+
+/* ---- device status bits (numerical failures; reference messages) ---- */
+#define MCFD_S_NONPHYSICAL_STATE 0x01  /* euler.py:34-39 non-finite or non-positive rho/p */
+#define MCFD_S_NONFINITE_RESIDUAL 0x02 /* solver.py:2716-2717 */
+#define MCFD_S_HLLC_NONFINITE 0x04     /* euler.py:164-165 */
+#define MCFD_S_ROE_SOUND 0x08          /* euler.py:191-192 */
+#define MCFD_S_ROE_NONFINITE 0x10      /* euler.py:260-261 */
+#define MCFD_S_FARFIELD_SOUND 0x20     /* solver.py:4382-4383 */
+#define MCFD_S_FARFIELD_STATE 0x40     /* solver.py:4402-4407 */
+#define MCFD_S_TIME_STEP 0x80          /* solver.py:4341-4342 */
+
+typedef struct mcfd_status {
+  int32_t code;       /* OR of MCFD_S_* bits since the last fetch */
+  int32_t first_cell; /* lowest cell id that set a state/residual/time-step bit, or -1 */
+  int32_t first_face; /* lowest flux-face index that set a flux bit, or -1 */
+  int32_t reserved;
+} mcfd_status;
+
+/* ---- scheme codes ---- */
+#define MCFD_FLUX_RUSANOV 0 /* euler.py:80-93 */
+#define MCFD_FLUX_HLLC 1    /* euler.py:96-166, _kernels.py:71-160 */
+#define MCFD_FLUX_ROE 2     /* euler.py:169-262 */
+#define MCFD_RECON_FIRST_ORDER 0
+#define MCFD_RECON_MUSCL_LINEAR 1
+#define MCFD_RECON_MUSCL_PARABOLIC 2
+/* limiter codes are the reference's own (solver.py:2303-2308) */
+#define MCFD_LIMITER_BARTH_JESPERSEN 0
+#define MCFD_LIMITER_MINMOD 1
+#define MCFD_LIMITER_VAN_LEER 2
+#define MCFD_LIMITER_VENKATAKRISHNAN 3
+/* time integration (model.py:28-34) */
+#define MCFD_TIME_EULER 0
+#define MCFD_TIME_RK2 1
+#define MCFD_TIME_RK3 2
+#define MCFD_TIME_RK4 3 /* SSPRK(5,4), solver.py:1128-1182 */
+
+typedef struct mcfd_config {
+  int32_t flux;           /* MCFD_FLUX_* */
+  int32_t reconstruction; /* MCFD_RECON_* */
+  int32_t limiter;        /* MCFD_LIMITER_* */
+  int32_t exact;          /* 1: reference operation order, no FMA contraction */
+  double gamma;           /* ratio of specific heats (NumericalSettings.gamma) */
+  double acceleration_x;  /* body force (solver.py:2709-2715) */
+  double acceleration_y;
+  double cfl;             /* used by mcfd_time_steps */
+  double reserved[4];
+} mcfd_config;
+
+/*
+ * Geometry description: the arrays of the reference `_Geometry`
+ * (solver.py:123-177) that the inviscid residual and the time step read.
+ * Index arrays are int64 as NumPy produces them; all arrays are host memory
+ * and are copied by mcfd_geom_create (the caller may free them afterwards).
+ * Counts of zero allow NULL pointers.
+ */
+typedef struct mcfd_geom_desc {
+  int64_t n_cells;
+  int64_t n_faces;
+  const double* areas;           /* [n_cells] */
+  const double* face_normals;    /* [n_faces][2] */
+  const double* face_lengths;    /* [n_faces] */
+  const int64_t* owners;         /* [n_faces] */
+  const int64_t* neighbours;     /* [n_faces], -1 on boundary faces */
+  int64_t n_interior;
+  const int64_t* interior_faces; /* [n_interior] ascending face ids */
+  int64_t n_periodic;
+  const int64_t* periodic_faces_a; /* [n_periodic] */
+  const int64_t* periodic_faces_b; /* [n_periodic] */
+  int64_t n_wall;                  /* wall + symmetry faces, reference order */
+  const int64_t* wall_faces;
+  const double* wall_velocities;   /* [n_faces][2] (may be NULL: zero) */
+  int64_t n_velocity_inlet;
+  const int64_t* velocity_inlet_faces;
+  const double* velocity_inlet_states; /* [n][4] primitive */
+  int64_t n_pressure_outlet;
+  const int64_t* pressure_outlet_faces;
+  const double* pressure_outlet_pressures; /* [n] */
+  int64_t n_far_field;
+  const int64_t* far_field_faces;
+  const double* far_field_states; /* [n][4] primitive */
+  int64_t n_gradient;             /* least-squares entries, reference order */
+  const int64_t* gradient_sources;
+  const int64_t* gradient_neighbours;
+  const double* gradient_coefficients_x;
+  const double* gradient_coefficients_y;
+  int64_t n_limiter;              /* must equal n_faces + n_interior */
+  const int64_t* limiter_cells;
+  const double* limiter_dx;
+  const double* limiter_dy;
+} mcfd_geom_desc;
+
+typedef struct mcfd_geom mcfd_geom; /* opaque device geometry + workspace */
+
+typedef struct mcfd_geom_info {
+  int64_t n_cells, n_faces, n_interior, n_periodic, n_boundary_flux;
+  int64_t n_flux_faces;     /* interior + periodic + wall + inlet/outlet/far faces */
+  int64_t n_gradient, n_limiter;
+  int64_t device_bytes;     /* device memory held by the handle */
+} mcfd_geom_info;
+
+/* Library version (MCFD_ABI_VERSION). */
+int mcfd_abi_version(void);
+/* Short description of a return code. */
+const char* mcfd_error_string(int code);
+
+/*
+ * Build the device geometry (CSR gathers in reference accumulation order,
+ * face segments, workspace) on the current CUDA device.  Replaces the
+ * reference's per-call use of `_Geometry` arrays inside `_residual`
+ * (solver.py:2437-2718) and `_stable_time_steps` (solver.py:4132-4343).
+ */
+int mcfd_geom_create(const mcfd_geom_desc* desc, mcfd_geom** out);
+int mcfd_geom_destroy(mcfd_geom* geom);
+int mcfd_geom_get_info(const mcfd_geom* geom, mcfd_geom_info* info);
+
+/*
+ * P = conservative_to_primitive(U) with the positivity check
+ * (euler.py:20-40; solver.py:1620-1629).  U, P: device [n_cells][4].
+ */
+int mcfd_primitive(mcfd_geom* geom, const mcfd_config* cfg, const double* U, double* P,
+                   void* stream);
+
+/*
+ * R = _residual(U, geometry, settings) (solver.py:2437-2718) for inviscid
+ * flow: reconstruction (first order / MUSCL linear with the four limiters),
+ * Rusanov/HLLC/Roe fluxes on interior, periodic, wall/symmetry,
+ * velocity-inlet, pressure-outlet and far-field faces, body force and the
+ * finiteness check.  U, R: device [n_cells][4].  R may be NULL (the status
+ * word is still updated).
+ */
+int mcfd_residual(mcfd_geom* geom, const mcfd_config* cfg, const double* U, double* R,
+                  void* stream);
+
+/*
+ * Local stable time steps (solver.py:4132-4343, inviscid part) from the
+ * primitive state P.  dt_cells (device [n_cells], may be NULL) receives
+ * CFL*A_i/Sigma_i; dt_min (device scalar, may be NULL) receives
+ * min(min_i dt_i, time_limit) — pass time_limit = end_time - time for the
+ * reference's global adaptive step (solver.py:455-461), or +inf.
+ */
+int mcfd_time_steps(mcfd_geom* geom, const mcfd_config* cfg, const double* P,
+                    double* dt_cells, double* dt_min, double time_limit, void* stream);
+
+/*
+ * One explicit step in place: U <- step(U).  `scheme` is MCFD_TIME_*
+ * (explicit Euler solver.py:532-565, SSP-RK2 566-674, SSP-RK3 675-806,
+ * SSPRK(5,4) 1128-1182).  dt: device pointer to one float64 (global step)
+ * or to [n_cells] (dt_per_cell = 1, local steady mode, _scale_cell_rate
+ * solver.py:1119-1125).  Every stage is fused: reconstruction, face flux,
+ * cell gather + stage combination + primitive recovery of the new stage.
+ * After the call the handle's primitive buffer holds P(U_new).
+ */
+int mcfd_explicit_step(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, double* U,
+                       const double* dt, int32_t dt_per_cell, void* stream);
+
+/* Device pointer to the handle's primitive buffer [n_cells][4] (valid after
+ * mcfd_primitive / mcfd_residual / mcfd_explicit_step on the same handle). */
+const double* mcfd_geom_primitive(const mcfd_geom* geom);
+
+/*
+ * Sum over cells of R[i][k]^2 for k = 0..3 into the device array sums[4]
+ * (deterministic two-level tree).  The reference's per-component RMS
+ * residual is sqrt(sums[k] / n_cells) (solver.py:944-950).
+ */
+int mcfd_residual_sumsq(mcfd_geom* geom, const double* R, double* sums, void* stream);
+
+/*
+ * Wait for `stream`, then return and clear the accumulated device status.
+ */
+int mcfd_status_fetch(mcfd_geom* geom, void* stream, mcfd_status* out);
+
+/* ---- measurement ---- */
+
+/* kernel classes for mcfd_profile_read */
+#define MCFD_PROF_PRIMITIVE 0
+#define MCFD_PROF_RECONSTRUCT 1
+#define MCFD_PROF_FLUX 2
+#define MCFD_PROF_GATHER 3
+#define MCFD_PROF_TIME_STEP 4
+#define MCFD_PROF_OTHER 5
+#define MCFD_PROF_COUNT 6
+
+/*
+ * When enabled, every kernel launch group of this handle is bracketed by CUDA
+ * events recorded on its launching stream.  mcfd_profile_read waits for the
+ * last event, writes per-class total milliseconds and launch-group counts
+ * (arrays of MCFD_PROF_COUNT), and clears the record.
+ */
+int mcfd_profile_enable(mcfd_geom* geom, int32_t enable);
+int mcfd_profile_read(mcfd_geom* geom, double* total_ms, int64_t* groups);
+
+/* Number of kernels this library has launched in the process so far. */
+int64_t mcfd_launch_count(void);
+
+/* ---- host helpers (no GPU needed) ---- */
+
+/*
+ * Cell centroids and areas by the shoelace formula in the reference's
+ * operation order (solver.py:1655-1676).  Returns MCFD_E_GEOMETRY and sets
+ * *bad_cell for a zero/invalid area ("Cell {id} has zero or invalid area.").
+ */
+int mcfd_host_cell_geometry(int64_t n_cells, const int64_t* cell_offsets,
+                            const int64_t* cell_nodes, const double* points, double* centers,
+                            double* areas, int64_t* bad_cell);
+
+/*
+ * Face centres, unit normals pointing out of the owner, and lengths
+ * (solver.py:1678-1695).  The length is sqrt(fma(ey, ey, ex*ex)) and the
+ * orientation test fma(n_y, d_y, n_x*d_x) — the FMA-based BLAS dot the
+ * reference's np.linalg.norm / np.dot resolve to on FMA hardware.
+ */
+int mcfd_host_face_geometry(int64_t n_faces, const int64_t* face_nodes, const double* points,
+                            const double* centers, const int64_t* owners, double* face_centers,
+                            double* normals, double* lengths, int64_t* bad_face);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MESHCFD_GB300_H */

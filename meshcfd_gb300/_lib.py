@@ -1,0 +1,165 @@
+"""ctypes binding of the native library (include/meshcfd_gb300.h).
+
+The library is built in-tree by :mod:`meshcfd_gb300.build`.  Loading fails
+loudly when it is missing: there is no CPU fallback for anything here.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+from .build import BUILD, LIBNAME
+
+_lock = threading.Lock()
+_native = None
+
+c_i32, c_i64, c_dbl, c_vp = C.c_int32, C.c_int64, C.c_double, C.c_void_p
+P_i64 = C.POINTER(C.c_int64)
+P_dbl = C.POINTER(C.c_double)
+
+
+class Status(C.Structure):
+    _fields_ = [("code", c_i32), ("first_cell", c_i32), ("first_face", c_i32), ("reserved", c_i32)]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("flux", c_i32),
+        ("reconstruction", c_i32),
+        ("limiter", c_i32),
+        ("exact", c_i32),
+        ("gamma", c_dbl),
+        ("acceleration_x", c_dbl),
+        ("acceleration_y", c_dbl),
+        ("cfl", c_dbl),
+        ("reserved", c_dbl * 4),
+    ]
+
+
+class GeomDesc(C.Structure):
+    _fields_ = [
+        ("n_cells", c_i64), ("n_faces", c_i64),
+        ("areas", P_dbl), ("face_normals", P_dbl), ("face_lengths", P_dbl),
+        ("owners", P_i64), ("neighbours", P_i64),
+        ("n_interior", c_i64), ("interior_faces", P_i64),
+        ("n_periodic", c_i64), ("periodic_faces_a", P_i64), ("periodic_faces_b", P_i64),
+        ("n_wall", c_i64), ("wall_faces", P_i64), ("wall_velocities", P_dbl),
+        ("n_velocity_inlet", c_i64), ("velocity_inlet_faces", P_i64), ("velocity_inlet_states", P_dbl),
+        ("n_pressure_outlet", c_i64), ("pressure_outlet_faces", P_i64), ("pressure_outlet_pressures", P_dbl),
+        ("n_far_field", c_i64), ("far_field_faces", P_i64), ("far_field_states", P_dbl),
+        ("n_gradient", c_i64), ("gradient_sources", P_i64), ("gradient_neighbours", P_i64),
+        ("gradient_coefficients_x", P_dbl), ("gradient_coefficients_y", P_dbl),
+        ("n_limiter", c_i64), ("limiter_cells", P_i64), ("limiter_dx", P_dbl), ("limiter_dy", P_dbl),
+    ]
+
+
+class GeomInfo(C.Structure):
+    _fields_ = [
+        ("n_cells", c_i64), ("n_faces", c_i64), ("n_interior", c_i64), ("n_periodic", c_i64),
+        ("n_boundary_flux", c_i64), ("n_flux_faces", c_i64), ("n_gradient", c_i64),
+        ("n_limiter", c_i64), ("device_bytes", c_i64),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/meshcfd_gb300.h declares.
+SIGNATURES = {
+    "mcfd_abi_version": (c_i32, []),
+    "mcfd_error_string": (C.c_char_p, [c_i32]),
+    "mcfd_geom_create": (c_i32, [C.POINTER(GeomDesc), C.POINTER(c_vp)]),
+    "mcfd_geom_destroy": (c_i32, [c_vp]),
+    "mcfd_geom_get_info": (c_i32, [c_vp, C.POINTER(GeomInfo)]),
+    "mcfd_primitive": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp]),
+    "mcfd_residual": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp]),
+    "mcfd_time_steps": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_dbl, c_vp]),
+    "mcfd_explicit_step": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp]),
+    "mcfd_geom_primitive": (c_vp, [c_vp]),
+    "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
+    "mcfd_profile_enable": (c_i32, [c_vp, c_i32]),
+    "mcfd_profile_read": (c_i32, [c_vp, P_dbl, P_i64]),
+    "mcfd_launch_count": (c_i64, []),
+    "mcfd_host_cell_geometry": (c_i32, [c_i64, P_i64, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
+    "mcfd_host_face_geometry": (c_i32, [c_i64, P_i64, P_dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
+}
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def _ptr(a: np.ndarray, kind):
+    return a.ctypes.data_as(kind) if a is not None and a.size else None
+
+
+class Native:
+    """Thin wrapper: raw ctypes functions plus NumPy-friendly host helpers."""
+
+    def __init__(self, path: Path):
+        self.path = path
+        self.lib = C.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(self.lib, name)
+            fn.restype = res
+            fn.argtypes = args
+            setattr(self, name, fn)
+
+    def check(self, rc: int, what: str) -> None:
+        if rc != 0:
+            raise NativeError(f"{what}: {self.mcfd_error_string(rc).decode()} (code {rc})")
+
+    def cell_geometry(self, offsets, nodes, points):
+        from .errors import SolverError
+
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        nodes = np.ascontiguousarray(nodes, dtype=np.int64)
+        points = np.ascontiguousarray(points, dtype=np.float64)
+        n = len(offsets) - 1
+        centers = np.empty((n, 2))
+        areas = np.empty(n)
+        bad = C.c_int64(-1)
+        rc = self.mcfd_host_cell_geometry(n, _ptr(offsets, P_i64), _ptr(nodes, P_i64), _ptr(points, P_dbl),
+                                          _ptr(centers, P_dbl), _ptr(areas, P_dbl), C.byref(bad))
+        if rc == 4:
+            raise SolverError(f"Cell {bad.value} has zero or invalid area.")
+        self.check(rc, "cell geometry")
+        return centers, areas
+
+    def face_geometry(self, faces, points, centers, owners):
+        from .errors import SolverError
+
+        faces = np.ascontiguousarray(faces, dtype=np.int64)
+        owners = np.ascontiguousarray(owners, dtype=np.int64)
+        n = len(faces)
+        fc = np.empty((n, 2))
+        normals = np.empty((n, 2))
+        lengths = np.empty(n)
+        bad = C.c_int64(-1)
+        rc = self.mcfd_host_face_geometry(n, _ptr(faces, P_i64), _ptr(np.ascontiguousarray(points), P_dbl),
+                                          _ptr(np.ascontiguousarray(centers), P_dbl), _ptr(owners, P_i64),
+                                          _ptr(fc, P_dbl), _ptr(normals, P_dbl), _ptr(lengths, P_dbl), C.byref(bad))
+        if rc == 4:
+            raise SolverError(f"Face {bad.value} has zero or invalid length.")
+        self.check(rc, "face geometry")
+        return fc, normals, lengths
+
+
+def library_path() -> Path:
+    return BUILD / LIBNAME
+
+
+def native() -> Native:
+    """Load (building first if the sources are newer) the native library."""
+    global _native
+    with _lock:
+        if _native is None:
+            from .build import build
+
+            path = build()
+            if not path.exists():
+                raise NativeError(f"native library missing: {path}")
+            _native = Native(path)
+        return _native

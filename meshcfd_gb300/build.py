@@ -1,0 +1,78 @@
+"""Compile the native library for sm_103a (in-tree, no build system needed).
+
+``python -m meshcfd_gb300.build`` or :func:`build` writes
+``meshcfd_gb300/_build/libmeshcfd_gb300.so``.  The kernel translation unit is
+compiled with ``-fmad=false`` (reference operation order); host code with
+``-ffp-contract=off`` (GCC on aarch64 would otherwise contract a*b+c).
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+CSRC = HERE / "csrc"
+BUILD = HERE / "_build"
+LIBNAME = "libmeshcfd_gb300.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# (source, extra flags)
+UNITS = [
+    ("mcfd_kernels.cu", ["-fmad=false"]),
+    ("mcfd_api.cu", []),
+]
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(path).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build meshcfd_gb300")
+    return path
+
+
+def _sources_newer(target: Path) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    deps = list(CSRC.glob("*")) + [HERE.parent / "include" / "meshcfd_gb300.h", Path(__file__)]
+    return any(p.stat().st_mtime > t for p in deps if p.exists())
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    target = BUILD / LIBNAME
+    if not force and not _sources_newer(target):
+        return target
+    common = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3"]
+
+    def compile_unit(unit):
+        src, extra = unit
+        obj = BUILD / (Path(src).stem + ".o")
+        cmd = [*common, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+        return obj, res.stderr
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as pool:
+        results = list(pool.map(compile_unit, UNITS))
+    if verbose:
+        for _, log in results:
+            sys.stderr.write(log)
+    tmp = BUILD / (LIBNAME + f".tmp{os.getpid()}")
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *[str(o) for o, _ in results]]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, target)
+    return target
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

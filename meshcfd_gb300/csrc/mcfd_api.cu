@@ -1,0 +1,727 @@
+// C ABI of the residual / explicit-step path: geometry packing (host), device
+// workspace, and the orchestration of kernels per entry point.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#include "mcfd_internal.h"
+
+using namespace mcfd;
+
+struct ProfRecord {
+  int cls;
+  cudaEvent_t start, stop;
+};
+
+struct mcfd_geom {
+  DevGeom g;
+  bool profiling = false;
+  std::vector<ProfRecord> records;
+  std::vector<cudaEvent_t> event_pool;
+  Workspace ws;
+  void* arena = nullptr;       // one device allocation for geometry + workspace
+  size_t arena_bytes = 0;
+  DevStatus* status = nullptr;  // inside the arena
+  DevStatus* host_status = nullptr;  // pinned
+  mcfd_geom_info info{};
+};
+
+namespace {
+
+constexpr int64_t kMaxIndex = (int64_t)1 << 30;
+
+struct Arena {
+  std::vector<std::pair<size_t, size_t>> pieces;  // offset, bytes
+  size_t size = 0;
+  size_t take(size_t bytes) {
+    size_t off = (size + 255) & ~(size_t)255;
+    size = off + (bytes ? bytes : 1);
+    return off;
+  }
+};
+
+// Stable counting sort of entries by key; returns CSR pointers and the order.
+void group_by(const std::vector<int>& key, int n_keys, std::vector<int>& ptr, std::vector<int>& order) {
+  ptr.assign(n_keys + 1, 0);
+  for (int k : key) ptr[k + 1]++;
+  for (int i = 0; i < n_keys; ++i) ptr[i + 1] += ptr[i];
+  order.resize(key.size());
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (size_t e = 0; e < key.size(); ++e) order[fill[key[e]]++] = (int)e;
+}
+
+bool in_range(int64_t v, int64_t n) { return v >= 0 && v < n; }
+
+}  // namespace
+
+
+// ---- helpers (C++ linkage)
+static int check_cfg(const mcfd_config* cfg) {
+  if (!cfg) return MCFD_E_ARG;
+  if (cfg->flux < 0 || cfg->flux > 2) return MCFD_E_ARG;
+  if (cfg->limiter < 0 || cfg->limiter > 3) return MCFD_E_ARG;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC) return MCFD_E_UNSUPPORTED;
+  if (cfg->reconstruction < 0 || cfg->reconstruction > 2) return MCFD_E_ARG;
+  if (!(cfg->gamma > 1.0)) return MCFD_E_ARG;
+  return MCFD_OK;
+}
+
+static int rc(cudaError_t e) { return e == cudaSuccess ? MCFD_OK : MCFD_E_CUDA; }
+
+static cudaEvent_t take_event(mcfd_geom* h) {
+  if (!h->event_pool.empty()) {
+    cudaEvent_t e = h->event_pool.back();
+    h->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Runs `launch` (returning cudaError_t), bracketed by events when profiling.
+template <typename F>
+static cudaError_t timed(mcfd_geom* h, int cls, cudaStream_t s, F&& launch) {
+  if (!h->profiling) return launch();
+  ProfRecord r{cls, take_event(h), take_event(h)};
+  cudaEventRecord(r.start, s);
+  cudaError_t e = launch();
+  cudaEventRecord(r.stop, s);
+  h->records.push_back(r);
+  return e;
+}
+
+// One residual evaluation of the state whose primitive is in ws.P, followed
+// by the gather with the given stage program.
+static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgram& prog,
+                         cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  if (cfg.reconstruction == MCFD_RECON_MUSCL_LINEAR)
+    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return launch_reconstruct(h->g, cfg, h->ws.P, h->ws.recon, s); });
+  if (e == cudaSuccess)
+    e = timed(h, MCFD_PROF_FLUX, s, [&] { return launch_flux(h->g, cfg, h->ws.P, h->ws.recon, h->ws.flux, s); });
+  if (e == cudaSuccess)
+    e = timed(h, MCFD_PROF_GATHER, s, [&] { return launch_gather(h->g, cfg, h->ws.P, h->ws.flux, prog, s); });
+  return e;
+}
+
+static StageTerm term(int kind, double coef, const double* x) {
+  StageTerm t;
+  t.kind = kind;
+  t.coef = coef;
+  t.x = x;
+  return t;
+}
+
+extern "C" {
+
+int mcfd_abi_version(void) { return MCFD_ABI_VERSION; }
+
+const char* mcfd_error_string(int code) {
+  switch (code) {
+    case MCFD_OK: return "ok";
+    case MCFD_E_ARG: return "invalid argument";
+    case MCFD_E_CUDA: return "CUDA runtime error";
+    case MCFD_E_UNSUPPORTED: return "option not supported by the GPU path";
+    case MCFD_E_GEOMETRY: return "inconsistent geometry description";
+    default: return "unknown error";
+  }
+}
+
+int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
+  if (!d || !out) return MCFD_E_ARG;
+  *out = nullptr;
+  const int64_t C = d->n_cells, F = d->n_faces, NI = d->n_interior, NP = d->n_periodic;
+  const int64_t NW = d->n_wall, NV = d->n_velocity_inlet, NO = d->n_pressure_outlet,
+                NF = d->n_far_field, NG = d->n_gradient, NL = d->n_limiter;
+  if (C <= 0 || F < 0 || C > kMaxIndex || F > kMaxIndex || NG > kMaxIndex) return MCFD_E_ARG;
+  if (NL != F + NI) return MCFD_E_GEOMETRY;
+  if (!d->areas || !d->owners || !d->neighbours || (F && (!d->face_normals || !d->face_lengths)))
+    return MCFD_E_ARG;
+  // ---- validate indices (so no kernel can index out of bounds)
+  for (int64_t f = 0; f < F; ++f) {
+    if (!in_range(d->owners[f], C)) return MCFD_E_GEOMETRY;
+    if (d->neighbours[f] >= C) return MCFD_E_GEOMETRY;
+  }
+  for (int64_t i = 0; i < NI; ++i) {
+    int64_t f = d->interior_faces[i];
+    if (!in_range(f, F) || d->neighbours[f] < 0) return MCFD_E_GEOMETRY;
+    if (i > 0 && f <= d->interior_faces[i - 1]) return MCFD_E_GEOMETRY;
+  }
+  auto check_faces = [&](const int64_t* faces, int64_t n) {
+    for (int64_t i = 0; i < n; ++i)
+      if (!in_range(faces[i], F) || d->neighbours[faces[i]] >= 0) return false;
+    return true;
+  };
+  if (!check_faces(d->periodic_faces_a, NP) || !check_faces(d->periodic_faces_b, NP) ||
+      !check_faces(d->wall_faces, NW) || !check_faces(d->velocity_inlet_faces, NV) ||
+      !check_faces(d->pressure_outlet_faces, NO) || !check_faces(d->far_field_faces, NF))
+    return MCFD_E_GEOMETRY;
+  for (int64_t e = 0; e < NG; ++e)
+    if (!in_range(d->gradient_sources[e], C) || !in_range(d->gradient_neighbours[e], C))
+      return MCFD_E_GEOMETRY;
+  for (int64_t s = 0; s < NL; ++s)
+    if (!in_range(d->limiter_cells[s], C)) return MCFD_E_GEOMETRY;
+  for (int64_t c = 0; c < C; ++c)
+    if (!(d->areas[c] > 0.0)) return MCFD_E_GEOMETRY;
+
+  // ---- flux faces
+  const int64_t n_flux = NI + NP + NW + NV + NO + NF;
+  if (n_flux > kMaxIndex) return MCFD_E_ARG;
+  int seg_begin[SEG_COUNT + 1];
+  seg_begin[SEG_INTERIOR] = 0;
+  seg_begin[SEG_PERIODIC] = (int)NI;
+  seg_begin[SEG_WALL] = (int)(NI + NP);
+  seg_begin[SEG_VIN] = (int)(NI + NP + NW);
+  seg_begin[SEG_POUT] = (int)(NI + NP + NW + NV);
+  seg_begin[SEG_FAR] = (int)(NI + NP + NW + NV + NO);
+  seg_begin[SEG_COUNT] = (int)n_flux;
+  std::vector<int> lslot(n_flux), rslot(n_flux, -1), lcell(n_flux), rcell(n_flux, -1);
+  std::vector<double> normal(2 * n_flux), wallv(2 * NW, 0.0), vin(4 * NV), pout(NO), far(4 * NF);
+  auto set_face = [&](int64_t k, int64_t f) {
+    lslot[k] = (int)f;
+    lcell[k] = (int)d->owners[f];
+    normal[2 * k] = d->face_normals[2 * f];
+    normal[2 * k + 1] = d->face_normals[2 * f + 1];
+  };
+  for (int64_t i = 0; i < NI; ++i) {
+    int64_t f = d->interior_faces[i];
+    set_face(i, f);
+    rslot[i] = (int)(F + i);
+    rcell[i] = (int)d->neighbours[f];
+  }
+  for (int64_t i = 0; i < NP; ++i) {
+    int64_t k = seg_begin[SEG_PERIODIC] + i;
+    set_face(k, d->periodic_faces_a[i]);
+    rslot[k] = (int)d->periodic_faces_b[i];
+    rcell[k] = (int)d->owners[d->periodic_faces_b[i]];
+  }
+  for (int64_t i = 0; i < NW; ++i) {
+    int64_t f = d->wall_faces[i];
+    set_face(seg_begin[SEG_WALL] + i, f);
+    if (d->wall_velocities) {
+      wallv[2 * i] = d->wall_velocities[2 * f];
+      wallv[2 * i + 1] = d->wall_velocities[2 * f + 1];
+    }
+  }
+  for (int64_t i = 0; i < NV; ++i) {
+    set_face(seg_begin[SEG_VIN] + i, d->velocity_inlet_faces[i]);
+    for (int k = 0; k < 4; ++k) vin[4 * i + k] = d->velocity_inlet_states[4 * i + k];
+  }
+  for (int64_t i = 0; i < NO; ++i) {
+    set_face(seg_begin[SEG_POUT] + i, d->pressure_outlet_faces[i]);
+    pout[i] = d->pressure_outlet_pressures[i];
+  }
+  for (int64_t i = 0; i < NF; ++i) {
+    set_face(seg_begin[SEG_FAR] + i, d->far_field_faces[i]);
+    for (int k = 0; k < 4; ++k) far[4 * i + k] = d->far_field_states[4 * i + k];
+  }
+
+  // ---- cell gather, interior part: the SciPy CSR divergence operator
+  // (solver.py:2160-2174) with data (-L)/A_owner and L/A_neighbour, summed per
+  // row in ascending face (column) order.
+  std::vector<int> key, gi_ptr, order;
+  std::vector<int> gi_flux;
+  std::vector<double> gi_coef;
+  {
+    key.resize(2 * NI);
+    std::vector<double> coef(2 * NI);
+    std::vector<int> col(2 * NI);
+    for (int64_t i = 0; i < NI; ++i) {
+      int64_t f = d->interior_faces[i];
+      int64_t o = d->owners[f], n = d->neighbours[f];
+      double L = d->face_lengths[f];
+      key[2 * i] = (int)o;
+      coef[2 * i] = -L / d->areas[o];
+      col[2 * i] = (int)i;
+      key[2 * i + 1] = (int)n;
+      coef[2 * i + 1] = L / d->areas[n];
+      col[2 * i + 1] = (int)i;
+    }
+    group_by(key, (int)C, gi_ptr, order);
+    gi_flux.resize(order.size());
+    gi_coef.resize(order.size());
+    for (size_t j = 0; j < order.size(); ++j) {
+      gi_flux[j] = col[order[j]];
+      gi_coef[j] = coef[order[j]];
+    }
+  }
+  // ---- cell gather, boundary part in the reference's group order
+  // (solver.py:2502-2704): periodic owners_a (-), periodic owners_b (+),
+  // walls, velocity inlets, pressure outlets, far field; within a group in
+  // face-list order (np.add.at is sequential).
+  std::vector<int> gb_ptr, gb_flux;
+  std::vector<double> gb_len;
+  {
+    std::vector<int> bkey, bflux;
+    std::vector<double> blen;
+    for (int64_t i = 0; i < NP; ++i) {
+      int64_t fa = d->periodic_faces_a[i];
+      bkey.push_back((int)d->owners[fa]);
+      bflux.push_back(seg_begin[SEG_PERIODIC] + (int)i);
+      blen.push_back(-d->face_lengths[fa]);
+    }
+    for (int64_t i = 0; i < NP; ++i) {
+      int64_t fa = d->periodic_faces_a[i], fb = d->periodic_faces_b[i];
+      bkey.push_back((int)d->owners[fb]);
+      bflux.push_back(seg_begin[SEG_PERIODIC] + (int)i);
+      blen.push_back(d->face_lengths[fa]);
+    }
+    for (int seg = SEG_WALL; seg <= SEG_FAR; ++seg) {
+      for (int k = seg_begin[seg]; k < seg_begin[seg + 1]; ++k) {
+        int64_t f = lslot[k];
+        bkey.push_back((int)d->owners[f]);
+        bflux.push_back(k);
+        blen.push_back(-d->face_lengths[f]);
+      }
+    }
+    group_by(bkey, (int)C, gb_ptr, order);
+    gb_flux.resize(order.size());
+    gb_len.resize(order.size());
+    for (size_t j = 0; j < order.size(); ++j) {
+      gb_flux[j] = bflux[order[j]];
+      gb_len[j] = blen[order[j]];
+    }
+  }
+  // ---- gradient entries grouped by source, reference order kept
+  std::vector<int> grad_ptr, grad_nb(NG);
+  std::vector<double> grad_cx(NG), grad_cy(NG);
+  {
+    key.resize(NG);
+    for (int64_t e = 0; e < NG; ++e) key[e] = (int)d->gradient_sources[e];
+    group_by(key, (int)C, grad_ptr, order);
+    for (int64_t j = 0; j < NG; ++j) {
+      int e = order[j];
+      grad_nb[j] = (int)d->gradient_neighbours[e];
+      grad_cx[j] = d->gradient_coefficients_x[e];
+      grad_cy[j] = d->gradient_coefficients_y[e];
+    }
+  }
+  // ---- limiter entries grouped by cell
+  std::vector<int> lim_ptr, lim_slot(NL);
+  std::vector<double> lim_d(2 * NL);
+  {
+    key.resize(NL);
+    for (int64_t s = 0; s < NL; ++s) key[s] = (int)d->limiter_cells[s];
+    group_by(key, (int)C, lim_ptr, order);
+    for (int64_t j = 0; j < NL; ++j) {
+      int s = order[j];
+      lim_slot[j] = s;
+      lim_d[2 * j] = d->limiter_dx[s];
+      lim_d[2 * j + 1] = d->limiter_dy[s];
+    }
+  }
+  // ---- time-step entries (solver.py:4206-4226)
+  std::vector<int> dt_ptr, dt_info;
+  std::vector<double> dt_n, dt_len;
+  {
+    std::vector<int> face_info(F, 0);
+    for (int64_t i = 0; i < NV; ++i) face_info[d->velocity_inlet_faces[i]] = (DT_VIN << 28) | (int)i;
+    for (int64_t i = 0; i < NO; ++i) face_info[d->pressure_outlet_faces[i]] = (DT_POUT << 28) | (int)i;
+    for (int64_t i = 0; i < NF; ++i) face_info[d->far_field_faces[i]] = (DT_FAR << 28) | (int)i;
+    std::vector<int> dface;
+    std::vector<int> dinfo;
+    key.clear();
+    for (int64_t f = 0; f < F; ++f) {
+      key.push_back((int)d->owners[f]);
+      dface.push_back((int)f);
+      dinfo.push_back(face_info[f]);
+    }
+    for (int64_t i = 0; i < NI; ++i) {
+      int64_t f = d->interior_faces[i];
+      key.push_back((int)d->neighbours[f]);
+      dface.push_back((int)f);
+      dinfo.push_back(0);
+    }
+    group_by(key, (int)C, dt_ptr, order);
+    dt_info.resize(order.size());
+    dt_n.resize(2 * order.size());
+    dt_len.resize(order.size());
+    for (size_t j = 0; j < order.size(); ++j) {
+      int f = dface[order[j]];
+      dt_info[j] = dinfo[order[j]];
+      dt_n[2 * j] = d->face_normals[2 * f];
+      dt_n[2 * j + 1] = d->face_normals[2 * f + 1];
+      dt_len[j] = d->face_lengths[f];
+    }
+  }
+
+  // ---- arena layout
+  Arena A;
+  auto bytes_i = [](size_t n) { return n * sizeof(int); };
+  auto bytes_d = [](size_t n) { return n * sizeof(double); };
+  const int partial_blocks = 152 * 4;
+  size_t o_area = A.take(bytes_d(C));
+  size_t o_grad_ptr = A.take(bytes_i(C + 1)), o_grad_nb = A.take(bytes_i(NG)),
+         o_grad_cx = A.take(bytes_d(NG)), o_grad_cy = A.take(bytes_d(NG));
+  size_t o_lim_ptr = A.take(bytes_i(C + 1)), o_lim_slot = A.take(bytes_i(NL)),
+         o_lim_d = A.take(bytes_d(2 * NL));
+  size_t o_lslot = A.take(bytes_i(n_flux)), o_rslot = A.take(bytes_i(n_flux)),
+         o_lcell = A.take(bytes_i(n_flux)), o_rcell = A.take(bytes_i(n_flux)),
+         o_normal = A.take(bytes_d(2 * n_flux)), o_wallv = A.take(bytes_d(2 * NW)),
+         o_vin = A.take(bytes_d(4 * NV)), o_pout = A.take(bytes_d(NO)), o_far = A.take(bytes_d(4 * NF));
+  size_t o_gi_ptr = A.take(bytes_i(C + 1)), o_gi_flux = A.take(bytes_i(gi_flux.size())),
+         o_gi_coef = A.take(bytes_d(gi_coef.size()));
+  size_t o_gb_ptr = A.take(bytes_i(C + 1)), o_gb_flux = A.take(bytes_i(gb_flux.size())),
+         o_gb_len = A.take(bytes_d(gb_len.size()));
+  size_t o_dt_ptr = A.take(bytes_i(C + 1)), o_dt_n = A.take(bytes_d(dt_n.size())),
+         o_dt_len = A.take(bytes_d(dt_len.size())), o_dt_info = A.take(bytes_i(dt_info.size()));
+  size_t o_status = A.take(sizeof(DevStatus));
+  size_t o_P = A.take(bytes_d(4 * C)), o_recon = A.take(bytes_d(4 * NL)),
+         o_flux = A.take(bytes_d(4 * n_flux));
+  size_t o_stage[4];
+  for (int k = 0; k < 4; ++k) o_stage[k] = A.take(bytes_d(4 * C));
+  size_t o_saved = A.take(bytes_d(4 * C));
+  size_t o_partials = A.take(bytes_d(4 * partial_blocks));
+
+  mcfd_geom* h = new mcfd_geom();
+  cudaError_t err = cudaMalloc(&h->arena, A.size);
+  if (err != cudaSuccess) {
+    delete h;
+    return MCFD_E_CUDA;
+  }
+  h->arena_bytes = A.size;
+  char* base = static_cast<char*>(h->arena);
+  std::vector<char> host(A.size, 0);
+  auto put = [&](size_t off, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(host.data() + off, src, bytes);
+  };
+  put(o_area, d->areas, bytes_d(C));
+  put(o_grad_ptr, grad_ptr.data(), bytes_i(C + 1));
+  put(o_grad_nb, grad_nb.data(), bytes_i(NG));
+  put(o_grad_cx, grad_cx.data(), bytes_d(NG));
+  put(o_grad_cy, grad_cy.data(), bytes_d(NG));
+  put(o_lim_ptr, lim_ptr.data(), bytes_i(C + 1));
+  put(o_lim_slot, lim_slot.data(), bytes_i(NL));
+  put(o_lim_d, lim_d.data(), bytes_d(2 * NL));
+  put(o_lslot, lslot.data(), bytes_i(n_flux));
+  put(o_rslot, rslot.data(), bytes_i(n_flux));
+  put(o_lcell, lcell.data(), bytes_i(n_flux));
+  put(o_rcell, rcell.data(), bytes_i(n_flux));
+  put(o_normal, normal.data(), bytes_d(2 * n_flux));
+  put(o_wallv, wallv.data(), bytes_d(2 * NW));
+  put(o_vin, vin.data(), bytes_d(4 * NV));
+  put(o_pout, pout.data(), bytes_d(NO));
+  put(o_far, far.data(), bytes_d(4 * NF));
+  put(o_gi_ptr, gi_ptr.data(), bytes_i(C + 1));
+  put(o_gi_flux, gi_flux.data(), bytes_i(gi_flux.size()));
+  put(o_gi_coef, gi_coef.data(), bytes_d(gi_coef.size()));
+  put(o_gb_ptr, gb_ptr.data(), bytes_i(C + 1));
+  put(o_gb_flux, gb_flux.data(), bytes_i(gb_flux.size()));
+  put(o_gb_len, gb_len.data(), bytes_d(gb_len.size()));
+  put(o_dt_ptr, dt_ptr.data(), bytes_i(C + 1));
+  put(o_dt_n, dt_n.data(), bytes_d(dt_n.size()));
+  put(o_dt_len, dt_len.data(), bytes_d(dt_len.size()));
+  put(o_dt_info, dt_info.data(), bytes_i(dt_info.size()));
+  DevStatus st0{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(), 0,
+                0x7ff0000000000000ULL};
+  put(o_status, &st0, sizeof(st0));
+  // geometry part only (workspace stays uninitialised)
+  err = cudaMemcpy(base, host.data(), o_P, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMallocHost(&h->host_status, sizeof(DevStatus));
+  if (err != cudaSuccess) {
+    cudaFree(h->arena);
+    delete h;
+    return MCFD_E_CUDA;
+  }
+  DevGeom& g = h->g;
+  g.n_cells = (int)C;
+  g.n_faces = (int)F;
+  g.n_flux = (int)n_flux;
+  g.n_slots = (int)NL;
+  for (int k = 0; k <= SEG_COUNT; ++k) g.seg_begin[k] = seg_begin[k];
+#define AT(T, off) reinterpret_cast<T>(base + (off))
+  g.area = AT(const double*, o_area);
+  g.grad_ptr = AT(const int*, o_grad_ptr);
+  g.grad_nb = AT(const int*, o_grad_nb);
+  g.grad_cx = AT(const double*, o_grad_cx);
+  g.grad_cy = AT(const double*, o_grad_cy);
+  g.lim_ptr = AT(const int*, o_lim_ptr);
+  g.lim_slot = AT(const int*, o_lim_slot);
+  g.lim_d = AT(const double2*, o_lim_d);
+  g.ff_lslot = AT(const int*, o_lslot);
+  g.ff_rslot = AT(const int*, o_rslot);
+  g.ff_lcell = AT(const int*, o_lcell);
+  g.ff_rcell = AT(const int*, o_rcell);
+  g.ff_normal = AT(const double2*, o_normal);
+  g.ff_wall_velocity = AT(const double2*, o_wallv);
+  g.ff_vin_state = AT(const double*, o_vin);
+  g.ff_pout_pressure = AT(const double*, o_pout);
+  g.ff_far_state = AT(const double*, o_far);
+  g.gi_ptr = AT(const int*, o_gi_ptr);
+  g.gi_flux = AT(const int*, o_gi_flux);
+  g.gi_coef = AT(const double*, o_gi_coef);
+  g.gb_ptr = AT(const int*, o_gb_ptr);
+  g.gb_flux = AT(const int*, o_gb_flux);
+  g.gb_len = AT(const double*, o_gb_len);
+  g.dt_ptr = AT(const int*, o_dt_ptr);
+  g.dt_normal = AT(const double2*, o_dt_n);
+  g.dt_len = AT(const double*, o_dt_len);
+  g.dt_info = AT(const int*, o_dt_info);
+  g.status = AT(DevStatus*, o_status);
+  h->status = g.status;
+  Workspace& w = h->ws;
+  w.P = AT(double*, o_P);
+  w.recon = AT(double*, o_recon);
+  w.flux = AT(double*, o_flux);
+  for (int k = 0; k < 4; ++k) w.stage[k] = AT(double*, o_stage[k]);
+  w.saved_r = AT(double*, o_saved);
+  w.partials = AT(double*, o_partials);
+  w.partial_blocks = partial_blocks;
+#undef AT
+  mcfd_geom_info& info = h->info;
+  info.n_cells = C;
+  info.n_faces = F;
+  info.n_interior = NI;
+  info.n_periodic = NP;
+  info.n_boundary_flux = NW + NV + NO + NF;
+  info.n_flux_faces = n_flux;
+  info.n_gradient = NG;
+  info.n_limiter = NL;
+  info.device_bytes = (int64_t)A.size;
+  *out = h;
+  return MCFD_OK;
+}
+
+int mcfd_geom_destroy(mcfd_geom* h) {
+  if (!h) return MCFD_OK;
+  for (ProfRecord& r : h->records) {
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.stop);
+  }
+  for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+  cudaError_t e1 = cudaFree(h->arena);
+  cudaError_t e2 = cudaFreeHost(h->host_status);
+  delete h;
+  return (e1 == cudaSuccess && e2 == cudaSuccess) ? MCFD_OK : MCFD_E_CUDA;
+}
+
+int mcfd_geom_get_info(const mcfd_geom* h, mcfd_geom_info* info) {
+  if (!h || !info) return MCFD_E_ARG;
+  *info = h->info;
+  return MCFD_OK;
+}
+
+const double* mcfd_geom_primitive(const mcfd_geom* h) { return h ? h->ws.P : nullptr; }
+
+
+
+int mcfd_primitive(mcfd_geom* h, const mcfd_config* cfg, const double* U, double* P, void* stream) {
+  if (!h || !U || !P) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return launch_primitive(h->g, *cfg, U, P, s); }));
+}
+
+
+int mcfd_residual(mcfd_geom* h, const mcfd_config* cfg, const double* U, double* R, void* stream) {
+  if (!h || !U) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return launch_primitive(h->g, *cfg, U, h->ws.P, s); });
+  StageProgram prog{};
+  prog.out_r = R;
+  if (e == cudaSuccess) e = stage(h, *cfg, prog, s);
+  return rc(e);
+}
+
+int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, double* dt_cells,
+                    double* dt_min, double time_limit, void* stream) {
+  if (!h || !P) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_TIME_STEP, s,
+                  [&] { return launch_time_steps(h->g, *cfg, P, dt_cells, dt_min, time_limit, s); }));
+}
+
+
+int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U,
+                       const double* dt, int32_t dt_per_cell, void* stream) {
+  if (!h || !U || !dt) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  Workspace& w = h->ws;
+  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return launch_primitive(h->g, *cfg, U, w.P, s); });
+  auto run = [&](std::initializer_list<StageTerm> terms, double* out, double* save_r) {
+    if (e != cudaSuccess) return;
+    StageProgram p{};
+    p.n_terms = 0;
+    for (const StageTerm& t : terms) p.t[p.n_terms++] = t;
+    p.dt = dt;
+    p.dt_per_cell = dt_per_cell;
+    p.out_u = out;
+    p.out_p = w.P;
+    p.out_r = save_r;
+    e = stage(h, *cfg, p, s);
+  };
+  double *X1 = w.stage[0], *X2 = w.stage[1], *X3 = w.stage[2], *X4 = w.stage[3];
+  switch (scheme) {
+    case MCFD_TIME_EULER:  // solver.py:532-533
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, U, nullptr);
+      break;
+    case MCFD_TIME_RK2:  // solver.py:566-627
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, X1, nullptr);
+      run({term(TERM_X, 0.5, U), term(TERM_X_PLUS_DTR, 0.5, X1)}, U, nullptr);
+      break;
+    case MCFD_TIME_RK3:  // solver.py:566-567, 676-678, 754-756
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, X1, nullptr);
+      run({term(TERM_X, 0.75, U), term(TERM_X_PLUS_DTR, 0.25, X1)}, X2, nullptr);
+      run({term(TERM_X, 1.0 / 3.0, U), term(TERM_X_PLUS_DTR, 2.0 / 3.0, X2)}, U, nullptr);
+      break;
+    default:  // SSPRK(5,4), solver.py:1128-1182
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 0.391752226571890, nullptr)}, X1, nullptr);
+      run({term(TERM_X, 0.444370493651235, U), term(TERM_X, 0.555629506348765, X1),
+           term(TERM_DTR, 0.368410593050371, nullptr)}, X2, nullptr);
+      run({term(TERM_X, 0.620101851488403, U), term(TERM_X, 0.379898148511597, X2),
+           term(TERM_DTR, 0.251891774271694, nullptr)}, X3, nullptr);
+      run({term(TERM_X, 0.178079954393132, U), term(TERM_X, 0.821920045606868, X3),
+           term(TERM_DTR, 0.544974750228521, nullptr)}, X4, w.saved_r);
+      run({term(TERM_X, 0.517231671970585, X2), term(TERM_X, 0.096059710526147, X3),
+           term(TERM_DTR_SAVED, 0.063692468666290, w.saved_r), term(TERM_X, 0.386708617503269, X4),
+           term(TERM_DTR, 0.226007483236906, nullptr)}, U, nullptr);
+      break;
+  }
+  return rc(e);
+}
+
+int mcfd_residual_sumsq(mcfd_geom* h, const double* R, double* sums, void* stream) {
+  if (!h || !R || !sums) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_OTHER, s,
+                  [&] { return launch_sumsq(h->g, R, h->ws.partials, h->ws.partial_blocks, sums, s); }));
+}
+
+int mcfd_status_fetch(mcfd_geom* h, void* stream, mcfd_status* out) {
+  if (!h || !out) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(h->host_status, h->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return MCFD_E_CUDA;
+  DevStatus st = *h->host_status;
+  out->code = st.code;
+  out->first_cell = st.first_cell == std::numeric_limits<int>::max() ? -1 : st.first_cell;
+  out->first_face = st.first_face == std::numeric_limits<int>::max() ? -1 : st.first_face;
+  out->reserved = 0;
+  if (st.code) {
+    DevStatus clear{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(), 0, st.dt_min_bits};
+    *h->host_status = clear;
+    e = cudaMemcpyAsync(h->status, h->host_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return MCFD_E_CUDA;
+  }
+  return MCFD_OK;
+}
+
+int mcfd_profile_enable(mcfd_geom* h, int32_t enable) {
+  if (!h) return MCFD_E_ARG;
+  h->profiling = enable != 0;
+  return MCFD_OK;
+}
+
+int mcfd_profile_read(mcfd_geom* h, double* total_ms, int64_t* groups) {
+  if (!h || !total_ms || !groups) return MCFD_E_ARG;
+  for (int k = 0; k < MCFD_PROF_COUNT; ++k) {
+    total_ms[k] = 0.0;
+    groups[k] = 0;
+  }
+  cudaError_t err = cudaSuccess;
+  if (!h->records.empty()) err = cudaEventSynchronize(h->records.back().stop);
+  for (ProfRecord& r : h->records) {
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, r.start, r.stop);
+    total_ms[r.cls] += ms;
+    groups[r.cls] += 1;
+    h->event_pool.push_back(r.start);
+    h->event_pool.push_back(r.stop);
+  }
+  h->records.clear();
+  return rc(err);
+}
+
+int64_t mcfd_launch_count(void) { return (int64_t)launch_count(); }
+
+// ------------------------------------------------------------- host helpers
+
+int mcfd_host_cell_geometry(int64_t n_cells, const int64_t* off, const int64_t* nodes,
+                            const double* pts, double* centers, double* areas, int64_t* bad_cell) {
+  if (!off || !nodes || !pts || !centers || !areas) return MCFD_E_ARG;
+  for (int64_t c = 0; c < n_cells; ++c) {
+    const int64_t b = off[c], e = off[c + 1], k = e - b;
+    // twice_area = sum(x0*y1 - x1*y0) over consecutive vertex pairs.  The
+    // reference uses Python's built-in sum(), which for floats (CPython >= 3.12)
+    // is Neumaier's compensated summation (Z. angew. Math. Mech. 54, 1974):
+    // running sum t, compensation c, c added once at the end when non-zero.
+    double twice = 0.0, comp = 0.0;
+    for (int64_t i = 0; i < k; ++i) {
+      const double* p0 = pts + 2 * nodes[b + i];
+      const double* p1 = pts + 2 * nodes[b + (i + 1) % k];
+      double x = p0[0] * p1[1] - p1[0] * p0[1];
+      if (i == 0) {
+        twice = x;  // 0 + x: the int start value folds exactly
+        continue;
+      }
+      double t = twice + x;
+      if (std::fabs(twice) >= std::fabs(x)) comp += (twice - t) + x;
+      else comp += (x - t) + twice;
+      twice = t;
+    }
+    if (comp != 0.0 && std::isfinite(comp)) twice += comp;
+    if (!std::isfinite(twice) || std::fabs(twice) <= 1e-15) {
+      if (bad_cell) *bad_cell = c;
+      return MCFD_E_GEOMETRY;
+    }
+    double xs = 0.0, ys = 0.0;
+    for (int64_t i = 0; i < k; ++i) {
+      const double* p0 = pts + 2 * nodes[b + i];
+      const double* p1 = pts + 2 * nodes[b + (i + 1) % k];
+      double cross = p0[0] * p1[1] - p1[0] * p0[1];
+      xs += (p0[0] + p1[0]) * cross;
+      ys += (p0[1] + p1[1]) * cross;
+    }
+    centers[2 * c] = xs / (3.0 * twice);
+    centers[2 * c + 1] = ys / (3.0 * twice);
+    areas[c] = 0.5 * std::fabs(twice);
+  }
+  return MCFD_OK;
+}
+
+int mcfd_host_face_geometry(int64_t n_faces, const int64_t* face_nodes, const double* pts,
+                            const double* centers, const int64_t* owners, double* face_centers,
+                            double* normals, double* lengths, int64_t* bad_face) {
+  if (!face_nodes || !pts || !centers || !owners || !face_centers || !normals || !lengths)
+    return MCFD_E_ARG;
+  for (int64_t f = 0; f < n_faces; ++f) {
+    const double* a = pts + 2 * face_nodes[2 * f];
+    const double* b = pts + 2 * face_nodes[2 * f + 1];
+    double ex = b[0] - a[0], ey = b[1] - a[1];
+    double length = std::sqrt(std::fma(ey, ey, ex * ex));
+    if (!std::isfinite(length) || length <= 1e-15) {
+      if (bad_face) *bad_face = f;
+      return MCFD_E_GEOMETRY;
+    }
+    double nx = ey / length, ny = -ex / length;
+    double cx = 0.5 * (a[0] + b[0]), cy = 0.5 * (a[1] + b[1]);
+    const double* o = centers + 2 * owners[f];
+    double dx = cx - o[0], dy = cy - o[1];
+    if (std::fma(ny, dy, nx * dx) < 0.0) {
+      nx = -nx;
+      ny = -ny;
+    }
+    face_centers[2 * f] = cx;
+    face_centers[2 * f + 1] = cy;
+    normals[2 * f] = nx;
+    normals[2 * f + 1] = ny;
+    lengths[f] = length;
+  }
+  return MCFD_OK;
+}
+
+}  // extern "C"

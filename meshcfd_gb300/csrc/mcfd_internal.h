@@ -1,0 +1,116 @@
+// Internal structures shared by the API (host packing) and kernel translation
+// units.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/meshcfd_gb300.h"
+
+namespace mcfd {
+
+// Flux-face segments, in the order the reference accumulates boundary groups
+// in _residual (solver.py:2502-2704): interior faces first (their sum is the
+// CSR divergence product, solver.py:2501), then periodic pairs, walls and
+// symmetry planes, velocity inlets, pressure outlets, far field.
+enum Segment { SEG_INTERIOR = 0, SEG_PERIODIC, SEG_WALL, SEG_VIN, SEG_POUT, SEG_FAR, SEG_COUNT };
+
+// Kinds of dt entries (exterior state used for the boundary spectral radius,
+// solver.py:4190-4220).
+enum DtKind { DT_PLAIN = 0, DT_VIN = 1, DT_POUT = 2, DT_FAR = 3 };
+
+struct DevStatus {
+  int code;
+  int first_cell;
+  int first_face;
+  int pad;
+  unsigned long long dt_min_bits;  // atomicMin target for the global time step
+};
+
+// Everything a kernel needs, by value.  Index arrays are int32 (sizes are
+// checked against 2^31 at creation).
+struct DevGeom {
+  int n_cells, n_faces, n_flux, n_slots;
+  int seg_begin[SEG_COUNT + 1];
+  const double* area;  // [C]
+  // least-squares gradient entries grouped by source cell, reference order
+  const int* grad_ptr;
+  const int* grad_nb;
+  const double* grad_cx;
+  const double* grad_cy;
+  // limiter entries grouped by cell: slot id (reference entry index) + offset
+  const int* lim_ptr;
+  const int* lim_slot;
+  const double2* lim_d;
+  // flux faces
+  const int* ff_lslot;  // recon slot of the interior-side state
+  const int* ff_rslot;  // recon slot of the other side (interior/periodic), else -1
+  const int* ff_lcell;  // cell of the left state
+  const int* ff_rcell;  // cell of the right state (interior/periodic), else -1
+  const double2* ff_normal;
+  const double2* ff_wall_velocity;  // indexed by flux face - seg_begin[SEG_WALL]
+  const double* ff_vin_state;       // [n_vin][4]
+  const double* ff_pout_pressure;   // [n_pout]
+  const double* ff_far_state;       // [n_far][4]
+  // cell gather: interior faces in ascending face order with the reference's
+  // CSR divergence coefficient, then boundary contributions in BC order with a
+  // signed face length.
+  const int* gi_ptr;
+  const int* gi_flux;
+  const double* gi_coef;
+  const int* gb_ptr;
+  const int* gb_flux;
+  const double* gb_len;
+  // time-step entries: owner side of every face in face order, then the
+  // neighbour side of interior faces.
+  const int* dt_ptr;
+  const double2* dt_normal;
+  const double* dt_len;
+  const int* dt_info;  // kind << 28 | index into the BC arrays
+  DevStatus* status;
+};
+
+// One term of an explicit stage combination, evaluated left to right.
+enum TermKind { TERM_X = 0, TERM_X_PLUS_DTR = 1, TERM_DTR = 2, TERM_DTR_SAVED = 3 };
+struct StageTerm {
+  int kind;
+  double coef;
+  const double* x;  // state (TERM_X, TERM_X_PLUS_DTR) or saved residual
+};
+struct StageProgram {
+  int n_terms;
+  StageTerm t[5];
+  const double* dt;  // device scalar or [C]
+  int dt_per_cell;
+  double* out_u;     // may be null (residual only)
+  double* out_p;     // primitive of out_u, may be null
+  double* out_r;     // residual store, may be null
+};
+
+struct Workspace {
+  double* P;      // [C][4]
+  double* recon;  // [slots][4]
+  double* flux;   // [n_flux][4]
+  double* stage[4];
+  double* saved_r;
+  double* partials;  // [blocks][4]
+  int partial_blocks;
+};
+
+// kernels (mcfd_kernels.cu)
+cudaError_t launch_primitive(const DevGeom& g, const mcfd_config& cfg, const double* U, double* P,
+                             cudaStream_t s);
+cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                               double* recon, cudaStream_t s);
+cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                        const double* recon, double* flux, cudaStream_t s);
+cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                          const double* flux, const StageProgram& prog, cudaStream_t s);
+cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                              double* dt_cells, double* dt_min, double time_limit,
+                              cudaStream_t s);
+long long launch_count();
+cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,
+                         double* sums, cudaStream_t s);
+
+}  // namespace mcfd

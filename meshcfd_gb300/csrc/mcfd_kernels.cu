@@ -1,0 +1,421 @@
+// Kernels of the FP64 residual / explicit-step path (sm_103a).
+//
+// This translation unit is compiled with -fmad=false: every multiply and add
+// rounds separately, as in the reference's NumPy/Python arithmetic, so each
+// kernel reproduces the reference bit for bit where the reference itself is
+// IEEE-deterministic (everything except pow() in the far-field state).
+//
+// Per explicit stage: reconstruct (per cell, MUSCL only) -> flux (per flux
+// face, one launch per face segment) -> gather (per cell: divergence in the
+// reference's accumulation order, boundary adds, body force, finiteness
+// check, stage combination, primitive recovery of the new stage state).
+// There are no atomics on the data path: the face->cell scatter of the
+// reference is a deterministic CSR gather.
+#include "mcfd_device.cuh"
+#include "mcfd_internal.h"
+
+namespace mcfd {
+
+static constexpr int kBlock = 256;
+
+__device__ __forceinline__ void flag_cell(DevStatus* st, int bits, int cell) {
+  atomicOr(&st->code, bits);
+  atomicMin(&st->first_cell, cell);
+}
+__device__ __forceinline__ void flag_face(DevStatus* st, int bits, int face) {
+  atomicOr(&st->code, bits);
+  atomicMin(&st->first_face, face);
+}
+
+// ---------------------------------------------------------------- primitive
+
+__global__ void __launch_bounds__(kBlock) k_primitive(int n, const double* __restrict__ U,
+                                                      double* __restrict__ P, double gamma,
+                                                      DevStatus* st) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  bool ok;
+  St4 p = cons_to_prim(ld4(U + 4 * (size_t)c), gamma, &ok);
+  if (!ok) flag_cell(st, MCFD_S_NONPHYSICAL_STATE, c);
+  st4(P + 4 * (size_t)c, p);
+}
+
+// ----------------------------------------------------------- reconstruction
+//
+// _kernels.linear_gradients_and_factors (_kernels.py:240-273) and
+// limited_gradient_factors (_kernels.py:10-67), as a per-cell gather: the
+// gradient sums run over this cell's entries in the reference's global entry
+// order (so the floating-point sums are identical), the local min/max and the
+// limiter minimum are order-free.  The result is written per limiter entry
+// ("slot") as the reconstructed face state P + phi * (grad . r), which is
+// exactly the left/right state of the fused flux kernel (_kernels.py:90-98)
+// and of _reconstruct (solver.py:2418-2434).
+
+template <int LIMITER>
+__global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double* __restrict__ P,
+                                                        double* __restrict__ recon) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.n_cells) return;
+  const St4 p = ld4(P + 4 * (size_t)c);
+  double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+  double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
+  const double pv[4] = {p.a, p.b, p.c, p.d};
+  const int e0 = g.grad_ptr[c], e1 = g.grad_ptr[c + 1];
+  for (int e = e0; e < e1; ++e) {
+    const int nb = g.grad_nb[e];
+    const double cx = g.grad_cx[e], cy = g.grad_cy[e];
+    const St4 q = ld4(P + 4 * (size_t)nb);
+    const double qv[4] = {q.a, q.b, q.c, q.d};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double d = qv[v] - pv[v];
+      gx[v] = gx[v] + cx * d;
+      gy[v] = gy[v] + cy * d;
+      if (qv[v] < lo[v]) lo[v] = qv[v];
+      if (qv[v] > hi[v]) hi[v] = qv[v];
+    }
+  }
+  double phi[4] = {1.0, 1.0, 1.0, 1.0};
+  const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
+  for (int s = s0; s < s1; ++s) {
+    const double2 d = g.lim_d[s];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double inc = gx[v] * d.x + gy[v] * d.y;
+      double f = limiter_face_factor<LIMITER>(pv[v], inc, lo[v], hi[v]);
+      if (f < phi[v]) phi[v] = f;
+    }
+  }
+  for (int s = s0; s < s1; ++s) {
+    const double2 d = g.lim_d[s];
+    double out[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (gx[v] * d.x + gy[v] * d.y);
+    st4(recon + 4 * (size_t)g.lim_slot[s], St4{out[0], out[1], out[2], out[3]});
+  }
+}
+
+// -------------------------------------------------------------------- fluxes
+
+template <int FLUX, bool KERNEL_HLLC>
+__device__ __forceinline__ int numerical_flux(const St4& L, const St4& R, double nx, double ny,
+                                              double gamma, double out[4]) {
+  if (FLUX == MCFD_FLUX_RUSANOV) {
+    rusanov_flux(L, R, nx, ny, gamma, out);
+    return 0;
+  } else if (FLUX == MCFD_FLUX_HLLC) {
+    return hllc_flux<KERNEL_HLLC>(L, R, nx, ny, gamma, out) ? 0 : MCFD_S_HLLC_NONFINITE;
+  } else {
+    return roe_flux(L, R, nx, ny, gamma, out);
+  }
+}
+
+// One launch per segment keeps every warp on one code path.  FIRST_ORDER
+// reads cell states directly (the reference's reconstruction is the identity
+// there: zero gradients, unit factors).
+template <int FLUX, int SEG, bool FIRST_ORDER, bool KERNEL_HLLC>
+__global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __restrict__ P,
+                                                 const double* __restrict__ recon,
+                                                 double* __restrict__ flux, double gamma) {
+  const int begin = g.seg_begin[SEG];
+  const int f = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= g.seg_begin[SEG + 1]) return;
+  const double2 n = g.ff_normal[f];
+  const St4 L = FIRST_ORDER ? ld4(P + 4 * (size_t)g.ff_lcell[f]) : ld4(recon + 4 * (size_t)g.ff_lslot[f]);
+  St4 R;
+  int bits = 0;
+  if (SEG == SEG_INTERIOR || SEG == SEG_PERIODIC) {
+    R = FIRST_ORDER ? ld4(P + 4 * (size_t)g.ff_rcell[f]) : ld4(recon + 4 * (size_t)g.ff_rslot[f]);
+  } else if (SEG == SEG_WALL) {
+    // solver.py:2536-2543: mirror the velocity relative to the wall velocity.
+    const double2 wv = g.ff_wall_velocity[f - begin];
+    double un = (L.b - wv.x) * n.x + (L.c - wv.y) * n.y;
+    R = St4{L.a, L.b - (2.0 * un) * n.x, L.c - (2.0 * un) * n.y, L.d};
+  } else if (SEG == SEG_VIN) {
+    R = ld4(g.ff_vin_state + 4 * (size_t)(f - begin));  // solver.py:2558
+  } else if (SEG == SEG_POUT) {
+    R = St4{L.a, L.b, L.c, g.ff_pout_pressure[f - begin]};  // solver.py:2581-2582
+  } else {
+    bits |= far_field_state(L, ld4(g.ff_far_state + 4 * (size_t)(f - begin)), n.x, n.y, gamma, &R);
+  }
+  double out[4];
+  bits |= numerical_flux<FLUX, (SEG == SEG_INTERIOR) && KERNEL_HLLC>(L, R, n.x, n.y, gamma, out);
+  if (bits) flag_face(g.status, bits, f);
+  st4(flux + 4 * (size_t)f, St4{out[0], out[1], out[2], out[3]});
+}
+
+// ------------------------------------------------------------ gather + stage
+
+__device__ __forceinline__ double stage_dt(const StageProgram& prog, int c) {
+  return prog.dt_per_cell ? prog.dt[c] : prog.dt[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
+                                                   const double* __restrict__ flux, double gamma,
+                                                   double ax, double ay, StageProgram prog) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.n_cells) return;
+  // interior divergence: SciPy CSR product, ascending face order
+  // (solver.py:2160-2174, 2501); derivative starts from zero.
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int j = g.gi_ptr[c], j1 = g.gi_ptr[c + 1]; j < j1; ++j) {
+    const double a = g.gi_coef[j];
+    const St4 F = ld4(flux + 4 * (size_t)g.gi_flux[j]);
+    s[0] = s[0] + a * F.a;
+    s[1] = s[1] + a * F.b;
+    s[2] = s[2] + a * F.c;
+    s[3] = s[3] + a * F.d;
+  }
+  double r[4] = {0.0 + s[0], 0.0 + s[1], 0.0 + s[2], 0.0 + s[3]};
+  // boundary groups: np.add.at(derivative, owners, -(flux*L)/A) in BC order
+  const int jb0 = g.gb_ptr[c], jb1 = g.gb_ptr[c + 1];
+  if (jb0 < jb1) {
+    const double area = g.area[c];
+    for (int j = jb0; j < jb1; ++j) {
+      const double len = g.gb_len[j];
+      const St4 F = ld4(flux + 4 * (size_t)g.gb_flux[j]);
+      r[0] = r[0] + (F.a * len) / area;
+      r[1] = r[1] + (F.b * len) / area;
+      r[2] = r[2] + (F.c * len) / area;
+      r[3] = r[3] + (F.d * len) / area;
+    }
+  }
+  const St4 p = ld4(P + 4 * (size_t)c);
+  if (ax != 0.0 || ay != 0.0) {  // solver.py:2709-2715
+    r[1] = r[1] + p.a * ax;
+    r[2] = r[2] + p.a * ay;
+    r[3] = r[3] + p.a * (ax * p.b + ay * p.c);
+  }
+  if (!(isfinite(r[0]) && isfinite(r[1]) && isfinite(r[2]) && isfinite(r[3])))
+    flag_cell(g.status, MCFD_S_NONFINITE_RESIDUAL, c);
+  if (prog.out_r) st4(prog.out_r + 4 * (size_t)c, St4{r[0], r[1], r[2], r[3]});
+  if (!prog.out_u) return;
+  const double dt = stage_dt(prog, c);
+  double u[4];
+  for (int t = 0; t < prog.n_terms; ++t) {
+    const StageTerm term = prog.t[t];
+    double v[4];
+    if (term.kind == TERM_X) {
+      const St4 x = ld4(term.x + 4 * (size_t)c);
+      v[0] = term.coef * x.a; v[1] = term.coef * x.b; v[2] = term.coef * x.c; v[3] = term.coef * x.d;
+    } else if (term.kind == TERM_X_PLUS_DTR) {
+      const St4 x = ld4(term.x + 4 * (size_t)c);
+      v[0] = term.coef * (x.a + dt * r[0]);
+      v[1] = term.coef * (x.b + dt * r[1]);
+      v[2] = term.coef * (x.c + dt * r[2]);
+      v[3] = term.coef * (x.d + dt * r[3]);
+    } else if (term.kind == TERM_DTR) {
+      const double cdt = term.coef * dt;
+      v[0] = cdt * r[0]; v[1] = cdt * r[1]; v[2] = cdt * r[2]; v[3] = cdt * r[3];
+    } else {
+      const double cdt = term.coef * dt;
+      const St4 x = ld4(term.x + 4 * (size_t)c);
+      v[0] = cdt * x.a; v[1] = cdt * x.b; v[2] = cdt * x.c; v[3] = cdt * x.d;
+    }
+    if (t == 0) {
+      u[0] = v[0]; u[1] = v[1]; u[2] = v[2]; u[3] = v[3];
+    } else {
+      u[0] = u[0] + v[0]; u[1] = u[1] + v[1]; u[2] = u[2] + v[2]; u[3] = u[3] + v[3];
+    }
+  }
+  const St4 U = St4{u[0], u[1], u[2], u[3]};
+  st4(prog.out_u + 4 * (size_t)c, U);
+  if (prog.out_p) {
+    bool ok;
+    const St4 q = cons_to_prim(U, gamma, &ok);
+    if (!ok) flag_cell(g.status, MCFD_S_NONPHYSICAL_STATE, c);
+    st4(prog.out_p + 4 * (size_t)c, q);
+  }
+}
+
+// --------------------------------------------------------------- time steps
+//
+// _stable_time_steps (solver.py:4132-4343), inviscid: per cell, the sum over
+// its owner-side faces (face order) of (|u.n| + c) * L — with the exterior
+// radius max'ed in on inlet / outlet / far-field faces — then over its
+// neighbour-side interior faces; dt = CFL * A / sum; global = min.
+
+__global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* __restrict__ P,
+                                                       double gamma, double cfl,
+                                                       double* __restrict__ dt_cells,
+                                                       int want_min) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  double dt = __longlong_as_double(0x7ff0000000000000LL);
+  if (c < g.n_cells) {
+    const St4 p = ld4(P + 4 * (size_t)c);
+    const double sound = sound_speed(p.a, p.d, gamma);
+    double sum = 0.0;
+    int bits = 0;
+    for (int e = g.dt_ptr[c], e1 = g.dt_ptr[c + 1]; e < e1; ++e) {
+      const double2 n = g.dt_normal[e];
+      const int info = g.dt_info[e];
+      double radius = fabs(p.b * n.x + p.c * n.y) + sound;
+      const int kind = info >> 28;
+      if (kind != DT_PLAIN) {
+        const int idx = info & 0x0fffffff;
+        St4 ext;
+        if (kind == DT_VIN) ext = ld4(g.ff_vin_state + 4 * (size_t)idx);
+        else if (kind == DT_POUT) ext = St4{p.a, p.b, p.c, g.ff_pout_pressure[idx]};
+        else bits |= far_field_state(p, ld4(g.ff_far_state + 4 * (size_t)idx), n.x, n.y, gamma, &ext);
+        double er = fabs(ext.b * n.x + ext.c * n.y) + sound_speed(ext.a, ext.d, gamma);
+        radius = (radius >= er) ? radius : er;  // np.maximum
+      }
+      sum = sum + radius * g.dt_len[e];
+    }
+    dt = (cfl * g.area[c]) / sum;
+    if (!isfinite(dt) || !(dt > 0.0)) bits |= MCFD_S_TIME_STEP;
+    if (bits) flag_cell(g.status, bits, c);
+    if (dt_cells) dt_cells[c] = dt;
+  }
+  if (!want_min) return;
+  // block minimum by warp shuffles, then one atomicMin on the bit pattern
+  // (positive doubles order like their unsigned bits).
+  double m = (c < g.n_cells && dt > 0.0) ? dt : __longlong_as_double(0x7ff0000000000000LL);
+  for (int off = 16; off > 0; off >>= 1) {
+    double o = __shfl_down_sync(0xffffffffu, m, off);
+    m = (o < m) ? o : m;
+  }
+  __shared__ double warp_min[kBlock / 32];
+  if ((threadIdx.x & 31) == 0) warp_min[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = warp_min[0];
+    for (int w = 1; w < kBlock / 32; ++w) b = (warp_min[w] < b) ? warp_min[w] : b;
+    atomicMin(&g.status->dt_min_bits, (unsigned long long)__double_as_longlong(b));
+  }
+}
+
+__global__ void k_time_step_finalize(DevStatus* st, double* dt_min, double time_limit) {
+  double stable = __longlong_as_double((long long)st->dt_min_bits);
+  // min(stable, end_time - time) with Python's min semantics (solver.py:455-461)
+  dt_min[0] = (time_limit < stable) ? time_limit : stable;
+  st->dt_min_bits = 0x7ff0000000000000ULL;
+}
+
+// ------------------------------------------------------------- sum of squares
+
+__global__ void __launch_bounds__(kBlock) k_sumsq_partial(int n, const double* __restrict__ R,
+                                                          double* __restrict__ partials) {
+  __shared__ double sh[4][kBlock];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const St4 r = ld4(R + 4 * (size_t)c);
+    acc[0] += r.a * r.a; acc[1] += r.b * r.b; acc[2] += r.c * r.c; acc[3] += r.d * r.d;
+  }
+  for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int width = kBlock / 2; width > 0; width >>= 1) {
+    if (threadIdx.x < width)
+      for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + width];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; ++k) partials[4 * blockIdx.x + k] = sh[k][0];
+}
+
+__global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums) {
+  if (threadIdx.x < 4) {
+    double s = 0.0;
+    for (int b = 0; b < blocks; ++b) s += partials[4 * b + threadIdx.x];
+    sums[threadIdx.x] = s;
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+
+static inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+// Kernels launched by this library (host-side counter, for measurement).
+static long long g_launches = 0;
+long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+static inline void count_launch(int n = 1) { __atomic_fetch_add(&g_launches, (long long)n, __ATOMIC_RELAXED); }
+
+cudaError_t launch_primitive(const DevGeom& g, const mcfd_config& cfg, const double* U, double* P,
+                             cudaStream_t s) {
+  if (g.n_cells > 0) count_launch(), k_primitive<<<blocks_for(g.n_cells), kBlock, 0, s>>>(g.n_cells, U, P, cfg.gamma, g.status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                               double* recon, cudaStream_t s) {
+  if (g.n_cells == 0) return cudaSuccess;
+  const int b = blocks_for(g.n_cells);
+  count_launch();
+  switch (cfg.limiter) {
+    case 0: k_reconstruct<0><<<b, kBlock, 0, s>>>(g, P, recon); break;
+    case 1: k_reconstruct<1><<<b, kBlock, 0, s>>>(g, P, recon); break;
+    case 2: k_reconstruct<2><<<b, kBlock, 0, s>>>(g, P, recon); break;
+    default: k_reconstruct<3><<<b, kBlock, 0, s>>>(g, P, recon); break;
+  }
+  return cudaGetLastError();
+}
+
+template <int FLUX, bool FO, bool KH>
+static void flux_segments(const DevGeom& g, const double* P, const double* recon, double* flux,
+                          double gamma, cudaStream_t s) {
+#define MCFD_SEG(SEGV)                                                              \
+  {                                                                                 \
+    int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                              \
+    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<blocks_for(n), kBlock, 0, s>>>(g, P, recon, flux, gamma); \
+  }
+  MCFD_SEG(SEG_INTERIOR)
+  MCFD_SEG(SEG_PERIODIC)
+  MCFD_SEG(SEG_WALL)
+  MCFD_SEG(SEG_VIN)
+  MCFD_SEG(SEG_POUT)
+  MCFD_SEG(SEG_FAR)
+#undef MCFD_SEG
+}
+
+cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                        const double* recon, double* flux, cudaStream_t s) {
+  const bool fo = cfg.reconstruction == MCFD_RECON_FIRST_ORDER;
+  // The reference evaluates interior HLLC faces with its fused compiled kernel
+  // when no curvature is present (solver.py:2479-2490); that kernel has its
+  // own branch order.  Parabolic reconstruction uses the NumPy form.
+  const bool kernel_hllc = cfg.reconstruction != MCFD_RECON_MUSCL_PARABOLIC;
+  switch (cfg.flux) {
+    case MCFD_FLUX_RUSANOV:
+      if (fo) flux_segments<0, true, false>(g, P, recon, flux, cfg.gamma, s);
+      else flux_segments<0, false, false>(g, P, recon, flux, cfg.gamma, s);
+      break;
+    case MCFD_FLUX_HLLC:
+      if (fo) flux_segments<1, true, true>(g, P, recon, flux, cfg.gamma, s);
+      else if (kernel_hllc) flux_segments<1, false, true>(g, P, recon, flux, cfg.gamma, s);
+      else flux_segments<1, false, false>(g, P, recon, flux, cfg.gamma, s);
+      break;
+    default:
+      if (fo) flux_segments<2, true, false>(g, P, recon, flux, cfg.gamma, s);
+      else flux_segments<2, false, false>(g, P, recon, flux, cfg.gamma, s);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                          const double* flux, const StageProgram& prog, cudaStream_t s) {
+  if (g.n_cells > 0)
+    count_launch(), k_gather<<<blocks_for(g.n_cells), kBlock, 0, s>>>(g, P, flux, cfg.gamma, cfg.acceleration_x,
+                                                      cfg.acceleration_y, prog);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                              double* dt_cells, double* dt_min, double time_limit,
+                              cudaStream_t s) {
+  if (g.n_cells > 0)
+    count_launch(), k_time_steps<<<blocks_for(g.n_cells), kBlock, 0, s>>>(g, P, cfg.gamma, cfg.cfl, dt_cells,
+                                                          dt_min != nullptr);
+  if (dt_min) count_launch(), k_time_step_finalize<<<1, 1, 0, s>>>(g.status, dt_min, time_limit);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,
+                         double* sums, cudaStream_t s) {
+  count_launch(2);
+  k_sumsq_partial<<<blocks, kBlock, 0, s>>>(g.n_cells, R, partials);
+  k_sumsq_final<<<1, 32, 0, s>>>(blocks, partials, sums);
+  return cudaGetLastError();
+}
+
+}  // namespace mcfd

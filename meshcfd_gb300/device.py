@@ -1,0 +1,199 @@
+"""Device geometry handle and the host-side calls of the C ABI.
+
+A :class:`DeviceGeometry` is built once per mesh from a reference
+``_Geometry`` (solver.py:123-177) or from :func:`meshcfd_gb300.geometry.
+build_geometry`; it owns the packed device arrays and workspace.  States are
+torch float64 tensors of shape (n_cells, 4) on the handle's CUDA device.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .errors import SolverError, raise_for_status
+from .model import FLUX_CODES, LIMITER_CODES, RECONSTRUCTION_CODES
+
+TIME_SCHEME_CODES = {"Explicit Euler": 0, "Explicit RK2": 1, "Explicit RK3": 2, "Explicit RK4": 3}
+
+
+def make_config(settings, exact: bool = True) -> _lib.Config:
+    """Map ``NumericalSettings`` (model.py:95-129) to the kernel config."""
+    if settings.viscosity_model != "Inviscid":
+        raise NotImplementedError("viscous terms are not implemented by the GPU residual path")
+    if settings.turbulence_model != "None":
+        raise NotImplementedError("SST turbulence is not implemented by the GPU residual path")
+    try:
+        flux = FLUX_CODES[settings.flux]
+        recon = RECONSTRUCTION_CODES[settings.reconstruction]
+        limiter = LIMITER_CODES[settings.limiter]
+    except KeyError as error:
+        raise SolverError(f"Unsupported scheme {error}") from error
+    if recon == 2:
+        raise NotImplementedError("MUSCL parabolic is not implemented by the GPU residual path")
+    cfg = _lib.Config()
+    cfg.flux, cfg.reconstruction, cfg.limiter, cfg.exact = flux, recon, limiter, int(exact)
+    cfg.gamma = float(settings.gamma)
+    cfg.acceleration_x = float(settings.acceleration_x)
+    cfg.acceleration_y = float(settings.acceleration_y)
+    cfg.cfl = float(settings.cfl)
+    return cfg
+
+
+def _stream_ptr(stream=None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _check_state(x: torch.Tensor, n_cells: int, name: str) -> None:
+    if x.dtype != torch.float64 or not x.is_cuda or x.shape != (n_cells, 4) or not x.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous CUDA float64 tensor of shape ({n_cells}, 4)")
+
+
+class DeviceGeometry:
+    """Packed device geometry + workspace for one mesh (one CUDA device)."""
+
+    def __init__(self, geometry, device=None):
+        if getattr(geometry, "pressure_inlets", ()) or getattr(geometry, "mass_flow_inlets", ()) \
+                or getattr(geometry, "mass_flow_outlets", ()):
+            raise NotImplementedError("pressure-inlet and mass-flow boundaries are not implemented on the GPU path")
+        self.lib = _lib.native()
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else torch.device(device).index or 0)
+        keep = {}
+
+        def a(name, dtype, shape=None, src=None):
+            v = getattr(geometry, name) if src is None else src
+            arr = np.ascontiguousarray(np.asarray(v, dtype=dtype))
+            if shape is not None:
+                arr = arr.reshape(shape)
+            keep[name] = arr
+            kind = _lib.P_i64 if dtype == np.int64 else _lib.P_dbl
+            return arr.ctypes.data_as(kind) if arr.size else None, len(arr)
+
+        d = _lib.GeomDesc()
+        d.areas, n_cells = a("areas", np.float64)
+        d.face_lengths, n_faces = a("face_lengths", np.float64)
+        d.n_cells, d.n_faces = n_cells, n_faces
+        d.face_normals, _ = a("face_normals", np.float64, (-1, 2))
+        d.owners, _ = a("owners", np.int64)
+        d.neighbours, _ = a("neighbours", np.int64)
+        d.interior_faces, d.n_interior = a("interior_faces", np.int64)
+        d.periodic_faces_a, d.n_periodic = a("periodic_faces_a", np.int64)
+        d.periodic_faces_b, _ = a("periodic_faces_b", np.int64)
+        d.wall_faces, d.n_wall = a("wall_faces", np.int64)
+        d.wall_velocities, _ = a("wall_velocities", np.float64, (-1, 2))
+        d.velocity_inlet_faces, d.n_velocity_inlet = a("velocity_inlet_faces", np.int64)
+        d.velocity_inlet_states, _ = a("velocity_inlet_states", np.float64, (-1, 4))
+        d.pressure_outlet_faces, d.n_pressure_outlet = a("pressure_outlet_faces", np.int64)
+        d.pressure_outlet_pressures, _ = a("pressure_outlet_pressures", np.float64)
+        d.far_field_faces, d.n_far_field = a("far_field_faces", np.int64)
+        d.far_field_states, _ = a("far_field_states", np.float64, (-1, 4))
+        d.gradient_sources, d.n_gradient = a("gradient_sources", np.int64)
+        d.gradient_neighbours, _ = a("gradient_neighbours", np.int64)
+        d.gradient_coefficients_x, _ = a("gradient_coefficients_x", np.float64)
+        d.gradient_coefficients_y, _ = a("gradient_coefficients_y", np.float64)
+        d.limiter_cells, d.n_limiter = a("limiter_cells", np.int64)
+        d.limiter_dx, _ = a("limiter_dx", np.float64)
+        d.limiter_dy, _ = a("limiter_dy", np.float64)
+        handle = C.c_void_p()
+        with torch.cuda.device(self.device):
+            rc = self.lib.mcfd_geom_create(C.byref(d), C.byref(handle))
+        if rc == 4:
+            raise SolverError("device geometry: inconsistent geometry arrays")
+        self.lib.check(rc, "mcfd_geom_create")
+        self.handle = handle.value
+        info = _lib.GeomInfo()
+        self.lib.check(self.lib.mcfd_geom_get_info(self.handle, C.byref(info)), "mcfd_geom_get_info")
+        self.info = info
+        self.n_cells = int(info.n_cells)
+        self.n_faces = int(info.n_faces)
+        self.n_interior = int(info.n_interior)
+        self.areas = torch.as_tensor(keep["areas"], device=self.device)
+        self._dt_min = torch.empty(1, dtype=torch.float64, device=self.device)
+
+    # ------------------------------------------------------------- lifetime
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.mcfd_geom_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --------------------------------------------------------------- status
+    def check_status(self, solver_error=SolverError, stream=None) -> None:
+        st = _lib.Status()
+        self.lib.check(self.lib.mcfd_status_fetch(self.handle, _stream_ptr(stream), C.byref(st)), "mcfd_status_fetch")
+        raise_for_status(st.code, solver_error)
+
+    def status_code(self, stream=None) -> int:
+        st = _lib.Status()
+        self.lib.check(self.lib.mcfd_status_fetch(self.handle, _stream_ptr(stream), C.byref(st)), "mcfd_status_fetch")
+        return int(st.code)
+
+    # ----------------------------------------------------------- operations
+    def primitive(self, U: torch.Tensor, cfg, out: torch.Tensor | None = None) -> torch.Tensor:
+        _check_state(U, self.n_cells, "U")
+        P = torch.empty_like(U) if out is None else out
+        self.lib.check(self.lib.mcfd_primitive(self.handle, C.byref(cfg), U.data_ptr(), P.data_ptr(), _stream_ptr()),
+                       "mcfd_primitive")
+        return P
+
+    def residual(self, U: torch.Tensor, cfg, out: torch.Tensor | None = None) -> torch.Tensor:
+        _check_state(U, self.n_cells, "U")
+        R = torch.empty_like(U) if out is None else out
+        self.lib.check(self.lib.mcfd_residual(self.handle, C.byref(cfg), U.data_ptr(), R.data_ptr(), _stream_ptr()),
+                       "mcfd_residual")
+        return R
+
+    def primitive_buffer(self) -> torch.Tensor:
+        """The handle's primitive buffer as a tensor view (valid after a
+        residual / primitive / step call)."""
+        ptr = self.lib.mcfd_geom_primitive(self.handle)
+        return _device_view(ptr, (self.n_cells, 4), self.device)
+
+    def time_steps(self, P: torch.Tensor, cfg, time_limit: float = math.inf, per_cell: bool = False,
+                   out_min: torch.Tensor | None = None):
+        _check_state(P, self.n_cells, "P")
+        dt_cells = torch.empty(self.n_cells, dtype=torch.float64, device=self.device) if per_cell else None
+        dt_min = self._dt_min if out_min is None else out_min
+        self.lib.check(self.lib.mcfd_time_steps(self.handle, C.byref(cfg), P.data_ptr(),
+                                                dt_cells.data_ptr() if dt_cells is not None else None,
+                                                dt_min.data_ptr(), float(time_limit), _stream_ptr()),
+                       "mcfd_time_steps")
+        return dt_cells, dt_min
+
+    def explicit_step(self, U: torch.Tensor, cfg, scheme: int, dt: torch.Tensor) -> None:
+        _check_state(U, self.n_cells, "U")
+        if dt.dtype != torch.float64 or not dt.is_cuda or dt.numel() not in (1, self.n_cells):
+            raise ValueError("dt must be a CUDA float64 tensor with 1 or n_cells elements")
+        per_cell = int(dt.numel() == self.n_cells and self.n_cells != 1)
+        self.lib.check(self.lib.mcfd_explicit_step(self.handle, C.byref(cfg), int(scheme), U.data_ptr(), dt.data_ptr(),
+                                                   per_cell, _stream_ptr()), "mcfd_explicit_step")
+
+    def residual_sumsq(self, R: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        _check_state(R, self.n_cells, "R")
+        sums = torch.empty(4, dtype=torch.float64, device=self.device) if out is None else out
+        self.lib.check(self.lib.mcfd_residual_sumsq(self.handle, R.data_ptr(), sums.data_ptr(), _stream_ptr()),
+                       "mcfd_residual_sumsq")
+        return sums
+
+
+def _device_view(ptr: int, shape, device) -> torch.Tensor:
+    """Wrap a library-owned device buffer (lifetime = the handle)."""
+    n = int(np.prod(shape))
+
+    class _Holder:
+        __cuda_array_interface__ = {
+            "shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3, "strides": None,
+        }
+
+    with torch.cuda.device(device):
+        return torch.as_tensor(_Holder(), device=device).view(*shape)

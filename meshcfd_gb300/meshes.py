@@ -1,0 +1,325 @@
+"""Seeded synthetic meshes and initial states for the benchmark workloads.
+
+The reference ships only a structured unit-square quad generator
+(``benchmarks/common.py:53-113``, ``tests/test_solver.py:57-131``).  The meshes
+here follow the same face convention: cells are visited in order, each cell's
+edges in vertex order, a face is created when an edge is first met (owner =
+that cell, orientation = that cell's vertex order) and the second cell to meet
+it becomes the neighbour.  Boundary faces are assigned to patches by position.
+All builders are vectorised so that multi-million-cell meshes take seconds.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from .model import (
+    BoundaryCondition,
+    Case,
+    FiniteVolumeMesh,
+    InitialState,
+    MeshPatch,
+    PeriodicBoundaryPair,
+)
+
+
+@dataclass
+class CellArray:
+    """Cells as a vertex CSR: cell ``c`` has vertices ``nodes[offsets[c]:offsets[c+1]]``."""
+
+    offsets: np.ndarray
+    nodes: np.ndarray
+
+    def __len__(self) -> int:
+        return len(self.offsets) - 1
+
+    def __iter__(self):
+        for c in range(len(self)):
+            yield tuple(int(v) for v in self.nodes[self.offsets[c]:self.offsets[c + 1]])
+
+    def __getitem__(self, c):
+        return tuple(int(v) for v in self.nodes[self.offsets[c]:self.offsets[c + 1]])
+
+
+def build_faces(points: np.ndarray, cells: CellArray, classify) -> FiniteVolumeMesh:
+    """Create faces, owners, neighbours and patches from cell vertex lists.
+
+    ``classify(a, b)`` maps the boundary edge end points (arrays (n,2)) to patch
+    ids (>= 0), returning a tuple ``(patch_ids, patch_names)``.
+    """
+    offsets = np.asarray(cells.offsets, dtype=np.int64)
+    nodes = np.asarray(cells.nodes, dtype=np.int64)
+    counts = np.diff(offsets)
+    n_cells = len(counts)
+    edge_cell = np.repeat(np.arange(n_cells, dtype=np.int64), counts)
+    position = np.arange(len(nodes), dtype=np.int64)
+    last = offsets[1:] - 1
+    next_index = position + 1
+    next_index[last] = offsets[:-1]
+    start = nodes
+    end = nodes[next_index]
+    n_points = len(points)
+    key = np.minimum(start, end) * n_points + np.maximum(start, end)
+    _, first, inverse = np.unique(key, return_index=True, return_inverse=True)
+    order = np.argsort(first, kind="stable")
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    face_of_edge = rank[inverse]
+    first_sorted = first[order]
+    faces = np.column_stack((start[first_sorted], end[first_sorted]))
+    owners = edge_cell[first_sorted]
+    neighbours = np.full(len(faces), -1, dtype=np.int64)
+    is_first = np.zeros(len(nodes), dtype=bool)
+    is_first[first_sorted] = True
+    second = ~is_first
+    if np.any(np.bincount(face_of_edge, minlength=len(faces)) > 2):
+        raise ValueError("non-manifold edge: more than two cells share a face")
+    neighbours[face_of_edge[second]] = edge_cell[second]
+    boundary = np.flatnonzero(neighbours < 0)
+    patch_ids = np.full(len(faces), -1, dtype=np.int64)
+    ids, names = classify(points[faces[boundary, 0]], points[faces[boundary, 1]])
+    patch_ids[boundary] = ids
+    if np.any(patch_ids[boundary] < 0):
+        raise ValueError("boundary face without a patch")
+    patches = tuple(
+        MeshPatch(pid, name, tuple(int(f) for f in boundary[ids == pid]))
+        for pid, name in enumerate(names)
+    )
+    signs = np.where(owners[face_of_edge] == edge_cell, 1, -1)
+    return FiniteVolumeMesh(
+        points=np.asarray(points, dtype=np.float64),
+        cells=cells,
+        faces=faces,
+        face_owners=owners,
+        face_neighbours=neighbours,
+        face_patch_ids=patch_ids,
+        patches=patches,
+        cell_face_ids=CellArray(offsets, face_of_edge),
+        cell_face_signs=CellArray(offsets, signs),
+    )
+
+
+def to_reference_mesh(mesh: FiniteVolumeMesh, mesh_type):
+    """Convert to the reference's tuple-based ``FiniteVolumeMesh`` (small meshes)."""
+    patch_type = type(mesh.patches[0]) if mesh.patches else None
+    return mesh_type(
+        points=tuple((float(x), float(y)) for x, y in np.asarray(mesh.points)),
+        cells=tuple(tuple(c) for c in mesh.cells),
+        faces=tuple((int(a), int(b)) for a, b in np.asarray(mesh.faces)),
+        face_owners=tuple(int(v) for v in mesh.face_owners),
+        face_neighbours=tuple(int(v) for v in mesh.face_neighbours),
+        face_patch_ids=tuple(int(v) for v in mesh.face_patch_ids),
+        patches=tuple(p for p in mesh.patches) if patch_type is None else mesh.patches,
+        cell_face_ids=tuple(tuple(c) for c in mesh.cell_face_ids),
+        cell_face_signs=tuple(tuple(c) for c in mesh.cell_face_signs),
+    )
+
+
+def _grid_points(nx, ny, x0, x1, y0, y1):
+    xs = x0 + (x1 - x0) * np.arange(nx + 1) / nx
+    ys = y0 + (y1 - y0) * np.arange(ny + 1) / ny
+    gx, gy = np.meshgrid(xs, ys)
+    points = np.column_stack((gx.ravel(), gy.ravel()))
+    # exact boundary coordinates, so that periodic patches match bit for bit
+    points[np.isclose(points[:, 0], x1), 0] = x1
+    points[np.isclose(points[:, 1], y1), 1] = y1
+    return points
+
+
+def _jitter_interior(points, nx, ny, hx, hy, amplitude, rng):
+    j, i = np.divmod(np.arange(len(points)), nx + 1)
+    interior = (i > 0) & (i < nx) & (j > 0) & (j < ny)
+    shift = rng.uniform(-amplitude, amplitude, size=(int(interior.sum()), 2))
+    points = points.copy()
+    points[interior, 0] += shift[:, 0] * hx
+    points[interior, 1] += shift[:, 1] * hy
+    return points
+
+
+def _split_cells(nx, ny, split_mask):
+    """Quads in row-major order; a split quad becomes two consecutive triangles
+    sharing its bottom-left to top-right diagonal (both counter-clockwise)."""
+    j, i = np.divmod(np.arange(nx * ny), nx)
+    bl = j * (nx + 1) + i
+    br = bl + 1
+    tr = br + nx + 1
+    tl = bl + nx + 1
+    counts = np.where(split_mask, 6, 4)
+    nodes = np.empty(int(counts.sum()), dtype=np.int64)
+    starts = np.concatenate(([0], np.cumsum(counts)[:-1]))
+    quad = ~split_mask
+    for k, v in enumerate((bl, br, tr, tl)):
+        nodes[starts[quad] + k] = v[quad]
+    for k, v in enumerate((bl, br, tr, bl, tr, tl)):
+        nodes[starts[split_mask] + k] = v[split_mask]
+    cell_counts = np.repeat(np.where(split_mask, 3, 4), np.where(split_mask, 2, 1))
+    offsets = np.concatenate(([0], np.cumsum(cell_counts))).astype(np.int64)
+    return CellArray(offsets, nodes)
+
+
+def _box_classifier(x0, x1, y0, y1):
+    names = ("bottom", "right", "top", "left")
+
+    def classify(a, b):
+        ids = np.full(len(a), -1, dtype=np.int64)
+        ids[(a[:, 1] == y0) & (b[:, 1] == y0)] = 0
+        ids[(a[:, 0] == x1) & (b[:, 0] == x1)] = 1
+        ids[(a[:, 1] == y1) & (b[:, 1] == y1)] = 2
+        ids[(a[:, 0] == x0) & (b[:, 0] == x0)] = 3
+        return ids, names
+
+    return classify
+
+
+def box_mesh(nx, ny, lx=1.0, ly=1.0, split="none", jitter=0.0, seed=0, x0=0.0, y0=0.0):
+    """Rectangle [x0,x0+lx]x[y0,y0+ly] of nx*ny quads.
+
+    ``split``: "none" (quads), "all" (two triangles per quad) or "half" (a
+    seed-chosen half of the quads, exactly nx*ny//2 of them, are split).
+    ``jitter``: interior vertices move uniformly by up to +-jitter*h per axis.
+    """
+    x1, y1 = x0 + lx, y0 + ly
+    rng = np.random.default_rng(seed)
+    points = _grid_points(nx, ny, x0, x1, y0, y1)
+    if split == "none":
+        mask = np.zeros(nx * ny, dtype=bool)
+    elif split == "all":
+        mask = np.ones(nx * ny, dtype=bool)
+    elif split == "half":
+        mask = np.zeros(nx * ny, dtype=bool)
+        mask[rng.permutation(nx * ny)[: (nx * ny) // 2]] = True
+    else:
+        raise ValueError(split)
+    if jitter:
+        points = _jitter_interior(points, nx, ny, lx / nx, ly / ny, jitter, rng)
+    cells = _split_cells(nx, ny, mask)
+    return build_faces(points, cells, _box_classifier(x0, x1, y0, y1))
+
+
+# ---------------------------------------------------------------- workloads
+
+RIEMANN_QUADRANTS = (
+    # (rho, u, v, p) for x>0.5,y>0.5 / x<0.5,y>0.5 / x<0.5,y<0.5 / x>0.5,y<0.5
+    (1.5, 0.0, 0.0, 1.5),
+    (0.5323, 1.206, 0.0, 0.3),
+    (0.138, 1.206, 1.206, 0.029),
+    (0.5323, 0.0, 1.206, 0.3),
+)
+
+
+def cell_centroids(mesh) -> np.ndarray:
+    """Vertex averages (used only to place initial conditions)."""
+    cells = mesh.cells
+    pts = np.asarray(mesh.points)
+    offsets, nodes = cells.offsets, cells.nodes
+    counts = np.diff(offsets)
+    owner = np.repeat(np.arange(len(counts)), counts)
+    cx = np.bincount(owner, weights=pts[nodes, 0]) / counts
+    cy = np.bincount(owner, weights=pts[nodes, 1]) / counts
+    return np.column_stack((cx, cy))
+
+
+def riemann_case(n=128, seed=0, jitter=0.2):
+    """Four-quadrant 2D Riemann problem on a jittered triangulated unit square.
+
+    Walls top and bottom, far field left and right.  The far-field state on each
+    side is the initial state of the quadrant pair it touches, averaged over the
+    two quadrants of that side (left: quadrants 1,2; right: 0,3)."""
+    mesh = box_mesh(n, n, 1.0, 1.0, split="all", jitter=jitter, seed=seed)
+    case = Case(name=f"riemann{n}", mesh=mesh)
+    s = RIEMANN_QUADRANTS
+    left = tuple(0.5 * (a + b) for a, b in zip(s[1], s[2]))
+    right = tuple(0.5 * (a + b) for a, b in zip(s[0], s[3]))
+    for condition in case.boundary_conditions:
+        if condition.patch_name in ("bottom", "top"):
+            condition.kind = "Wall"
+            condition.mechanical_condition = "Slip"
+        else:
+            st = left if condition.patch_name == "left" else right
+            condition.kind = "Far Field"
+            condition.values = {"density": st[0], "velocity_x": st[1], "velocity_y": st[2], "pressure": st[3]}
+    num = case.numerics
+    num.flux, num.reconstruction = "Rusanov", "First order"
+    num.time_integration, num.cfl = "Explicit Euler", 0.5
+    num.end_time, num.max_iterations = 1.0e30, 100
+    num.residual_tolerance = 1e-300
+    centers = cell_centroids(mesh)
+    east = centers[:, 0] > 0.5
+    north = centers[:, 1] > 0.5
+    quadrant = np.where(north, np.where(east, 0, 1), np.where(east, 3, 2))
+    primitive = np.asarray(s, dtype=np.float64)[quadrant]
+    return case, primitive
+
+
+def vortex_primitive(centers, t=0.0, beta=5.0, mach=0.5, angle_deg=45.0, gamma=1.4,
+                     center=(5.0, 5.0), period=(10.0, 10.0)):
+    """Isentropic vortex (strength beta) advected by a free stream of Mach
+    ``mach`` at ``angle_deg``; exact solution at time ``t`` on the periodic box."""
+    speed = mach * math.sqrt(gamma)  # free stream rho=1, p=1, so c = sqrt(gamma)
+    ux = speed * math.cos(math.radians(angle_deg))
+    uy = speed * math.sin(math.radians(angle_deg))
+    cx = (center[0] + ux * t) % period[0]
+    cy = (center[1] + uy * t) % period[1]
+    dx = centers[:, 0] - cx
+    dy = centers[:, 1] - cy
+    dx -= period[0] * np.round(dx / period[0])
+    dy -= period[1] * np.round(dy / period[1])
+    r2 = dx * dx + dy * dy
+    ex = np.exp(0.5 * (1.0 - r2))
+    temperature = 1.0 - (gamma - 1.0) * beta**2 / (8.0 * gamma * math.pi**2) * np.exp(1.0 - r2)
+    rho = temperature ** (1.0 / (gamma - 1.0))
+    u = ux - beta / (2.0 * math.pi) * ex * dy
+    v = uy + beta / (2.0 * math.pi) * ex * dx
+    p = rho**gamma
+    return np.column_stack((rho, u, v, p))
+
+
+def vortex_case(n=1024, seed=0, jitter=0.15, split="half", length=10.0):
+    """Isentropic vortex on a periodic [0,L]^2 box of n*n quads, a seed-chosen
+    half of them split into triangles (split="all": every quad split)."""
+    mesh = box_mesh(n, n, length, length, split=split, jitter=jitter, seed=seed)
+    case = Case(name=f"vortex{n}", mesh=mesh)
+    for condition in case.boundary_conditions:
+        condition.kind = "Periodic"
+    case.periodic_pairs = [
+        PeriodicBoundaryPair(1, 3, "x", length),
+        PeriodicBoundaryPair(0, 2, "y", length),
+    ]
+    num = case.numerics
+    num.flux, num.reconstruction, num.limiter = "HLLC", "MUSCL linear", "Venkatakrishnan"
+    num.time_integration, num.cfl = "Explicit RK3", 0.8
+    num.end_time, num.max_iterations = 1.0e30, 100
+    num.residual_tolerance = 1e-300
+    return case, None
+
+
+def periodic_case(nx, ny, lx=1.0, ly=1.0, split="none", jitter=0.0, seed=0):
+    mesh = box_mesh(nx, ny, lx, ly, split=split, jitter=jitter, seed=seed)
+    case = Case(name="periodic", mesh=mesh)
+    for condition in case.boundary_conditions:
+        condition.kind = "Periodic"
+    case.periodic_pairs = [
+        PeriodicBoundaryPair(1, 3, "x", lx),
+        PeriodicBoundaryPair(0, 2, "y", ly),
+    ]
+    return case
+
+
+def smooth_primitive(n_cells, seed=0, amplitude=0.05):
+    """A smooth, positive, non-uniform state keyed by cell id (as the reference
+    benchmark does, benchmarks/common.py:128-140) plus a seeded perturbation."""
+    cell = np.arange(n_cells, dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    noise = rng.uniform(-1.0, 1.0, size=(n_cells, 4)) * amplitude * 0.1
+    rho = 1.0 + 0.02 * np.sin(0.017 * cell) + noise[:, 0]
+    u = 0.20 + 0.03 * np.sin(0.011 * cell) + noise[:, 1]
+    v = 0.03 * np.cos(0.013 * cell) + noise[:, 2]
+    p = 1.0 + 0.02 * np.cos(0.019 * cell) + noise[:, 3]
+    return np.column_stack((rho, u, v, p))
+
+
+def states_from_primitive(primitive) -> tuple:
+    return tuple(InitialState(*map(float, row)) for row in np.asarray(primitive))

@@ -1,0 +1,135 @@
+"""GPU time loop for the explicit integrators, mirroring the reference's
+``solve_case`` step loop (solver.py:437-1008) with the state kept in HBM.
+
+Per step: time step on the device (global adaptive: min over cells and
+``end_time - time``; global fixed; local steady: per-cell array and its mean),
+one fused explicit step, the status word checked, callbacks and convergence
+history as the reference emits them.  Adaptation and SST are outside this
+path.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from time import thread_time
+
+import numpy as np
+import torch
+
+from .device import TIME_SCHEME_CODES, DeviceGeometry, make_config
+from .errors import SolverError, raise_for_status
+
+
+@dataclass(frozen=True)
+class SolverProgress:
+    """Mirror of ``SolverProgress`` (solver.py:57-66)."""
+
+    step: int
+    time: float
+    time_step: float
+    residuals: tuple
+    states: object = None
+    mesh: object = None
+    cpu_time: float = 0.0
+    warning: str | None = None
+
+
+@dataclass(frozen=True)
+class SolverResult:
+    """Mirror of ``SolverResult`` (solver.py:69-76); ``conservative`` keeps the
+    final device state."""
+
+    states: object
+    time: float
+    steps: int
+    residual: float
+    completed: bool
+    cpu_time: float = 0.0
+    conservative: torch.Tensor | None = None
+
+
+def run_explicit(geom: DeviceGeometry, settings, U: torch.Tensor, *, start_time: float = 0.0,
+                 step_offset: int = 0, progress_callback=None, cancel_callback=None,
+                 solution_callback=None, solution_interval: int = 1, exact: bool = True,
+                 solver_error=SolverError, check_every: int = 1, final_residual: bool = True):
+    """Advance ``U`` (device (C,4) float64, modified in place) like the
+    reference's explicit loop.  Returns a :class:`SolverResult`."""
+    cpu_start = thread_time()
+    if settings.time_integration not in TIME_SCHEME_CODES:
+        raise NotImplementedError(f"{settings.time_integration} is not an explicit integrator")
+    cfg = make_config(settings, exact)
+    scheme = TIME_SCHEME_CODES[settings.time_integration]
+    local = settings.time_step_mode == "Local (steady)"
+    fixed = settings.time_step_mode == "Global fixed"
+    dev = geom.device
+    dt_dev = torch.empty(1, dtype=torch.float64, device=dev)
+    R = torch.empty_like(U)
+    sums = torch.empty(4, dtype=torch.float64, device=dev)
+    time = start_time
+    steps = step_offset
+    completed = False
+    derivative_valid = False
+    for local_step in range(1, settings.max_iterations + 1):
+        step = step_offset + local_step
+        if cancel_callback is not None and cancel_callback():
+            break
+        try:
+            P = geom.primitive(U, cfg, out=geom.primitive_buffer())
+            if local:
+                dt_cells, _ = geom.time_steps(P, cfg, per_cell=True)
+                time_step = float(dt_cells.mean())
+                dt_arg = dt_cells
+            elif fixed:
+                time_step = min(settings.fixed_time_step, settings.end_time - time)
+                dt_dev.fill_(time_step)
+                dt_arg = dt_dev
+            else:
+                geom.time_steps(P, cfg, time_limit=settings.end_time - time, out_min=dt_dev)
+                time_step = float(dt_dev.item())
+                dt_arg = dt_dev
+            code = geom.status_code() if (local_step % check_every == 0 or local) else 0
+            raise_for_status(code, solver_error)
+            if not math.isfinite(time_step) or time_step <= 0.0:
+                raise solver_error("The stable time step is non-positive or non-finite.")
+            geom.explicit_step(U, cfg, scheme, dt_arg)
+            derivative_valid = False
+            if local_step % check_every == 0:
+                raise_for_status(geom.status_code(), solver_error)
+        except (FloatingPointError, ValueError, ZeroDivisionError) as error:
+            raise solver_error(f"Solver failed at step {step}: {error}") from error
+        time += time_step
+        steps = step
+        steady_converged = False
+        if local:
+            geom.residual(U, cfg, out=R)
+            derivative_valid = True
+            raise_for_status(geom.status_code(), solver_error)
+            s = geom.residual_sumsq(R, out=sums)
+            steady_residual = math.sqrt(float(s.sum()) / (4 * geom.n_cells))
+            steady_converged = steady_residual <= settings.residual_tolerance
+        end_time_reached = (not local) and time >= settings.end_time * (1.0 - 1e-13)
+        final_step = (end_time_reached or steady_converged or local_step == settings.max_iterations
+                      or (cancel_callback is not None and cancel_callback()))
+        if progress_callback is not None and (step % settings.convergence_history_interval == 0 or final_step):
+            if not derivative_valid:
+                geom.residual(U, cfg, out=R)
+            s = geom.residual_sumsq(R, out=sums).cpu().numpy()
+            rms = tuple(float(v) for v in np.sqrt(s / geom.n_cells))
+            progress_callback(SolverProgress(step, time, time_step, rms, None, None, thread_time() - cpu_start))
+        if solution_callback is not None and step % solution_interval == 0:
+            solution_callback(step, time, U)
+        if end_time_reached:
+            time = settings.end_time
+            completed = True
+            break
+        if steady_converged:
+            completed = True
+            break
+    raise_for_status(geom.status_code(), solver_error)
+    residual = float("nan")
+    if final_residual:
+        geom.residual(U, cfg, out=R)
+        raise_for_status(geom.status_code(), solver_error)
+        residual = math.sqrt(float(geom.residual_sumsq(R, out=sums).sum()) / (4 * geom.n_cells))
+    return SolverResult(None, time, steps, residual, completed, thread_time() - cpu_start, U)

@@ -1,0 +1,644 @@
+/*
+ * ORACLE — test infrastructure only; never part of the product path.
+ *
+ * A CPU restatement, in plain C, of the reference's residual / time-step hot
+ * path (jesuspueblas/meshcfd, src/meshcfd/core).  It follows the reference's
+ * own loop structure: the compiled kernels' global entry loops
+ * (_kernels.py), the SciPy CSR divergence product, and the sequential
+ * np.add.at scatters per boundary group, in the order _residual runs them.
+ * It shares no code with the CUDA path.  Compile with -ffp-contract=off (no
+ * FMA contraction; NumPy's elementwise ops round every product).
+ *
+ * Parity is pinned: tests/golden holds residuals, time steps and explicit
+ * steps produced by the reference itself, and the CPU tests check this file
+ * against them bit for bit.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_NONPHYSICAL 0x01
+#define ORC_NONFINITE_RESIDUAL 0x02
+#define ORC_HLLC_NONFINITE 0x04
+#define ORC_ROE_SOUND 0x08
+#define ORC_ROE_NONFINITE 0x10
+#define ORC_FARFIELD_SOUND 0x20
+#define ORC_FARFIELD_STATE 0x40
+#define ORC_TIME_STEP 0x80
+#define ORC_ARG 0x1000
+
+typedef struct {
+  int64_t n_cells, n_faces;
+  const double *centers, *areas, *face_centers, *face_normals, *face_lengths, *wall_velocities;
+  const int64_t *owners, *neighbours;
+  int64_t n_interior;
+  const int64_t* interior_faces;
+  const double *interior_owner_offsets, *interior_neighbour_offsets;
+  int64_t n_periodic;
+  const int64_t *periodic_faces_a, *periodic_faces_b;
+  int64_t n_wall;
+  const int64_t* wall_faces;
+  int64_t n_vin;
+  const int64_t* vin_faces;
+  const double* vin_states;
+  int64_t n_pout;
+  const int64_t* pout_faces;
+  const double* pout_pressures;
+  int64_t n_far;
+  const int64_t* far_faces;
+  const double* far_states;
+  int64_t n_gradient;
+  const int64_t *gradient_sources, *gradient_neighbours;
+  const double *gradient_cx, *gradient_cy;
+  int64_t n_limiter;
+  const int64_t* limiter_cells;
+  const double *limiter_dx, *limiter_dy;
+} orc_geom;
+
+typedef struct {
+  int32_t flux, reconstruction, limiter, pad;
+  double gamma, acceleration_x, acceleration_y, cfl;
+} orc_settings;
+
+/* ------------------------------------------------------------ euler.py */
+
+/* euler.conservative_to_primitive (euler.py:20-40) */
+int orc_conservative_to_primitive(int64_t n, const double* U, double gamma, double* P) {
+  int bad = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double* u = U + 4 * i;
+    double rho = u[0];
+    double vx = u[1] / rho, vy = u[2] / rho;
+    double p = (gamma - 1.0) * (u[3] - 0.5 * (u[1] * u[1] + u[2] * u[2]) / rho);
+    P[4 * i] = rho;
+    P[4 * i + 1] = vx;
+    P[4 * i + 2] = vy;
+    P[4 * i + 3] = p;
+    if (!isfinite(rho) || !isfinite(vx) || !isfinite(vy) || !isfinite(p) || rho <= 0.0 || p <= 0.0)
+      bad = ORC_NONPHYSICAL;
+  }
+  return bad;
+}
+
+/* euler.primitive_to_conservative (euler.py:8-17) */
+void orc_primitive_to_conservative(int64_t n, const double* P, double gamma, double* U) {
+  for (int64_t i = 0; i < n; ++i) {
+    const double* q = P + 4 * i;
+    U[4 * i] = q[0];
+    U[4 * i + 1] = q[0] * q[1];
+    U[4 * i + 2] = q[0] * q[2];
+    U[4 * i + 3] = q[3] / (gamma - 1.0) + 0.5 * q[0] * (q[1] * q[1] + q[2] * q[2]);
+  }
+}
+
+/* euler.physical_flux (euler.py:43-57), one row */
+static void physical_flux(const double* q, const double* n, double gamma, double* F, double* U) {
+  double rho = q[0], vx = q[1], vy = q[2], p = q[3];
+  U[0] = rho;
+  U[1] = rho * vx;
+  U[2] = rho * vy;
+  U[3] = p / (gamma - 1.0) + 0.5 * rho * (vx * vx + vy * vy);
+  double un = vx * n[0] + vy * n[1];
+  F[0] = rho * un;
+  F[1] = rho * vx * un + p * n[0];
+  F[2] = rho * vy * un + p * n[1];
+  F[3] = (U[3] + p) * un;
+}
+
+static double sound(const double* q, double gamma) { return sqrt(gamma * q[3] / q[0]); }
+
+/* euler._rusanov_flux (euler.py:80-93) */
+static int rusanov(const double* L, const double* R, const double* n, double gamma, double* out) {
+  double FL[4], UL[4], FR[4], UR[4];
+  physical_flux(L, n, gamma, FL, UL);
+  physical_flux(R, n, gamma, FR, UR);
+  double nl = L[1] * n[0] + L[2] * n[1], nr = R[1] * n[0] + R[2] * n[1];
+  double a = fabs(nl) + sound(L, gamma), b = fabs(nr) + sound(R, gamma);
+  double s = a >= b ? a : b;
+  for (int k = 0; k < 4; ++k) out[k] = 0.5 * (FL[k] + FR[k] - s * (UR[k] - UL[k]));
+  return 0;
+}
+
+/* star state of euler._hllc_flux (euler.py:122-148) */
+static void hllc_star(const double* q, const double* U, double un, double wave, double contact,
+                      const double* n, double* star) {
+  double factor = q[0] * (wave - un) / (wave - contact);
+  double vx = q[1] + (contact - un) * n[0];
+  double vy = q[2] + (contact - un) * n[1];
+  double energy = factor * (U[3] / q[0] + (contact - un) * (contact + q[3] / (q[0] * (wave - un))));
+  star[0] = factor;
+  star[1] = factor * vx;
+  star[2] = factor * vy;
+  star[3] = energy;
+}
+
+/* euler._hllc_flux (euler.py:96-166), vectorised form's selection */
+static int hllc_numpy(const double* L, const double* R, const double* n, double gamma, double* out) {
+  double FL[4], UL[4], FR[4], UR[4];
+  physical_flux(L, n, gamma, FL, UL);
+  physical_flux(R, n, gamma, FR, UR);
+  double unl = L[1] * n[0] + L[2] * n[1], unr = R[1] * n[0] + R[2] * n[1];
+  double cl = sound(L, gamma), cr = sound(R, gamma);
+  double a = unl - cl, b = unr - cr;
+  double wl = b < a ? b : a;
+  a = unl + cl;
+  b = unr + cr;
+  double wr = b > a ? b : a;
+  double den = L[0] * (wl - unl) - R[0] * (wr - unr);
+  double safe = fabs(den) > 1e-14 ? den : copysign(1e-14, den);
+  double contact = (R[3] - L[3] + L[0] * unl * (wl - unl) - R[0] * unr * (wr - unr)) / safe;
+  double star[4];
+  if (wl >= 0.0) {
+    for (int k = 0; k < 4; ++k) out[k] = FL[k];
+  } else if (contact >= 0.0) {
+    hllc_star(L, UL, unl, wl, contact, n, star);
+    for (int k = 0; k < 4; ++k) out[k] = FL[k] + wl * (star[k] - UL[k]);
+  } else if (wr > 0.0) {
+    hllc_star(R, UR, unr, wr, contact, n, star);
+    for (int k = 0; k < 4; ++k) out[k] = FR[k] + wr * (star[k] - UR[k]);
+  } else {
+    for (int k = 0; k < 4; ++k) out[k] = FR[k];
+  }
+  for (int k = 0; k < 4; ++k)
+    if (!isfinite(out[k])) return ORC_HLLC_NONFINITE;
+  return 0;
+}
+
+/* euler._roe_flux (euler.py:169-262); np.einsum's four-term reduction on the
+ * reference's platform adds (t0 + t2) + (t1 + t3). */
+static int roe(const double* L, const double* R, const double* n, double gamma, double* out) {
+  double FL[4], UL[4], FR[4], UR[4];
+  physical_flux(L, n, gamma, FL, UL);
+  physical_flux(R, n, gamma, FR, UR);
+  double rl = sqrt(L[0]), rr = sqrt(R[0]);
+  double den = rl + rr;
+  double vx = (rl * L[1] + rr * R[1]) / den;
+  double vy = (rl * L[2] + rr * R[2]) / den;
+  double H = (rl * (L[3] / L[0] + 0.5 * (L[1] * L[1] + L[2] * L[2])) +
+              rr * (R[3] / R[0] + 0.5 * (R[1] * R[1] + R[2] * R[2]))) / den;
+  double un = vx * n[0] + vy * n[1];
+  double ut = vx * -n[1] + vy * n[0];
+  double c2 = (gamma - 1.0) * (H - 0.5 * (vx * vx + vy * vy));
+  if (c2 <= 0.0 || !isfinite(c2)) return ORC_ROE_SOUND;
+  double c = sqrt(c2), ravg = rl * rr;
+  double unl = L[1] * n[0] + L[2] * n[1], unr = R[1] * n[0] + R[2] * n[1];
+  double utl = L[1] * -n[1] + L[2] * n[0], utr = R[1] * -n[1] + R[2] * n[0];
+  double dr = R[0] - L[0], dun = unr - unl, dut = utr - utl, dp = R[3] - L[3];
+  double s[4];
+  s[0] = (dp - ravg * c * dun) / (2.0 * c2);
+  s[3] = (dp + ravg * c * dun) / (2.0 * c2);
+  s[1] = dr - dp / c2;
+  s[2] = ravg * dut;
+  double lam[4] = {un - c, un, un, un + c};
+  double fix = 0.1 * c, w[4];
+  for (int j = 0; j < 4; ++j) {
+    double a = fabs(lam[j]);
+    if (a < fix) a = 0.5 * (a * a / fix + fix);
+    w[j] = a * s[j];
+  }
+  double E[4][4] = {{1.0, 1.0, 0.0, 1.0},
+                    {un - c, un, 0.0, un + c},
+                    {ut, ut, 1.0, ut},
+                    {H - un * c, 0.5 * (un * un + ut * ut), ut, H + un * c}};
+  double d[4];
+  for (int i = 0; i < 4; ++i) {
+    double t0 = E[i][0] * w[0], t1 = E[i][1] * w[1], t2 = E[i][2] * w[2], t3 = E[i][3] * w[3];
+    d[i] = (t0 + t2) + (t1 + t3);
+  }
+  double diss[4] = {d[0], d[1] * n[0] - d[2] * n[1], d[1] * n[1] + d[2] * n[0], d[3]};
+  for (int k = 0; k < 4; ++k) {
+    out[k] = 0.5 * (FL[k] + FR[k] - diss[k]);
+    if (!isfinite(out[k])) return ORC_ROE_NONFINITE;
+  }
+  return 0;
+}
+
+/* euler.numerical_flux (euler.py:60-73) */
+static int numerical_flux(int scheme, const double* L, const double* R, const double* n, double gamma,
+                          double* out) {
+  if (scheme == 0) return rusanov(L, R, n, gamma, out);
+  if (scheme == 1) return hllc_numpy(L, R, n, gamma, out);
+  return roe(L, R, n, gamma, out);
+}
+
+/* ------------------------------------------------------------ _kernels.py */
+
+/* limited_gradient_factors (_kernels.py:10-67) */
+static void limited_gradient_factors(int64_t C, const double* P, const double* grad, const orc_geom* g,
+                                     int code, double* factors) {
+  double* lo = (double*)malloc(sizeof(double) * 4 * C);
+  double* hi = (double*)malloc(sizeof(double) * 4 * C);
+  memcpy(lo, P, sizeof(double) * 4 * C);
+  memcpy(hi, P, sizeof(double) * 4 * C);
+  for (int64_t i = 0; i < 4 * C; ++i) factors[i] = 1.0;
+  for (int64_t e = 0; e < g->n_gradient; ++e) {
+    int64_t s = g->gradient_sources[e], nb = g->gradient_neighbours[e];
+    for (int v = 0; v < 4; ++v) {
+      double value = P[4 * nb + v];
+      if (value < lo[4 * s + v]) lo[4 * s + v] = value;
+      if (value > hi[4 * s + v]) hi[4 * s + v] = value;
+    }
+  }
+  for (int64_t e = 0; e < g->n_limiter; ++e) {
+    int64_t c = g->limiter_cells[e];
+    double dx = g->limiter_dx[e], dy = g->limiter_dy[e];
+    for (int v = 0; v < 4; ++v) {
+      double cv = P[4 * c + v];
+      double inc = grad[8 * c + 2 * v] * dx + grad[8 * c + 2 * v + 1] * dy;
+      double m = fabs(cv);
+      double tol = 1e-14 * (1.0 > m ? 1.0 : m);
+      double ratio = 1.0;
+      if (inc > tol) ratio = (hi[4 * c + v] - cv) / inc;
+      else if (inc < -tol) ratio = (lo[4 * c + v] - cv) / inc;
+      ratio = 0.0 > ratio ? 0.0 : ratio;
+      double f;
+      if (code <= 1) f = 1.0 < ratio ? 1.0 : ratio;
+      else if (code == 2) {
+        if (ratio > 0.0) {
+          double q = 2.0 * ratio / (1.0 + ratio);
+          f = q < 1.0 ? q : 1.0;
+        } else f = 0.0;
+      } else {
+        double eps = 1e-12;
+        f = (ratio * ratio + 2.0 * ratio + eps) / (ratio * ratio + ratio + 2.0 + eps);
+        f = 1.0 < f ? 1.0 : f;
+      }
+      if (f < factors[4 * c + v]) factors[4 * c + v] = f;
+    }
+  }
+  free(lo);
+  free(hi);
+}
+
+/* linear_gradients_and_factors (_kernels.py:240-273); grad is (C,4,2) */
+void orc_linear_gradients_and_factors(const orc_geom* g, const double* P, int code, double* grad,
+                                      double* factors) {
+  int64_t C = g->n_cells;
+  memset(grad, 0, sizeof(double) * 8 * C);
+  for (int64_t e = 0; e < g->n_gradient; ++e) {
+    int64_t s = g->gradient_sources[e], nb = g->gradient_neighbours[e];
+    double cx = g->gradient_cx[e], cy = g->gradient_cy[e];
+    for (int v = 0; v < 4; ++v) {
+      double d = P[4 * nb + v] - P[4 * s + v];
+      grad[8 * s + 2 * v] += cx * d;
+      grad[8 * s + 2 * v + 1] += cy * d;
+    }
+  }
+  limited_gradient_factors(C, P, grad, g, code, factors);
+}
+
+/* reconstruct_hllc_flux (_kernels.py:71-160), one face */
+static void kernel_hllc(const double* left, const double* right, const double* n, double gamma,
+                        double* out) {
+  double rl = left[0], vxl = left[1], vyl = left[2], pl = left[3];
+  double rr = right[0], vxr = right[1], vyr = right[2], pr = right[3];
+  double nx = n[0], ny = n[1];
+  double unl = vxl * nx + vyl * ny, unr = vxr * nx + vyr * ny;
+  double cl = sqrt(gamma * pl / rl), cr = sqrt(gamma * pr / rr);
+  double a = unl - cl, b = unr - cr;
+  double wl = b < a ? b : a;
+  a = unl + cl;
+  b = unr + cr;
+  double wr = b > a ? b : a;
+  double el = pl / (gamma - 1.0) + 0.5 * rl * (vxl * vxl + vyl * vyl);
+  double er = pr / (gamma - 1.0) + 0.5 * rr * (vxr * vxr + vyr * vyr);
+  double sl[4] = {rl, rl * vxl, rl * vyl, el}, sr[4] = {rr, rr * vxr, rr * vyr, er};
+  double fl[4] = {rl * unl, rl * vxl * unl + pl * nx, rl * vyl * unl + pl * ny, (el + pl) * unl};
+  double fr[4] = {rr * unr, rr * vxr * unr + pr * nx, rr * vyr * unr + pr * ny, (er + pr) * unr};
+  double den = rl * (wl - unl) - rr * (wr - unr);
+  if (fabs(den) <= 1e-14) den = copysign(1e-14, den);
+  double contact = (pr - pl + rl * unl * (wl - unl) - rr * unr * (wr - unr)) / den;
+  if (wl >= 0.0) {
+    for (int k = 0; k < 4; ++k) out[k] = fl[k];
+    return;
+  }
+  if (wr <= 0.0) {
+    for (int k = 0; k < 4; ++k) out[k] = fr[k];
+    return;
+  }
+  double rho, vx, vy, pressure, un, wave, energy;
+  const double *state, *phys;
+  if (contact >= 0.0) {
+    rho = rl; vx = vxl; vy = vyl; pressure = pl; un = unl; wave = wl; energy = el; state = sl; phys = fl;
+  } else {
+    rho = rr; vx = vxr; vy = vyr; pressure = pr; un = unr; wave = wr; energy = er; state = sr; phys = fr;
+  }
+  double factor = rho * (wave - un) / (wave - contact);
+  double svx = vx + (contact - un) * nx, svy = vy + (contact - un) * ny;
+  double se = factor * (energy / rho + (contact - un) * (contact + pressure / (rho * (wave - un))));
+  double star[4] = {factor, factor * svx, factor * svy, se};
+  for (int k = 0; k < 4; ++k) out[k] = phys[k] + wave * (star[k] - state[k]);
+}
+
+/* ------------------------------------------------------------ solver.py */
+
+/* _reconstruct (solver.py:2418-2434), one row */
+static void reconstruct(const double* P, const double* grad, const double* fac, int64_t c, double ox,
+                        double oy, double* out) {
+  for (int v = 0; v < 4; ++v) {
+    double inc = grad[8 * c + 2 * v] * ox + grad[8 * c + 2 * v + 1] * oy;
+    out[v] = P[4 * c + v] + fac[4 * c + v] * inc;
+  }
+}
+
+/* _far_field_boundary_states (solver.py:4350-4409), one row */
+static int far_field(const double* in, const double* far, const double* n, double gamma, double* ext) {
+  double ni = in[1] * n[0] + in[2] * n[1], nf = far[1] * n[0] + far[2] * n[1];
+  double ci = sound(in, gamma), cf = sound(far, gamma);
+  memcpy(ext, in, 4 * sizeof(double));
+  if (ni <= -ci) {
+    memcpy(ext, far, 4 * sizeof(double));
+    return 0;
+  }
+  if (ni >= ci) return 0;
+  double out_inv = ni + 2.0 * ci / (gamma - 1.0);
+  double in_inv = nf - 2.0 * cf / (gamma - 1.0);
+  double vb = 0.5 * (out_inv + in_inv);
+  double cb = 0.25 * (gamma - 1.0) * (out_inv - in_inv);
+  if (!isfinite(cb) || cb <= 0.0) return ORC_FARFIELD_SOUND;
+  const double* src = vb < 0.0 ? far : in;
+  double entropy = src[3] / pow(src[0], gamma);
+  double rho = pow(cb * cb / (gamma * entropy), 1.0 / (gamma - 1.0));
+  double p = entropy * pow(rho, gamma);
+  double tx = -n[1], ty = n[0];
+  double vt = src[1] * tx + src[2] * ty;
+  ext[0] = rho;
+  ext[1] = vb * n[0] + vt * tx;
+  ext[2] = vb * n[1] + vt * ty;
+  ext[3] = p;
+  if (!isfinite(ext[0]) || !isfinite(ext[1]) || !isfinite(ext[2]) || !isfinite(ext[3]) || rho <= 0.0 ||
+      p <= 0.0)
+    return ORC_FARFIELD_STATE;
+  return 0;
+}
+
+/* SciPy CSR rows of interior_divergence_operator (solver.py:2160-2174):
+ * for every cell, its interior-face columns in ascending order. */
+typedef struct {
+  int64_t* ptr;
+  int64_t* col;
+  double* val;
+} orc_csr;
+
+static void divergence_operator(const orc_geom* g, orc_csr* D) {
+  int64_t C = g->n_cells, NI = g->n_interior;
+  D->ptr = (int64_t*)calloc(C + 1, sizeof(int64_t));
+  D->col = (int64_t*)malloc(sizeof(int64_t) * (2 * NI + 1));
+  D->val = (double*)malloc(sizeof(double) * (2 * NI + 1));
+  for (int64_t i = 0; i < NI; ++i) {
+    int64_t f = g->interior_faces[i];
+    D->ptr[g->owners[f] + 1]++;
+    D->ptr[g->neighbours[f] + 1]++;
+  }
+  for (int64_t c = 0; c < C; ++c) D->ptr[c + 1] += D->ptr[c];
+  int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (C + 1));
+  memcpy(fill, D->ptr, sizeof(int64_t) * (C + 1));
+  for (int64_t i = 0; i < NI; ++i) { /* columns arrive in ascending order */
+    int64_t f = g->interior_faces[i], o = g->owners[f], nb = g->neighbours[f];
+    double L = g->face_lengths[f];
+    D->col[fill[o]] = i;
+    D->val[fill[o]++] = -L / g->areas[o];
+    D->col[fill[nb]] = i;
+    D->val[fill[nb]++] = L / g->areas[nb];
+  }
+  free(fill);
+}
+
+typedef struct {
+  int64_t n;
+  const int64_t* faces;
+} group_t;
+
+/* _residual (solver.py:2437-2718), inviscid, no turbulence */
+int orc_residual(const orc_geom* g, const orc_settings* s, const double* U, double* R) {
+  int64_t C = g->n_cells, NI = g->n_interior;
+  double gamma = s->gamma;
+  int status = 0;
+  double* P = (double*)malloc(sizeof(double) * 4 * C);
+  double* grad = (double*)calloc(8 * C, sizeof(double));
+  double* fac = (double*)malloc(sizeof(double) * 4 * C);
+  status |= orc_conservative_to_primitive(C, U, gamma, P);
+  if (status) goto done;
+  if (s->reconstruction == 1 && g->n_gradient) {
+    orc_linear_gradients_and_factors(g, P, s->limiter, grad, fac);
+  } else {
+    for (int64_t i = 0; i < 4 * C; ++i) fac[i] = 1.0;
+  }
+  memset(R, 0, sizeof(double) * 4 * C);
+  if (NI) {
+    double* flux = (double*)malloc(sizeof(double) * 4 * NI);
+    for (int64_t i = 0; i < NI; ++i) {
+      int64_t f = g->interior_faces[i], o = g->owners[f], nb = g->neighbours[f];
+      double L[4], Rt[4];
+      const double* n = g->face_normals + 2 * f;
+      const double* oo = g->interior_owner_offsets + 2 * i;
+      const double* no = g->interior_neighbour_offsets + 2 * i;
+      reconstruct(P, grad, fac, o, oo[0], oo[1], L);
+      reconstruct(P, grad, fac, nb, no[0], no[1], Rt);
+      if (s->flux == 1) kernel_hllc(L, Rt, n, gamma, flux + 4 * i);
+      else status |= numerical_flux(s->flux, L, Rt, n, gamma, flux + 4 * i);
+    }
+    orc_csr D;
+    divergence_operator(g, &D);
+    for (int64_t c = 0; c < C; ++c) {
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int64_t j = D.ptr[c]; j < D.ptr[c + 1]; ++j)
+        for (int v = 0; v < 4; ++v) acc[v] += D.val[j] * flux[4 * D.col[j] + v];
+      for (int v = 0; v < 4; ++v) R[4 * c + v] += acc[v];
+    }
+    free(D.ptr);
+    free(D.col);
+    free(D.val);
+    free(flux);
+  }
+  if (g->n_periodic) {
+    int64_t NP = g->n_periodic;
+    double* integ = (double*)malloc(sizeof(double) * 4 * NP);
+    for (int64_t i = 0; i < NP; ++i) {
+      int64_t fa = g->periodic_faces_a[i], fb = g->periodic_faces_b[i];
+      int64_t oa = g->owners[fa], ob = g->owners[fb];
+      double L[4], Rt[4], fl[4];
+      reconstruct(P, grad, fac, oa, g->face_centers[2 * fa] - g->centers[2 * oa],
+                  g->face_centers[2 * fa + 1] - g->centers[2 * oa + 1], L);
+      reconstruct(P, grad, fac, ob, g->face_centers[2 * fb] - g->centers[2 * ob],
+                  g->face_centers[2 * fb + 1] - g->centers[2 * ob + 1], Rt);
+      status |= numerical_flux(s->flux, L, Rt, g->face_normals + 2 * fa, gamma, fl);
+      for (int v = 0; v < 4; ++v) integ[4 * i + v] = fl[v] * g->face_lengths[fa];
+    }
+    for (int64_t i = 0; i < NP; ++i) {
+      int64_t oa = g->owners[g->periodic_faces_a[i]];
+      for (int v = 0; v < 4; ++v) R[4 * oa + v] += -integ[4 * i + v] / g->areas[oa];
+    }
+    for (int64_t i = 0; i < NP; ++i) {
+      int64_t ob = g->owners[g->periodic_faces_b[i]];
+      for (int v = 0; v < 4; ++v) R[4 * ob + v] += integ[4 * i + v] / g->areas[ob];
+    }
+    free(integ);
+  }
+  /* wall / symmetry, velocity inlet, pressure outlet, far field (solver.py:2529-2625) */
+  group_t groups[4] = {{g->n_wall, g->wall_faces}, {g->n_vin, g->vin_faces},
+                       {g->n_pout, g->pout_faces}, {g->n_far, g->far_faces}};
+  for (int k = 0; k < 4; ++k) {
+    int64_t n = groups[k].n;
+    if (!n) continue;
+    double* contrib = (double*)malloc(sizeof(double) * 4 * n);
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t f = groups[k].faces[i], o = g->owners[f];
+      const double* nrm = g->face_normals + 2 * f;
+      double in[4], ext[4], fl[4];
+      reconstruct(P, grad, fac, o, g->face_centers[2 * f] - g->centers[2 * o],
+                  g->face_centers[2 * f + 1] - g->centers[2 * o + 1], in);
+      memcpy(ext, in, sizeof(ext));
+      if (k == 0) {
+        double wx = g->wall_velocities ? g->wall_velocities[2 * f] : 0.0;
+        double wy = g->wall_velocities ? g->wall_velocities[2 * f + 1] : 0.0;
+        double un = (in[1] - wx) * nrm[0] + (in[2] - wy) * nrm[1];
+        ext[1] -= 2.0 * un * nrm[0];
+        ext[2] -= 2.0 * un * nrm[1];
+      } else if (k == 1) {
+        memcpy(ext, g->vin_states + 4 * i, sizeof(ext));
+      } else if (k == 2) {
+        ext[3] = g->pout_pressures[i];
+      } else {
+        status |= far_field(in, g->far_states + 4 * i, nrm, gamma, ext);
+      }
+      status |= numerical_flux(s->flux, in, ext, nrm, gamma, fl);
+      for (int v = 0; v < 4; ++v) contrib[4 * i + v] = -(fl[v] * g->face_lengths[f]) / g->areas[o];
+    }
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t o = g->owners[groups[k].faces[i]];
+      for (int v = 0; v < 4; ++v) R[4 * o + v] += contrib[4 * i + v];
+    }
+    free(contrib);
+  }
+  if (s->acceleration_x != 0.0 || s->acceleration_y != 0.0) {
+    for (int64_t c = 0; c < C; ++c) R[4 * c + 1] += P[4 * c] * s->acceleration_x;
+    for (int64_t c = 0; c < C; ++c) R[4 * c + 2] += P[4 * c] * s->acceleration_y;
+    for (int64_t c = 0; c < C; ++c)
+      R[4 * c + 3] += P[4 * c] * (s->acceleration_x * P[4 * c + 1] + s->acceleration_y * P[4 * c + 2]);
+  }
+  for (int64_t i = 0; i < 4 * C; ++i)
+    if (!isfinite(R[i])) {
+      status |= ORC_NONFINITE_RESIDUAL;
+      break;
+    }
+done:
+  free(P);
+  free(grad);
+  free(fac);
+  return status;
+}
+
+/* _stable_time_steps (solver.py:4132-4343), inviscid */
+int orc_stable_time_steps(const orc_geom* g, const orc_settings* s, const double* P, double* dt) {
+  int64_t C = g->n_cells, F = g->n_faces;
+  double gamma = s->gamma;
+  int status = 0;
+  double* radius = (double*)malloc(sizeof(double) * (F + 1));
+  double* cs = (double*)malloc(sizeof(double) * C);
+  for (int64_t c = 0; c < C; ++c) cs[c] = sound(P + 4 * c, gamma);
+  for (int64_t f = 0; f < F; ++f) {
+    int64_t o = g->owners[f];
+    radius[f] = fabs(P[4 * o + 1] * g->face_normals[2 * f] + P[4 * o + 2] * g->face_normals[2 * f + 1]) + cs[o];
+  }
+  /* exterior radius on inlet / outlet / far-field faces (solver.py:4190-4220) */
+  for (int k = 0; k < 3; ++k) {
+    int64_t n = k == 0 ? g->n_vin : (k == 1 ? g->n_pout : g->n_far);
+    const int64_t* faces = k == 0 ? g->vin_faces : (k == 1 ? g->pout_faces : g->far_faces);
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t f = faces[i], o = g->owners[f];
+      const double* nrm = g->face_normals + 2 * f;
+      double ext[4];
+      memcpy(ext, P + 4 * o, sizeof(ext));
+      if (k == 0) memcpy(ext, g->vin_states + 4 * i, sizeof(ext));
+      else if (k == 1) ext[3] = g->pout_pressures[i];
+      else status |= far_field(P + 4 * o, g->far_states + 4 * i, nrm, gamma, ext);
+      double er = fabs(ext[1] * nrm[0] + ext[2] * nrm[1]) + sound(ext, gamma);
+      radius[f] = radius[f] >= er ? radius[f] : er;
+    }
+  }
+  double* sum = (double*)calloc(C, sizeof(double));
+  for (int64_t f = 0; f < F; ++f) sum[g->owners[f]] += radius[f] * g->face_lengths[f];
+  for (int64_t i = 0; i < g->n_interior; ++i) {
+    int64_t f = g->interior_faces[i], nb = g->neighbours[f];
+    double r = fabs(P[4 * nb + 1] * g->face_normals[2 * f] + P[4 * nb + 2] * g->face_normals[2 * f + 1]) + cs[nb];
+    sum[nb] += r * g->face_lengths[f];
+  }
+  for (int64_t c = 0; c < C; ++c) {
+    dt[c] = s->cfl * g->areas[c] / sum[c];
+    if (!isfinite(dt[c]) || dt[c] <= 0.0) status |= ORC_TIME_STEP;
+  }
+  free(radius);
+  free(cs);
+  free(sum);
+  return status;
+}
+
+/* One explicit step (solver.py:532-806 and 1128-1182).  dt is a scalar
+ * (dt_per_cell = 0) or [C] (local steady mode, _scale_cell_rate). */
+int orc_explicit_step(const orc_geom* g, const orc_settings* s, int scheme, double* U, const double* dt,
+                      int dt_per_cell) {
+  int64_t C = g->n_cells, N = 4 * C;
+  int st = 0;
+  double* R = (double*)malloc(sizeof(double) * N);
+  double* X[5];
+  for (int k = 0; k < 5; ++k) X[k] = (double*)malloc(sizeof(double) * N);
+  double* R3 = (double*)malloc(sizeof(double) * N);
+  double* Pchk = (double*)malloc(sizeof(double) * N);
+#define DT(i) (dt_per_cell ? dt[(i) / 4] : dt[0])
+#define RES(src)                   \
+  do {                             \
+    st |= orc_residual(g, s, src, R); \
+    if (st) goto out;              \
+  } while (0)
+  memcpy(X[0], U, sizeof(double) * N);
+  if (scheme == 3) {
+    static const double c1 = 0.391752226571890, a20 = 0.444370493651235, a21 = 0.555629506348765,
+                        c2 = 0.368410593050371, a30 = 0.620101851488403, a32 = 0.379898148511597,
+                        c3 = 0.251891774271694, a40 = 0.178079954393132, a43 = 0.821920045606868,
+                        c4 = 0.544974750228521, a52 = 0.517231671970585, a53 = 0.096059710526147,
+                        c5 = 0.063692468666290, a54 = 0.386708617503269, c6 = 0.226007483236906;
+    RES(X[0]);
+    for (int64_t i = 0; i < N; ++i) X[1][i] = X[0][i] + (c1 * DT(i)) * R[i];
+    RES(X[1]);
+    for (int64_t i = 0; i < N; ++i) X[2][i] = a20 * X[0][i] + a21 * X[1][i] + (c2 * DT(i)) * R[i];
+    RES(X[2]);
+    for (int64_t i = 0; i < N; ++i) X[3][i] = a30 * X[0][i] + a32 * X[2][i] + (c3 * DT(i)) * R[i];
+    RES(X[3]);
+    memcpy(R3, R, sizeof(double) * N);
+    for (int64_t i = 0; i < N; ++i) X[4][i] = a40 * X[0][i] + a43 * X[3][i] + (c4 * DT(i)) * R[i];
+    RES(X[4]);
+    for (int64_t i = 0; i < N; ++i)
+      U[i] = a52 * X[2][i] + a53 * X[3][i] + (c5 * DT(i)) * R3[i] + a54 * X[4][i] + (c6 * DT(i)) * R[i];
+  } else {
+    RES(X[0]);
+    for (int64_t i = 0; i < N; ++i) X[1][i] = X[0][i] + DT(i) * R[i];
+    if (scheme == 0) {
+      memcpy(U, X[1], sizeof(double) * N);
+    } else {
+      st |= orc_conservative_to_primitive(C, X[1], s->gamma, Pchk);
+      if (st) goto out;
+      RES(X[1]);
+      if (scheme == 1) {
+        for (int64_t i = 0; i < N; ++i) U[i] = 0.5 * X[0][i] + 0.5 * (X[1][i] + DT(i) * R[i]);
+      } else {
+        for (int64_t i = 0; i < N; ++i) X[2][i] = 0.75 * X[0][i] + 0.25 * (X[1][i] + DT(i) * R[i]);
+        st |= orc_conservative_to_primitive(C, X[2], s->gamma, Pchk);
+        if (st) goto out;
+        RES(X[2]);
+        for (int64_t i = 0; i < N; ++i)
+          U[i] = (1.0 / 3.0) * X[0][i] + (2.0 / 3.0) * (X[2][i] + DT(i) * R[i]);
+      }
+    }
+  }
+  st |= orc_conservative_to_primitive(C, U, s->gamma, Pchk);
+out:
+#undef DT
+#undef RES
+  free(R);
+  for (int k = 0; k < 5; ++k) free(X[k]);
+  free(R3);
+  free(Pchk);
+  return st;
+}

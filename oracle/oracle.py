@@ -1,0 +1,238 @@
+"""ORACLE — test infrastructure only (tests, smoke check, CPU baseline).
+
+ctypes wrapper of ``mcfd_oracle.c``, the plain-C restatement of the
+reference's residual / time-step / explicit-step path, plus a small driver of
+the reference's explicit time loop (``solve_case``, solver.py:437-806) for
+multi-step parity runs.  The product never imports this module.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libmcfd_oracle.so"
+
+FLUX = {"Rusanov": 0, "HLLC": 1, "Roe": 2}
+RECON = {"First order": 0, "MUSCL linear": 1, "MUSCL parabolic": 2}
+LIMITER = {"Barth-Jespersen": 0, "Minmod": 1, "Van Leer": 2, "Venkatakrishnan": 3}
+SCHEME = {"Explicit Euler": 0, "Explicit RK2": 1, "Explicit RK3": 2, "Explicit RK4": 3}
+
+STATUS_TEXT = {
+    0x01: "Euler state has non-finite or non-positive density or pressure.",
+    0x02: "Spatial residual contains non-finite values.",
+    0x04: "HLLC flux produced a non-finite value.",
+    0x08: "Roe average has a non-positive sound speed.",
+    0x10: "Roe flux produced a non-finite value.",
+    0x20: "Far-field characteristics produced invalid sound speed.",
+    0x40: "Far-field characteristics produced an invalid state.",
+    0x80: "Local stable time steps must be positive and finite.",
+}
+
+P64 = C.POINTER(C.c_int64)
+PD = C.POINTER(C.c_double)
+
+
+class OrcGeom(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int64), ("n_faces", C.c_int64),
+        ("centers", PD), ("areas", PD), ("face_centers", PD), ("face_normals", PD), ("face_lengths", PD),
+        ("wall_velocities", PD), ("owners", P64), ("neighbours", P64),
+        ("n_interior", C.c_int64), ("interior_faces", P64),
+        ("interior_owner_offsets", PD), ("interior_neighbour_offsets", PD),
+        ("n_periodic", C.c_int64), ("periodic_faces_a", P64), ("periodic_faces_b", P64),
+        ("n_wall", C.c_int64), ("wall_faces", P64),
+        ("n_vin", C.c_int64), ("vin_faces", P64), ("vin_states", PD),
+        ("n_pout", C.c_int64), ("pout_faces", P64), ("pout_pressures", PD),
+        ("n_far", C.c_int64), ("far_faces", P64), ("far_states", PD),
+        ("n_gradient", C.c_int64), ("gradient_sources", P64), ("gradient_neighbours", P64),
+        ("gradient_cx", PD), ("gradient_cy", PD),
+        ("n_limiter", C.c_int64), ("limiter_cells", P64), ("limiter_dx", PD), ("limiter_dy", PD),
+    ]
+
+
+class OrcSettings(C.Structure):
+    _fields_ = [("flux", C.c_int32), ("reconstruction", C.c_int32), ("limiter", C.c_int32), ("pad", C.c_int32),
+                ("gamma", C.c_double), ("acceleration_x", C.c_double), ("acceleration_y", C.c_double),
+                ("cfl", C.c_double)]
+
+
+def build(force: bool = False) -> Path:
+    src = HERE / "mcfd_oracle.c"
+    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        LIB.parent.mkdir(exist_ok=True)
+        subprocess.run(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c99", "-shared",
+                        "-o", str(LIB), str(src), "-lm"], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build()))
+        _lib.orc_residual.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), PD, PD]
+        _lib.orc_stable_time_steps.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), PD, PD]
+        _lib.orc_explicit_step.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), C.c_int, PD, PD, C.c_int]
+        _lib.orc_conservative_to_primitive.argtypes = [C.c_int64, PD, C.c_double, PD]
+        _lib.orc_primitive_to_conservative.argtypes = [C.c_int64, PD, C.c_double, PD]
+        _lib.orc_linear_gradients_and_factors.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD]
+    return _lib
+
+
+class OracleError(ValueError):
+    pass
+
+
+def _raise(code: int):
+    for bit, text in STATUS_TEXT.items():
+        if code & bit:
+            raise OracleError(text)
+    if code:
+        raise OracleError(f"oracle status {code:#x}")
+
+
+class Oracle:
+    """Binds one geometry (reference ``_Geometry`` or ``meshcfd_gb300`` Geometry)."""
+
+    def __init__(self, geometry):
+        g = geometry
+        keep = {}
+
+        def arr(name, dtype, shape=None):
+            v = getattr(g, name, None)
+            if v is None:
+                return None
+            a = np.ascontiguousarray(np.asarray(v, dtype=dtype))
+            if shape is not None:
+                a = a.reshape(shape)
+            keep[name] = a
+            return a
+
+        def p(a, kind):
+            return a.ctypes.data_as(kind) if a is not None and a.size else None
+
+        n_cells = len(g.areas)
+        n_faces = len(g.face_lengths)
+        fields = dict(
+            centers=arr("centers", np.float64, (-1, 2)), areas=arr("areas", np.float64),
+            face_centers=arr("face_centers", np.float64, (-1, 2)), face_normals=arr("face_normals", np.float64, (-1, 2)),
+            face_lengths=arr("face_lengths", np.float64), wall_velocities=arr("wall_velocities", np.float64, (-1, 2)),
+            owners=arr("owners", np.int64), neighbours=arr("neighbours", np.int64),
+            interior_faces=arr("interior_faces", np.int64),
+            interior_owner_offsets=arr("interior_owner_offsets", np.float64, (-1, 2)),
+            interior_neighbour_offsets=arr("interior_neighbour_offsets", np.float64, (-1, 2)),
+            periodic_faces_a=arr("periodic_faces_a", np.int64), periodic_faces_b=arr("periodic_faces_b", np.int64),
+            wall_faces=arr("wall_faces", np.int64),
+            vin_faces=arr("velocity_inlet_faces", np.int64), vin_states=arr("velocity_inlet_states", np.float64, (-1, 4)),
+            pout_faces=arr("pressure_outlet_faces", np.int64), pout_pressures=arr("pressure_outlet_pressures", np.float64),
+            far_faces=arr("far_field_faces", np.int64), far_states=arr("far_field_states", np.float64, (-1, 4)),
+            gradient_sources=arr("gradient_sources", np.int64), gradient_neighbours=arr("gradient_neighbours", np.int64),
+            gradient_cx=arr("gradient_coefficients_x", np.float64), gradient_cy=arr("gradient_coefficients_y", np.float64),
+            limiter_cells=arr("limiter_cells", np.int64), limiter_dx=arr("limiter_dx", np.float64),
+            limiter_dy=arr("limiter_dy", np.float64),
+        )
+        if getattr(g, "pressure_inlets", ()) or getattr(g, "mass_flow_inlets", ()) or getattr(g, "mass_flow_outlets", ()):
+            raise NotImplementedError("oracle: pressure-inlet / mass-flow boundaries")
+        s = OrcGeom()
+        s.n_cells, s.n_faces = n_cells, n_faces
+        for name, a in fields.items():
+            kind = P64 if a is not None and a.dtype == np.int64 else PD
+            setattr(s, name, p(a, kind))
+        s.n_interior = len(fields["interior_faces"])
+        s.n_periodic = len(fields["periodic_faces_a"])
+        s.n_wall = len(fields["wall_faces"])
+        s.n_vin = len(fields["vin_faces"])
+        s.n_pout = len(fields["pout_faces"])
+        s.n_far = len(fields["far_faces"])
+        s.n_gradient = len(fields["gradient_sources"])
+        s.n_limiter = len(fields["limiter_cells"])
+        self.struct = s
+        self._keep = keep
+        self.n_cells = n_cells
+
+    @staticmethod
+    def settings(num) -> OrcSettings:
+        s = OrcSettings()
+        s.flux = FLUX[num.flux]
+        s.reconstruction = RECON[num.reconstruction]
+        s.limiter = LIMITER[num.limiter]
+        s.gamma = num.gamma
+        s.acceleration_x = num.acceleration_x
+        s.acceleration_y = num.acceleration_y
+        s.cfl = num.cfl
+        return s
+
+    def primitive(self, U, gamma):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        P = np.empty_like(U)
+        code = lib().orc_conservative_to_primitive(len(U), U.ctypes.data_as(PD), gamma, P.ctypes.data_as(PD))
+        _raise(code)
+        return P
+
+    def conservative(self, P, gamma):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        U = np.empty_like(P)
+        lib().orc_primitive_to_conservative(len(P), P.ctypes.data_as(PD), gamma, U.ctypes.data_as(PD))
+        return U
+
+    def residual(self, U, num):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        R = np.empty_like(U)
+        s = self.settings(num)
+        _raise(lib().orc_residual(C.byref(self.struct), C.byref(s), U.ctypes.data_as(PD), R.ctypes.data_as(PD)))
+        return R
+
+    def gradients_and_factors(self, P, limiter):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        grad = np.empty((len(P), 4, 2))
+        fac = np.empty((len(P), 4))
+        lib().orc_linear_gradients_and_factors(C.byref(self.struct), P.ctypes.data_as(PD), LIMITER[limiter],
+                                               grad.ctypes.data_as(PD), fac.ctypes.data_as(PD))
+        return grad, fac
+
+    def stable_time_steps(self, P, num):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        dt = np.empty(len(P))
+        s = self.settings(num)
+        _raise(lib().orc_stable_time_steps(C.byref(self.struct), C.byref(s), P.ctypes.data_as(PD), dt.ctypes.data_as(PD)))
+        return dt
+
+    def explicit_step(self, U, num, dt):
+        U = np.array(U, dtype=np.float64, order="C", copy=True)
+        dt_arr = np.ascontiguousarray(np.atleast_1d(np.asarray(dt, dtype=np.float64)))
+        s = self.settings(num)
+        code = lib().orc_explicit_step(C.byref(self.struct), C.byref(s), SCHEME[num.time_integration],
+                                       U.ctypes.data_as(PD), dt_arr.ctypes.data_as(PD), int(dt_arr.size > 1))
+        _raise(code)
+        return U
+
+    def solve(self, U, num, steps, time=0.0, history=None):
+        """The reference's explicit loop (solver.py:437-806) for ``steps`` steps:
+        primitive check, time step (global adaptive / fixed / local), one step."""
+        U = np.array(U, dtype=np.float64, copy=True)
+        for _ in range(steps):
+            P = self.primitive(U, num.gamma)
+            if num.time_step_mode == "Local (steady)":
+                dt = self.stable_time_steps(P, num)
+                time_step = float(np.mean(dt))
+            elif num.time_step_mode == "Global fixed":
+                time_step = min(num.fixed_time_step, num.end_time - time)
+                dt = time_step
+            else:
+                time_step = min(float(np.min(self.stable_time_steps(P, num))), num.end_time - time)
+                dt = time_step
+            if not math.isfinite(time_step) or time_step <= 0.0:
+                raise OracleError("The stable time step is non-positive or non-finite.")
+            U = self.explicit_step(U, num, dt)
+            time += time_step
+            if history is not None:
+                history.append((time_step, U.copy()))
+        return U, time

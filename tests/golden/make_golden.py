@@ -1,0 +1,172 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Run from the repository root:  python tests/golden/make_golden.py
+(needs a reference checkout, see reference_shim.py).  Each .npz holds the
+reference's own geometry arrays (prefixed ``geom_``), the input state and the
+reference's outputs, so the tests can run without the reference:
+
+* residual_<case>.npz  — ``_residual`` for every flux x reconstruction x
+  limiter combination, with and without a body force, plus
+  ``_stable_time_steps``;
+* solve_<case>.npz     — final states of ``solve_case`` after N explicit steps.
+"""
+
+from __future__ import annotations
+
+import itertools
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(HERE.parents[1]))
+
+from reference_shim import import_reference, reference_case  # noqa: E402
+
+from meshcfd_gb300.meshes import (  # noqa: E402
+    box_mesh,
+    cell_centroids,
+    periodic_case,
+    riemann_case,
+    smooth_primitive,
+    vortex_case,
+    vortex_primitive,
+)
+from meshcfd_gb300.model import Case  # noqa: E402
+
+GEOM_FIELDS = (
+    "centers", "areas", "face_centers", "face_normals", "face_lengths", "wall_velocities", "owners",
+    "neighbours", "interior_faces", "interior_owners", "interior_neighbours", "interior_normals",
+    "interior_lengths", "interior_owner_offsets", "interior_neighbour_offsets", "wall_faces",
+    "symmetry_faces", "periodic_faces_a", "periodic_faces_b", "velocity_inlet_faces",
+    "velocity_inlet_states", "pressure_outlet_faces", "pressure_outlet_pressures", "far_field_faces",
+    "far_field_states", "gradient_sources", "gradient_neighbours", "gradient_dx", "gradient_dy",
+    "gradient_coefficients_x", "gradient_coefficients_y", "limiter_cells", "limiter_dx", "limiter_dy",
+)
+FLUXES = ("Rusanov", "HLLC", "Roe")
+LIMITERS = ("Barth-Jespersen", "Minmod", "Van Leer", "Venkatakrishnan")
+
+
+def channel_case(nx=7, ny=5):
+    mesh = box_mesh(nx, ny, 2.0, 1.0, split="half", jitter=0.2, seed=5)
+    case = Case(name="channel", mesh=mesh)
+    for c in case.boundary_conditions:
+        if c.patch_name == "left":
+            c.kind = "Velocity Inlet"
+            c.values = {"density": 1.0, "velocity_x": 0.3, "velocity_y": 0.05, "temperature": 1.0 / 287.05}
+        elif c.patch_name == "right":
+            c.kind = "Pressure Outlet"
+            c.values = {"pressure": 0.95}
+        elif c.patch_name == "top":
+            c.kind = "Symmetry"
+        else:
+            c.kind = "Wall"
+            c.mechanical_condition = "Slip"
+    return case
+
+
+def mesh_arrays(case):
+    m = case.mesh
+    return {
+        "mesh_points": np.asarray(m.points), "mesh_cell_offsets": np.asarray(m.cells.offsets),
+        "mesh_cell_nodes": np.asarray(m.cells.nodes), "mesh_faces": np.asarray(m.faces),
+        "mesh_face_owners": np.asarray(m.face_owners), "mesh_face_neighbours": np.asarray(m.face_neighbours),
+        "mesh_face_patch_ids": np.asarray(m.face_patch_ids),
+    }
+
+
+def geometry_arrays(geometry):
+    return {f"geom_{name}": np.asarray(getattr(geometry, name)) for name in GEOM_FIELDS}
+
+
+def perturbed_primitive(n, seed):
+    P = smooth_primitive(n, seed=seed, amplitude=2.0)
+    P[:, 1] += 0.3 * np.sin(np.arange(n))
+    P[:, 3] *= 1.0 + 0.2 * np.cos(0.7 * np.arange(n))
+    return P
+
+
+def residual_fixture(name, case, ref):
+    rc = reference_case(case, ref)
+    rg = ref.solver._build_geometry(rc.mesh, rc)
+    out = {**mesh_arrays(case), **geometry_arrays(rg)}
+    n = len(rg.areas)
+    P = perturbed_primitive(n, seed=1)
+    U = ref.euler.primitive_to_conservative(P, 1.4)
+    out["U"] = U
+    num = rc.numerics
+    keys = []
+    for flux, recon, limiter, force in itertools.product(FLUXES, ("First order", "MUSCL linear"), LIMITERS, (0, 1)):
+        if recon == "First order" and limiter != "Barth-Jespersen":
+            continue
+        num.flux, num.reconstruction, num.limiter = flux, recon, limiter
+        num.acceleration_x, num.acceleration_y = (0.3, -0.2) if force else (0.0, 0.0)
+        key = f"R|{flux}|{recon}|{limiter}|{force}"
+        out[key] = ref.solver._residual(U, rg, num)
+        keys.append(key)
+    num.acceleration_x = num.acceleration_y = 0.0
+    num.cfl = 0.7
+    out["dt_cells"] = ref.solver._stable_time_steps(ref.euler.conservative_to_primitive(U, 1.4), rg, num)
+    # limiter factors and gradients of the compiled kernels, for every code
+    Pp = ref.euler.conservative_to_primitive(U, 1.4)
+    for code in range(4):
+        g, f = ref.kernels.linear_gradients_and_factors(
+            Pp, rg.gradient_sources, rg.gradient_neighbours, rg.gradient_coefficients_x,
+            rg.gradient_coefficients_y, rg.limiter_cells, rg.limiter_dx, rg.limiter_dy, code)
+        out[f"grad|{code}"] = g
+        out[f"factors|{code}"] = f
+    out["cfl"] = np.array(0.7)
+    np.savez_compressed(HERE / f"residual_{name}.npz", **out)
+    print(name, n, "cells,", len(keys), "residuals")
+
+
+def solve_fixture(name, case, primitive, settings, steps, ref):
+    rc = reference_case(case, ref)
+    for key, value in settings.items():
+        setattr(rc.numerics, key, value)
+    rc.numerics.max_iterations = steps
+    rc.numerics.end_time = 1.0e30
+    rc.numerics.residual_tolerance = 1e-300
+    rc.numerics.convergence_history_interval = steps + 1
+    rg = ref.solver._build_geometry(rc.mesh, rc)
+    states = tuple(ref.model.InitialState(*map(float, row)) for row in primitive)
+    result = ref.solver.solve_case(rc, states)
+    final = np.array([(s.density, s.velocity_x, s.velocity_y, s.pressure) for s in result.states])
+    out = {**mesh_arrays(case), **geometry_arrays(rg), "P0": primitive, "P_final": final,
+           "time": np.array(result.time), "steps": np.array(result.steps)}
+    for key, value in settings.items():
+        out[f"set|{key}"] = np.array(value)
+    np.savez_compressed(HERE / f"solve_{name}.npz", **out)
+    print(name, len(primitive), "cells,", result.steps, "steps, t =", result.time)
+
+
+def main():
+    ref = import_reference()
+    riemann, riemann_p = riemann_case(16)
+    residual_fixture("riemann16", riemann, ref)
+    residual_fixture("periodic_mixed", periodic_case(8, 6, split="half", jitter=0.25, seed=2), ref)
+    residual_fixture("channel", channel_case(), ref)
+
+    solve_fixture("riemann16_euler", riemann, riemann_p,
+                  {"flux": "Rusanov", "reconstruction": "First order", "time_integration": "Explicit Euler",
+                   "cfl": 0.5}, 40, ref)
+    vortex, _ = vortex_case(12, seed=0, jitter=0.15, split="half")
+    vp = vortex_primitive(cell_centroids(vortex.mesh))
+    solve_fixture("vortex12_rk3", vortex, vp,
+                  {"flux": "HLLC", "reconstruction": "MUSCL linear", "limiter": "Venkatakrishnan",
+                   "time_integration": "Explicit RK3", "cfl": 0.8}, 12, ref)
+    chan = channel_case()
+    cp = perturbed_primitive(len(chan.mesh.cells), seed=3)
+    cp[:, 0] = np.abs(cp[:, 0])
+    solve_fixture("channel_rk4_local", chan, cp,
+                  {"flux": "Roe", "reconstruction": "MUSCL linear", "limiter": "Barth-Jespersen",
+                   "time_integration": "Explicit RK4", "cfl": 0.6, "time_step_mode": "Local (steady)"}, 6, ref)
+    solve_fixture("channel_rk2_vanleer", chan, cp,
+                  {"flux": "HLLC", "reconstruction": "MUSCL linear", "limiter": "Van Leer",
+                   "time_integration": "Explicit RK2", "cfl": 0.6, "acceleration_x": 0.2}, 8, ref)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,58 @@
+"""Import the reference package (jesuspueblas/meshcfd) from a local checkout.
+
+Test infrastructure only: used to generate the golden fixtures in this folder
+and by CPU tests that compare against the live reference when a checkout is
+present.  Numba is not installed here, so a stub ``numba.njit`` (identity
+decorator) is registered first: the reference's compiled kernels then run as
+plain Python with the same operation order.  PyQt5 is absent, so only the
+non-GUI modules are imported.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import types
+from pathlib import Path
+
+REFERENCE = Path(os.environ.get("MESHCFD_REFERENCE", "/root/reference"))
+
+
+def available() -> bool:
+    return (REFERENCE / "src" / "meshcfd" / "core" / "solver.py").exists()
+
+
+def import_reference():
+    """Return the reference's ``meshcfd.core`` modules as a namespace."""
+    if not available():
+        raise ImportError(f"reference checkout not found at {REFERENCE}")
+    if "numba" not in sys.modules:
+        stub = types.ModuleType("numba")
+        stub.njit = lambda *a, **k: (a[0] if a and callable(a[0]) else (lambda f: f))
+        sys.modules["numba"] = stub
+    for p in (str(REFERENCE / "src"), str(REFERENCE)):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    from meshcfd.core import _kernels, euler, model, solver  # noqa: E402
+
+    return types.SimpleNamespace(solver=solver, euler=euler, model=model, kernels=_kernels)
+
+
+def reference_case(case, ref):
+    """Rebuild one of our cases with the reference's own dataclasses."""
+    from meshcfd_gb300.meshes import to_reference_mesh
+
+    m = ref.model
+    mesh = to_reference_mesh(case.mesh, m.FiniteVolumeMesh)
+    mesh.patches = tuple(m.MeshPatch(p.id, p.name, tuple(int(f) for f in p.face_ids)) for p in case.mesh.patches)
+    rcase = m.Case(name=case.name, mesh=mesh)
+    rcase.boundary_conditions = [
+        m.BoundaryCondition(c.patch_id, c.patch_name, c.kind, dict(c.values), c.thermal_condition,
+                            c.mechanical_condition)
+        for c in case.boundary_conditions
+    ]
+    rcase.periodic_pairs = [m.PeriodicBoundaryPair(p.patch_a_id, p.patch_b_id, p.axis, p.pitch)
+                            for p in case.periodic_pairs]
+    for key, value in vars(case.numerics).items():
+        setattr(rcase.numerics, key, value)
+    return rcase

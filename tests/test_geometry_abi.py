@@ -1,0 +1,108 @@
+"""Host side: geometry builder vs the reference's geometry (golden), mesh
+generators, and the C ABI library's exports (no GPU needed)."""
+
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, fixture_mesh, load_fixture
+
+FIELDS = ("centers", "areas", "face_centers", "face_normals", "face_lengths", "interior_faces",
+          "interior_owner_offsets", "interior_neighbour_offsets", "wall_faces", "periodic_faces_a",
+          "periodic_faces_b", "velocity_inlet_faces", "velocity_inlet_states", "pressure_outlet_faces",
+          "pressure_outlet_pressures", "far_field_faces", "far_field_states", "gradient_sources",
+          "gradient_neighbours", "gradient_coefficients_x", "gradient_coefficients_y", "limiter_cells",
+          "limiter_dx", "limiter_dy")
+
+
+def _case_for(name):
+    from make_golden import channel_case
+    from meshcfd_gb300.meshes import periodic_case, riemann_case
+
+    return {"riemann16": lambda: riemann_case(16)[0],
+            "periodic_mixed": lambda: periodic_case(8, 6, split="half", jitter=0.25, seed=2),
+            "channel": channel_case}[name]()
+
+
+@pytest.mark.parametrize("name", ("riemann16", "periodic_mixed", "channel"))
+def test_geometry_builder_is_bit_exact(name):
+    from meshcfd_gb300.geometry import build_geometry
+
+    data, ref = load_fixture(f"residual_{name}.npz")
+    case = _case_for(name)
+    # the generator reproduces the fixture's mesh exactly
+    mesh = fixture_mesh(data)
+    np.testing.assert_array_equal(np.asarray(case.mesh.points), mesh.points)
+    np.testing.assert_array_equal(np.asarray(case.mesh.faces), mesh.faces)
+    g = build_geometry(case.mesh, case)
+    for field in FIELDS:
+        np.testing.assert_array_equal(np.asarray(getattr(g, field)).reshape(np.shape(getattr(ref, field))),
+                                      getattr(ref, field), err_msg=field)
+
+
+def test_workload_mesh_sizes():
+    from meshcfd_gb300.meshes import riemann_case, vortex_case
+
+    case, P = riemann_case(128)
+    m = case.mesh
+    assert len(m.cells) == 32768 and len(m.faces) == 49408
+    assert int((np.asarray(m.face_neighbours) >= 0).sum()) == 48896
+    assert P.shape == (32768, 4)
+    v, _ = vortex_case(32)
+    assert len(v.mesh.cells) == 32 * 32 + 32 * 32 // 2
+
+
+def test_periodic_matching_rejects_mismatch():
+    from meshcfd_gb300.errors import SolverError
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import periodic_case
+
+    case = periodic_case(4, 3)
+    case.periodic_pairs[0] = type(case.periodic_pairs[0])(1, 3, "x", 2.0)  # stale pitch
+    with pytest.raises(SolverError, match="stale axis or pitch"):
+        build_geometry(case.mesh, case)
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "meshcfd_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mcfd_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    from meshcfd_gb300 import _lib
+
+    native = _lib.native()
+    declared = _declared_symbols()
+    assert len(declared) >= 10
+    for name in declared:
+        assert hasattr(native.lib, name), name
+    assert set(declared) == set(_lib.SIGNATURES), "ctypes signatures out of sync with the header"
+    assert native.mcfd_abi_version() == 1
+    assert native.mcfd_error_string(3) == b"option not supported by the GPU path"
+
+
+def test_host_geometry_helpers_reject_degenerate_cells():
+    from meshcfd_gb300 import _lib
+    from meshcfd_gb300.errors import SolverError
+
+    native = _lib.native()
+    points = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0]])
+    with pytest.raises(SolverError, match="Cell 0 has zero or invalid area"):
+        native.cell_geometry(np.array([0, 3]), np.array([0, 1, 2]), points)
+    with pytest.raises(SolverError, match="Face 0 has zero or invalid length"):
+        native.face_geometry(np.array([[0, 0]]), points, np.zeros((1, 2)), np.array([0]))
+
+
+def test_config_mapping_rejects_unsupported_models():
+    from meshcfd_gb300.device import make_config
+    from meshcfd_gb300.model import NumericalSettings
+
+    with pytest.raises(NotImplementedError):
+        make_config(NumericalSettings(viscosity_model="Constant"))
+    with pytest.raises(NotImplementedError):
+        make_config(NumericalSettings(reconstruction="MUSCL parabolic"))
+    cfg = make_config(NumericalSettings(flux="Roe", limiter="Van Leer", reconstruction="MUSCL linear"))
+    assert (cfg.flux, cfg.limiter, cfg.reconstruction) == (2, 2, 1)
