@@ -36,6 +36,7 @@ extern "C" {
 #define MCFD_E_CUDA 2        /* a CUDA runtime call failed */
 #define MCFD_E_UNSUPPORTED 3 /* option outside what the GPU path implements */
 #define MCFD_E_GEOMETRY 4    /* geometry description inconsistent */
+#define MCFD_E_TOO_LARGE 5   /* size beyond the fixed scratch of the allocation-free entry point */
 
 /* ---- device status bits (numerical failures; reference messages) ---- */
 #define MCFD_S_NONPHYSICAL_STATE 0x01  /* euler.py:34-39 non-finite or non-positive rho/p */
@@ -229,6 +230,19 @@ int mcfd_profile_read(mcfd_geom* geom, double* total_ms, int64_t* groups);
 
 /* Number of kernels this library has launched in the process so far. */
 int64_t mcfd_launch_count(void);
+
+/*
+ * Allocation-free sum of squares: sums[k] = sum over i < n_cells of
+ * R[i][k]^2 (k = 0..3), the same reduction and summation order as
+ * mcfd_residual_sumsq, but with no geometry handle and no device allocation.
+ * No counterpart in the reference (it exists for callers that cannot call
+ * cudaMalloc, such as a monitor inside a host time loop whose device memory is
+ * owned by another allocator).  Its scratch is a fixed 19,456-byte __device__
+ * array shared by all calls: overlapping calls race.  The first call on each
+ * device looks up that array's address (call it once before any stream
+ * capture).  n_cells above 2^30 returns MCFD_E_TOO_LARGE.
+ */
+int mcfd_residual_sumsq_noalloc(const double* R, int64_t n_cells, double* sums, void* stream);
 
 /* ---- host helpers (no GPU needed) ---- */
 

@@ -82,6 +82,7 @@ SIGNATURES = {
     "mcfd_profile_enable": (c_i32, [c_vp, c_i32]),
     "mcfd_profile_read": (c_i32, [c_vp, P_dbl, P_i64]),
     "mcfd_launch_count": (c_i64, []),
+    "mcfd_residual_sumsq_noalloc": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "mcfd_host_cell_geometry": (c_i32, [c_i64, P_i64, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
     "mcfd_host_face_geometry": (c_i32, [c_i64, P_i64, P_dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
 }

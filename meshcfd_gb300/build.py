@@ -25,6 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("mcfd_kernels.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),
+    ("mcfd_noalloc.cu", ["-fmad=false"]),
 ]
 
 

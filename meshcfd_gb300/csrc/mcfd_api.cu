@@ -126,6 +126,7 @@ const char* mcfd_error_string(int code) {
     case MCFD_E_CUDA: return "CUDA runtime error";
     case MCFD_E_UNSUPPORTED: return "option not supported by the GPU path";
     case MCFD_E_GEOMETRY: return "inconsistent geometry description";
+    case MCFD_E_TOO_LARGE: return "size exceeds the maximum of the allocation-free entry point";
     default: return "unknown error";
   }
 }

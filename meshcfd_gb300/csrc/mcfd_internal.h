@@ -110,6 +110,9 @@ cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const do
                               double* dt_cells, double* dt_min, double time_limit,
                               cudaStream_t s);
 long long launch_count();
+// reduction kernels of the sum of squares (defined in mcfd_kernels.cu)
+__global__ void k_sumsq_partial(int n, const double* __restrict__ R, double* __restrict__ partials);
+__global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums);
 cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,
                          double* sums, cudaStream_t s);
 
