@@ -39,7 +39,7 @@ UNIT = "cell-updates/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gpu", "reference"), default="gpu")
     ap.add_argument("--workload", default="vortex1024", choices=("vortex1024", "vortex1024all", "vortex512", "vortex256"))
@@ -47,6 +47,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=5, help="RK3 steps of the CPU baseline sample")
     ap.add_argument("--profile-steps", type=int, default=3)
+    ap.add_argument("--mode", choices=("fast", "exact", "fma"), default="fast",
+                    help="exact: reference operation order, bit-exact; fast: exact arithmetic with the "
+                         "limiter minimum through the smallest ratio; fma: shared reciprocals + FMA "
+                         "(outside the 1e-12 bar on fine meshes)")
+    ap.add_argument("--parity-steps", type=int, default=10)
+    ap.add_argument("--variant-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -224,7 +230,12 @@ def run_gpu(args):
 
     case, settings, g, P0, config = make_workload(args.workload)
     config["parallelism"] = f"replicas x{world}"
-    cfg = make_config(settings)
+    cfg = make_config(settings, mode=args.mode)
+    config["precision"] = {
+        "exact": "fp64, reference operation order (no FMA), bit-exact",
+        "fast": "fp64, reference arithmetic, limiter minimum through the smallest ratio",
+        "fma": "fp64, FMA + shared reciprocals",
+    }[args.mode]
     native = _lib.native()
     dg = DeviceGeometry(g, device)
     C = dg.n_cells
@@ -334,6 +345,57 @@ def run_gpu(args):
                "h2d_bytes_per_step": int(host.numel() * 8), "d2h_bytes_per_step": int(out.numel() * 8),
                "ms_per_step": ms2 / args.steps}
 
+    # parity of this run's kernels against the bit-exact path (which the
+    # parity tests hold equal to the reference): one residual, and
+    # --parity-steps steps, from the initial state of the workload
+    parity = None
+    if args.parity_steps > 0:
+        cfg_exact = make_config(settings, mode="exact")
+        U0 = torch.as_tensor(U_init, device=device)
+        Ra = dg.residual(U0, cfg)
+        Rb = dg.residual(U0, cfg_exact)
+        res_err = float((Ra - Rb).abs().max() / Rb.abs().max())
+        Ua, Ub = U0.clone(), U0.clone()
+        for Uc, cf in ((Ua, cfg), (Ub, cfg_exact)):
+            Pc = dg.primitive(Uc, cf)
+            Pc = Pc.clone()
+            for _ in range(args.parity_steps):
+                dg.time_steps(Pc, cf, out_min=dt)
+                dg.explicit_step(Uc, cf, 2, dt)
+                Pc = dg.primitive(Uc, cf)
+        dg.check_status()
+        parity = {"reference": "bit-exact path (equal to the reference, see tests/test_gpu_parity.py)",
+                  "residual_max_rel_err": res_err, "steps": args.parity_steps,
+                  "state_max_rel_err": float((Ua - Ub).abs().max() / Ub.abs().max())}
+
+    # the other kernel variants on the same workload: step time and the
+    # residual's deviation from the bit-exact path
+    variants = {}
+    if args.variant_steps > 0:
+        cfg_exact = make_config(settings, mode="exact")
+        U0 = torch.as_tensor(U_init, device=device)
+        Rb = dg.residual(U0, cfg_exact)
+        for mode in ("exact", "fast", "fma"):
+            cf = make_config(settings, mode=mode)
+            Ra = dg.residual(U0, cf)
+            err = float((Ra - Rb).abs().max() / Rb.abs().max())
+            Uv = U0.clone()
+            dg.primitive(Uv, cf, out=P)
+            for _ in range(2):
+                dg.time_steps(P, cf, out_min=dt)
+                dg.explicit_step(Uv, cf, 2, dt)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(args.variant_steps):
+                dg.time_steps(P, cf, out_min=dt)
+                dg.explicit_step(Uv, cf, 2, dt)
+            b.record(stream)
+            torch.cuda.synchronize()
+            msv = a.elapsed_time(b) / args.variant_steps
+            variants[mode] = {"ms_per_step": msv, "value": C / (msv * 1e-3), "residual_max_rel_err": err}
+        dg.check_status()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, secs = cpu_oracle_rate(g, settings, P0, args.cpu_steps)
@@ -347,7 +409,8 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded vortex mesh and state)",
             "config": config, "gpu_launches": int(launches), "roofline": roofline, "kernels": kernels,
-            "e2e": e2e, "cpu_baseline": cpu, "clocks": clock,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clock, "parity": parity, "mode": args.mode,
+            "variants": variants,
         }
         print(json.dumps(line))
     if dist is not None:

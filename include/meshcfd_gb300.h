@@ -67,6 +67,10 @@ typedef struct mcfd_status {
 #define MCFD_LIMITER_MINMOD 1
 #define MCFD_LIMITER_VAN_LEER 2
 #define MCFD_LIMITER_VENKATAKRISHNAN 3
+/* kernel variants */
+#define MCFD_MODE_EXACT 0 /* reference operation order, no FMA: bit-exact */
+#define MCFD_MODE_FAST 1  /* exact arithmetic, limiter minimum via the smallest ratio */
+#define MCFD_MODE_FMA 2   /* + shared reciprocals and FMA: ~1e-11 on fine meshes */
 /* time integration (model.py:28-34) */
 #define MCFD_TIME_EULER 0
 #define MCFD_TIME_RK2 1
@@ -77,7 +81,7 @@ typedef struct mcfd_config {
   int32_t flux;           /* MCFD_FLUX_* */
   int32_t reconstruction; /* MCFD_RECON_* */
   int32_t limiter;        /* MCFD_LIMITER_* */
-  int32_t exact;          /* 1: reference operation order, no FMA contraction */
+  int32_t mode;           /* MCFD_MODE_*: kernel variant */
   double gamma;           /* ratio of specific heats (NumericalSettings.gamma) */
   double acceleration_x;  /* body force (solver.py:2709-2715) */
   double acceleration_y;

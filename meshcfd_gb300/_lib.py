@@ -31,7 +31,7 @@ class Config(C.Structure):
         ("flux", c_i32),
         ("reconstruction", c_i32),
         ("limiter", c_i32),
-        ("exact", c_i32),
+        ("mode", c_i32),
         ("gamma", c_dbl),
         ("acceleration_x", c_dbl),
         ("acceleration_y", c_dbl),

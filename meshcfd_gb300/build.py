@@ -23,7 +23,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, extra flags)
 UNITS = [
-    ("mcfd_kernels.cu", ["-fmad=false"]),
+    ("mcfd_kernels_exact.cu", ["-fmad=false"]),
+    ("mcfd_kernels_fast.cu", ["-fmad=false"]),
+    ("mcfd_kernels_fma.cu", ["-fmad=true"]),
+    ("mcfd_kernels_common.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),
     ("mcfd_noalloc.cu", ["-fmad=false"]),
 ]

@@ -65,6 +65,7 @@ static int check_cfg(const mcfd_config* cfg) {
   if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC) return MCFD_E_UNSUPPORTED;
   if (cfg->reconstruction < 0 || cfg->reconstruction > 2) return MCFD_E_ARG;
   if (!(cfg->gamma > 1.0)) return MCFD_E_ARG;
+  if (cfg->mode < MCFD_MODE_EXACT || cfg->mode > MCFD_MODE_FMA) return MCFD_E_ARG;
   return MCFD_OK;
 }
 
@@ -93,17 +94,21 @@ static cudaError_t timed(mcfd_geom* h, int cls, cudaStream_t s, F&& launch) {
   return e;
 }
 
+// Kernel variant dispatch on cfg.mode.
+#define MCFD_DISPATCH(cfg, call) \
+  ((cfg).mode == MCFD_MODE_FAST ? fast::call : (cfg).mode == MCFD_MODE_FMA ? fma::call : exact::call)
+
 // One residual evaluation of the state whose primitive is in ws.P, followed
 // by the gather with the given stage program.
 static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgram& prog,
                          cudaStream_t s) {
   cudaError_t e = cudaSuccess;
   if (cfg.reconstruction == MCFD_RECON_MUSCL_LINEAR)
-    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return launch_reconstruct(h->g, cfg, h->ws.P, h->ws.recon, s); });
+    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return MCFD_DISPATCH(cfg, launch_reconstruct(h->g, cfg, h->ws.P, h->ws.recon, s)); });
   if (e == cudaSuccess)
-    e = timed(h, MCFD_PROF_FLUX, s, [&] { return launch_flux(h->g, cfg, h->ws.P, h->ws.recon, h->ws.flux, s); });
+    e = timed(h, MCFD_PROF_FLUX, s, [&] { return MCFD_DISPATCH(cfg, launch_flux(h->g, cfg, h->ws.P, h->ws.recon, h->ws.flux, s)); });
   if (e == cudaSuccess)
-    e = timed(h, MCFD_PROF_GATHER, s, [&] { return launch_gather(h->g, cfg, h->ws.P, h->ws.flux, prog, s); });
+    e = timed(h, MCFD_PROF_GATHER, s, [&] { return MCFD_DISPATCH(cfg, launch_gather(h->g, cfg, h->ws.P, h->ws.flux, prog, s)); });
   return e;
 }
 
@@ -514,7 +519,7 @@ int mcfd_primitive(mcfd_geom* h, const mcfd_config* cfg, const double* U, double
   int c = check_cfg(cfg);
   if (c) return c;
   cudaStream_t s = (cudaStream_t)stream;
-  return rc(timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return launch_primitive(h->g, *cfg, U, P, s); }));
+  return rc(timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, P, s)); }));
 }
 
 
@@ -523,7 +528,7 @@ int mcfd_residual(mcfd_geom* h, const mcfd_config* cfg, const double* U, double*
   int c = check_cfg(cfg);
   if (c) return c;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return launch_primitive(h->g, *cfg, U, h->ws.P, s); });
+  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, h->ws.P, s)); });
   StageProgram prog{};
   prog.out_r = R;
   if (e == cudaSuccess) e = stage(h, *cfg, prog, s);
@@ -538,7 +543,7 @@ int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, doubl
   if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_TIME_STEP, s,
-                  [&] { return launch_time_steps(h->g, *cfg, P, dt_cells, dt_min, time_limit, s); }));
+                  [&] { return MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, dt_min, time_limit, s)); }));
 }
 
 
@@ -550,7 +555,7 @@ int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, dou
   if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Workspace& w = h->ws;
-  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return launch_primitive(h->g, *cfg, U, w.P, s); });
+  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, w.P, s)); });
   auto run = [&](std::initializer_list<StageTerm> terms, double* out, double* save_r) {
     if (e != cudaSuccess) return;
     StageProgram p{};

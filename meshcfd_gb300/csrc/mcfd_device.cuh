@@ -32,12 +32,61 @@ __device__ __forceinline__ void st4(double* p, const St4& s) {
   q[1] = make_double2(s.c, s.d);
 }
 
-// Python / NumPy min/max semantics on non-NaN data, written as selects.
-__device__ __forceinline__ double py_min(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double py_max(double a, double b) { return (b > a) ? b : a; }
+
+// ---------------------------------------------------------------------------
+// IEEE-754 comparisons evaluated on the integer pipe.  On GB300 the FP64 pipe
+// issues ~1/38 the integer rate (measured), and compares / min / max /
+// finiteness tests take FP64 issue slots like arithmetic does.  Each helper
+// below returns exactly the IEEE result for non-NaN operands (signed zeros
+// compare equal); NaN never reaches a decision whose outcome matters (every
+// path that can produce NaN also sets a status bit from a finiteness test).
+namespace icmp {
+
+__device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+
+// Monotone key: x < y  <=>  key(x) < key(y); -0 and +0 both map to 0.
+__device__ __forceinline__ long long key(double x) {
+  long long b = bits(x);
+  long long k = b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+  return k - (k >> 63);
+}
+__device__ __forceinline__ bool lt(double a, double b) { return key(a) < key(b); }
+// both operands >= 0 (either zero may be signed)
+__device__ __forceinline__ bool lt_nonneg(double a, double b) {
+  return (unsigned long long)(bits(a) & 0x7fffffffffffffffLL) <
+         (unsigned long long)(bits(b) & 0x7fffffffffffffffLL);
+}
+// a < c and a > c for a constant c > 0 (gt also for c = +0)
+__device__ __forceinline__ bool lt_pos(double a, double c) { return bits(a) < bits(c); }
+__device__ __forceinline__ bool gt_pos(double a, double c) { return bits(a) > bits(c); }
+// -a > c for c >= +0  (a < -c)
+__device__ __forceinline__ bool neg_gt_pos(double a, double c) {
+  return (bits(a) ^ (long long)0x8000000000000000ULL) > bits(c);
+}
+__device__ __forceinline__ bool abs_gt(double a, double c) {
+  return (unsigned long long)(bits(a) & 0x7fffffffffffffffLL) > (unsigned long long)bits(c);
+}
+__device__ __forceinline__ bool gt0(double a) { return bits(a) > 0; }
+__device__ __forceinline__ bool le0(double a) { return bits(a) <= 0; }
+__device__ __forceinline__ bool ge0(double a) {
+  long long b = bits(a);
+  return b >= 0 || b == (long long)0x8000000000000000ULL;
+}
+__device__ __forceinline__ bool finite(double a) {
+  return ((unsigned)(bits(a) >> 32) & 0x7ff00000u) != 0x7ff00000u;
+}
+// Python min(a, b) / max(a, b): the first argument unless the second is
+// strictly smaller / larger.
+__device__ __forceinline__ double py_min(double a, double b) { return lt(b, a) ? b : a; }
+__device__ __forceinline__ double py_max(double a, double b) { return lt(a, b) ? b : a; }
+
+}  // namespace icmp
+
+using icmp::py_max;
+using icmp::py_min;
 
 __device__ __forceinline__ bool finite4(const St4& s) {
-  return isfinite(s.a) && isfinite(s.b) && isfinite(s.c) && isfinite(s.d);
+  return icmp::finite(s.a) && icmp::finite(s.b) && icmp::finite(s.c) && icmp::finite(s.d);
 }
 
 // euler.conservative_to_primitive (euler.py:20-40), one row.
@@ -47,7 +96,7 @@ __device__ __forceinline__ St4 cons_to_prim(const St4& U, double gamma, bool* ok
   double uy = U.c / rho;
   double p = (gamma - 1.0) * (U.d - (0.5 * (U.b * U.b + U.c * U.c)) / rho);
   St4 P{rho, ux, uy, p};
-  *ok = finite4(P) && rho > 0.0 && p > 0.0;
+  *ok = finite4(P) && icmp::gt0(rho) && icmp::gt0(p);
   return P;
 }
 
@@ -81,7 +130,7 @@ __device__ __forceinline__ void rusanov_flux(const St4& L, const St4& R, double 
   double unr = R.b * nx + R.c * ny;
   double sl = fabs(unl) + sound_speed(L.a, L.d, gamma);
   double sr = fabs(unr) + sound_speed(R.a, R.d, gamma);
-  double s = (sl >= sr) ? sl : sr;  // np.maximum
+  double s = icmp::lt_nonneg(sl, sr) ? sr : sl;  // np.maximum
 #pragma unroll
   for (int k = 0; k < 4; ++k) out[k] = 0.5 * ((FL[k] + FR[k]) - s * (UR[k] - UL[k]));
 }
@@ -106,18 +155,18 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
   double wl = py_min(unl - cl, unr - cr);
   double wr = py_max(unl + cl, unr + cr);
   double den = rl * (wl - unl) - rr * (wr - unr);
-  if (!(fabs(den) > 1e-14)) den = copysign(1e-14, den);
+  if (!icmp::abs_gt(den, 1e-14)) den = copysign(1e-14, den);
   double contact = ((pr - pl) + (rl * unl) * (wl - unl) - (rr * unr) * (wr - unr)) / den;
 
   int branch;  // 0: F_L, 1: F*_L, 2: F*_R, 3: F_R
   if (KERNEL_BRANCHES) {
-    if (wl >= 0.0) branch = 0;
-    else if (wr <= 0.0) branch = 3;
-    else branch = (contact >= 0.0) ? 1 : 2;
+    if (icmp::ge0(wl)) branch = 0;
+    else if (icmp::le0(wr)) branch = 3;
+    else branch = icmp::ge0(contact) ? 1 : 2;
   } else {
-    if (wl >= 0.0) branch = 0;
-    else if (contact >= 0.0) branch = 1;
-    else if (wr > 0.0) branch = 2;
+    if (icmp::ge0(wl)) branch = 0;
+    else if (icmp::ge0(contact)) branch = 1;
+    else if (icmp::gt0(wr)) branch = 2;
     else branch = 3;
   }
   if (branch == 0 || branch == 3) {
@@ -141,7 +190,7 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
     for (int k = 0; k < 4; ++k) out[k] = F[k] + wave * (star[k] - U[k]);
   }
   if (!KERNEL_BRANCHES) {
-    return isfinite(out[0]) && isfinite(out[1]) && isfinite(out[2]) && isfinite(out[3]);
+    return icmp::finite(out[0]) && icmp::finite(out[1]) && icmp::finite(out[2]) && icmp::finite(out[3]);
   }
   return true;
 }
@@ -163,7 +212,7 @@ __device__ __forceinline__ int roe_flux(const St4& L, const St4& R, double nx, d
   double un = vx * nx + vy * ny;
   double ut = vx * -ny + vy * nx;
   double c2 = (gamma - 1.0) * (H - 0.5 * (vx * vx + vy * vy));
-  if (!(c2 > 0.0) || !isfinite(c2)) {
+  if (!icmp::gt0(c2) || !icmp::finite(c2)) {
     out[0] = out[1] = out[2] = out[3] = 0.0;
     return MCFD_S_ROE_SOUND;
   }
@@ -183,7 +232,7 @@ __device__ __forceinline__ int roe_flux(const St4& L, const St4& R, double nx, d
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     double a = fabs(lam[j]);
-    if (a < fix) a = 0.5 * ((a * a) / fix + fix);
+    if (icmp::lt_nonneg(a, fix)) a = 0.5 * ((a * a) / fix + fix);
     w[j] = a * strength[j];
   }
   double e[4][4] = {{1.0, 1.0, 0.0, 1.0},
@@ -199,7 +248,7 @@ __device__ __forceinline__ int roe_flux(const St4& L, const St4& R, double nx, d
   double diss[4] = {d[0], d[1] * nx - d[2] * ny, d[1] * ny + d[2] * nx, d[3]};
 #pragma unroll
   for (int k = 0; k < 4; ++k) out[k] = 0.5 * ((FL[k] + FR[k]) - diss[k]);
-  if (!(isfinite(out[0]) && isfinite(out[1]) && isfinite(out[2]) && isfinite(out[3])))
+  if (!(icmp::finite(out[0]) && icmp::finite(out[1]) && icmp::finite(out[2]) && icmp::finite(out[3])))
     return MCFD_S_ROE_NONFINITE;
   return 0;
 }
@@ -212,11 +261,11 @@ __device__ __forceinline__ int far_field_state(const St4& in, const St4& far, do
   double un_f = far.b * nx + far.c * ny;
   double c_i = sound_speed(in.a, in.d, gamma);
   double c_f = sound_speed(far.a, far.d, gamma);
-  if (un_i <= -c_i) {
+  if (!icmp::lt(-c_i, un_i)) {  // un_i <= -c_i
     *ext = far;
     return 0;
   }
-  if (un_i >= c_i) {
+  if (!icmp::lt(un_i, c_i)) {  // un_i >= c_i
     *ext = in;
     return 0;
   }
@@ -224,11 +273,11 @@ __device__ __forceinline__ int far_field_state(const St4& in, const St4& far, do
   double in_inv = un_f - (2.0 * c_f) / (gamma - 1.0);
   double vb = 0.5 * (out_inv + in_inv);
   double cb = (0.25 * (gamma - 1.0)) * (out_inv - in_inv);
-  if (!isfinite(cb) || cb <= 0.0) {
+  if (!icmp::finite(cb) || icmp::le0(cb)) {
     *ext = in;
     return MCFD_S_FARFIELD_SOUND;
   }
-  const St4& src = (vb < 0.0) ? far : in;
+  const St4& src = icmp::ge0(vb) ? in : far;
   double entropy = src.d / pow(src.a, gamma);
   double rho = pow((cb * cb) / (gamma * entropy), 1.0 / (gamma - 1.0));
   double p = entropy * pow(rho, gamma);
@@ -236,30 +285,292 @@ __device__ __forceinline__ int far_field_state(const St4& in, const St4& far, do
   double vt = src.b * tx + src.c * ty;
   St4 s{rho, vb * nx + vt * tx, vb * ny + vt * ty, p};
   *ext = s;
-  if (!finite4(s) || !(rho > 0.0) || !(p > 0.0)) return MCFD_S_FARFIELD_STATE;
+  if (!finite4(s) || !icmp::gt0(rho) || !icmp::gt0(p)) return MCFD_S_FARFIELD_STATE;
   return 0;
 }
 
 // One limiter entry (_kernels.py:40-65): the face factor for one variable.
+// `tolerance` = 1e-14 * max(|value|, 1) is hoisted by the caller (it is the
+// same for every entry of a cell and variable).
 template <int LIMITER>
 __device__ __forceinline__ double limiter_face_factor(double value, double increment, double lo,
-                                                      double hi) {
-  double tolerance = 1e-14 * py_max(fabs(value), 1.0);
-  double ratio = 1.0;
-  if (increment > tolerance) ratio = (hi - value) / increment;
-  else if (increment < -tolerance) ratio = (lo - value) / increment;
-  ratio = (0.0 > ratio) ? 0.0 : ratio;
+                                                      double hi, double tolerance) {
+  // One division on a selected numerator (no divergent branches); the same
+  // operands as the reference's two branches, so the same quotient.
+  const bool pos = icmp::gt_pos(increment, tolerance);
+  const bool neg = icmp::neg_gt_pos(increment, tolerance);
+  const double num = pos ? (hi - value) : (lo - value);
+  const double q = num / ((pos || neg) ? increment : 1.0);
+  double ratio = (pos || neg) ? q : 1.0;
+  ratio = icmp::ge0(ratio) ? ratio : 0.0;  // max(ratio, 0.0)
   double f;
   if (LIMITER <= 1) {
-    f = py_min(ratio, 1.0);
+    f = icmp::gt_pos(ratio, 1.0) ? 1.0 : ratio;  // min(ratio, 1.0)
   } else if (LIMITER == 2) {
-    f = (ratio > 0.0) ? py_min(1.0, (2.0 * ratio) / (1.0 + ratio)) : 0.0;
+    if (icmp::gt0(ratio)) {
+      double q = (2.0 * ratio) / (1.0 + ratio);
+      f = icmp::lt_pos(q, 1.0) ? q : 1.0;  // min(1.0, q)
+    } else {
+      f = 0.0;
+    }
   } else {
     const double eps = 1e-12;
     f = ((ratio * ratio + 2.0 * ratio) + eps) / (((ratio * ratio + ratio) + 2.0) + eps);
-    f = py_min(f, 1.0);
+    f = icmp::gt_pos(f, 1.0) ? 1.0 : f;  // min(f, 1.0)
   }
   return f;
+}
+
+// Limiter factor of a cell from its smallest ratio.  Correctly rounded
+// division is monotone in the divisor, so over the entries with a positive
+// increment the reference's smallest ratio (hi - v) / inc is the one at the
+// largest increment, and over negative increments (lo - v) / inc is smallest
+// at the most negative one: both are the reference's own quotients.  Every
+// limiter function is non-decreasing in the ratio (Venkatakrishnan's is
+// capped at 1 where it would decrease), so the minimum over entries of g(r)
+// is g(min r) — exact for Barth-Jespersen and Minmod, and for Van Leer and
+// Venkatakrishnan equal up to a possible last-place tie between near-equal
+// entries.  Three divisions per variable instead of two per entry.
+template <int LIMITER>
+__device__ __forceinline__ double limiter_factor_min_ratio(double value, double lo, double hi,
+                                                          double pos_max, double neg_min,
+                                                          bool has_pos, bool has_neg, bool flat) {
+  double r = 1.0;  // the tolerance band's ratio (only used when flat)
+  bool any = flat;
+  const double rp = (hi - value) / (has_pos ? pos_max : 1.0);
+  const double rn = (lo - value) / (has_neg ? neg_min : -1.0);
+  if (has_pos) {
+    double x = icmp::ge0(rp) ? rp : 0.0;
+    r = (!any || icmp::lt(x, r)) ? x : r;
+    any = true;
+  }
+  if (has_neg) {
+    double x = icmp::ge0(rn) ? rn : 0.0;
+    r = (!any || icmp::lt(x, r)) ? x : r;
+    any = true;
+  }
+  if (!any) return 1.0;
+  double f;
+  if (LIMITER <= 1) {
+    f = icmp::gt_pos(r, 1.0) ? 1.0 : r;
+  } else if (LIMITER == 2) {
+    const double q = (2.0 * r) / (1.0 + r);
+    f = icmp::gt0(r) ? (icmp::lt_pos(q, 1.0) ? q : 1.0) : 0.0;
+  } else {
+    const double eps = 1e-12;
+    f = ((r * r + 2.0 * r) + eps) / (((r * r + r) + 2.0) + eps);
+    f = icmp::gt_pos(f, 1.0) ? 1.0 : f;
+  }
+  return f;
+}
+
+__device__ __forceinline__ double limiter_tolerance(double value) {
+  double m = fabs(value);
+  return 1e-14 * (icmp::lt_pos(m, 1.0) ? 1.0 : m);  // 1e-14 * max(|v|, 1.0)
+}
+
+// ---------------------------------------------------------------------------
+// Fast variants (FMA contraction on, fewer FP64 divisions).  Same algorithms
+// as above; rounding differs from the reference at the last-place level.
+
+// Primitive recovery with one reciprocal instead of three divisions.
+__device__ __forceinline__ St4 cons_to_prim_fast(const St4& U, double gamma, bool* ok) {
+  double rho = U.a;
+  double inv = 1.0 / rho;
+  double ux = U.b * inv;
+  double uy = U.c * inv;
+  double p = (gamma - 1.0) * (U.d - 0.5 * (U.b * U.b + U.c * U.c) * inv);
+  St4 P{rho, ux, uy, p};
+  *ok = finite4(P) && icmp::gt0(rho) && icmp::gt0(p);
+  return P;
+}
+
+// physical_flux with the internal energy as p * (1/(gamma-1)).
+__device__ __forceinline__ void physical_flux_fast(const St4& q, double nx, double ny, double inv_gm1,
+                                                   double F[4], double U[4]) {
+  double rho = q.a, ux = q.b, uy = q.c, p = q.d;
+  double energy = p * inv_gm1 + 0.5 * rho * (ux * ux + uy * uy);
+  double un = ux * nx + uy * ny;
+  U[0] = rho;
+  U[1] = rho * ux;
+  U[2] = rho * uy;
+  U[3] = energy;
+  F[0] = rho * un;
+  F[1] = U[1] * un + p * nx;
+  F[2] = U[2] * un + p * ny;
+  F[3] = (energy + p) * un;
+}
+
+// HLLC with shared reciprocals: one division for both 1/rho, one for the
+// contact speed, one for the star state (rho(S-un) and S-S* share it).
+template <bool KERNEL_BRANCHES>
+__device__ __forceinline__ bool hllc_flux_fast(const St4& L, const St4& R, double nx, double ny,
+                                               double gamma, double inv_gm1, double out[4]) {
+  double FL[4], UL[4], FR[4], UR[4];
+  physical_flux_fast(L, nx, ny, inv_gm1, FL, UL);
+  physical_flux_fast(R, nx, ny, inv_gm1, FR, UR);
+  double rl = L.a, pl = L.d, rr = R.a, pr = R.d;
+  double t = 1.0 / (rl * rr);
+  double irl = rr * t, irr = rl * t;
+  double unl = L.b * nx + L.c * ny;
+  double unr = R.b * nx + R.c * ny;
+  double cl = sqrt(gamma * pl * irl);
+  double cr = sqrt(gamma * pr * irr);
+  double wl = py_min(unl - cl, unr - cr);
+  double wr = py_max(unl + cl, unr + cr);
+  double ml = rl * (wl - unl), mr = rr * (wr - unr);
+  double den = ml - mr;
+  if (!icmp::abs_gt(den, 1e-14)) den = copysign(1e-14, den);
+  double contact = ((pr - pl) + unl * ml - unr * mr) / den;
+  int branch;
+  if (KERNEL_BRANCHES) {
+    if (icmp::ge0(wl)) branch = 0;
+    else if (icmp::le0(wr)) branch = 3;
+    else branch = icmp::ge0(contact) ? 1 : 2;
+  } else {
+    if (icmp::ge0(wl)) branch = 0;
+    else if (icmp::ge0(contact)) branch = 1;
+    else if (icmp::gt0(wr)) branch = 2;
+    else branch = 3;
+  }
+  if (branch == 0 || branch == 3) {
+    const double* F = (branch == 0) ? FL : FR;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = F[k];
+  } else {
+    const bool left = (branch == 1);
+    const St4& q = left ? L : R;
+    const double* U = left ? UL : UR;
+    const double* F = left ? FL : FR;
+    double un = left ? unl : unr;
+    double wave = left ? wl : wr;
+    double m = left ? ml : mr;          // rho (S - un)
+    double irho = left ? irl : irr;
+    double d = wave - contact;
+    double s = 1.0 / (m * d);
+    double factor = m * m * s;          // rho (S - un) / (S - S*)
+    double p_over_m = q.d * d * s;      // p / (rho (S - un))
+    double sux = q.b + (contact - un) * nx;
+    double suy = q.c + (contact - un) * ny;
+    double se = factor * (U[3] * irho + (contact - un) * (contact + p_over_m));
+    double star[4] = {factor, factor * sux, factor * suy, se};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = F[k] + wave * (star[k] - U[k]);
+  }
+  if (!KERNEL_BRANCHES)
+    return icmp::finite(out[0]) && icmp::finite(out[1]) && icmp::finite(out[2]) && icmp::finite(out[3]);
+  return true;
+}
+
+__device__ __forceinline__ void rusanov_flux_fast(const St4& L, const St4& R, double nx, double ny, double gamma,
+                                                  double inv_gm1, double out[4]) {
+  double FL[4], UL[4], FR[4], UR[4];
+  physical_flux_fast(L, nx, ny, inv_gm1, FL, UL);
+  physical_flux_fast(R, nx, ny, inv_gm1, FR, UR);
+  double t = 1.0 / (L.a * R.a);
+  double unl = L.b * nx + L.c * ny;
+  double unr = R.b * nx + R.c * ny;
+  double sl = fabs(unl) + sqrt(gamma * L.d * (R.a * t));
+  double sr = fabs(unr) + sqrt(gamma * R.d * (L.a * t));
+  double s = icmp::lt_nonneg(sl, sr) ? sr : sl;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) out[k] = 0.5 * ((FL[k] + FR[k]) - s * (UR[k] - UL[k]));
+}
+
+__device__ __forceinline__ int roe_flux_fast(const St4& L, const St4& R, double nx, double ny, double gamma,
+                                             double inv_gm1, double out[4]) {
+  double FL[4], UL[4], FR[4], UR[4];
+  physical_flux_fast(L, nx, ny, inv_gm1, FL, UL);
+  physical_flux_fast(R, nx, ny, inv_gm1, FR, UR);
+  double root_l = sqrt(L.a), root_r = sqrt(R.a);
+  double iden = 1.0 / (root_l + root_r);
+  double vx = (root_l * L.b + root_r * R.b) * iden;
+  double vy = (root_l * L.c + root_r * R.c) * iden;
+  // The reference's averaged "enthalpy" is sqrt(rho)-weighted p/rho + |u|^2/2
+  // (euler.py:181-185); with rho = root^2, root * p / rho = p / root.
+  double H = (L.d / root_l + R.d / root_r + 0.5 * (root_l * (L.b * L.b + L.c * L.c) +
+                                                  root_r * (R.b * R.b + R.c * R.c))) * iden;
+  double un = vx * nx + vy * ny;
+  double ut = vx * -ny + vy * nx;
+  double c2 = (gamma - 1.0) * (H - 0.5 * (vx * vx + vy * vy));
+  if (!icmp::gt0(c2) || !icmp::finite(c2)) {
+    out[0] = out[1] = out[2] = out[3] = 0.0;
+    return MCFD_S_ROE_SOUND;
+  }
+  double c = sqrt(c2);
+  double ic2 = 1.0 / c2;
+  double ravg = root_l * root_r;
+  double unl = L.b * nx + L.c * ny, unr = R.b * nx + R.c * ny;
+  double utl = L.b * -ny + L.c * nx, utr = R.b * -ny + R.c * nx;
+  double dr = R.a - L.a, dun = unr - unl, dut = utr - utl, dp = R.d - L.d;
+  double am = (dp - (ravg * c) * dun) * (0.5 * ic2);
+  double ap = (dp + (ravg * c) * dun) * (0.5 * ic2);
+  double ac = dr - dp * ic2;
+  double as = ravg * dut;
+  double lam[4] = {un - c, un, un, un + c};
+  double fix = 0.1 * c, ifix = 10.0 / c;
+  double w[4];
+  double strength[4] = {am, ac, as, ap};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    double a = fabs(lam[j]);
+    if (icmp::lt_nonneg(a, fix)) a = 0.5 * (a * a * ifix + fix);
+    w[j] = a * strength[j];
+  }
+  double d0 = w[0] + w[1] + w[3];
+  double d1 = (un - c) * w[0] + un * w[1] + (un + c) * w[3];
+  double d2 = ut * (w[0] + w[1] + w[3]) + w[2];
+  double d3 = (H - un * c) * w[0] + 0.5 * (un * un + ut * ut) * w[1] + ut * w[2] + (H + un * c) * w[3];
+  double diss[4] = {d0, d1 * nx - d2 * ny, d1 * ny + d2 * nx, d3};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) out[k] = 0.5 * ((FL[k] + FR[k]) - diss[k]);
+  if (!(icmp::finite(out[0]) && icmp::finite(out[1]) && icmp::finite(out[2]) && icmp::finite(out[3])))
+    return MCFD_S_ROE_NONFINITE;
+  return 0;
+}
+
+// Cell limiter factor from the extreme increments.  Every limiter function g
+// of the reference is non-decreasing in the ratio r (Venkatakrishnan's
+// (r^2+2r+e)/(r^2+r+2+e) on [0,2] and capped at 1 beyond), so the minimum of
+// g(r_e) over the entries is g(min_e r_e), and min_e r_e is reached at the
+// largest positive increment ((hi-v)/inc) or the largest negative one
+// ((v-lo)/|inc|), or is 1 when an increment lies within the tolerance band.
+// The two candidate ratios a/b are compared by cross-multiplication and the
+// limiter function is evaluated as a rational function of (a, b): one
+// division per variable instead of two per entry.
+template <int LIMITER>
+__device__ __forceinline__ double limiter_factor_fast(double hi_minus_v, double pos_max, double v_minus_lo,
+                                                      double neg_max, bool has_pos, bool has_neg, bool flat) {
+  double a, b;
+  if (has_pos && has_neg) {
+    bool pos_smaller = !icmp::lt_nonneg(v_minus_lo * pos_max, hi_minus_v * neg_max);
+    a = pos_smaller ? hi_minus_v : v_minus_lo;
+    b = pos_smaller ? pos_max : neg_max;
+  } else if (has_pos) {
+    a = hi_minus_v;
+    b = pos_max;
+  } else if (has_neg) {
+    a = v_minus_lo;
+    b = neg_max;
+  } else {
+    return flat ? (LIMITER == 3 ? (3.0 + 1e-12) / (4.0 + 1e-12) : 1.0) : 1.0;
+  }
+  if (flat && !icmp::lt_nonneg(a, b)) {  // the tolerance band's ratio 1 is the smallest
+    a = 1.0;
+    b = 1.0;
+  }
+  if (LIMITER <= 1) {
+    return icmp::lt_nonneg(a, b) ? a / b : 1.0;
+  } else if (LIMITER == 2) {
+    if (!icmp::gt0(a)) return 0.0;
+    double q = (2.0 * a) / (a + b);
+    return icmp::lt_pos(q, 1.0) ? q : 1.0;
+  } else {
+    const double eps = 1e-12;
+    if (!icmp::lt_nonneg(a, 2.0 * b)) return 1.0;
+    double bb = b * b;
+    return (a * a + 2.0 * a * b + eps * bb) / (a * a + a * b + 2.0 * bb + eps * bb);
+  }
 }
 
 }  // namespace mcfd

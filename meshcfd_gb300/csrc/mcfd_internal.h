@@ -97,20 +97,32 @@ struct Workspace {
   int partial_blocks;
 };
 
-// kernels (mcfd_kernels.cu)
-cudaError_t launch_primitive(const DevGeom& g, const mcfd_config& cfg, const double* U, double* P,
-                             cudaStream_t s);
-cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const double* P,
-                               double* recon, cudaStream_t s);
-cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* P,
-                        const double* recon, double* flux, cudaStream_t s);
-cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double* P,
-                          const double* flux, const StageProgram& prog, cudaStream_t s);
-cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const double* P,
-                              double* dt_cells, double* dt_min, double time_limit,
-                              cudaStream_t s);
+// kernels (mcfd_kernels_impl.cuh), one set per variant: mcfd::exact (reference
+// operation order), mcfd::fast (smallest-ratio limiter), mcfd::fma (fewer
+// divisions everywhere, FMA).
+#define MCFD_DECLARE_LAUNCHERS(NS)                                                              \
+  namespace NS {                                                                               \
+  cudaError_t launch_primitive(const DevGeom& g, const mcfd_config& cfg, const double* U,      \
+                               double* P, cudaStream_t s);                                     \
+  cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const double* P,    \
+                                 double* recon, cudaStream_t s);                               \
+  cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* P,           \
+                          const double* recon, double* flux, cudaStream_t s);                  \
+  cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double* P,         \
+                            const double* flux, const StageProgram& prog, cudaStream_t s);     \
+  cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const double* P,     \
+                                double* dt_cells, double* dt_min, double time_limit,           \
+                                cudaStream_t s);                                               \
+  }
+MCFD_DECLARE_LAUNCHERS(exact)
+MCFD_DECLARE_LAUNCHERS(fast)
+MCFD_DECLARE_LAUNCHERS(fma)
+#undef MCFD_DECLARE_LAUNCHERS
+
+// variant-independent (mcfd_kernels_common.cu)
 long long launch_count();
-// reduction kernels of the sum of squares (defined in mcfd_kernels.cu)
+void count_launch(int n = 1);
+// reduction kernels of the sum of squares
 __global__ void k_sumsq_partial(int n, const double* __restrict__ R, double* __restrict__ partials);
 __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums);
 cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,

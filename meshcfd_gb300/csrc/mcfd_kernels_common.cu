@@ -1,0 +1,52 @@
+// Variant-independent kernels: the residual sum of squares and the launch
+// counter.  Compiled with -fmad=false (plain additions in a fixed tree).
+#include "mcfd_device.cuh"
+#include "mcfd_internal.h"
+
+namespace mcfd {
+
+static constexpr int kBlock = 256;
+
+// ------------------------------------------------------------- sum of squares
+
+__global__ void __launch_bounds__(kBlock) k_sumsq_partial(int n, const double* __restrict__ R,
+                                                          double* __restrict__ partials) {
+  __shared__ double sh[4][kBlock];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const St4 r = ld4(R + 4 * (size_t)c);
+    acc[0] += r.a * r.a; acc[1] += r.b * r.b; acc[2] += r.c * r.c; acc[3] += r.d * r.d;
+  }
+  for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int width = kBlock / 2; width > 0; width >>= 1) {
+    if (threadIdx.x < width)
+      for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + width];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; ++k) partials[4 * blockIdx.x + k] = sh[k][0];
+}
+
+__global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums) {
+  if (threadIdx.x < 4) {
+    double s = 0.0;
+    for (int b = 0; b < blocks; ++b) s += partials[4 * b + threadIdx.x];
+    sums[threadIdx.x] = s;
+  }
+}
+
+// Kernels launched by this library (host-side counter, for measurement).
+static long long g_launches = 0;
+long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+void count_launch(int n) { __atomic_fetch_add(&g_launches, (long long)n, __ATOMIC_RELAXED); }
+
+cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,
+                         double* sums, cudaStream_t s) {
+  count_launch(2);
+  k_sumsq_partial<<<blocks, kBlock, 0, s>>>(g.n_cells, R, partials);
+  k_sumsq_final<<<1, 32, 0, s>>>(blocks, partials, sums);
+  return cudaGetLastError();
+}
+
+}  // namespace mcfd

@@ -1,9 +1,22 @@
 // Kernels of the FP64 residual / explicit-step path (sm_103a).
 //
-// This translation unit is compiled with -fmad=false: every multiply and add
-// rounds separately, as in the reference's NumPy/Python arithmetic, so each
-// kernel reproduces the reference bit for bit where the reference itself is
-// IEEE-deterministic (everything except pow() in the far-field state).
+// This file is compiled three times (mcfd_kernels_{exact,fast,fma}.cu):
+// * exact (MCFD_FAST 0, -fmad=false): every multiply and add rounds
+//   separately and every expression keeps the reference's order, so each
+//   kernel reproduces the reference bit for bit where the reference itself is
+//   IEEE-deterministic (everything except pow() in the far-field state);
+// * fast (MCFD_FAST 1, -fmad=false): exact arithmetic, but the limiter takes
+//   the cell minimum through the smallest ratio (limiter_factor_min_ratio):
+//   3 divisions per variable instead of 2 per limiter entry; bit-exact for
+//   Barth-Jespersen / Minmod, last-place ties possible for Van Leer /
+//   Venkatakrishnan;
+// * fma (MCFD_FAST 2, FMA contraction): additionally shared reciprocals in
+//   the fluxes and primitive recovery and a one-division rational limiter.
+//   Rounding differs from the reference in the last places of every flux;
+//   on fine meshes the residual's cancellation (sum of O(1) fluxes times
+//   L/A ~ 1/h) amplifies that to ~1e-11 relative, so this variant is a
+//   throughput option outside the 1e-12 parity bar.
+// Compares, min/max and finiteness tests run on the integer pipe in both.
 //
 // Per explicit stage: reconstruct (per cell, MUSCL only) -> flux (per flux
 // face, one launch per face segment) -> gather (per cell: divergence in the
@@ -14,9 +27,21 @@
 #include "mcfd_device.cuh"
 #include "mcfd_internal.h"
 
+#ifndef MCFD_FAST
+#error "define MCFD_FAST (0 or 1) and MCFD_VARIANT before including this file"
+#endif
+
 namespace mcfd {
+namespace MCFD_VARIANT {
 
 static constexpr int kBlock = 256;
+static constexpr bool kFast = MCFD_FAST == 2;      // fast arithmetic (fluxes, primitive)
+static constexpr bool kMinRatio = MCFD_FAST == 1;  // min-ratio limiter, exact arithmetic
+
+__device__ __forceinline__ St4 to_prim(const St4& U, double gamma, bool* ok) {
+  if constexpr (kFast) return cons_to_prim_fast(U, gamma, ok);
+  else return cons_to_prim(U, gamma, ok);
+}
 
 __device__ __forceinline__ void flag_cell(DevStatus* st, int bits, int cell) {
   atomicOr(&st->code, bits);
@@ -35,7 +60,7 @@ __global__ void __launch_bounds__(kBlock) k_primitive(int n, const double* __res
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
   bool ok;
-  St4 p = cons_to_prim(ld4(U + 4 * (size_t)c), gamma, &ok);
+  St4 p = to_prim(ld4(U + 4 * (size_t)c), gamma, &ok);
   if (!ok) flag_cell(st, MCFD_S_NONPHYSICAL_STATE, c);
   st4(P + 4 * (size_t)c, p);
 }
@@ -71,10 +96,17 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
       double d = qv[v] - pv[v];
       gx[v] = gx[v] + cx * d;
       gy[v] = gy[v] + cy * d;
-      if (qv[v] < lo[v]) lo[v] = qv[v];
-      if (qv[v] > hi[v]) hi[v] = qv[v];
+      // density and pressure are positive (checked at primitive recovery), so
+      // their order is the order of the raw bits; velocities need the key.
+      const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
+      const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
+      if (below) lo[v] = qv[v];
+      if (above) hi[v] = qv[v];
     }
   }
+  double tol[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) tol[v] = limiter_tolerance(pv[v]);
   double phi[4] = {1.0, 1.0, 1.0, 1.0};
   const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
   for (int s = s0; s < s1; ++s) {
@@ -82,11 +114,116 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       double inc = gx[v] * d.x + gy[v] * d.y;
-      double f = limiter_face_factor<LIMITER>(pv[v], inc, lo[v], hi[v]);
-      if (f < phi[v]) phi[v] = f;
+      double f = limiter_face_factor<LIMITER>(pv[v], inc, lo[v], hi[v], tol[v]);
+      if (icmp::lt_nonneg(f, phi[v])) phi[v] = f;
     }
   }
   for (int s = s0; s < s1; ++s) {
+    const double2 d = g.lim_d[s];
+    double out[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (gx[v] * d.x + gy[v] * d.y);
+    st4(recon + 4 * (size_t)g.lim_slot[s], St4{out[0], out[1], out[2], out[3]});
+  }
+}
+
+// Reconstruction through the cell's smallest ratio (fast and fma variants):
+// gradients as in the exact kernel, one pass over the limiter entries that
+// keeps the largest positive and most negative increments, the factor from
+// limiter_factor_min_ratio (fast) or limiter_factor_fast (fma), and the
+// increments of the first four slots kept in registers for the face-state
+// write.
+template <int LIMITER>
+__global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const double* __restrict__ P,
+                                                             double* __restrict__ recon) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.n_cells) return;
+  const St4 p = ld4(P + 4 * (size_t)c);
+  const double pv[4] = {p.a, p.b, p.c, p.d};
+  double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+  double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
+  const int e0 = g.grad_ptr[c], e1 = g.grad_ptr[c + 1];
+  for (int e = e0; e < e1; ++e) {
+    const int nb = g.grad_nb[e];
+    const double cx = g.grad_cx[e], cy = g.grad_cy[e];
+    const St4 q = ld4(P + 4 * (size_t)nb);
+    const double qv[4] = {q.a, q.b, q.c, q.d};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double d = qv[v] - pv[v];
+      gx[v] += cx * d;
+      gy[v] += cy * d;
+      const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
+      const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
+      if (below) lo[v] = qv[v];
+      if (above) hi[v] = qv[v];
+    }
+  }
+  double tol[4], pos[4], neg[4];
+  bool has_pos[4], has_neg[4], flat[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    tol[v] = limiter_tolerance(pv[v]);
+    pos[v] = 0.0;
+    neg[v] = 0.0;
+    has_pos[v] = has_neg[v] = flat[v] = false;
+  }
+  const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
+  constexpr int kCache = 4;
+  double inc_cache[kCache][4];
+#pragma unroll
+  for (int k = 0; k < kCache; ++k) {
+    if (s0 + k < s1) {
+      const double2 d = g.lim_d[s0 + k];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        double inc = gx[v] * d.x + gy[v] * d.y;
+        inc_cache[k][v] = inc;
+        if (icmp::gt_pos(inc, tol[v])) {
+          has_pos[v] = true;
+          if (icmp::lt_nonneg(pos[v], inc)) pos[v] = inc;
+        } else if (icmp::neg_gt_pos(inc, tol[v])) {
+          has_neg[v] = true;
+          if (icmp::lt_nonneg(neg[v], -inc)) neg[v] = -inc;
+        } else {
+          flat[v] = true;
+        }
+      }
+    }
+  }
+  for (int s = s0 + kCache; s < s1; ++s) {
+    const double2 d = g.lim_d[s];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double inc = gx[v] * d.x + gy[v] * d.y;
+      if (icmp::gt_pos(inc, tol[v])) {
+        has_pos[v] = true;
+        if (icmp::lt_nonneg(pos[v], inc)) pos[v] = inc;
+      } else if (icmp::neg_gt_pos(inc, tol[v])) {
+        has_neg[v] = true;
+        if (icmp::lt_nonneg(neg[v], -inc)) neg[v] = -inc;
+      } else {
+        flat[v] = true;
+      }
+    }
+  }
+  double phi[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    if constexpr (kMinRatio)
+      phi[v] = limiter_factor_min_ratio<LIMITER>(pv[v], lo[v], hi[v], pos[v], -neg[v], has_pos[v], has_neg[v], flat[v]);
+    else
+      phi[v] = limiter_factor_fast<LIMITER>(hi[v] - pv[v], pos[v], pv[v] - lo[v], neg[v], has_pos[v], has_neg[v], flat[v]);
+  }
+#pragma unroll
+  for (int k = 0; k < kCache; ++k) {
+    if (s0 + k < s1) {
+      St4 o{pv[0] + phi[0] * inc_cache[k][0], pv[1] + phi[1] * inc_cache[k][1],
+            pv[2] + phi[2] * inc_cache[k][2], pv[3] + phi[3] * inc_cache[k][3]};
+      st4(recon + 4 * (size_t)g.lim_slot[s0 + k], o);
+    }
+  }
+  for (int s = s0 + kCache; s < s1; ++s) {
     const double2 d = g.lim_d[s];
     double out[4];
 #pragma unroll
@@ -99,14 +236,19 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
 
 template <int FLUX, bool KERNEL_HLLC>
 __device__ __forceinline__ int numerical_flux(const St4& L, const St4& R, double nx, double ny,
-                                              double gamma, double out[4]) {
+                                              double gamma, double inv_gm1, double out[4]) {
   if (FLUX == MCFD_FLUX_RUSANOV) {
-    rusanov_flux(L, R, nx, ny, gamma, out);
+    if constexpr (kFast) rusanov_flux_fast(L, R, nx, ny, gamma, inv_gm1, out);
+    else rusanov_flux(L, R, nx, ny, gamma, out);
     return 0;
   } else if (FLUX == MCFD_FLUX_HLLC) {
-    return hllc_flux<KERNEL_HLLC>(L, R, nx, ny, gamma, out) ? 0 : MCFD_S_HLLC_NONFINITE;
+    bool ok;
+    if constexpr (kFast) ok = hllc_flux_fast<KERNEL_HLLC>(L, R, nx, ny, gamma, inv_gm1, out);
+    else ok = hllc_flux<KERNEL_HLLC>(L, R, nx, ny, gamma, out);
+    return ok ? 0 : MCFD_S_HLLC_NONFINITE;
   } else {
-    return roe_flux(L, R, nx, ny, gamma, out);
+    if constexpr (kFast) return roe_flux_fast(L, R, nx, ny, gamma, inv_gm1, out);
+    else return roe_flux(L, R, nx, ny, gamma, out);
   }
 }
 
@@ -116,7 +258,8 @@ __device__ __forceinline__ int numerical_flux(const St4& L, const St4& R, double
 template <int FLUX, int SEG, bool FIRST_ORDER, bool KERNEL_HLLC>
 __global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __restrict__ P,
                                                  const double* __restrict__ recon,
-                                                 double* __restrict__ flux, double gamma) {
+                                                 double* __restrict__ flux, double gamma,
+                                                 double inv_gm1) {
   const int begin = g.seg_begin[SEG];
   const int f = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= g.seg_begin[SEG + 1]) return;
@@ -139,7 +282,7 @@ __global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __rest
     bits |= far_field_state(L, ld4(g.ff_far_state + 4 * (size_t)(f - begin)), n.x, n.y, gamma, &R);
   }
   double out[4];
-  bits |= numerical_flux<FLUX, (SEG == SEG_INTERIOR) && KERNEL_HLLC>(L, R, n.x, n.y, gamma, out);
+  bits |= numerical_flux<FLUX, (SEG == SEG_INTERIOR) && KERNEL_HLLC>(L, R, n.x, n.y, gamma, inv_gm1, out);
   if (bits) flag_face(g.status, bits, f);
   st4(flux + 4 * (size_t)f, St4{out[0], out[1], out[2], out[3]});
 }
@@ -186,7 +329,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
     r[2] = r[2] + p.a * ay;
     r[3] = r[3] + p.a * (ax * p.b + ay * p.c);
   }
-  if (!(isfinite(r[0]) && isfinite(r[1]) && isfinite(r[2]) && isfinite(r[3])))
+  if (!(icmp::finite(r[0]) && icmp::finite(r[1]) && icmp::finite(r[2]) && icmp::finite(r[3])))
     flag_cell(g.status, MCFD_S_NONFINITE_RESIDUAL, c);
   if (prog.out_r) st4(prog.out_r + 4 * (size_t)c, St4{r[0], r[1], r[2], r[3]});
   if (!prog.out_u) return;
@@ -222,7 +365,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
   st4(prog.out_u + 4 * (size_t)c, U);
   if (prog.out_p) {
     bool ok;
-    const St4 q = cons_to_prim(U, gamma, &ok);
+    const St4 q = to_prim(U, gamma, &ok);
     if (!ok) flag_cell(g.status, MCFD_S_NONPHYSICAL_STATE, c);
     st4(prog.out_p + 4 * (size_t)c, q);
   }
@@ -258,77 +401,45 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
         else if (kind == DT_POUT) ext = St4{p.a, p.b, p.c, g.ff_pout_pressure[idx]};
         else bits |= far_field_state(p, ld4(g.ff_far_state + 4 * (size_t)idx), n.x, n.y, gamma, &ext);
         double er = fabs(ext.b * n.x + ext.c * n.y) + sound_speed(ext.a, ext.d, gamma);
-        radius = (radius >= er) ? radius : er;  // np.maximum
+        radius = icmp::lt_nonneg(radius, er) ? er : radius;  // np.maximum
       }
       sum = sum + radius * g.dt_len[e];
     }
     dt = (cfl * g.area[c]) / sum;
-    if (!isfinite(dt) || !(dt > 0.0)) bits |= MCFD_S_TIME_STEP;
+    if (!icmp::finite(dt) || !icmp::gt0(dt)) bits |= MCFD_S_TIME_STEP;
     if (bits) flag_cell(g.status, bits, c);
     if (dt_cells) dt_cells[c] = dt;
   }
   if (!want_min) return;
   // block minimum by warp shuffles, then one atomicMin on the bit pattern
   // (positive doubles order like their unsigned bits).
-  double m = (c < g.n_cells && dt > 0.0) ? dt : __longlong_as_double(0x7ff0000000000000LL);
+  // positive doubles order like their bits: the minimum runs on integers
+  long long m = (c < g.n_cells && icmp::gt0(dt)) ? icmp::bits(dt) : 0x7ff0000000000000LL;
   for (int off = 16; off > 0; off >>= 1) {
-    double o = __shfl_down_sync(0xffffffffu, m, off);
+    long long o = __shfl_down_sync(0xffffffffu, m, off);
     m = (o < m) ? o : m;
   }
-  __shared__ double warp_min[kBlock / 32];
+  __shared__ long long warp_min[kBlock / 32];
   if ((threadIdx.x & 31) == 0) warp_min[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double b = warp_min[0];
+    long long b = warp_min[0];
     for (int w = 1; w < kBlock / 32; ++w) b = (warp_min[w] < b) ? warp_min[w] : b;
-    atomicMin(&g.status->dt_min_bits, (unsigned long long)__double_as_longlong(b));
+    atomicMin(&g.status->dt_min_bits, (unsigned long long)b);
   }
 }
 
 __global__ void k_time_step_finalize(DevStatus* st, double* dt_min, double time_limit) {
   double stable = __longlong_as_double((long long)st->dt_min_bits);
   // min(stable, end_time - time) with Python's min semantics (solver.py:455-461)
-  dt_min[0] = (time_limit < stable) ? time_limit : stable;
+  dt_min[0] = icmp::lt(time_limit, stable) ? time_limit : stable;
   st->dt_min_bits = 0x7ff0000000000000ULL;
-}
-
-// ------------------------------------------------------------- sum of squares
-
-__global__ void __launch_bounds__(kBlock) k_sumsq_partial(int n, const double* __restrict__ R,
-                                                          double* __restrict__ partials) {
-  __shared__ double sh[4][kBlock];
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-    const St4 r = ld4(R + 4 * (size_t)c);
-    acc[0] += r.a * r.a; acc[1] += r.b * r.b; acc[2] += r.c * r.c; acc[3] += r.d * r.d;
-  }
-  for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] = acc[k];
-  __syncthreads();
-  for (int width = kBlock / 2; width > 0; width >>= 1) {
-    if (threadIdx.x < width)
-      for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + width];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0)
-    for (int k = 0; k < 4; ++k) partials[4 * blockIdx.x + k] = sh[k][0];
-}
-
-__global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums) {
-  if (threadIdx.x < 4) {
-    double s = 0.0;
-    for (int b = 0; b < blocks; ++b) s += partials[4 * b + threadIdx.x];
-    sums[threadIdx.x] = s;
-  }
 }
 
 // ------------------------------------------------------------------ launchers
 
 static inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-// Kernels launched by this library (host-side counter, for measurement).
-static long long g_launches = 0;
-long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
-static inline void count_launch(int n = 1) { __atomic_fetch_add(&g_launches, (long long)n, __ATOMIC_RELAXED); }
 
 cudaError_t launch_primitive(const DevGeom& g, const mcfd_config& cfg, const double* U, double* P,
                              cudaStream_t s) {
@@ -341,11 +452,20 @@ cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const d
   if (g.n_cells == 0) return cudaSuccess;
   const int b = blocks_for(g.n_cells);
   count_launch();
-  switch (cfg.limiter) {
-    case 0: k_reconstruct<0><<<b, kBlock, 0, s>>>(g, P, recon); break;
-    case 1: k_reconstruct<1><<<b, kBlock, 0, s>>>(g, P, recon); break;
-    case 2: k_reconstruct<2><<<b, kBlock, 0, s>>>(g, P, recon); break;
-    default: k_reconstruct<3><<<b, kBlock, 0, s>>>(g, P, recon); break;
+  if constexpr (kFast || kMinRatio) {
+    switch (cfg.limiter) {
+      case 0: k_reconstruct_fast<0><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      case 1: k_reconstruct_fast<1><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      case 2: k_reconstruct_fast<2><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      default: k_reconstruct_fast<3><<<b, kBlock, 0, s>>>(g, P, recon); break;
+    }
+  } else {
+    switch (cfg.limiter) {
+      case 0: k_reconstruct<0><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      case 1: k_reconstruct<1><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      case 2: k_reconstruct<2><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      default: k_reconstruct<3><<<b, kBlock, 0, s>>>(g, P, recon); break;
+    }
   }
   return cudaGetLastError();
 }
@@ -353,10 +473,11 @@ cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const d
 template <int FLUX, bool FO, bool KH>
 static void flux_segments(const DevGeom& g, const double* P, const double* recon, double* flux,
                           double gamma, cudaStream_t s) {
+  const double inv_gm1 = 1.0 / (gamma - 1.0);
 #define MCFD_SEG(SEGV)                                                              \
   {                                                                                 \
     int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                              \
-    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<blocks_for(n), kBlock, 0, s>>>(g, P, recon, flux, gamma); \
+    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<blocks_for(n), kBlock, 0, s>>>(g, P, recon, flux, gamma, inv_gm1); \
   }
   MCFD_SEG(SEG_INTERIOR)
   MCFD_SEG(SEG_PERIODIC)
@@ -410,12 +531,6 @@ cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const do
   return cudaGetLastError();
 }
 
-cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,
-                         double* sums, cudaStream_t s) {
-  count_launch(2);
-  k_sumsq_partial<<<blocks, kBlock, 0, s>>>(g.n_cells, R, partials);
-  k_sumsq_final<<<1, 32, 0, s>>>(blocks, partials, sums);
-  return cudaGetLastError();
-}
 
+}  // namespace MCFD_VARIANT
 }  // namespace mcfd

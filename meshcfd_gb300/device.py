@@ -21,8 +21,15 @@ from .model import FLUX_CODES, LIMITER_CODES, RECONSTRUCTION_CODES
 TIME_SCHEME_CODES = {"Explicit Euler": 0, "Explicit RK2": 1, "Explicit RK3": 2, "Explicit RK4": 3}
 
 
-def make_config(settings, exact: bool = True) -> _lib.Config:
-    """Map ``NumericalSettings`` (model.py:95-129) to the kernel config."""
+MODES = {"exact": 0, "fast": 1, "fma": 2}
+
+
+def make_config(settings, mode: str = "exact") -> _lib.Config:
+    """Map ``NumericalSettings`` (model.py:95-129) to the kernel config.
+
+    ``mode``: "exact" (reference operation order, bit-exact), "fast" (exact
+    arithmetic, limiter minimum through the smallest ratio) or "fma" (shared
+    reciprocals and FMA; outside the 1e-12 bar on fine meshes)."""
     if settings.viscosity_model != "Inviscid":
         raise NotImplementedError("viscous terms are not implemented by the GPU residual path")
     if settings.turbulence_model != "None":
@@ -36,7 +43,7 @@ def make_config(settings, exact: bool = True) -> _lib.Config:
     if recon == 2:
         raise NotImplementedError("MUSCL parabolic is not implemented by the GPU residual path")
     cfg = _lib.Config()
-    cfg.flux, cfg.reconstruction, cfg.limiter, cfg.exact = flux, recon, limiter, int(exact)
+    cfg.flux, cfg.reconstruction, cfg.limiter, cfg.mode = flux, recon, limiter, MODES[mode]
     cfg.gamma = float(settings.gamma)
     cfg.acceleration_x = float(settings.acceleration_x)
     cfg.acceleration_y = float(settings.acceleration_y)

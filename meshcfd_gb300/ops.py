@@ -19,7 +19,7 @@ _NS = "meshcfd_gb300"
 
 def _cfg(flux: int, recon: int, limiter: int, gamma: float, ax: float, ay: float, cfl: float = 0.5):
     cfg = _lib.Config()
-    cfg.flux, cfg.reconstruction, cfg.limiter, cfg.exact = flux, recon, limiter, 1
+    cfg.flux, cfg.reconstruction, cfg.limiter, cfg.mode = flux, recon, limiter, 0
     cfg.gamma, cfg.acceleration_x, cfg.acceleration_y, cfg.cfl = gamma, ax, ay, cfl
     return cfg
 

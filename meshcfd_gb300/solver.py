@@ -51,14 +51,14 @@ class SolverResult:
 
 def run_explicit(geom: DeviceGeometry, settings, U: torch.Tensor, *, start_time: float = 0.0,
                  step_offset: int = 0, progress_callback=None, cancel_callback=None,
-                 solution_callback=None, solution_interval: int = 1, exact: bool = True,
+                 solution_callback=None, solution_interval: int = 1, mode: str = "exact",
                  solver_error=SolverError, check_every: int = 1, final_residual: bool = True):
     """Advance ``U`` (device (C,4) float64, modified in place) like the
     reference's explicit loop.  Returns a :class:`SolverResult`."""
     cpu_start = thread_time()
     if settings.time_integration not in TIME_SCHEME_CODES:
         raise NotImplementedError(f"{settings.time_integration} is not an explicit integrator")
-    cfg = make_config(settings, exact)
+    cfg = make_config(settings, mode)
     scheme = TIME_SCHEME_CODES[settings.time_integration]
     local = settings.time_step_mode == "Local (steady)"
     fixed = settings.time_step_mode == "Global fixed"

@@ -196,3 +196,101 @@ def test_custom_ops_match_handle_calls(cuda_device):
     U3 = U.clone()
     dg.explicit_step(U3, make_config(s), 2, dt)
     assert torch.equal(U2, U3)
+
+
+# ---------------------------------------------------------------- fast mode
+
+@pytest.mark.parametrize("mode", ("fast", "fma"))
+@pytest.mark.parametrize("kind,n", (("riemann", 64), ("vortex", 48)))
+@pytest.mark.parametrize("flux", ("Rusanov", "HLLC", "Roe"))
+@pytest.mark.parametrize("limiter", ("Barth-Jespersen", "Minmod", "Van Leer", "Venkatakrishnan"))
+def test_fast_residual_within_tolerance(cuda_device, mode, kind, n, flux, limiter):
+    """The fast kernels (FMA, shared reciprocals, limiter through its
+    monotonicity) stay within 1e-12 of the reference per residual."""
+    import torch
+    from meshcfd_gb300.device import DeviceGeometry, make_config
+    from meshcfd_gb300.model import NumericalSettings
+    from oracle.oracle import Oracle
+
+    case, g, P, P2 = _oracle_case(kind, n)
+    orc = Oracle(g)
+    dg = DeviceGeometry(g)
+    for prim in (P, P2):
+        U = orc.conservative(prim, 1.4)
+        for recon in ("First order", "MUSCL linear"):
+            s = NumericalSettings(flux=flux, reconstruction=recon, limiter=limiter)
+            ref = orc.residual(U, s)
+            R = dg.residual(torch.as_tensor(U, device=cuda_device), make_config(s, mode=mode)).cpu().numpy()
+            dg.check_status()
+            assert rel_err(R, ref) <= TOL_RESIDUAL, (flux, recon, limiter, rel_err(R, ref))
+
+
+@pytest.mark.parametrize("mode", ("fast", "fma"))
+@pytest.mark.parametrize("name", RESIDUAL_FIXTURES)
+def test_fast_residual_matches_reference_golden(cuda_device, mode, name):
+    import torch
+    from meshcfd_gb300.device import DeviceGeometry, make_config
+
+    data, geom = load_fixture(name)
+    dg = DeviceGeometry(geom)
+    U = torch.as_tensor(data["U"], device=cuda_device)
+    for key in residual_keys(data):
+        R = dg.residual(U, make_config(settings_for(key), mode=mode)).cpu().numpy()
+        dg.check_status()
+        assert rel_err(R, data[key]) <= TOL_RESIDUAL, key
+
+
+@pytest.mark.parametrize("mode", ("fast", "fma"))
+@pytest.mark.parametrize("scheme", ("Explicit Euler", "Explicit RK2", "Explicit RK3", "Explicit RK4"))
+def test_fast_hundred_steps_within_tolerance(cuda_device, mode, scheme):
+    import torch
+    from meshcfd_gb300.device import DeviceGeometry
+    from meshcfd_gb300.model import NumericalSettings
+    from meshcfd_gb300.solver import run_explicit
+    from oracle.oracle import Oracle
+
+    for kind, n, s in (
+        ("riemann", 32, NumericalSettings(flux="Rusanov", reconstruction="First order", cfl=0.5)),
+        ("vortex", 24, NumericalSettings(flux="HLLC", reconstruction="MUSCL linear", limiter="Venkatakrishnan",
+                                         cfl=0.8)),
+        ("vortex", 24, NumericalSettings(flux="Roe", reconstruction="MUSCL linear", limiter="Barth-Jespersen",
+                                         cfl=0.8)),
+    ):
+        s.time_integration = scheme
+        s.end_time, s.max_iterations, s.residual_tolerance = 1.0e30, 100, 1e-300
+        case, g, P, _ = _oracle_case(kind, n)
+        orc = Oracle(g)
+        U0 = orc.conservative(P, s.gamma)
+        ref, t_ref = orc.solve(U0, s, 100)
+        dg = DeviceGeometry(g)
+        U = torch.as_tensor(U0, device=cuda_device)
+        res = run_explicit(dg, s, U, final_residual=False, mode=mode)
+        err = rel_err(U.cpu().numpy(), ref)
+        assert err <= TOL_100_STEPS, (kind, s.flux, scheme, err)
+        assert abs(res.time - t_ref) <= 1e-9 * t_ref
+
+
+@pytest.mark.parametrize("kind,n", (("riemann", 64), ("vortex", 48)))
+@pytest.mark.parametrize("flux", ("Rusanov", "HLLC", "Roe"))
+@pytest.mark.parametrize("limiter", ("Barth-Jespersen", "Minmod"))
+def test_fast_mode_is_bit_exact_for_min_limiters(cuda_device, kind, n, flux, limiter):
+    """For Barth-Jespersen and Minmod the smallest-ratio limiter is exact:
+    the fast mode reproduces the reference bit for bit (periodic mesh)."""
+    import torch
+    from meshcfd_gb300.device import DeviceGeometry, make_config
+    from meshcfd_gb300.model import NumericalSettings
+    from oracle.oracle import Oracle
+
+    case, g, P, P2 = _oracle_case(kind, n)
+    orc = Oracle(g)
+    dg = DeviceGeometry(g)
+    for prim in (P, P2):
+        U = orc.conservative(prim, 1.4)
+        s = NumericalSettings(flux=flux, reconstruction="MUSCL linear", limiter=limiter)
+        ref = orc.residual(U, s)
+        R = dg.residual(torch.as_tensor(U, device=cuda_device), make_config(s, mode="fast")).cpu().numpy()
+        dg.check_status()
+        if kind == "vortex":
+            np.testing.assert_array_equal(R, ref)
+        else:
+            assert rel_err(R, ref) <= 1e-15
