@@ -37,6 +37,8 @@ extern "C" {
 #define MCFD_E_UNSUPPORTED 3 /* option outside what the GPU path implements */
 #define MCFD_E_GEOMETRY 4    /* geometry description inconsistent */
 #define MCFD_E_TOO_LARGE 5   /* size beyond the fixed scratch of the allocation-free entry point */
+#define MCFD_E_NOT_CONVERGED 6 /* GMRES reached its iteration limit (solver.py:1526-1529) */
+#define MCFD_E_BREAKDOWN 7     /* GMRES broke down (solver.py:1522-1523) */
 
 /* ---- device status bits (numerical failures; reference messages) ---- */
 #define MCFD_S_NONPHYSICAL_STATE 0x01  /* euler.py:34-39 non-finite or non-positive rho/p */
@@ -212,6 +214,69 @@ int mcfd_residual_sumsq(mcfd_geom* geom, const double* R, double* sums, void* st
  */
 int mcfd_status_fetch(mcfd_geom* geom, void* stream, mcfd_status* out);
 
+/* ---- implicit Euler (solver.py:1185-1567) ---- */
+
+/*
+ * Prepare the linearised implicit operator at state U (device [n_cells][4]):
+ * the first-order scalar preconditioner (_implicit_preconditioner,
+ * solver.py:1185-1300, assembled from P(U) and the time step), the
+ * first-order residual R1(U) (jacobian_rate, solver.py:1445) with cfg's flux,
+ * and |U / scales| (solver.py:1543).  dt: device scalar or [n_cells]
+ * (dt_per_cell); it must stay valid while the operator is used.  scales:
+ * host [4], the per-variable scaling of the Newton iteration.
+ */
+int mcfd_implicit_prepare(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* dt,
+                          int32_t dt_per_cell, const double* scales, void* stream);
+/* out = v - dt [R1(U + eps s v) - R1(U)] / (eps s), eps = sqrt(eps_mach)
+ * max(1,|U/s|) / |v| (_matrix_free_implicit_operator, solver.py:1532-1567).
+ * v, out: device [4 n_cells]. */
+int mcfd_implicit_matvec(mcfd_geom* geom, const double* v, double* out, void* stream);
+/* Select the Jacobian of the GMRES operator: 0 = the reference's finite
+ * difference (default), 1 = the exact Jacobian (mcfd_jvp of R1). */
+int mcfd_implicit_set_jacobian(mcfd_geom* geom, int32_t exact);
+/* Exact Jacobian-vector product of the residual: dR = (dR/dU)(U) dU, for the
+ * same settings as mcfd_residual (forward mode; limiter and flux switches
+ * differentiated on the branch the state takes).  No counterpart in the
+ * reference, which only forms finite differences (solver.py:1532-1567).
+ * U, dU, dR: device [n_cells][4]. */
+int mcfd_jvp(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* dU, double* dR,
+             void* stream);
+/* Reverse-mode product of the residual: U_bar = (dR/dU)(U)^T lambda, the
+ * transpose of mcfd_jvp's Jacobian (same switches).  far_bar (device
+ * [n_far_field][4], may be NULL) receives lambda^T dR/d(far-field state) per
+ * far-field face.  No counterpart in the reference.  U, lambda, U_bar: device
+ * [n_cells][4]. */
+int mcfd_vjp(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* lambda, double* U_bar,
+             double* far_bar, void* stream);
+/* Pressure force on the wall faces along (dir_x, dir_y): J = sum over wall
+ * faces of p(owner) (n . dir) L, with n pointing out of the fluid cell; dJdU
+ * (device [n_cells][4], may be NULL) receives dJ/dU.  J: host scalar. */
+int mcfd_wall_force(mcfd_geom* geom, const mcfd_config* cfg, const double* U, double dir_x, double dir_y,
+                    double* J, double* dJdU, void* stream);
+/* x = (D+U)^-1 D (D+L)^-1 v with the prepared scalar matrix applied to each
+ * of the four variables (LU-SGS, solver.py:1302-1323); level-scheduled sweeps
+ * in natural cell order. */
+int mcfd_lusgs_apply(mcfd_geom* geom, const double* v, double* x, void* stream);
+/* Solve operator(x) = b with restarted GMRES(krylov_dim) preconditioned by
+ * LU-SGS, as _solve_gmres drives SciPy's gmres (solver.py:1489-1529; left
+ * preconditioning, modified Gram-Schmidt, Givens rotations).  b, x: device
+ * [4 n_cells].  Returns MCFD_OK, MCFD_E_NOT_CONVERGED or MCFD_E_BREAKDOWN. */
+int mcfd_gmres(mcfd_geom* geom, const double* b, double* x, double tol, int32_t max_iter,
+               int32_t krylov_dim, int32_t* iterations, void* stream);
+/* Newton equation e = U - U0 - dt R (solver.py:1415-1418): writes
+ * b = -(e / scales) when b is non-NULL and returns norms[0] = max|e / s|,
+ * norms[1] = max|(U - U0) / s| (host [2]). */
+int mcfd_implicit_equation(mcfd_geom* geom, const double* U, const double* U0, const double* R,
+                           const double* dt, int32_t dt_per_cell, const double* scales, double* b,
+                           double* norms, void* stream);
+/* Maxima for the variable scaling (solver.py:1393-1413), host [9]:
+ * max rho, max|u|, max|v|, max c, max p, max|U_0|, max|U_1|, max|U_2|, max|U_3|. */
+int mcfd_implicit_scale_maxima(mcfd_geom* geom, const mcfd_config* cfg, const double* U,
+                               double* maxima, void* stream);
+/* out = U + (damping * dx) * scales (line-search candidate, solver.py:1462-1464). */
+int mcfd_implicit_candidate(mcfd_geom* geom, const double* U, const double* dx, double damping,
+                            const double* scales, double* out, void* stream);
+
 /* ---- measurement ---- */
 
 /* kernel classes for mcfd_profile_read */
@@ -231,6 +296,18 @@ int mcfd_status_fetch(mcfd_geom* geom, void* stream, mcfd_status* out);
  */
 int mcfd_profile_enable(mcfd_geom* geom, int32_t enable);
 int mcfd_profile_read(mcfd_geom* geom, double* total_ms, int64_t* groups);
+
+/*
+ * Batched cases (no counterpart in the reference, which solves one case per
+ * call): the geometry holds independent cases back to back, cells of case k
+ * in [case_offsets[k], case_offsets[k+1]) (device int32 [n_cases + 1]).
+ * Writes each case's global stable time step (min over its cells,
+ * solver.py:4117-4129) to dt_case (device [n_cases]) and broadcasts it to
+ * dt_cells (device [n_cells]) for mcfd_explicit_step with dt_per_cell = 1.
+ */
+int mcfd_batch_time_steps(mcfd_geom* geom, const mcfd_config* cfg, const double* P,
+                          const int32_t* case_offsets, int32_t n_cases, double* dt_case,
+                          double* dt_cells, void* stream);
 
 /* Number of kernels this library has launched in the process so far. */
 int64_t mcfd_launch_count(void);

@@ -79,9 +79,21 @@ SIGNATURES = {
     "mcfd_geom_primitive": (c_vp, [c_vp]),
     "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
+    "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),
+    "mcfd_implicit_matvec": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_implicit_set_jacobian": (c_i32, [c_vp, c_i32]),
+    "mcfd_jvp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_vjp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_wall_force": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_dbl, c_dbl, P_dbl, c_vp, c_vp]),
+    "mcfd_lusgs_apply": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_gmres": (c_i32, [c_vp, c_vp, c_vp, c_dbl, c_i32, c_i32, C.POINTER(c_i32), c_vp]),
+    "mcfd_implicit_equation": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, P_dbl, c_vp, P_dbl, c_vp]),
+    "mcfd_implicit_scale_maxima": (c_i32, [c_vp, C.POINTER(Config), c_vp, P_dbl, c_vp]),
+    "mcfd_implicit_candidate": (c_i32, [c_vp, c_vp, c_vp, c_dbl, P_dbl, c_vp, c_vp]),
     "mcfd_profile_enable": (c_i32, [c_vp, c_i32]),
     "mcfd_profile_read": (c_i32, [c_vp, P_dbl, P_i64]),
     "mcfd_launch_count": (c_i64, []),
+    "mcfd_batch_time_steps": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
     "mcfd_residual_sumsq_noalloc": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "mcfd_host_cell_geometry": (c_i32, [c_i64, P_i64, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
     "mcfd_host_face_geometry": (c_i32, [c_i64, P_i64, P_dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),

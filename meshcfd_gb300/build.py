@@ -27,6 +27,9 @@ UNITS = [
     ("mcfd_kernels_fast.cu", ["-fmad=false"]),
     ("mcfd_kernels_fma.cu", ["-fmad=true"]),
     ("mcfd_kernels_common.cu", ["-fmad=false"]),
+    ("mcfd_implicit.cu", ["-fmad=false"]),
+    ("mcfd_jvp.cu", ["-fmad=false"]),
+    ("mcfd_vjp.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),
     ("mcfd_noalloc.cu", ["-fmad=false"]),
 ]

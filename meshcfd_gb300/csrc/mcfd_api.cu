@@ -1,11 +1,15 @@
 // C ABI of the residual / explicit-step path: geometry packing (host), device
 // workspace, and the orchestration of kernels per entry point.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
 #include <vector>
 
+#include "mcfd_implicit.h"
+#include "mcfd_jvp.h"
+#include "mcfd_vjp.h"
 #include "mcfd_internal.h"
 
 using namespace mcfd;
@@ -26,6 +30,14 @@ struct mcfd_geom {
   DevStatus* status = nullptr;  // inside the arena
   DevStatus* host_status = nullptr;  // pinned
   mcfd_geom_info info{};
+  ImplicitTopology topo;       // host copy for the implicit path (built lazily)
+  ImplicitState imp;
+  bool imp_built = false;
+  mcfd_config imp_cfg{};       // first-order settings of the prepared operator
+  int imp_exact_jacobian = 0;  // GMRES operator: 0 finite differences (reference), 1 exact JVP
+  JvpWork jvp;                 // tangent workspace (allocated on first use)
+  VjpWork vjp;                 // adjoint workspace (allocated on first use)
+  std::vector<void*> jvp_owned;
 };
 
 namespace {
@@ -132,6 +144,8 @@ const char* mcfd_error_string(int code) {
     case MCFD_E_UNSUPPORTED: return "option not supported by the GPU path";
     case MCFD_E_GEOMETRY: return "inconsistent geometry description";
     case MCFD_E_TOO_LARGE: return "size exceeds the maximum of the allocation-free entry point";
+    case MCFD_E_NOT_CONVERGED: return "GMRES did not converge";
+    case MCFD_E_BREAKDOWN: return "GMRES broke down";
     default: return "unknown error";
   }
 }
@@ -185,10 +199,11 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   seg_begin[SEG_FAR] = (int)(NI + NP + NW + NV + NO);
   seg_begin[SEG_COUNT] = (int)n_flux;
   std::vector<int> lslot(n_flux), rslot(n_flux, -1), lcell(n_flux), rcell(n_flux, -1);
-  std::vector<double> normal(2 * n_flux), wallv(2 * NW, 0.0), vin(4 * NV), pout(NO), far(4 * NF);
+  std::vector<double> normal(2 * n_flux), flen(n_flux), wallv(2 * NW, 0.0), vin(4 * NV), pout(NO), far(4 * NF);
   auto set_face = [&](int64_t k, int64_t f) {
     lslot[k] = (int)f;
     lcell[k] = (int)d->owners[f];
+    flen[k] = d->face_lengths[f];
     normal[2 * k] = d->face_normals[2 * f];
     normal[2 * k + 1] = d->face_normals[2 * f + 1];
   };
@@ -292,18 +307,31 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
     }
   }
   // ---- gradient entries grouped by source, reference order kept
-  std::vector<int> grad_ptr, grad_nb(NG);
+  std::vector<int> grad_ptr, grad_nb(NG), grad_twin(NG, -1);
   std::vector<double> grad_cx(NG), grad_cy(NG);
+  bool twins_ok = (NG % 2) == 0;
   {
     key.resize(NG);
     for (int64_t e = 0; e < NG; ++e) key[e] = (int)d->gradient_sources[e];
     group_by(key, (int)C, grad_ptr, order);
+    std::vector<int> pos(NG);
     for (int64_t j = 0; j < NG; ++j) {
       int e = order[j];
+      pos[e] = (int)j;
       grad_nb[j] = (int)d->gradient_neighbours[e];
       grad_cx[j] = d->gradient_coefficients_x[e];
       grad_cy[j] = d->gradient_coefficients_y[e];
     }
+    // the reference appends entries in pairs (a -> b, b -> a) per face
+    // (solver.py:2004-2021): the twin of entry e is e ^ 1
+    for (int64_t e = 0; twins_ok && e < NG; ++e) {
+      const int64_t t = e ^ 1;
+      if (d->gradient_sources[e] != d->gradient_neighbours[t] || d->gradient_neighbours[e] != d->gradient_sources[t])
+        twins_ok = false;
+      else
+        grad_twin[pos[e]] = pos[t];
+    }
+    if (!twins_ok) std::fill(grad_twin.begin(), grad_twin.end(), -1);
   }
   // ---- limiter entries grouped by cell
   std::vector<int> lim_ptr, lim_slot(NL);
@@ -361,12 +389,12 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   const int partial_blocks = 152 * 4;
   size_t o_area = A.take(bytes_d(C));
   size_t o_grad_ptr = A.take(bytes_i(C + 1)), o_grad_nb = A.take(bytes_i(NG)),
-         o_grad_cx = A.take(bytes_d(NG)), o_grad_cy = A.take(bytes_d(NG));
+         o_grad_cx = A.take(bytes_d(NG)), o_grad_cy = A.take(bytes_d(NG)), o_grad_twin = A.take(bytes_i(NG));
   size_t o_lim_ptr = A.take(bytes_i(C + 1)), o_lim_slot = A.take(bytes_i(NL)),
          o_lim_d = A.take(bytes_d(2 * NL));
   size_t o_lslot = A.take(bytes_i(n_flux)), o_rslot = A.take(bytes_i(n_flux)),
          o_lcell = A.take(bytes_i(n_flux)), o_rcell = A.take(bytes_i(n_flux)),
-         o_normal = A.take(bytes_d(2 * n_flux)), o_wallv = A.take(bytes_d(2 * NW)),
+         o_normal = A.take(bytes_d(2 * n_flux)), o_flen = A.take(bytes_d(n_flux)), o_wallv = A.take(bytes_d(2 * NW)),
          o_vin = A.take(bytes_d(4 * NV)), o_pout = A.take(bytes_d(NO)), o_far = A.take(bytes_d(4 * NF));
   size_t o_gi_ptr = A.take(bytes_i(C + 1)), o_gi_flux = A.take(bytes_i(gi_flux.size())),
          o_gi_coef = A.take(bytes_d(gi_coef.size()));
@@ -399,6 +427,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   put(o_grad_nb, grad_nb.data(), bytes_i(NG));
   put(o_grad_cx, grad_cx.data(), bytes_d(NG));
   put(o_grad_cy, grad_cy.data(), bytes_d(NG));
+  put(o_grad_twin, grad_twin.data(), bytes_i(NG));
   put(o_lim_ptr, lim_ptr.data(), bytes_i(C + 1));
   put(o_lim_slot, lim_slot.data(), bytes_i(NL));
   put(o_lim_d, lim_d.data(), bytes_d(2 * NL));
@@ -407,6 +436,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   put(o_lcell, lcell.data(), bytes_i(n_flux));
   put(o_rcell, rcell.data(), bytes_i(n_flux));
   put(o_normal, normal.data(), bytes_d(2 * n_flux));
+  put(o_flen, flen.data(), bytes_d(n_flux));
   put(o_wallv, wallv.data(), bytes_d(2 * NW));
   put(o_vin, vin.data(), bytes_d(4 * NV));
   put(o_pout, pout.data(), bytes_d(NO));
@@ -437,6 +467,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   g.n_faces = (int)F;
   g.n_flux = (int)n_flux;
   g.n_slots = (int)NL;
+  g.n_gradient = (int)NG;
   for (int k = 0; k <= SEG_COUNT; ++k) g.seg_begin[k] = seg_begin[k];
 #define AT(T, off) reinterpret_cast<T>(base + (off))
   g.area = AT(const double*, o_area);
@@ -444,6 +475,8 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   g.grad_nb = AT(const int*, o_grad_nb);
   g.grad_cx = AT(const double*, o_grad_cx);
   g.grad_cy = AT(const double*, o_grad_cy);
+  g.grad_twin = AT(const int*, o_grad_twin);
+  g.has_twins = twins_ok ? 1 : 0;
   g.lim_ptr = AT(const int*, o_lim_ptr);
   g.lim_slot = AT(const int*, o_lim_slot);
   g.lim_d = AT(const double2*, o_lim_d);
@@ -452,6 +485,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   g.ff_lcell = AT(const int*, o_lcell);
   g.ff_rcell = AT(const int*, o_rcell);
   g.ff_normal = AT(const double2*, o_normal);
+  g.ff_len = AT(const double*, o_flen);
   g.ff_wall_velocity = AT(const double2*, o_wallv);
   g.ff_vin_state = AT(const double*, o_vin);
   g.ff_pout_pressure = AT(const double*, o_pout);
@@ -487,6 +521,35 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   info.n_gradient = NG;
   info.n_limiter = NL;
   info.device_bytes = (int64_t)A.size;
+  // topology of the implicit preconditioner (solver.py:1185-1300)
+  {
+    ImplicitTopology& t = h->topo;
+    t.n_cells = (int)C;
+    t.n_interior = (int)NI;
+    for (int64_t i = 0; i < NI; ++i) {
+      int64_t f = d->interior_faces[i];
+      double2 n = make_double2(d->face_normals[2 * f], d->face_normals[2 * f + 1]);
+      t.coupling_a.push_back((int)d->owners[f]);
+      t.coupling_b.push_back((int)d->neighbours[f]);
+      t.coupling_na.push_back(n);
+      t.coupling_nb.push_back(n);
+      t.coupling_len.push_back(d->face_lengths[f]);
+    }
+    for (int64_t i = 0; i < NP; ++i) {
+      int64_t fa = d->periodic_faces_a[i], fb = d->periodic_faces_b[i];
+      t.coupling_a.push_back((int)d->owners[fa]);
+      t.coupling_b.push_back((int)d->owners[fb]);
+      t.coupling_na.push_back(make_double2(d->face_normals[2 * fa], d->face_normals[2 * fa + 1]));
+      t.coupling_nb.push_back(make_double2(d->face_normals[2 * fb], d->face_normals[2 * fb + 1]));
+      t.coupling_len.push_back(d->face_lengths[fa]);
+    }
+    for (int64_t f = 0; f < F; ++f) {
+      if (d->neighbours[f] >= 0) continue;
+      t.boundary_owner.push_back((int)d->owners[f]);
+      t.boundary_normal.push_back(make_double2(d->face_normals[2 * f], d->face_normals[2 * f + 1]));
+      t.boundary_len.push_back(d->face_lengths[f]);
+    }
+  }
   *out = h;
   return MCFD_OK;
 }
@@ -498,6 +561,8 @@ int mcfd_geom_destroy(mcfd_geom* h) {
     cudaEventDestroy(r.stop);
   }
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+  if (h->imp_built) implicit_free(h->imp);
+  for (void* p : h->jvp_owned) cudaFree(p);
   cudaError_t e1 = cudaFree(h->arena);
   cudaError_t e2 = cudaFreeHost(h->host_status);
   delete h;
@@ -626,6 +691,210 @@ int mcfd_status_fetch(mcfd_geom* h, void* stream, mcfd_status* out) {
   return MCFD_OK;
 }
 
+
+// ------------------------------------------------------------- implicit Euler
+
+static int ensure_implicit(mcfd_geom* h) {
+  if (h->imp_built) return MCFD_OK;
+  if (implicit_build(h->imp, h->topo) != cudaSuccess) {
+    implicit_free(h->imp);
+    return MCFD_E_CUDA;
+  }
+  h->imp_built = true;
+  return MCFD_OK;
+}
+
+static ScaleVec scale_of(const double* scales) {
+  ScaleVec v;
+  for (int k = 0; k < 4; ++k) v.v[k] = scales[k];
+  return v;
+}
+
+// first-order residual of the prepared operator
+static cudaError_t residual_first_order(mcfd_geom* h, const double* U, double* R, cudaStream_t s) {
+  const mcfd_config& c = h->imp_cfg;
+  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(c, launch_primitive(h->g, c, U, h->ws.P, s)); });
+  StageProgram prog{};
+  prog.out_r = R;
+  if (e == cudaSuccess) e = stage(h, c, prog, s);
+  return e;
+}
+
+int mcfd_implicit_prepare(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double* dt,
+                          int32_t dt_per_cell, const double* scales, void* stream) {
+  if (!h || !U || !dt || !scales) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if ((c = ensure_implicit(h))) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  ImplicitState& st = h->imp;
+  h->imp_cfg = *cfg;
+  h->imp_cfg.reconstruction = MCFD_RECON_FIRST_ORDER;  // replace(settings, reconstruction="First order")
+  st.scale = scale_of(scales);
+  st.dt = dt;
+  st.dt_per_cell = dt_per_cell;
+  const size_t bytes = 4 * (size_t)h->g.n_cells * sizeof(double);
+  cudaError_t e = cudaMemcpyAsync(st.state, U, bytes, cudaMemcpyDeviceToDevice, s);
+  // preconditioner from the state's primitive variables
+  if (e == cudaSuccess)
+    e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, h->ws.P, s)); });
+  if (e == cudaSuccess)
+    e = timed(h, MCFD_PROF_OTHER, s, [&] { return implicit_assemble(st, h->ws.P, h->g.area, dt, dt_per_cell, cfg->gamma, s); });
+  // jacobian_rate = R1(state)
+  if (e == cudaSuccess) e = residual_first_order(h, U, st.rate, s);
+  // |state / scale|
+  if (e == cudaSuccess) e = implicit_scaled_sumsq(st, U, st.scale, st.scalars + 8, s);
+  double sumsq = 0.0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&sumsq, st.scalars + 8, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  st.state_norm = std::sqrt(sumsq);
+  st.prepared = e == cudaSuccess;
+  return rc(e);
+}
+
+static int ensure_jvp(mcfd_geom* h) {
+  if (h->jvp.P) return MCFD_OK;
+  const size_t c4 = 4 * (size_t)h->g.n_cells * sizeof(double);
+  const size_t s4 = 4 * (size_t)h->g.n_slots * sizeof(double);
+  const size_t f4 = 4 * (size_t)std::max(h->g.n_flux, 1) * sizeof(double);
+  double** fields[] = {&h->jvp.P, &h->jvp.dP, &h->jvp.recon, &h->jvp.drecon, &h->jvp.dflux, &h->jvp.sv, &h->jvp.dR};
+  const size_t sizes[] = {c4, c4, s4, s4, f4, c4, c4};
+  for (int k = 0; k < 7; ++k) {
+    if (cudaMalloc((void**)fields[k], sizes[k]) != cudaSuccess) return MCFD_E_CUDA;
+    h->jvp_owned.push_back(*fields[k]);
+  }
+  return MCFD_OK;
+}
+
+static MatvecFn implicit_operator(mcfd_geom* h) {
+  if (h->imp_exact_jacobian)
+    return [h](const double* v, double* out, cudaStream_t ss) {
+      return timed(h, MCFD_PROF_OTHER, ss, [&] { return exact_operator(h->g, h->imp_cfg, h->imp, h->jvp, v, out, ss); });
+    };
+  return [h](const double* v, double* out, cudaStream_t ss) {
+    ResidualFn r1 = [h](const double* U, double* R, cudaStream_t s2) { return residual_first_order(h, U, R, s2); };
+    return fd_operator(h->imp, r1, v, out, ss);
+  };
+}
+
+int mcfd_implicit_matvec(mcfd_geom* h, const double* v, double* out, void* stream) {
+  if (!h || !v || !out || !h->imp_built || !h->imp.prepared) return MCFD_E_ARG;
+  return rc(implicit_operator(h)(v, out, (cudaStream_t)stream));
+}
+
+int mcfd_implicit_set_jacobian(mcfd_geom* h, int32_t exact) {
+  if (!h) return MCFD_E_ARG;
+  if (exact) {
+    int c = ensure_jvp(h);
+    if (c) return c;
+  }
+  h->imp_exact_jacobian = exact != 0;
+  return MCFD_OK;
+}
+
+static int ensure_vjp(mcfd_geom* h) {
+  if (h->vjp.P) return MCFD_OK;
+  const size_t c4 = 4 * (size_t)h->g.n_cells * sizeof(double);
+  const size_t s4 = 4 * (size_t)std::max(h->g.n_slots, 1) * sizeof(double);
+  const size_t e4 = 4 * (size_t)std::max(h->g.n_gradient, 1) * sizeof(double);
+  double** fields[] = {&h->vjp.P, &h->vjp.recon, &h->vjp.slot_bar, &h->vjp.pbar, &h->vjp.ent_bar, &h->vjp.partials};
+  const size_t sizes[] = {c4, s4, s4, c4, e4, 608 * sizeof(double)};
+  for (int k = 0; k < 6; ++k) {
+    if (cudaMalloc((void**)fields[k], sizes[k]) != cudaSuccess) return MCFD_E_CUDA;
+    h->jvp_owned.push_back(*fields[k]);
+  }
+  return MCFD_OK;
+}
+
+int mcfd_vjp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double* lambda, double* U_bar,
+             double* far_bar, void* stream) {
+  if (!h || !U || !lambda || !U_bar) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if (cfg->reconstruction != MCFD_RECON_FIRST_ORDER && !h->g.has_twins) return MCFD_E_UNSUPPORTED;
+  if ((c = ensure_vjp(h))) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return launch_vjp(h->g, *cfg, U, lambda, h->vjp, U_bar, far_bar, s); }));
+}
+
+int mcfd_wall_force(mcfd_geom* h, const mcfd_config* cfg, const double* U, double dir_x, double dir_y, double* J,
+                    double* dJdU, void* stream) {
+  if (!h || !U || !J) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if ((c = ensure_vjp(h))) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = launch_wall_force(h->g, *cfg, U, dir_x, dir_y, h->vjp, h->vjp.partials + 600, dJdU, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(J, h->vjp.partials + 600, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return rc(e);
+}
+
+int mcfd_jvp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double* dU, double* dR, void* stream) {
+  if (!h || !U || !dU || !dR) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if ((c = ensure_jvp(h))) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return launch_jvp(h->g, *cfg, U, dU, h->jvp, dR, s); }));
+}
+
+int mcfd_lusgs_apply(mcfd_geom* h, const double* v, double* x, void* stream) {
+  if (!h || !v || !x || !h->imp_built || !h->imp.prepared) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return lusgs_apply(h->imp, v, x, s); }));
+}
+
+int mcfd_gmres(mcfd_geom* h, const double* b, double* x, double tol, int32_t max_iter, int32_t krylov_dim,
+               int32_t* iterations, void* stream) {
+  if (!h || !b || !x || !h->imp_built || !h->imp.prepared || max_iter <= 0 || krylov_dim <= 0) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  MatvecFn mv = implicit_operator(h);
+  int it = 0;
+  int r = gmres_solve(h->imp, mv, b, x, tol, max_iter, krylov_dim, &it, s);
+  if (iterations) *iterations = it;
+  switch (r) {
+    case GMRES_OK: return MCFD_OK;
+    case GMRES_NOT_CONVERGED: return MCFD_E_NOT_CONVERGED;
+    case GMRES_BREAKDOWN: return MCFD_E_BREAKDOWN;
+    default: return MCFD_E_CUDA;
+  }
+}
+
+int mcfd_implicit_equation(mcfd_geom* h, const double* U, const double* U0, const double* R, const double* dt,
+                           int32_t dt_per_cell, const double* scales, double* b, double* norms, void* stream) {
+  if (!h || !U || !U0 || !R || !dt || !scales || !norms) return MCFD_E_ARG;
+  int c = ensure_implicit(h);
+  if (c) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  ImplicitState& st = h->imp;
+  cudaError_t e = implicit_equation(st, U, U0, R, dt, dt_per_cell, scale_of(scales), b, st.scalars + 10, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(norms, st.scalars + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return rc(e);
+}
+
+int mcfd_implicit_scale_maxima(mcfd_geom* h, const mcfd_config* cfg, const double* U, double* maxima,
+                               void* stream) {
+  if (!h || !U || !maxima) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if ((c = ensure_implicit(h))) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  ImplicitState& st = h->imp;
+  cudaError_t e = MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, h->ws.P, s));
+  if (e == cudaSuccess) e = implicit_maxima(st, U, h->ws.P, cfg->gamma, st.scalars + 16, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(maxima, st.scalars + 16, 9 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return rc(e);
+}
+
+int mcfd_implicit_candidate(mcfd_geom* h, const double* U, const double* dx, double damping, const double* scales,
+                            double* out, void* stream) {
+  if (!h || !U || !dx || !scales || !out) return MCFD_E_ARG;
+  return rc(implicit_candidate(h->g.n_cells, U, dx, damping, scale_of(scales), out, (cudaStream_t)stream));
+}
+
 int mcfd_profile_enable(mcfd_geom* h, int32_t enable) {
   if (!h) return MCFD_E_ARG;
   h->profiling = enable != 0;
@@ -653,6 +922,21 @@ int mcfd_profile_read(mcfd_geom* h, double* total_ms, int64_t* groups) {
 }
 
 int64_t mcfd_launch_count(void) { return (int64_t)launch_count(); }
+
+int mcfd_batch_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, const int32_t* case_offsets,
+                          int32_t n_cases, double* dt_case, double* dt_cells, void* stream) {
+  if (!h || !P || !case_offsets || n_cases <= 0 || !dt_case || !dt_cells) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = timed(h, MCFD_PROF_TIME_STEP, s, [&] {
+    cudaError_t r = MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, nullptr, 0.0, s));
+    if (r == cudaSuccess) r = launch_case_time_steps(h->g.n_cells, n_cases, case_offsets, dt_case, dt_cells, s);
+    return r;
+  });
+  return rc(e);
+}
 
 // ------------------------------------------------------------- host helpers
 

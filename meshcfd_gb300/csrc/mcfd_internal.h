@@ -30,7 +30,7 @@ struct DevStatus {
 // Everything a kernel needs, by value.  Index arrays are int32 (sizes are
 // checked against 2^31 at creation).
 struct DevGeom {
-  int n_cells, n_faces, n_flux, n_slots;
+  int n_cells, n_faces, n_flux, n_slots, n_gradient;
   int seg_begin[SEG_COUNT + 1];
   const double* area;  // [C]
   // least-squares gradient entries grouped by source cell, reference order
@@ -38,6 +38,8 @@ struct DevGeom {
   const int* grad_nb;
   const double* grad_cx;
   const double* grad_cy;
+  const int* grad_twin;  // CSR position of the paired entry (b -> a for a -> b), or -1
+  int has_twins;
   // limiter entries grouped by cell: slot id (reference entry index) + offset
   const int* lim_ptr;
   const int* lim_slot;
@@ -48,6 +50,7 @@ struct DevGeom {
   const int* ff_lcell;  // cell of the left state
   const int* ff_rcell;  // cell of the right state (interior/periodic), else -1
   const double2* ff_normal;
+  const double* ff_len;             // face length (periodic pairs: face a's)
   const double2* ff_wall_velocity;  // indexed by flux face - seg_begin[SEG_WALL]
   const double* ff_vin_state;       // [n_vin][4]
   const double* ff_pout_pressure;   // [n_pout]
@@ -122,6 +125,8 @@ MCFD_DECLARE_LAUNCHERS(fma)
 // variant-independent (mcfd_kernels_common.cu)
 long long launch_count();
 void count_launch(int n = 1);
+cudaError_t launch_case_time_steps(int n_cells, int n_cases, const int* offsets, double* dt_case,
+                                   double* dt_cells, cudaStream_t s);
 // reduction kernels of the sum of squares
 __global__ void k_sumsq_partial(int n, const double* __restrict__ R, double* __restrict__ partials);
 __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums);

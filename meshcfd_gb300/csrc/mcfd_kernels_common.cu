@@ -36,6 +36,56 @@ __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, d
   }
 }
 
+// ------------------------------------------------------------ batched cases
+
+// Per-case minimum of positive per-cell time steps (one block per case; the
+// doubles' bit patterns order like the values), written to dt_case.
+__global__ void __launch_bounds__(kBlock) k_case_min(const int* __restrict__ offsets,
+                                                     const double* __restrict__ dt_cells,
+                                                     double* __restrict__ dt_case) {
+  const int k = blockIdx.x;
+  const int b = offsets[k], e = offsets[k + 1];
+  long long m = 0x7ff0000000000000LL;
+  for (int c = b + threadIdx.x; c < e; c += blockDim.x) {
+    const long long v = __double_as_longlong(dt_cells[c]);
+    m = v < m ? v : m;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const long long o = __shfl_down_sync(0xffffffffu, m, off);
+    m = o < m ? o : m;
+  }
+  __shared__ long long wmin[kBlock / 32];
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long r = wmin[0];
+    for (int w = 1; w < kBlock / 32; ++w) r = wmin[w] < r ? wmin[w] : r;
+    dt_case[k] = __longlong_as_double(r);
+  }
+}
+
+// dt_cells[c] = dt_case[case of c] (binary search in the offset table)
+__global__ void k_case_broadcast(int n_cells, int n_cases, const int* __restrict__ offsets,
+                                 const double* __restrict__ dt_case, double* __restrict__ dt_cells) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cells) return;
+  int lo = 0, hi = n_cases;  // offsets[lo] <= c < offsets[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (offsets[mid] <= c) lo = mid;
+    else hi = mid;
+  }
+  dt_cells[c] = dt_case[lo];
+}
+
+cudaError_t launch_case_time_steps(int n_cells, int n_cases, const int* offsets, double* dt_case,
+                                   double* dt_cells, cudaStream_t s) {
+  count_launch(2);
+  k_case_min<<<n_cases, kBlock, 0, s>>>(offsets, dt_cells, dt_case);
+  k_case_broadcast<<<(n_cells + kBlock - 1) / kBlock, kBlock, 0, s>>>(n_cells, n_cases, offsets, dt_case, dt_cells);
+  return cudaGetLastError();
+}
+
 // Kernels launched by this library (host-side counter, for measurement).
 static long long g_launches = 0;
 long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }

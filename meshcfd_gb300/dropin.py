@@ -9,6 +9,7 @@ GPU-backed versions taking and returning NumPy arrays:
 * ``_stable_time_steps(primitive, geometry, settings, turbulence=None)`` solver.py:4132
 * ``_stable_time_step(primitive, geometry, settings, turbulence=None)``  solver.py:4117
 * ``_explicit_rk4_step(state, time_step, geometry, settings)``          solver.py:1128
+* ``_implicit_euler_step(initial, time_step, geometry, settings, ...)``  solver.py:1337
 
 so ``solve_case`` runs unchanged on top of them.  :func:`solve_case` goes
 further: it keeps the state in HBM for the whole explicit loop and returns the
@@ -27,7 +28,7 @@ import torch
 from .device import TIME_SCHEME_CODES, DeviceGeometry, make_config
 from .errors import raise_for_status
 
-_PATCHED = ("_residual", "_stable_time_steps", "_stable_time_step", "_explicit_rk4_step")
+_PATCHED = ("_residual", "_stable_time_steps", "_stable_time_step", "_explicit_rk4_step", "_implicit_euler_step")
 
 
 class _Cache:
@@ -123,6 +124,26 @@ def make_explicit_rk4_step(module=None):
     return _explicit_rk4_step
 
 
+def make_implicit_euler_step(module=None):
+    solver_error = _solver_error(module) or ValueError
+
+    def _implicit_euler_step(initial, time_step, geometry, settings, allow_time_step_reduction=True):
+        from .implicit import ImplicitEuler
+
+        if np.shape(initial)[1] != 4:
+            raise NotImplementedError("SST state is not implemented by the GPU implicit step")
+        dg = _cache.get(geometry)
+        dev = _device()
+        U0 = torch.as_tensor(np.array(initial, dtype=np.float64, order="C"), device=dev)
+        dt = torch.as_tensor(np.atleast_1d(np.asarray(time_step, dtype=np.float64)).copy(), device=dev)
+        stepper = ImplicitEuler(dg, settings, solver_error=solver_error)
+        state, used = stepper.step(U0, dt, allow_time_step_reduction)
+        used_np = used.cpu().numpy()
+        return state.cpu().numpy(), (float(used_np[0]) if np.ndim(time_step) == 0 else used_np)
+
+    return _implicit_euler_step
+
+
 def install(module):
     """Patch ``module`` (the reference's ``meshcfd.core.solver``) in place.
     Returns the originals for :func:`uninstall`."""
@@ -131,6 +152,7 @@ def install(module):
     module._stable_time_steps = make_stable_time_steps(module)
     module._stable_time_step = make_stable_time_step(module)
     module._explicit_rk4_step = make_explicit_rk4_step(module)
+    module._implicit_euler_step = make_implicit_euler_step(module)
     return originals
 
 

@@ -142,6 +142,51 @@ def solve_fixture(name, case, primitive, settings, steps, ref):
     print(name, len(primitive), "cells,", result.steps, "steps, t =", result.time)
 
 
+def implicit_fixture(name, case, primitive, settings, steps, ref):
+    """Implicit Euler: the LU-SGS preconditioner and the finite-difference
+    operator applied to seeded vectors, and solve_case after ``steps`` steps."""
+    from dataclasses import replace
+
+    rc = reference_case(case, ref)
+    for key, value in settings.items():
+        setattr(rc.numerics, key, value)
+    num = rc.numerics
+    rg = ref.solver._build_geometry(rc.mesh, rc)
+    out = {**mesh_arrays(case), **geometry_arrays(rg), "P0": primitive}
+    n = len(primitive)
+    U = ref.euler.primitive_to_conservative(primitive, num.gamma)
+    dt = ref.solver._stable_time_steps(primitive, rg, num)
+    first = replace(num, reconstruction="First order")
+    rng = np.random.default_rng(11)
+    v = rng.standard_normal(4 * n)
+    M = ref.solver._implicit_preconditioner(primitive, rg, first, dt, 4)
+    out.update(U=U, dt_cells=dt, v=v, lusgs_v=M.matvec(v))
+    rho = max(float(np.max(primitive[:, 0])), 1e-12)
+    speed = max(float(np.max(np.abs(primitive[:, 1:3]))),
+                float(np.max(np.sqrt(num.gamma * primitive[:, 3] / primitive[:, 0]))), 1e-12)
+    scales = np.maximum(np.max(np.abs(U), axis=0), 1e-12)
+    scales[0] = max(scales[0], rho)
+    scales[1:3] = np.maximum(scales[1:3], rho * speed)
+    scales[3] = max(scales[3], rho * speed**2, float(np.max(primitive[:, 3])) / (num.gamma - 1.0))
+    scale_grid = scales[None, :]
+    rate = ref.solver._time_state_rhs(U, rg, first)
+    op = ref.solver._matrix_free_implicit_operator(U, rate, scale_grid, dt, rg, first)
+    out.update(scales=scales, operator_v=op.matvec(v))
+    num.max_iterations = steps
+    num.end_time = 1.0e30
+    num.residual_tolerance = 1e-300
+    num.convergence_history_interval = steps + 1
+    states = tuple(ref.model.InitialState(*map(float, row)) for row in primitive)
+    result = ref.solver.solve_case(rc, states)
+    out["P_final"] = np.array([(s.density, s.velocity_x, s.velocity_y, s.pressure) for s in result.states])
+    out["time"] = np.array(result.time)
+    out["steps"] = np.array(result.steps)
+    for key, value in settings.items():
+        out[f"set|{key}"] = np.array(value)
+    np.savez_compressed(HERE / f"implicit_{name}.npz", **out)
+    print("implicit", name, n, "cells,", result.steps, "steps, t =", result.time)
+
+
 def main():
     ref = import_reference()
     riemann, riemann_p = riemann_case(16)
@@ -163,6 +208,18 @@ def main():
     solve_fixture("channel_rk4_local", chan, cp,
                   {"flux": "Roe", "reconstruction": "MUSCL linear", "limiter": "Barth-Jespersen",
                    "time_integration": "Explicit RK4", "cfl": 0.6, "time_step_mode": "Local (steady)"}, 6, ref)
+    implicit_fixture("channel", chan, cp,
+                     {"flux": "Roe", "reconstruction": "MUSCL linear", "limiter": "Barth-Jespersen",
+                      "time_integration": "Implicit Euler", "time_step_mode": "Local (steady)", "cfl": 50.0,
+                      "gmres_tolerance": 1e-3, "gmres_krylov_dimension": 30, "implicit_preconditioner": "LU-SGS"},
+                     4, ref)
+    per = periodic_case(8, 6, split="half", jitter=0.25, seed=2)
+    pp = perturbed_primitive(len(per.mesh.cells), seed=4)
+    pp[:, 0] = np.abs(pp[:, 0])
+    implicit_fixture("periodic", per, pp,
+                     {"flux": "Rusanov", "reconstruction": "First order", "time_integration": "Implicit Euler",
+                      "time_step_mode": "Global adaptive", "cfl": 20.0, "gmres_tolerance": 1e-6,
+                      "gmres_krylov_dimension": 10, "implicit_preconditioner": "LU-SGS"}, 3, ref)
     solve_fixture("channel_rk2_vanleer", chan, cp,
                   {"flux": "HLLC", "reconstruction": "MUSCL linear", "limiter": "Van Leer",
                    "time_integration": "Explicit RK2", "cfl": 0.6, "acceleration_x": 0.2}, 8, ref)

@@ -61,3 +61,38 @@ def test_oracle_solve_matches_reference(name):
         assert time == float(data["time"])
     else:
         assert abs(time - float(data["time"])) <= 1e-14 * float(data["time"])
+
+
+@pytest.mark.parametrize("name", ("implicit_channel.npz", "implicit_periodic.npz"))
+def test_oracle_implicit_matches_reference(name):
+    """The oracle's restatement of the implicit Euler pieces against the
+    reference: LU-SGS application, the finite-difference operator, and the
+    implicit solve_case."""
+    from dataclasses import replace
+
+    from conftest import solve_settings
+    from oracle.implicit import ImplicitOracle
+
+    data, geom = load_fixture(name)
+    s = solve_settings(data)
+    imp = ImplicitOracle(geom)
+    first = replace(s, reconstruction="First order")
+    M = imp.preconditioner(data["P0"], first, data["dt_cells"])
+    np.testing.assert_allclose(M.matvec(data["v"]), data["lusgs_v"], rtol=1e-13, atol=1e-13 * np.abs(data["lusgs_v"]).max())
+    U = data["U"]
+    rate = imp.orc.residual(U, first)
+    op = imp.operator(U, rate, data["scales"][None, :], data["dt_cells"], first)
+    np.testing.assert_allclose(op.matvec(data["v"]), data["operator_v"], rtol=1e-12,
+                               atol=1e-12 * np.abs(data["operator_v"]).max())
+    # the implicit loop (local steady or global adaptive time step)
+    Uc = U.copy()
+    time = 0.0
+    for _ in range(int(data["steps"])):
+        P = imp.orc.primitive(Uc, s.gamma)
+        dt = imp.orc.stable_time_steps(P, s)
+        step = dt if s.time_step_mode == "Local (steady)" else float(np.min(dt))
+        Uc, used = imp.step(Uc, step, s)
+        time += float(np.mean(used))
+    P = imp.orc.primitive(Uc, s.gamma)
+    assert np.abs(P - data["P_final"]).max() <= 1e-10 * np.abs(data["P_final"]).max()
+    assert abs(time - float(data["time"])) <= 1e-12 * float(data["time"])
