@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gpu", "reference"), default="gpu")
     ap.add_argument("--workload", default="vortex1024",
-                    choices=("vortex1024", "vortex1024all", "vortex512", "vortex256", "batch256"))
+                    choices=("vortex1024", "vortex1024all", "vortex512", "vortex256", "batch256", "adjoint"))
+    ap.add_argument("--checkpoint-every", type=int, default=20)
     ap.add_argument("--batch-cases", type=int, default=256)
     ap.add_argument("--graph-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
@@ -500,10 +501,83 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def run_adjoint(args):
+    """Adjoint workload: O-grid 1024x512 around a cylinder (seed 2, Mach 0.3
+    free stream, slip wall, far field), HLLC / MUSCL-Venkatakrishnan, RK3 with
+    a fixed time step for ``--steps`` steps (default 400 here), checkpoints
+    every ``--checkpoint-every`` steps; the wall pressure force along x at the
+    final state and its gradient with respect to the initial state and the
+    far-field states by the discrete adjoint.  Reports the adjoint / forward
+    cost ratio (lower is better)."""
+    import torch
+
+    from meshcfd_gb300.adjoint import WallForceAdjoint
+    from meshcfd_gb300.device import DeviceGeometry
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import ogrid_case
+    from oracle.oracle import Oracle
+
+    device = torch.device("cuda", 0)
+    steps = args.steps if args.steps != 100 else 400
+    t0 = time.perf_counter()
+    case, P0 = ogrid_case(1024, 512, seed=2, mach=0.3)
+    g = build_geometry(case.mesh, case)
+    setup_s = time.perf_counter() - t0
+    settings = case.numerics
+    orc = Oracle(g)
+    U0h = orc.conservative(P0, settings.gamma)
+    dt = 0.9 * float(orc.stable_time_steps(P0, settings).min())
+    dg = DeviceGeometry(g, device)
+    adj = WallForceAdjoint(dg, settings, dt, direction=(1.0, 0.0), checkpoint_every=args.checkpoint_every,
+                           mode=args.mode)
+    U0 = torch.as_tensor(U0h, device=device)
+    for _ in range(max(1, args.warmup)):  # warm-up: a short forward + adjoint
+        adj.gradient(U0, min(steps, args.checkpoint_every + 1))
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    before = _launches()
+    with ClockSampler(0) as clocks:
+        ev[0].record()
+        UN = adj.forward(U0, steps)
+        ev[1].record()
+        J, dJ = adj.functional(UN)
+        lam0 = adj.backward(dJ)
+        ev[2].record()
+        torch.cuda.synchronize()
+    launches = _launches() - before
+    fwd_ms, adj_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    C = int(dg.n_cells)
+    line = {
+        "metric": "RK3 wall-force adjoint / forward cost ratio", "value": adj_ms / fwd_ms, "unit": "ratio",
+        "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": (fwd_ms + adj_ms) / steps,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded O-grid, free-stream start)",
+        "config": {"workload": f"O-grid 1024x512 around a cylinder ({C} cells), Mach 0.3, HLLC, MUSCL linear, "
+                               f"Venkatakrishnan, RK3 fixed dt, {steps} steps, checkpoint every "
+                               f"{args.checkpoint_every}", "mode": args.mode, "dt": dt, "setup_s": setup_s,
+                   "l2_flush": "working set larger than L2"},
+        "forward": {"ms": fwd_ms, "cell_updates_per_s": C * steps / (fwd_ms * 1e-3)},
+        "adjoint": {"ms": adj_ms, "cell_updates_per_s": C * steps / (adj_ms * 1e-3),
+                    "work_per_step": "1 replayed RK3 step + 3 residual VJPs"},
+        "J": J, "grad_norm": float(lam0.norm()), "far_grad_norm": float(adj.far_acc.norm()),
+        "gpu_launches": launches, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+
+
+def _launches():
+    from meshcfd_gb300._lib import native
+
+    return int(native().mcfd_launch_count())
+
+
 def main():
     args = parse()
     if args.workload == "batch256":
         run_batch(args)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args)
         return
     if args.impl == "reference":
         run_reference(args)

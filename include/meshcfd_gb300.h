@@ -201,6 +201,12 @@ int mcfd_explicit_step(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, 
 /* Device pointer to the handle's primitive buffer [n_cells][4] (valid after
  * mcfd_primitive / mcfd_residual / mcfd_explicit_step on the same handle). */
 const double* mcfd_geom_primitive(const mcfd_geom* geom);
+/* Device pointer to intermediate stage state k (0..3) [n_cells][4] of the
+ * last mcfd_explicit_step on the handle: for RK2 k = 0 is U1; for RK3 k = 0, 1
+ * are U1, U2; for SSPRK(5,4) k = 0..3 are U1..U4.  Valid until the next call
+ * on the handle; NULL for k out of range.  Used to replay a step's stages in
+ * reverse (no counterpart in the reference). */
+const double* mcfd_geom_stage_state(const mcfd_geom* geom, int32_t k);
 
 /*
  * Sum over cells of R[i][k]^2 for k = 0..3 into the device array sums[4]

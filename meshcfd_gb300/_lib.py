@@ -77,6 +77,7 @@ SIGNATURES = {
     "mcfd_time_steps": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_dbl, c_vp]),
     "mcfd_explicit_step": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp]),
     "mcfd_geom_primitive": (c_vp, [c_vp]),
+    "mcfd_geom_stage_state": (c_vp, [c_vp, C.c_int32]),
     "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
     "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),

@@ -1,0 +1,176 @@
+"""Discrete adjoint of a wall pressure force through SSP-RK3 time marching.
+
+There is no counterpart in the reference (its solver is not differentiable).
+The forward run is the reference's RK3 step (solver.py:566-567, 676-678,
+754-756) with a fixed time step; the functional is the wall pressure force
+J = sum over wall faces of p (n . d) L at the final state (`mcfd_wall_force`).
+The adjoint walks the steps backwards with the transposed residual Jacobian
+(`mcfd_vjp`, three products per step), replaying each segment of
+``checkpoint_every`` steps from its stored state with the forward step and
+keeping the stage states it leaves (`mcfd_geom_stage_state`), so the
+linearisation points are the forward run's own, bit for bit.  For one step
+U1 = U + dt R(U), U2 = 3/4 U + 1/4 (U1 + dt R(U1)), U' = 1/3 U + 2/3 (U2 + dt R(U2)):
+
+    l2 = 2/3 (l' + dt R(U2)^T l'),   l1 = 1/4 (l2 + dt R(U1)^T l2),
+    l  = 1/3 l' + 3/4 l2 + l1 + dt R(U)^T l1,
+
+and the far-field-state gradient collects the same products' parameter parts.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from .device import DeviceGeometry, _device_view, _stream_ptr, make_config
+
+
+class ResidualFunction(torch.autograd.Function):
+    """R = residual(U) with the hand-written reverse mode as its backward."""
+
+    @staticmethod
+    def forward(ctx, U, geom: DeviceGeometry, cfg):
+        ctx.save_for_backward(U)
+        ctx.geom, ctx.cfg = geom, cfg
+        return geom.residual(U.contiguous(), cfg)
+
+    @staticmethod
+    def backward(ctx, grad_R):
+        (U,) = ctx.saved_tensors
+        geom, cfg = ctx.geom, ctx.cfg
+        out = torch.empty_like(U)
+        geom.lib.check(geom.lib.mcfd_vjp(geom.handle, C.byref(cfg), U.data_ptr(), grad_R.contiguous().data_ptr(),
+                                         out.data_ptr(), None, _stream_ptr()), "mcfd_vjp")
+        return out, None, None
+
+
+class WallForceAdjoint:
+    """Forward RK3 with checkpoints and the reverse sweep for one geometry."""
+
+    def __init__(self, geom: DeviceGeometry, settings, dt: float, direction=(1.0, 0.0), checkpoint_every: int = 20,
+                 mode: str = "exact"):
+        self.geom = geom
+        self.cfg = make_config(settings, mode)
+        self.cfg_vjp = make_config(settings, "exact")
+        self.dt = float(dt)
+        self.direction = direction
+        self.k = int(checkpoint_every)
+        dev = geom.device
+        self.dt_dev = torch.full((1,), self.dt, dtype=torch.float64, device=dev)
+        self.W = torch.empty(geom.n_cells, 4, dtype=torch.float64, device=dev)
+        self.far = torch.zeros(max(geom.n_far_field, 1), 4, dtype=torch.float64, device=dev)
+        self.far_acc = torch.zeros_like(self.far)
+        self.checkpoints = []
+        self.steps = 0
+
+    # ---------------------------------------------------------------- forward
+    def step(self, U):
+        self.geom.explicit_step(U, self.cfg, 2, self.dt_dev)
+
+    def forward(self, U0: torch.Tensor, steps: int) -> torch.Tensor:
+        U = U0.clone()
+        self.checkpoints = [U0.clone()]
+        for s in range(1, steps + 1):
+            self.step(U)
+            if s % self.k == 0 and s < steps:
+                self.checkpoints.append(U.clone())
+        self.steps = steps
+        self.geom.check_status()
+        return U
+
+    def functional(self, U):
+        J = (C.c_double * 1)()
+        dJ = torch.empty_like(U)
+        self.geom.lib.check(self.geom.lib.mcfd_wall_force(self.geom.handle, C.byref(self.cfg), U.data_ptr(),
+                                                          float(self.direction[0]), float(self.direction[1]), J,
+                                                          dJ.data_ptr(), _stream_ptr()), "mcfd_wall_force")
+        return float(J[0]), dJ
+
+    # --------------------------------------------------------------- reverse
+    def _vjp(self, U, lam, far_weight):
+        lib = self.geom.lib
+        lib.check(lib.mcfd_vjp(self.geom.handle, C.byref(self.cfg_vjp), U.data_ptr(), lam.data_ptr(),
+                               self.W.data_ptr(), self.far.data_ptr(), _stream_ptr()), "mcfd_vjp")
+        if far_weight:
+            self.far_acc.add_(self.far, alpha=far_weight)
+        return self.W
+
+    def _replay(self, U):
+        """Advance U one step in place and return the step's stage states
+        (U1, U2) as copies of the handle's stage buffers."""
+        self.step(U)
+        lib, n = self.geom.lib, self.geom.n_cells
+        return tuple(_device_view(lib.mcfd_geom_stage_state(self.geom.handle, k), (n, 4), self.geom.device).clone()
+                     for k in (0, 1))
+
+    def backward(self, lam_final: torch.Tensor) -> torch.Tensor:
+        """Adjoint of the initial state; the far-field-state gradient per
+        far-field face accumulates in ``self.far_acc``.  Each segment is
+        replayed from its checkpoint with the forward step, keeping every
+        step's three stage states (3 x checkpoint_every states at most)."""
+        dt = self.dt
+        lam = lam_final.clone()
+        self.far_acc.zero_()
+        for seg in range(len(self.checkpoints) - 1, -1, -1):
+            start = seg * self.k
+            end = min(start + self.k, self.steps)
+            U = self.checkpoints[seg].clone()
+            stages = []
+            for _ in range(start, end):
+                U0 = U.clone()
+                U1, U2 = self._replay(U)
+                stages.append((U0, U1, U2))
+            for U0, U1, U2 in reversed(stages):
+                w = self._vjp(U2, lam, (2.0 / 3.0) * dt)
+                lam2 = (2.0 / 3.0) * (lam + dt * w)
+                new = (1.0 / 3.0) * lam
+                w = self._vjp(U1, lam2, 0.25 * dt)
+                lam1 = 0.25 * (lam2 + dt * w)
+                new += 0.75 * lam2
+                w = self._vjp(U0, lam1, dt)
+                new += lam1 + dt * w
+                lam = new
+            del stages
+        self.geom.check_status()
+        return lam
+
+    def gradient(self, U0: torch.Tensor, steps: int):
+        """J, dJ/dU0 (device), far-field-state gradient per far face (host)."""
+        UN = self.forward(U0, steps)
+        J, dJ = self.functional(UN)
+        lam0 = self.backward(dJ)
+        return J, lam0, self.far_acc.cpu().numpy()
+
+
+class WallForceFunction(torch.autograd.Function):
+    """J(U0) = wall force after ``steps`` RK3 steps from U0, as a torch op whose
+    backward is the checkpointed discrete adjoint."""
+
+    @staticmethod
+    def forward(ctx, U0, adjoint: WallForceAdjoint, steps: int):
+        UN = adjoint.forward(U0.contiguous(), int(steps))
+        J, dJ = adjoint.functional(UN)
+        ctx.adjoint, ctx.dJ = adjoint, dJ
+        return torch.tensor(J, dtype=torch.float64, device=U0.device)
+
+    @staticmethod
+    def backward(ctx, grad_J):
+        lam0 = ctx.adjoint.backward(ctx.dJ)
+        return grad_J * lam0, None, None
+
+
+def conservative_jacobian_T(P: np.ndarray, lam: np.ndarray, gamma: float) -> np.ndarray:
+    """Per cell, (dU/dP)^T lambda for U = primitive_to_conservative(P)
+    (euler.py:8-17): the chain rule from an initial state given in
+    primitive variables (rows of P) to those variables."""
+    rho, u, v, p = P.T
+    l0, l1, l2, l3 = lam.T
+    out = np.column_stack((
+        l0 + l1 * u + l2 * v + l3 * 0.5 * (u * u + v * v),
+        l1 * rho + l3 * rho * u,
+        l2 * rho + l3 * rho * v,
+        l3 / (gamma - 1.0),
+    ))
+    return out

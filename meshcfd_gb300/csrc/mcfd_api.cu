@@ -577,6 +577,10 @@ int mcfd_geom_get_info(const mcfd_geom* h, mcfd_geom_info* info) {
 
 const double* mcfd_geom_primitive(const mcfd_geom* h) { return h ? h->ws.P : nullptr; }
 
+const double* mcfd_geom_stage_state(const mcfd_geom* h, int32_t k) {
+  return (h && k >= 0 && k < 4) ? h->ws.stage[k] : nullptr;
+}
+
 
 
 int mcfd_primitive(mcfd_geom* h, const mcfd_config* cfg, const double* U, double* P, void* stream) {
@@ -798,7 +802,7 @@ static int ensure_vjp(mcfd_geom* h) {
   const size_t s4 = 4 * (size_t)std::max(h->g.n_slots, 1) * sizeof(double);
   const size_t e4 = 4 * (size_t)std::max(h->g.n_gradient, 1) * sizeof(double);
   double** fields[] = {&h->vjp.P, &h->vjp.recon, &h->vjp.slot_bar, &h->vjp.pbar, &h->vjp.ent_bar, &h->vjp.partials};
-  const size_t sizes[] = {c4, s4, s4, c4, e4, 608 * sizeof(double)};
+  const size_t sizes[] = {c4, s4, s4, c4, e4, 616 * sizeof(double)};  // 608 block sums + the total
   for (int k = 0; k < 6; ++k) {
     if (cudaMalloc((void**)fields[k], sizes[k]) != cudaSuccess) return MCFD_E_CUDA;
     h->jvp_owned.push_back(*fields[k]);
@@ -824,8 +828,8 @@ int mcfd_wall_force(mcfd_geom* h, const mcfd_config* cfg, const double* U, doubl
   if (c) return c;
   if ((c = ensure_vjp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = launch_wall_force(h->g, *cfg, U, dir_x, dir_y, h->vjp, h->vjp.partials + 600, dJdU, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(J, h->vjp.partials + 600, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaError_t e = launch_wall_force(h->g, *cfg, U, dir_x, dir_y, h->vjp, h->vjp.partials + 608, dJdU, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(J, h->vjp.partials + 608, sizeof(double), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return rc(e);
 }

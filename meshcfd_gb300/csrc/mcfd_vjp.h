@@ -11,7 +11,7 @@ struct VjpWork {
   double* slot_bar = nullptr;  // face-state adjoints [slots][4]
   double* pbar = nullptr;      // primitive adjoints [C][4] (also per-cell scratch)
   double* ent_bar = nullptr;   // per gradient entry: share for the neighbour [E][4]
-  double* partials = nullptr;  // reduction scratch [608]
+  double* partials = nullptr;  // reduction scratch [608 block sums + 8]
 };
 
 cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U, const double* lambda,

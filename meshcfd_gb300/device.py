@@ -119,6 +119,7 @@ class DeviceGeometry:
         self.n_cells = int(info.n_cells)
         self.n_faces = int(info.n_faces)
         self.n_interior = int(info.n_interior)
+        self.n_far_field = int(d.n_far_field)
         self.areas = torch.as_tensor(keep["areas"], device=self.device)
         self._dt_min = torch.empty(1, dtype=torch.float64, device=self.device)
 

@@ -323,3 +323,68 @@ def smooth_primitive(n_cells, seed=0, amplitude=0.05):
 
 def states_from_primitive(primitive) -> tuple:
     return tuple(InitialState(*map(float, row)) for row in np.asarray(primitive))
+
+
+def ogrid_case(n_theta=1024, n_r=512, radius=0.5, half_width=10.0, growth=None, seed=2, jitter=0.1, mach=0.3):
+    """O-grid of n_theta x n_r quads around a cylinder of ``radius`` centred in
+    the square [-half_width, half_width]^2: radial lines from the circle to the
+    square, points spaced geometrically along them (ratio ``growth``, default
+    chosen so the first spacing is ~ the circumferential spacing at the wall),
+    interior points jittered by up to ``jitter`` of the local spacing (seeded).
+    Slip wall on the cylinder, far field (free stream at Mach ``mach`` along x,
+    rho = 1, p = 1/gamma... p = 1) on the square."""
+    rng = np.random.default_rng(seed)
+    theta = 2.0 * math.pi * np.arange(n_theta) / n_theta
+    c, s = np.cos(theta), np.sin(theta)
+    inner = radius * np.column_stack((c, s))
+    scale = half_width / np.maximum(np.abs(c), np.abs(s))
+    outer = scale[:, None] * np.column_stack((c, s))
+    if growth is None:
+        first = 2.0 * math.pi * radius / n_theta
+        span = float(np.min(scale)) - radius
+        lo, hi = 1.0 + 1e-9, 2.0
+        for _ in range(100):  # first spacing span*(g-1)/(g^n-1) = first
+            g = 0.5 * (lo + hi)
+            if span * (g - 1.0) / (g**n_r - 1.0) > first:
+                lo = g
+            else:
+                hi = g
+        growth = 0.5 * (lo + hi)
+    t = (growth ** np.arange(n_r + 1) - 1.0) / (growth**n_r - 1.0)
+    pts = inner[None, :, :] + t[:, None, None] * (outer - inner)[None, :, :]
+    if jitter:
+        dt = np.diff(t)
+        h_r = np.minimum(dt[:-1], dt[1:])[:, None] * np.linalg.norm(outer - inner, axis=1)[None, :]
+        h_t = 2.0 * math.pi * np.linalg.norm(pts[1:-1], axis=2) / n_theta
+        h = np.minimum(h_r, h_t)
+        pts[1:-1] += (rng.uniform(-jitter, jitter, size=(n_r - 1, n_theta, 2)) * h[:, :, None])
+    points = pts.reshape(-1, 2)
+    j, i = np.divmod(np.arange(n_theta * n_r), n_theta)
+    ip = (i + 1) % n_theta
+    quad = np.column_stack((j * n_theta + i, j * n_theta + ip, (j + 1) * n_theta + ip, (j + 1) * n_theta + i))
+    cells = CellArray(np.arange(0, 4 * len(quad) + 1, 4, dtype=np.int64), quad.ravel().astype(np.int64))
+    inner_ids = set(range(n_theta))
+
+    def classify(a, b):
+        ra = np.linalg.norm(a, axis=1)
+        ids = np.where(ra < 0.5 * (radius + half_width), 0, 1)
+        return ids, ("cylinder", "farfield")
+
+    mesh = build_faces(points, cells, classify)
+    del inner_ids
+    case = Case(name=f"ogrid{n_theta}x{n_r}", mesh=mesh)
+    gamma = case.numerics.gamma
+    u = mach * math.sqrt(gamma)
+    for cond in case.boundary_conditions:
+        if cond.patch_name == "cylinder":
+            cond.kind = "Wall"
+            cond.mechanical_condition = "Slip"
+        else:
+            cond.kind = "Far Field"
+            cond.values = {"density": 1.0, "velocity_x": u, "velocity_y": 0.0, "pressure": 1.0}
+    num = case.numerics
+    num.flux, num.reconstruction, num.limiter = "HLLC", "MUSCL linear", "Venkatakrishnan"
+    num.time_integration, num.cfl = "Explicit RK3", 0.8
+    num.time_step_mode, num.end_time, num.residual_tolerance = "Global fixed", 1.0e30, 1e-300
+    P = np.tile((1.0, u, 0.0, 1.0), (len(mesh.cells), 1))
+    return case, P
