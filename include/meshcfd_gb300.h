@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define MCFD_ABI_VERSION 1
+#define MCFD_ABI_VERSION 2
 
 /* ---- return codes (host-side failures) ---- */
 #define MCFD_OK 0
@@ -132,6 +132,15 @@ typedef struct mcfd_geom_desc {
   const int64_t* limiter_cells;
   const double* limiter_dx;
   const double* limiter_dy;
+  /* two-ring stencil of MUSCL parabolic (_parabolic_stencil,
+   * solver.py:2241-2291), entries grouped by source in the reference's
+   * order; n_parabolic = 0 when the geometry was built without it (the
+   * reference then reconstructs linearly, solver.py:2327-2329). */
+  int64_t n_parabolic;
+  const int64_t* parabolic_sources;
+  const int64_t* parabolic_neighbours;
+  const double* parabolic_dx;
+  const double* parabolic_dy;
 } mcfd_geom_desc;
 
 typedef struct mcfd_geom mcfd_geom; /* opaque device geometry + workspace */
@@ -197,6 +206,15 @@ int mcfd_time_steps(mcfd_geom* geom, const mcfd_config* cfg, const double* P,
  */
 int mcfd_explicit_step(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, double* U,
                        const double* dt, int32_t dt_per_cell, void* stream);
+
+/* The reconstruction fields of the reference for primitive P [n_cells][4]:
+ * MUSCL linear -> _limited_gradients (solver.py:2294-2319): gradients
+ * [n_cells][4][2] and factors [n_cells][4]; MUSCL parabolic ->
+ * _parabolic_reconstruction (solver.py:2322-2415): also curvature
+ * [n_cells][4][3] (xx, xy, yy; may be NULL).  Device arrays; exact
+ * arithmetic whatever cfg->mode. */
+int mcfd_reconstruction(mcfd_geom* geom, const mcfd_config* cfg, const double* P, double* gradients,
+                        double* curvature, double* factors, void* stream);
 
 /* Device pointer to the handle's primitive buffer [n_cells][4] (valid after
  * mcfd_primitive / mcfd_residual / mcfd_explicit_step on the same handle). */

@@ -54,6 +54,8 @@ class GeomDesc(C.Structure):
         ("n_gradient", c_i64), ("gradient_sources", P_i64), ("gradient_neighbours", P_i64),
         ("gradient_coefficients_x", P_dbl), ("gradient_coefficients_y", P_dbl),
         ("n_limiter", c_i64), ("limiter_cells", P_i64), ("limiter_dx", P_dbl), ("limiter_dy", P_dbl),
+        ("n_parabolic", c_i64), ("parabolic_sources", P_i64), ("parabolic_neighbours", P_i64),
+        ("parabolic_dx", P_dbl), ("parabolic_dy", P_dbl),
     ]
 
 
@@ -64,6 +66,8 @@ class GeomInfo(C.Structure):
         ("n_limiter", c_i64), ("device_bytes", c_i64),
     ]
 
+
+ABI_VERSION = 2  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
 
 # name -> (restype, argtypes); every symbol include/meshcfd_gb300.h declares.
 SIGNATURES = {
@@ -78,6 +82,7 @@ SIGNATURES = {
     "mcfd_explicit_step": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp]),
     "mcfd_geom_primitive": (c_vp, [c_vp]),
     "mcfd_geom_stage_state": (c_vp, [c_vp, C.c_int32]),
+    "mcfd_reconstruction": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
     "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),
@@ -120,6 +125,8 @@ class Native:
             fn.restype = res
             fn.argtypes = args
             setattr(self, name, fn)
+        if self.mcfd_abi_version() != ABI_VERSION:
+            raise NativeError(f"{path}: ABI version {self.mcfd_abi_version()}, expected {ABI_VERSION} (rebuild)")
 
     def check(self, rc: int, what: str) -> None:
         if rc != 0:

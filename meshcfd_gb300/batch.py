@@ -136,6 +136,9 @@ def concatenate(geometries) -> tuple[Geometry, BatchLayout]:
         gradient_dx=cat("gradient_dx"), gradient_dy=cat("gradient_dy"),
         gradient_coefficients_x=cat("gradient_coefficients_x"), gradient_coefficients_y=cat("gradient_coefficients_y"),
         limiter_cells=lim_cells, limiter_dx=lim_dx, limiter_dy=lim_dy,
+        parabolic_sources=cat("parabolic_sources", "cell").astype(np.int64),
+        parabolic_neighbours=cat("parabolic_neighbours", "cell").astype(np.int64),
+        parabolic_dx=cat("parabolic_dx"), parabolic_dy=cat("parabolic_dy"),
     )
     return geo, BatchLayout(cells.astype(np.int64), faces.astype(np.int64), len(geometries))
 

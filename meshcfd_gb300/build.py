@@ -30,6 +30,7 @@ UNITS = [
     ("mcfd_implicit.cu", ["-fmad=false"]),
     ("mcfd_jvp.cu", ["-fmad=false"]),
     ("mcfd_vjp.cu", ["-fmad=false"]),
+    ("mcfd_parabolic.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),
     ("mcfd_noalloc.cu", ["-fmad=false"]),
 ]

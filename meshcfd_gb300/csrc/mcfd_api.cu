@@ -74,7 +74,6 @@ static int check_cfg(const mcfd_config* cfg) {
   if (!cfg) return MCFD_E_ARG;
   if (cfg->flux < 0 || cfg->flux > 2) return MCFD_E_ARG;
   if (cfg->limiter < 0 || cfg->limiter > 3) return MCFD_E_ARG;
-  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC) return MCFD_E_UNSUPPORTED;
   if (cfg->reconstruction < 0 || cfg->reconstruction > 2) return MCFD_E_ARG;
   if (!(cfg->gamma > 1.0)) return MCFD_E_ARG;
   if (cfg->mode < MCFD_MODE_EXACT || cfg->mode > MCFD_MODE_FMA) return MCFD_E_ARG;
@@ -117,6 +116,8 @@ static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgra
   cudaError_t e = cudaSuccess;
   if (cfg.reconstruction == MCFD_RECON_MUSCL_LINEAR)
     e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return MCFD_DISPATCH(cfg, launch_reconstruct(h->g, cfg, h->ws.P, h->ws.recon, s)); });
+  else if (cfg.reconstruction == MCFD_RECON_MUSCL_PARABOLIC)
+    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return launch_reconstruct_parabolic(h->g, cfg, h->ws.P, h->ws.recon, s); });
   if (e == cudaSuccess)
     e = timed(h, MCFD_PROF_FLUX, s, [&] { return MCFD_DISPATCH(cfg, launch_flux(h->g, cfg, h->ws.P, h->ws.recon, h->ws.flux, s)); });
   if (e == cudaSuccess)
@@ -184,6 +185,12 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
       return MCFD_E_GEOMETRY;
   for (int64_t s = 0; s < NL; ++s)
     if (!in_range(d->limiter_cells[s], C)) return MCFD_E_GEOMETRY;
+  const int64_t NE = d->n_parabolic;
+  if (NE < 0 || NE > kMaxIndex) return MCFD_E_ARG;
+  if (NE && (!d->parabolic_sources || !d->parabolic_neighbours || !d->parabolic_dx || !d->parabolic_dy))
+    return MCFD_E_ARG;
+  for (int64_t e = 0; e < NE; ++e)
+    if (!in_range(d->parabolic_sources[e], C) || !in_range(d->parabolic_neighbours[e], C)) return MCFD_E_GEOMETRY;
   for (int64_t c = 0; c < C; ++c)
     if (!(d->areas[c] > 0.0)) return MCFD_E_GEOMETRY;
 
@@ -347,6 +354,20 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
       lim_d[2 * j + 1] = d->limiter_dy[s];
     }
   }
+  // ---- two-ring stencil entries grouped by source, reference order kept
+  std::vector<int> par_ptr, par_nb(NE);
+  std::vector<double> par_d(2 * NE);
+  {
+    key.resize(NE);
+    for (int64_t e = 0; e < NE; ++e) key[e] = (int)d->parabolic_sources[e];
+    group_by(key, (int)C, par_ptr, order);
+    for (int64_t j = 0; j < NE; ++j) {
+      int e = order[j];
+      par_nb[j] = (int)d->parabolic_neighbours[e];
+      par_d[2 * j] = d->parabolic_dx[e];
+      par_d[2 * j + 1] = d->parabolic_dy[e];
+    }
+  }
   // ---- time-step entries (solver.py:4206-4226)
   std::vector<int> dt_ptr, dt_info;
   std::vector<double> dt_n, dt_len;
@@ -392,6 +413,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
          o_grad_cx = A.take(bytes_d(NG)), o_grad_cy = A.take(bytes_d(NG)), o_grad_twin = A.take(bytes_i(NG));
   size_t o_lim_ptr = A.take(bytes_i(C + 1)), o_lim_slot = A.take(bytes_i(NL)),
          o_lim_d = A.take(bytes_d(2 * NL));
+  size_t o_par_ptr = A.take(bytes_i(C + 1)), o_par_nb = A.take(bytes_i(NE)), o_par_d = A.take(bytes_d(2 * NE));
   size_t o_lslot = A.take(bytes_i(n_flux)), o_rslot = A.take(bytes_i(n_flux)),
          o_lcell = A.take(bytes_i(n_flux)), o_rcell = A.take(bytes_i(n_flux)),
          o_normal = A.take(bytes_d(2 * n_flux)), o_flen = A.take(bytes_d(n_flux)), o_wallv = A.take(bytes_d(2 * NW)),
@@ -431,6 +453,9 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   put(o_lim_ptr, lim_ptr.data(), bytes_i(C + 1));
   put(o_lim_slot, lim_slot.data(), bytes_i(NL));
   put(o_lim_d, lim_d.data(), bytes_d(2 * NL));
+  put(o_par_ptr, par_ptr.data(), bytes_i(C + 1));
+  put(o_par_nb, par_nb.data(), bytes_i(NE));
+  put(o_par_d, par_d.data(), bytes_d(2 * NE));
   put(o_lslot, lslot.data(), bytes_i(n_flux));
   put(o_rslot, rslot.data(), bytes_i(n_flux));
   put(o_lcell, lcell.data(), bytes_i(n_flux));
@@ -480,6 +505,10 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   g.lim_ptr = AT(const int*, o_lim_ptr);
   g.lim_slot = AT(const int*, o_lim_slot);
   g.lim_d = AT(const double2*, o_lim_d);
+  g.n_parabolic = (int)NE;
+  g.par_ptr = AT(const int*, o_par_ptr);
+  g.par_nb = AT(const int*, o_par_nb);
+  g.par_d = AT(const double2*, o_par_d);
   g.ff_lslot = AT(const int*, o_lslot);
   g.ff_rslot = AT(const int*, o_rslot);
   g.ff_lcell = AT(const int*, o_lcell);
@@ -576,6 +605,17 @@ int mcfd_geom_get_info(const mcfd_geom* h, mcfd_geom_info* info) {
 }
 
 const double* mcfd_geom_primitive(const mcfd_geom* h) { return h ? h->ws.P : nullptr; }
+
+int mcfd_reconstruction(mcfd_geom* h, const mcfd_config* cfg, const double* P, double* gradients,
+                        double* curvature, double* factors, void* stream) {
+  if (!h || !P || !gradients || !factors) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if (cfg->reconstruction == MCFD_RECON_FIRST_ORDER) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_RECONSTRUCT, s,
+                  [&] { return launch_reconstruction_fields(h->g, *cfg, P, gradients, curvature, factors, s); }));
+}
 
 const double* mcfd_geom_stage_state(const mcfd_geom* h, int32_t k) {
   return (h && k >= 0 && k < 4) ? h->ws.stage[k] : nullptr;
@@ -815,6 +855,7 @@ int mcfd_vjp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   if (!h || !U || !lambda || !U_bar) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC) return MCFD_E_UNSUPPORTED;
   if (cfg->reconstruction != MCFD_RECON_FIRST_ORDER && !h->g.has_twins) return MCFD_E_UNSUPPORTED;
   if ((c = ensure_vjp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
@@ -838,6 +879,7 @@ int mcfd_jvp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   if (!h || !U || !dU || !dR) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC) return MCFD_E_UNSUPPORTED;
   if ((c = ensure_jvp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return launch_jvp(h->g, *cfg, U, dU, h->jvp, dR, s); }));

@@ -44,6 +44,11 @@ struct DevGeom {
   const int* lim_ptr;
   const int* lim_slot;
   const double2* lim_d;
+  // MUSCL-parabolic two-ring stencil grouped by source, reference order
+  int n_parabolic;
+  const int* par_ptr;
+  const int* par_nb;
+  const double2* par_d;
   // flux faces
   const int* ff_lslot;  // recon slot of the interior-side state
   const int* ff_rslot;  // recon slot of the other side (interior/periodic), else -1
@@ -127,6 +132,12 @@ long long launch_count();
 void count_launch(int n = 1);
 cudaError_t launch_case_time_steps(int n_cells, int n_cases, const int* offsets, double* dt_case,
                                    double* dt_cells, cudaStream_t s);
+// MUSCL parabolic and the reference's reconstruction fields (mcfd_parabolic.cu;
+// exact arithmetic in every mode)
+cudaError_t launch_reconstruct_parabolic(const DevGeom& g, const mcfd_config& cfg, const double* P, double* recon,
+                                         cudaStream_t s);
+cudaError_t launch_reconstruction_fields(const DevGeom& g, const mcfd_config& cfg, const double* P, double* grad,
+                                         double* curv, double* fac, cudaStream_t s);
 // reduction kernels of the sum of squares
 __global__ void k_sumsq_partial(int n, const double* __restrict__ R, double* __restrict__ partials);
 __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums);

@@ -29,7 +29,8 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
 
     ``mode``: "exact" (reference operation order, bit-exact), "fast" (exact
     arithmetic, limiter minimum through the smallest ratio) or "fma" (shared
-    reciprocals and FMA; outside the 1e-12 bar on fine meshes)."""
+    reciprocals and FMA; outside the 1e-12 bar on fine meshes).  MUSCL
+    parabolic reconstructs with exact arithmetic in every mode."""
     if settings.viscosity_model != "Inviscid":
         raise NotImplementedError("viscous terms are not implemented by the GPU residual path")
     if settings.turbulence_model != "None":
@@ -40,8 +41,6 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
         limiter = LIMITER_CODES[settings.limiter]
     except KeyError as error:
         raise SolverError(f"Unsupported scheme {error}") from error
-    if recon == 2:
-        raise NotImplementedError("MUSCL parabolic is not implemented by the GPU residual path")
     cfg = _lib.Config()
     cfg.flux, cfg.reconstruction, cfg.limiter, cfg.mode = flux, recon, limiter, MODES[mode]
     cfg.gamma = float(settings.gamma)
@@ -106,6 +105,13 @@ class DeviceGeometry:
         d.limiter_cells, d.n_limiter = a("limiter_cells", np.int64)
         d.limiter_dx, _ = a("limiter_dx", np.float64)
         d.limiter_dy, _ = a("limiter_dy", np.float64)
+        empty_i, empty_d = np.empty(0, dtype=np.int64), np.empty(0)
+        d.parabolic_sources, d.n_parabolic = a("parabolic_sources", np.int64,
+                                               src=getattr(geometry, "parabolic_sources", empty_i))
+        d.parabolic_neighbours, _ = a("parabolic_neighbours", np.int64,
+                                      src=getattr(geometry, "parabolic_neighbours", empty_i))
+        d.parabolic_dx, _ = a("parabolic_dx", np.float64, src=getattr(geometry, "parabolic_dx", empty_d))
+        d.parabolic_dy, _ = a("parabolic_dy", np.float64, src=getattr(geometry, "parabolic_dy", empty_d))
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             rc = self.lib.mcfd_geom_create(C.byref(d), C.byref(handle))
@@ -160,6 +166,18 @@ class DeviceGeometry:
         self.lib.check(self.lib.mcfd_residual(self.handle, C.byref(cfg), U.data_ptr(), R.data_ptr(), _stream_ptr()),
                        "mcfd_residual")
         return R
+
+    def reconstruction(self, P: torch.Tensor, cfg):
+        """(gradients (C,4,2), curvature (C,4,3) or None, factors (C,4)) of
+        _limited_gradients / _parabolic_reconstruction (solver.py:2294-2415)."""
+        _check_state(P, self.n_cells, "P")
+        grad = torch.empty(self.n_cells, 4, 2, dtype=torch.float64, device=self.device)
+        fac = torch.empty(self.n_cells, 4, dtype=torch.float64, device=self.device)
+        curv = torch.empty(self.n_cells, 4, 3, dtype=torch.float64, device=self.device) if cfg.reconstruction == 2 else None
+        self.lib.check(self.lib.mcfd_reconstruction(self.handle, C.byref(cfg), P.data_ptr(), grad.data_ptr(),
+                                                    curv.data_ptr() if curv is not None else None, fac.data_ptr(),
+                                                    _stream_ptr()), "mcfd_reconstruction")
+        return grad, curv, fac
 
     def primitive_buffer(self) -> torch.Tensor:
         """The handle's primitive buffer as a tensor view (valid after a

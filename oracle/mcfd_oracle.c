@@ -13,6 +13,7 @@
  * steps produced by the reference itself, and the CPU tests check this file
  * against them bit for bit.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -54,6 +55,9 @@ typedef struct {
   int64_t n_limiter;
   const int64_t* limiter_cells;
   const double *limiter_dx, *limiter_dy;
+  int64_t n_parabolic; /* two-ring stencil entries, source-major (solver.py:2241-2291) */
+  const int64_t *parabolic_sources, *parabolic_neighbours;
+  const double *parabolic_dx, *parabolic_dy;
 } orc_geom;
 
 typedef struct {
@@ -333,13 +337,247 @@ static void kernel_hllc(const double* left, const double* right, const double* n
 
 /* ------------------------------------------------------------ solver.py */
 
-/* _reconstruct (solver.py:2418-2434), one row */
-static void reconstruct(const double* P, const double* grad, const double* fac, int64_t c, double ox,
-                        double oy, double* out) {
+/* _reconstruct (solver.py:2418-2434), one row; curv (C,4,3) or NULL */
+static void reconstruct(const double* P, const double* grad, const double* fac, const double* curv, int64_t c,
+                        double ox, double oy, double* out) {
   for (int v = 0; v < 4; ++v) {
     double inc = grad[8 * c + 2 * v] * ox + grad[8 * c + 2 * v + 1] * oy;
+    if (curv) {
+      const double* k = curv + 12 * c + 3 * v;
+      inc += 0.5 * k[0] * (ox * ox) + k[1] * (ox * oy) + 0.5 * k[2] * (oy * oy);
+    }
     out[v] = P[4 * c + v] + fac[4 * c + v] * inc;
   }
+}
+
+/* ---------------------------------------------- _parabolic_reconstruction */
+
+/* Gaussian elimination with partial pivoting (row interchange to the first
+ * largest |a_ik|, unit lower factor): the factorisation LAPACK's gesv uses
+ * behind np.linalg.solve, in plain right-looking order.  Returns 0 on a zero
+ * or non-finite pivot. */
+static int lu5(double A[5][5], int piv[5]) {
+  for (int k = 0; k < 5; ++k) {
+    int p = k;
+    double best = fabs(A[k][k]);
+    for (int i = k + 1; i < 5; ++i)
+      if (fabs(A[i][k]) > best) {
+        best = fabs(A[i][k]);
+        p = i;
+      }
+    piv[k] = p;
+    if (!(best > 0.0) || !isfinite(best)) return 0;
+    if (p != k)
+      for (int j = 0; j < 5; ++j) {
+        double t = A[k][j];
+        A[k][j] = A[p][j];
+        A[p][j] = t;
+      }
+    for (int i = k + 1; i < 5; ++i) {
+      double l = A[i][k] / A[k][k];
+      A[i][k] = l;
+      for (int j = k + 1; j < 5; ++j) A[i][j] = A[i][j] - l * A[k][j];
+    }
+  }
+  return 1;
+}
+
+/* b: [5][m] right-hand sides, overwritten with the solution. */
+static void lu5_solve(double LU[5][5], const int piv[5], double* b, int m) {
+  for (int k = 0; k < 5; ++k)
+    if (piv[k] != k)
+      for (int v = 0; v < m; ++v) {
+        double t = b[k * m + v];
+        b[k * m + v] = b[piv[k] * m + v];
+        b[piv[k] * m + v] = t;
+      }
+  for (int i = 1; i < 5; ++i)
+    for (int j = 0; j < i; ++j)
+      for (int v = 0; v < m; ++v) b[i * m + v] = b[i * m + v] - LU[i][j] * b[j * m + v];
+  for (int i = 4; i >= 0; --i) {
+    for (int j = i + 1; j < 5; ++j)
+      for (int v = 0; v < m; ++v) b[i * m + v] = b[i * m + v] - LU[i][j] * b[j * m + v];
+    for (int v = 0; v < m; ++v) b[i * m + v] = b[i * m + v] / LU[i][i];
+  }
+}
+
+/* Singular values by one-sided Jacobi rotations (Hestenes' method), then
+ * the rank rule of np.linalg.matrix_rank: count of s > max(s) * 5 * eps. */
+static int jacobi_rank5(const double M[5][5]) {
+  double A[5][5];
+  memcpy(A, M, sizeof(A));
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    int rotated = 0;
+    for (int p = 0; p < 4; ++p)
+      for (int q = p + 1; q < 5; ++q) {
+        double alpha = 0.0, beta = 0.0, gam = 0.0;
+        for (int i = 0; i < 5; ++i) {
+          alpha += A[i][p] * A[i][p];
+          beta += A[i][q] * A[i][q];
+          gam += A[i][p] * A[i][q];
+        }
+        if (!(fabs(gam) > 1e-15 * sqrt(alpha * beta))) continue;
+        rotated = 1;
+        double zeta = (beta - alpha) / (2.0 * gam);
+        double t = fabs(zeta) > 1e150 ? 0.5 / zeta
+                                      : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+        for (int i = 0; i < 5; ++i) {
+          double ap = A[i][p], aq = A[i][q];
+          A[i][p] = c * ap - sn * aq;
+          A[i][q] = sn * ap + c * aq;
+        }
+      }
+    if (!rotated) break;
+  }
+  double sv[5], smax = 0.0;
+  for (int j = 0; j < 5; ++j) {
+    double n2 = 0.0;
+    for (int i = 0; i < 5; ++i) n2 += A[i][j] * A[i][j];
+    sv[j] = sqrt(n2);
+    if (sv[j] > smax) smax = sv[j];
+  }
+  int rank = 0;
+  for (int j = 0; j < 5; ++j)
+    if (sv[j] > smax * 5.0 * DBL_EPSILON) ++rank;
+  return rank;
+}
+
+/* np.linalg.matrix_rank(M) == 5, decided without an SVD where the LU shows a
+ * Frobenius condition number kappa_F = |M|_F |M^-1|_F below 1e12: then
+ * s_min / s_max >= 1 / kappa_F is far above the 5 eps threshold.  Otherwise
+ * (singular pivot, ill-conditioned) the Jacobi singular values decide. */
+static int full_rank5(const double M[5][5], double LU[5][5], const int piv[5], int lu_ok) {
+  if (lu_ok) {
+    double X[25];
+    for (int i = 0; i < 25; ++i) X[i] = (i % 6 == 0) ? 1.0 : 0.0;
+    lu5_solve(LU, piv, X, 5);
+    double na = 0.0, ni = 0.0;
+    for (int i = 0; i < 5; ++i)
+      for (int j = 0; j < 5; ++j) {
+        na += M[i][j] * M[i][j];
+        ni += X[5 * i + j] * X[5 * i + j];
+      }
+    double kappa = sqrt(na) * sqrt(ni);
+    if (isfinite(kappa) && kappa < 1e12) return 1;
+  }
+  return jacobi_rank5(M) == 5;
+}
+
+/* _parabolic_reconstruction (solver.py:2322-2415): linear gradients and
+ * factors (_limited_gradients), then for full-rank cells the weighted
+ * least-squares quadratic fit over the two-ring stencil (np.add.at in entry
+ * order, np.linalg.solve), and the limiter applied to the quadratic
+ * increment with the two-ring local extrema. */
+int orc_parabolic_reconstruction(const orc_geom* g, const double* P, int code, double* grad, double* curv,
+                                 double* fac) {
+  int64_t C = g->n_cells, NE = g->n_parabolic;
+  if (g->n_gradient) orc_linear_gradients_and_factors(g, P, code, grad, fac);
+  else {
+    memset(grad, 0, sizeof(double) * 8 * C);
+    for (int64_t i = 0; i < 4 * C; ++i) fac[i] = 1.0;
+  }
+  memset(curv, 0, sizeof(double) * 12 * C);
+  if (NE == 0) return 0;
+  double* scales = (double*)calloc(C, sizeof(double));
+  double* M = (double*)calloc(25 * C, sizeof(double));
+  double* B = (double*)calloc(20 * C, sizeof(double));
+  double* lo = (double*)malloc(sizeof(double) * 4 * C);
+  double* hi = (double*)malloc(sizeof(double) * 4 * C);
+  double* pf = (double*)malloc(sizeof(double) * 4 * C);
+  unsigned char* full = (unsigned char*)calloc(C, 1);
+  for (int64_t e = 0; e < NE; ++e) {
+    int64_t s = g->parabolic_sources[e];
+    double a = fabs(g->parabolic_dx[e]), b = fabs(g->parabolic_dy[e]);
+    double m = a >= b ? a : b;
+    if (m > scales[s]) scales[s] = m;
+  }
+  for (int64_t c = 0; c < C; ++c)
+    if (!(scales[c] >= 1e-300)) scales[c] = 1e-300;
+  for (int64_t e = 0; e < NE; ++e) {
+    int64_t s = g->parabolic_sources[e], nb = g->parabolic_neighbours[e];
+    double nx = g->parabolic_dx[e] / scales[s], ny = g->parabolic_dy[e] / scales[s];
+    double d[5] = {nx, ny, 0.5 * (nx * nx), nx * ny, 0.5 * (ny * ny)};
+    double r2 = nx * nx + ny * ny;
+    double w = 1.0 / (r2 >= 1e-300 ? r2 : 1e-300);
+    double diff[4];
+    for (int v = 0; v < 4; ++v) diff[v] = P[4 * nb + v] - P[4 * s + v];
+    for (int i = 0; i < 5; ++i) {
+      double wi = w * d[i];
+      for (int j = 0; j < 5; ++j) M[25 * s + 5 * i + j] += wi * d[j];
+      for (int v = 0; v < 4; ++v) B[20 * s + 4 * i + v] += wi * diff[v];
+    }
+  }
+  for (int64_t c = 0; c < C; ++c) {
+    double A[5][5], LU[5][5];
+    int piv[5];
+    for (int i = 0; i < 5; ++i)
+      for (int j = 0; j < 5; ++j) A[i][j] = LU[i][j] = M[25 * c + 5 * i + j];
+    int ok = lu5(LU, piv);
+    if (!full_rank5(A, LU, piv, ok)) continue;
+    full[c] = 1;
+    double x[20];
+    memcpy(x, B + 20 * c, sizeof(x));
+    lu5_solve(LU, piv, x, 4);
+    double sc = scales[c], sc2 = sc * sc;
+    for (int v = 0; v < 4; ++v) {
+      grad[8 * c + 2 * v] = x[0 * 4 + v] / sc;
+      grad[8 * c + 2 * v + 1] = x[1 * 4 + v] / sc;
+      curv[12 * c + 3 * v] = x[2 * 4 + v] / sc2;
+      curv[12 * c + 3 * v + 1] = x[3 * 4 + v] / sc2;
+      curv[12 * c + 3 * v + 2] = x[4 * 4 + v] / sc2;
+    }
+  }
+  memcpy(lo, P, sizeof(double) * 4 * C);
+  memcpy(hi, P, sizeof(double) * 4 * C);
+  for (int64_t e = 0; e < NE; ++e) {
+    int64_t s = g->parabolic_sources[e], nb = g->parabolic_neighbours[e];
+    for (int v = 0; v < 4; ++v) {
+      double q = P[4 * nb + v];
+      if (q < lo[4 * s + v]) lo[4 * s + v] = q;
+      if (q > hi[4 * s + v]) hi[4 * s + v] = q;
+    }
+  }
+  for (int64_t i = 0; i < 4 * C; ++i) pf[i] = 1.0;
+  for (int64_t e = 0; e < g->n_limiter; ++e) {
+    int64_t c = g->limiter_cells[e];
+    double dx = g->limiter_dx[e], dy = g->limiter_dy[e];
+    for (int v = 0; v < 4; ++v) {
+      const double* k = curv + 12 * c + 3 * v;
+      double inc = grad[8 * c + 2 * v] * dx + grad[8 * c + 2 * v + 1] * dy + 0.5 * k[0] * (dx * dx) +
+                   k[1] * (dx * dy) + 0.5 * k[2] * (dy * dy);
+      double cv = P[4 * c + v], m = fabs(cv);
+      double tol = 1e-14 * (m > 1.0 ? m : 1.0);
+      double ratio = 1.0;
+      if (inc > tol) ratio = (hi[4 * c + v] - cv) / inc;
+      else if (inc < -tol) ratio = (lo[4 * c + v] - cv) / inc;
+      ratio = ratio >= 0.0 ? ratio : 0.0;
+      double f;
+      if (code <= 1) f = ratio < 1.0 ? ratio : 1.0;
+      else if (code == 2) {
+        if (ratio > 0.0) {
+          double q = 2.0 * ratio / (1.0 + ratio);
+          f = 1.0 < q ? 1.0 : q;
+        } else f = 0.0;
+      } else {
+        double eps = 1e-12;
+        f = (ratio * ratio + 2.0 * ratio + eps) / (ratio * ratio + ratio + 2.0 + eps);
+        f = f < 1.0 ? f : 1.0;
+      }
+      if (f < pf[4 * c + v]) pf[4 * c + v] = f;
+    }
+  }
+  for (int64_t c = 0; c < C; ++c)
+    if (full[c])
+      for (int v = 0; v < 4; ++v) fac[4 * c + v] = pf[4 * c + v];
+  free(scales);
+  free(M);
+  free(B);
+  free(lo);
+  free(hi);
+  free(pf);
+  free(full);
+  return 0;
 }
 
 /* _far_field_boundary_states (solver.py:4350-4409), one row */
@@ -418,9 +656,13 @@ int orc_residual(const orc_geom* g, const orc_settings* s, const double* U, doub
   double* P = (double*)malloc(sizeof(double) * 4 * C);
   double* grad = (double*)calloc(8 * C, sizeof(double));
   double* fac = (double*)malloc(sizeof(double) * 4 * C);
+  double* curv = NULL;
   status |= orc_conservative_to_primitive(C, U, gamma, P);
   if (status) goto done;
-  if (s->reconstruction == 1 && g->n_gradient) {
+  if (s->reconstruction == 2) {
+    curv = (double*)calloc(12 * C, sizeof(double));
+    orc_parabolic_reconstruction(g, P, s->limiter, grad, curv, fac);
+  } else if (s->reconstruction == 1 && g->n_gradient) {
     orc_linear_gradients_and_factors(g, P, s->limiter, grad, fac);
   } else {
     for (int64_t i = 0; i < 4 * C; ++i) fac[i] = 1.0;
@@ -434,9 +676,9 @@ int orc_residual(const orc_geom* g, const orc_settings* s, const double* U, doub
       const double* n = g->face_normals + 2 * f;
       const double* oo = g->interior_owner_offsets + 2 * i;
       const double* no = g->interior_neighbour_offsets + 2 * i;
-      reconstruct(P, grad, fac, o, oo[0], oo[1], L);
-      reconstruct(P, grad, fac, nb, no[0], no[1], Rt);
-      if (s->flux == 1) kernel_hllc(L, Rt, n, gamma, flux + 4 * i);
+      reconstruct(P, grad, fac, curv, o, oo[0], oo[1], L);
+      reconstruct(P, grad, fac, curv, nb, no[0], no[1], Rt);
+      if (s->flux == 1 && !curv) kernel_hllc(L, Rt, n, gamma, flux + 4 * i);
       else status |= numerical_flux(s->flux, L, Rt, n, gamma, flux + 4 * i);
     }
     orc_csr D;
@@ -459,9 +701,9 @@ int orc_residual(const orc_geom* g, const orc_settings* s, const double* U, doub
       int64_t fa = g->periodic_faces_a[i], fb = g->periodic_faces_b[i];
       int64_t oa = g->owners[fa], ob = g->owners[fb];
       double L[4], Rt[4], fl[4];
-      reconstruct(P, grad, fac, oa, g->face_centers[2 * fa] - g->centers[2 * oa],
+      reconstruct(P, grad, fac, curv, oa, g->face_centers[2 * fa] - g->centers[2 * oa],
                   g->face_centers[2 * fa + 1] - g->centers[2 * oa + 1], L);
-      reconstruct(P, grad, fac, ob, g->face_centers[2 * fb] - g->centers[2 * ob],
+      reconstruct(P, grad, fac, curv, ob, g->face_centers[2 * fb] - g->centers[2 * ob],
                   g->face_centers[2 * fb + 1] - g->centers[2 * ob + 1], Rt);
       status |= numerical_flux(s->flux, L, Rt, g->face_normals + 2 * fa, gamma, fl);
       for (int v = 0; v < 4; ++v) integ[4 * i + v] = fl[v] * g->face_lengths[fa];
@@ -487,7 +729,7 @@ int orc_residual(const orc_geom* g, const orc_settings* s, const double* U, doub
       int64_t f = groups[k].faces[i], o = g->owners[f];
       const double* nrm = g->face_normals + 2 * f;
       double in[4], ext[4], fl[4];
-      reconstruct(P, grad, fac, o, g->face_centers[2 * f] - g->centers[2 * o],
+      reconstruct(P, grad, fac, curv, o, g->face_centers[2 * f] - g->centers[2 * o],
                   g->face_centers[2 * f + 1] - g->centers[2 * o + 1], in);
       memcpy(ext, in, sizeof(ext));
       if (k == 0) {
@@ -527,6 +769,7 @@ done:
   free(P);
   free(grad);
   free(fac);
+  free(curv);
   return status;
 }
 

@@ -53,6 +53,8 @@ class OrcGeom(C.Structure):
         ("n_gradient", C.c_int64), ("gradient_sources", P64), ("gradient_neighbours", P64),
         ("gradient_cx", PD), ("gradient_cy", PD),
         ("n_limiter", C.c_int64), ("limiter_cells", P64), ("limiter_dx", PD), ("limiter_dy", PD),
+        ("n_parabolic", C.c_int64), ("parabolic_sources", P64), ("parabolic_neighbours", P64),
+        ("parabolic_dx", PD), ("parabolic_dy", PD),
     ]
 
 
@@ -84,6 +86,7 @@ def lib():
         _lib.orc_conservative_to_primitive.argtypes = [C.c_int64, PD, C.c_double, PD]
         _lib.orc_primitive_to_conservative.argtypes = [C.c_int64, PD, C.c_double, PD]
         _lib.orc_linear_gradients_and_factors.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD]
+        _lib.orc_parabolic_reconstruction.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD, PD]
     return _lib
 
 
@@ -138,6 +141,9 @@ class Oracle:
             gradient_cx=arr("gradient_coefficients_x", np.float64), gradient_cy=arr("gradient_coefficients_y", np.float64),
             limiter_cells=arr("limiter_cells", np.int64), limiter_dx=arr("limiter_dx", np.float64),
             limiter_dy=arr("limiter_dy", np.float64),
+            parabolic_sources=arr("parabolic_sources", np.int64),
+            parabolic_neighbours=arr("parabolic_neighbours", np.int64),
+            parabolic_dx=arr("parabolic_dx", np.float64), parabolic_dy=arr("parabolic_dy", np.float64),
         )
         if getattr(g, "pressure_inlets", ()) or getattr(g, "mass_flow_inlets", ()) or getattr(g, "mass_flow_outlets", ()):
             raise NotImplementedError("oracle: pressure-inlet / mass-flow boundaries")
@@ -154,6 +160,7 @@ class Oracle:
         s.n_far = len(fields["far_faces"])
         s.n_gradient = len(fields["gradient_sources"])
         s.n_limiter = len(fields["limiter_cells"])
+        s.n_parabolic = 0 if fields["parabolic_sources"] is None else len(fields["parabolic_sources"])
         self.struct = s
         self._keep = keep
         self.n_cells = n_cells
@@ -197,6 +204,17 @@ class Oracle:
         lib().orc_linear_gradients_and_factors(C.byref(self.struct), P.ctypes.data_as(PD), LIMITER[limiter],
                                                grad.ctypes.data_as(PD), fac.ctypes.data_as(PD))
         return grad, fac
+
+    def parabolic_reconstruction(self, P, limiter):
+        """(gradients (C,4,2), curvature (C,4,3), factors (C,4)) of
+        _parabolic_reconstruction (solver.py:2322-2415)."""
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        grad = np.empty((len(P), 4, 2))
+        curv = np.empty((len(P), 4, 3))
+        fac = np.empty((len(P), 4))
+        lib().orc_parabolic_reconstruction(C.byref(self.struct), P.ctypes.data_as(PD), LIMITER[limiter],
+                                           grad.ctypes.data_as(PD), curv.ctypes.data_as(PD), fac.ctypes.data_as(PD))
+        return grad, curv, fac
 
     def stable_time_steps(self, P, num):
         P = np.ascontiguousarray(P, dtype=np.float64)

@@ -8,7 +8,11 @@ reference's outputs, so the tests can run without the reference:
 * residual_<case>.npz  — ``_residual`` for every flux x reconstruction x
   limiter combination, with and without a body force, plus
   ``_stable_time_steps``;
-* solve_<case>.npz     — final states of ``solve_case`` after N explicit steps.
+* solve_<case>.npz     — final states of ``solve_case`` after N explicit steps;
+* parabolic_<case>.npz — ``_residual`` with MUSCL parabolic reconstruction for
+  every flux x limiter (with and without a body force) and the outputs of
+  ``_parabolic_reconstruction`` per limiter, on a geometry built with the
+  two-ring stencil.
 """
 
 from __future__ import annotations
@@ -77,8 +81,11 @@ def mesh_arrays(case):
     }
 
 
-def geometry_arrays(geometry):
-    return {f"geom_{name}": np.asarray(getattr(geometry, name)) for name in GEOM_FIELDS}
+PARABOLIC_FIELDS = ("parabolic_sources", "parabolic_neighbours", "parabolic_dx", "parabolic_dy")
+
+
+def geometry_arrays(geometry, fields=GEOM_FIELDS):
+    return {f"geom_{name}": np.asarray(getattr(geometry, name)) for name in fields}
 
 
 def perturbed_primitive(n, seed):
@@ -122,6 +129,40 @@ def residual_fixture(name, case, ref):
     print(name, n, "cells,", len(keys), "residuals")
 
 
+def strip_case(nx=6, ny=2):
+    """Unsplit, unjittered 6x2 quads: every two-ring stencil has two rows of
+    cell centres, so every 5x5 normal matrix is rank deficient."""
+    mesh = box_mesh(nx, ny, 3.0, 1.0, split="none", jitter=0.0, seed=0)
+    case = channel_case()
+    case.mesh = mesh
+    return case
+
+
+def parabolic_fixture(name, case, ref):
+    case.numerics.reconstruction = "MUSCL parabolic"
+    rc = reference_case(case, ref)
+    rg = ref.solver._build_geometry(rc.mesh, rc)
+    out = {**mesh_arrays(case), **geometry_arrays(rg, GEOM_FIELDS + PARABOLIC_FIELDS)}
+    n = len(rg.areas)
+    P = perturbed_primitive(n, seed=1)
+    U = ref.euler.primitive_to_conservative(P, 1.4)
+    out["U"] = U
+    num = rc.numerics
+    keys = []
+    for flux, limiter, force in itertools.product(FLUXES, LIMITERS, (0, 1)):
+        num.flux, num.limiter = flux, limiter
+        num.acceleration_x, num.acceleration_y = (0.3, -0.2) if force else (0.0, 0.0)
+        key = f"R|{flux}|MUSCL parabolic|{limiter}|{force}"
+        out[key] = ref.solver._residual(U, rg, num)
+        keys.append(key)
+    Pp = ref.euler.conservative_to_primitive(U, 1.4)
+    for code, limiter in enumerate(LIMITERS):
+        g, k, f = ref.solver._parabolic_reconstruction(Pp, rg, limiter)
+        out[f"pgrad|{code}"], out[f"pcurv|{code}"], out[f"pfactors|{code}"] = g, k, f
+    np.savez_compressed(HERE / f"parabolic_{name}.npz", **out)
+    print("parabolic", name, n, "cells,", len(rg.parabolic_sources), "stencil entries,", len(keys), "residuals")
+
+
 def solve_fixture(name, case, primitive, settings, steps, ref):
     rc = reference_case(case, ref)
     for key, value in settings.items():
@@ -134,7 +175,8 @@ def solve_fixture(name, case, primitive, settings, steps, ref):
     states = tuple(ref.model.InitialState(*map(float, row)) for row in primitive)
     result = ref.solver.solve_case(rc, states)
     final = np.array([(s.density, s.velocity_x, s.velocity_y, s.pressure) for s in result.states])
-    out = {**mesh_arrays(case), **geometry_arrays(rg), "P0": primitive, "P_final": final,
+    fields = GEOM_FIELDS + (PARABOLIC_FIELDS if rc.numerics.reconstruction == "MUSCL parabolic" else ())
+    out = {**mesh_arrays(case), **geometry_arrays(rg, fields), "P0": primitive, "P_final": final,
            "time": np.array(result.time), "steps": np.array(result.steps)}
     for key, value in settings.items():
         out[f"set|{key}"] = np.array(value)
@@ -187,8 +229,10 @@ def implicit_fixture(name, case, primitive, settings, steps, ref):
     print("implicit", name, n, "cells,", result.steps, "steps, t =", result.time)
 
 
-def main():
+def main(only=None):
     ref = import_reference()
+    if only == "parabolic":
+        return parabolic_main(ref)
     riemann, riemann_p = riemann_case(16)
     residual_fixture("riemann16", riemann, ref)
     residual_fixture("periodic_mixed", periodic_case(8, 6, split="half", jitter=0.25, seed=2), ref)
@@ -225,5 +269,18 @@ def main():
                    "time_integration": "Explicit RK2", "cfl": 0.6, "acceleration_x": 0.2}, 8, ref)
 
 
+def parabolic_main(ref):
+    riemann, _ = riemann_case(16)
+    parabolic_fixture("riemann16", riemann, ref)
+    parabolic_fixture("periodic_mixed", periodic_case(8, 6, split="half", jitter=0.25, seed=2), ref)
+    parabolic_fixture("channel", channel_case(), ref)
+    parabolic_fixture("strip", strip_case(), ref)
+    vortex, _ = vortex_case(12, seed=0, jitter=0.15, split="half")
+    vp = vortex_primitive(cell_centroids(vortex.mesh))
+    solve_fixture("vortex12_rk3_parabolic", vortex, vp,
+                  {"flux": "HLLC", "reconstruction": "MUSCL parabolic", "limiter": "Venkatakrishnan",
+                   "time_integration": "Explicit RK3", "cfl": 0.8}, 8, ref)
+
+
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -80,7 +80,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(native.lib, name), name
     assert set(declared) == set(_lib.SIGNATURES), "ctypes signatures out of sync with the header"
-    assert native.mcfd_abi_version() == 1
+    assert native.mcfd_abi_version() == _lib.ABI_VERSION == 2
     assert native.mcfd_error_string(3) == b"option not supported by the GPU path"
 
 
@@ -103,6 +103,21 @@ def test_config_mapping_rejects_unsupported_models():
     with pytest.raises(NotImplementedError):
         make_config(NumericalSettings(viscosity_model="Constant"))
     with pytest.raises(NotImplementedError):
-        make_config(NumericalSettings(reconstruction="MUSCL parabolic"))
+        make_config(NumericalSettings(turbulence_model="SST"))
+    assert make_config(NumericalSettings(reconstruction="MUSCL parabolic")).reconstruction == 2
     cfg = make_config(NumericalSettings(flux="Roe", limiter="Van Leer", reconstruction="MUSCL linear"))
     assert (cfg.flux, cfg.limiter, cfg.reconstruction) == (2, 2, 1)
+
+
+@pytest.mark.parametrize("name", ("riemann16", "periodic_mixed", "channel"))
+def test_parabolic_stencil_is_bit_exact(name):
+    """The two-ring stencil (solver.py:2241-2291) of a geometry built for
+    MUSCL parabolic, against the reference's own."""
+    from meshcfd_gb300.geometry import build_geometry
+
+    data, ref = load_fixture(f"parabolic_{name}.npz")
+    case = _case_for(name)
+    case.numerics.reconstruction = "MUSCL parabolic"
+    g = build_geometry(case.mesh, case)
+    for field in ("parabolic_sources", "parabolic_neighbours", "parabolic_dx", "parabolic_dy"):
+        np.testing.assert_array_equal(np.asarray(getattr(g, field)), getattr(ref, field), err_msg=field)
