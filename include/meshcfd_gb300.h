@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define MCFD_ABI_VERSION 2
+#define MCFD_ABI_VERSION 3
 
 /* ---- return codes (host-side failures) ---- */
 #define MCFD_OK 0
@@ -49,12 +49,23 @@ extern "C" {
 #define MCFD_S_FARFIELD_SOUND 0x20     /* solver.py:4382-4383 */
 #define MCFD_S_FARFIELD_STATE 0x40     /* solver.py:4402-4407 */
 #define MCFD_S_TIME_STEP 0x80          /* solver.py:4341-4342 */
+/* pressure-inlet and mass-flow boundaries (messages name the patch given
+ * by mcfd_status.first_patch) */
+#define MCFD_S_PIN_DIRECTION 0x100        /* solver.py:4424-4428 */
+#define MCFD_S_PIN_SUPERSONIC_OUT 0x200   /* solver.py:4433-4437 */
+#define MCFD_S_PIN_SUPERSONIC_IN 0x400    /* solver.py:4445-4449 */
+#define MCFD_S_PIN_INCOMPATIBLE 0x800     /* solver.py:4465-4469 */
+#define MCFD_S_PIN_STATE 0x1000           /* solver.py:4491-4494 */
+#define MCFD_S_MFI_DIRECTION 0x2000       /* solver.py:4508-4512 */
+#define MCFD_S_MFI_PRESSURE 0x4000        /* solver.py:4513-4516 */
+#define MCFD_S_MFI_FLOW_RATE 0x8000       /* solver.py:4536-4540 */
+#define MCFD_S_MFO_DENSITY 0x10000        /* solver.py:4563-4566 */
 
 typedef struct mcfd_status {
   int32_t code;       /* OR of MCFD_S_* bits since the last fetch */
   int32_t first_cell; /* lowest cell id that set a state/residual/time-step bit, or -1 */
   int32_t first_face; /* lowest flux-face index that set a flux bit, or -1 */
-  int32_t reserved;
+  int32_t first_patch; /* lowest boundary-patch index (mcfd_geom_desc.bc_*) that set a boundary bit, or -1 */
 } mcfd_status;
 
 /* ---- scheme codes ---- */
@@ -88,8 +99,14 @@ typedef struct mcfd_config {
   double acceleration_x;  /* body force (solver.py:2709-2715) */
   double acceleration_y;
   double cfl;             /* used by mcfd_time_steps */
-  double reserved[4];
+  double gas_constant;    /* NumericalSettings.gas_constant: pressure-inlet / mass-flow states */
+  double reserved[3];
 } mcfd_config;
+
+/* boundary patch kinds (solver.py:81-103) */
+#define MCFD_BC_PRESSURE_INLET 0
+#define MCFD_BC_MASS_FLOW_INLET 1
+#define MCFD_BC_MASS_FLOW_OUTLET 2
 
 /*
  * Geometry description: the arrays of the reference `_Geometry`
@@ -141,6 +158,19 @@ typedef struct mcfd_geom_desc {
   const int64_t* parabolic_neighbours;
   const double* parabolic_dx;
   const double* parabolic_dy;
+  /* pressure-inlet, mass-flow-inlet and mass-flow-outlet patches
+   * (_Geometry.pressure_inlets / mass_flow_inlets / mass_flow_outlets), in
+   * the reference's order: all pressure inlets, then the mass-flow inlets,
+   * then the mass-flow outlets. */
+  int64_t n_bc_patches;
+  const int32_t* bc_kind;      /* [n] MCFD_BC_* */
+  const double* bc_values;     /* [n][4]: pressure inlet: total pressure, total temperature, direction x, y;
+                                  mass-flow inlet: mass flow, total temperature, direction x, y;
+                                  mass-flow outlet: mass flow, float(np.sum(face lengths)), 0, 0 */
+  const int64_t* bc_offsets;   /* [n + 1] into bc_faces */
+  const int64_t* bc_faces;     /* boundary face ids, patch by patch */
+  const double* bc_direction_normal; /* [len(bc_faces)] normals @ direction as the reference computes it
+                                        (inlets; 0 for outlets) */
 } mcfd_geom_desc;
 
 typedef struct mcfd_geom mcfd_geom; /* opaque device geometry + workspace */

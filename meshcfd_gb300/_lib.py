@@ -23,7 +23,7 @@ P_dbl = C.POINTER(C.c_double)
 
 
 class Status(C.Structure):
-    _fields_ = [("code", c_i32), ("first_cell", c_i32), ("first_face", c_i32), ("reserved", c_i32)]
+    _fields_ = [("code", c_i32), ("first_cell", c_i32), ("first_face", c_i32), ("first_patch", c_i32)]
 
 
 class Config(C.Structure):
@@ -36,7 +36,8 @@ class Config(C.Structure):
         ("acceleration_x", c_dbl),
         ("acceleration_y", c_dbl),
         ("cfl", c_dbl),
-        ("reserved", c_dbl * 4),
+        ("gas_constant", c_dbl),
+        ("reserved", c_dbl * 3),
     ]
 
 
@@ -56,6 +57,8 @@ class GeomDesc(C.Structure):
         ("n_limiter", c_i64), ("limiter_cells", P_i64), ("limiter_dx", P_dbl), ("limiter_dy", P_dbl),
         ("n_parabolic", c_i64), ("parabolic_sources", P_i64), ("parabolic_neighbours", P_i64),
         ("parabolic_dx", P_dbl), ("parabolic_dy", P_dbl),
+        ("n_bc_patches", c_i64), ("bc_kind", C.POINTER(C.c_int32)), ("bc_values", P_dbl), ("bc_offsets", P_i64),
+        ("bc_faces", P_i64), ("bc_direction_normal", P_dbl),
     ]
 
 
@@ -67,7 +70,7 @@ class GeomInfo(C.Structure):
     ]
 
 
-ABI_VERSION = 2  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
+ABI_VERSION = 3  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
 
 # name -> (restype, argtypes); every symbol include/meshcfd_gb300.h declares.
 SIGNATURES = {

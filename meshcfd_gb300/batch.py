@@ -106,6 +106,13 @@ def concatenate(geometries) -> tuple[Geometry, BatchLayout]:
             parts.append(np.where(a >= 0, a + cells[k], a))
         return np.concatenate(parts)
 
+    def shift_patches(name):
+        # boundary patches keep their order case by case, faces shifted
+        from dataclasses import replace
+
+        return tuple(replace(b, faces=np.asarray(b.faces, dtype=np.int64) + faces[k])
+                     for k, g in enumerate(geometries) for b in getattr(g, name, ()))
+
     # limiter entries: owner side of every face, then neighbour side of
     # interior faces — over the whole batch (slot ids are positions)
     lim_cells = np.concatenate(
@@ -131,7 +138,8 @@ def concatenate(geometries) -> tuple[Geometry, BatchLayout]:
         pressure_outlet_faces=cat("pressure_outlet_faces", "face"),
         pressure_outlet_pressures=cat("pressure_outlet_pressures"),
         far_field_faces=cat("far_field_faces", "face"), far_field_states=cat("far_field_states", width=4),
-        pressure_inlets=(), mass_flow_inlets=(), mass_flow_outlets=(),
+        pressure_inlets=shift_patches("pressure_inlets"), mass_flow_inlets=shift_patches("mass_flow_inlets"),
+        mass_flow_outlets=shift_patches("mass_flow_outlets"),
         gradient_sources=cat("gradient_sources", "cell"), gradient_neighbours=cat("gradient_neighbours", "cell"),
         gradient_dx=cat("gradient_dx"), gradient_dy=cat("gradient_dy"),
         gradient_coefficients_x=cat("gradient_coefficients_x"), gradient_coefficients_y=cat("gradient_coefficients_y"),

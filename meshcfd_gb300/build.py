@@ -31,6 +31,7 @@ UNITS = [
     ("mcfd_jvp.cu", ["-fmad=false"]),
     ("mcfd_vjp.cu", ["-fmad=false"]),
     ("mcfd_parabolic.cu", ["-fmad=false"]),
+    ("mcfd_boundary.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),
     ("mcfd_noalloc.cu", ["-fmad=false"]),
 ]

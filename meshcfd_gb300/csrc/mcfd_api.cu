@@ -118,6 +118,10 @@ static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgra
     e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return MCFD_DISPATCH(cfg, launch_reconstruct(h->g, cfg, h->ws.P, h->ws.recon, s)); });
   else if (cfg.reconstruction == MCFD_RECON_MUSCL_PARABOLIC)
     e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return launch_reconstruct_parabolic(h->g, cfg, h->ws.P, h->ws.recon, s); });
+  if (e == cudaSuccess && h->g.n_bc_patches > 0) {
+    const double* recon = cfg.reconstruction == MCFD_RECON_FIRST_ORDER ? nullptr : h->ws.recon;
+    e = timed(h, MCFD_PROF_FLUX, s, [&] { return launch_bc_states(h->g, cfg, h->ws.P, recon, h->g.bc_ext, s); });
+  }
   if (e == cudaSuccess)
     e = timed(h, MCFD_PROF_FLUX, s, [&] { return MCFD_DISPATCH(cfg, launch_flux(h->g, cfg, h->ws.P, h->ws.recon, h->ws.flux, s)); });
   if (e == cudaSuccess)
@@ -191,11 +195,24 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
     return MCFD_E_ARG;
   for (int64_t e = 0; e < NE; ++e)
     if (!in_range(d->parabolic_sources[e], C) || !in_range(d->parabolic_neighbours[e], C)) return MCFD_E_GEOMETRY;
+  const int64_t NBP = d->n_bc_patches;
+  if (NBP < 0 || NBP > kMaxIndex) return MCFD_E_ARG;
+  if (NBP && (!d->bc_kind || !d->bc_values || !d->bc_offsets || !d->bc_direction_normal)) return MCFD_E_ARG;
+  const int64_t NB = NBP ? d->bc_offsets[NBP] : 0;
+  if (NBP) {
+    if (d->bc_offsets[0] != 0) return MCFD_E_GEOMETRY;
+    for (int64_t k = 0; k < NBP; ++k) {
+      if (d->bc_offsets[k + 1] < d->bc_offsets[k]) return MCFD_E_GEOMETRY;
+      if (d->bc_kind[k] < MCFD_BC_PRESSURE_INLET || d->bc_kind[k] > MCFD_BC_MASS_FLOW_OUTLET) return MCFD_E_ARG;
+    }
+    if (NB > kMaxIndex || (NB && !d->bc_faces)) return MCFD_E_ARG;
+    if (!check_faces(d->bc_faces, NB)) return MCFD_E_GEOMETRY;
+  }
   for (int64_t c = 0; c < C; ++c)
     if (!(d->areas[c] > 0.0)) return MCFD_E_GEOMETRY;
 
   // ---- flux faces
-  const int64_t n_flux = NI + NP + NW + NV + NO + NF;
+  const int64_t n_flux = NI + NP + NW + NV + NO + NF + NB;
   if (n_flux > kMaxIndex) return MCFD_E_ARG;
   int seg_begin[SEG_COUNT + 1];
   seg_begin[SEG_INTERIOR] = 0;
@@ -204,6 +221,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   seg_begin[SEG_VIN] = (int)(NI + NP + NW);
   seg_begin[SEG_POUT] = (int)(NI + NP + NW + NV);
   seg_begin[SEG_FAR] = (int)(NI + NP + NW + NV + NO);
+  seg_begin[SEG_BCX] = (int)(NI + NP + NW + NV + NO + NF);
   seg_begin[SEG_COUNT] = (int)n_flux;
   std::vector<int> lslot(n_flux), rslot(n_flux, -1), lcell(n_flux), rcell(n_flux, -1);
   std::vector<double> normal(2 * n_flux), flen(n_flux), wallv(2 * NW, 0.0), vin(4 * NV), pout(NO), far(4 * NF);
@@ -245,6 +263,17 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   for (int64_t i = 0; i < NF; ++i) {
     set_face(seg_begin[SEG_FAR] + i, d->far_field_faces[i]);
     for (int k = 0; k < 4; ++k) far[4 * i + k] = d->far_field_states[4 * i + k];
+  }
+  std::vector<int> bc_ptr(NBP + 1, 0), bc_kind(NBP);
+  std::vector<double> bc_values(4 * NBP), bc_dn(NB);
+  for (int64_t k = 0; k < NBP; ++k) {
+    bc_ptr[k + 1] = (int)d->bc_offsets[k + 1];
+    bc_kind[k] = d->bc_kind[k];
+    for (int j = 0; j < 4; ++j) bc_values[4 * k + j] = d->bc_values[4 * k + j];
+  }
+  for (int64_t i = 0; i < NB; ++i) {
+    set_face(seg_begin[SEG_BCX] + i, d->bc_faces[i]);
+    bc_dn[i] = d->bc_direction_normal[i];
   }
 
   // ---- cell gather, interior part: the SciPy CSR divergence operator
@@ -297,7 +326,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
       bflux.push_back(seg_begin[SEG_PERIODIC] + (int)i);
       blen.push_back(d->face_lengths[fa]);
     }
-    for (int seg = SEG_WALL; seg <= SEG_FAR; ++seg) {
+    for (int seg = SEG_WALL; seg < SEG_COUNT; ++seg) {
       for (int k = seg_begin[seg]; k < seg_begin[seg + 1]; ++k) {
         int64_t f = lslot[k];
         bkey.push_back((int)d->owners[f]);
@@ -376,6 +405,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
     for (int64_t i = 0; i < NV; ++i) face_info[d->velocity_inlet_faces[i]] = (DT_VIN << 28) | (int)i;
     for (int64_t i = 0; i < NO; ++i) face_info[d->pressure_outlet_faces[i]] = (DT_POUT << 28) | (int)i;
     for (int64_t i = 0; i < NF; ++i) face_info[d->far_field_faces[i]] = (DT_FAR << 28) | (int)i;
+    for (int64_t i = 0; i < NB; ++i) face_info[d->bc_faces[i]] = (DT_BCX << 28) | (int)i;
     std::vector<int> dface;
     std::vector<int> dinfo;
     key.clear();
@@ -414,6 +444,8 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   size_t o_lim_ptr = A.take(bytes_i(C + 1)), o_lim_slot = A.take(bytes_i(NL)),
          o_lim_d = A.take(bytes_d(2 * NL));
   size_t o_par_ptr = A.take(bytes_i(C + 1)), o_par_nb = A.take(bytes_i(NE)), o_par_d = A.take(bytes_d(2 * NE));
+  size_t o_bc_ptr = A.take(bytes_i(NBP + 1)), o_bc_kind = A.take(bytes_i(NBP)), o_bc_values = A.take(bytes_d(4 * NBP)),
+         o_bc_dn = A.take(bytes_d(NB));
   size_t o_lslot = A.take(bytes_i(n_flux)), o_rslot = A.take(bytes_i(n_flux)),
          o_lcell = A.take(bytes_i(n_flux)), o_rcell = A.take(bytes_i(n_flux)),
          o_normal = A.take(bytes_d(2 * n_flux)), o_flen = A.take(bytes_d(n_flux)), o_wallv = A.take(bytes_d(2 * NW)),
@@ -431,6 +463,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   for (int k = 0; k < 4; ++k) o_stage[k] = A.take(bytes_d(4 * C));
   size_t o_saved = A.take(bytes_d(4 * C));
   size_t o_partials = A.take(bytes_d(4 * partial_blocks));
+  size_t o_bc_ext = A.take(bytes_d(4 * NB)), o_bc_ext_dt = A.take(bytes_d(4 * NB)), o_bc_terms = A.take(bytes_d(NB));
 
   mcfd_geom* h = new mcfd_geom();
   cudaError_t err = cudaMalloc(&h->arena, A.size);
@@ -456,6 +489,10 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   put(o_par_ptr, par_ptr.data(), bytes_i(C + 1));
   put(o_par_nb, par_nb.data(), bytes_i(NE));
   put(o_par_d, par_d.data(), bytes_d(2 * NE));
+  put(o_bc_ptr, bc_ptr.data(), bytes_i(NBP + 1));
+  put(o_bc_kind, bc_kind.data(), bytes_i(NBP));
+  put(o_bc_values, bc_values.data(), bytes_d(4 * NBP));
+  put(o_bc_dn, bc_dn.data(), bytes_d(NB));
   put(o_lslot, lslot.data(), bytes_i(n_flux));
   put(o_rslot, rslot.data(), bytes_i(n_flux));
   put(o_lcell, lcell.data(), bytes_i(n_flux));
@@ -476,7 +513,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   put(o_dt_n, dt_n.data(), bytes_d(dt_n.size()));
   put(o_dt_len, dt_len.data(), bytes_d(dt_len.size()));
   put(o_dt_info, dt_info.data(), bytes_i(dt_info.size()));
-  DevStatus st0{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(), 0,
+  DevStatus st0{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(), std::numeric_limits<int>::max(),
                 0x7ff0000000000000ULL};
   put(o_status, &st0, sizeof(st0));
   // geometry part only (workspace stays uninitialised)
@@ -509,6 +546,14 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   g.par_ptr = AT(const int*, o_par_ptr);
   g.par_nb = AT(const int*, o_par_nb);
   g.par_d = AT(const double2*, o_par_d);
+  g.n_bc_patches = (int)NBP;
+  g.bc_ptr = AT(const int*, o_bc_ptr);
+  g.bc_kind = AT(const int*, o_bc_kind);
+  g.bc_values = AT(const double*, o_bc_values);
+  g.bc_dn = AT(const double*, o_bc_dn);
+  g.bc_ext = AT(double*, o_bc_ext);
+  g.bc_ext_dt = AT(double*, o_bc_ext_dt);
+  g.bc_terms = AT(double*, o_bc_terms);
   g.ff_lslot = AT(const int*, o_lslot);
   g.ff_rslot = AT(const int*, o_rslot);
   g.ff_lcell = AT(const int*, o_lcell);
@@ -545,7 +590,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   info.n_faces = F;
   info.n_interior = NI;
   info.n_periodic = NP;
-  info.n_boundary_flux = NW + NV + NO + NF;
+  info.n_boundary_flux = NW + NV + NO + NF + NB;
   info.n_flux_faces = n_flux;
   info.n_gradient = NG;
   info.n_limiter = NL;
@@ -652,7 +697,13 @@ int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, doubl
   if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_TIME_STEP, s,
-                  [&] { return MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, dt_min, time_limit, s)); }));
+                  [&] {
+                    cudaError_t r = cudaSuccess;
+                    if (h->g.n_bc_patches > 0) r = launch_bc_states(h->g, *cfg, P, nullptr, h->g.bc_ext_dt, s);
+                    if (r == cudaSuccess)
+                      r = MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, dt_min, time_limit, s));
+                    return r;
+                  }));
 }
 
 
@@ -724,9 +775,10 @@ int mcfd_status_fetch(mcfd_geom* h, void* stream, mcfd_status* out) {
   out->code = st.code;
   out->first_cell = st.first_cell == std::numeric_limits<int>::max() ? -1 : st.first_cell;
   out->first_face = st.first_face == std::numeric_limits<int>::max() ? -1 : st.first_face;
-  out->reserved = 0;
+  out->first_patch = st.first_patch == std::numeric_limits<int>::max() ? -1 : st.first_patch;
   if (st.code) {
-    DevStatus clear{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(), 0, st.dt_min_bits};
+    DevStatus clear{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(),
+                    std::numeric_limits<int>::max(), st.dt_min_bits};
     *h->host_status = clear;
     e = cudaMemcpyAsync(h->status, h->host_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -855,7 +907,7 @@ int mcfd_vjp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   if (!h || !U || !lambda || !U_bar) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
-  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC) return MCFD_E_UNSUPPORTED;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0) return MCFD_E_UNSUPPORTED;
   if (cfg->reconstruction != MCFD_RECON_FIRST_ORDER && !h->g.has_twins) return MCFD_E_UNSUPPORTED;
   if ((c = ensure_vjp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
@@ -879,7 +931,7 @@ int mcfd_jvp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   if (!h || !U || !dU || !dR) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
-  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC) return MCFD_E_UNSUPPORTED;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0) return MCFD_E_UNSUPPORTED;
   if ((c = ensure_jvp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return launch_jvp(h->g, *cfg, U, dU, h->jvp, dR, s); }));
@@ -977,7 +1029,9 @@ int mcfd_batch_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P,
   if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = timed(h, MCFD_PROF_TIME_STEP, s, [&] {
-    cudaError_t r = MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, nullptr, 0.0, s));
+    cudaError_t r = cudaSuccess;
+    if (h->g.n_bc_patches > 0) r = launch_bc_states(h->g, *cfg, P, nullptr, h->g.bc_ext_dt, s);
+    if (r == cudaSuccess) r = MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, nullptr, 0.0, s));
     if (r == cudaSuccess) r = launch_case_time_steps(h->g.n_cells, n_cases, case_offsets, dt_case, dt_cells, s);
     return r;
   });

@@ -13,17 +13,19 @@ namespace mcfd {
 // in _residual (solver.py:2502-2704): interior faces first (their sum is the
 // CSR divergence product, solver.py:2501), then periodic pairs, walls and
 // symmetry planes, velocity inlets, pressure outlets, far field.
-enum Segment { SEG_INTERIOR = 0, SEG_PERIODIC, SEG_WALL, SEG_VIN, SEG_POUT, SEG_FAR, SEG_COUNT };
+// SEG_BCX: pressure-inlet and mass-flow faces, whose exterior states come from
+// the per-patch boundary kernel (mcfd_boundary.cu) before the flux launch.
+enum Segment { SEG_INTERIOR = 0, SEG_PERIODIC, SEG_WALL, SEG_VIN, SEG_POUT, SEG_FAR, SEG_BCX, SEG_COUNT };
 
 // Kinds of dt entries (exterior state used for the boundary spectral radius,
 // solver.py:4190-4220).
-enum DtKind { DT_PLAIN = 0, DT_VIN = 1, DT_POUT = 2, DT_FAR = 3 };
+enum DtKind { DT_PLAIN = 0, DT_VIN = 1, DT_POUT = 2, DT_FAR = 3, DT_BCX = 4 };
 
 struct DevStatus {
   int code;
   int first_cell;
   int first_face;
-  int pad;
+  int first_patch;
   unsigned long long dt_min_bits;  // atomicMin target for the global time step
 };
 
@@ -60,6 +62,15 @@ struct DevGeom {
   const double* ff_vin_state;       // [n_vin][4]
   const double* ff_pout_pressure;   // [n_pout]
   const double* ff_far_state;       // [n_far][4]
+  // pressure-inlet / mass-flow patches over the SEG_BCX faces
+  int n_bc_patches;
+  const int* bc_ptr;       // [patches + 1], positions within SEG_BCX
+  const int* bc_kind;      // [patches]
+  const double* bc_values; // [patches][4]
+  const double* bc_dn;     // [n_bcx] direction . normal
+  double* bc_ext;          // [n_bcx][4] exterior states of the residual (written per evaluation)
+  double* bc_ext_dt;       // [n_bcx][4] exterior states of the time step (from cell values)
+  double* bc_terms;        // [n_bcx] mass-flow inlet scratch
   // cell gather: interior faces in ascending face order with the reference's
   // CSR divergence coefficient, then boundary contributions in BC order with a
   // signed face length.
@@ -138,6 +149,11 @@ cudaError_t launch_reconstruct_parabolic(const DevGeom& g, const mcfd_config& cf
                                          cudaStream_t s);
 cudaError_t launch_reconstruction_fields(const DevGeom& g, const mcfd_config& cfg, const double* P, double* grad,
                                          double* curv, double* fac, cudaStream_t s);
+// pressure-inlet and mass-flow exterior states (mcfd_boundary.cu; exact
+// arithmetic): from the face states of the residual (recon per slot, or P for
+// first order when recon is null) into ext
+cudaError_t launch_bc_states(const DevGeom& g, const mcfd_config& cfg, const double* P, const double* recon,
+                             double* ext, cudaStream_t s);
 // reduction kernels of the sum of squares
 __global__ void k_sumsq_partial(int n, const double* __restrict__ R, double* __restrict__ partials);
 __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums);

@@ -278,8 +278,10 @@ __global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __rest
     R = ld4(g.ff_vin_state + 4 * (size_t)(f - begin));  // solver.py:2558
   } else if (SEG == SEG_POUT) {
     R = St4{L.a, L.b, L.c, g.ff_pout_pressure[f - begin]};  // solver.py:2581-2582
-  } else {
+  } else if (SEG == SEG_FAR) {
     bits |= far_field_state(L, ld4(g.ff_far_state + 4 * (size_t)(f - begin)), n.x, n.y, gamma, &R);
+  } else {
+    R = ld4(g.bc_ext + 4 * (size_t)(f - begin));  // solver.py:2626-2698, states from k_bc_states
   }
   double out[4];
   bits |= numerical_flux<FLUX, (SEG == SEG_INTERIOR) && KERNEL_HLLC>(L, R, n.x, n.y, gamma, inv_gm1, out);
@@ -399,7 +401,8 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
         St4 ext;
         if (kind == DT_VIN) ext = ld4(g.ff_vin_state + 4 * (size_t)idx);
         else if (kind == DT_POUT) ext = St4{p.a, p.b, p.c, g.ff_pout_pressure[idx]};
-        else bits |= far_field_state(p, ld4(g.ff_far_state + 4 * (size_t)idx), n.x, n.y, gamma, &ext);
+        else if (kind == DT_FAR) bits |= far_field_state(p, ld4(g.ff_far_state + 4 * (size_t)idx), n.x, n.y, gamma, &ext);
+        else ext = ld4(g.bc_ext_dt + 4 * (size_t)idx);  // solver.py:4153-4188, states from k_bc_states
         double er = fabs(ext.b * n.x + ext.c * n.y) + sound_speed(ext.a, ext.d, gamma);
         radius = icmp::lt_nonneg(radius, er) ? er : radius;  // np.maximum
       }
@@ -485,6 +488,7 @@ static void flux_segments(const DevGeom& g, const double* P, const double* recon
   MCFD_SEG(SEG_VIN)
   MCFD_SEG(SEG_POUT)
   MCFD_SEG(SEG_FAR)
+  MCFD_SEG(SEG_BCX)
 #undef MCFD_SEG
 }
 

@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .errors import SolverError, raise_for_status
+from .errors import SolverError, StatusCode, raise_for_status
 from .model import FLUX_CODES, LIMITER_CODES, RECONSTRUCTION_CODES
 
 TIME_SCHEME_CODES = {"Explicit Euler": 0, "Explicit RK2": 1, "Explicit RK3": 2, "Explicit RK4": 3}
@@ -47,6 +47,7 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
     cfg.acceleration_x = float(settings.acceleration_x)
     cfg.acceleration_y = float(settings.acceleration_y)
     cfg.cfl = float(settings.cfl)
+    cfg.gas_constant = float(settings.gas_constant)
     return cfg
 
 
@@ -64,9 +65,6 @@ class DeviceGeometry:
     """Packed device geometry + workspace for one mesh (one CUDA device)."""
 
     def __init__(self, geometry, device=None):
-        if getattr(geometry, "pressure_inlets", ()) or getattr(geometry, "mass_flow_inlets", ()) \
-                or getattr(geometry, "mass_flow_outlets", ()):
-            raise NotImplementedError("pressure-inlet and mass-flow boundaries are not implemented on the GPU path")
         self.lib = _lib.native()
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else torch.device(device).index or 0)
         keep = {}
@@ -112,6 +110,16 @@ class DeviceGeometry:
                                       src=getattr(geometry, "parabolic_neighbours", empty_i))
         d.parabolic_dx, _ = a("parabolic_dx", np.float64, src=getattr(geometry, "parabolic_dx", empty_d))
         d.parabolic_dy, _ = a("parabolic_dy", np.float64, src=getattr(geometry, "parabolic_dy", empty_d))
+        bc = boundary_patches(geometry)
+        self.bc_patch_names = bc["names"]
+        d.n_bc_patches = len(bc["names"])
+        if d.n_bc_patches:
+            keep["bc_kind"] = bc["kind"]
+            d.bc_kind = bc["kind"].ctypes.data_as(C.POINTER(C.c_int32))
+            d.bc_values, _ = a("bc_values", np.float64, src=bc["values"])
+            d.bc_offsets, _ = a("bc_offsets", np.int64, src=bc["offsets"])
+            d.bc_faces, _ = a("bc_faces", np.int64, src=bc["faces"])
+            d.bc_direction_normal, _ = a("bc_direction_normal", np.float64, src=bc["direction_normal"])
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             rc = self.lib.mcfd_geom_create(C.byref(d), C.byref(handle))
@@ -143,14 +151,17 @@ class DeviceGeometry:
 
     # --------------------------------------------------------------- status
     def check_status(self, solver_error=SolverError, stream=None) -> None:
-        st = _lib.Status()
-        self.lib.check(self.lib.mcfd_status_fetch(self.handle, _stream_ptr(stream), C.byref(st)), "mcfd_status_fetch")
-        raise_for_status(st.code, solver_error)
+        raise_for_status(self.status_code(stream), solver_error)
 
-    def status_code(self, stream=None) -> int:
+    def status_code(self, stream=None) -> StatusCode:
+        """The device status bits since the last fetch (an int), carrying the
+        name of the lowest failing boundary patch as ``.patch``."""
         st = _lib.Status()
         self.lib.check(self.lib.mcfd_status_fetch(self.handle, _stream_ptr(stream), C.byref(st)), "mcfd_status_fetch")
-        return int(st.code)
+        code = StatusCode(st.code)
+        if 0 <= st.first_patch < len(self.bc_patch_names):
+            code.patch = self.bc_patch_names[st.first_patch]
+        return code
 
     # ----------------------------------------------------------- operations
     def primitive(self, U: torch.Tensor, cfg, out: torch.Tensor | None = None) -> torch.Tensor:
@@ -210,6 +221,46 @@ class DeviceGeometry:
         self.lib.check(self.lib.mcfd_residual_sumsq(self.handle, R.data_ptr(), sums.data_ptr(), _stream_ptr()),
                        "mcfd_residual_sumsq")
         return sums
+
+
+BC_PRESSURE_INLET, BC_MASS_FLOW_INLET, BC_MASS_FLOW_OUTLET = 0, 1, 2
+
+
+def boundary_patches(geometry) -> dict:
+    """The pressure-inlet, mass-flow-inlet and mass-flow-outlet patches of a
+    geometry (solver.py:81-103) as the C ABI's patch table, in the order the
+    residual visits them (solver.py:2626-2698).  The per-face n . direction is
+    NumPy's own ``normals @ direction`` (solver.py:4423, 4507), whose BLAS
+    rounding the states depend on; the outlet's total length is NumPy's own
+    ``np.sum`` (solver.py:4568)."""
+    normals_all = np.asarray(geometry.face_normals, dtype=np.float64).reshape(-1, 2)
+    lengths_all = np.asarray(geometry.face_lengths, dtype=np.float64)
+    names, kinds, values, offsets, faces, dn = [], [], [], [0], [], []
+    for kind, patches in ((BC_PRESSURE_INLET, getattr(geometry, "pressure_inlets", ())),
+                          (BC_MASS_FLOW_INLET, getattr(geometry, "mass_flow_inlets", ())),
+                          (BC_MASS_FLOW_OUTLET, getattr(geometry, "mass_flow_outlets", ()))):
+        for b in patches:
+            f = np.asarray(b.faces, dtype=np.int64)
+            if kind == BC_PRESSURE_INLET:
+                if not math.isclose(float(np.linalg.norm(b.direction)), 1.0):  # solver.py:4420-4423
+                    raise SolverError(f"Pressure inlet '{b.patch_name}' has an invalid flow direction.")
+                values.append((b.total_pressure, b.total_temperature, b.direction[0], b.direction[1]))
+                dn.append(normals_all[f] @ np.asarray(b.direction, dtype=np.float64))
+            elif kind == BC_MASS_FLOW_INLET:
+                values.append((b.mass_flow, b.total_temperature, b.direction[0], b.direction[1]))
+                dn.append(normals_all[f] @ np.asarray(b.direction, dtype=np.float64))
+            else:
+                values.append((b.mass_flow, float(np.sum(lengths_all[f])), 0.0, 0.0))
+                dn.append(np.zeros(len(f)))
+            names.append(b.patch_name)
+            kinds.append(kind)
+            faces.append(f)
+            offsets.append(offsets[-1] + len(f))
+    cat = (lambda parts, dtype: np.concatenate(parts).astype(dtype) if parts else np.empty(0, dtype=dtype))
+    return {"names": names, "kind": np.asarray(kinds, dtype=np.int32),
+            "values": np.asarray(values, dtype=np.float64).reshape(-1, 4),
+            "offsets": np.asarray(offsets, dtype=np.int64), "faces": cat(faces, np.int64),
+            "direction_normal": cat(dn, np.float64)}
 
 
 def _device_view(ptr: int, shape, device) -> torch.Tensor:

@@ -12,6 +12,8 @@ that callers matching on them keep working:
 * solver.py:4383     "Far-field characteristics produced invalid sound speed."
 * solver.py:4407     "Far-field characteristics produced an invalid state."
 * solver.py:4342     "Local stable time steps must be positive and finite."
+* solver.py:4424-4566 the pressure-inlet / mass-flow messages, which name the
+  boundary patch.
 """
 
 from __future__ import annotations
@@ -30,6 +32,22 @@ STATUS_ROE_NONFINITE = 1 << 4
 STATUS_FARFIELD_SOUND = 1 << 5
 STATUS_FARFIELD_STATE = 1 << 6
 STATUS_TIME_STEP = 1 << 7
+STATUS_PIN_DIRECTION = 1 << 8
+STATUS_PIN_SUPERSONIC_OUT = 1 << 9
+STATUS_PIN_SUPERSONIC_IN = 1 << 10
+STATUS_PIN_INCOMPATIBLE = 1 << 11
+STATUS_PIN_STATE = 1 << 12
+STATUS_MFI_DIRECTION = 1 << 13
+STATUS_MFI_PRESSURE = 1 << 14
+STATUS_MFI_FLOW_RATE = 1 << 15
+STATUS_MFO_DENSITY = 1 << 16
+
+
+class StatusCode(int):
+    """Device status bits plus the name of the lowest failing boundary patch
+    (``patch``), for the messages that name it."""
+
+    patch = None
 
 # (bit, exception class, message) in the order the reference would raise them
 # within one residual evaluation: the state check runs first (inside the
@@ -42,6 +60,19 @@ STATUS_MESSAGES = (
      "Far-field characteristics produced invalid sound speed."),
     (STATUS_FARFIELD_STATE, SolverError,
      "Far-field characteristics produced an invalid state."),
+    (STATUS_PIN_DIRECTION, SolverError,
+     "Pressure inlet '{patch}' flow direction must point into the domain across every face."),
+    (STATUS_PIN_SUPERSONIC_OUT, SolverError, "Pressure inlet '{patch}' cannot prescribe a supersonic outflow."),
+    (STATUS_PIN_SUPERSONIC_IN, SolverError,
+     "Pressure inlet '{patch}' needs Mach number to define a supersonic inflow."),
+    (STATUS_PIN_INCOMPATIBLE, SolverError,
+     "Pressure inlet '{patch}' total conditions are incompatible with the interior characteristic state."),
+    (STATUS_PIN_STATE, SolverError, "Pressure inlet '{patch}' produced an invalid state."),
+    (STATUS_MFI_DIRECTION, SolverError,
+     "Mass-flow inlet '{patch}' direction must point into the domain across every face."),
+    (STATUS_MFI_PRESSURE, SolverError, "Mass-flow inlet '{patch}' has invalid interior pressure."),
+    (STATUS_MFI_FLOW_RATE, SolverError, "Mass-flow inlet '{patch}' cannot satisfy the configured flow rate."),
+    (STATUS_MFO_DENSITY, SolverError, "Mass-flow outlet '{patch}' has invalid interior density."),
     (STATUS_HLLC_NONFINITE, ValueError, "HLLC flux produced a non-finite value."),
     (STATUS_ROE_NONFINITE, ValueError, "Roe flux produced a non-finite value."),
     (STATUS_NONFINITE_RESIDUAL, SolverError, "Spatial residual contains non-finite values."),
@@ -58,6 +89,8 @@ def raise_for_status(code: int, solver_error=SolverError) -> None:
         return
     for bit, kind, message in STATUS_MESSAGES:
         if code & bit:
+            if "{patch}" in message:
+                message = message.format(patch=getattr(code, "patch", None) or "?")
             if kind is SolverError:
                 raise solver_error(message)
             raise kind(message)

@@ -174,12 +174,14 @@ def _box_classifier(x0, x1, y0, y1):
     return classify
 
 
-def box_mesh(nx, ny, lx=1.0, ly=1.0, split="none", jitter=0.0, seed=0, x0=0.0, y0=0.0):
+def box_mesh(nx, ny, lx=1.0, ly=1.0, split="none", jitter=0.0, seed=0, x0=0.0, y0=0.0, separate_left=False):
     """Rectangle [x0,x0+lx]x[y0,y0+ly] of nx*ny quads.
 
     ``split``: "none" (quads), "all" (two triangles per quad) or "half" (a
     seed-chosen half of the quads, exactly nx*ny//2 of them, are split).
     ``jitter``: interior vertices move uniformly by up to +-jitter*h per axis.
+    ``separate_left``: every face of the left side is a patch of its own
+    ("left0" bottom to "left{ny-1}" top) instead of one "left" patch.
     """
     x1, y1 = x0 + lx, y0 + ly
     rng = np.random.default_rng(seed)
@@ -196,7 +198,19 @@ def box_mesh(nx, ny, lx=1.0, ly=1.0, split="none", jitter=0.0, seed=0, x0=0.0, y
     if jitter:
         points = _jitter_interior(points, nx, ny, lx / nx, ly / ny, jitter, rng)
     cells = _split_cells(nx, ny, mask)
-    return build_faces(points, cells, _box_classifier(x0, x1, y0, y1))
+    classify = _box_classifier(x0, x1, y0, y1)
+    if separate_left:
+        base = classify
+
+        def classify(a, b):
+            ids, names = base(a, b)
+            left = np.flatnonzero(ids == 3)
+            rank = np.argsort(np.argsort(a[left, 1] + b[left, 1], kind="stable"), kind="stable")
+            ids = ids.copy()
+            ids[left] = 3 + rank
+            return ids, names[:3] + tuple(f"left{k}" for k in range(len(left)))
+
+    return build_faces(points, cells, classify)
 
 
 # ---------------------------------------------------------------- workloads

@@ -27,6 +27,15 @@
 #define ORC_FARFIELD_SOUND 0x20
 #define ORC_FARFIELD_STATE 0x40
 #define ORC_TIME_STEP 0x80
+#define ORC_PIN_DIRECTION 0x100
+#define ORC_PIN_SUPERSONIC_OUT 0x200
+#define ORC_PIN_SUPERSONIC_IN 0x400
+#define ORC_PIN_INCOMPATIBLE 0x800
+#define ORC_PIN_STATE 0x1000
+#define ORC_MFI_DIRECTION 0x2000
+#define ORC_MFI_PRESSURE 0x4000
+#define ORC_MFI_FLOW_RATE 0x8000
+#define ORC_MFO_DENSITY 0x10000
 #define ORC_ARG 0x1000
 
 typedef struct {
@@ -58,11 +67,20 @@ typedef struct {
   int64_t n_parabolic; /* two-ring stencil entries, source-major (solver.py:2241-2291) */
   const int64_t *parabolic_sources, *parabolic_neighbours;
   const double *parabolic_dx, *parabolic_dy;
+  /* pressure-inlet (0), mass-flow-inlet (1), mass-flow-outlet (2) patches in
+   * the reference's order; values per patch: (total p, total T, dir x, dir y)
+   * / (mass flow, total T, dir x, dir y) / (mass flow, sum of lengths, 0, 0);
+   * bc_dn: NumPy's normals @ direction per face */
+  int64_t n_bc_patches;
+  const int32_t* bc_kind;
+  const double* bc_values;
+  const int64_t *bc_offsets, *bc_faces;
+  const double* bc_dn;
 } orc_geom;
 
 typedef struct {
   int32_t flux, reconstruction, limiter, pad;
-  double gamma, acceleration_x, acceleration_y, cfl;
+  double gamma, acceleration_x, acceleration_y, cfl, gas_constant;
 } orc_settings;
 
 /* ------------------------------------------------------------ euler.py */
@@ -611,6 +629,175 @@ static int far_field(const double* in, const double* far, const double* n, doubl
   return 0;
 }
 
+/* NumPy's pairwise summation of a contiguous float64 array (np.sum). */
+static double pairwise(const double* a, int64_t n) {
+  if (n < 8) {
+    double r = 0.0;
+    for (int64_t i = 0; i < n; ++i) r += a[i];
+    return r;
+  }
+  if (n <= 128) {
+    double r[8];
+    for (int j = 0; j < 8; ++j) r[j] = a[j];
+    int64_t i = 8;
+    for (; i < n - (n % 8); i += 8)
+      for (int j = 0; j < 8; ++j) r[j] += a[i + j];
+    double res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+    for (; i < n; ++i) res += a[i];
+    return res;
+  }
+  int64_t n2 = n / 2;
+  n2 -= n2 % 8;
+  return pairwise(a, n2) + pairwise(a + n2, n - n2);
+}
+
+/* invariant_at of _pressure_inlet_boundary_states; Python's float
+ * candidate**2 is libm pow(candidate, 2.0) */
+static double pin_invariant(double m, double dn, double a0, double gamma) {
+  double ratio = 1.0 + 0.5 * (gamma - 1.0) * pow(m, 2.0);
+  double sound = a0 / sqrt(ratio);
+  return sound * (dn * m + 2.0 / (gamma - 1.0));
+}
+
+/* _pressure_inlet_boundary_states (solver.py:4412-4496), one patch of n faces;
+ * in/ext [n][4], nrm [n][2] */
+static int pressure_inlet_states(int64_t n, const double* in, const double* nrm, const double* dn, const double* v,
+                                 double gamma, double R, double* ext) {
+  for (int64_t i = 0; i < n; ++i)
+    if (dn[i] >= -1e-12) return ORC_PIN_DIRECTION;
+  double* c = (double*)malloc(sizeof(double) * (n + 1));
+  double* un = (double*)malloc(sizeof(double) * (n + 1));
+  double* mach = (double*)malloc(sizeof(double) * (n + 1));
+  int st = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    c[i] = sqrt(gamma * in[4 * i + 3] / in[4 * i]);
+    un[i] = in[4 * i + 1] * nrm[2 * i] + in[4 * i + 2] * nrm[2 * i + 1];
+    if (un[i] / c[i] >= 1.0) st = ORC_PIN_SUPERSONIC_OUT;
+  }
+  double a0 = sqrt(gamma * R * v[1]);
+  for (int64_t i = 0; i < n && !st; ++i) {
+    if (un[i] / c[i] <= -1.0) {
+      st = ORC_PIN_SUPERSONIC_IN;
+      break;
+    }
+    double outgoing = un[i] + 2.0 * c[i] / (gamma - 1.0);
+    double lo_v = pin_invariant(0.0, dn[i], a0, gamma), hi_v = pin_invariant(1.0, dn[i], a0, gamma);
+    if (!(hi_v <= outgoing && outgoing <= lo_v)) {
+      st = ORC_PIN_INCOMPATIBLE;
+      break;
+    }
+    double low = 0.0, high = 1.0;
+    for (int it = 0; it < 64; ++it) {
+      double mid = 0.5 * (low + high);
+      if (pin_invariant(mid, dn[i], a0, gamma) > outgoing) low = mid;
+      else high = mid;
+    }
+    mach[i] = 0.5 * (low + high);
+  }
+  for (int64_t i = 0; i < n && !st; ++i) {
+    double t = v[1] / (1.0 + 0.5 * (gamma - 1.0) * (mach[i] * mach[i]));
+    double p = v[0] * pow(t / v[1], gamma / (gamma - 1.0));
+    double rho = p / (R * t);
+    double speed = mach[i] * sqrt(gamma * R * t);
+    double* e = ext + 4 * i;
+    e[0] = rho;
+    e[1] = speed * v[2];
+    e[2] = speed * v[3];
+    e[3] = p;
+    if (!isfinite(e[0]) || !isfinite(e[1]) || !isfinite(e[2]) || !isfinite(e[3]) || rho <= 0.0 || p <= 0.0)
+      st = ORC_PIN_STATE;
+  }
+  free(c);
+  free(un);
+  free(mach);
+  return st;
+}
+
+/* _mass_flow_inlet_boundary_states (solver.py:4499-4554), one patch; the
+ * velocity speed * direction on every face (the reference's one-row velocity
+ * array works only for single-face patches) */
+static int mass_flow_inlet_states(int64_t n, const double* in, const double* dn, const double* len,
+                                  const double* v, double gamma, double R, double* ext) {
+  for (int64_t i = 0; i < n; ++i)
+    if (-dn[i] <= 1e-12) return ORC_MFI_DIRECTION;
+  for (int64_t i = 0; i < n; ++i)
+    if (in[4 * i + 3] <= 0.0 || !isfinite(in[4 * i + 3])) return ORC_MFI_PRESSURE;
+  double cp = gamma * R / (gamma - 1.0);
+  double* terms = (double*)malloc(sizeof(double) * (n + 1));
+#define FLOW_AT(speed, out)                                                         \
+  do {                                                                              \
+    double t_ = v[1] - pow((speed), 2.0) / (2.0 * cp);                              \
+    for (int64_t i = 0; i < n; ++i)                                                 \
+      terms[i] = in[4 * i + 3] / (R * t_) * (speed) * (-dn[i]) * len[i];            \
+    out = 0.0 + pairwise(terms, n);                                                 \
+  } while (0)
+  double low = 0.0, high = sqrt(2.0 * cp * v[1]) * (1.0 - 1e-12), flow;
+  FLOW_AT(high, flow);
+  if (flow < v[0]) {
+    free(terms);
+    return ORC_MFI_FLOW_RATE;
+  }
+  for (int it = 0; it < 80; ++it) {
+    double mid = 0.5 * (low + high);
+    FLOW_AT(mid, flow);
+    if (flow < v[0]) low = mid;
+    else high = mid;
+  }
+#undef FLOW_AT
+  free(terms);
+  double speed = 0.5 * (low + high);
+  double t = v[1] - pow(speed, 2.0) / (2.0 * cp);
+  for (int64_t i = 0; i < n; ++i) {
+    ext[4 * i] = in[4 * i + 3] / (R * t);
+    ext[4 * i + 1] = speed * v[2];
+    ext[4 * i + 2] = speed * v[3];
+    ext[4 * i + 3] = in[4 * i + 3];
+  }
+  return 0;
+}
+
+/* _mass_flow_outlet_boundary_states (solver.py:4557-4577), one patch */
+static int mass_flow_outlet_states(int64_t n, const double* in, const double* nrm, const double* v, double* ext) {
+  for (int64_t i = 0; i < n; ++i)
+    if (in[4 * i] <= 0.0 || !isfinite(in[4 * i])) return ORC_MFO_DENSITY;
+  for (int64_t i = 0; i < n; ++i) {
+    double nx = nrm[2 * i], ny = nrm[2 * i + 1];
+    double vn = v[0] / (v[1] * in[4 * i]);
+    double vt = in[4 * i + 1] * -ny + in[4 * i + 2] * nx;
+    ext[4 * i] = in[4 * i];
+    ext[4 * i + 1] = vn * nx + vt * -ny;
+    ext[4 * i + 2] = vn * ny + vt * nx;
+    ext[4 * i + 3] = in[4 * i + 3];
+  }
+  return 0;
+}
+
+/* exterior states of one boundary patch k from interior states in [n][4] */
+int bc_patch_states(const orc_geom* g, int64_t k, const double* in, double gamma, double R, double* ext) {
+  int64_t b = g->bc_offsets[k], n = g->bc_offsets[k + 1] - b;
+  double* nrm = (double*)malloc(sizeof(double) * 2 * (n + 1));
+  double* len = (double*)malloc(sizeof(double) * (n + 1));
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t f = g->bc_faces[b + i];
+    nrm[2 * i] = g->face_normals[2 * f];
+    nrm[2 * i + 1] = g->face_normals[2 * f + 1];
+    len[i] = g->face_lengths[f];
+  }
+  const double* v = g->bc_values + 4 * k;
+  int st;
+  if (g->bc_kind[k] == 0) st = pressure_inlet_states(n, in, nrm, g->bc_dn + b, v, gamma, R, ext);
+  else if (g->bc_kind[k] == 1) st = mass_flow_inlet_states(n, in, g->bc_dn + b, len, v, gamma, R, ext);
+  else st = mass_flow_outlet_states(n, in, nrm, v, ext);
+  free(nrm);
+  free(len);
+  return st;
+}
+
+/* exported for tests: the exterior states of boundary patch k */
+int orc_bc_states(const orc_geom* g, int64_t k, const double* in, double gamma, double R, double* ext) {
+  return bc_patch_states(g, k, in, gamma, R, ext);
+}
+
 /* SciPy CSR rows of interior_divergence_operator (solver.py:2160-2174):
  * for every cell, its interior-face columns in ascending order. */
 typedef struct {
@@ -754,6 +941,32 @@ int orc_residual(const orc_geom* g, const orc_settings* s, const double* U, doub
     }
     free(contrib);
   }
+  /* pressure inlets, mass-flow inlets, mass-flow outlets (solver.py:2626-2698) */
+  for (int64_t k = 0; k < g->n_bc_patches && !status; ++k) {
+    int64_t b = g->bc_offsets[k], n = g->bc_offsets[k + 1] - b;
+    double* in = (double*)malloc(sizeof(double) * 4 * (n + 1));
+    double* ext = (double*)malloc(sizeof(double) * 4 * (n + 1));
+    double* contrib = (double*)malloc(sizeof(double) * 4 * (n + 1));
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t f = g->bc_faces[b + i], o = g->owners[f];
+      reconstruct(P, grad, fac, curv, o, g->face_centers[2 * f] - g->centers[2 * o],
+                  g->face_centers[2 * f + 1] - g->centers[2 * o + 1], in + 4 * i);
+    }
+    status |= bc_patch_states(g, k, in, gamma, s->gas_constant, ext);
+    for (int64_t i = 0; i < n && !status; ++i) {
+      int64_t f = g->bc_faces[b + i], o = g->owners[f];
+      double fl[4];
+      status |= numerical_flux(s->flux, in + 4 * i, ext + 4 * i, g->face_normals + 2 * f, gamma, fl);
+      for (int v = 0; v < 4; ++v) contrib[4 * i + v] = -(fl[v] * g->face_lengths[f]) / g->areas[o];
+    }
+    for (int64_t i = 0; i < n && !status; ++i) {
+      int64_t o = g->owners[g->bc_faces[b + i]];
+      for (int v = 0; v < 4; ++v) R[4 * o + v] += contrib[4 * i + v];
+    }
+    free(in);
+    free(ext);
+    free(contrib);
+  }
   if (s->acceleration_x != 0.0 || s->acceleration_y != 0.0) {
     for (int64_t c = 0; c < C; ++c) R[4 * c + 1] += P[4 * c] * s->acceleration_x;
     for (int64_t c = 0; c < C; ++c) R[4 * c + 2] += P[4 * c] * s->acceleration_y;
@@ -800,6 +1013,22 @@ int orc_stable_time_steps(const orc_geom* g, const orc_settings* s, const double
       double er = fabs(ext[1] * nrm[0] + ext[2] * nrm[1]) + sound(ext, gamma);
       radius[f] = radius[f] >= er ? radius[f] : er;
     }
+  }
+  /* pressure-inlet and mass-flow faces: states from the cell values */
+  for (int64_t k = 0; k < g->n_bc_patches; ++k) {
+    int64_t b = g->bc_offsets[k], n = g->bc_offsets[k + 1] - b;
+    double* in = (double*)malloc(sizeof(double) * 4 * (n + 1));
+    double* ext = (double*)malloc(sizeof(double) * 4 * (n + 1));
+    for (int64_t i = 0; i < n; ++i) memcpy(in + 4 * i, P + 4 * g->owners[g->bc_faces[b + i]], 4 * sizeof(double));
+    status |= bc_patch_states(g, k, in, gamma, s->gas_constant, ext);
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t f = g->bc_faces[b + i];
+      const double* nrm = g->face_normals + 2 * f;
+      double er = fabs(ext[4 * i + 1] * nrm[0] + ext[4 * i + 2] * nrm[1]) + sound(ext + 4 * i, gamma);
+      radius[f] = radius[f] >= er ? radius[f] : er;
+    }
+    free(in);
+    free(ext);
   }
   double* sum = (double*)calloc(C, sizeof(double));
   for (int64_t f = 0; f < F; ++f) sum[g->owners[f]] += radius[f] * g->face_lengths[f];

@@ -32,6 +32,15 @@ STATUS_TEXT = {
     0x20: "Far-field characteristics produced invalid sound speed.",
     0x40: "Far-field characteristics produced an invalid state.",
     0x80: "Local stable time steps must be positive and finite.",
+    0x100: "Pressure inlet flow direction must point into the domain across every face.",
+    0x200: "Pressure inlet cannot prescribe a supersonic outflow.",
+    0x400: "Pressure inlet needs Mach number to define a supersonic inflow.",
+    0x800: "Pressure inlet total conditions are incompatible with the interior characteristic state.",
+    0x1000: "Pressure inlet produced an invalid state.",
+    0x2000: "Mass-flow inlet direction must point into the domain across every face.",
+    0x4000: "Mass-flow inlet has invalid interior pressure.",
+    0x8000: "Mass-flow inlet cannot satisfy the configured flow rate.",
+    0x10000: "Mass-flow outlet has invalid interior density.",
 }
 
 P64 = C.POINTER(C.c_int64)
@@ -55,13 +64,15 @@ class OrcGeom(C.Structure):
         ("n_limiter", C.c_int64), ("limiter_cells", P64), ("limiter_dx", PD), ("limiter_dy", PD),
         ("n_parabolic", C.c_int64), ("parabolic_sources", P64), ("parabolic_neighbours", P64),
         ("parabolic_dx", PD), ("parabolic_dy", PD),
+        ("n_bc_patches", C.c_int64), ("bc_kind", C.POINTER(C.c_int32)), ("bc_values", PD), ("bc_offsets", P64),
+        ("bc_faces", P64), ("bc_dn", PD),
     ]
 
 
 class OrcSettings(C.Structure):
     _fields_ = [("flux", C.c_int32), ("reconstruction", C.c_int32), ("limiter", C.c_int32), ("pad", C.c_int32),
                 ("gamma", C.c_double), ("acceleration_x", C.c_double), ("acceleration_y", C.c_double),
-                ("cfl", C.c_double)]
+                ("cfl", C.c_double), ("gas_constant", C.c_double)]
 
 
 def build(force: bool = False) -> Path:
@@ -87,6 +98,7 @@ def lib():
         _lib.orc_primitive_to_conservative.argtypes = [C.c_int64, PD, C.c_double, PD]
         _lib.orc_linear_gradients_and_factors.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD]
         _lib.orc_parabolic_reconstruction.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD, PD]
+        _lib.orc_bc_states.argtypes = [C.POINTER(OrcGeom), C.c_int64, PD, C.c_double, C.c_double, PD]
     return _lib
 
 
@@ -100,6 +112,32 @@ def _raise(code: int):
             raise OracleError(text)
     if code:
         raise OracleError(f"oracle status {code:#x}")
+
+
+def _boundary_patches(g):
+    """Pressure-inlet / mass-flow patches of a geometry in the reference's
+    order, with NumPy's own ``normals @ direction`` (solver.py:4423, 4507) and
+    ``np.sum`` of the outlet face lengths (solver.py:4568)."""
+    normals = np.asarray(g.face_normals, dtype=np.float64).reshape(-1, 2)
+    lengths = np.asarray(g.face_lengths, dtype=np.float64)
+    kinds, values, offsets, faces, dn = [], [], [0], [], []
+    for kind, patches in ((0, getattr(g, "pressure_inlets", ())), (1, getattr(g, "mass_flow_inlets", ())),
+                          (2, getattr(g, "mass_flow_outlets", ()))):
+        for b in patches:
+            f = np.asarray(b.faces, dtype=np.int64)
+            if kind == 2:
+                values.append((b.mass_flow, float(np.sum(lengths[f])), 0.0, 0.0))
+                dn.append(np.zeros(len(f)))
+            else:
+                first = b.total_pressure if kind == 0 else b.mass_flow
+                values.append((first, b.total_temperature, b.direction[0], b.direction[1]))
+                dn.append(normals[f] @ np.asarray(b.direction, dtype=np.float64))
+            kinds.append(kind)
+            faces.append(f)
+            offsets.append(offsets[-1] + len(f))
+    cat = (lambda parts, dt: np.ascontiguousarray(np.concatenate(parts), dtype=dt) if parts else np.empty(0, dt))
+    return {"kind": np.asarray(kinds, dtype=np.int32), "values": np.ascontiguousarray(values, dtype=np.float64),
+            "offsets": np.asarray(offsets, dtype=np.int64), "faces": cat(faces, np.int64), "dn": cat(dn, np.float64)}
 
 
 class Oracle:
@@ -145,8 +183,6 @@ class Oracle:
             parabolic_neighbours=arr("parabolic_neighbours", np.int64),
             parabolic_dx=arr("parabolic_dx", np.float64), parabolic_dy=arr("parabolic_dy", np.float64),
         )
-        if getattr(g, "pressure_inlets", ()) or getattr(g, "mass_flow_inlets", ()) or getattr(g, "mass_flow_outlets", ()):
-            raise NotImplementedError("oracle: pressure-inlet / mass-flow boundaries")
         s = OrcGeom()
         s.n_cells, s.n_faces = n_cells, n_faces
         for name, a in fields.items():
@@ -161,6 +197,15 @@ class Oracle:
         s.n_gradient = len(fields["gradient_sources"])
         s.n_limiter = len(fields["limiter_cells"])
         s.n_parabolic = 0 if fields["parabolic_sources"] is None else len(fields["parabolic_sources"])
+        bc = _boundary_patches(g)
+        s.n_bc_patches = len(bc["kind"])
+        if s.n_bc_patches:
+            keep.update({"bc_" + k: v for k, v in bc.items()})
+            s.bc_kind = bc["kind"].ctypes.data_as(C.POINTER(C.c_int32))
+            s.bc_values = p(bc["values"], PD)
+            s.bc_offsets = p(bc["offsets"], P64)
+            s.bc_faces = p(bc["faces"], P64)
+            s.bc_dn = p(bc["dn"], PD)
         self.struct = s
         self._keep = keep
         self.n_cells = n_cells
@@ -175,6 +220,7 @@ class Oracle:
         s.acceleration_x = num.acceleration_x
         s.acceleration_y = num.acceleration_y
         s.cfl = num.cfl
+        s.gas_constant = num.gas_constant
         return s
 
     def primitive(self, U, gamma):
@@ -215,6 +261,15 @@ class Oracle:
         lib().orc_parabolic_reconstruction(C.byref(self.struct), P.ctypes.data_as(PD), LIMITER[limiter],
                                            grad.ctypes.data_as(PD), curv.ctypes.data_as(PD), fac.ctypes.data_as(PD))
         return grad, curv, fac
+
+    def boundary_states(self, k, interior, gamma, gas_constant):
+        """Exterior states of boundary patch ``k`` (pressure inlets, then
+        mass-flow inlets, then outlets) for interior states (n, 4)."""
+        interior = np.ascontiguousarray(interior, dtype=np.float64)
+        ext = np.empty_like(interior)
+        _raise(lib().orc_bc_states(C.byref(self.struct), k, interior.ctypes.data_as(PD), gamma, gas_constant,
+                                   ext.ctypes.data_as(PD)))
+        return ext
 
     def stable_time_steps(self, P, num):
         P = np.ascontiguousarray(P, dtype=np.float64)

@@ -19,9 +19,23 @@ def pytest_configure(config):
 def load_fixture(name):
     """Load a golden .npz as a dict (arrays) with a geometry namespace."""
     data = dict(np.load(GOLDEN / name, allow_pickle=False))
+    patches = ([], [], [])
+    if "bcp_kind" in data:
+        off = data["bcp_offsets"]
+        for k, (kind, pname, v) in enumerate(zip(data["bcp_kind"], data["bcp_names"], data["bcp_values"])):
+            faces = data["bcp_faces"][off[k]:off[k + 1]]
+            if kind == 0:
+                b = types.SimpleNamespace(faces=faces, total_pressure=float(v[0]), total_temperature=float(v[1]),
+                                          direction=np.asarray(v[2:4]), patch_name=str(pname))
+            elif kind == 1:
+                b = types.SimpleNamespace(faces=faces, mass_flow=float(v[0]), total_temperature=float(v[1]),
+                                          direction=np.asarray(v[2:4]), patch_name=str(pname))
+            else:
+                b = types.SimpleNamespace(faces=faces, mass_flow=float(v[0]), patch_name=str(pname))
+            patches[int(kind)].append(b)
     geom = types.SimpleNamespace(
         **{k[5:]: v for k, v in data.items() if k.startswith("geom_")},
-        pressure_inlets=(), mass_flow_inlets=(), mass_flow_outlets=(),
+        pressure_inlets=tuple(patches[0]), mass_flow_inlets=tuple(patches[1]), mass_flow_outlets=tuple(patches[2]),
     )
     return data, geom
 

@@ -9,6 +9,9 @@ reference's outputs, so the tests can run without the reference:
   limiter combination, with and without a body force, plus
   ``_stable_time_steps``;
 * solve_<case>.npz     — final states of ``solve_case`` after N explicit steps;
+* bc_<kind>.npz        — ``_residual`` and ``_stable_time_steps`` with
+  pressure-inlet or mass-flow inlet / outlet boundaries (plus
+  solve_<kind>_rk3.npz);
 * parabolic_<case>.npz — ``_residual`` with MUSCL parabolic reconstruction for
   every flux x limiter (with and without a body force) and the outputs of
   ``_parabolic_reconstruction`` per limiter, on a geometry built with the
@@ -85,7 +88,33 @@ PARABOLIC_FIELDS = ("parabolic_sources", "parabolic_neighbours", "parabolic_dx",
 
 
 def geometry_arrays(geometry, fields=GEOM_FIELDS):
-    return {f"geom_{name}": np.asarray(getattr(geometry, name)) for name in fields}
+    out = {f"geom_{name}": np.asarray(getattr(geometry, name)) for name in fields}
+    out.update(bc_patch_arrays(geometry))
+    return out
+
+
+def bc_patch_arrays(geometry):
+    """Pressure-inlet / mass-flow patches as flat arrays (kind 0 / 1 / 2;
+    values: total p, total T, direction / mass flow, total T, direction /
+    mass flow)."""
+    kinds, names, values, offsets, faces = [], [], [], [0], []
+    for kind, patches in ((0, geometry.pressure_inlets), (1, geometry.mass_flow_inlets),
+                          (2, geometry.mass_flow_outlets)):
+        for b in patches:
+            if kind == 0:
+                values.append((b.total_pressure, b.total_temperature, *b.direction))
+            elif kind == 1:
+                values.append((b.mass_flow, b.total_temperature, *b.direction))
+            else:
+                values.append((b.mass_flow, 0.0, 0.0, 0.0))
+            kinds.append(kind)
+            names.append(b.patch_name)
+            faces.extend(int(f) for f in b.faces)
+            offsets.append(len(faces))
+    if not kinds:
+        return {}
+    return {"bcp_kind": np.asarray(kinds), "bcp_names": np.asarray(names), "bcp_values": np.asarray(values),
+            "bcp_offsets": np.asarray(offsets), "bcp_faces": np.asarray(faces, dtype=np.int64)}
 
 
 def perturbed_primitive(n, seed):
@@ -127,6 +156,79 @@ def residual_fixture(name, case, ref):
     out["cfl"] = np.array(0.7)
     np.savez_compressed(HERE / f"residual_{name}.npz", **out)
     print(name, n, "cells,", len(keys), "residuals")
+
+
+def bc_case(kind, nx=16, ny=9):
+    """Jittered half-split channel [0,2]x[0,1] with slip walls top and bottom
+    and, left -> right, a pressure inlet -> pressure outlet ("pinlet") or a
+    mass-flow inlet -> mass-flow outlet ("massflow"); gas constant 287.05,
+    so temperature 1/287.05 means R T = 1.  The reference's mass-flow inlet
+    state only works for single-face patches (its velocity array has one row,
+    solver.py:4552-4554), so in "massflow" every left face is an inlet patch
+    of its own with its share of the flow rate."""
+    mesh = box_mesh(nx, ny, 2.0, 1.0, split="half", jitter=0.2, seed=7, separate_left=(kind == "massflow"))
+    case = Case(name=kind, mesh=mesh)
+    for c in case.boundary_conditions:
+        if c.patch_name.startswith("left") and kind == "massflow":
+            c.kind = "Mass Flow Inlet"
+            c.values = {"mass_flow": 0.3 / ny, "temperature": 1.1 / 287.05, "velocity_x": 1.0, "velocity_y": -0.1}
+        elif c.patch_name == "left":
+            if kind == "pinlet":
+                c.kind = "Pressure Inlet"
+                c.values = {"pressure": 1.2, "temperature": 1.1 / 287.05, "velocity_x": 1.0, "velocity_y": 0.2}
+            else:
+                c.kind = "Mass Flow Inlet"
+                c.values = {"mass_flow": 0.3, "temperature": 1.1 / 287.05, "velocity_x": 1.0, "velocity_y": -0.1}
+        elif c.patch_name == "right":
+            if kind == "pinlet":
+                c.kind = "Pressure Outlet"
+                c.values = {"pressure": 0.95}
+            else:
+                c.kind = "Mass Flow Outlet"
+                c.values = {"mass_flow": 0.3}
+        else:
+            c.kind = "Wall"
+            c.mechanical_condition = "Slip"
+    return case
+
+
+def bc_primitive(n, seed):
+    rng = np.random.default_rng(seed)
+    base = np.array([1.0, 0.3, 0.0, 1.0])
+    return base + np.array([0.05, 0.05, 0.05, 0.05]) * rng.standard_normal((n, 4))
+
+
+def bc_fixture(kind, ref):
+    """Residuals (3 fluxes x first order / MUSCL linear BJ, Venkatakrishnan /
+    MUSCL parabolic Venkatakrishnan), stable time steps and a short RK3 solve
+    with pressure-inlet or mass-flow boundaries."""
+    case = bc_case(kind)
+    case.numerics.reconstruction = "MUSCL parabolic"
+    rc = reference_case(case, ref)
+    rg = ref.solver._build_geometry(rc.mesh, rc)
+    out = {**mesh_arrays(case), **geometry_arrays(rg, GEOM_FIELDS + PARABOLIC_FIELDS)}
+    n = len(rg.areas)
+    P = bc_primitive(n, seed=5)
+    U = ref.euler.primitive_to_conservative(P, 1.4)
+    out["U"] = U
+    num = rc.numerics
+    keys = []
+    for flux, (recon, limiter) in itertools.product(FLUXES, (("First order", "Barth-Jespersen"),
+                                                             ("MUSCL linear", "Barth-Jespersen"),
+                                                             ("MUSCL linear", "Venkatakrishnan"),
+                                                             ("MUSCL parabolic", "Venkatakrishnan"))):
+        num.flux, num.reconstruction, num.limiter = flux, recon, limiter
+        key = f"R|{flux}|{recon}|{limiter}|0"
+        out[key] = ref.solver._residual(U, rg, num)
+        keys.append(key)
+    num.cfl = 0.7
+    out["dt_cells"] = ref.solver._stable_time_steps(P, rg, num)
+    out["cfl"] = np.array(0.7)
+    np.savez_compressed(HERE / f"bc_{kind}.npz", **out)
+    print("bc", kind, n, "cells,", len(keys), "residuals")
+    solve_fixture(f"{kind}_rk3", bc_case(kind), P,
+                  {"flux": "HLLC", "reconstruction": "MUSCL linear", "limiter": "Venkatakrishnan",
+                   "time_integration": "Explicit RK3", "cfl": 0.6}, 10, ref)
 
 
 def strip_case(nx=6, ny=2):
@@ -233,6 +335,10 @@ def main(only=None):
     ref = import_reference()
     if only == "parabolic":
         return parabolic_main(ref)
+    if only == "bc":
+        bc_fixture("pinlet", ref)
+        bc_fixture("massflow", ref)
+        return None
     riemann, riemann_p = riemann_case(16)
     residual_fixture("riemann16", riemann, ref)
     residual_fixture("periodic_mixed", periodic_case(8, 6, split="half", jitter=0.25, seed=2), ref)
