@@ -255,6 +255,14 @@ const double* mcfd_geom_primitive(const mcfd_geom* geom);
  * on the handle; NULL for k out of range.  Used to replay a step's stages in
  * reverse (no counterpart in the reference). */
 const double* mcfd_geom_stage_state(const mcfd_geom* geom, int32_t k);
+/* mcfd_explicit_step that also copies, for every stage k, the primitive state
+ * it evaluates the residual at into stage_P[k] ([n_cells][4]) and, for MUSCL,
+ * its face states into stage_recon[k] ([n_limiter][4], may be NULL): the
+ * linearisation points a reverse sweep needs (mcfd_vjp_at).  n_stages >= the
+ * scheme's stage count (1, 2, 3, 5).  No counterpart in the reference. */
+int mcfd_explicit_step_record(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, double* U,
+                              const double* dt, int32_t dt_per_cell, double* const* stage_P,
+                              double* const* stage_recon, int32_t n_stages, void* stream);
 
 /*
  * Sum over cells of R[i][k]^2 for k = 0..3 into the device array sums[4]
@@ -302,6 +310,10 @@ int mcfd_jvp(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const dou
  * [n_cells][4]. */
 int mcfd_vjp(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* lambda, double* U_bar,
              double* far_bar, void* stream);
+/* mcfd_vjp at a state whose primitive P and (MUSCL) face states recon the
+ * caller already has (from mcfd_explicit_step_record). */
+int mcfd_vjp_at(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* P, const double* recon,
+                const double* lambda, double* U_bar, double* far_bar, void* stream);
 /* Pressure force on the wall faces along (dir_x, dir_y): J = sum over wall
  * faces of p(owner) (n . dir) L, with n pointing out of the fluid cell; dJdU
  * (device [n_cells][4], may be NULL) receives dJ/dU.  J: host scalar. */

@@ -85,7 +85,10 @@ SIGNATURES = {
     "mcfd_explicit_step": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp]),
     "mcfd_geom_primitive": (c_vp, [c_vp]),
     "mcfd_geom_stage_state": (c_vp, [c_vp, C.c_int32]),
-    "mcfd_reconstruction": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_reconstruction": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_explicit_step_record": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp, c_vp, c_i32,
+                                          c_vp]),
+    "mcfd_vjp_at": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
     "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),

@@ -5,10 +5,11 @@ The forward run is the reference's RK3 step (solver.py:566-567, 676-678,
 754-756) with a fixed time step; the functional is the wall pressure force
 J = sum over wall faces of p (n . d) L at the final state (`mcfd_wall_force`).
 The adjoint walks the steps backwards with the transposed residual Jacobian
-(`mcfd_vjp`, three products per step), replaying each segment of
-``checkpoint_every`` steps from its stored state with the forward step and
-keeping the stage states it leaves (`mcfd_geom_stage_state`), so the
-linearisation points are the forward run's own, bit for bit.  For one step
+(`mcfd_vjp_at`, three products per step), replaying each segment of
+``checkpoint_every`` steps from its stored state with the forward step, which
+records every stage's state, primitive and face states
+(`mcfd_explicit_step_record`), so the linearisation points are the forward
+run's own, bit for bit.  For one step
 U1 = U + dt R(U), U2 = 3/4 U + 1/4 (U1 + dt R(U1)), U' = 1/3 U + 2/3 (U2 + dt R(U2)):
 
     l2 = 2/3 (l' + dt R(U2)^T l'),   l1 = 1/4 (l2 + dt R(U1)^T l2),
@@ -53,7 +54,8 @@ class WallForceAdjoint:
                  mode: str = "exact"):
         self.geom = geom
         self.cfg = make_config(settings, mode)
-        self.cfg_vjp = make_config(settings, "exact")
+        # the reverse sweep linearises at the forward step's own face states
+        self.cfg_vjp = make_config(settings, "exact" if mode == "fma" else mode)
         self.dt = float(dt)
         self.direction = direction
         self.k = int(checkpoint_every)
@@ -89,27 +91,38 @@ class WallForceAdjoint:
         return float(J[0]), dJ
 
     # --------------------------------------------------------------- reverse
-    def _vjp(self, U, lam, far_weight):
+    def _vjp(self, U, P, recon, lam, far_weight):
         lib = self.geom.lib
-        lib.check(lib.mcfd_vjp(self.geom.handle, C.byref(self.cfg_vjp), U.data_ptr(), lam.data_ptr(),
-                               self.W.data_ptr(), self.far.data_ptr(), _stream_ptr()), "mcfd_vjp")
+        lib.check(lib.mcfd_vjp_at(self.geom.handle, C.byref(self.cfg_vjp), U.data_ptr(), P.data_ptr(),
+                                  recon.data_ptr() if recon is not None else None, lam.data_ptr(),
+                                  self.W.data_ptr(), self.far.data_ptr(), _stream_ptr()), "mcfd_vjp_at")
         if far_weight:
             self.far_acc.add_(self.far, alpha=far_weight)
         return self.W
 
     def _replay(self, U):
-        """Advance U one step in place and return the step's stage states
-        (U1, U2) as copies of the handle's stage buffers."""
-        self.step(U)
-        lib, n = self.geom.lib, self.geom.n_cells
-        return tuple(_device_view(lib.mcfd_geom_stage_state(self.geom.handle, k), (n, 4), self.geom.device).clone()
-                     for k in (0, 1))
+        """Advance U one step in place; returns the step's stage states
+        (U0, U1, U2) and, per stage, the primitive and face states the
+        residual was evaluated at (the reverse sweep's linearisation points,
+        copied during the step)."""
+        g, lib, n = self.geom, self.geom.lib, self.geom.n_cells
+        dev = g.device
+        U0 = U.clone()
+        Ps = [torch.empty(n, 4, dtype=torch.float64, device=dev) for _ in range(3)]
+        recons = ([torch.empty(int(g.info.n_limiter), 4, dtype=torch.float64, device=dev) for _ in range(3)]
+                  if self.cfg.reconstruction != 0 else [None] * 3)
+        p_ptrs = (C.c_void_p * 3)(*[t.data_ptr() for t in Ps])
+        r_ptrs = (C.c_void_p * 3)(*[t.data_ptr() if t is not None else None for t in recons])
+        lib.check(lib.mcfd_explicit_step_record(g.handle, C.byref(self.cfg), 2, U.data_ptr(), self.dt_dev.data_ptr(),
+                                                0, p_ptrs, r_ptrs, 3, _stream_ptr()), "mcfd_explicit_step_record")
+        U1, U2 = (_device_view(lib.mcfd_geom_stage_state(g.handle, k), (n, 4), dev).clone() for k in (0, 1))
+        return (U0, U1, U2), Ps, recons
 
     def backward(self, lam_final: torch.Tensor) -> torch.Tensor:
         """Adjoint of the initial state; the far-field-state gradient per
         far-field face accumulates in ``self.far_acc``.  Each segment is
         replayed from its checkpoint with the forward step, keeping every
-        step's three stage states (3 x checkpoint_every states at most)."""
+        step's stage states and their primitive and face states."""
         dt = self.dt
         lam = lam_final.clone()
         self.far_acc.zero_()
@@ -117,22 +130,18 @@ class WallForceAdjoint:
             start = seg * self.k
             end = min(start + self.k, self.steps)
             U = self.checkpoints[seg].clone()
-            stages = []
-            for _ in range(start, end):
-                U0 = U.clone()
-                U1, U2 = self._replay(U)
-                stages.append((U0, U1, U2))
-            for U0, U1, U2 in reversed(stages):
-                w = self._vjp(U2, lam, (2.0 / 3.0) * dt)
+            records = [self._replay(U) for _ in range(start, end)]
+            for (U0, U1, U2), Ps, recons in reversed(records):
+                w = self._vjp(U2, Ps[2], recons[2], lam, (2.0 / 3.0) * dt)
                 lam2 = (2.0 / 3.0) * (lam + dt * w)
                 new = (1.0 / 3.0) * lam
-                w = self._vjp(U1, lam2, 0.25 * dt)
+                w = self._vjp(U1, Ps[1], recons[1], lam2, 0.25 * dt)
                 lam1 = 0.25 * (lam2 + dt * w)
                 new += 0.75 * lam2
-                w = self._vjp(U0, lam1, dt)
+                w = self._vjp(U0, Ps[0], recons[0], lam1, dt)
                 new += lam1 + dt * w
                 lam = new
-            del stages
+            del records
         self.geom.check_status()
         return lam
 

@@ -29,7 +29,7 @@ UNITS = [
     ("mcfd_kernels_common.cu", ["-fmad=false"]),
     ("mcfd_implicit.cu", ["-fmad=false"]),
     ("mcfd_jvp.cu", ["-fmad=false"]),
-    ("mcfd_vjp.cu", ["-fmad=false"]),
+    ("mcfd_vjp.cu", ["-fmad=true"]),
     ("mcfd_parabolic.cu", ["-fmad=false"]),
     ("mcfd_boundary.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),

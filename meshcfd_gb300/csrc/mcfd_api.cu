@@ -38,6 +38,10 @@ struct mcfd_geom {
   JvpWork jvp;                 // tangent workspace (allocated on first use)
   VjpWork vjp;                 // adjoint workspace (allocated on first use)
   std::vector<void*> jvp_owned;
+  // mcfd_explicit_step_record: per-stage copies of the primitive and face states
+  double* const* rec_P = nullptr;
+  double* const* rec_recon = nullptr;
+  int rec_n = 0, rec_k = 0;
 };
 
 namespace {
@@ -121,6 +125,13 @@ static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgra
   if (e == cudaSuccess && h->g.n_bc_patches > 0) {
     const double* recon = cfg.reconstruction == MCFD_RECON_FIRST_ORDER ? nullptr : h->ws.recon;
     e = timed(h, MCFD_PROF_FLUX, s, [&] { return launch_bc_states(h->g, cfg, h->ws.P, recon, h->g.bc_ext, s); });
+  }
+  if (e == cudaSuccess && h->rec_P && h->rec_k < h->rec_n) {  // mcfd_explicit_step_record
+    const int k = h->rec_k++;
+    e = cudaMemcpyAsync(h->rec_P[k], h->ws.P, 4 * sizeof(double) * (size_t)h->g.n_cells, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && h->rec_recon && h->rec_recon[k] && cfg.reconstruction != MCFD_RECON_FIRST_ORDER)
+      e = cudaMemcpyAsync(h->rec_recon[k], h->ws.recon, 4 * sizeof(double) * (size_t)h->g.n_slots,
+                          cudaMemcpyDeviceToDevice, s);
   }
   if (e == cudaSuccess)
     e = timed(h, MCFD_PROF_FLUX, s, [&] { return MCFD_DISPATCH(cfg, launch_flux(h->g, cfg, h->ws.P, h->ws.recon, h->ws.flux, s)); });
@@ -662,6 +673,25 @@ int mcfd_reconstruction(mcfd_geom* h, const mcfd_config* cfg, const double* P, d
                   [&] { return launch_reconstruction_fields(h->g, *cfg, P, gradients, curvature, factors, s); }));
 }
 
+int mcfd_explicit_step_record(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U, const double* dt,
+                              int32_t dt_per_cell, double* const* stage_P, double* const* stage_recon,
+                              int32_t n_stages, void* stream) {
+  static const int kStages[4] = {1, 2, 3, 5};
+  if (!h || !stage_P || scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4 || n_stages < kStages[scheme])
+    return MCFD_E_ARG;
+  for (int k = 0; k < kStages[scheme]; ++k)
+    if (!stage_P[k]) return MCFD_E_ARG;
+  h->rec_P = stage_P;
+  h->rec_recon = stage_recon;
+  h->rec_n = n_stages;
+  h->rec_k = 0;
+  const int r = mcfd_explicit_step(h, cfg, scheme, U, dt, dt_per_cell, stream);
+  h->rec_P = nullptr;
+  h->rec_recon = nullptr;
+  h->rec_n = h->rec_k = 0;
+  return r;
+}
+
 const double* mcfd_geom_stage_state(const mcfd_geom* h, int32_t k) {
   return (h && k >= 0 && k < 4) ? h->ws.stage[k] : nullptr;
 }
@@ -911,7 +941,21 @@ int mcfd_vjp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   if (cfg->reconstruction != MCFD_RECON_FIRST_ORDER && !h->g.has_twins) return MCFD_E_UNSUPPORTED;
   if ((c = ensure_vjp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
-  return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return launch_vjp(h->g, *cfg, U, lambda, h->vjp, U_bar, far_bar, s); }));
+  return rc(timed(h, MCFD_PROF_OTHER, s,
+                  [&] { return launch_vjp(h->g, *cfg, U, nullptr, nullptr, lambda, h->vjp, U_bar, far_bar, s); }));
+}
+
+int mcfd_vjp_at(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double* P, const double* recon,
+                const double* lambda, double* U_bar, double* far_bar, void* stream) {
+  if (!h || !U || !P || !lambda || !U_bar) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0) return MCFD_E_UNSUPPORTED;
+  if (cfg->reconstruction != MCFD_RECON_FIRST_ORDER && (!h->g.has_twins || !recon)) return MCFD_E_UNSUPPORTED;
+  if ((c = ensure_vjp(h))) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  return rc(timed(h, MCFD_PROF_OTHER, s,
+                  [&] { return launch_vjp(h->g, *cfg, U, P, recon, lambda, h->vjp, U_bar, far_bar, s); }));
 }
 
 int mcfd_wall_force(mcfd_geom* h, const mcfd_config* cfg, const double* U, double dir_x, double dir_y, double* J,

@@ -138,6 +138,17 @@ MCFD_DECLARE_LAUNCHERS(fast)
 MCFD_DECLARE_LAUNCHERS(fma)
 #undef MCFD_DECLARE_LAUNCHERS
 
+// Launch shape of a face segment: 256-thread blocks when the segment fills
+// the 152 SMs, otherwise warp-multiple blocks spread over all SMs (a boundary
+// segment of a few thousand faces would sit on a handful of SMs).
+inline int seg_threads(int n) {
+  if (n >= 152 * 256) return 256;
+  int t = (n + 151) / 152;
+  t = ((t + 31) / 32) * 32;
+  return t < 32 ? 32 : (t > 256 ? 256 : t);
+}
+inline int seg_blocks(int n) { return (n + seg_threads(n) - 1) / seg_threads(n); }
+
 // variant-independent (mcfd_kernels_common.cu)
 long long launch_count();
 void count_launch(int n = 1);

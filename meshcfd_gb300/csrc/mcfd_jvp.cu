@@ -194,7 +194,7 @@ void flux_tangent_segments(const DevGeom& g, const double* P, const double* dP, 
 #define MCFD_SEG(SEGV)                                                                                     \
   {                                                                                                        \
     int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                                                     \
-    if (n > 0) count_launch(), k_flux_tangent<FLUX, SEGV, FO, KH><<<blocks_for(n), kBlock, 0, s>>>(        \
+    if (n > 0) count_launch(), k_flux_tangent<FLUX, SEGV, FO, KH><<<seg_blocks(n), seg_threads(n), 0, s>>>( \
                    g, P, dP, recon, drecon, dflux, gamma);                                                 \
   }
   MCFD_SEG(SEG_INTERIOR)

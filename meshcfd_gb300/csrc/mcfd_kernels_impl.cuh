@@ -480,7 +480,7 @@ static void flux_segments(const DevGeom& g, const double* P, const double* recon
 #define MCFD_SEG(SEGV)                                                              \
   {                                                                                 \
     int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                              \
-    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<blocks_for(n), kBlock, 0, s>>>(g, P, recon, flux, gamma, inv_gm1); \
+    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<seg_blocks(n), seg_threads(n), 0, s>>>(g, P, recon, flux, gamma, inv_gm1); \
   }
   MCFD_SEG(SEG_INTERIOR)
   MCFD_SEG(SEG_PERIODIC)

@@ -16,7 +16,8 @@
 //   through each entry's twin (b -> a for a -> b), then U_bar = (dP/dU)^T P_bar.
 // Switches (HLLC region, limiter band, extreme neighbour, min over entries)
 // follow the state's values: the result is the transpose of mcfd_jvp's
-// Jacobian to rounding.
+// Jacobian to rounding.  Compiled with FMA contraction and shared
+// reciprocals: derivatives need accuracy, not the reference's rounding.
 #include "mcfd_ad.cuh"
 #include "mcfd_internal.h"
 #include "mcfd_vjp.h"
@@ -32,6 +33,240 @@ __device__ __forceinline__ ad::Dual<N> seed(double v, int k) {
   ad::Dual<N> x(v);
   if (k >= 0) x.d[k] = 1.0;
   return x;
+}
+
+// ------------------------------------------------ hand-written reverse mode
+//
+// Reverse sweeps of the Rusanov and HLLC fluxes (the same expressions, branch
+// choices and Python min / max tie rules as mcfd_ad.cuh, so the result is
+// the transpose of the forward-mode Jacobian to rounding) at a fraction of
+// the cost of the 4x8 dual-number Jacobian.  qb accumulates.
+
+// physical_flux (euler.py:43-57): adjoints of F and of U = (r, r u, r v, E)
+__device__ __forceinline__ void physical_bar(const St4& q, double nx, double ny, double inv_gm1, const double Fb[4],
+                                             const double Ub[4], double qb[4]) {
+  const double r = q.a, u = q.b, v = q.c, p = q.d;
+  const double un = u * nx + v * ny;
+  const double E = p * inv_gm1 + 0.5 * r * (u * u + v * v);
+  const double unb = Fb[0] * r + Fb[1] * (r * u) + Fb[2] * (r * v) + Fb[3] * (E + p);
+  const double U1b = Fb[1] * un + Ub[1], U2b = Fb[2] * un + Ub[2], Eb = Fb[3] * un + Ub[3];
+  qb[0] += Fb[0] * un + Ub[0] + U1b * u + U2b * v + Eb * (0.5 * (u * u + v * v));
+  qb[1] += U1b * r + Eb * (r * u) + unb * nx;
+  qb[2] += U2b * r + Eb * (r * v) + unb * ny;
+  qb[3] += Fb[1] * nx + Fb[2] * ny + Fb[3] * un + Eb * inv_gm1;
+}
+
+// c = sqrt(gamma p / r): dc/dp = gamma / (2 r c), dc/dr = -c / (2 r)
+struct Sound {
+  double c, dp, dr;
+};
+__device__ __forceinline__ Sound sound_d(const St4& q, double gamma) {
+  const double inv_r = 1.0 / q.a;
+  const double c = sqrt(gamma * q.d * inv_r);
+  const double h = 0.5 * inv_r;
+  return Sound{c, gamma * h / c, -c * h};
+}
+
+__device__ __forceinline__ void rusanov_bar(const St4& L, const St4& R, double nx, double ny, double gamma,
+                                            double inv_gm1, const double Fb[4], double Lb[4], double Rb[4]) {
+  const double unl = L.b * nx + L.c * ny, unr = R.b * nx + R.c * ny;
+  const Sound sl_ = sound_d(L, gamma), sr_ = sound_d(R, gamma);
+  const double sl = fabs(unl) + sl_.c, sr = fabs(unr) + sr_.c;
+  const bool left = sl >= sr;
+  const double s = left ? sl : sr;
+  const double UL[4] = {L.a, L.a * L.b, L.a * L.c, L.d * inv_gm1 + 0.5 * L.a * (L.b * L.b + L.c * L.c)};
+  const double UR[4] = {R.a, R.a * R.b, R.a * R.c, R.d * inv_gm1 + 0.5 * R.a * (R.b * R.b + R.c * R.c)};
+  double FLb[4], ULb[4], URb[4], sb = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    FLb[k] = 0.5 * Fb[k];
+    sb -= 0.5 * Fb[k] * (UR[k] - UL[k]);
+    URb[k] = -0.5 * s * Fb[k];
+    ULb[k] = 0.5 * s * Fb[k];
+  }
+  physical_bar(L, nx, ny, inv_gm1, FLb, ULb, Lb);
+  physical_bar(R, nx, ny, inv_gm1, FLb, URb, Rb);
+  double* qb = left ? Lb : Rb;
+  const Sound& sd = left ? sl_ : sr_;
+  const double unb = (left ? unl : unr) < 0.0 ? -sb : sb;
+  qb[0] += sb * sd.dr;
+  qb[1] += unb * nx;
+  qb[2] += unb * ny;
+  qb[3] += sb * sd.dp;
+}
+
+template <bool KERNEL_BRANCHES>
+__device__ __forceinline__ void hllc_bar(const St4& L, const St4& R, double nx, double ny, double gamma,
+                                         double inv_gm1, const double Fb[4], double Lb[4], double Rb[4]) {
+  const double zero[4] = {0.0, 0.0, 0.0, 0.0};
+  const double unl = L.b * nx + L.c * ny, unr = R.b * nx + R.c * ny;
+  const Sound sl_ = sound_d(L, gamma), sr_ = sound_d(R, gamma);
+  const double cl = sl_.c, cr = sr_.c;
+  const double a1 = unl - cl, b1 = unr - cr;
+  const bool wl_right = b1 < a1;
+  const double wl = wl_right ? b1 : a1;
+  const double a2 = unl + cl, b2 = unr + cr;
+  const bool wr_right = b2 > a2;
+  const double wr = wr_right ? b2 : a2;
+  double den = L.a * (wl - unl) - R.a * (wr - unr);
+  const bool guarded = !(fabs(den) > 1e-14);
+  if (guarded) den = copysign(1e-14, den);
+  const double inv_den = 1.0 / den;
+  const double contact = ((R.d - L.d) + L.a * unl * (wl - unl) - R.a * unr * (wr - unr)) * inv_den;
+  int branch;
+  if (KERNEL_BRANCHES) {
+    if (wl >= 0.0) branch = 0;
+    else if (wr <= 0.0) branch = 3;
+    else branch = contact >= 0.0 ? 1 : 2;
+  } else {
+    if (wl >= 0.0) branch = 0;
+    else if (contact >= 0.0) branch = 1;
+    else if (wr > 0.0) branch = 2;
+    else branch = 3;
+  }
+  if (branch == 0) {
+    physical_bar(L, nx, ny, inv_gm1, Fb, zero, Lb);
+    return;
+  }
+  if (branch == 3) {
+    physical_bar(R, nx, ny, inv_gm1, Fb, zero, Rb);
+    return;
+  }
+  const bool left = branch == 1;
+  const St4& q = left ? L : R;
+  double* qb = left ? Lb : Rb;
+  const double un = left ? unl : unr, w = left ? wl : wr;
+  const double r = q.a, u = q.b, v = q.c, p = q.d;
+  const double inv_r = 1.0 / r;
+  const double E = p * inv_gm1 + 0.5 * r * (u * u + v * v);
+  const double Uq[4] = {r, r * u, r * v, E};
+  const double wu = w - un;
+  const double B = w - contact, inv_B = 1.0 / B, A = r * wu, factor = A * inv_B;
+  const double dc = contact - un;
+  const double sux = u + dc * nx, suy = v + dc * ny;
+  const double inv_Z = inv_r / wu;  // 1 / (r (w - un))
+  const double pz = p * inv_Z;
+  const double Y = contact + pz, Er = E * inv_r, X = Er + dc * Y;
+  const double star[4] = {factor, factor * sux, factor * suy, factor * X};
+  double wb = 0.0, Uqb[4], starb[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    wb += Fb[k] * (star[k] - Uq[k]);
+    starb[k] = w * Fb[k];
+    Uqb[k] = -w * Fb[k];
+  }
+  const double factorb = starb[0] + starb[1] * sux + starb[2] * suy + starb[3] * X;
+  const double suxb = starb[1] * factor, suyb = starb[2] * factor, Xb = starb[3] * factor;
+  double rb = -Xb * Er * inv_r, ub = suxb, vb = suyb, unb = 0.0, contactb = 0.0;
+  Uqb[3] += Xb * inv_r;
+  const double dcb = Xb * Y + suxb * nx + suyb * ny;
+  const double Yb = Xb * dc;
+  contactb += Yb;
+  const double pb = Yb * inv_Z;
+  const double Zb = -Yb * pz * inv_Z;
+  rb += Zb * wu;
+  wb += Zb * r;
+  unb -= Zb * r;
+  contactb += dcb;
+  unb -= dcb;
+  const double Ab = factorb * inv_B, Bb = -factorb * factor * inv_B;
+  rb += Ab * wu;
+  wb += Ab * r;
+  unb -= Ab * r;
+  wb += Bb;
+  contactb -= Bb;
+  physical_bar(q, nx, ny, inv_gm1, Fb, Uqb, qb);
+  qb[0] += rb;
+  qb[1] += ub + unb * nx;
+  qb[2] += vb + unb * ny;
+  qb[3] += pb;
+  double unlb = 0.0, unrb = 0.0, wlb = left ? wb : 0.0, wrb = left ? 0.0 : wb, clb = 0.0, crb = 0.0;
+  const double numb = contactb * inv_den, denb = guarded ? 0.0 : -contactb * contact * inv_den;
+  Rb[3] += numb;
+  Lb[3] -= numb;
+  Lb[0] += numb * unl * (wl - unl) + denb * (wl - unl);
+  unlb += numb * (L.a * (wl - unl) - L.a * unl) - denb * L.a;
+  wlb += numb * (L.a * unl) + denb * L.a;
+  Rb[0] -= numb * unr * (wr - unr) + denb * (wr - unr);
+  unrb -= numb * (R.a * (wr - unr) - R.a * unr) - denb * R.a;
+  wrb -= numb * (R.a * unr) + denb * R.a;
+  if (wl_right) {
+    unrb += wlb;
+    crb -= wlb;
+  } else {
+    unlb += wlb;
+    clb -= wlb;
+  }
+  if (wr_right) {
+    unrb += wrb;
+    crb += wrb;
+  } else {
+    unlb += wrb;
+    clb += wrb;
+  }
+  Lb[0] += clb * sl_.dr;
+  Lb[3] += clb * sl_.dp;
+  Rb[0] += crb * sr_.dr;
+  Rb[3] += crb * sr_.dp;
+  Lb[1] += unlb * nx;
+  Lb[2] += unlb * ny;
+  Rb[1] += unrb * nx;
+  Rb[2] += unrb * ny;
+}
+
+// Face VJP by the hand-written reverse (Rusanov / HLLC on every segment but
+// the far field, whose ghost state keeps the dual-number path).
+template <int FLUX, int SEG, bool FO, bool KH>
+__global__ void __launch_bounds__(kBlock) k_vjp_face_rev(DevGeom g, const double* __restrict__ P,
+                                                         const double* __restrict__ recon,
+                                                         const double* __restrict__ lambda, double gamma,
+                                                         double* __restrict__ slot_bar) {
+  const int begin = g.seg_begin[SEG];
+  const int f = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= g.seg_begin[SEG + 1]) return;
+  const double2 n = g.ff_normal[f];
+  const double len = g.ff_len[f];
+  const int lc = g.ff_lcell[f];
+  const St4 la = ld4(lambda + 4 * (size_t)lc);
+  const double wl = -len / g.area[lc];
+  double fb[4] = {wl * la.a, wl * la.b, wl * la.c, wl * la.d};
+  if (SEG == SEG_INTERIOR || SEG == SEG_PERIODIC) {
+    const St4 lb = ld4(lambda + 4 * (size_t)g.ff_rcell[f]);
+    const double wr = len / g.area[g.ff_rcell[f]];
+    fb[0] += wr * lb.a; fb[1] += wr * lb.b; fb[2] += wr * lb.c; fb[3] += wr * lb.d;
+  }
+  const St4 L = FO ? ld4(P + 4 * (size_t)lc) : ld4(recon + 4 * (size_t)g.ff_lslot[f]);
+  St4 R;
+  double2 wv = make_double2(0.0, 0.0);
+  if (SEG == SEG_INTERIOR || SEG == SEG_PERIODIC) {
+    R = FO ? ld4(P + 4 * (size_t)g.ff_rcell[f]) : ld4(recon + 4 * (size_t)g.ff_rslot[f]);
+  } else if (SEG == SEG_WALL) {
+    wv = g.ff_wall_velocity[f - begin];
+    const double un = (L.b - wv.x) * n.x + (L.c - wv.y) * n.y;
+    R = St4{L.a, L.b - 2.0 * un * n.x, L.c - 2.0 * un * n.y, L.d};
+  } else if (SEG == SEG_VIN) {
+    R = ld4(g.ff_vin_state + 4 * (size_t)(f - begin));
+  } else {
+    R = St4{L.a, L.b, L.c, g.ff_pout_pressure[f - begin]};
+  }
+  double Lb[4] = {0.0, 0.0, 0.0, 0.0}, Rb[4] = {0.0, 0.0, 0.0, 0.0};
+  const double inv_gm1 = 1.0 / (gamma - 1.0);
+  if (FLUX == MCFD_FLUX_RUSANOV) rusanov_bar(L, R, n.x, n.y, gamma, inv_gm1, fb, Lb, Rb);
+  else hllc_bar<(SEG == SEG_INTERIOR) && KH>(L, R, n.x, n.y, gamma, inv_gm1, fb, Lb, Rb);
+  if (SEG == SEG_WALL) {  // R = mirror(L)
+    const double unb = -2.0 * (Rb[1] * n.x + Rb[2] * n.y);
+    Lb[0] += Rb[0];
+    Lb[1] += Rb[1] + unb * n.x;
+    Lb[2] += Rb[2] + unb * n.y;
+    Lb[3] += Rb[3];
+  } else if (SEG == SEG_POUT) {
+    Lb[0] += Rb[0];
+    Lb[1] += Rb[1];
+    Lb[2] += Rb[2];
+  }
+  st4(slot_bar + 4 * (size_t)g.ff_lslot[f], St4{Lb[0], Lb[1], Lb[2], Lb[3]});
+  if (SEG == SEG_INTERIOR || SEG == SEG_PERIODIC)
+    st4(slot_bar + 4 * (size_t)g.ff_rslot[f], St4{Rb[0], Rb[1], Rb[2], Rb[3]});
 }
 
 template <int FLUX, int SEG, bool FO, bool KH>
@@ -93,13 +328,13 @@ __device__ __forceinline__ double limiter_slope(double r) {
   if (LIMITER <= 1) return r < 1.0 ? 1.0 : 0.0;
   if (LIMITER == 2) {
     if (!(r > 0.0)) return 0.0;
-    const double q = 2.0 * r / (1.0 + r);
-    return q < 1.0 ? 2.0 / ((1.0 + r) * (1.0 + r)) : 0.0;
+    return r < 1.0 ? 2.0 / ((1.0 + r) * (1.0 + r)) : 0.0;  // 2r / (1 + r) < 1 iff r < 1
   }
   const double eps = 1e-12;
   const double N = r * r + 2.0 * r + eps, D = r * r + r + 2.0 + eps;
-  if (N / D > 1.0) return 0.0;
-  return ((2.0 * r + 2.0) * D - N * (2.0 * r + 1.0)) / (D * D);
+  if (N > D) return 0.0;  // capped at 1
+  const double inv_D = 1.0 / D;
+  return ((2.0 * r + 2.0) * D - N * (2.0 * r + 1.0)) * (inv_D * inv_D);
 }
 
 template <int LIMITER, bool FO>
@@ -134,14 +369,46 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
         if (icmp::lt(hi[v], qv[v])) { hi[v] = qv[v]; hi_e[v] = e; }
       }
     }
+    // phi = min over entries of f(max(r, 0)), arg = its first entry.  Every
+    // limiter f is nondecreasing in r and correctly rounded division is
+    // monotone, so among entries with a positive increment the smallest
+    // factor sits at the largest increment, among negative ones at the most
+    // negative; entries inside the tolerance band give f(1).  Three
+    // candidates per variable instead of a division per entry.
     double phi[4] = {1.0, 1.0, 1.0, 1.0};
     int arg[4] = {-1, -1, -1, -1};
-    for (int s = s0; s < s1; ++s) {
-      const double2 dd = g.lim_d[s];
+    {
+      double tol[4], pmax[4], nmin[4];
+      int ps[4] = {-1, -1, -1, -1}, ns[4] = {-1, -1, -1, -1}, fs[4] = {-1, -1, -1, -1};
       for (int v = 0; v < 4; ++v) {
-        const double inc = gx[v] * dd.x + gy[v] * dd.y;
-        const double f = limiter_face_factor<LIMITER>(pv[v], inc, lo[v], hi[v], limiter_tolerance(pv[v]));
-        if (icmp::lt_nonneg(f, phi[v])) { phi[v] = f; arg[v] = s; }
+        tol[v] = limiter_tolerance(pv[v]);
+        pmax[v] = 0.0;
+        nmin[v] = 0.0;
+      }
+      for (int s = s0; s < s1; ++s) {
+        const double2 dd = g.lim_d[s];
+        for (int v = 0; v < 4; ++v) {
+          const double inc = gx[v] * dd.x + gy[v] * dd.y;
+          if (icmp::gt_pos(inc, tol[v])) {
+            if (ps[v] < 0 || inc > pmax[v]) { pmax[v] = inc; ps[v] = s; }
+          } else if (icmp::neg_gt_pos(inc, tol[v])) {
+            if (ns[v] < 0 || inc < nmin[v]) { nmin[v] = inc; ns[v] = s; }
+          } else if (fs[v] < 0) {
+            fs[v] = s;
+          }
+        }
+      }
+      for (int v = 0; v < 4; ++v) {
+        const int cand[3] = {ps[v], ns[v], fs[v]};
+        const double cinc[3] = {pmax[v], nmin[v], 0.0};
+        for (int k = 0; k < 3; ++k) {
+          if (cand[k] < 0) continue;
+          const double f = limiter_face_factor<LIMITER>(pv[v], cinc[k], lo[v], hi[v], tol[v]);
+          if (icmp::lt_nonneg(f, phi[v]) || (f == phi[v] && arg[v] >= 0 && cand[k] < arg[v])) {
+            phi[v] = f;
+            arg[v] = cand[k];
+          }
+        }
       }
     }
     // reverse of Q_s = P + phi (G . r_s)
@@ -167,11 +434,12 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
       const bool pos = icmp::gt_pos(inc, tol), neg = icmp::neg_gt_pos(inc, tol);
       if (!(pos || neg)) continue;
       const double num = pos ? hi[v] - pv[v] : lo[v] - pv[v];
-      const double r = num / inc;
+      const double inv_inc = 1.0 / inc;
+      const double r = num * inv_inc;
       if (!(r > 0.0)) continue;
       const double rb = limiter_slope<LIMITER>(r) * phib[v];
-      const double numb = rb / inc;
-      const double incb = -rb * r / inc;
+      const double numb = rb * inv_inc;
+      const double incb = -numb * r;
       pb[v] -= numb;
       const int ee = pos ? hi_e[v] : lo_e[v];
       if (ee < 0) pb[v] += numb;  // the extreme is the cell itself
@@ -273,8 +541,15 @@ void face_segments(const DevGeom& g, const double* P, const double* recon, const
 #define MCFD_SEG(SEGV)                                                                                          \
   {                                                                                                             \
     int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                                                          \
-    if (n > 0) count_launch(), k_vjp_face<FLUX, SEGV, FO, KH><<<blocks_for(n), kBlock, 0, s>>>(                 \
-                   g, P, recon, lambda, gamma, slot_bar, far_bar);                                              \
+    if (n > 0) {                                                                                                \
+      count_launch();                                                                                           \
+      if (FLUX != MCFD_FLUX_ROE && SEGV != SEG_FAR)                                                             \
+        k_vjp_face_rev<(FLUX == MCFD_FLUX_ROE ? MCFD_FLUX_HLLC : FLUX), SEGV, FO, KH>                           \
+            <<<seg_blocks(n), seg_threads(n), 0, s>>>(g, P, recon, lambda, gamma, slot_bar);                    \
+      else                                                                                                      \
+        k_vjp_face<FLUX, SEGV, FO, KH><<<seg_blocks(n), seg_threads(n), 0, s>>>(g, P, recon, lambda, gamma,     \
+                                                                                slot_bar, far_bar);             \
+    }                                                                                                           \
   }
   MCFD_SEG(SEG_INTERIOR)
   MCFD_SEG(SEG_PERIODIC)
@@ -287,42 +562,51 @@ void face_segments(const DevGeom& g, const double* P, const double* recon, const
 
 }  // namespace
 
-cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U, const double* lambda,
-                       const VjpWork& w, double* ubar, double* far_bar, cudaStream_t s) {
+cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U, const double* P_in,
+                       const double* recon_in, const double* lambda, const VjpWork& w, double* ubar,
+                       double* far_bar, cudaStream_t s) {
   const int C = g.n_cells;
   const bool fo = cfg.reconstruction == MCFD_RECON_FIRST_ORDER;
   if (!fo && !g.has_twins) return cudaErrorNotSupported;
-  cudaError_t e = exact::launch_primitive(g, cfg, U, w.P, s);
-  if (e == cudaSuccess && !fo) e = exact::launch_reconstruct(g, cfg, w.P, w.recon, s);
+  // face states as the forward step of the same mode computes them (the fast
+  // kernel's limiter minimum equals the exact one; fma would not), unless
+  // the caller recorded them during the forward step
+  const double* P = P_in ? P_in : w.P;
+  const double* recon = recon_in ? recon_in : w.recon;
+  cudaError_t e = cudaSuccess;
+  if (!P_in) e = exact::launch_primitive(g, cfg, U, w.P, s);
+  if (e == cudaSuccess && !fo && !recon_in)
+    e = cfg.mode == MCFD_MODE_FAST ? fast::launch_reconstruct(g, cfg, P, w.recon, s)
+                                   : exact::launch_reconstruct(g, cfg, P, w.recon, s);
   if (e != cudaSuccess) return e;
   cudaMemsetAsync(w.slot_bar, 0, 4 * sizeof(double) * (size_t)g.n_slots, s);
   const bool kh = cfg.reconstruction != MCFD_RECON_MUSCL_PARABOLIC;
   switch (cfg.flux) {
     case MCFD_FLUX_RUSANOV:
-      if (fo) face_segments<0, true, false>(g, w.P, w.recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else face_segments<0, false, false>(g, w.P, w.recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      if (fo) face_segments<0, true, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      else face_segments<0, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
       break;
     case MCFD_FLUX_HLLC:
-      if (fo) face_segments<1, true, true>(g, w.P, w.recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else if (kh) face_segments<1, false, true>(g, w.P, w.recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else face_segments<1, false, false>(g, w.P, w.recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      if (fo) face_segments<1, true, true>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      else if (kh) face_segments<1, false, true>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      else face_segments<1, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
       break;
     default:
-      if (fo) face_segments<2, true, false>(g, w.P, w.recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else face_segments<2, false, false>(g, w.P, w.recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      if (fo) face_segments<2, true, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      else face_segments<2, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
       break;
   }
   count_launch(2);
   const double ax = cfg.acceleration_x, ay = cfg.acceleration_y;
   if (fo) {
-    k_vjp_cell<0, true><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar);
+    k_vjp_cell<0, true><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar);
     k_vjp_collect<true><<<blocks_for(C), kBlock, 0, s>>>(g, U, w.pbar, w.ent_bar, cfg.gamma, ubar);
   } else {
     switch (cfg.limiter) {
-      case 0: k_vjp_cell<0, false><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
-      case 1: k_vjp_cell<1, false><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
-      case 2: k_vjp_cell<2, false><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
-      default: k_vjp_cell<3, false><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
+      case 0: k_vjp_cell<0, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
+      case 1: k_vjp_cell<1, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
+      case 2: k_vjp_cell<2, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
+      default: k_vjp_cell<3, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
     }
     k_vjp_collect<false><<<blocks_for(C), kBlock, 0, s>>>(g, U, w.pbar, w.ent_bar, cfg.gamma, ubar);
   }

@@ -14,7 +14,10 @@ struct VjpWork {
   double* partials = nullptr;  // reduction scratch [608 block sums + 8]
 };
 
-cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U, const double* lambda,
+// P_in / recon_in: primitive and face states of U when the caller has them
+// (null: computed here)
+cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U, const double* P_in,
+                       const double* recon_in, const double* lambda,
                        const VjpWork& w, double* ubar, double* far_bar, cudaStream_t s);
 cudaError_t launch_wall_force(const DevGeom& g, const mcfd_config& cfg, const double* U, double dx, double dy,
                               const VjpWork& w, double* J_dev, double* dJdU, cudaStream_t s);

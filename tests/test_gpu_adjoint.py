@@ -203,3 +203,36 @@ def test_checkpoint_interval_does_not_change_the_gradient(cuda_device):
     J = WallForceFunction.apply(Ux, WallForceAdjoint(dg, case.numerics, dt, checkpoint_every=4), STEPS)
     (g0,) = torch.autograd.grad(2.0 * J, Ux)
     assert torch.equal(g0, 2.0 * lams[0])
+
+
+def test_recorded_step_and_vjp_at_match_plain_calls(cuda_device):
+    """mcfd_explicit_step_record advances exactly like mcfd_explicit_step and
+    records each stage's primitive and face states; mcfd_vjp_at at those
+    states equals mcfd_vjp bit for bit."""
+    from meshcfd_gb300.device import DeviceGeometry, make_config
+    from oracle.oracle import Oracle
+
+    case, g, P0, _ = _ogrid()
+    U0 = torch.as_tensor(Oracle(g).conservative(P0, 1.4), device=cuda_device)
+    dg = DeviceGeometry(g)
+    cfg = make_config(case.numerics)
+    dt = torch.full((1,), _dt(g, case, P0), dtype=torch.float64, device=cuda_device)
+    n, nl = dg.n_cells, int(dg.info.n_limiter)
+    Ps = [torch.empty(n, 4, dtype=torch.float64, device=cuda_device) for _ in range(3)]
+    Rs = [torch.empty(nl, 4, dtype=torch.float64, device=cuda_device) for _ in range(3)]
+    Ua, Ub = U0.clone(), U0.clone()
+    dg.explicit_step(Ua, cfg, 2, dt)
+    stream = torch.cuda.current_stream().cuda_stream
+    assert dg.lib.mcfd_explicit_step_record(dg.handle, C.byref(cfg), 2, Ub.data_ptr(), dt.data_ptr(), 0,
+                                            (C.c_void_p * 3)(*[t.data_ptr() for t in Ps]),
+                                            (C.c_void_p * 3)(*[t.data_ptr() for t in Rs]), 3, stream) == 0
+    dg.check_status()
+    assert torch.equal(Ua, Ub)
+    assert torch.equal(Ps[0], dg.primitive(U0, cfg))
+    lam = torch.as_tensor(np.random.default_rng(3).standard_normal((n, 4)), device=cuda_device)
+    a, b = torch.empty_like(lam), torch.empty_like(lam)
+    assert dg.lib.mcfd_vjp(dg.handle, C.byref(cfg), U0.data_ptr(), lam.data_ptr(), a.data_ptr(), None, stream) == 0
+    assert dg.lib.mcfd_vjp_at(dg.handle, C.byref(cfg), U0.data_ptr(), Ps[0].data_ptr(), Rs[0].data_ptr(),
+                              lam.data_ptr(), b.data_ptr(), None, stream) == 0
+    dg.check_status()
+    assert torch.equal(a, b)
