@@ -18,6 +18,7 @@ single-threaded CPU path) on the host cores for the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import os
@@ -45,6 +46,9 @@ def parse():
     ap.add_argument("--workload", default="vortex1024",
                     choices=("vortex1024", "vortex1024all", "vortex512", "vortex256", "batch256", "adjoint"))
     ap.add_argument("--checkpoint-every", type=int, default=20)
+    ap.add_argument("--batch-adjoint-steps", type=int, default=20)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--batch-adjoint-checkpoint", type=int, default=5)
     ap.add_argument("--batch-cases", type=int, default=256)
     ap.add_argument("--graph-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
@@ -243,9 +247,9 @@ def run_gpu(args):
     native = _lib.native()
     dg = DeviceGeometry(g, device)
     C = dg.n_cells
-    from oracle.oracle import Oracle  # only to build the seeded initial conservative state
+    from meshcfd_gb300.device import primitive_to_conservative
 
-    U_init = Oracle(g).conservative(P0, settings.gamma)
+    U_init = primitive_to_conservative(P0, settings.gamma)
     U = torch.as_tensor(U_init, device=device)
     dt = torch.empty(1, dtype=torch.float64, device=device)
     P = dg.primitive_buffer()
@@ -255,6 +259,8 @@ def run_gpu(args):
         dg.time_steps(P, cfg, out_min=dt)
         dg.explicit_step(U, cfg, 2, dt)
 
+    dg.primitive(U, cfg, out=P)
+    tuned = dg.autotune(U, cfg) if not args.no_autotune else None
     dg.primitive(U, cfg, out=P)
     for _ in range(args.warmup):
         step()
@@ -418,6 +424,7 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded vortex mesh and state)",
             "config": config, "gpu_launches": int(launches), "roofline": roofline, "kernels": kernels,
+            "autotune": tuned,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clock, "parity": parity, "mode": args.mode,
             "variants": variants,
         }
@@ -436,19 +443,20 @@ def run_batch(args):
     from meshcfd_gb300.batch import BatchStepper, batch_workload, build_batch
     from meshcfd_gb300.device import DeviceGeometry
     from meshcfd_gb300.solver import run_explicit
-    from oracle.oracle import Oracle
+    from meshcfd_gb300.device import primitive_to_conservative
 
     device = torch.device("cuda", 0)
     t0 = time.perf_counter()
     cases = batch_workload(n_cases=args.batch_cases)
     geo, layout, P0, geoms = build_batch(cases)
     settings = cases[0][0].numerics
-    U0 = Oracle(geo).conservative(P0, settings.gamma)
+    U0 = primitive_to_conservative(P0, settings.gamma)
     dg = DeviceGeometry(geo, device)
     setup_s = time.perf_counter() - t0
     steps = args.steps
     stepper = BatchStepper(dg, layout, settings, mode=args.mode)
     U = torch.as_tensor(U0, device=device)
+    tuned = dg.autotune(U, stepper.cfg) if not args.no_autotune else None
     gsteps = max(1, min(args.graph_steps, steps))
     stepper.capture(U, gsteps)
     for _ in range(max(1, args.warmup // gsteps)):
@@ -485,6 +493,9 @@ def run_batch(args):
                for k in range(layout.n_cases))
     n_cells = int(dg.n_cells)
     value = layout.n_cases * done_steps / (batched_ms * 1e-3)
+    adjoint = None
+    if args.batch_adjoint_steps > 0:
+        adjoint = batched_adjoint(dg, layout, settings, U0, stepper, args)
     line = {
         "metric": "batched case-steps/s (RK3 HLLC-MUSCL, 256 uneven cases)", "value": value, "unit": "case-steps/s",
         "n_gpus": 1, "steps": done_steps, "warmup": args.warmup, "ms_per_step": batched_ms / done_steps,
@@ -497,8 +508,49 @@ def run_batch(args):
         "one_at_a_time": {"case_steps_per_s": layout.n_cases * done_steps / (single_ms * 1e-3), "ms": single_ms},
         "batched_over_one_at_a_time": single_ms / batched_ms,
         "bit_identical": bool(same), "clocks": clocks.summary(),
+        "batched_adjoint": adjoint, "autotune": tuned,
     }
     print(json.dumps(line))
+
+
+def batched_adjoint(dg, layout, settings, U0, stepper, args):
+    """Every case's wall-force gradient (the y force on its slip walls) by one
+    checkpointed RK3 adjoint over the whole batch: each case keeps its own
+    fixed time step (the stable step of its initial state), so the steps are
+    per cell."""
+    import torch
+
+    from meshcfd_gb300.adjoint import WallForceAdjoint
+
+    device = dg.device
+    U = torch.as_tensor(U0, device=device)
+    stepper_dt = stepper.dt_cells
+    P = dg.primitive(U, stepper.cfg, out=dg.primitive_buffer())
+    dg.lib.check(dg.lib.mcfd_batch_time_steps(dg.handle, C.byref(stepper.cfg), P.data_ptr(),
+                                              stepper.offsets.data_ptr(), layout.n_cases,
+                                              stepper.dt_case.data_ptr(), stepper_dt.data_ptr(),
+                                              torch.cuda.current_stream().cuda_stream), "mcfd_batch_time_steps")
+    dt_cells = stepper_dt.clone()
+    steps, every = args.batch_adjoint_steps, args.batch_adjoint_checkpoint
+    # the channels' walls are horizontal: the wall force along y
+    adj = WallForceAdjoint(dg, settings, dt_cells, direction=(0.0, 1.0), checkpoint_every=every, mode=args.mode,
+                           case_offsets=layout.cell_offsets)
+    adj.gradient(U, min(2, steps))  # warm-up
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    UN = adj.forward(U, steps)
+    ev[1].record()
+    J, dJ = adj.functional(UN)
+    lam0 = adj.backward(dJ)
+    ev[2].record()
+    torch.cuda.synchronize()
+    J_cases = adj.functional_per_case(UN)
+    fwd, bwd = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    return {"steps": steps, "checkpoint_every": every, "forward_ms": fwd, "adjoint_ms": bwd,
+            "adjoint_over_forward": bwd / fwd,
+            "cases_gradients_per_s": layout.n_cases / ((fwd + bwd) * 1e-3),
+            "sum_of_case_forces": float(np.sum(J_cases)), "J_total": J, "grad_norm": float(lam0.norm())}
 
 
 def run_adjoint(args):
@@ -514,8 +566,8 @@ def run_adjoint(args):
     from meshcfd_gb300.adjoint import WallForceAdjoint
     from meshcfd_gb300.device import DeviceGeometry
     from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.device import make_config, primitive_to_conservative
     from meshcfd_gb300.meshes import ogrid_case
-    from oracle.oracle import Oracle
 
     device = torch.device("cuda", 0)
     steps = args.steps if args.steps != 100 else 400
@@ -524,13 +576,13 @@ def run_adjoint(args):
     g = build_geometry(case.mesh, case)
     setup_s = time.perf_counter() - t0
     settings = case.numerics
-    orc = Oracle(g)
-    U0h = orc.conservative(P0, settings.gamma)
-    dt = 0.9 * float(orc.stable_time_steps(P0, settings).min())
+    U0 = torch.as_tensor(primitive_to_conservative(P0, settings.gamma), device=device)
     dg = DeviceGeometry(g, device)
+    cfg = make_config(settings, args.mode)
+    _, dt_min = dg.time_steps(dg.primitive(U0, cfg), cfg)
+    dt = 0.9 * float(dt_min)
     adj = WallForceAdjoint(dg, settings, dt, direction=(1.0, 0.0), checkpoint_every=args.checkpoint_every,
                            mode=args.mode)
-    U0 = torch.as_tensor(U0h, device=device)
     for _ in range(max(1, args.warmup)):  # warm-up: a short forward + adjoint
         adj.gradient(U0, min(steps, args.checkpoint_every + 1))
     torch.cuda.synchronize()

@@ -255,6 +255,14 @@ const double* mcfd_geom_primitive(const mcfd_geom* geom);
  * on the handle; NULL for k out of range.  Used to replay a step's stages in
  * reverse (no counterpart in the reference). */
 const double* mcfd_geom_stage_state(const mcfd_geom* geom, int32_t k);
+/* Choose the launch shapes of the stage kernels for this geometry and
+ * settings by timing candidates on the state U (device [n_cells][4]):
+ * reconstruction and gather threads per block in {64, 128, 256}, flux
+ * threads in {64, 128, 256} x faces per thread in {1, 2, 4}.  The choice
+ * stays with the handle; chosen (host [4]) receives reconstruction threads,
+ * flux threads, flux faces per thread, gather threads (0: default).
+ * Synchronises the stream.  No counterpart in the reference. */
+int mcfd_autotune(mcfd_geom* geom, const mcfd_config* cfg, const double* U, int32_t* chosen, void* stream);
 /* mcfd_explicit_step that also copies, for every stage k, the primitive state
  * it evaluates the residual at into stage_P[k] ([n_cells][4]) and, for MUSCL,
  * its face states into stage_recon[k] ([n_limiter][4], may be NULL): the

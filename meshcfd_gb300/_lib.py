@@ -89,6 +89,7 @@ SIGNATURES = {
     "mcfd_explicit_step_record": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp, c_vp, c_i32,
                                           c_vp]),
     "mcfd_vjp_at": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_autotune": (c_i32, [c_vp, C.POINTER(Config), c_vp, C.POINTER(c_i32), c_vp]),
     "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
     "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),

@@ -48,19 +48,36 @@ class ResidualFunction(torch.autograd.Function):
 
 
 class WallForceAdjoint:
-    """Forward RK3 with checkpoints and the reverse sweep for one geometry."""
+    """Forward RK3 with checkpoints and the reverse sweep for one geometry.
 
-    def __init__(self, geom: DeviceGeometry, settings, dt: float, direction=(1.0, 0.0), checkpoint_every: int = 20,
-                 mode: str = "exact"):
+    ``dt``: one fixed time step, or a CUDA tensor of per-cell steps (a batch
+    of cases, each with its own step).  With ``case_offsets`` (cell offsets
+    of the cases of a batch) :meth:`functional_per_case` gives every case's
+    wall force; the gradient of their sum restricted to a case's cells is
+    that case's gradient, because the cases do not interact."""
+
+    def __init__(self, geom: DeviceGeometry, settings, dt, direction=(1.0, 0.0), checkpoint_every: int = 20,
+                 mode: str = "exact", case_offsets=None):
         self.geom = geom
         self.cfg = make_config(settings, mode)
         # the reverse sweep linearises at the forward step's own face states
         self.cfg_vjp = make_config(settings, "exact" if mode == "fma" else mode)
-        self.dt = float(dt)
+        dev = geom.device
+        if isinstance(dt, torch.Tensor):
+            if dt.shape != (geom.n_cells,) or dt.dtype != torch.float64 or not dt.is_cuda:
+                raise ValueError("per-cell dt must be a CUDA float64 tensor of shape (n_cells,)")
+            self.per_cell = True
+            self.dt_dev = dt.contiguous()
+            self.dt = self.dt_dev.view(-1, 1)
+            self.far_dt = self.dt_dev[geom.far_owner].view(-1, 1)
+        else:
+            self.per_cell = False
+            self.dt = float(dt)
+            self.dt_dev = torch.full((1,), self.dt, dtype=torch.float64, device=dev)
+            self.far_dt = self.dt
         self.direction = direction
         self.k = int(checkpoint_every)
-        dev = geom.device
-        self.dt_dev = torch.full((1,), self.dt, dtype=torch.float64, device=dev)
+        self.case_offsets = None if case_offsets is None else np.asarray(case_offsets, dtype=np.int64)
         self.W = torch.empty(geom.n_cells, 4, dtype=torch.float64, device=dev)
         self.far = torch.zeros(max(geom.n_far_field, 1), 4, dtype=torch.float64, device=dev)
         self.far_acc = torch.zeros_like(self.far)
@@ -70,6 +87,14 @@ class WallForceAdjoint:
     # ---------------------------------------------------------------- forward
     def step(self, U):
         self.geom.explicit_step(U, self.cfg, 2, self.dt_dev)
+
+    def functional_per_case(self, U) -> np.ndarray:
+        """The wall force of every case (``case_offsets``) at state U."""
+        g = self.geom
+        P = g.primitive(U, self.cfg)
+        w = g.wall_normal_length[:, 0] * self.direction[0] + g.wall_normal_length[:, 1] * self.direction[1]
+        lengths = torch.as_tensor(np.diff(self.case_offsets), device=g.device)
+        return torch.segment_reduce(P[:, 3] * w, "sum", lengths=lengths).cpu().numpy()
 
     def forward(self, U0: torch.Tensor, steps: int) -> torch.Tensor:
         U = U0.clone()
@@ -91,13 +116,18 @@ class WallForceAdjoint:
         return float(J[0]), dJ
 
     # --------------------------------------------------------------- reverse
-    def _vjp(self, U, P, recon, lam, far_weight):
+    def _vjp(self, U, P, recon, lam, coef):
+        """W = R'(U)^T lam; the far-field-state gradient accumulates with
+        weight coef dt (dt of each far face's owner cell)."""
         lib = self.geom.lib
         lib.check(lib.mcfd_vjp_at(self.geom.handle, C.byref(self.cfg_vjp), U.data_ptr(), P.data_ptr(),
                                   recon.data_ptr() if recon is not None else None, lam.data_ptr(),
                                   self.W.data_ptr(), self.far.data_ptr(), _stream_ptr()), "mcfd_vjp_at")
-        if far_weight:
-            self.far_acc.add_(self.far, alpha=far_weight)
+        if self.geom.n_far_field:
+            if self.per_cell:
+                self.far_acc.addcmul_(self.far, self.far_dt, value=coef)
+            else:
+                self.far_acc.add_(self.far, alpha=coef * self.dt)
         return self.W
 
     def _replay(self, U):
@@ -114,7 +144,8 @@ class WallForceAdjoint:
         p_ptrs = (C.c_void_p * 3)(*[t.data_ptr() for t in Ps])
         r_ptrs = (C.c_void_p * 3)(*[t.data_ptr() if t is not None else None for t in recons])
         lib.check(lib.mcfd_explicit_step_record(g.handle, C.byref(self.cfg), 2, U.data_ptr(), self.dt_dev.data_ptr(),
-                                                0, p_ptrs, r_ptrs, 3, _stream_ptr()), "mcfd_explicit_step_record")
+                                                int(self.per_cell), p_ptrs, r_ptrs, 3, _stream_ptr()),
+                  "mcfd_explicit_step_record")
         U1, U2 = (_device_view(lib.mcfd_geom_stage_state(g.handle, k), (n, 4), dev).clone() for k in (0, 1))
         return (U0, U1, U2), Ps, recons
 
@@ -132,13 +163,13 @@ class WallForceAdjoint:
             U = self.checkpoints[seg].clone()
             records = [self._replay(U) for _ in range(start, end)]
             for (U0, U1, U2), Ps, recons in reversed(records):
-                w = self._vjp(U2, Ps[2], recons[2], lam, (2.0 / 3.0) * dt)
+                w = self._vjp(U2, Ps[2], recons[2], lam, 2.0 / 3.0)
                 lam2 = (2.0 / 3.0) * (lam + dt * w)
                 new = (1.0 / 3.0) * lam
-                w = self._vjp(U1, Ps[1], recons[1], lam2, 0.25 * dt)
+                w = self._vjp(U1, Ps[1], recons[1], lam2, 0.25)
                 lam1 = 0.25 * (lam2 + dt * w)
                 new += 0.75 * lam2
-                w = self._vjp(U0, Ps[0], recons[0], lam1, dt)
+                w = self._vjp(U0, Ps[0], recons[0], lam1, 1.0)
                 new += lam1 + dt * w
                 lam = new
             del records

@@ -158,6 +158,8 @@ class BatchStepper:
     """Explicit steps of a batch with one global time step per case."""
 
     def __init__(self, dg: DeviceGeometry, layout: BatchLayout, settings, mode: str = "fast"):
+        """The stage kernels' launch shapes can be tuned for the batch with
+        ``dg.autotune(U, stepper.cfg)`` before :meth:`capture`."""
         self.dg = dg
         self.layout = layout
         self.cfg = make_config(settings, mode)

@@ -692,6 +692,78 @@ int mcfd_explicit_step_record(mcfd_geom* h, const mcfd_config* cfg, int32_t sche
   return r;
 }
 
+int mcfd_autotune(mcfd_geom* h, const mcfd_config* cfg, const double* U, int32_t* chosen, void* stream) {
+  if (!h || !U || !chosen) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, h->ws.P, s));
+  if (e != cudaSuccess) return MCFD_E_CUDA;
+  cudaEvent_t a = take_event(h), b = take_event(h);
+  // mean time of 3 launches after one warm-up
+  auto time_ms = [&](auto&& launch) -> float {
+    launch();
+    cudaEventRecord(a, s);
+    for (int r = 0; r < 3; ++r) launch();
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms / 3.0f;
+  };
+  static const int kThreads[3] = {64, 128, 256};
+  static const int kFaces[3] = {1, 2, 4};
+  DevGeom& g = h->g;
+  const bool muscl = cfg->reconstruction == MCFD_RECON_MUSCL_LINEAR;
+  auto recon = [&] {
+    if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC)
+      launch_reconstruct_parabolic(g, *cfg, h->ws.P, h->ws.recon, s);
+    else if (muscl)
+      MCFD_DISPATCH(*cfg, launch_reconstruct(g, *cfg, h->ws.P, h->ws.recon, s));
+  };
+  int best_recon = 0, best_flux_t = 0, best_flux_f = 1, best_gather = 0;
+  if (muscl) {
+    float best = 1e30f;
+    for (int t : kThreads) {
+      g.tune_recon_threads = t;
+      const float ms = time_ms(recon);
+      if (ms < best) best = ms, best_recon = t;
+    }
+    g.tune_recon_threads = best_recon;
+  }
+  recon();
+  {
+    float best = 1e30f;
+    for (int t : kThreads)
+      for (int f : kFaces) {
+        g.tune_flux_threads = t;
+        g.tune_flux_faces = f;
+        const float ms = time_ms([&] { MCFD_DISPATCH(*cfg, launch_flux(g, *cfg, h->ws.P, h->ws.recon, h->ws.flux, s)); });
+        if (ms < best) best = ms, best_flux_t = t, best_flux_f = f;
+      }
+    g.tune_flux_threads = best_flux_t;
+    g.tune_flux_faces = best_flux_f;
+  }
+  {
+    StageProgram prog{};
+    prog.out_r = h->ws.saved_r;
+    float best = 1e30f;
+    for (int t : kThreads) {
+      g.tune_gather_threads = t;
+      const float ms = time_ms([&] { MCFD_DISPATCH(*cfg, launch_gather(g, *cfg, h->ws.P, h->ws.flux, prog, s)); });
+      if (ms < best) best = ms, best_gather = t;
+    }
+    g.tune_gather_threads = best_gather;
+  }
+  h->event_pool.push_back(a);
+  h->event_pool.push_back(b);
+  chosen[0] = best_recon;
+  chosen[1] = best_flux_t;
+  chosen[2] = best_flux_f;
+  chosen[3] = best_gather;
+  return rc(cudaGetLastError());
+}
+
 const double* mcfd_geom_stage_state(const mcfd_geom* h, int32_t k) {
   return (h && k >= 0 && k < 4) ? h->ws.stage[k] : nullptr;
 }

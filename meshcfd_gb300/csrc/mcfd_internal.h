@@ -87,6 +87,8 @@ struct DevGeom {
   const double* dt_len;
   const int* dt_info;  // kind << 28 | index into the BC arrays
   DevStatus* status;
+  // launch shapes chosen by mcfd_autotune (0: the defaults)
+  int tune_recon_threads, tune_flux_threads, tune_flux_faces, tune_gather_threads;
 };
 
 // One term of an explicit stage combination, evaluated left to right.
@@ -148,6 +150,16 @@ inline int seg_threads(int n) {
   return t < 32 ? 32 : (t > 256 ? 256 : t);
 }
 inline int seg_blocks(int n) { return (n + seg_threads(n) - 1) / seg_threads(n); }
+// flux launch shape with the autotuned threads / faces per thread, if any
+inline int flux_threads(const DevGeom& g, int n) {
+  return g.tune_flux_threads && n >= 152 * g.tune_flux_threads ? g.tune_flux_threads : seg_threads(n);
+}
+inline int flux_blocks(const DevGeom& g, int n) {
+  const int t = flux_threads(g, n);
+  const int per_block = t * (g.tune_flux_threads && n >= 152 * g.tune_flux_threads && g.tune_flux_faces > 1
+                                 ? g.tune_flux_faces : 1);
+  return (n + per_block - 1) / per_block;
+}
 
 // variant-independent (mcfd_kernels_common.cu)
 long long launch_count();

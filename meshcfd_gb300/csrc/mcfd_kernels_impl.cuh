@@ -260,9 +260,9 @@ __global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __rest
                                                  const double* __restrict__ recon,
                                                  double* __restrict__ flux, double gamma,
                                                  double inv_gm1) {
-  const int begin = g.seg_begin[SEG];
-  const int f = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= g.seg_begin[SEG + 1]) return;
+  const int begin = g.seg_begin[SEG], end = g.seg_begin[SEG + 1];
+  // grid-stride: the autotuner may give each thread several faces
+  for (int f = begin + blockIdx.x * blockDim.x + threadIdx.x; f < end; f += gridDim.x * blockDim.x) {
   const double2 n = g.ff_normal[f];
   const St4 L = FIRST_ORDER ? ld4(P + 4 * (size_t)g.ff_lcell[f]) : ld4(recon + 4 * (size_t)g.ff_lslot[f]);
   St4 R;
@@ -287,6 +287,7 @@ __global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __rest
   bits |= numerical_flux<FLUX, (SEG == SEG_INTERIOR) && KERNEL_HLLC>(L, R, n.x, n.y, gamma, inv_gm1, out);
   if (bits) flag_face(g.status, bits, f);
   st4(flux + 4 * (size_t)f, St4{out[0], out[1], out[2], out[3]});
+  }
 }
 
 // ------------------------------------------------------------ gather + stage
@@ -453,21 +454,22 @@ cudaError_t launch_primitive(const DevGeom& g, const mcfd_config& cfg, const dou
 cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const double* P,
                                double* recon, cudaStream_t s) {
   if (g.n_cells == 0) return cudaSuccess;
-  const int b = blocks_for(g.n_cells);
+  const int t = g.tune_recon_threads ? g.tune_recon_threads : kBlock;
+  const int b = (g.n_cells + t - 1) / t;
   count_launch();
   if constexpr (kFast || kMinRatio) {
     switch (cfg.limiter) {
-      case 0: k_reconstruct_fast<0><<<b, kBlock, 0, s>>>(g, P, recon); break;
-      case 1: k_reconstruct_fast<1><<<b, kBlock, 0, s>>>(g, P, recon); break;
-      case 2: k_reconstruct_fast<2><<<b, kBlock, 0, s>>>(g, P, recon); break;
-      default: k_reconstruct_fast<3><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      case 0: k_reconstruct_fast<0><<<b, t, 0, s>>>(g, P, recon); break;
+      case 1: k_reconstruct_fast<1><<<b, t, 0, s>>>(g, P, recon); break;
+      case 2: k_reconstruct_fast<2><<<b, t, 0, s>>>(g, P, recon); break;
+      default: k_reconstruct_fast<3><<<b, t, 0, s>>>(g, P, recon); break;
     }
   } else {
     switch (cfg.limiter) {
-      case 0: k_reconstruct<0><<<b, kBlock, 0, s>>>(g, P, recon); break;
-      case 1: k_reconstruct<1><<<b, kBlock, 0, s>>>(g, P, recon); break;
-      case 2: k_reconstruct<2><<<b, kBlock, 0, s>>>(g, P, recon); break;
-      default: k_reconstruct<3><<<b, kBlock, 0, s>>>(g, P, recon); break;
+      case 0: k_reconstruct<0><<<b, t, 0, s>>>(g, P, recon); break;
+      case 1: k_reconstruct<1><<<b, t, 0, s>>>(g, P, recon); break;
+      case 2: k_reconstruct<2><<<b, t, 0, s>>>(g, P, recon); break;
+      default: k_reconstruct<3><<<b, t, 0, s>>>(g, P, recon); break;
     }
   }
   return cudaGetLastError();
@@ -480,7 +482,7 @@ static void flux_segments(const DevGeom& g, const double* P, const double* recon
 #define MCFD_SEG(SEGV)                                                              \
   {                                                                                 \
     int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                              \
-    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<seg_blocks(n), seg_threads(n), 0, s>>>(g, P, recon, flux, gamma, inv_gm1); \
+    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<flux_blocks(g, n), flux_threads(g, n), 0, s>>>(g, P, recon, flux, gamma, inv_gm1); \
   }
   MCFD_SEG(SEG_INTERIOR)
   MCFD_SEG(SEG_PERIODIC)
@@ -520,7 +522,9 @@ cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* 
 cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double* P,
                           const double* flux, const StageProgram& prog, cudaStream_t s) {
   if (g.n_cells > 0)
-    count_launch(), k_gather<<<blocks_for(g.n_cells), kBlock, 0, s>>>(g, P, flux, cfg.gamma, cfg.acceleration_x,
+    count_launch(), k_gather<<<(g.n_cells + (g.tune_gather_threads ? g.tune_gather_threads : kBlock) - 1) /
+                                   (g.tune_gather_threads ? g.tune_gather_threads : kBlock),
+                               g.tune_gather_threads ? g.tune_gather_threads : kBlock, 0, s>>>(g, P, flux, cfg.gamma, cfg.acceleration_x,
                                                       cfg.acceleration_y, prog);
   return cudaGetLastError();
 }

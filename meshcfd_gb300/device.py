@@ -51,6 +51,15 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
     return cfg
 
 
+def primitive_to_conservative(primitive, gamma: float) -> np.ndarray:
+    """Host conversion (rho, u, v, p) -> (rho, rho u, rho v, E) in the
+    reference's expression order (euler.py:8-17)."""
+    P = np.asarray(primitive, dtype=np.float64)
+    rho, u, v, p = P.T
+    E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)
+    return np.column_stack((rho, rho * u, rho * v, E))
+
+
 def _stream_ptr(stream=None) -> int:
     s = stream if stream is not None else torch.cuda.current_stream()
     return s.cuda_stream
@@ -135,6 +144,16 @@ class DeviceGeometry:
         self.n_interior = int(info.n_interior)
         self.n_far_field = int(d.n_far_field)
         self.areas = torch.as_tensor(keep["areas"], device=self.device)
+        owners = keep["owners"]
+        # owner cell of every far-field face and the wall-force weight of
+        # every cell, sum over its wall / symmetry faces of n L (the adjoint's
+        # per-cell time steps and per-case functionals)
+        self.far_owner = torch.as_tensor(owners[keep["far_field_faces"]], device=self.device)
+        wall = keep["wall_faces"]
+        normals = keep["face_normals"].reshape(-1, 2)
+        wn = np.zeros((n_cells, 2))
+        np.add.at(wn, owners[wall], normals[wall] * keep["face_lengths"][wall, None])
+        self.wall_normal_length = torch.as_tensor(wn, device=self.device)
         self._dt_min = torch.empty(1, dtype=torch.float64, device=self.device)
 
     # ------------------------------------------------------------- lifetime
@@ -189,6 +208,16 @@ class DeviceGeometry:
                                                     curv.data_ptr() if curv is not None else None, fac.data_ptr(),
                                                     _stream_ptr()), "mcfd_reconstruction")
         return grad, curv, fac
+
+    def autotune(self, U: torch.Tensor, cfg) -> dict:
+        """Time the stage kernels' launch shapes on state U and keep the
+        fastest for this handle (mcfd_autotune)."""
+        _check_state(U, self.n_cells, "U")
+        chosen = (C.c_int32 * 4)()
+        self.lib.check(self.lib.mcfd_autotune(self.handle, C.byref(cfg), U.data_ptr(), chosen, _stream_ptr()),
+                       "mcfd_autotune")
+        return {"reconstruct_threads": chosen[0], "flux_threads": chosen[1], "flux_faces_per_thread": chosen[2],
+                "gather_threads": chosen[3]}
 
     def primitive_buffer(self) -> torch.Tensor:
         """The handle's primitive buffer as a tensor view (valid after a

@@ -74,3 +74,46 @@ def test_batch_steps_equal_single_case_steps(cuda_device):
         s.max_iterations = 5
         run_explicit(single, s, Uk, mode="fast", final_residual=False)
         np.testing.assert_array_equal(Uk.cpu().numpy(), Ub[a:b])
+
+
+@pytest.mark.gpu
+def test_batched_adjoint_equals_single_case_adjoints(cuda_device):
+    """One reverse sweep over the concatenated batch gives every case its own
+    wall-force gradient, bit for bit what the case's own adjoint gives (each
+    case with its own fixed time step, per-cell in the batch)."""
+    import torch
+    from meshcfd_gb300.adjoint import WallForceAdjoint
+    from meshcfd_gb300.device import DeviceGeometry
+    from oracle.oracle import Oracle
+
+    cases, (geo, layout, P0, geoms) = _small_batch()
+    s = cases[0][0].numerics
+    U0 = Oracle(geo).conservative(P0, s.gamma)
+    off = layout.cell_offsets
+    dts = []
+    for k, g in enumerate(geoms):
+        orc = Oracle(g)
+        dts.append(0.5 * float(orc.stable_time_steps(orc.primitive(U0[off[k]:off[k + 1]], s.gamma), s).min()))
+    dt_cells = torch.as_tensor(np.repeat(dts, np.diff(off)), device=cuda_device)
+    steps, every = 9, 4
+    d = (0.0, 1.0)  # the channels' walls are horizontal
+    adj = WallForceAdjoint(DeviceGeometry(geo), s, dt_cells, direction=d, checkpoint_every=every, mode="fast",
+                           case_offsets=off)
+    U = torch.as_tensor(U0, device=cuda_device)
+    UN = adj.forward(U, steps)
+    J_cases = adj.functional_per_case(UN)
+    _, dJ = adj.functional(UN)
+    lam = adj.backward(dJ).cpu().numpy()
+    far = adj.far_acc.cpu().numpy()
+    far_start = 0
+    for k, g in enumerate(geoms):
+        single = WallForceAdjoint(DeviceGeometry(g), s, dts[k], direction=d, checkpoint_every=every, mode="fast")
+        Jk, lam_k, far_k = single.gradient(torch.as_tensor(U0[off[k]:off[k + 1]], device=cuda_device), steps)
+        assert abs(Jk) > 1e-3 and float(np.abs(lam_k.cpu().numpy()).max()) > 1e-6
+        np.testing.assert_array_equal(lam[off[k]:off[k + 1]], lam_k.cpu().numpy())
+        nf = len(g.far_field_faces)
+        # far-field weights: dt per face owner in the batch, a scalar alone
+        # (another rounding order of the same products)
+        assert np.abs(far[far_start:far_start + nf] - far_k[:nf]).max() <= 1e-13 * np.abs(far_k[:nf]).max()
+        far_start += nf
+        assert abs(J_cases[k] - Jk) <= 1e-12 * abs(Jk)

@@ -294,3 +294,27 @@ def test_fast_mode_is_bit_exact_for_min_limiters(cuda_device, kind, n, flux, lim
             np.testing.assert_array_equal(R, ref)
         else:
             assert rel_err(R, ref) <= 1e-15
+
+
+def test_autotuned_launch_shapes_give_identical_results(cuda_device):
+    """mcfd_autotune only changes launch shapes: every face and cell is
+    computed by the same code, so results are bit-identical."""
+    import torch
+    from meshcfd_gb300.device import DeviceGeometry, make_config
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import cell_centroids, vortex_case, vortex_primitive
+    from oracle.oracle import Oracle
+
+    case, _ = vortex_case(128, split="half")
+    s = case.numerics
+    s.flux, s.reconstruction, s.limiter = "HLLC", "MUSCL linear", "Venkatakrishnan"
+    g = build_geometry(case.mesh, case)
+    U0 = torch.as_tensor(Oracle(g).conservative(vortex_primitive(cell_centroids(case.mesh)), s.gamma),
+                         device=cuda_device)
+    dg = DeviceGeometry(g)
+    cfg = make_config(s, "fast")
+    before = dg.residual(U0, cfg).clone()
+    chosen = dg.autotune(U0, cfg)
+    assert chosen["reconstruct_threads"] in (64, 128, 256) and chosen["gather_threads"] in (64, 128, 256)
+    assert chosen["flux_threads"] in (64, 128, 256) and chosen["flux_faces_per_thread"] in (1, 2, 4)
+    assert torch.equal(dg.residual(U0, cfg), before)
