@@ -59,6 +59,17 @@ class MassFlowInlet:
 
 
 @dataclass(frozen=True)
+class WallThermalBoundary:
+    """Mirror of ``_WallThermalBoundary`` (solver.py:106-111)."""
+
+    faces: np.ndarray
+    condition: str
+    value: float
+    patch_name: str
+    mechanical_condition: str
+
+
+@dataclass(frozen=True)
 class MassFlowOutlet:
     """Mirror of ``_MassFlowOutlet`` (solver.py:99-103)."""
 
@@ -116,6 +127,10 @@ class Geometry:
     parabolic_dx: np.ndarray = field(default_factory=lambda: np.empty(0))
     parabolic_dy: np.ndarray = field(default_factory=lambda: np.empty(0))
     periodic_shifts: np.ndarray = field(default_factory=lambda: np.empty((0, 2)))
+    # viscous terms (solver.py:1817-1820, 1886-1922): every non-periodic
+    # boundary face in face order, and the walls' thermal / mechanical data
+    diffusive_boundary_faces: np.ndarray = field(default_factory=lambda: np.empty(0, dtype=np.int64))
+    wall_thermal_boundaries: tuple = ()
 
 
 # ----------------------------------------------------------------- helpers
@@ -384,6 +399,7 @@ def build_geometry(mesh: FiniteVolumeMesh, case) -> Geometry:
     pout_faces, pout_pressures = [], []
     far_faces, far_states = [], []
     pressure_inlets, mass_flow_inlets, mass_flow_outlets = [], [], []
+    wall_thermal = []
     boundary_patch = patch_ids[boundary_faces]
     for pid, condition in conditions.items():
         fids = boundary_faces[boundary_patch == pid]
@@ -399,10 +415,22 @@ def build_geometry(mesh: FiniteVolumeMesh, case) -> Geometry:
             vin_faces.append(fids)
             vin_states.append(np.tile((density, vx, vy, pressure), (len(fids), 1)))
         elif condition.kind == "Wall":
-            if case.numerics.viscosity_model != "Inviscid":
-                raise SolverError("Viscous walls are not supported by the GPU residual path.")
             if condition.mechanical_condition == "Prescribed velocity":
                 raise SolverError("Prescribed-velocity walls need the reference geometry (expression evaluation).")
+            if case.numerics.viscosity_model != "Inviscid":
+                mechanical = condition.mechanical_condition
+                if mechanical not in ("Slip", "No-slip", "Prescribed velocity"):
+                    raise SolverError(f"Unsupported mechanical condition on wall '{name}'.")
+                thermal = condition.thermal_condition
+                if thermal == "Temperature":
+                    value = _positive_boundary_value(condition.values.get("temperature", 300.0),
+                                                     f"Wall temperature for '{name}'")
+                elif thermal == "Heat Flux":
+                    value = _finite_boundary_value(condition.values.get("heat_flux", 0.0),
+                                                   f"Wall heat flux for '{name}'")
+                else:
+                    raise SolverError(f"Unsupported thermal condition on wall '{name}'.")
+                wall_thermal.append(WallThermalBoundary(fids, thermal, value, name, mechanical))
         elif condition.kind == "Pressure Outlet":
             pressure = _positive_boundary_value(condition.values.get("pressure", 101325.0), f"Static pressure for outlet '{name}'")
             pout_faces.append(fids)
@@ -528,6 +556,8 @@ def build_geometry(mesh: FiniteVolumeMesh, case) -> Geometry:
         parabolic_dx=parabolic[2],
         parabolic_dy=parabolic[3],
         periodic_shifts=shifts,
+        diffusive_boundary_faces=boundary_faces[not_periodic].astype(np.int64),
+        wall_thermal_boundaries=tuple(wall_thermal),
     )
 
 

@@ -987,7 +987,8 @@ done:
 }
 
 /* _stable_time_steps (solver.py:4132-4343), inviscid */
-int orc_stable_time_steps(const orc_geom* g, const orc_settings* s, const double* P, double* dt) {
+int orc_stable_time_steps(const orc_geom* g, const orc_settings* s, const double* P, const double* diffusion,
+                          double* dt) {
   int64_t C = g->n_cells, F = g->n_faces;
   double gamma = s->gamma;
   int status = 0;
@@ -1037,6 +1038,9 @@ int orc_stable_time_steps(const orc_geom* g, const orc_settings* s, const double
     double r = fabs(P[4 * nb + 1] * g->face_normals[2 * f] + P[4 * nb + 2] * g->face_normals[2 * f + 1]) + cs[nb];
     sum[nb] += r * g->face_lengths[f];
   }
+  /* viscous terms: spectral_sum += 2 * diffusion_sum (solver.py:4331) */
+  if (diffusion)
+    for (int64_t c = 0; c < C; ++c) sum[c] += 2.0 * diffusion[c];
   for (int64_t c = 0; c < C; ++c) {
     dt[c] = s->cfl * g->areas[c] / sum[c];
     if (!isfinite(dt[c]) || dt[c] <= 0.0) status |= ORC_TIME_STEP;

@@ -92,7 +92,7 @@ def lib():
     if _lib is None:
         _lib = C.CDLL(str(build()))
         _lib.orc_residual.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), PD, PD]
-        _lib.orc_stable_time_steps.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), PD, PD]
+        _lib.orc_stable_time_steps.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), PD, PD, PD]
         _lib.orc_explicit_step.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), C.c_int, PD, PD, C.c_int]
         _lib.orc_conservative_to_primitive.argtypes = [C.c_int64, PD, C.c_double, PD]
         _lib.orc_primitive_to_conservative.argtypes = [C.c_int64, PD, C.c_double, PD]
@@ -209,6 +209,8 @@ class Oracle:
         self.struct = s
         self._keep = keep
         self.n_cells = n_cells
+        self.geometry = g
+        self._divergence = None
 
     @staticmethod
     def settings(num) -> OrcSettings:
@@ -236,11 +238,45 @@ class Oracle:
         lib().orc_primitive_to_conservative(len(P), P.ctypes.data_as(PD), gamma, U.ctypes.data_as(PD))
         return U
 
+    def divergence(self, flux):
+        """interior_divergence_operator @ flux (solver.py:2160-2174), SciPy CSR
+        as the reference builds it."""
+        if self._divergence is None:
+            from scipy.sparse import coo_matrix
+
+            g = self.geometry
+            faces = np.asarray(g.interior_faces)
+            o, n = np.asarray(g.owners)[faces], np.asarray(g.neighbours)[faces]
+            L, A = np.asarray(g.face_lengths)[faces], np.asarray(g.areas)
+            ids = np.arange(len(faces))
+            self._divergence = coo_matrix((np.concatenate((-L / A[o], L / A[n])),
+                                           (np.concatenate((o, n)), np.concatenate((ids, ids)))),
+                                          shape=(self.n_cells, len(faces))).tocsr()
+        return self._divergence @ flux
+
     def residual(self, U, num):
         U = np.ascontiguousarray(U, dtype=np.float64)
         R = np.empty_like(U)
+        viscous = getattr(num, "viscosity_model", "Inviscid") != "Inviscid"
         s = self.settings(num)
-        _raise(lib().orc_residual(C.byref(self.struct), C.byref(s), U.ctypes.data_as(PD), R.ctypes.data_as(PD)))
+        if viscous:  # body force after the viscous terms (solver.py:2699-2715)
+            s.acceleration_x = s.acceleration_y = 0.0
+        code = lib().orc_residual(C.byref(self.struct), C.byref(s), U.ctypes.data_as(PD), R.ctypes.data_as(PD))
+        if not viscous:
+            _raise(code)
+            return R
+        _raise(code & ~0x02)
+        from .viscous import viscous_residual
+
+        P = self.primitive(U, num.gamma)
+        R = R + viscous_residual(P, self.geometry, num, self, self.divergence)
+        ax, ay = num.acceleration_x, num.acceleration_y
+        if ax != 0.0 or ay != 0.0:
+            R[:, 1] += P[:, 0] * ax
+            R[:, 2] += P[:, 0] * ay
+            R[:, 3] += P[:, 0] * (ax * P[:, 1] + ay * P[:, 2])
+        if not np.isfinite(R).all():
+            _raise(0x02)
         return R
 
     def gradients_and_factors(self, P, limiter):
@@ -275,10 +311,19 @@ class Oracle:
         P = np.ascontiguousarray(P, dtype=np.float64)
         dt = np.empty(len(P))
         s = self.settings(num)
-        _raise(lib().orc_stable_time_steps(C.byref(self.struct), C.byref(s), P.ctypes.data_as(PD), dt.ctypes.data_as(PD)))
+        diff = None
+        if getattr(num, "viscosity_model", "Inviscid") != "Inviscid":
+            from .viscous import diffusion_sum
+
+            diff = np.ascontiguousarray(diffusion_sum(P, self.geometry, num))
+        _raise(lib().orc_stable_time_steps(C.byref(self.struct), C.byref(s), P.ctypes.data_as(PD),
+                                           diff.ctypes.data_as(PD) if diff is not None else None,
+                                           dt.ctypes.data_as(PD)))
         return dt
 
     def explicit_step(self, U, num, dt):
+        if getattr(num, "viscosity_model", "Inviscid") != "Inviscid":
+            return self._explicit_step_python(U, num, dt)
         U = np.array(U, dtype=np.float64, order="C", copy=True)
         dt_arr = np.ascontiguousarray(np.atleast_1d(np.asarray(dt, dtype=np.float64)))
         s = self.settings(num)
@@ -286,6 +331,30 @@ class Oracle:
                                        U.ctypes.data_as(PD), dt_arr.ctypes.data_as(PD), int(dt_arr.size > 1))
         _raise(code)
         return U
+
+    def _explicit_step_python(self, U, num, dt):
+        """The explicit stage combinations (solver.py:532-756) around
+        :meth:`residual` (for settings the C step does not cover)."""
+        U0 = np.array(U, dtype=np.float64, copy=True)
+        d = np.asarray(dt, dtype=np.float64)
+        d = d[:, None] if d.ndim == 1 and d.size > 1 else float(d.reshape(-1)[0])
+        scheme = SCHEME[num.time_integration]
+        if scheme == 3:
+            raise NotImplementedError("oracle: viscous SSPRK(5,4) step")
+        U1 = U0 + d * self.residual(U0, num)
+        if scheme == 0:
+            self.primitive(U1, num.gamma)
+            return U1
+        self.primitive(U1, num.gamma)
+        if scheme == 1:
+            out = 0.5 * U0 + 0.5 * (U1 + d * self.residual(U1, num))
+            self.primitive(out, num.gamma)
+            return out
+        U2 = 0.75 * U0 + 0.25 * (U1 + d * self.residual(U1, num))
+        self.primitive(U2, num.gamma)
+        out = (1.0 / 3.0) * U0 + (2.0 / 3.0) * (U2 + d * self.residual(U2, num))
+        self.primitive(out, num.gamma)
+        return out
 
     def solve(self, U, num, steps, time=0.0, history=None):
         """The reference's explicit loop (solver.py:437-806) for ``steps`` steps:

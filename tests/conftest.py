@@ -33,11 +33,31 @@ def load_fixture(name):
             else:
                 b = types.SimpleNamespace(faces=faces, mass_flow=float(v[0]), patch_name=str(pname))
             patches[int(kind)].append(b)
+    walls = []
+    if "wt_offsets" in data:
+        off = data["wt_offsets"]
+        for k in range(len(off) - 1):
+            walls.append(types.SimpleNamespace(faces=data["wt_faces"][off[k]:off[k + 1]],
+                                               condition=str(data["wt_condition"][k]), value=float(data["wt_value"][k]),
+                                               patch_name=str(data["wt_names"][k]),
+                                               mechanical_condition=str(data["wt_mechanical"][k])))
+    kinds = {}
+    if "patch_kind_ids" in data:
+        kinds = {int(i): str(n) for i, n in zip(data["patch_kind_ids"], data["patch_kind_names"])}
     geom = types.SimpleNamespace(
         **{k[5:]: v for k, v in data.items() if k.startswith("geom_")},
         pressure_inlets=tuple(patches[0]), mass_flow_inlets=tuple(patches[1]), mass_flow_outlets=tuple(patches[2]),
+        wall_thermal_boundaries=tuple(walls), patch_kinds=kinds,
     )
     return data, geom
+
+
+def viscous_settings_for(key, data):
+    """Settings of a viscous fixture key R|flux|recon|limiter|force|model."""
+    s = settings_for("|".join(key.split("|")[:5]))
+    s.viscosity_model = key.split("|")[5]
+    s.dynamic_viscosity = float(data["dynamic_viscosity"])
+    return s
 
 
 def fixture_mesh(data):

@@ -231,6 +231,109 @@ def bc_fixture(kind, ref):
                    "time_integration": "Explicit RK3", "cfl": 0.6}, 10, ref)
 
 
+def viscous_case(kind):
+    """Cases for the laminar viscous terms.  "noslip": no-slip walls with
+    fixed temperature (bottom) and heat flux (top), velocity inlet, pressure
+    outlet, constant viscosity 0.01 (R T = 1 units).  "mixed": slip wall
+    with heat flux (top), symmetry (bottom), far field (left), mass-flow
+    outlet (right).  "periodic": periodic box in SI units (air at ~300 K)."""
+    if kind == "periodic":
+        case = periodic_case(8, 6, split="half", jitter=0.25, seed=2)
+        case.numerics.viscosity_model = "Sutherland"
+        return case
+    mesh = box_mesh(16, 9, 2.0, 1.0, split="half", jitter=0.2, seed=11)
+    case = Case(name=f"viscous-{kind}", mesh=mesh)
+    rt = 1.0 / 287.05
+    for c in case.boundary_conditions:
+        if kind == "noslip":
+            if c.patch_name == "left":
+                c.kind = "Velocity Inlet"
+                c.values = {"density": 1.0, "velocity_x": 0.3, "velocity_y": 0.05, "temperature": rt}
+            elif c.patch_name == "right":
+                c.kind = "Pressure Outlet"
+                c.values = {"pressure": 0.95}
+            elif c.patch_name == "bottom":
+                c.kind, c.mechanical_condition, c.thermal_condition = "Wall", "No-slip", "Temperature"
+                c.values = {"temperature": 1.1 * rt}
+            else:
+                c.kind, c.mechanical_condition, c.thermal_condition = "Wall", "No-slip", "Heat Flux"
+                c.values = {"heat_flux": 0.02}
+        else:
+            if c.patch_name == "left":
+                c.kind = "Far Field"
+                c.values = {"density": 1.0, "velocity_x": 0.3, "velocity_y": 0.0, "pressure": 1.0}
+            elif c.patch_name == "right":
+                c.kind = "Mass Flow Outlet"
+                c.values = {"mass_flow": 0.3}
+            elif c.patch_name == "bottom":
+                c.kind = "Symmetry"
+            else:
+                c.kind, c.mechanical_condition, c.thermal_condition = "Wall", "Slip", "Heat Flux"
+                c.values = {"heat_flux": -0.01}
+    case.numerics.viscosity_model = "Constant"
+    case.numerics.dynamic_viscosity = 0.01
+    return case
+
+
+def viscous_primitive(kind, n, seed):
+    if kind == "periodic":  # air near 300 K
+        rng = np.random.default_rng(seed)
+        base = np.array([1.2, 30.0, -10.0, 1.2 * 287.05 * 300.0])
+        return base * (1.0 + 0.05 * rng.standard_normal((n, 4)))
+    return bc_primitive(n, seed)
+
+
+def viscous_fixture(kind, ref):
+    case = viscous_case(kind)
+    case.numerics.reconstruction = "MUSCL parabolic"
+    rc = reference_case(case, ref)
+    rg = ref.solver._build_geometry(rc.mesh, rc)
+    out = {**mesh_arrays(case), **geometry_arrays(rg, GEOM_FIELDS + PARABOLIC_FIELDS
+                                                  + ("diffusive_boundary_faces", "patch_ids"))}
+    out.update(viscous_geometry_arrays(rg))
+    n = len(rg.areas)
+    P = viscous_primitive(kind, n, seed=5)
+    U = ref.euler.primitive_to_conservative(P, 1.4)
+    out["U"] = U
+    num = rc.numerics
+    out["dynamic_viscosity"] = np.array(num.dynamic_viscosity)
+    # the wall cases run in R T = 1 units, where Sutherland's law (fit to air
+    # in kelvin) does not apply; the periodic box is in SI units
+    models = ("Sutherland", "Constant") if kind == "periodic" else ("Constant",)
+    keys = []
+    for model in models:
+        num.viscosity_model = model
+        out[f"V|{model}"] = ref.solver._viscous_residual(P, rg, num)
+        out[f"G|{model}"] = ref.solver._viscous_gradients(P, rg, num)
+        for flux, (recon, limiter) in itertools.product(FLUXES, (("First order", "Barth-Jespersen"),
+                                                                 ("MUSCL linear", "Venkatakrishnan"))):
+            num.flux, num.reconstruction, num.limiter = flux, recon, limiter
+            key = f"R|{flux}|{recon}|{limiter}|0|{model}"
+            out[key] = ref.solver._residual(U, rg, num)
+            keys.append(key)
+        num.cfl = 0.7
+        out[f"dt|{model}"] = ref.solver._stable_time_steps(P, rg, num)
+    np.savez_compressed(HERE / f"viscous_{kind}.npz", **out)
+    print("viscous", kind, n, "cells,", len(keys), "residuals")
+
+
+def viscous_geometry_arrays(rg):
+    """Wall thermal data and patch kinds of a reference geometry."""
+    faces, offsets, cond, values, mech, names = [], [0], [], [], [], []
+    for b in rg.wall_thermal_boundaries:
+        faces.extend(int(f) for f in b.faces)
+        offsets.append(len(faces))
+        cond.append(b.condition)
+        values.append(b.value)
+        mech.append(b.mechanical_condition)
+        names.append(b.patch_name)
+    kinds = sorted(rg.patch_kinds.items())
+    return {"wt_faces": np.asarray(faces, dtype=np.int64), "wt_offsets": np.asarray(offsets),
+            "wt_condition": np.asarray(cond), "wt_value": np.asarray(values, dtype=float),
+            "wt_mechanical": np.asarray(mech), "wt_names": np.asarray(names),
+            "patch_kind_ids": np.asarray([k for k, _ in kinds]), "patch_kind_names": np.asarray([v for _, v in kinds])}
+
+
 def strip_case(nx=6, ny=2):
     """Unsplit, unjittered 6x2 quads: every two-ring stencil has two rows of
     cell centres, so every 5x5 normal matrix is rank deficient."""
@@ -278,7 +381,11 @@ def solve_fixture(name, case, primitive, settings, steps, ref):
     result = ref.solver.solve_case(rc, states)
     final = np.array([(s.density, s.velocity_x, s.velocity_y, s.pressure) for s in result.states])
     fields = GEOM_FIELDS + (PARABOLIC_FIELDS if rc.numerics.reconstruction == "MUSCL parabolic" else ())
+    viscous = rc.numerics.viscosity_model != "Inviscid"
+    if viscous:
+        fields = fields + ("diffusive_boundary_faces", "patch_ids")
     out = {**mesh_arrays(case), **geometry_arrays(rg, fields), "P0": primitive, "P_final": final,
+           **(viscous_geometry_arrays(rg) if viscous else {}),
            "time": np.array(result.time), "steps": np.array(result.steps)}
     for key, value in settings.items():
         out[f"set|{key}"] = np.array(value)
@@ -335,6 +442,15 @@ def main(only=None):
     ref = import_reference()
     if only == "parabolic":
         return parabolic_main(ref)
+    if only == "viscous":
+        for kind in ("noslip", "mixed", "periodic"):
+            viscous_fixture(kind, ref)
+        case = viscous_case("noslip")
+        solve_fixture("viscous_noslip_rk3", case, viscous_primitive("noslip", len(case.mesh.cells), 5),
+                      {"flux": "HLLC", "reconstruction": "MUSCL linear", "limiter": "Venkatakrishnan",
+                       "time_integration": "Explicit RK3", "cfl": 0.5, "viscosity_model": "Constant",
+                       "dynamic_viscosity": 0.01}, 10, ref)
+        return None
     if only == "bc":
         bc_fixture("pinlet", ref)
         bc_fixture("massflow", ref)
