@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define MCFD_ABI_VERSION 3
+#define MCFD_ABI_VERSION 4
 
 /* ---- return codes (host-side failures) ---- */
 #define MCFD_OK 0
@@ -60,6 +60,10 @@ extern "C" {
 #define MCFD_S_MFI_PRESSURE 0x4000        /* solver.py:4513-4516 */
 #define MCFD_S_MFI_FLOW_RATE 0x8000       /* solver.py:4536-4540 */
 #define MCFD_S_MFO_DENSITY 0x10000        /* solver.py:4563-4566 */
+/* laminar viscous terms */
+#define MCFD_S_VISC_TEMPERATURE 0x20000   /* solver.py:3620-3621 */
+#define MCFD_S_VISC_SUTHERLAND 0x40000    /* solver.py:2734-2735 */
+#define MCFD_S_VISC_DISTANCE 0x80000      /* solver.py:3944-3945 */
 
 typedef struct mcfd_status {
   int32_t code;       /* OR of MCFD_S_* bits since the last fetch */
@@ -99,9 +103,28 @@ typedef struct mcfd_config {
   double acceleration_x;  /* body force (solver.py:2709-2715) */
   double acceleration_y;
   double cfl;             /* used by mcfd_time_steps */
-  double gas_constant;    /* NumericalSettings.gas_constant: pressure-inlet / mass-flow states */
-  double reserved[3];
+  double gas_constant;    /* NumericalSettings.gas_constant: pressure-inlet / mass-flow / viscous terms */
+  int32_t viscosity_model; /* MCFD_VISC_* */
+  int32_t reserved_i;
+  double dynamic_viscosity;                /* Constant model */
+  double sutherland_reference_viscosity;   /* Sutherland model (solver.py:2721-2737) */
+  double sutherland_reference_temperature;
+  double sutherland_temperature;
+  double prandtl_number;
+  double reserved[2];
 } mcfd_config;
+
+/* viscosity models (model.py:24) */
+#define MCFD_VISC_INVISCID 0
+#define MCFD_VISC_CONSTANT 1
+#define MCFD_VISC_SUTHERLAND 2
+/* kinds of diffusive boundary faces (viscous terms, solver.py:3650-3690, 3947-4030) */
+#define MCFD_DIFF_WALL_NO_SLIP 0
+#define MCFD_DIFF_WALL_SLIP 1
+#define MCFD_DIFF_SYMMETRY 2
+#define MCFD_DIFF_INLET 3      /* exterior state given: velocity / pressure / mass-flow inlet, far field */
+#define MCFD_DIFF_OTHER 4      /* zero normal gradient (outlets) */
+#define MCFD_DIFF_WALL_UNKNOWN 5 /* wall without thermal data: the viscous path refuses it */
 
 /* boundary patch kinds (solver.py:81-103) */
 #define MCFD_BC_PRESSURE_INLET 0
@@ -171,6 +194,21 @@ typedef struct mcfd_geom_desc {
   const int64_t* bc_faces;     /* boundary face ids, patch by patch */
   const double* bc_direction_normal; /* [len(bc_faces)] normals @ direction as the reference computes it
                                         (inlets; 0 for outlets) */
+  /* laminar viscous terms (needed only with a viscosity model) */
+  const double* gradient_dx;        /* [n_gradient] raw offsets of the gradient entries */
+  const double* gradient_dy;
+  int64_t n_diffusive;              /* non-periodic boundary faces, ascending (diffusive_boundary_faces) */
+  const int64_t* diffusive_faces;
+  const int32_t* diffusive_kind;    /* MCFD_DIFF_* */
+  const int32_t* diffusive_thermal; /* walls: 0 fixed temperature, 1 heat flux */
+  const double* diffusive_value;    /* walls: temperature or heat flux */
+  const int32_t* diffusive_inlet;   /* inlets: source << 28 | index: 1 velocity inlet, 2 pressure-inlet /
+                                       mass-flow patch face (bc_faces position), 3 far field */
+  const double* diffusive_normal_distance; /* float(np.dot(face_center - cell_center, normal)) */
+  const double* diffusive_ghost_offset;    /* [n][2] 2 d n (walls, symmetry) or 2 (face_center - center) */
+  const double* diffusive_offset;          /* [n][2] face_center - cell_center */
+  const double* interior_distance; /* [n_interior] |(c_neighbour - c_owner) . n| (time-step diffusion) */
+  const double* periodic_distance; /* [n_periodic] |(f_a - c_a) . n_a| + |(f_b - c_b) . n_b| */
 } mcfd_geom_desc;
 
 typedef struct mcfd_geom mcfd_geom; /* opaque device geometry + workspace */

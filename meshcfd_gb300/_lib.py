@@ -37,7 +37,14 @@ class Config(C.Structure):
         ("acceleration_y", c_dbl),
         ("cfl", c_dbl),
         ("gas_constant", c_dbl),
-        ("reserved", c_dbl * 3),
+        ("viscosity_model", c_i32),
+        ("reserved_i", c_i32),
+        ("dynamic_viscosity", c_dbl),
+        ("sutherland_reference_viscosity", c_dbl),
+        ("sutherland_reference_temperature", c_dbl),
+        ("sutherland_temperature", c_dbl),
+        ("prandtl_number", c_dbl),
+        ("reserved", c_dbl * 2),
     ]
 
 
@@ -59,6 +66,12 @@ class GeomDesc(C.Structure):
         ("parabolic_dx", P_dbl), ("parabolic_dy", P_dbl),
         ("n_bc_patches", c_i64), ("bc_kind", C.POINTER(C.c_int32)), ("bc_values", P_dbl), ("bc_offsets", P_i64),
         ("bc_faces", P_i64), ("bc_direction_normal", P_dbl),
+        ("gradient_dx", P_dbl), ("gradient_dy", P_dbl),
+        ("n_diffusive", c_i64), ("diffusive_faces", P_i64), ("diffusive_kind", C.POINTER(C.c_int32)),
+        ("diffusive_thermal", C.POINTER(C.c_int32)), ("diffusive_value", P_dbl),
+        ("diffusive_inlet", C.POINTER(C.c_int32)), ("diffusive_normal_distance", P_dbl),
+        ("diffusive_ghost_offset", P_dbl), ("diffusive_offset", P_dbl),
+        ("interior_distance", P_dbl), ("periodic_distance", P_dbl),
     ]
 
 
@@ -70,7 +83,7 @@ class GeomInfo(C.Structure):
     ]
 
 
-ABI_VERSION = 3  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
+ABI_VERSION = 4  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
 
 # name -> (restype, argtypes); every symbol include/meshcfd_gb300.h declares.
 SIGNATURES = {

@@ -32,6 +32,7 @@ UNITS = [
     ("mcfd_vjp.cu", ["-fmad=true"]),
     ("mcfd_parabolic.cu", ["-fmad=false"]),
     ("mcfd_boundary.cu", ["-fmad=false"]),
+    ("mcfd_viscous.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),
     ("mcfd_noalloc.cu", ["-fmad=false"]),
 ]

@@ -38,6 +38,7 @@ struct mcfd_geom {
   JvpWork jvp;                 // tangent workspace (allocated on first use)
   VjpWork vjp;                 // adjoint workspace (allocated on first use)
   std::vector<void*> jvp_owned;
+  ViscousWork visc;            // laminar viscous workspace (allocated on first use)
   // mcfd_explicit_step_record: per-stage copies of the primitive and face states
   double* const* rec_P = nullptr;
   double* const* rec_recon = nullptr;
@@ -81,6 +82,9 @@ static int check_cfg(const mcfd_config* cfg) {
   if (cfg->reconstruction < 0 || cfg->reconstruction > 2) return MCFD_E_ARG;
   if (!(cfg->gamma > 1.0)) return MCFD_E_ARG;
   if (cfg->mode < MCFD_MODE_EXACT || cfg->mode > MCFD_MODE_FMA) return MCFD_E_ARG;
+  if (cfg->viscosity_model < MCFD_VISC_INVISCID || cfg->viscosity_model > MCFD_VISC_SUTHERLAND) return MCFD_E_ARG;
+  if (cfg->viscosity_model != MCFD_VISC_INVISCID && (!(cfg->gas_constant > 0.0) || !(cfg->prandtl_number > 0.0)))
+    return MCFD_E_ARG;
   return MCFD_OK;
 }
 
@@ -115,8 +119,26 @@ static cudaError_t timed(mcfd_geom* h, int cls, cudaStream_t s, F&& launch) {
 
 // One residual evaluation of the state whose primitive is in ws.P, followed
 // by the gather with the given stage program.
-static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgram& prog,
+// The laminar viscous workspace, allocated on the first viscous call; refuses
+// geometries without the viscous tables (or with walls lacking thermal data).
+static int ensure_viscous(mcfd_geom* h, const mcfd_config* cfg) {
+  if (cfg->viscosity_model == MCFD_VISC_INVISCID) return MCFD_OK;
+  if (!h->g.viscous_ok) return MCFD_E_UNSUPPORTED;
+  if (h->visc.cell) return MCFD_OK;
+  const size_t C = h->g.n_cells, NF = h->g.seg_begin[SEG_PERIODIC + 1], ND = h->g.n_diffusive;
+  double** fields[] = {&h->visc.cell, &h->visc.grad, &h->visc.flux, &h->visc.bflux, &h->visc.r, &h->visc.diff};
+  const size_t sizes[] = {4 * C, 6 * C, 4 * (NF > 0 ? NF : 1), 4 * (ND > 0 ? ND : 1), 4 * C, C};
+  for (int k = 0; k < 6; ++k) {
+    if (cudaMalloc((void**)fields[k], sizes[k] * sizeof(double)) != cudaSuccess) return MCFD_E_CUDA;
+    h->jvp_owned.push_back(*fields[k]);
+  }
+  h->g.visc_diff = h->visc.diff;
+  return MCFD_OK;
+}
+
+static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgram& prog_in,
                          cudaStream_t s) {
+  StageProgram prog = prog_in;
   cudaError_t e = cudaSuccess;
   if (cfg.reconstruction == MCFD_RECON_MUSCL_LINEAR)
     e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return MCFD_DISPATCH(cfg, launch_reconstruct(h->g, cfg, h->ws.P, h->ws.recon, s)); });
@@ -125,6 +147,12 @@ static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgra
   if (e == cudaSuccess && h->g.n_bc_patches > 0) {
     const double* recon = cfg.reconstruction == MCFD_RECON_FIRST_ORDER ? nullptr : h->ws.recon;
     e = timed(h, MCFD_PROF_FLUX, s, [&] { return launch_bc_states(h->g, cfg, h->ws.P, recon, h->g.bc_ext, s); });
+  }
+  if (e == cudaSuccess && cfg.viscosity_model != MCFD_VISC_INVISCID) {  // solver.py:2699-2702
+    if (h->g.n_bc_patches > 0) e = launch_bc_states(h->g, cfg, h->ws.P, nullptr, h->g.bc_ext_dt, s);
+    if (e == cudaSuccess)
+      e = timed(h, MCFD_PROF_OTHER, s, [&] { return launch_viscous_residual(h->g, cfg, h->ws.P, h->visc, s); });
+    prog.visc_r = h->visc.r;
   }
   if (e == cudaSuccess && h->rec_P && h->rec_k < h->rec_n) {  // mcfd_explicit_step_record
     const int k = h->rec_k++;
@@ -210,6 +238,12 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   if (NBP < 0 || NBP > kMaxIndex) return MCFD_E_ARG;
   if (NBP && (!d->bc_kind || !d->bc_values || !d->bc_offsets || !d->bc_direction_normal)) return MCFD_E_ARG;
   const int64_t NB = NBP ? d->bc_offsets[NBP] : 0;
+  const int64_t ND = d->n_diffusive;
+  if (ND < 0 || ND > kMaxIndex) return MCFD_E_ARG;
+  if (ND && (!d->diffusive_faces || !d->diffusive_kind || !d->diffusive_thermal || !d->diffusive_value ||
+             !d->diffusive_inlet || !d->diffusive_normal_distance || !d->diffusive_ghost_offset ||
+             !d->diffusive_offset))
+    return MCFD_E_ARG;
   if (NBP) {
     if (d->bc_offsets[0] != 0) return MCFD_E_GEOMETRY;
     for (int64_t k = 0; k < NBP; ++k) {
@@ -218,6 +252,13 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
     }
     if (NB > kMaxIndex || (NB && !d->bc_faces)) return MCFD_E_ARG;
     if (!check_faces(d->bc_faces, NB)) return MCFD_E_GEOMETRY;
+  }
+  if (ND && !check_faces(d->diffusive_faces, ND)) return MCFD_E_GEOMETRY;
+  for (int64_t j = 0; j < ND; ++j) {
+    const int src = d->diffusive_inlet[j] >> 28, idx = d->diffusive_inlet[j] & 0x0fffffff;
+    const int64_t limit = src == 1 ? NV : src == 2 ? NB : src == 3 ? NF : 1;
+    if (src < 0 || src > 3 || idx >= limit || d->diffusive_kind[j] < 0 || d->diffusive_kind[j] > 5)
+      return MCFD_E_GEOMETRY;
   }
   for (int64_t c = 0; c < C; ++c)
     if (!(d->areas[c] > 0.0)) return MCFD_E_GEOMETRY;
@@ -353,6 +394,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
       gb_len[j] = blen[order[j]];
     }
   }
+  std::vector<int> order_grad;
   // ---- gradient entries grouped by source, reference order kept
   std::vector<int> grad_ptr, grad_nb(NG), grad_twin(NG, -1);
   std::vector<double> grad_cx(NG), grad_cy(NG);
@@ -361,6 +403,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
     key.resize(NG);
     for (int64_t e = 0; e < NG; ++e) key[e] = (int)d->gradient_sources[e];
     group_by(key, (int)C, grad_ptr, order);
+    order_grad = order;
     std::vector<int> pos(NG);
     for (int64_t j = 0; j < NG; ++j) {
       int e = order[j];
@@ -407,6 +450,98 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
       par_d[2 * j] = d->parabolic_dx[e];
       par_d[2 * j + 1] = d->parabolic_dy[e];
     }
+  }
+  // ---- laminar viscous tables (solver.py:3615-4114, 4250-4335)
+  const bool has_viscous = (d->gradient_dx && d->gradient_dy) || NG == 0;
+  std::vector<double> grad_d(has_viscous ? 2 * NG : 0);
+  if (has_viscous)
+    for (int64_t j = 0; j < NG; ++j) {
+      const int e = order_grad[j];
+      grad_d[2 * j] = d->gradient_dx[e];
+      grad_d[2 * j + 1] = d->gradient_dy[e];
+    }
+  std::vector<int> vb_ptr, vb_j(ND), diff_owner(ND), diff_kind(ND), diff_thermal(ND), diff_inlet(ND);
+  std::vector<double> diff_normal(2 * ND), diff_len(ND), diff_value(ND), diff_nd(ND), diff_ghost(2 * ND),
+      diff_offset(2 * ND), diff_wallv(2 * ND, 0.0);
+  bool viscous_ok = has_viscous;
+  {
+    key.resize(ND);
+    for (int64_t j = 0; j < ND; ++j) {
+      const int64_t f = d->diffusive_faces[j];
+      key[j] = (int)d->owners[f];
+      diff_owner[j] = (int)d->owners[f];
+      diff_normal[2 * j] = d->face_normals[2 * f];
+      diff_normal[2 * j + 1] = d->face_normals[2 * f + 1];
+      diff_len[j] = d->face_lengths[f];
+      diff_kind[j] = d->diffusive_kind[j];
+      diff_thermal[j] = d->diffusive_thermal[j];
+      diff_inlet[j] = d->diffusive_inlet[j];
+      diff_value[j] = d->diffusive_value[j];
+      diff_nd[j] = d->diffusive_normal_distance[j];
+      for (int k = 0; k < 2; ++k) {
+        diff_ghost[2 * j + k] = d->diffusive_ghost_offset[2 * j + k];
+        diff_offset[2 * j + k] = d->diffusive_offset[2 * j + k];
+        if (d->wall_velocities) diff_wallv[2 * j + k] = d->wall_velocities[2 * f + k];
+      }
+      if (diff_kind[j] == MCFD_DIFF_WALL_UNKNOWN) viscous_ok = false;
+    }
+    group_by(key, (int)C, vb_ptr, order);
+    for (int64_t i = 0; i < ND; ++i) vb_j[i] = order[i];
+  }
+  // viscous gather: periodic side a (pair order), side b, then diffusive faces
+  std::vector<int> vg_ptr, vg_code;
+  {
+    std::vector<int> code;
+    key.clear();
+    for (int64_t k = 0; k < NP; ++k) key.push_back((int)d->owners[d->periodic_faces_a[k]]), code.push_back((int)k);
+    for (int64_t k = 0; k < NP; ++k)
+      key.push_back((int)d->owners[d->periodic_faces_b[k]]), code.push_back((1 << 28) | (int)k);
+    for (int64_t j = 0; j < ND; ++j) key.push_back(diff_owner[j]), code.push_back((2 << 28) | (int)j);
+    group_by(key, (int)C, vg_ptr, order);
+    vg_code.resize(order.size());
+    for (size_t i = 0; i < order.size(); ++i) vg_code[i] = code[order[i]];
+  }
+  // time-step diffusion: interior owners, interior neighbours, periodic a, b, diffusive faces
+  std::vector<int> vd_ptr, vd_other;
+  std::vector<double> vd_len, vd_dist;
+  if (has_viscous && (NI == 0 || d->interior_distance) && (NP == 0 || d->periodic_distance)) {
+    std::vector<int> other;
+    std::vector<double> len, dist;
+    key.clear();
+    for (int side = 0; side < 2; ++side)
+      for (int64_t i = 0; i < NI; ++i) {
+        const int64_t f = d->interior_faces[i];
+        key.push_back((int)(side ? d->neighbours[f] : d->owners[f]));
+        other.push_back((int)(side ? d->owners[f] : d->neighbours[f]));
+        len.push_back(d->face_lengths[f]);
+        dist.push_back(d->interior_distance[i]);
+      }
+    for (int side = 0; side < 2; ++side)
+      for (int64_t k = 0; k < NP; ++k) {
+        const int64_t fa = d->periodic_faces_a[k], fb = d->periodic_faces_b[k];
+        key.push_back((int)(side ? d->owners[fb] : d->owners[fa]));
+        other.push_back((int)(side ? d->owners[fa] : d->owners[fb]));
+        len.push_back(d->face_lengths[fa]);
+        dist.push_back(d->periodic_distance[k]);
+      }
+    for (int64_t j = 0; j < ND; ++j) {
+      key.push_back(diff_owner[j]);
+      other.push_back(-1);
+      len.push_back(diff_len[j]);
+      dist.push_back(std::fabs(diff_nd[j]));
+    }
+    group_by(key, (int)C, vd_ptr, order);
+    vd_other.resize(order.size());
+    vd_len.resize(order.size());
+    vd_dist.resize(order.size());
+    for (size_t i = 0; i < order.size(); ++i) {
+      vd_other[i] = other[order[i]];
+      vd_len[i] = len[order[i]];
+      vd_dist[i] = dist[order[i]];
+    }
+  } else {
+    viscous_ok = false;
+    vd_ptr.assign(C + 1, 0);
   }
   // ---- time-step entries (solver.py:4206-4226)
   std::vector<int> dt_ptr, dt_info;
@@ -457,6 +592,15 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   size_t o_par_ptr = A.take(bytes_i(C + 1)), o_par_nb = A.take(bytes_i(NE)), o_par_d = A.take(bytes_d(2 * NE));
   size_t o_bc_ptr = A.take(bytes_i(NBP + 1)), o_bc_kind = A.take(bytes_i(NBP)), o_bc_values = A.take(bytes_d(4 * NBP)),
          o_bc_dn = A.take(bytes_d(NB));
+  size_t o_grad_d = A.take(bytes_d(grad_d.size())), o_vb_ptr = A.take(bytes_i(vb_ptr.size())),
+         o_vb_j = A.take(bytes_i(ND)), o_diff_owner = A.take(bytes_i(ND)), o_diff_normal = A.take(bytes_d(2 * ND)),
+         o_diff_len = A.take(bytes_d(ND)), o_diff_kind = A.take(bytes_i(ND)), o_diff_thermal = A.take(bytes_i(ND)),
+         o_diff_value = A.take(bytes_d(ND)), o_diff_inlet = A.take(bytes_i(ND)), o_diff_nd = A.take(bytes_d(ND)),
+         o_diff_ghost = A.take(bytes_d(2 * ND)), o_diff_offset = A.take(bytes_d(2 * ND)),
+         o_diff_wallv = A.take(bytes_d(2 * ND)), o_vg_ptr = A.take(bytes_i(vg_ptr.size())),
+         o_vg_code = A.take(bytes_i(vg_code.size())), o_vd_ptr = A.take(bytes_i(vd_ptr.size())),
+         o_vd_other = A.take(bytes_i(vd_other.size())), o_vd_len = A.take(bytes_d(vd_len.size())),
+         o_vd_dist = A.take(bytes_d(vd_dist.size()));
   size_t o_lslot = A.take(bytes_i(n_flux)), o_rslot = A.take(bytes_i(n_flux)),
          o_lcell = A.take(bytes_i(n_flux)), o_rcell = A.take(bytes_i(n_flux)),
          o_normal = A.take(bytes_d(2 * n_flux)), o_flen = A.take(bytes_d(n_flux)), o_wallv = A.take(bytes_d(2 * NW)),
@@ -504,6 +648,26 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   put(o_bc_kind, bc_kind.data(), bytes_i(NBP));
   put(o_bc_values, bc_values.data(), bytes_d(4 * NBP));
   put(o_bc_dn, bc_dn.data(), bytes_d(NB));
+  put(o_grad_d, grad_d.data(), bytes_d(grad_d.size()));
+  put(o_vb_ptr, vb_ptr.data(), bytes_i(vb_ptr.size()));
+  put(o_vb_j, vb_j.data(), bytes_i(ND));
+  put(o_diff_owner, diff_owner.data(), bytes_i(ND));
+  put(o_diff_normal, diff_normal.data(), bytes_d(2 * ND));
+  put(o_diff_len, diff_len.data(), bytes_d(ND));
+  put(o_diff_kind, diff_kind.data(), bytes_i(ND));
+  put(o_diff_thermal, diff_thermal.data(), bytes_i(ND));
+  put(o_diff_value, diff_value.data(), bytes_d(ND));
+  put(o_diff_inlet, diff_inlet.data(), bytes_i(ND));
+  put(o_diff_nd, diff_nd.data(), bytes_d(ND));
+  put(o_diff_ghost, diff_ghost.data(), bytes_d(2 * ND));
+  put(o_diff_offset, diff_offset.data(), bytes_d(2 * ND));
+  put(o_diff_wallv, diff_wallv.data(), bytes_d(2 * ND));
+  put(o_vg_ptr, vg_ptr.data(), bytes_i(vg_ptr.size()));
+  put(o_vg_code, vg_code.data(), bytes_i(vg_code.size()));
+  put(o_vd_ptr, vd_ptr.data(), bytes_i(vd_ptr.size()));
+  put(o_vd_other, vd_other.data(), bytes_i(vd_other.size()));
+  put(o_vd_len, vd_len.data(), bytes_d(vd_len.size()));
+  put(o_vd_dist, vd_dist.data(), bytes_d(vd_dist.size()));
   put(o_lslot, lslot.data(), bytes_i(n_flux));
   put(o_rslot, rslot.data(), bytes_i(n_flux));
   put(o_lcell, lcell.data(), bytes_i(n_flux));
@@ -565,6 +729,29 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   g.bc_ext = AT(double*, o_bc_ext);
   g.bc_ext_dt = AT(double*, o_bc_ext_dt);
   g.bc_terms = AT(double*, o_bc_terms);
+  g.has_viscous = has_viscous ? 1 : 0;
+  g.viscous_ok = viscous_ok ? 1 : 0;
+  g.n_diffusive = (int)ND;
+  g.grad_d = AT(const double2*, o_grad_d);
+  g.vb_ptr = AT(const int*, o_vb_ptr);
+  g.vb_j = AT(const int*, o_vb_j);
+  g.diff_owner = AT(const int*, o_diff_owner);
+  g.diff_normal = AT(const double2*, o_diff_normal);
+  g.diff_len = AT(const double*, o_diff_len);
+  g.diff_kind = AT(const int*, o_diff_kind);
+  g.diff_thermal = AT(const int*, o_diff_thermal);
+  g.diff_value = AT(const double*, o_diff_value);
+  g.diff_inlet = AT(const int*, o_diff_inlet);
+  g.diff_nd = AT(const double*, o_diff_nd);
+  g.diff_ghost = AT(const double2*, o_diff_ghost);
+  g.diff_offset = AT(const double2*, o_diff_offset);
+  g.diff_wallv = AT(const double2*, o_diff_wallv);
+  g.vg_ptr = AT(const int*, o_vg_ptr);
+  g.vg_code = AT(const int*, o_vg_code);
+  g.vd_ptr = AT(const int*, o_vd_ptr);
+  g.vd_other = AT(const int*, o_vd_other);
+  g.vd_len = AT(const double*, o_vd_len);
+  g.vd_dist = AT(const double*, o_vd_dist);
   g.ff_lslot = AT(const int*, o_lslot);
   g.ff_rslot = AT(const int*, o_rslot);
   g.ff_lcell = AT(const int*, o_lcell);
@@ -783,6 +970,7 @@ int mcfd_residual(mcfd_geom* h, const mcfd_config* cfg, const double* U, double*
   if (!h || !U) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
+  if ((c = ensure_viscous(h, cfg))) return c;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, h->ws.P, s)); });
   StageProgram prog{};
@@ -796,12 +984,15 @@ int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, doubl
   if (!h || !P) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
+  if ((c = ensure_viscous(h, cfg))) return c;
   if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_TIME_STEP, s,
                   [&] {
                     cudaError_t r = cudaSuccess;
                     if (h->g.n_bc_patches > 0) r = launch_bc_states(h->g, *cfg, P, nullptr, h->g.bc_ext_dt, s);
+                    if (r == cudaSuccess && cfg->viscosity_model != MCFD_VISC_INVISCID)
+                      r = launch_viscous_diffusion(h->g, *cfg, P, h->visc, s);
                     if (r == cudaSuccess)
                       r = MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, dt_min, time_limit, s));
                     return r;
@@ -814,6 +1005,7 @@ int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, dou
   if (!h || !U || !dt) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
+  if ((c = ensure_viscous(h, cfg))) return c;
   if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Workspace& w = h->ws;
@@ -923,6 +1115,7 @@ int mcfd_implicit_prepare(mcfd_geom* h, const mcfd_config* cfg, const double* U,
   if (!h || !U || !dt || !scales) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
+  if ((c = ensure_viscous(h, cfg))) return c;
   if ((c = ensure_implicit(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
   ImplicitState& st = h->imp;
@@ -1009,7 +1202,9 @@ int mcfd_vjp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   if (!h || !U || !lambda || !U_bar) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
-  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0) return MCFD_E_UNSUPPORTED;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0 ||
+      cfg->viscosity_model != MCFD_VISC_INVISCID)
+    return MCFD_E_UNSUPPORTED;
   if (cfg->reconstruction != MCFD_RECON_FIRST_ORDER && !h->g.has_twins) return MCFD_E_UNSUPPORTED;
   if ((c = ensure_vjp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1022,7 +1217,9 @@ int mcfd_vjp_at(mcfd_geom* h, const mcfd_config* cfg, const double* U, const dou
   if (!h || !U || !P || !lambda || !U_bar) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
-  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0) return MCFD_E_UNSUPPORTED;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0 ||
+      cfg->viscosity_model != MCFD_VISC_INVISCID)
+    return MCFD_E_UNSUPPORTED;
   if (cfg->reconstruction != MCFD_RECON_FIRST_ORDER && (!h->g.has_twins || !recon)) return MCFD_E_UNSUPPORTED;
   if ((c = ensure_vjp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1047,7 +1244,9 @@ int mcfd_jvp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   if (!h || !U || !dU || !dR) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
-  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0) return MCFD_E_UNSUPPORTED;
+  if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0 ||
+      cfg->viscosity_model != MCFD_VISC_INVISCID)
+    return MCFD_E_UNSUPPORTED;
   if ((c = ensure_jvp(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return launch_jvp(h->g, *cfg, U, dU, h->jvp, dR, s); }));
@@ -1142,11 +1341,14 @@ int mcfd_batch_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P,
   if (!h || !P || !case_offsets || n_cases <= 0 || !dt_case || !dt_cells) return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
+  if ((c = ensure_viscous(h, cfg))) return c;
   if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = timed(h, MCFD_PROF_TIME_STEP, s, [&] {
     cudaError_t r = cudaSuccess;
     if (h->g.n_bc_patches > 0) r = launch_bc_states(h->g, *cfg, P, nullptr, h->g.bc_ext_dt, s);
+    if (r == cudaSuccess && cfg->viscosity_model != MCFD_VISC_INVISCID)
+      r = launch_viscous_diffusion(h->g, *cfg, P, h->visc, s);
     if (r == cudaSuccess) r = MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, nullptr, 0.0, s));
     if (r == cudaSuccess) r = launch_case_time_steps(h->g.n_cells, n_cases, case_offsets, dt_case, dt_cells, s);
     return r;

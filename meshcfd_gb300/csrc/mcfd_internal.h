@@ -87,6 +87,33 @@ struct DevGeom {
   const double* dt_len;
   const int* dt_info;  // kind << 28 | index into the BC arrays
   DevStatus* status;
+  // laminar viscous terms (n_diffusive = 0 when the geometry carries none)
+  int has_viscous;            // the descriptor gave the viscous tables
+  int n_diffusive;
+  const double2* grad_d;      // [n_gradient] raw offsets, grouped like grad_nb
+  const int* vb_ptr;          // [C + 1] diffusive faces per owner cell (positions j), diffusive order
+  const int* vb_j;
+  int viscous_ok;             // every diffusive wall face has thermal data
+  const int* diff_owner;      // [n_diffusive] owner cell
+  const double2* diff_normal;
+  const double* diff_len;
+  const int* diff_kind;       // MCFD_DIFF_*
+  const int* diff_thermal;
+  const double* diff_value;
+  const int* diff_inlet;      // source << 28 | index
+  const double* diff_nd;
+  const double2* diff_ghost;
+  const double2* diff_offset;
+  const double2* diff_wallv;
+  // viscous gather: periodic a (+), periodic b (-), diffusive faces, per cell in reference order
+  const int* vg_ptr;
+  const int* vg_code;         // kind << 28 | index: 0 periodic a (index k), 1 periodic b, 2 diffusive face j
+  // time-step diffusion entries per cell: owner / neighbour side of interior faces, periodic, diffusive
+  const int* vd_ptr;
+  const int* vd_other;        // other cell, or -1 on diffusive boundary faces
+  const double* vd_len;
+  const double* vd_dist;      // raw distance (the kernel takes max(d, 1e-14))
+  const double* visc_diff;    // [C] diffusion sum of the last viscous time step (workspace)
   // launch shapes chosen by mcfd_autotune (0: the defaults)
   int tune_recon_threads, tune_flux_threads, tune_flux_faces, tune_gather_threads;
 };
@@ -106,6 +133,7 @@ struct StageProgram {
   double* out_u;     // may be null (residual only)
   double* out_p;     // primitive of out_u, may be null
   double* out_r;     // residual store, may be null
+  const double* visc_r;  // laminar viscous residual added before the body force, may be null
 };
 
 struct Workspace {
@@ -172,6 +200,21 @@ cudaError_t launch_reconstruct_parabolic(const DevGeom& g, const mcfd_config& cf
                                          cudaStream_t s);
 cudaError_t launch_reconstruction_fields(const DevGeom& g, const mcfd_config& cfg, const double* P, double* grad,
                                          double* curv, double* fac, cudaStream_t s);
+// laminar viscous terms (mcfd_viscous.cu): residual of the primitive state P
+// into work.r (needs the cell-value boundary states in g.bc_ext_dt), and the
+// time step's diffusion sum into diff
+struct ViscousWork {
+  double* cell = nullptr;   // [C][4] T, mu, conductivity, effective diffusivity
+  double* grad = nullptr;   // [C][6] (du, dv, dT) x (x, y)
+  double* flux = nullptr;   // [n_interior + n_periodic][4]
+  double* bflux = nullptr;  // [n_diffusive][4]
+  double* r = nullptr;      // [C][4]
+  double* diff = nullptr;   // [C]
+};
+cudaError_t launch_viscous_residual(const DevGeom& g, const mcfd_config& cfg, const double* P, const ViscousWork& w,
+                                    cudaStream_t s);
+cudaError_t launch_viscous_diffusion(const DevGeom& g, const mcfd_config& cfg, const double* P,
+                                     const ViscousWork& w, cudaStream_t s);
 // pressure-inlet and mass-flow exterior states (mcfd_boundary.cu; exact
 // arithmetic): from the face states of the residual (recon per slot, or P for
 // first order when recon is null) into ext

@@ -327,6 +327,13 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
     }
   }
   const St4 p = ld4(P + 4 * (size_t)c);
+  if (prog.visc_r) {  // derivative += _viscous_residual(...) (solver.py:2699-2702)
+    const St4 v = ld4(prog.visc_r + 4 * (size_t)c);
+    r[0] = r[0] + v.a;
+    r[1] = r[1] + v.b;
+    r[2] = r[2] + v.c;
+    r[3] = r[3] + v.d;
+  }
   if (ax != 0.0 || ay != 0.0) {  // solver.py:2709-2715
     r[1] = r[1] + p.a * ax;
     r[2] = r[2] + p.a * ay;
@@ -384,7 +391,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
 __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* __restrict__ P,
                                                        double gamma, double cfl,
                                                        double* __restrict__ dt_cells,
-                                                       int want_min) {
+                                                       int want_min, const double* __restrict__ diffusion) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   double dt = __longlong_as_double(0x7ff0000000000000LL);
   if (c < g.n_cells) {
@@ -409,6 +416,7 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
       }
       sum = sum + radius * g.dt_len[e];
     }
+    if (diffusion) sum += 2.0 * diffusion[c];  // viscous terms (solver.py:4331)
     dt = (cfl * g.area[c]) / sum;
     if (!icmp::finite(dt) || !icmp::gt0(dt)) bits |= MCFD_S_TIME_STEP;
     if (bits) flag_cell(g.status, bits, c);
@@ -534,7 +542,8 @@ cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const do
                               cudaStream_t s) {
   if (g.n_cells > 0)
     count_launch(), k_time_steps<<<blocks_for(g.n_cells), kBlock, 0, s>>>(g, P, cfg.gamma, cfg.cfl, dt_cells,
-                                                          dt_min != nullptr);
+                                                          dt_min != nullptr,
+                                                          cfg.viscosity_model ? g.visc_diff : nullptr);
   if (dt_min) count_launch(), k_time_step_finalize<<<1, 1, 0, s>>>(g.status, dt_min, time_limit);
   return cudaGetLastError();
 }

@@ -31,8 +31,9 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
     arithmetic, limiter minimum through the smallest ratio) or "fma" (shared
     reciprocals and FMA; outside the 1e-12 bar on fine meshes).  MUSCL
     parabolic reconstructs with exact arithmetic in every mode."""
-    if settings.viscosity_model != "Inviscid":
-        raise NotImplementedError("viscous terms are not implemented by the GPU residual path")
+    viscous = {"Inviscid": 0, "Constant": 1, "Sutherland": 2}
+    if settings.viscosity_model not in viscous:
+        raise SolverError(f"Unsupported viscosity model '{settings.viscosity_model}'.")
     if settings.turbulence_model != "None":
         raise NotImplementedError("SST turbulence is not implemented by the GPU residual path")
     try:
@@ -48,6 +49,12 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
     cfg.acceleration_y = float(settings.acceleration_y)
     cfg.cfl = float(settings.cfl)
     cfg.gas_constant = float(settings.gas_constant)
+    cfg.viscosity_model = viscous[settings.viscosity_model]
+    cfg.dynamic_viscosity = float(settings.dynamic_viscosity)
+    cfg.sutherland_reference_viscosity = float(settings.sutherland_reference_viscosity)
+    cfg.sutherland_reference_temperature = float(settings.sutherland_reference_temperature)
+    cfg.sutherland_temperature = float(settings.sutherland_temperature)
+    cfg.prandtl_number = float(settings.prandtl_number)
     return cfg
 
 
@@ -129,6 +136,22 @@ class DeviceGeometry:
             d.bc_offsets, _ = a("bc_offsets", np.int64, src=bc["offsets"])
             d.bc_faces, _ = a("bc_faces", np.int64, src=bc["faces"])
             d.bc_direction_normal, _ = a("bc_direction_normal", np.float64, src=bc["direction_normal"])
+        vt = viscous_tables(geometry, bc) \
+            if hasattr(geometry, "diffusive_boundary_faces") and hasattr(geometry, "gradient_dx") else None
+        if vt is not None:
+            d.gradient_dx, _ = a("gradient_dx", np.float64)
+            d.gradient_dy, _ = a("gradient_dy", np.float64)
+            d.diffusive_faces, d.n_diffusive = a("diffusive_faces", np.int64, src=vt["faces"])
+            for name in ("kind", "thermal", "inlet"):
+                arr = vt[name]
+                keep["diffusive_" + name] = arr
+                setattr(d, "diffusive_" + name, arr.ctypes.data_as(C.POINTER(C.c_int32)) if arr.size else None)
+            d.diffusive_value, _ = a("diffusive_value", np.float64, src=vt["value"])
+            d.diffusive_normal_distance, _ = a("diffusive_nd", np.float64, src=vt["nd"])
+            d.diffusive_ghost_offset, _ = a("diffusive_ghost", np.float64, src=vt["ghost"])
+            d.diffusive_offset, _ = a("diffusive_offset", np.float64, src=vt["offset"])
+            d.interior_distance, _ = a("interior_distance", np.float64, src=vt["interior_distance"])
+            d.periodic_distance, _ = a("periodic_distance", np.float64, src=vt["periodic_distance"])
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             rc = self.lib.mcfd_geom_create(C.byref(d), C.byref(handle))
@@ -290,6 +313,72 @@ def boundary_patches(geometry) -> dict:
             "values": np.asarray(values, dtype=np.float64).reshape(-1, 4),
             "offsets": np.asarray(offsets, dtype=np.int64), "faces": cat(faces, np.int64),
             "direction_normal": cat(dn, np.float64)}
+
+
+DIFF_WALL_NO_SLIP, DIFF_WALL_SLIP, DIFF_SYMMETRY, DIFF_INLET, DIFF_OTHER, DIFF_WALL_UNKNOWN = range(6)
+
+
+def viscous_tables(geometry, bc) -> dict:
+    """The laminar viscous tables of the C ABI for a geometry: per diffusive
+    boundary face (solver.py:1817-1820) its kind, wall thermal data, inlet
+    state source, the normal distance and ghost offset exactly as the
+    reference computes them (NumPy's own np.dot, solver.py:3651-3655), and
+    the time step's face distances (solver.py:4266-4299)."""
+    owners = np.asarray(geometry.owners)
+    neighbours = np.asarray(geometry.neighbours)
+    normals = np.asarray(geometry.face_normals, dtype=np.float64).reshape(-1, 2)
+    fc = np.asarray(geometry.face_centers, dtype=np.float64).reshape(-1, 2)
+    centers = np.asarray(geometry.centers, dtype=np.float64).reshape(-1, 2)
+    faces = np.asarray(geometry.diffusive_boundary_faces, dtype=np.int64)
+    kinds = getattr(geometry, "patch_kinds", {})
+    patch_ids = np.asarray(getattr(geometry, "patch_ids", np.zeros(len(owners), dtype=np.int64)))
+    walls = {int(f): b for b in getattr(geometry, "wall_thermal_boundaries", ()) for f in b.faces}
+    inlet = {}
+    for i, f in enumerate(np.asarray(geometry.velocity_inlet_faces)):
+        inlet[int(f)] = (1 << 28) | i
+    for k, bkind in enumerate(bc["kind"]):
+        if bkind in (BC_PRESSURE_INLET, BC_MASS_FLOW_INLET):
+            for pos in range(int(bc["offsets"][k]), int(bc["offsets"][k + 1])):
+                inlet[int(bc["faces"][pos])] = (2 << 28) | pos
+    for i, f in enumerate(np.asarray(geometry.far_field_faces)):
+        inlet[int(f)] = (3 << 28) | i
+    n = len(faces)
+    out = {"faces": faces, "kind": np.zeros(n, dtype=np.int32), "thermal": np.zeros(n, dtype=np.int32),
+           "inlet": np.zeros(n, dtype=np.int32), "value": np.zeros(n), "nd": np.zeros(n),
+           "ghost": np.zeros((n, 2)), "offset": np.zeros((n, 2))}
+    for j, f in enumerate(faces):
+        o = int(owners[f])
+        nrm = normals[f]
+        off = fc[f] - centers[o]
+        nd = float(np.dot(off, nrm))
+        kind = kinds.get(int(patch_ids[f]), "")
+        out["offset"][j] = off
+        out["nd"][j] = nd
+        out["ghost"][j] = 2.0 * nd * nrm if kind in ("Wall", "Symmetry") else 2.0 * off
+        if kind == "Wall":
+            w = walls.get(int(f))
+            if w is None:
+                out["kind"][j] = DIFF_WALL_UNKNOWN
+            else:
+                no_slip = w.mechanical_condition in ("No-slip", "Prescribed velocity")
+                out["kind"][j] = DIFF_WALL_NO_SLIP if no_slip else DIFF_WALL_SLIP
+                out["thermal"][j] = 0 if w.condition == "Temperature" else 1
+                out["value"][j] = w.value
+        elif kind == "Symmetry":
+            out["kind"][j] = DIFF_SYMMETRY
+        elif int(f) in inlet:
+            out["kind"][j] = DIFF_INLET
+            out["inlet"][j] = inlet[int(f)]
+        else:
+            out["kind"][j] = DIFF_OTHER
+    interior = np.asarray(geometry.interior_faces, dtype=np.int64)
+    o, nb = owners[interior], neighbours[interior]
+    out["interior_distance"] = np.abs(np.sum((centers[nb] - centers[o]) * normals[interior], axis=1))
+    fa = np.asarray(geometry.periodic_faces_a, dtype=np.int64)
+    fb = np.asarray(geometry.periodic_faces_b, dtype=np.int64)
+    out["periodic_distance"] = (np.abs(np.sum((fc[fa] - centers[owners[fa]]) * normals[fa], axis=1))
+                                + np.abs(np.sum((fc[fb] - centers[owners[fb]]) * normals[fb], axis=1)))
+    return out
 
 
 def _device_view(ptr: int, shape, device) -> torch.Tensor:

@@ -41,6 +41,9 @@ STATUS_MFI_DIRECTION = 1 << 13
 STATUS_MFI_PRESSURE = 1 << 14
 STATUS_MFI_FLOW_RATE = 1 << 15
 STATUS_MFO_DENSITY = 1 << 16
+STATUS_VISC_TEMPERATURE = 1 << 17
+STATUS_VISC_SUTHERLAND = 1 << 18
+STATUS_VISC_DISTANCE = 1 << 19
 
 
 class StatusCode(int):
@@ -73,6 +76,9 @@ STATUS_MESSAGES = (
     (STATUS_MFI_PRESSURE, SolverError, "Mass-flow inlet '{patch}' has invalid interior pressure."),
     (STATUS_MFI_FLOW_RATE, SolverError, "Mass-flow inlet '{patch}' cannot satisfy the configured flow rate."),
     (STATUS_MFO_DENSITY, SolverError, "Mass-flow outlet '{patch}' has invalid interior density."),
+    (STATUS_VISC_TEMPERATURE, SolverError, "Viscous flow requires finite positive temperature."),
+    (STATUS_VISC_SUTHERLAND, SolverError, "Sutherland law produced an invalid viscosity."),
+    (STATUS_VISC_DISTANCE, SolverError, "Boundary face has invalid cell-center distance."),
     (STATUS_HLLC_NONFINITE, ValueError, "HLLC flux produced a non-finite value."),
     (STATUS_ROE_NONFINITE, ValueError, "Roe flux produced a non-finite value."),
     (STATUS_NONFINITE_RESIDUAL, SolverError, "Spatial residual contains non-finite values."),

@@ -80,7 +80,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(native.lib, name), name
     assert set(declared) == set(_lib.SIGNATURES), "ctypes signatures out of sync with the header"
-    assert native.mcfd_abi_version() == _lib.ABI_VERSION == 3
+    assert native.mcfd_abi_version() == _lib.ABI_VERSION == 4
     assert native.mcfd_error_string(3) == b"option not supported by the GPU path"
 
 
@@ -100,8 +100,7 @@ def test_config_mapping_rejects_unsupported_models():
     from meshcfd_gb300.device import make_config
     from meshcfd_gb300.model import NumericalSettings
 
-    with pytest.raises(NotImplementedError):
-        make_config(NumericalSettings(viscosity_model="Constant"))
+    assert make_config(NumericalSettings(viscosity_model="Sutherland")).viscosity_model == 2
     with pytest.raises(NotImplementedError):
         make_config(NumericalSettings(turbulence_model="SST"))
     assert make_config(NumericalSettings(reconstruction="MUSCL parabolic")).reconstruction == 2
