@@ -437,6 +437,17 @@ int64_t mcfd_launch_count(void);
  */
 int mcfd_residual_sumsq_noalloc(const double* R, int64_t n_cells, double* sums, void* stream);
 
+/*
+ * Element-wise IEEE binary64 division and square root exactly as the
+ * residual kernels evaluate them (integer-pipe routines, round to nearest
+ * even; bit-identical to the FP64 unit): quotient[i] = a[i] / b[i] and
+ * root[i] = sqrt(a[i]) for i < n.  Device arrays; either output may be NULL
+ * (b is read only for the quotient).  No reference counterpart: it exposes
+ * the arithmetic the residual path is built on, for verification.
+ */
+int mcfd_ieee_div_sqrt(const double* a, const double* b, int64_t n, double* quotient, double* root,
+                       void* stream);
+
 /* ---- host helpers (no GPU needed) ---- */
 
 /*

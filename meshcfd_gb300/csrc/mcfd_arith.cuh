@@ -1,0 +1,209 @@
+// IEEE-754 binary64 division and square root, round to nearest even,
+// evaluated on the integer pipe.
+//
+// On GB300 one FP64 division or square root costs ~8.6 FP64 issue slots
+// (~58 G/s per GPU) while the integer pipe runs ~38x the FP64 rate, so the
+// residual path's 8-12 divisions per face or cell dominate its FP64 budget.
+// These routines return exactly the IEEE result (the same bits as the FP64
+// unit's `a / b` and `sqrt(x)`) for every input:
+//
+// * normal operands with a normal result take the integer path: the
+//   reciprocal (division) or reciprocal square root (square root) of the
+//   53-bit significand is seeded from the fp32 approximation instructions
+//   (rcp.approx / rsqrt.approx, relative error < 2^-21 after truncating the
+//   significand to 24 bits) and refined by two Newton-Raphson steps in 64-bit
+//   fixed point (x' = x + x (1 - b x), y' = y + y (1 - m y^2) / 2; error
+//   ~2^-44, then ~2^-61).  The truncated quotient (root) with two bits below
+//   the last place is then corrected with its exact integer remainder
+//   (A 2^54 - Q B, resp. M 2^56 - S^2, both within a few units of the
+//   divisor and so exact in 64-bit two's complement) until 0 <= remainder <
+//   divisor — the classical exact-rounding test of a Newton quotient (e.g.
+//   Brent & Zimmermann, Modern Computer Arithmetic, 2010, secs. 3.4-3.5) —
+//   and rounded to nearest even from the guard bit and the sticky bit
+//   (remainder != 0);
+// * zeros, subnormals, infinities, NaN, negative square-root arguments and
+//   quotients that overflow or underflow fall back to the FP64 unit, and so
+//   does a remainder still out of range after the correction (it cannot be
+//   for the error bounds above; the test keeps the result exact regardless).
+//
+// The header also compiles as plain C++ (the host seeds are the correctly
+// rounded fp32 reciprocal and reciprocal root), so the integer algorithm can
+// be checked on the host against its IEEE division and square root.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#include <cuda_runtime.h>
+#define MCFD_IA_FN __host__ __device__ __forceinline__
+#else
+#define MCFD_IA_FN static inline
+#endif
+
+namespace mcfd {
+namespace ia {
+
+typedef unsigned long long u64;
+
+MCFD_IA_FN u64 mulhi(u64 a, u64 b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return (u64)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+MCFD_IA_FN u64 bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (u64)__double_as_longlong(x);
+#else
+  u64 r;
+  memcpy(&r, &x, 8);
+  return r;
+#endif
+}
+MCFD_IA_FN double from_bits(u64 b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)b);
+#else
+  double r;
+  memcpy(&r, &b, 8);
+  return r;
+#endif
+}
+// fp32 approximations of 1/t and 1/sqrt(t), t a positive normal float
+MCFD_IA_FN float rcp_seed(float t) {
+#if defined(__CUDA_ARCH__)
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(t));
+  return y;
+#else
+  return 1.0f / t;
+#endif
+}
+MCFD_IA_FN float rsqrt_seed(float t) {
+#if defined(__CUDA_ARCH__)
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(t));
+  return y;
+#else
+  return 1.0f / sqrtf(t);
+#endif
+}
+// truncating float -> uint32 conversion, saturating at 2^32 - 1 (v > 0)
+MCFD_IA_FN unsigned to_u32(float v) {
+#if defined(__CUDA_ARCH__)
+  return __float2uint_rz(v);
+#else
+  return v >= 4294967296.0f ? 0xffffffffu : (unsigned)v;
+#endif
+}
+
+static constexpr u64 kMant = 0x000fffffffffffffull;
+static constexpr u64 kImpl = 0x0010000000000000ull;
+static constexpr u64 kSign = 0x8000000000000000ull;
+
+// Round the 55-bit truncated significand q (53 bits, guard bit, one more bit)
+// with the remainder's sticky bit; returns the 53-bit significand and bumps e
+// when rounding carries into the next binade.
+MCFD_IA_FN u64 round_q55(u64 q, bool inexact_tail, int& e) {
+  u64 m = q >> 2;
+  const u64 guard = (q >> 1) & 1ull;
+  const u64 sticky = (q & 1ull) | (u64)inexact_tail;
+  m += guard & (sticky | (m & 1ull));
+  const unsigned carry = (unsigned)(m >> 53);
+  e += (int)carry;
+  return m >> carry;
+}
+
+MCFD_IA_FN double div_rn(double a, double b) {
+  const u64 ia = bits(a), ib = bits(b);
+  const unsigned ea = (unsigned)(ia >> 52) & 0x7ffu, eb = (unsigned)(ib >> 52) & 0x7ffu;
+  const u64 ma = (ia & kMant) | kImpl, mb = (ib & kMant) | kImpl;
+  const unsigned sh = ma < mb ? 1u : 0u;
+  const u64 A = ma << sh;  // A / mb in [1, 2)
+  int e = (int)ea - (int)eb + 1023 - (int)sh;
+  // seed: x32 ~ 2^87 / (mb >> 29) ~ 2^84 / mb (the float conversion is exact)
+  const unsigned x32 = to_u32(rcp_seed((float)(unsigned)(mb >> 29)) * 0x1p55f);
+  // Newton step 1 on X = x32 2^32 (~2^116 / mb): D = 2^84 - mb x32 (mod 2^64,
+  // |D| < 2^62), X += X D / 2^84
+  long long D = -(long long)(mb * (u64)x32);
+  u64 ad = D < 0 ? (u64)(-D) : (u64)D;
+  u64 h = (mulhi((u64)x32, ad) << 12) | (((u64)x32 * ad) >> 52);
+  u64 X = (u64)x32 << 32;
+  X = D < 0 ? X - h : X + h;
+  // Newton step 2: D = 2^84 - (mb X >> 32), X += X D / 2^84
+  {
+    const u64 ph = mulhi(mb, X), pl = mb * X;
+    D = -(long long)((ph << 32) | (pl >> 32));
+    ad = D < 0 ? (u64)(-D) : (u64)D;
+    h = mulhi(X, ad) >> 20;
+    X = D < 0 ? X - h : X + h;
+  }
+  // Q = floor(A 2^54 / mb) in [2^54, 2^55), corrected by the exact remainder
+  u64 Q = (mulhi(A, X) << 2) | ((A * X) >> 62);
+  long long R = (long long)((A << 54) - Q * mb);
+  const long long B = (long long)mb;
+  if (R < 0) {
+    Q -= 1; R += B;
+    if (R < 0) { Q -= 1; R += B; }
+  } else if (R >= B) {
+    Q += 1; R -= B;
+    if (R >= B) { Q += 1; R -= B; }
+  }
+  const bool in_range = R >= 0 && R < B;
+  const bool underflow = e < 1;
+  const u64 m = round_q55(Q, R != 0, e);
+  if (ea - 1u >= 0x7feu || eb - 1u >= 0x7feu || underflow || e > 2046 || !in_range) return a / b;
+  return from_bits(((ia ^ ib) & kSign) | ((u64)e << 52) | (m & kMant));
+}
+
+MCFD_IA_FN double sqrt_rn(double x) {
+  const u64 ix = bits(x);
+  const unsigned ex = (unsigned)(ix >> 52);   // a set sign bit puts ex out of range
+  const unsigned odd = (ex & 1u) ^ 1u;        // the unbiased exponent is odd
+  const u64 M = ((ix & kMant) | kImpl) << odd;  // [2^52, 2^54), even exponent left
+  int e = (((int)ex - 1023 - (int)odd) >> 1) + 1023;
+  // seed: y32 ~ 2^43 / sqrt(M >> 30) ~ 2^31 / sqrt(M / 2^54)
+  const unsigned y32 = to_u32(rsqrt_seed((float)(unsigned)(M >> 30)) * 0x1p43f);
+  // Newton step 1 on Y = y32 2^32: D = 2^80 - (M y32^2 >> 36) (|D| < 2^60),
+  // Y += Y D / 2^81
+  u64 S2 = (u64)y32 * y32;
+  long long D = -(long long)((mulhi(M, S2) << 28) | ((M * S2) >> 36));
+  u64 ad = D < 0 ? (u64)(-D) : (u64)D;
+  u64 h = (mulhi((u64)y32, ad) << 15) | (((u64)y32 * ad) >> 49);
+  u64 Y = (u64)y32 << 32;
+  Y = D < 0 ? Y - h : Y + h;
+  // Newton step 2: S2 = Y^2 / 2^64, D = 2^80 - (M S2 >> 36), Y += Y D / 2^81
+  {
+    S2 = mulhi(Y, Y);
+    D = -(long long)((mulhi(M, S2) << 28) | ((M * S2) >> 36));
+    ad = D < 0 ? (u64)(-D) : (u64)D;
+    h = mulhi(Y, ad) >> 17;
+    Y = D < 0 ? Y - h : Y + h;
+  }
+  // S = floor(sqrt(M 2^56)) in [2^54, 2^55), corrected by R = M 2^56 - S^2
+  u64 S = (mulhi(M, Y) << 2) | ((M * Y) >> 62);
+  long long R = (long long)((M << 56) - S * S);
+  if (R < 0) {
+    S -= 1; R += (long long)(2 * S + 1);
+    if (R < 0) { S -= 1; R += (long long)(2 * S + 1); }
+  } else if (R > (long long)(2 * S)) {
+    R -= (long long)(2 * S + 1); S += 1;
+    if (R > (long long)(2 * S)) { R -= (long long)(2 * S + 1); S += 1; }
+  }
+  const bool in_range = R >= 0 && R <= (long long)(2 * S);
+  const u64 m = round_q55(S, R != 0, e);
+  if (ex - 1u >= 0x7feu || !in_range) return sqrt(x);
+  return from_bits(((u64)e << 52) | (m & kMant));
+}
+
+}  // namespace ia
+
+using ia::div_rn;
+using ia::sqrt_rn;
+
+}  // namespace mcfd
+
+#undef MCFD_IA_FN

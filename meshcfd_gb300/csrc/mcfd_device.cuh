@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include "../../include/meshcfd_gb300.h"
+#include "mcfd_arith.cuh"
 
 namespace mcfd {
 
@@ -92,9 +93,9 @@ __device__ __forceinline__ bool finite4(const St4& s) {
 // euler.conservative_to_primitive (euler.py:20-40), one row.
 __device__ __forceinline__ St4 cons_to_prim(const St4& U, double gamma, bool* ok) {
   double rho = U.a;
-  double ux = U.b / rho;
-  double uy = U.c / rho;
-  double p = (gamma - 1.0) * (U.d - (0.5 * (U.b * U.b + U.c * U.c)) / rho);
+  double ux = div_rn(U.b, rho);
+  double uy = div_rn(U.c, rho);
+  double p = (gamma - 1.0) * (U.d - div_rn(0.5 * (U.b * U.b + U.c * U.c), rho));
   St4 P{rho, ux, uy, p};
   *ok = finite4(P) && icmp::gt0(rho) && icmp::gt0(p);
   return P;
@@ -104,7 +105,7 @@ __device__ __forceinline__ St4 cons_to_prim(const St4& U, double gamma, bool* ok
 __device__ __forceinline__ void physical_flux(const St4& q, double nx, double ny, double gamma,
                                               double F[4], double U[4]) {
   double rho = q.a, ux = q.b, uy = q.c, p = q.d;
-  double energy = p / (gamma - 1.0) + (0.5 * rho) * (ux * ux + uy * uy);
+  double energy = div_rn(p, gamma - 1.0) + (0.5 * rho) * (ux * ux + uy * uy);
   double un = ux * nx + uy * ny;
   U[0] = rho;
   U[1] = rho * ux;
@@ -117,7 +118,7 @@ __device__ __forceinline__ void physical_flux(const St4& q, double nx, double ny
 }
 
 __device__ __forceinline__ double sound_speed(double rho, double p, double gamma) {
-  return sqrt((gamma * p) / rho);
+  return sqrt_rn(div_rn(gamma * p, rho));
 }
 
 // euler._rusanov_flux (euler.py:80-93).
@@ -156,7 +157,7 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
   double wr = py_max(unl + cl, unr + cr);
   double den = rl * (wl - unl) - rr * (wr - unr);
   if (!icmp::abs_gt(den, 1e-14)) den = copysign(1e-14, den);
-  double contact = ((pr - pl) + (rl * unl) * (wl - unl) - (rr * unr) * (wr - unr)) / den;
+  double contact = div_rn((pr - pl) + (rl * unl) * (wl - unl) - (rr * unr) * (wr - unr), den);
 
   int branch;  // 0: F_L, 1: F*_L, 2: F*_R, 3: F_R
   if (KERNEL_BRANCHES) {
@@ -181,10 +182,10 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
     double un = left ? unl : unr;
     double wave = left ? wl : wr;
     double rho = q.a, pressure = q.d;
-    double factor = (rho * (wave - un)) / (wave - contact);
+    double factor = div_rn(rho * (wave - un), wave - contact);
     double sux = q.b + (contact - un) * nx;
     double suy = q.c + (contact - un) * ny;
-    double se = factor * (U[3] / rho + (contact - un) * (contact + pressure / (rho * (wave - un))));
+    double se = factor * (div_rn(U[3], rho) + (contact - un) * (contact + div_rn(pressure, rho * (wave - un))));
     double star[4] = {factor, factor * sux, factor * suy, se};
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = F[k] + wave * (star[k] - U[k]);
@@ -203,12 +204,12 @@ __device__ __forceinline__ int roe_flux(const St4& L, const St4& R, double nx, d
   double FL[4], UL[4], FR[4], UR[4];
   physical_flux(L, nx, ny, gamma, FL, UL);
   physical_flux(R, nx, ny, gamma, FR, UR);
-  double root_l = sqrt(L.a), root_r = sqrt(R.a);
+  double root_l = sqrt_rn(L.a), root_r = sqrt_rn(R.a);
   double den = root_l + root_r;
-  double vx = (root_l * L.b + root_r * R.b) / den;
-  double vy = (root_l * L.c + root_r * R.c) / den;
-  double H = (root_l * (L.d / L.a + 0.5 * (L.b * L.b + L.c * L.c)) +
-              root_r * (R.d / R.a + 0.5 * (R.b * R.b + R.c * R.c))) / den;
+  double vx = div_rn(root_l * L.b + root_r * R.b, den);
+  double vy = div_rn(root_l * L.c + root_r * R.c, den);
+  double H = div_rn(root_l * (div_rn(L.d, L.a) + 0.5 * (L.b * L.b + L.c * L.c)) +
+                    root_r * (div_rn(R.d, R.a) + 0.5 * (R.b * R.b + R.c * R.c)), den);
   double un = vx * nx + vy * ny;
   double ut = vx * -ny + vy * nx;
   double c2 = (gamma - 1.0) * (H - 0.5 * (vx * vx + vy * vy));
@@ -216,14 +217,14 @@ __device__ __forceinline__ int roe_flux(const St4& L, const St4& R, double nx, d
     out[0] = out[1] = out[2] = out[3] = 0.0;
     return MCFD_S_ROE_SOUND;
   }
-  double c = sqrt(c2);
+  double c = sqrt_rn(c2);
   double ravg = root_l * root_r;
   double unl = L.b * nx + L.c * ny, unr = R.b * nx + R.c * ny;
   double utl = L.b * -ny + L.c * nx, utr = R.b * -ny + R.c * nx;
   double dr = R.a - L.a, dun = unr - unl, dut = utr - utl, dp = R.d - L.d;
-  double am = (dp - (ravg * c) * dun) / (2.0 * c2);
-  double ap = (dp + (ravg * c) * dun) / (2.0 * c2);
-  double ac = dr - dp / c2;
+  double am = div_rn(dp - (ravg * c) * dun, 2.0 * c2);
+  double ap = div_rn(dp + (ravg * c) * dun, 2.0 * c2);
+  double ac = dr - div_rn(dp, c2);
   double as = ravg * dut;
   double lam[4] = {un - c, un, un, un + c};
   double fix = 0.1 * c;
@@ -232,7 +233,7 @@ __device__ __forceinline__ int roe_flux(const St4& L, const St4& R, double nx, d
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     double a = fabs(lam[j]);
-    if (icmp::lt_nonneg(a, fix)) a = 0.5 * ((a * a) / fix + fix);
+    if (icmp::lt_nonneg(a, fix)) a = 0.5 * (div_rn(a * a, fix) + fix);
     w[j] = a * strength[j];
   }
   double e[4][4] = {{1.0, 1.0, 0.0, 1.0},
@@ -269,8 +270,8 @@ __device__ __forceinline__ int far_field_state(const St4& in, const St4& far, do
     *ext = in;
     return 0;
   }
-  double out_inv = un_i + (2.0 * c_i) / (gamma - 1.0);
-  double in_inv = un_f - (2.0 * c_f) / (gamma - 1.0);
+  double out_inv = un_i + div_rn(2.0 * c_i, gamma - 1.0);
+  double in_inv = un_f - div_rn(2.0 * c_f, gamma - 1.0);
   double vb = 0.5 * (out_inv + in_inv);
   double cb = (0.25 * (gamma - 1.0)) * (out_inv - in_inv);
   if (!icmp::finite(cb) || icmp::le0(cb)) {
@@ -278,8 +279,8 @@ __device__ __forceinline__ int far_field_state(const St4& in, const St4& far, do
     return MCFD_S_FARFIELD_SOUND;
   }
   const St4& src = icmp::ge0(vb) ? in : far;
-  double entropy = src.d / pow(src.a, gamma);
-  double rho = pow((cb * cb) / (gamma * entropy), 1.0 / (gamma - 1.0));
+  double entropy = div_rn(src.d, pow(src.a, gamma));
+  double rho = pow(div_rn(cb * cb, gamma * entropy), div_rn(1.0, gamma - 1.0));
   double p = entropy * pow(rho, gamma);
   double tx = -ny, ty = nx;
   double vt = src.b * tx + src.c * ty;
@@ -300,7 +301,7 @@ __device__ __forceinline__ double limiter_face_factor(double value, double incre
   const bool pos = icmp::gt_pos(increment, tolerance);
   const bool neg = icmp::neg_gt_pos(increment, tolerance);
   const double num = pos ? (hi - value) : (lo - value);
-  const double q = num / ((pos || neg) ? increment : 1.0);
+  const double q = div_rn(num, (pos || neg) ? increment : 1.0);
   double ratio = (pos || neg) ? q : 1.0;
   ratio = icmp::ge0(ratio) ? ratio : 0.0;  // max(ratio, 0.0)
   double f;
@@ -308,14 +309,14 @@ __device__ __forceinline__ double limiter_face_factor(double value, double incre
     f = icmp::gt_pos(ratio, 1.0) ? 1.0 : ratio;  // min(ratio, 1.0)
   } else if (LIMITER == 2) {
     if (icmp::gt0(ratio)) {
-      double q = (2.0 * ratio) / (1.0 + ratio);
+      double q = div_rn(2.0 * ratio, 1.0 + ratio);
       f = icmp::lt_pos(q, 1.0) ? q : 1.0;  // min(1.0, q)
     } else {
       f = 0.0;
     }
   } else {
     const double eps = 1e-12;
-    f = ((ratio * ratio + 2.0 * ratio) + eps) / (((ratio * ratio + ratio) + 2.0) + eps);
+    f = div_rn((ratio * ratio + 2.0 * ratio) + eps, ((ratio * ratio + ratio) + 2.0) + eps);
     f = icmp::gt_pos(f, 1.0) ? 1.0 : f;  // min(f, 1.0)
   }
   return f;
@@ -337,8 +338,8 @@ __device__ __forceinline__ double limiter_factor_min_ratio(double value, double 
                                                           bool has_pos, bool has_neg, bool flat) {
   double r = 1.0;  // the tolerance band's ratio (only used when flat)
   bool any = flat;
-  const double rp = (hi - value) / (has_pos ? pos_max : 1.0);
-  const double rn = (lo - value) / (has_neg ? neg_min : -1.0);
+  const double rp = div_rn(hi - value, has_pos ? pos_max : 1.0);
+  const double rn = div_rn(lo - value, has_neg ? neg_min : -1.0);
   if (has_pos) {
     double x = icmp::ge0(rp) ? rp : 0.0;
     r = (!any || icmp::lt(x, r)) ? x : r;
@@ -354,11 +355,11 @@ __device__ __forceinline__ double limiter_factor_min_ratio(double value, double 
   if (LIMITER <= 1) {
     f = icmp::gt_pos(r, 1.0) ? 1.0 : r;
   } else if (LIMITER == 2) {
-    const double q = (2.0 * r) / (1.0 + r);
+    const double q = div_rn(2.0 * r, 1.0 + r);
     f = icmp::gt0(r) ? (icmp::lt_pos(q, 1.0) ? q : 1.0) : 0.0;
   } else {
     const double eps = 1e-12;
-    f = ((r * r + 2.0 * r) + eps) / (((r * r + r) + 2.0) + eps);
+    f = div_rn((r * r + 2.0 * r) + eps, ((r * r + r) + 2.0) + eps);
     f = icmp::gt_pos(f, 1.0) ? 1.0 : f;
   }
   return f;
@@ -376,7 +377,7 @@ __device__ __forceinline__ double limiter_tolerance(double value) {
 // Primitive recovery with one reciprocal instead of three divisions.
 __device__ __forceinline__ St4 cons_to_prim_fast(const St4& U, double gamma, bool* ok) {
   double rho = U.a;
-  double inv = 1.0 / rho;
+  double inv = div_rn(1.0, rho);
   double ux = U.b * inv;
   double uy = U.c * inv;
   double p = (gamma - 1.0) * (U.d - 0.5 * (U.b * U.b + U.c * U.c) * inv);
@@ -410,18 +411,18 @@ __device__ __forceinline__ bool hllc_flux_fast(const St4& L, const St4& R, doubl
   physical_flux_fast(L, nx, ny, inv_gm1, FL, UL);
   physical_flux_fast(R, nx, ny, inv_gm1, FR, UR);
   double rl = L.a, pl = L.d, rr = R.a, pr = R.d;
-  double t = 1.0 / (rl * rr);
+  double t = div_rn(1.0, rl * rr);
   double irl = rr * t, irr = rl * t;
   double unl = L.b * nx + L.c * ny;
   double unr = R.b * nx + R.c * ny;
-  double cl = sqrt(gamma * pl * irl);
-  double cr = sqrt(gamma * pr * irr);
+  double cl = sqrt_rn(gamma * pl * irl);
+  double cr = sqrt_rn(gamma * pr * irr);
   double wl = py_min(unl - cl, unr - cr);
   double wr = py_max(unl + cl, unr + cr);
   double ml = rl * (wl - unl), mr = rr * (wr - unr);
   double den = ml - mr;
   if (!icmp::abs_gt(den, 1e-14)) den = copysign(1e-14, den);
-  double contact = ((pr - pl) + unl * ml - unr * mr) / den;
+  double contact = div_rn((pr - pl) + unl * ml - unr * mr, den);
   int branch;
   if (KERNEL_BRANCHES) {
     if (icmp::ge0(wl)) branch = 0;
@@ -447,7 +448,7 @@ __device__ __forceinline__ bool hllc_flux_fast(const St4& L, const St4& R, doubl
     double m = left ? ml : mr;          // rho (S - un)
     double irho = left ? irl : irr;
     double d = wave - contact;
-    double s = 1.0 / (m * d);
+    double s = div_rn(1.0, m * d);
     double factor = m * m * s;          // rho (S - un) / (S - S*)
     double p_over_m = q.d * d * s;      // p / (rho (S - un))
     double sux = q.b + (contact - un) * nx;
@@ -467,11 +468,11 @@ __device__ __forceinline__ void rusanov_flux_fast(const St4& L, const St4& R, do
   double FL[4], UL[4], FR[4], UR[4];
   physical_flux_fast(L, nx, ny, inv_gm1, FL, UL);
   physical_flux_fast(R, nx, ny, inv_gm1, FR, UR);
-  double t = 1.0 / (L.a * R.a);
+  double t = div_rn(1.0, L.a * R.a);
   double unl = L.b * nx + L.c * ny;
   double unr = R.b * nx + R.c * ny;
-  double sl = fabs(unl) + sqrt(gamma * L.d * (R.a * t));
-  double sr = fabs(unr) + sqrt(gamma * R.d * (L.a * t));
+  double sl = fabs(unl) + sqrt_rn(gamma * L.d * (R.a * t));
+  double sr = fabs(unr) + sqrt_rn(gamma * R.d * (L.a * t));
   double s = icmp::lt_nonneg(sl, sr) ? sr : sl;
 #pragma unroll
   for (int k = 0; k < 4; ++k) out[k] = 0.5 * ((FL[k] + FR[k]) - s * (UR[k] - UL[k]));
@@ -482,13 +483,13 @@ __device__ __forceinline__ int roe_flux_fast(const St4& L, const St4& R, double 
   double FL[4], UL[4], FR[4], UR[4];
   physical_flux_fast(L, nx, ny, inv_gm1, FL, UL);
   physical_flux_fast(R, nx, ny, inv_gm1, FR, UR);
-  double root_l = sqrt(L.a), root_r = sqrt(R.a);
-  double iden = 1.0 / (root_l + root_r);
+  double root_l = sqrt_rn(L.a), root_r = sqrt_rn(R.a);
+  double iden = div_rn(1.0, root_l + root_r);
   double vx = (root_l * L.b + root_r * R.b) * iden;
   double vy = (root_l * L.c + root_r * R.c) * iden;
   // The reference's averaged "enthalpy" is sqrt(rho)-weighted p/rho + |u|^2/2
   // (euler.py:181-185); with rho = root^2, root * p / rho = p / root.
-  double H = (L.d / root_l + R.d / root_r + 0.5 * (root_l * (L.b * L.b + L.c * L.c) +
+  double H = (div_rn(L.d, root_l) + div_rn(R.d, root_r) + 0.5 * (root_l * (L.b * L.b + L.c * L.c) +
                                                   root_r * (R.b * R.b + R.c * R.c))) * iden;
   double un = vx * nx + vy * ny;
   double ut = vx * -ny + vy * nx;
@@ -497,8 +498,8 @@ __device__ __forceinline__ int roe_flux_fast(const St4& L, const St4& R, double 
     out[0] = out[1] = out[2] = out[3] = 0.0;
     return MCFD_S_ROE_SOUND;
   }
-  double c = sqrt(c2);
-  double ic2 = 1.0 / c2;
+  double c = sqrt_rn(c2);
+  double ic2 = div_rn(1.0, c2);
   double ravg = root_l * root_r;
   double unl = L.b * nx + L.c * ny, unr = R.b * nx + R.c * ny;
   double utl = L.b * -ny + L.c * nx, utr = R.b * -ny + R.c * nx;
@@ -508,7 +509,7 @@ __device__ __forceinline__ int roe_flux_fast(const St4& L, const St4& R, double 
   double ac = dr - dp * ic2;
   double as = ravg * dut;
   double lam[4] = {un - c, un, un, un + c};
-  double fix = 0.1 * c, ifix = 10.0 / c;
+  double fix = 0.1 * c, ifix = div_rn(10.0, c);
   double w[4];
   double strength[4] = {am, ac, as, ap};
 #pragma unroll
@@ -553,23 +554,23 @@ __device__ __forceinline__ double limiter_factor_fast(double hi_minus_v, double 
     a = v_minus_lo;
     b = neg_max;
   } else {
-    return flat ? (LIMITER == 3 ? (3.0 + 1e-12) / (4.0 + 1e-12) : 1.0) : 1.0;
+    return flat ? (LIMITER == 3 ? div_rn(3.0 + 1e-12, 4.0 + 1e-12) : 1.0) : 1.0;
   }
   if (flat && !icmp::lt_nonneg(a, b)) {  // the tolerance band's ratio 1 is the smallest
     a = 1.0;
     b = 1.0;
   }
   if (LIMITER <= 1) {
-    return icmp::lt_nonneg(a, b) ? a / b : 1.0;
+    return icmp::lt_nonneg(a, b) ? div_rn(a, b) : 1.0;
   } else if (LIMITER == 2) {
     if (!icmp::gt0(a)) return 0.0;
-    double q = (2.0 * a) / (a + b);
+    double q = div_rn(2.0 * a, a + b);
     return icmp::lt_pos(q, 1.0) ? q : 1.0;
   } else {
     const double eps = 1e-12;
     if (!icmp::lt_nonneg(a, 2.0 * b)) return 1.0;
     double bb = b * b;
-    return (a * a + 2.0 * a * b + eps * bb) / (a * a + a * b + 2.0 * bb + eps * bb);
+    return div_rn(a * a + 2.0 * a * b + eps * bb, a * a + a * b + 2.0 * bb + eps * bb);
   }
 }
 

@@ -1,5 +1,6 @@
-// Variant-independent kernels: the residual sum of squares and the launch
-// counter.  Compiled with -fmad=false (plain additions in a fixed tree).
+// Variant-independent kernels: the residual sum of squares, the launch
+// counter and the element-wise division / square root entry point.  Compiled
+// with -fmad=false (plain additions in a fixed tree).
 #include "mcfd_device.cuh"
 #include "mcfd_internal.h"
 
@@ -99,4 +100,29 @@ cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, in
   return cudaGetLastError();
 }
 
+// ------------------------------------------------- division and square root
+
+__global__ void __launch_bounds__(kBlock) k_ieee_div_sqrt(long long n, const double* __restrict__ a,
+                                                          const double* __restrict__ b,
+                                                          double* __restrict__ quotient,
+                                                          double* __restrict__ root) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double x = a[i];
+    if (quotient) quotient[i] = div_rn(x, b[i]);
+    if (root) root[i] = sqrt_rn(x);
+  }
+}
+
 }  // namespace mcfd
+
+extern "C" int mcfd_ieee_div_sqrt(const double* a, const double* b, int64_t n, double* quotient,
+                                  double* root, void* stream) {
+  if (n < 0 || (n > 0 && !a) || (quotient && !b)) return MCFD_E_ARG;
+  if (n == 0 || (!quotient && !root)) return MCFD_OK;
+  const long long blocks = (n + mcfd::kBlock - 1) / mcfd::kBlock;
+  mcfd::count_launch(1);
+  mcfd::k_ieee_div_sqrt<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), mcfd::kBlock, 0,
+                          static_cast<cudaStream_t>(stream)>>>(n, a, b, quotient, root);
+  return cudaGetLastError() == cudaSuccess ? MCFD_OK : MCFD_E_CUDA;
+}

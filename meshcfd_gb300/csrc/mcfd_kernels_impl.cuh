@@ -320,10 +320,10 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
     for (int j = jb0; j < jb1; ++j) {
       const double len = g.gb_len[j];
       const St4 F = ld4(flux + 4 * (size_t)g.gb_flux[j]);
-      r[0] = r[0] + (F.a * len) / area;
-      r[1] = r[1] + (F.b * len) / area;
-      r[2] = r[2] + (F.c * len) / area;
-      r[3] = r[3] + (F.d * len) / area;
+      r[0] = r[0] + div_rn(F.a * len, area);
+      r[1] = r[1] + div_rn(F.b * len, area);
+      r[2] = r[2] + div_rn(F.c * len, area);
+      r[3] = r[3] + div_rn(F.d * len, area);
     }
   }
   const St4 p = ld4(P + 4 * (size_t)c);
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
       sum = sum + radius * g.dt_len[e];
     }
     if (diffusion) sum += 2.0 * diffusion[c];  // viscous terms (solver.py:4331)
-    dt = (cfl * g.area[c]) / sum;
+    dt = div_rn(cfl * g.area[c], sum);
     if (!icmp::finite(dt) || !icmp::gt0(dt)) bits |= MCFD_S_TIME_STEP;
     if (bits) flag_cell(g.status, bits, c);
     if (dt_cells) dt_cells[c] = dt;
