@@ -579,12 +579,28 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
     }
   }
 
+  // ---- visiting order of the per-cell stage kernels: cells grouped by their
+  // entry counts (stable), so that each warp's loops share one trip count
+  std::vector<int> cell_order(C);
+  {
+    auto count = [](const std::vector<int>& ptr, size_t c) { return ptr.empty() ? 0 : ptr[c + 1] - ptr[c]; };
+    std::vector<long long> ckey(C);
+    for (size_t c = 0; c < C; ++c) {
+      const long long k0 = count(grad_ptr, c), k1 = count(lim_ptr, c), k2 = count(gi_ptr, c),
+                      k3 = count(gb_ptr, c), k4 = count(dt_ptr, c);
+      auto clamp = [](long long v) { return v < 0 ? 0 : (v > 4095 ? 4095 : v); };
+      ckey[c] = (((clamp(k0) * 4096 + clamp(k1)) * 4096 + clamp(k2)) * 4096 + clamp(k3)) * 64 + (k4 > 63 ? 63 : k4);
+    }
+    for (size_t c = 0; c < C; ++c) cell_order[c] = (int)c;
+    std::stable_sort(cell_order.begin(), cell_order.end(), [&](int a, int b) { return ckey[a] < ckey[b]; });
+  }
+
   // ---- arena layout
   Arena A;
   auto bytes_i = [](size_t n) { return n * sizeof(int); };
   auto bytes_d = [](size_t n) { return n * sizeof(double); };
   const int partial_blocks = 152 * 4;
-  size_t o_area = A.take(bytes_d(C));
+  size_t o_area = A.take(bytes_d(C)), o_cell_order = A.take(bytes_i(C));
   size_t o_grad_ptr = A.take(bytes_i(C + 1)), o_grad_nb = A.take(bytes_i(NG)),
          o_grad_cx = A.take(bytes_d(NG)), o_grad_cy = A.take(bytes_d(NG)), o_grad_twin = A.take(bytes_i(NG));
   size_t o_lim_ptr = A.take(bytes_i(C + 1)), o_lim_slot = A.take(bytes_i(NL)),
@@ -633,6 +649,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
     if (bytes) std::memcpy(host.data() + off, src, bytes);
   };
   put(o_area, d->areas, bytes_d(C));
+  put(o_cell_order, cell_order.data(), bytes_i(C));
   put(o_grad_ptr, grad_ptr.data(), bytes_i(C + 1));
   put(o_grad_nb, grad_nb.data(), bytes_i(NG));
   put(o_grad_cx, grad_cx.data(), bytes_d(NG));
@@ -708,6 +725,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   for (int k = 0; k <= SEG_COUNT; ++k) g.seg_begin[k] = seg_begin[k];
 #define AT(T, off) reinterpret_cast<T>(base + (off))
   g.area = AT(const double*, o_area);
+  g.cell_order = AT(const int*, o_cell_order);
   g.grad_ptr = AT(const int*, o_grad_ptr);
   g.grad_nb = AT(const int*, o_grad_nb);
   g.grad_cx = AT(const double*, o_grad_cx);

@@ -1,5 +1,5 @@
 // IEEE-754 binary64 division and square root, round to nearest even,
-// evaluated on the integer pipe.
+// evaluated on the integer pipe (plus exact negation and doubling).
 //
 // On GB300 one FP64 division or square root costs ~8.6 FP64 issue slots
 // (~58 G/s per GPU) while the integer pipe runs ~38x the FP64 rate, so the
@@ -199,10 +199,24 @@ MCFD_IA_FN double sqrt_rn(double x) {
   return from_bits(((u64)e << 52) | (m & kMant));
 }
 
+// -x (IEEE negation is exact: the sign bit flips, also for zeros and NaN)
+MCFD_IA_FN double negate(double x) { return from_bits(bits(x) ^ kSign); }
+
+// 2 x, exact: the exponent field steps by one for normal x below the largest
+// binade; zeros, subnormals, the top binade, infinities and NaN go to the FP64
+// unit.
+MCFD_IA_FN double twice(double x) {
+  const u64 b = bits(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  return e - 1u < 2045u ? from_bits(b + (1ull << 52)) : 2.0 * x;
+}
+
 }  // namespace ia
 
 using ia::div_rn;
+using ia::negate;
 using ia::sqrt_rn;
+using ia::twice;
 
 }  // namespace mcfd
 

@@ -142,12 +142,13 @@ __device__ __forceinline__ void rusanov_flux(const St4& L, const St4& R, double 
 // (euler.py:155-163): S_L>=0 -> F_L, S*>=0 -> F*_L, S_R>0 -> F*_R, else F_R,
 // followed by its finiteness check (euler.py:164-165).  Returns false when the
 // NumPy form produced a non-finite value.
+//
+// Every branch uses one side's physical flux and conservative state only, so
+// the side is chosen first and its physical flux evaluated alone (the same
+// expressions as for both sides, so the same values).
 template <bool KERNEL_BRANCHES>
 __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx, double ny,
                                           double gamma, double out[4]) {
-  double FL[4], UL[4], FR[4], UR[4];
-  physical_flux(L, nx, ny, gamma, FL, UL);
-  physical_flux(R, nx, ny, gamma, FR, UR);
   double rl = L.a, pl = L.d, rr = R.a, pr = R.d;
   double unl = L.b * nx + L.c * ny;
   double unr = R.b * nx + R.c * ny;
@@ -170,15 +171,14 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
     else if (icmp::gt0(wr)) branch = 2;
     else branch = 3;
   }
+  const bool left = branch <= 1;
+  const St4 q = left ? L : R;
+  double F[4], U[4];
+  physical_flux(q, nx, ny, gamma, F, U);
   if (branch == 0 || branch == 3) {
-    const double* F = (branch == 0) ? FL : FR;
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = F[k];
   } else {
-    const bool left = (branch == 1);
-    const St4& q = left ? L : R;
-    const double* U = left ? UL : UR;
-    const double* F = left ? FL : FR;
     double un = left ? unl : unr;
     double wave = left ? wl : wr;
     double rho = q.a, pressure = q.d;
@@ -355,11 +355,12 @@ __device__ __forceinline__ double limiter_factor_min_ratio(double value, double 
   if (LIMITER <= 1) {
     f = icmp::gt_pos(r, 1.0) ? 1.0 : r;
   } else if (LIMITER == 2) {
-    const double q = div_rn(2.0 * r, 1.0 + r);
+    const double q = div_rn(twice(r), 1.0 + r);
     f = icmp::gt0(r) ? (icmp::lt_pos(q, 1.0) ? q : 1.0) : 0.0;
   } else {
     const double eps = 1e-12;
-    f = div_rn((r * r + 2.0 * r) + eps, ((r * r + r) + 2.0) + eps);
+    const double rr = r * r;
+    f = div_rn((rr + twice(r)) + eps, ((rr + r) + 2.0) + eps);
     f = icmp::gt_pos(f, 1.0) ? 1.0 : f;
   }
   return f;
@@ -407,9 +408,6 @@ __device__ __forceinline__ void physical_flux_fast(const St4& q, double nx, doub
 template <bool KERNEL_BRANCHES>
 __device__ __forceinline__ bool hllc_flux_fast(const St4& L, const St4& R, double nx, double ny,
                                                double gamma, double inv_gm1, double out[4]) {
-  double FL[4], UL[4], FR[4], UR[4];
-  physical_flux_fast(L, nx, ny, inv_gm1, FL, UL);
-  physical_flux_fast(R, nx, ny, inv_gm1, FR, UR);
   double rl = L.a, pl = L.d, rr = R.a, pr = R.d;
   double t = div_rn(1.0, rl * rr);
   double irl = rr * t, irr = rl * t;
@@ -434,15 +432,14 @@ __device__ __forceinline__ bool hllc_flux_fast(const St4& L, const St4& R, doubl
     else if (icmp::gt0(wr)) branch = 2;
     else branch = 3;
   }
+  const bool left = branch <= 1;
+  const St4 q = left ? L : R;
+  double F[4], U[4];
+  physical_flux_fast(q, nx, ny, inv_gm1, F, U);
   if (branch == 0 || branch == 3) {
-    const double* F = (branch == 0) ? FL : FR;
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = F[k];
   } else {
-    const bool left = (branch == 1);
-    const St4& q = left ? L : R;
-    const double* U = left ? UL : UR;
-    const double* F = left ? FL : FR;
     double un = left ? unl : unr;
     double wave = left ? wl : wr;
     double m = left ? ml : mr;          // rho (S - un)

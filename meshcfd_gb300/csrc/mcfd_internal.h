@@ -35,6 +35,9 @@ struct DevGeom {
   int n_cells, n_faces, n_flux, n_slots, n_gradient;
   int seg_begin[SEG_COUNT + 1];
   const double* area;  // [C]
+  // cells grouped by (gradient, limiter, gather, time-step) entry counts,
+  // stable in cell id: the visiting order of the per-cell stage kernels
+  const int* cell_order;  // [C]
   // least-squares gradient entries grouped by source cell, reference order
   const int* grad_ptr;
   const int* grad_nb;

@@ -75,12 +75,19 @@ __global__ void __launch_bounds__(kBlock) k_primitive(int n, const double* __res
 // ("slot") as the reconstructed face state P + phi * (grad . r), which is
 // exactly the left/right state of the fused flux kernel (_kernels.py:90-98)
 // and of _reconstruct (solver.py:2418-2434).
+//
+// The per-cell kernels visit cells through g.cell_order, which groups cells
+// with the same stencil and face counts so that a warp's loops share one trip
+// count (on mixed meshes a warp of triangles and quads otherwise runs every
+// triangle lane idle through the fourth entry, which still costs FP64 issue
+// slots).  Each cell's arithmetic and outputs do not depend on the order.
 
 template <int LIMITER>
 __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double* __restrict__ P,
                                                         double* __restrict__ recon) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.n_cells) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n_cells) return;
+  const int c = g.cell_order[i];
   const St4 p = ld4(P + 4 * (size_t)c);
   double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
   double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
@@ -136,8 +143,9 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
 template <int LIMITER>
 __global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const double* __restrict__ P,
                                                              double* __restrict__ recon) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.n_cells) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n_cells) return;
+  const int c = g.cell_order[i];
   const St4 p = ld4(P + 4 * (size_t)c);
   const double pv[4] = {p.a, p.b, p.c, p.d};
   double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
@@ -184,7 +192,8 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const do
           if (icmp::lt_nonneg(pos[v], inc)) pos[v] = inc;
         } else if (icmp::neg_gt_pos(inc, tol[v])) {
           has_neg[v] = true;
-          if (icmp::lt_nonneg(neg[v], -inc)) neg[v] = -inc;
+          const double m = negate(inc);
+          if (icmp::lt_nonneg(neg[v], m)) neg[v] = m;
         } else {
           flat[v] = true;
         }
@@ -201,7 +210,8 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const do
         if (icmp::lt_nonneg(pos[v], inc)) pos[v] = inc;
       } else if (icmp::neg_gt_pos(inc, tol[v])) {
         has_neg[v] = true;
-        if (icmp::lt_nonneg(neg[v], -inc)) neg[v] = -inc;
+        const double m = negate(inc);
+        if (icmp::lt_nonneg(neg[v], m)) neg[v] = m;
       } else {
         flat[v] = true;
       }
@@ -211,7 +221,7 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const do
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
     if constexpr (kMinRatio)
-      phi[v] = limiter_factor_min_ratio<LIMITER>(pv[v], lo[v], hi[v], pos[v], -neg[v], has_pos[v], has_neg[v], flat[v]);
+      phi[v] = limiter_factor_min_ratio<LIMITER>(pv[v], lo[v], hi[v], pos[v], negate(neg[v]), has_pos[v], has_neg[v], flat[v]);
     else
       phi[v] = limiter_factor_fast<LIMITER>(hi[v] - pv[v], pos[v], pv[v] - lo[v], neg[v], has_pos[v], has_neg[v], flat[v]);
   }
@@ -299,8 +309,9 @@ __device__ __forceinline__ double stage_dt(const StageProgram& prog, int c) {
 __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
                                                    const double* __restrict__ flux, double gamma,
                                                    double ax, double ay, StageProgram prog) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.n_cells) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n_cells) return;
+  const int c = g.cell_order[i];
   // interior divergence: SciPy CSR product, ascending face order
   // (solver.py:2160-2174, 2501); derivative starts from zero.
   double s[4] = {0.0, 0.0, 0.0, 0.0};
@@ -392,9 +403,11 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
                                                        double gamma, double cfl,
                                                        double* __restrict__ dt_cells,
                                                        int want_min, const double* __restrict__ diffusion) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < g.n_cells;
+  const int c = active ? g.cell_order[i] : 0;
   double dt = __longlong_as_double(0x7ff0000000000000LL);
-  if (c < g.n_cells) {
+  if (active) {
     const St4 p = ld4(P + 4 * (size_t)c);
     const double sound = sound_speed(p.a, p.d, gamma);
     double sum = 0.0;
@@ -426,7 +439,7 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
   // block minimum by warp shuffles, then one atomicMin on the bit pattern
   // (positive doubles order like their unsigned bits).
   // positive doubles order like their bits: the minimum runs on integers
-  long long m = (c < g.n_cells && icmp::gt0(dt)) ? icmp::bits(dt) : 0x7ff0000000000000LL;
+  long long m = (active && icmp::gt0(dt)) ? icmp::bits(dt) : 0x7ff0000000000000LL;
   for (int off = 16; off > 0; off >>= 1) {
     long long o = __shfl_down_sync(0xffffffffu, m, off);
     m = (o < m) ? o : m;

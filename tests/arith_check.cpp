@@ -1,4 +1,4 @@
-// Host check of the integer-pipe division and square root
+// Host check of the integer-pipe division, square root, doubling and negation
 // (meshcfd_gb300/csrc/mcfd_arith.cuh compiled as plain C++) against the
 // host's IEEE binary64 division and square root, bit for bit.
 //
@@ -65,6 +65,10 @@ static void check(double a, double b) {
   const double s = mcfd::sqrt_rn(a), sr = std::sqrt(a);
   if (!same(s, sr)) {
     if (!g_bad) printf("sqrt %a: got %a expected %a\n", a, s, sr);
+    ++g_bad;
+  }
+  if (!same(mcfd::twice(a), 2.0 * a) || !same(mcfd::negate(a), -a)) {
+    if (!g_bad) printf("twice / negate %a\n", a);
     ++g_bad;
   }
 }
