@@ -1,5 +1,5 @@
 // IEEE-754 binary64 division and square root, round to nearest even,
-// evaluated on the integer pipe (plus exact negation and doubling).
+// evaluated on the integer pipe (plus exact negation, doubling and 0 + x).
 //
 // On GB300 one FP64 division or square root costs ~8.6 FP64 issue slots
 // (~58 G/s per GPU) while the integer pipe runs ~38x the FP64 rate, so the
@@ -21,10 +21,12 @@
 //   Brent & Zimmermann, Modern Computer Arithmetic, 2010, secs. 3.4-3.5) —
 //   and rounded to nearest even from the guard bit and the sticky bit
 //   (remainder != 0);
-// * zeros, subnormals, infinities, NaN, negative square-root arguments and
-//   quotients that overflow or underflow fall back to the FP64 unit, and so
-//   does a remainder still out of range after the correction (it cannot be
-//   for the error bounds above; the test keeps the result exact regardless).
+// * a zero dividend over a normal divisor gives the signed zero directly;
+//   other zeros, subnormals, infinities, NaN, negative square-root arguments
+//   and quotients that overflow or underflow fall back to the FP64 unit, and
+//   so does a remainder still out of range after the correction (it cannot
+//   be for the error bounds above; the test keeps the result exact
+//   regardless).
 //
 // The header also compiles as plain C++ (the host seeds are the correctly
 // rounded fp32 reciprocal and reciprocal root), so the integer algorithm can
@@ -38,8 +40,10 @@
 #if defined(__CUDACC__)
 #include <cuda_runtime.h>
 #define MCFD_IA_FN __host__ __device__ __forceinline__
+#define MCFD_IA_SLOW static __host__ __device__ __noinline__
 #else
 #define MCFD_IA_FN static inline
+#define MCFD_IA_SLOW static
 #endif
 
 namespace mcfd {
@@ -100,6 +104,13 @@ MCFD_IA_FN unsigned to_u32(float v) {
 #endif
 }
 
+// The FP64 unit's results for the operands the integer path leaves out.  Out
+// of line, so that the rare fallback is a branch around a call rather than
+// instructions predicated into every evaluation (predicated-off FP64
+// instructions still take FP64 issue slots).
+MCFD_IA_SLOW double div_fp64(double a, double b) { return a / b; }
+MCFD_IA_SLOW double sqrt_fp64(double x) { return sqrt(x); }
+
 static constexpr u64 kMant = 0x000fffffffffffffull;
 static constexpr u64 kImpl = 0x0010000000000000ull;
 static constexpr u64 kSign = 0x8000000000000000ull;
@@ -155,8 +166,12 @@ MCFD_IA_FN double div_rn(double a, double b) {
   const bool in_range = R >= 0 && R < B;
   const bool underflow = e < 1;
   const u64 m = round_q55(Q, R != 0, e);
-  if (ea - 1u >= 0x7feu || eb - 1u >= 0x7feu || underflow || e > 2046 || !in_range) return a / b;
-  return from_bits(((ia ^ ib) & kSign) | ((u64)e << 52) | (m & kMant));
+  // a zero dividend over a normal divisor gives a signed zero (a limiter
+  // ratio's numerator is zero at every local extremum)
+  const bool a_zero = (ia << 1) == 0ull;
+  if (eb - 1u >= 0x7feu || (!a_zero && (ea - 1u >= 0x7feu || underflow || e > 2046 || !in_range)))
+    return div_fp64(a, b);
+  return from_bits(a_zero ? ((ia ^ ib) & kSign) : (((ia ^ ib) & kSign) | ((u64)e << 52) | (m & kMant)));
 }
 
 MCFD_IA_FN double sqrt_rn(double x) {
@@ -195,7 +210,7 @@ MCFD_IA_FN double sqrt_rn(double x) {
   }
   const bool in_range = R >= 0 && R <= (long long)(2 * S);
   const u64 m = round_q55(S, R != 0, e);
-  if (ex - 1u >= 0x7feu || !in_range) return sqrt(x);
+  if (ex - 1u >= 0x7feu || !in_range) return sqrt_fp64(x);
   return from_bits(((u64)e << 52) | (m & kMant));
 }
 
@@ -211,13 +226,18 @@ MCFD_IA_FN double twice(double x) {
   return e - 1u < 2045u ? from_bits(b + (1ull << 52)) : 2.0 * x;
 }
 
+// 0.0 + x, exact: x itself except that -0 becomes +0
+MCFD_IA_FN double plus_zero(double x) { return bits(x) == kSign ? 0.0 : x; }
+
 }  // namespace ia
 
 using ia::div_rn;
 using ia::negate;
+using ia::plus_zero;
 using ia::sqrt_rn;
 using ia::twice;
 
 }  // namespace mcfd
 
 #undef MCFD_IA_FN
+#undef MCFD_IA_SLOW

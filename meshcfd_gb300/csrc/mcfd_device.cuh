@@ -101,12 +101,12 @@ __device__ __forceinline__ St4 cons_to_prim(const St4& U, double gamma, bool* ok
   return P;
 }
 
-// euler.physical_flux (euler.py:43-57): flux and conservative state.
-__device__ __forceinline__ void physical_flux(const St4& q, double nx, double ny, double gamma,
-                                              double F[4], double U[4]) {
+// euler.physical_flux (euler.py:43-57): flux and conservative state, with
+// the normal velocity un = ux nx + uy ny given (the callers compute it too).
+__device__ __forceinline__ void physical_flux_un(const St4& q, double un, double nx, double ny, double gamma,
+                                                 double F[4], double U[4]) {
   double rho = q.a, ux = q.b, uy = q.c, p = q.d;
   double energy = div_rn(p, gamma - 1.0) + (0.5 * rho) * (ux * ux + uy * uy);
-  double un = ux * nx + uy * ny;
   U[0] = rho;
   U[1] = rho * ux;
   U[2] = rho * uy;
@@ -115,6 +115,11 @@ __device__ __forceinline__ void physical_flux(const St4& q, double nx, double ny
   F[1] = (rho * ux) * un + p * nx;
   F[2] = (rho * uy) * un + p * ny;
   F[3] = (energy + p) * un;
+}
+
+__device__ __forceinline__ void physical_flux(const St4& q, double nx, double ny, double gamma,
+                                              double F[4], double U[4]) {
+  physical_flux_un(q, q.b * nx + q.c * ny, nx, ny, gamma, F, U);
 }
 
 __device__ __forceinline__ double sound_speed(double rho, double p, double gamma) {
@@ -173,13 +178,13 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
   }
   const bool left = branch <= 1;
   const St4 q = left ? L : R;
+  const double un = left ? unl : unr;
   double F[4], U[4];
-  physical_flux(q, nx, ny, gamma, F, U);
+  physical_flux_un(q, un, nx, ny, gamma, F, U);
   if (branch == 0 || branch == 3) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = F[k];
   } else {
-    double un = left ? unl : unr;
     double wave = left ? wl : wr;
     double rho = q.a, pressure = q.d;
     double factor = div_rn(rho * (wave - un), wave - contact);
@@ -388,11 +393,10 @@ __device__ __forceinline__ St4 cons_to_prim_fast(const St4& U, double gamma, boo
 }
 
 // physical_flux with the internal energy as p * (1/(gamma-1)).
-__device__ __forceinline__ void physical_flux_fast(const St4& q, double nx, double ny, double inv_gm1,
-                                                   double F[4], double U[4]) {
+__device__ __forceinline__ void physical_flux_fast_un(const St4& q, double un, double nx, double ny,
+                                                      double inv_gm1, double F[4], double U[4]) {
   double rho = q.a, ux = q.b, uy = q.c, p = q.d;
   double energy = p * inv_gm1 + 0.5 * rho * (ux * ux + uy * uy);
-  double un = ux * nx + uy * ny;
   U[0] = rho;
   U[1] = rho * ux;
   U[2] = rho * uy;
@@ -401,6 +405,11 @@ __device__ __forceinline__ void physical_flux_fast(const St4& q, double nx, doub
   F[1] = U[1] * un + p * nx;
   F[2] = U[2] * un + p * ny;
   F[3] = (energy + p) * un;
+}
+
+__device__ __forceinline__ void physical_flux_fast(const St4& q, double nx, double ny, double inv_gm1,
+                                                   double F[4], double U[4]) {
+  physical_flux_fast_un(q, q.b * nx + q.c * ny, nx, ny, inv_gm1, F, U);
 }
 
 // HLLC with shared reciprocals: one division for both 1/rho, one for the
@@ -434,13 +443,13 @@ __device__ __forceinline__ bool hllc_flux_fast(const St4& L, const St4& R, doubl
   }
   const bool left = branch <= 1;
   const St4 q = left ? L : R;
+  const double un = left ? unl : unr;
   double F[4], U[4];
-  physical_flux_fast(q, nx, ny, inv_gm1, F, U);
+  physical_flux_fast_un(q, un, nx, ny, inv_gm1, F, U);
   if (branch == 0 || branch == 3) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = F[k];
   } else {
-    double un = left ? unl : unr;
     double wave = left ? wl : wr;
     double m = left ? ml : mr;          // rho (S - un)
     double irho = left ? irl : irr;

@@ -138,15 +138,14 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
 // gradients as in the exact kernel, one pass over the limiter entries that
 // keeps the largest positive and most negative increments, the factor from
 // limiter_factor_min_ratio (fast) or limiter_factor_fast (fma), and the
-// increments of the first four slots kept in registers for the face-state
-// write.
-template <int LIMITER>
-__global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const double* __restrict__ P,
-                                                             double* __restrict__ recon) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g.n_cells) return;
-  const int c = g.cell_order[i];
-  const St4 p = ld4(P + 4 * (size_t)c);
+// increments kept in registers for the face-state write.  NS > 0 compiles the
+// cell for exactly NS limiter entries (triangles 3, quadrilaterals 4; the
+// cell order makes the count warp-uniform); NS = 0 handles any count, caching
+// the first four increments.
+template <int LIMITER, int NS>
+__device__ __forceinline__ void reconstruct_cell_fast(const DevGeom& g, const double* __restrict__ P,
+                                                      double* __restrict__ recon, int c, const St4& p,
+                                                      int s0, int s1) {
   const double pv[4] = {p.a, p.b, p.c, p.d};
   double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
   double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
@@ -176,45 +175,37 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const do
     neg[v] = 0.0;
     has_pos[v] = has_neg[v] = flat[v] = false;
   }
-  const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
-  constexpr int kCache = 4;
+  auto classify = [&](int v, double inc) {
+    if (icmp::gt_pos(inc, tol[v])) {
+      has_pos[v] = true;
+      if (icmp::lt_nonneg(pos[v], inc)) pos[v] = inc;
+    } else if (icmp::neg_gt_pos(inc, tol[v])) {
+      has_neg[v] = true;
+      const double m = negate(inc);
+      if (icmp::lt_nonneg(neg[v], m)) neg[v] = m;
+    } else {
+      flat[v] = true;
+    }
+  };
+  constexpr int kCache = NS > 0 ? NS : 4;
   double inc_cache[kCache][4];
 #pragma unroll
   for (int k = 0; k < kCache; ++k) {
-    if (s0 + k < s1) {
+    if (NS > 0 || s0 + k < s1) {
       const double2 d = g.lim_d[s0 + k];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         double inc = gx[v] * d.x + gy[v] * d.y;
         inc_cache[k][v] = inc;
-        if (icmp::gt_pos(inc, tol[v])) {
-          has_pos[v] = true;
-          if (icmp::lt_nonneg(pos[v], inc)) pos[v] = inc;
-        } else if (icmp::neg_gt_pos(inc, tol[v])) {
-          has_neg[v] = true;
-          const double m = negate(inc);
-          if (icmp::lt_nonneg(neg[v], m)) neg[v] = m;
-        } else {
-          flat[v] = true;
-        }
+        classify(v, inc);
       }
     }
   }
-  for (int s = s0 + kCache; s < s1; ++s) {
-    const double2 d = g.lim_d[s];
+  if (NS == 0) {
+    for (int s = s0 + kCache; s < s1; ++s) {
+      const double2 d = g.lim_d[s];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      double inc = gx[v] * d.x + gy[v] * d.y;
-      if (icmp::gt_pos(inc, tol[v])) {
-        has_pos[v] = true;
-        if (icmp::lt_nonneg(pos[v], inc)) pos[v] = inc;
-      } else if (icmp::neg_gt_pos(inc, tol[v])) {
-        has_neg[v] = true;
-        const double m = negate(inc);
-        if (icmp::lt_nonneg(neg[v], m)) neg[v] = m;
-      } else {
-        flat[v] = true;
-      }
+      for (int v = 0; v < 4; ++v) classify(v, gx[v] * d.x + gy[v] * d.y);
     }
   }
   double phi[4];
@@ -227,19 +218,34 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const do
   }
 #pragma unroll
   for (int k = 0; k < kCache; ++k) {
-    if (s0 + k < s1) {
+    if (NS > 0 || s0 + k < s1) {
       St4 o{pv[0] + phi[0] * inc_cache[k][0], pv[1] + phi[1] * inc_cache[k][1],
             pv[2] + phi[2] * inc_cache[k][2], pv[3] + phi[3] * inc_cache[k][3]};
       st4(recon + 4 * (size_t)g.lim_slot[s0 + k], o);
     }
   }
-  for (int s = s0 + kCache; s < s1; ++s) {
-    const double2 d = g.lim_d[s];
-    double out[4];
+  if (NS == 0) {
+    for (int s = s0 + kCache; s < s1; ++s) {
+      const double2 d = g.lim_d[s];
+      double out[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (gx[v] * d.x + gy[v] * d.y);
-    st4(recon + 4 * (size_t)g.lim_slot[s], St4{out[0], out[1], out[2], out[3]});
+      for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (gx[v] * d.x + gy[v] * d.y);
+      st4(recon + 4 * (size_t)g.lim_slot[s], St4{out[0], out[1], out[2], out[3]});
+    }
   }
+}
+
+template <int LIMITER>
+__global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const double* __restrict__ P,
+                                                             double* __restrict__ recon) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n_cells) return;
+  const int c = g.cell_order[i];
+  const St4 p = ld4(P + 4 * (size_t)c);
+  const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
+  if (s1 - s0 == 3) reconstruct_cell_fast<LIMITER, 3>(g, P, recon, c, p, s0, s1);
+  else if (s1 - s0 == 4) reconstruct_cell_fast<LIMITER, 4>(g, P, recon, c, p, s0, s1);
+  else reconstruct_cell_fast<LIMITER, 0>(g, P, recon, c, p, s0, s1);
 }
 
 // -------------------------------------------------------------------- fluxes
@@ -306,6 +312,16 @@ __device__ __forceinline__ double stage_dt(const StageProgram& prog, int c) {
   return prog.dt_per_cell ? prog.dt[c] : prog.dt[0];
 }
 
+// Stage-combination shapes with their own code path (the generic loop over
+// runtime term kinds lets the compiler predicate every kind's arithmetic into
+// each evaluation, and predicated-off FP64 instructions still take FP64 issue
+// slots):
+//   SHAPE_EULER   u = x + dt r      terms {X 1.0 x, DTR 1.0} (1.0 * v == v)
+//   SHAPE_X_XDTR  u = c0 x0 + c1 (x1 + dt r)   terms {X c0 x0, X_PLUS_DTR c1 x1}
+// EXTRAS compiles the viscous residual and body-force adds in.
+enum GatherShape { SHAPE_GENERIC = 0, SHAPE_EULER = 1, SHAPE_X_XDTR = 2 };
+
+template <int SHAPE, bool EXTRAS>
 __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
                                                    const double* __restrict__ flux, double gamma,
                                                    double ax, double ay, StageProgram prog) {
@@ -323,7 +339,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
     s[2] = s[2] + a * F.c;
     s[3] = s[3] + a * F.d;
   }
-  double r[4] = {0.0 + s[0], 0.0 + s[1], 0.0 + s[2], 0.0 + s[3]};
+  double r[4] = {plus_zero(s[0]), plus_zero(s[1]), plus_zero(s[2]), plus_zero(s[3])};  // 0.0 + s
   // boundary groups: np.add.at(derivative, owners, -(flux*L)/A) in BC order
   const int jb0 = g.gb_ptr[c], jb1 = g.gb_ptr[c + 1];
   if (jb0 < jb1) {
@@ -337,18 +353,20 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
       r[3] = r[3] + div_rn(F.d * len, area);
     }
   }
-  const St4 p = ld4(P + 4 * (size_t)c);
-  if (prog.visc_r) {  // derivative += _viscous_residual(...) (solver.py:2699-2702)
-    const St4 v = ld4(prog.visc_r + 4 * (size_t)c);
-    r[0] = r[0] + v.a;
-    r[1] = r[1] + v.b;
-    r[2] = r[2] + v.c;
-    r[3] = r[3] + v.d;
-  }
-  if (ax != 0.0 || ay != 0.0) {  // solver.py:2709-2715
-    r[1] = r[1] + p.a * ax;
-    r[2] = r[2] + p.a * ay;
-    r[3] = r[3] + p.a * (ax * p.b + ay * p.c);
+  if (EXTRAS) {
+    if (prog.visc_r) {  // derivative += _viscous_residual(...) (solver.py:2699-2702)
+      const St4 v = ld4(prog.visc_r + 4 * (size_t)c);
+      r[0] = r[0] + v.a;
+      r[1] = r[1] + v.b;
+      r[2] = r[2] + v.c;
+      r[3] = r[3] + v.d;
+    }
+    if (icmp::abs_gt(ax, 0.0) || icmp::abs_gt(ay, 0.0)) {  // ax != 0 or ay != 0 (solver.py:2709-2715)
+      const St4 p = ld4(P + 4 * (size_t)c);
+      r[1] = r[1] + p.a * ax;
+      r[2] = r[2] + p.a * ay;
+      r[3] = r[3] + p.a * (ax * p.b + ay * p.c);
+    }
   }
   if (!(icmp::finite(r[0]) && icmp::finite(r[1]) && icmp::finite(r[2]) && icmp::finite(r[3])))
     flag_cell(g.status, MCFD_S_NONFINITE_RESIDUAL, c);
@@ -356,6 +374,21 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
   if (!prog.out_u) return;
   const double dt = stage_dt(prog, c);
   double u[4];
+  if (SHAPE == SHAPE_EULER) {
+    const St4 x = ld4(prog.t[0].x + 4 * (size_t)c);
+    u[0] = x.a + dt * r[0];
+    u[1] = x.b + dt * r[1];
+    u[2] = x.c + dt * r[2];
+    u[3] = x.d + dt * r[3];
+  } else if (SHAPE == SHAPE_X_XDTR) {
+    const double c0 = prog.t[0].coef, c1 = prog.t[1].coef;
+    const St4 x0 = ld4(prog.t[0].x + 4 * (size_t)c);
+    const St4 x1 = ld4(prog.t[1].x + 4 * (size_t)c);
+    u[0] = c0 * x0.a + c1 * (x1.a + dt * r[0]);
+    u[1] = c0 * x0.b + c1 * (x1.b + dt * r[1]);
+    u[2] = c0 * x0.c + c1 * (x1.c + dt * r[2]);
+    u[3] = c0 * x0.d + c1 * (x1.d + dt * r[3]);
+  } else {
   for (int t = 0; t < prog.n_terms; ++t) {
     const StageTerm term = prog.t[t];
     double v[4];
@@ -381,6 +414,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
     } else {
       u[0] = u[0] + v[0]; u[1] = u[1] + v[1]; u[2] = u[2] + v[2]; u[3] = u[3] + v[3];
     }
+  }
   }
   const St4 U = St4{u[0], u[1], u[2], u[3]};
   st4(prog.out_u + 4 * (size_t)c, U);
@@ -542,11 +576,28 @@ cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* 
 
 cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double* P,
                           const double* flux, const StageProgram& prog, cudaStream_t s) {
-  if (g.n_cells > 0)
-    count_launch(), k_gather<<<(g.n_cells + (g.tune_gather_threads ? g.tune_gather_threads : kBlock) - 1) /
-                                   (g.tune_gather_threads ? g.tune_gather_threads : kBlock),
-                               g.tune_gather_threads ? g.tune_gather_threads : kBlock, 0, s>>>(g, P, flux, cfg.gamma, cfg.acceleration_x,
-                                                      cfg.acceleration_y, prog);
+  if (g.n_cells <= 0) return cudaSuccess;
+  int shape = SHAPE_GENERIC;
+  if (prog.out_u && prog.n_terms == 2 && prog.t[0].kind == TERM_X) {
+    if (prog.t[1].kind == TERM_DTR && prog.t[0].coef == 1.0 && prog.t[1].coef == 1.0) shape = SHAPE_EULER;
+    else if (prog.t[1].kind == TERM_X_PLUS_DTR) shape = SHAPE_X_XDTR;
+  }
+  const bool extras = prog.visc_r || cfg.acceleration_x != 0.0 || cfg.acceleration_y != 0.0;
+  const int t = g.tune_gather_threads ? g.tune_gather_threads : kBlock;
+  const int b = (g.n_cells + t - 1) / t;
+  const double ax = cfg.acceleration_x, ay = cfg.acceleration_y;
+  count_launch();
+#define MCFD_GATHER(SH, EX) k_gather<SH, EX><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
+  if (extras) {
+    if (shape == SHAPE_EULER) MCFD_GATHER(SHAPE_EULER, true);
+    else if (shape == SHAPE_X_XDTR) MCFD_GATHER(SHAPE_X_XDTR, true);
+    else MCFD_GATHER(SHAPE_GENERIC, true);
+  } else {
+    if (shape == SHAPE_EULER) MCFD_GATHER(SHAPE_EULER, false);
+    else if (shape == SHAPE_X_XDTR) MCFD_GATHER(SHAPE_X_XDTR, false);
+    else MCFD_GATHER(SHAPE_GENERIC, false);
+  }
+#undef MCFD_GATHER
   return cudaGetLastError();
 }
 
