@@ -1,5 +1,6 @@
 // IEEE-754 binary64 division and square root, round to nearest even,
-// evaluated on the integer pipe (plus exact negation, doubling and 0 + x).
+// evaluated on the integer pipe (plus exact negation, absolute value,
+// doubling and 0 + x).
 //
 // On GB300 one FP64 division or square root costs ~8.6 FP64 issue slots
 // (~58 G/s per GPU) while the integer pipe runs ~38x the FP64 rate, so the
@@ -115,6 +116,28 @@ static constexpr u64 kMant = 0x000fffffffffffffull;
 static constexpr u64 kImpl = 0x0010000000000000ull;
 static constexpr u64 kSign = 0x8000000000000000ull;
 
+// Sign-bit operations kept as integer instructions: written as plain integer
+// code, the compiler may recognise them as floating-point negation / absolute
+// value / copysign and give them to the FP64 pipe.
+MCFD_IA_FN u64 sign_xor(u64 b, u64 s) {
+#if defined(__CUDA_ARCH__)
+  u64 r;
+  asm("xor.b64 %0, %1, %2;" : "=l"(r) : "l"(b), "l"(s));
+  return r;
+#else
+  return b ^ s;
+#endif
+}
+MCFD_IA_FN u64 bits_and(u64 b, u64 m) {
+#if defined(__CUDA_ARCH__)
+  u64 r;
+  asm("and.b64 %0, %1, %2;" : "=l"(r) : "l"(b), "l"(m));
+  return r;
+#else
+  return b & m;
+#endif
+}
+
 // Round the 55-bit truncated significand q (53 bits, guard bit, one more bit)
 // with the remainder's sticky bit; returns the 53-bit significand and bumps e
 // when rounding carries into the next binade.
@@ -215,15 +238,27 @@ MCFD_IA_FN double sqrt_rn(double x) {
 }
 
 // -x (IEEE negation is exact: the sign bit flips, also for zeros and NaN)
-MCFD_IA_FN double negate(double x) { return from_bits(bits(x) ^ kSign); }
+MCFD_IA_FN double negate(double x) { return from_bits(sign_xor(bits(x), kSign)); }
 
-// 2 x, exact: the exponent field steps by one for normal x below the largest
-// binade; zeros, subnormals, the top binade, infinities and NaN go to the FP64
-// unit.
+// copysign(m, s) for m >= +0: m with the sign of s
+MCFD_IA_FN double with_sign_of(double m, double s) { return from_bits(bits(m) | bits_and(bits(s), kSign)); }
+
+// |x| (clears the sign bit, as the IEEE abs operation does)
+MCFD_IA_FN double abs_of(double x) { return from_bits(bits_and(bits(x), ~kSign)); }
+
+// 2 x, exact, on integers: the exponent field steps by one for normal x below
+// the top binade; zeros and subnormals shift their significand left (which
+// carries into the exponent field where 2 x is normal); the top binade
+// overflows to infinity; infinities stay, NaN is returned quiet.
 MCFD_IA_FN double twice(double x) {
-  const u64 b = bits(x);
-  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
-  return e - 1u < 2045u ? from_bits(b + (1ull << 52)) : 2.0 * x;
+  const u64 b = bits(x), sign = b & kSign, mag = b & ~kSign;
+  const unsigned e = (unsigned)(mag >> 52);
+  u64 r;
+  if (e == 0u) r = sign | (mag << 1);
+  else if (e < 2046u) r = b + (1ull << 52);
+  else if (e == 2046u) r = sign | 0x7ff0000000000000ull;
+  else r = (mag & kMant) ? (b | 0x0008000000000000ull) : b;
+  return from_bits(r);
 }
 
 // 0.0 + x, exact: x itself except that -0 becomes +0
@@ -231,9 +266,11 @@ MCFD_IA_FN double plus_zero(double x) { return bits(x) == kSign ? 0.0 : x; }
 
 }  // namespace ia
 
+using ia::abs_of;
 using ia::div_rn;
 using ia::negate;
 using ia::plus_zero;
+using ia::with_sign_of;
 using ia::sqrt_rn;
 using ia::twice;
 

@@ -37,7 +37,9 @@ __device__ __forceinline__ void st4(double* p, const St4& s) {
 // ---------------------------------------------------------------------------
 // IEEE-754 comparisons evaluated on the integer pipe.  On GB300 the FP64 pipe
 // issues ~1/38 the integer rate (measured), and compares / min / max /
-// finiteness tests take FP64 issue slots like arithmetic does.  Each helper
+// finiteness tests take FP64 issue slots like arithmetic does.  Sign and
+// exponent masks go through ia::bits_and / ia::sign_xor so that they stay
+// integer instructions.  Each helper
 // below returns exactly the IEEE result for non-NaN operands (signed zeros
 // compare equal); NaN never reaches a decision whose outcome matters (every
 // path that can produce NaN also sets a status bit from a finiteness test).
@@ -54,18 +56,17 @@ __device__ __forceinline__ long long key(double x) {
 __device__ __forceinline__ bool lt(double a, double b) { return key(a) < key(b); }
 // both operands >= 0 (either zero may be signed)
 __device__ __forceinline__ bool lt_nonneg(double a, double b) {
-  return (unsigned long long)(bits(a) & 0x7fffffffffffffffLL) <
-         (unsigned long long)(bits(b) & 0x7fffffffffffffffLL);
+  return ia::bits_and(ia::bits(a), ~ia::kSign) < ia::bits_and(ia::bits(b), ~ia::kSign);
 }
 // a < c and a > c for a constant c > 0 (gt also for c = +0)
 __device__ __forceinline__ bool lt_pos(double a, double c) { return bits(a) < bits(c); }
 __device__ __forceinline__ bool gt_pos(double a, double c) { return bits(a) > bits(c); }
 // -a > c for c >= +0  (a < -c)
 __device__ __forceinline__ bool neg_gt_pos(double a, double c) {
-  return (bits(a) ^ (long long)0x8000000000000000ULL) > bits(c);
+  return (long long)ia::sign_xor(ia::bits(a), ia::kSign) > bits(c);
 }
 __device__ __forceinline__ bool abs_gt(double a, double c) {
-  return (unsigned long long)(bits(a) & 0x7fffffffffffffffLL) > (unsigned long long)bits(c);
+  return ia::bits_and(ia::bits(a), ~ia::kSign) > (unsigned long long)bits(c);
 }
 __device__ __forceinline__ bool gt0(double a) { return bits(a) > 0; }
 __device__ __forceinline__ bool le0(double a) { return bits(a) <= 0; }
@@ -74,7 +75,7 @@ __device__ __forceinline__ bool ge0(double a) {
   return b >= 0 || b == (long long)0x8000000000000000ULL;
 }
 __device__ __forceinline__ bool finite(double a) {
-  return ((unsigned)(bits(a) >> 32) & 0x7ff00000u) != 0x7ff00000u;
+  return ia::bits_and(ia::bits(a), 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
 }
 // Python min(a, b) / max(a, b): the first argument unless the second is
 // strictly smaller / larger.
@@ -134,8 +135,8 @@ __device__ __forceinline__ void rusanov_flux(const St4& L, const St4& R, double 
   physical_flux(R, nx, ny, gamma, FR, UR);
   double unl = L.b * nx + L.c * ny;
   double unr = R.b * nx + R.c * ny;
-  double sl = fabs(unl) + sound_speed(L.a, L.d, gamma);
-  double sr = fabs(unr) + sound_speed(R.a, R.d, gamma);
+  double sl = abs_of(unl) + sound_speed(L.a, L.d, gamma);
+  double sr = abs_of(unr) + sound_speed(R.a, R.d, gamma);
   double s = icmp::lt_nonneg(sl, sr) ? sr : sl;  // np.maximum
 #pragma unroll
   for (int k = 0; k < 4; ++k) out[k] = 0.5 * ((FL[k] + FR[k]) - s * (UR[k] - UL[k]));
@@ -162,7 +163,7 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
   double wl = py_min(unl - cl, unr - cr);
   double wr = py_max(unl + cl, unr + cr);
   double den = rl * (wl - unl) - rr * (wr - unr);
-  if (!icmp::abs_gt(den, 1e-14)) den = copysign(1e-14, den);
+  if (!icmp::abs_gt(den, 1e-14)) den = with_sign_of(1e-14, den);
   double contact = div_rn((pr - pl) + (rl * unl) * (wl - unl) - (rr * unr) * (wr - unr), den);
 
   int branch;  // 0: F_L, 1: F*_L, 2: F*_R, 3: F_R
@@ -237,7 +238,7 @@ __device__ __forceinline__ int roe_flux(const St4& L, const St4& R, double nx, d
   double strength[4] = {am, ac, as, ap};
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    double a = fabs(lam[j]);
+    double a = abs_of(lam[j]);
     if (icmp::lt_nonneg(a, fix)) a = 0.5 * (div_rn(a * a, fix) + fix);
     w[j] = a * strength[j];
   }
@@ -372,7 +373,7 @@ __device__ __forceinline__ double limiter_factor_min_ratio(double value, double 
 }
 
 __device__ __forceinline__ double limiter_tolerance(double value) {
-  double m = fabs(value);
+  double m = abs_of(value);
   return 1e-14 * (icmp::lt_pos(m, 1.0) ? 1.0 : m);  // 1e-14 * max(|v|, 1.0)
 }
 
@@ -428,7 +429,7 @@ __device__ __forceinline__ bool hllc_flux_fast(const St4& L, const St4& R, doubl
   double wr = py_max(unl + cl, unr + cr);
   double ml = rl * (wl - unl), mr = rr * (wr - unr);
   double den = ml - mr;
-  if (!icmp::abs_gt(den, 1e-14)) den = copysign(1e-14, den);
+  if (!icmp::abs_gt(den, 1e-14)) den = with_sign_of(1e-14, den);
   double contact = div_rn((pr - pl) + unl * ml - unr * mr, den);
   int branch;
   if (KERNEL_BRANCHES) {
@@ -477,8 +478,8 @@ __device__ __forceinline__ void rusanov_flux_fast(const St4& L, const St4& R, do
   double t = div_rn(1.0, L.a * R.a);
   double unl = L.b * nx + L.c * ny;
   double unr = R.b * nx + R.c * ny;
-  double sl = fabs(unl) + sqrt_rn(gamma * L.d * (R.a * t));
-  double sr = fabs(unr) + sqrt_rn(gamma * R.d * (L.a * t));
+  double sl = abs_of(unl) + sqrt_rn(gamma * L.d * (R.a * t));
+  double sr = abs_of(unr) + sqrt_rn(gamma * R.d * (L.a * t));
   double s = icmp::lt_nonneg(sl, sr) ? sr : sl;
 #pragma unroll
   for (int k = 0; k < 4; ++k) out[k] = 0.5 * ((FL[k] + FR[k]) - s * (UR[k] - UL[k]));
@@ -520,7 +521,7 @@ __device__ __forceinline__ int roe_flux_fast(const St4& L, const St4& R, double 
   double strength[4] = {am, ac, as, ap};
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    double a = fabs(lam[j]);
+    double a = abs_of(lam[j]);
     if (icmp::lt_nonneg(a, fix)) a = 0.5 * (a * a * ifix + fix);
     w[j] = a * strength[j];
   }

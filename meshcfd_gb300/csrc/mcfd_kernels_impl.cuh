@@ -235,16 +235,82 @@ __device__ __forceinline__ void reconstruct_cell_fast(const DevGeom& g, const do
   }
 }
 
+// The same cell for exactly NS limiter entries, one variable at a time: the
+// variable's increments, limiter factor and face values are finished before
+// the next variable starts, which keeps one variable's limiter state live
+// instead of four (fewer registers than the all-variables form, so no FP64
+// work is recomputed to relieve register pressure).  Face values are stored
+// per variable.
+template <int LIMITER, int NS>
+__device__ __forceinline__ void reconstruct_cell_fast_by_variable(const DevGeom& g, const double* __restrict__ P,
+                                                                  double* __restrict__ recon, int c,
+                                                                  const St4& p, int s0) {
+  const double pv[4] = {p.a, p.b, p.c, p.d};
+  double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+  double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
+  const int e0 = g.grad_ptr[c], e1 = g.grad_ptr[c + 1];
+  for (int e = e0; e < e1; ++e) {
+    const int nb = g.grad_nb[e];
+    const double cx = g.grad_cx[e], cy = g.grad_cy[e];
+    const St4 q = ld4(P + 4 * (size_t)nb);
+    const double qv[4] = {q.a, q.b, q.c, q.d};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double d = qv[v] - pv[v];
+      gx[v] += cx * d;
+      gy[v] += cy * d;
+      const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
+      const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
+      if (below) lo[v] = qv[v];
+      if (above) hi[v] = qv[v];
+    }
+  }
+  double2 dk[NS];
+  size_t out[NS];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    dk[k] = g.lim_d[s0 + k];
+    out[k] = 4 * (size_t)g.lim_slot[s0 + k];
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const double tol = limiter_tolerance(pv[v]);
+    double pos = 0.0, neg = 0.0, inc[NS];
+    bool has_pos = false, has_neg = false, flat = false;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      inc[k] = gx[v] * dk[k].x + gy[v] * dk[k].y;
+      if (icmp::gt_pos(inc[k], tol)) {
+        has_pos = true;
+        if (icmp::lt_nonneg(pos, inc[k])) pos = inc[k];
+      } else if (icmp::neg_gt_pos(inc[k], tol)) {
+        has_neg = true;
+        const double m = negate(inc[k]);
+        if (icmp::lt_nonneg(neg, m)) neg = m;
+      } else {
+        flat = true;
+      }
+    }
+    double phi;
+    if constexpr (kMinRatio)
+      phi = limiter_factor_min_ratio<LIMITER>(pv[v], lo[v], hi[v], pos, negate(neg), has_pos, has_neg, flat);
+    else
+      phi = limiter_factor_fast<LIMITER>(hi[v] - pv[v], pos, pv[v] - lo[v], neg, has_pos, has_neg, flat);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) recon[out[k] + v] = pv[v] + phi * inc[k];
+  }
+}
+
 template <int LIMITER>
-__global__ void __launch_bounds__(kBlock) k_reconstruct_fast(DevGeom g, const double* __restrict__ P,
-                                                             double* __restrict__ recon) {
+__global__ void __launch_bounds__(kBlock, 2) k_reconstruct_fast(DevGeom g, const double* __restrict__ P,
+                                                                double* __restrict__ recon) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n_cells) return;
   const int c = g.cell_order[i];
   const St4 p = ld4(P + 4 * (size_t)c);
   const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
-  if (s1 - s0 == 3) reconstruct_cell_fast<LIMITER, 3>(g, P, recon, c, p, s0, s1);
-  else if (s1 - s0 == 4) reconstruct_cell_fast<LIMITER, 4>(g, P, recon, c, p, s0, s1);
+  if (s1 - s0 == 3) reconstruct_cell_fast_by_variable<LIMITER, 3>(g, P, recon, c, p, s0);
+  else if (s1 - s0 == 4) reconstruct_cell_fast_by_variable<LIMITER, 4>(g, P, recon, c, p, s0);
   else reconstruct_cell_fast<LIMITER, 0>(g, P, recon, c, p, s0, s1);
 }
 
@@ -449,7 +515,7 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
     for (int e = g.dt_ptr[c], e1 = g.dt_ptr[c + 1]; e < e1; ++e) {
       const double2 n = g.dt_normal[e];
       const int info = g.dt_info[e];
-      double radius = fabs(p.b * n.x + p.c * n.y) + sound;
+      double radius = abs_of(p.b * n.x + p.c * n.y) + sound;
       const int kind = info >> 28;
       if (kind != DT_PLAIN) {
         const int idx = info & 0x0fffffff;
@@ -458,7 +524,7 @@ __global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* 
         else if (kind == DT_POUT) ext = St4{p.a, p.b, p.c, g.ff_pout_pressure[idx]};
         else if (kind == DT_FAR) bits |= far_field_state(p, ld4(g.ff_far_state + 4 * (size_t)idx), n.x, n.y, gamma, &ext);
         else ext = ld4(g.bc_ext_dt + 4 * (size_t)idx);  // solver.py:4153-4188, states from k_bc_states
-        double er = fabs(ext.b * n.x + ext.c * n.y) + sound_speed(ext.a, ext.d, gamma);
+        double er = abs_of(ext.b * n.x + ext.c * n.y) + sound_speed(ext.a, ext.d, gamma);
         radius = icmp::lt_nonneg(radius, er) ? er : radius;  // np.maximum
       }
       sum = sum + radius * g.dt_len[e];

@@ -1,4 +1,4 @@
-// Host check of the integer-pipe division, square root, doubling, negation and 0 + x
+// Host check of the integer-pipe division, square root, doubling, negation, absolute value and 0 + x
 // (meshcfd_gb300/csrc/mcfd_arith.cuh compiled as plain C++) against the
 // host's IEEE binary64 division and square root, bit for bit.
 //
@@ -67,7 +67,8 @@ static void check(double a, double b) {
     if (!g_bad) printf("sqrt %a: got %a expected %a\n", a, s, sr);
     ++g_bad;
   }
-  if (!same(mcfd::twice(a), 2.0 * a) || !same(mcfd::negate(a), -a) || !same(mcfd::plus_zero(a), 0.0 + a)) {
+  if (!same(mcfd::twice(a), 2.0 * a) || !same(mcfd::negate(a), -a) || !same(mcfd::plus_zero(a), 0.0 + a) ||
+      !same(mcfd::abs_of(a), std::fabs(a))) {
     if (!g_bad) printf("twice / negate %a\n", a);
     ++g_bad;
   }
