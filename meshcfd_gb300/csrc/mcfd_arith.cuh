@@ -1,5 +1,5 @@
-// IEEE-754 binary64 division and square root, round to nearest even,
-// evaluated on the integer pipe (plus exact negation, absolute value,
+// IEEE-754 binary64 division, square root and multiplication, round to
+// nearest even, evaluated on the integer pipe (plus exact negation, absolute value,
 // doubling and 0 + x).
 //
 // On GB300 one FP64 division or square root costs ~8.6 FP64 issue slots
@@ -59,9 +59,15 @@ MCFD_IA_FN u64 mulhi(u64 a, u64 b) {
   return (u64)(((unsigned __int128)a * b) >> 64);
 #endif
 }
+// The bit pattern of x.  On the device the move is an inline mov.b64, which
+// the compiler cannot see through: integer tests on the bits (zero tests,
+// exponent classes, sign masks) would otherwise be recognised as the
+// equivalent floating-point compares and issued to the FP64 pipe.
 MCFD_IA_FN u64 bits(double x) {
 #if defined(__CUDA_ARCH__)
-  return (u64)__double_as_longlong(x);
+  u64 r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+  return r;
 #else
   u64 r;
   memcpy(&r, &x, 8);
@@ -110,6 +116,7 @@ MCFD_IA_FN unsigned to_u32(float v) {
 // instructions predicated into every evaluation (predicated-off FP64
 // instructions still take FP64 issue slots).
 MCFD_IA_SLOW double div_fp64(double a, double b) { return a / b; }
+MCFD_IA_SLOW double mul_fp64(double a, double b) { return a * b; }
 MCFD_IA_SLOW double sqrt_fp64(double x) { return sqrt(x); }
 
 static constexpr u64 kMant = 0x000fffffffffffffull;
@@ -197,6 +204,45 @@ MCFD_IA_FN double div_rn(double a, double b) {
   return from_bits(a_zero ? ((ia ^ ib) & kSign) : (((ia ^ ib) & kSign) | ((u64)e << 52) | (m & kMant)));
 }
 
+// a * b, round to nearest even.  The 106-bit product of the significands is
+// built from four 32 x 32 -> 64-bit products (53 = 21 + 32 bits), normalised
+// by at most one bit and rounded from its guard bit and the sticky OR of the
+// bits below.  A zero operand times a finite one gives the signed zero; other
+// zeros, subnormals, infinities, NaN and products that overflow or underflow
+// go to the FP64 unit.
+MCFD_IA_FN double mul_rn(double a, double b) {
+  const u64 ia = bits(a), ib = bits(b);
+  const unsigned ea = (unsigned)(ia >> 52) & 0x7ffu, eb = (unsigned)(ib >> 52) & 0x7ffu;
+  const u64 ma = (ia & kMant) | kImpl, mb = (ib & kMant) | kImpl;
+  const unsigned a0 = (unsigned)ma, a1 = (unsigned)(ma >> 32), b0 = (unsigned)mb, b1 = (unsigned)(mb >> 32);
+  const u64 p00 = (u64)a0 * b0, mid = (u64)a0 * b1 + (u64)a1 * b0, p11 = (u64)a1 * b1;
+  const u64 lo = p00 + (mid << 32);
+  const u64 hi = p11 + (mid >> 32) + (u64)(lo < p00);  // product = hi 2^64 + lo < 2^106
+  const unsigned top = (unsigned)(hi >> 41);            // product >= 2^105
+  // 53-bit significand, guard bit and sticky bits below it
+  u64 m, guard, sticky;
+  if (top) {
+    m = (hi << 11) | (lo >> 53);
+    guard = (lo >> 52) & 1ull;
+    sticky = (u64)((lo & 0x000fffffffffffffull) != 0ull);
+  } else {
+    m = (hi << 12) | (lo >> 52);
+    guard = (lo >> 51) & 1ull;
+    sticky = (u64)((lo & 0x0007ffffffffffffull) != 0ull);
+  }
+  int e = (int)ea + (int)eb - 1023 + (int)top;
+  const bool underflow = e < 1;
+  m += guard & (sticky | (m & 1ull));
+  const unsigned carry = (unsigned)(m >> 53);
+  m >>= carry;
+  e += (int)carry;
+  const u64 sign = bits_and(sign_xor(ia, ib), kSign);
+  const bool a_zero = (ia << 1) == 0ull, b_zero = (ib << 1) == 0ull;
+  const bool zero = (a_zero && eb != 0x7ffu) || (b_zero && ea != 0x7ffu);
+  if (!zero && (ea - 1u >= 0x7feu || eb - 1u >= 0x7feu || underflow || e > 2046)) return mul_fp64(a, b);
+  return from_bits(zero ? sign : (sign | ((u64)e << 52) | (m & kMant)));
+}
+
 MCFD_IA_FN double sqrt_rn(double x) {
   const u64 ix = bits(x);
   const unsigned ex = (unsigned)(ix >> 52);   // a set sign bit puts ex out of range
@@ -268,6 +314,7 @@ MCFD_IA_FN double plus_zero(double x) { return bits(x) == kSign ? 0.0 : x; }
 
 using ia::abs_of;
 using ia::div_rn;
+using ia::mul_rn;
 using ia::negate;
 using ia::plus_zero;
 using ia::with_sign_of;

@@ -45,7 +45,7 @@ __device__ __forceinline__ void st4(double* p, const St4& s) {
 // path that can produce NaN also sets a status bit from a finiteness test).
 namespace icmp {
 
-__device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ long long bits(double x) { return (long long)ia::bits(x); }
 
 // Monotone key: x < y  <=>  key(x) < key(y); -0 and +0 both map to 0.
 __device__ __forceinline__ long long key(double x) {

@@ -1,4 +1,4 @@
-// Host check of the integer-pipe division, square root, doubling, negation, absolute value and 0 + x
+// Host check of the integer-pipe division, multiplication, square root, doubling, negation, absolute value and 0 + x
 // (meshcfd_gb300/csrc/mcfd_arith.cuh compiled as plain C++) against the
 // host's IEEE binary64 division and square root, bit for bit.
 //
@@ -60,6 +60,11 @@ static void check(double a, double b) {
   const double q = mcfd::div_rn(a, b), qr = a / b;
   if (!same(q, qr)) {
     if (!g_bad) printf("div %a / %a: got %a expected %a\n", a, b, q, qr);
+    ++g_bad;
+  }
+  const double p = mcfd::mul_rn(a, b), pr = a * b;
+  if (!same(p, pr)) {
+    if (!g_bad) printf("mul %a * %a: got %a expected %a\n", a, b, p, pr);
     ++g_bad;
   }
   const double s = mcfd::sqrt_rn(a), sr = std::sqrt(a);
