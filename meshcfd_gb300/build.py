@@ -4,6 +4,13 @@
 ``meshcfd_gb300/_build/libmeshcfd_gb300.so``.  The kernel translation unit is
 compiled with ``-fmad=false`` (reference operation order); host code with
 ``-ffp-contract=off`` (GCC on aarch64 would otherwise contract a*b+c).
+
+Extra nvcc options may be given in the environment variable
+``MESHCFD_GB300_NVCC_FLAGS`` (split on whitespace), for example
+``-DMCFD_INT_MUL=3`` to choose which products of the exact-arithmetic
+kernels run on the integer pipe (the default is per variant, see
+mcfd_kernels_impl.cuh); a build with other options than the existing
+library's is forced.
 """
 
 from __future__ import annotations
@@ -56,10 +63,13 @@ def _sources_newer(target: Path) -> bool:
 def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     target = BUILD / LIBNAME
-    if not force and not _sources_newer(target):
+    extra_flags = os.environ.get("MESHCFD_GB300_NVCC_FLAGS", "").split()
+    stamp = BUILD / "nvcc_flags.txt"
+    flags_changed = (stamp.read_text() if stamp.exists() else "") != " ".join(extra_flags)
+    if not force and not flags_changed and not _sources_newer(target):
         return target
     common = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3"]
+              "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3", *extra_flags]
 
     def compile_unit(unit):
         src, extra = unit
@@ -81,6 +91,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, target)
+    stamp.write_text(" ".join(extra_flags))
     return target
 
 

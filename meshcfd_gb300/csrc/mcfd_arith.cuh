@@ -102,6 +102,14 @@ MCFD_IA_FN float rsqrt_seed(float t) {
   return 1.0f / sqrtf(t);
 #endif
 }
+// (hi:lo) >> s, low 32 bits, for 0 <= s < 32 (a funnel shift)
+MCFD_IA_FN unsigned shr_funnel(unsigned lo, unsigned hi, unsigned s) {
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_r(lo, hi, s);
+#else
+  return (unsigned)((((unsigned long long)hi << 32) | lo) >> s);
+#endif
+}
 // truncating float -> uint32 conversion, saturating at 2^32 - 1 (v > 0)
 MCFD_IA_FN unsigned to_u32(float v) {
 #if defined(__CUDA_ARCH__)
@@ -204,43 +212,45 @@ MCFD_IA_FN double div_rn(double a, double b) {
   return from_bits(a_zero ? ((ia ^ ib) & kSign) : (((ia ^ ib) & kSign) | ((u64)e << 52) | (m & kMant)));
 }
 
-// a * b, round to nearest even.  The 106-bit product of the significands is
-// built from four 32 x 32 -> 64-bit products (53 = 21 + 32 bits), normalised
-// by at most one bit and rounded from its guard bit and the sticky OR of the
-// bits below.  A zero operand times a finite one gives the signed zero; other
-// zeros, subnormals, infinities, NaN and products that overflow or underflow
-// go to the FP64 unit.
+// a * b, round to nearest even, in 32-bit words.  With the significands
+// split as a = a1 2^32 + a0 (a1 21 bits), the 106-bit product is summed by
+// columns with 32 x 32 + 64 -> 64-bit multiply-adds; its top 53 bits (from
+// bit 52 + top, top = product >= 2^105) are funnel-shifted out and rounded
+// from the guard bit and the sticky OR of the bits below.  A rounding carry
+// out of 53 bits leaves exactly 2^53, whose stored significand field is zero,
+// so only the exponent moves.  A zero operand times a finite one gives the
+// signed zero; other zeros, subnormals, infinities, NaN and products that
+// overflow or underflow go to the FP64 unit.
 MCFD_IA_FN double mul_rn(double a, double b) {
   const u64 ia = bits(a), ib = bits(b);
-  const unsigned ea = (unsigned)(ia >> 52) & 0x7ffu, eb = (unsigned)(ib >> 52) & 0x7ffu;
-  const u64 ma = (ia & kMant) | kImpl, mb = (ib & kMant) | kImpl;
-  const unsigned a0 = (unsigned)ma, a1 = (unsigned)(ma >> 32), b0 = (unsigned)mb, b1 = (unsigned)(mb >> 32);
-  const u64 p00 = (u64)a0 * b0, mid = (u64)a0 * b1 + (u64)a1 * b0, p11 = (u64)a1 * b1;
-  const u64 lo = p00 + (mid << 32);
-  const u64 hi = p11 + (mid >> 32) + (u64)(lo < p00);  // product = hi 2^64 + lo < 2^106
-  const unsigned top = (unsigned)(hi >> 41);            // product >= 2^105
-  // 53-bit significand, guard bit and sticky bits below it
-  u64 m, guard, sticky;
-  if (top) {
-    m = (hi << 11) | (lo >> 53);
-    guard = (lo >> 52) & 1ull;
-    sticky = (u64)((lo & 0x000fffffffffffffull) != 0ull);
-  } else {
-    m = (hi << 12) | (lo >> 52);
-    guard = (lo >> 51) & 1ull;
-    sticky = (u64)((lo & 0x0007ffffffffffffull) != 0ull);
-  }
-  int e = (int)ea + (int)eb - 1023 + (int)top;
-  const bool underflow = e < 1;
-  m += guard & (sticky | (m & 1ull));
-  const unsigned carry = (unsigned)(m >> 53);
-  m >>= carry;
-  e += (int)carry;
-  const u64 sign = bits_and(sign_xor(ia, ib), kSign);
-  const bool a_zero = (ia << 1) == 0ull, b_zero = (ib << 1) == 0ull;
-  const bool zero = (a_zero && eb != 0x7ffu) || (b_zero && ea != 0x7ffu);
-  if (!zero && (ea - 1u >= 0x7feu || eb - 1u >= 0x7feu || underflow || e > 2046)) return mul_fp64(a, b);
-  return from_bits(zero ? sign : (sign | ((u64)e << 52) | (m & kMant)));
+  const unsigned ahi = (unsigned)(ia >> 32), bhi = (unsigned)(ib >> 32);
+  const unsigned a0 = (unsigned)ia, b0 = (unsigned)ib;
+  const unsigned ea = (ahi >> 20) & 0x7ffu, eb = (bhi >> 20) & 0x7ffu;
+  const unsigned a1 = (ahi & 0xfffffu) | 0x100000u, b1 = (bhi & 0xfffffu) | 0x100000u;
+  // columns: product = w3:w2 2^64 + w1 2^32 + w0
+  const u64 p00 = (u64)a0 * b0;
+  const u64 t = (u64)a0 * b1 + (p00 >> 32);
+  const u64 u = (u64)a1 * b0 + (unsigned)t;
+  const unsigned w0 = (unsigned)p00, w1 = (unsigned)u;
+  const u64 w23 = (u64)a1 * b1 + (t >> 32) + (u >> 32);  // < 2^42
+  const unsigned w2 = (unsigned)w23, w3 = (unsigned)(w23 >> 32);
+  const unsigned top = w3 >> 9;  // product >= 2^105
+  const unsigned sh = 20u + top;  // the significand starts at bit 52 + top = 32 + sh
+  const unsigned m_lo = shr_funnel(w1, w2, sh), m_hi = shr_funnel(w2, w3, sh);
+  const unsigned guard = (w1 >> (sh - 1u)) & 1u;
+  const unsigned sticky = ((w1 & ((1u << (sh - 1u)) - 1u)) | w0) != 0u ? 1u : 0u;
+  const unsigned inc = guard & (sticky | m_lo);
+  const unsigned r_lo = m_lo + inc;
+  const unsigned r_hi = m_hi + (r_lo < inc ? 1u : 0u);  // 2^20 <= r_hi <= 2^21
+  const unsigned carry = r_hi >> 21;
+  const int e0 = (int)ea + (int)eb - 1023 + (int)top;
+  const int e = e0 + (int)carry;
+  const unsigned sign = (ahi ^ bhi) & 0x80000000u;
+  const bool zero = ((ahi << 1) | a0) == 0u || ((bhi << 1) | b0) == 0u;
+  const bool special = ea - 1u >= 0x7feu || eb - 1u >= 0x7feu;
+  if (zero ? (ea == 0x7ffu || eb == 0x7ffu) : (special || e0 < 1 || e > 2046)) return mul_fp64(a, b);
+  const unsigned hi_word = zero ? sign : (sign | ((unsigned)e << 20) | (r_hi & 0xfffffu));
+  return from_bits(((u64)hi_word << 32) | (zero ? 0u : r_lo));
 }
 
 MCFD_IA_FN double sqrt_rn(double x) {

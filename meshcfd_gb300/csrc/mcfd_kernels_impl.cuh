@@ -38,6 +38,36 @@ static constexpr int kBlock = 256;
 static constexpr bool kFast = MCFD_FAST == 2;      // fast arithmetic (fluxes, primitive)
 static constexpr bool kMinRatio = MCFD_FAST == 1;  // min-ratio limiter, exact arithmetic
 
+// Products that the exact-arithmetic variants evaluate on the integer pipe
+// (mul_rn, the same IEEE result) to take load off the FP64 pipe, which bounds
+// these kernels.  MCFD_INT_MUL is a mask of the call sites that do so; the
+// fma variant always keeps the native product so that it can contract into
+// DFMA.
+enum IntMulSite {
+  MUL_GRADIENT = 1,   // reconstruction: gradient sums  c (q - p)
+  MUL_INCREMENT = 2,  // reconstruction: face increments  grad . r
+  MUL_OUTPUT = 4,     // reconstruction: limited face value  phi inc
+  MUL_GATHER = 8,     // gather: divergence  a F and the stage combination
+};
+// Defaults measured on the 1024^2 vortex RK3 step (GB300): all sites for the
+// exact variant (+7 %), gradient + output + gather for the fast variant
+// (+8 %; its variable-at-a-time increments lose from the longer chains).
+#ifndef MCFD_INT_MUL
+#if MCFD_FAST == 0
+#define MCFD_INT_MUL 15
+#elif MCFD_FAST == 1
+#define MCFD_INT_MUL 13
+#else
+#define MCFD_INT_MUL 0
+#endif
+#endif
+
+template <int SITE>
+__device__ __forceinline__ double kmul(double a, double b) {
+  if constexpr (kFast || (MCFD_INT_MUL & SITE) == 0) return a * b;
+  else return mul_rn(a, b);
+}
+
 __device__ __forceinline__ St4 to_prim(const St4& U, double gamma, bool* ok) {
   if constexpr (kFast) return cons_to_prim_fast(U, gamma, ok);
   else return cons_to_prim(U, gamma, ok);
@@ -101,8 +131,8 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       double d = qv[v] - pv[v];
-      gx[v] = gx[v] + cx * d;
-      gy[v] = gy[v] + cy * d;
+      gx[v] = gx[v] + kmul<MUL_GRADIENT>(cx, d);
+      gy[v] = gy[v] + kmul<MUL_GRADIENT>(cy, d);
       // density and pressure are positive (checked at primitive recovery), so
       // their order is the order of the raw bits; velocities need the key.
       const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
@@ -120,7 +150,7 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
     const double2 d = g.lim_d[s];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      double inc = gx[v] * d.x + gy[v] * d.y;
+      double inc = kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y);
       double f = limiter_face_factor<LIMITER>(pv[v], inc, lo[v], hi[v], tol[v]);
       if (icmp::lt_nonneg(f, phi[v])) phi[v] = f;
     }
@@ -129,7 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double*
     const double2 d = g.lim_d[s];
     double out[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (gx[v] * d.x + gy[v] * d.y);
+    for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y));
     st4(recon + 4 * (size_t)g.lim_slot[s], St4{out[0], out[1], out[2], out[3]});
   }
 }
@@ -158,8 +188,8 @@ __device__ __forceinline__ void reconstruct_cell_fast(const DevGeom& g, const do
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       double d = qv[v] - pv[v];
-      gx[v] += cx * d;
-      gy[v] += cy * d;
+      gx[v] += kmul<MUL_GRADIENT>(cx, d);
+      gy[v] += kmul<MUL_GRADIENT>(cy, d);
       const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
       const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
       if (below) lo[v] = qv[v];
@@ -195,7 +225,7 @@ __device__ __forceinline__ void reconstruct_cell_fast(const DevGeom& g, const do
       const double2 d = g.lim_d[s0 + k];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        double inc = gx[v] * d.x + gy[v] * d.y;
+        double inc = kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y);
         inc_cache[k][v] = inc;
         classify(v, inc);
       }
@@ -205,7 +235,7 @@ __device__ __forceinline__ void reconstruct_cell_fast(const DevGeom& g, const do
     for (int s = s0 + kCache; s < s1; ++s) {
       const double2 d = g.lim_d[s];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) classify(v, gx[v] * d.x + gy[v] * d.y);
+      for (int v = 0; v < 4; ++v) classify(v, kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y));
     }
   }
   double phi[4];
@@ -229,7 +259,7 @@ __device__ __forceinline__ void reconstruct_cell_fast(const DevGeom& g, const do
       const double2 d = g.lim_d[s];
       double out[4];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (gx[v] * d.x + gy[v] * d.y);
+      for (int v = 0; v < 4; ++v) out[v] = pv[v] + phi[v] * (kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y));
       st4(recon + 4 * (size_t)g.lim_slot[s], St4{out[0], out[1], out[2], out[3]});
     }
   }
@@ -257,8 +287,8 @@ __device__ __forceinline__ void reconstruct_cell_fast_by_variable(const DevGeom&
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       double d = qv[v] - pv[v];
-      gx[v] += cx * d;
-      gy[v] += cy * d;
+      gx[v] += kmul<MUL_GRADIENT>(cx, d);
+      gy[v] += kmul<MUL_GRADIENT>(cy, d);
       const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
       const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
       if (below) lo[v] = qv[v];
@@ -279,7 +309,7 @@ __device__ __forceinline__ void reconstruct_cell_fast_by_variable(const DevGeom&
     bool has_pos = false, has_neg = false, flat = false;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      inc[k] = gx[v] * dk[k].x + gy[v] * dk[k].y;
+      inc[k] = kmul<MUL_INCREMENT>(gx[v], dk[k].x) + kmul<MUL_INCREMENT>(gy[v], dk[k].y);
       if (icmp::gt_pos(inc[k], tol)) {
         has_pos = true;
         if (icmp::lt_nonneg(pos, inc[k])) pos = inc[k];
@@ -297,7 +327,7 @@ __device__ __forceinline__ void reconstruct_cell_fast_by_variable(const DevGeom&
     else
       phi = limiter_factor_fast<LIMITER>(hi[v] - pv[v], pos, pv[v] - lo[v], neg, has_pos, has_neg, flat);
 #pragma unroll
-    for (int k = 0; k < NS; ++k) recon[out[k] + v] = pv[v] + phi * inc[k];
+    for (int k = 0; k < NS; ++k) recon[out[k] + v] = pv[v] + kmul<MUL_OUTPUT>(phi, inc[k]);
   }
 }
 
@@ -400,10 +430,10 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
   for (int j = g.gi_ptr[c], j1 = g.gi_ptr[c + 1]; j < j1; ++j) {
     const double a = g.gi_coef[j];
     const St4 F = ld4(flux + 4 * (size_t)g.gi_flux[j]);
-    s[0] = s[0] + a * F.a;
-    s[1] = s[1] + a * F.b;
-    s[2] = s[2] + a * F.c;
-    s[3] = s[3] + a * F.d;
+    s[0] = s[0] + kmul<MUL_GATHER>(a, F.a);
+    s[1] = s[1] + kmul<MUL_GATHER>(a, F.b);
+    s[2] = s[2] + kmul<MUL_GATHER>(a, F.c);
+    s[3] = s[3] + kmul<MUL_GATHER>(a, F.d);
   }
   double r[4] = {plus_zero(s[0]), plus_zero(s[1]), plus_zero(s[2]), plus_zero(s[3])};  // 0.0 + s
   // boundary groups: np.add.at(derivative, owners, -(flux*L)/A) in BC order
@@ -442,18 +472,18 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
   double u[4];
   if (SHAPE == SHAPE_EULER) {
     const St4 x = ld4(prog.t[0].x + 4 * (size_t)c);
-    u[0] = x.a + dt * r[0];
-    u[1] = x.b + dt * r[1];
-    u[2] = x.c + dt * r[2];
-    u[3] = x.d + dt * r[3];
+    u[0] = x.a + kmul<MUL_GATHER>(dt, r[0]);
+    u[1] = x.b + kmul<MUL_GATHER>(dt, r[1]);
+    u[2] = x.c + kmul<MUL_GATHER>(dt, r[2]);
+    u[3] = x.d + kmul<MUL_GATHER>(dt, r[3]);
   } else if (SHAPE == SHAPE_X_XDTR) {
     const double c0 = prog.t[0].coef, c1 = prog.t[1].coef;
     const St4 x0 = ld4(prog.t[0].x + 4 * (size_t)c);
     const St4 x1 = ld4(prog.t[1].x + 4 * (size_t)c);
-    u[0] = c0 * x0.a + c1 * (x1.a + dt * r[0]);
-    u[1] = c0 * x0.b + c1 * (x1.b + dt * r[1]);
-    u[2] = c0 * x0.c + c1 * (x1.c + dt * r[2]);
-    u[3] = c0 * x0.d + c1 * (x1.d + dt * r[3]);
+    u[0] = kmul<MUL_GATHER>(c0, x0.a) + kmul<MUL_GATHER>(c1, x1.a + kmul<MUL_GATHER>(dt, r[0]));
+    u[1] = kmul<MUL_GATHER>(c0, x0.b) + kmul<MUL_GATHER>(c1, x1.b + kmul<MUL_GATHER>(dt, r[1]));
+    u[2] = kmul<MUL_GATHER>(c0, x0.c) + kmul<MUL_GATHER>(c1, x1.c + kmul<MUL_GATHER>(dt, r[2]));
+    u[3] = kmul<MUL_GATHER>(c0, x0.d) + kmul<MUL_GATHER>(c1, x1.d + kmul<MUL_GATHER>(dt, r[3]));
   } else {
   for (int t = 0; t < prog.n_terms; ++t) {
     const StageTerm term = prog.t[t];
