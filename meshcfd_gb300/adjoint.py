@@ -75,6 +75,7 @@ class WallForceAdjoint:
             self.dt = float(dt)
             self.dt_dev = torch.full((1,), self.dt, dtype=torch.float64, device=dev)
             self.far_dt = self.dt
+        self.dt_col = self.dt_dev.view(-1, 1)
         self.direction = direction
         self.k = int(checkpoint_every)
         self.case_offsets = None if case_offsets is None else np.asarray(case_offsets, dtype=np.int64)
@@ -130,6 +131,11 @@ class WallForceAdjoint:
                 self.far_acc.add_(self.far, alpha=coef * self.dt)
         return self.W
 
+    def _plus_dt(self, x, w):
+        """x + dt w as one kernel; a scalar dt is a 1x1 tensor, so that a
+        batch (per-cell dt) and a single case round identically."""
+        return torch.addcmul(x, w, self.dt_col)
+
     def _replay(self, U):
         """Advance U one step in place; returns the step's stage states
         (U0, U1, U2) and, per stage, the primitive and face states the
@@ -164,13 +170,12 @@ class WallForceAdjoint:
             records = [self._replay(U) for _ in range(start, end)]
             for (U0, U1, U2), Ps, recons in reversed(records):
                 w = self._vjp(U2, Ps[2], recons[2], lam, 2.0 / 3.0)
-                lam2 = (2.0 / 3.0) * (lam + dt * w)
-                new = (1.0 / 3.0) * lam
+                lam2 = self._plus_dt(lam, w).mul_(2.0 / 3.0)
                 w = self._vjp(U1, Ps[1], recons[1], lam2, 0.25)
-                lam1 = 0.25 * (lam2 + dt * w)
-                new += 0.75 * lam2
+                lam1 = self._plus_dt(lam2, w).mul_(0.25)
                 w = self._vjp(U0, Ps[0], recons[0], lam1, 1.0)
-                new += lam1 + dt * w
+                new = self._plus_dt(lam1, w)
+                new.add_(lam, alpha=1.0 / 3.0).add_(lam2, alpha=0.75)
                 lam = new
             del records
         self.geom.check_status()

@@ -64,7 +64,7 @@ __device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, const Dual<N>& b)
 template <int N>
 __device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r;
-  const double ib = 1.0 / b.v;
+  const double ib = div_rn(1.0, b.v);
   r.v = a.v * ib;
 #pragma unroll
   for (int k = 0; k < N; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
@@ -73,15 +73,15 @@ __device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b)
 template <int N>
 __device__ __forceinline__ Dual<N> sqrt(const Dual<N>& a) {
   Dual<N> r;
-  r.v = ::sqrt(a.v);
-  const double h = 0.5 / r.v;
+  r.v = sqrt_rn(a.v);
+  const double h = div_rn(0.5, r.v);
 #pragma unroll
   for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * h;
   return r;
 }
 template <int N>
 __device__ __forceinline__ Dual<N> fabs(const Dual<N>& a) {
-  return a.v < 0.0 ? -a : a;
+  return icmp::neg_gt_pos(a.v, 0.0) ? -a : a;  // a.v < 0
 }
 template <int N>
 __device__ __forceinline__ Dual<N> pow(const Dual<N>& a, double e) {
@@ -106,11 +106,11 @@ struct S4 {
 
 template <typename T>
 __device__ __forceinline__ T tmin(const T& a, const T& b) {  // Python min(a, b)
-  return val(b) < val(a) ? b : a;
+  return icmp::lt(val(b), val(a)) ? b : a;
 }
 template <typename T>
 __device__ __forceinline__ T tmax(const T& a, const T& b) {  // Python max(a, b)
-  return val(b) > val(a) ? b : a;
+  return icmp::lt(val(a), val(b)) ? b : a;
 }
 
 // euler.conservative_to_primitive

@@ -37,6 +37,7 @@ struct mcfd_geom {
   int imp_exact_jacobian = 0;  // GMRES operator: 0 finite differences (reference), 1 exact JVP
   JvpWork jvp;                 // tangent workspace (allocated on first use)
   VjpWork vjp;                 // adjoint workspace (allocated on first use)
+  SideStream side;             // boundary face segments of the forward flux
   std::vector<void*> jvp_owned;
   ViscousWork visc;            // laminar viscous workspace (allocated on first use)
   // mcfd_explicit_step_record: per-stage copies of the primitive and face states
@@ -140,12 +141,18 @@ static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgra
                          cudaStream_t s) {
   StageProgram prog = prog_in;
   cudaError_t e = cudaSuccess;
+  // mcfd_explicit_step_record: the face states go straight into the caller's
+  // record buffer (the primitive is copied below)
+  const bool record = h->rec_P && h->rec_k < h->rec_n;
+  double* recon_out = h->ws.recon;
+  if (record && h->rec_recon && h->rec_recon[h->rec_k] && cfg.reconstruction != MCFD_RECON_FIRST_ORDER)
+    recon_out = h->rec_recon[h->rec_k];
   if (cfg.reconstruction == MCFD_RECON_MUSCL_LINEAR)
-    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return MCFD_DISPATCH(cfg, launch_reconstruct(h->g, cfg, h->ws.P, h->ws.recon, s)); });
+    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return MCFD_DISPATCH(cfg, launch_reconstruct(h->g, cfg, h->ws.P, recon_out, s)); });
   else if (cfg.reconstruction == MCFD_RECON_MUSCL_PARABOLIC)
-    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return launch_reconstruct_parabolic(h->g, cfg, h->ws.P, h->ws.recon, s); });
+    e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return launch_reconstruct_parabolic(h->g, cfg, h->ws.P, recon_out, s); });
   if (e == cudaSuccess && h->g.n_bc_patches > 0) {
-    const double* recon = cfg.reconstruction == MCFD_RECON_FIRST_ORDER ? nullptr : h->ws.recon;
+    const double* recon = cfg.reconstruction == MCFD_RECON_FIRST_ORDER ? nullptr : recon_out;
     e = timed(h, MCFD_PROF_FLUX, s, [&] { return launch_bc_states(h->g, cfg, h->ws.P, recon, h->g.bc_ext, s); });
   }
   if (e == cudaSuccess && cfg.viscosity_model != MCFD_VISC_INVISCID) {  // solver.py:2699-2702
@@ -154,15 +161,12 @@ static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgra
       e = timed(h, MCFD_PROF_OTHER, s, [&] { return launch_viscous_residual(h->g, cfg, h->ws.P, h->visc, s); });
     prog.visc_r = h->visc.r;
   }
-  if (e == cudaSuccess && h->rec_P && h->rec_k < h->rec_n) {  // mcfd_explicit_step_record
+  if (e == cudaSuccess && record) {
     const int k = h->rec_k++;
     e = cudaMemcpyAsync(h->rec_P[k], h->ws.P, 4 * sizeof(double) * (size_t)h->g.n_cells, cudaMemcpyDeviceToDevice, s);
-    if (e == cudaSuccess && h->rec_recon && h->rec_recon[k] && cfg.reconstruction != MCFD_RECON_FIRST_ORDER)
-      e = cudaMemcpyAsync(h->rec_recon[k], h->ws.recon, 4 * sizeof(double) * (size_t)h->g.n_slots,
-                          cudaMemcpyDeviceToDevice, s);
   }
   if (e == cudaSuccess)
-    e = timed(h, MCFD_PROF_FLUX, s, [&] { return MCFD_DISPATCH(cfg, launch_flux(h->g, cfg, h->ws.P, h->ws.recon, h->ws.flux, s)); });
+    e = timed(h, MCFD_PROF_FLUX, s, [&] { return MCFD_DISPATCH(cfg, launch_flux(h->g, cfg, h->ws.P, recon_out, h->ws.flux, s, &h->side)); });
   if (e == cudaSuccess)
     e = timed(h, MCFD_PROF_GATHER, s, [&] { return MCFD_DISPATCH(cfg, launch_gather(h->g, cfg, h->ws.P, h->ws.flux, prog, s)); });
   return e;
@@ -711,7 +715,13 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   // geometry part only (workspace stays uninitialised)
   err = cudaMemcpy(base, host.data(), o_P, cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMallocHost(&h->host_status, sizeof(DevStatus));
+  if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&h->side.stream, cudaStreamNonBlocking);
+  if (err == cudaSuccess) err = cudaEventCreateWithFlags(&h->side.fork, cudaEventDisableTiming);
+  if (err == cudaSuccess) err = cudaEventCreateWithFlags(&h->side.join, cudaEventDisableTiming);
   if (err != cudaSuccess) {
+    if (h->side.stream) cudaStreamDestroy(h->side.stream);
+    if (h->side.fork) cudaEventDestroy(h->side.fork);
+    if (h->host_status) cudaFreeHost(h->host_status);
     cudaFree(h->arena);
     delete h;
     return MCFD_E_CUDA;
@@ -853,6 +863,12 @@ int mcfd_geom_destroy(mcfd_geom* h) {
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
   if (h->imp_built) implicit_free(h->imp);
   for (void* p : h->jvp_owned) cudaFree(p);
+  if (h->side.stream) cudaStreamDestroy(h->side.stream);
+  if (h->side.fork) cudaEventDestroy(h->side.fork);
+  if (h->side.join) cudaEventDestroy(h->side.join);
+  if (h->vjp.side) cudaStreamDestroy(h->vjp.side);
+  if (h->vjp.fork) cudaEventDestroy(h->vjp.fork);
+  if (h->vjp.join) cudaEventDestroy(h->vjp.join);
   cudaError_t e1 = cudaFree(h->arena);
   cudaError_t e2 = cudaFreeHost(h->host_status);
   delete h;
@@ -943,7 +959,7 @@ int mcfd_autotune(mcfd_geom* h, const mcfd_config* cfg, const double* U, int32_t
       for (int f : kFaces) {
         g.tune_flux_threads = t;
         g.tune_flux_faces = f;
-        const float ms = time_ms([&] { MCFD_DISPATCH(*cfg, launch_flux(g, *cfg, h->ws.P, h->ws.recon, h->ws.flux, s)); });
+        const float ms = time_ms([&] { MCFD_DISPATCH(*cfg, launch_flux(g, *cfg, h->ws.P, h->ws.recon, h->ws.flux, s, nullptr)); });
         if (ms < best) best = ms, best_flux_t = t, best_flux_f = f;
       }
     g.tune_flux_threads = best_flux_t;
@@ -1212,6 +1228,10 @@ static int ensure_vjp(mcfd_geom* h) {
     if (cudaMalloc((void**)fields[k], sizes[k]) != cudaSuccess) return MCFD_E_CUDA;
     h->jvp_owned.push_back(*fields[k]);
   }
+  if (cudaStreamCreateWithFlags(&h->vjp.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->vjp.fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->vjp.join, cudaEventDisableTiming) != cudaSuccess)
+    return MCFD_E_CUDA;
   return MCFD_OK;
 }
 

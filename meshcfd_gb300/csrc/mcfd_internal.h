@@ -149,6 +149,13 @@ struct Workspace {
   int partial_blocks;
 };
 
+// A second stream with fork / join events: the boundary face segments run on
+// it concurrently with the interior faces (disjoint outputs).
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
 // kernels (mcfd_kernels_impl.cuh), one set per variant: mcfd::exact (reference
 // operation order), mcfd::fast (smallest-ratio limiter), mcfd::fma (fewer
 // divisions everywhere, FMA).
@@ -159,7 +166,8 @@ struct Workspace {
   cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const double* P,    \
                                  double* recon, cudaStream_t s);                               \
   cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* P,           \
-                          const double* recon, double* flux, cudaStream_t s);                  \
+                          const double* recon, double* flux, cudaStream_t s,                   \
+                          const SideStream* side);                                             \
   cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double* P,         \
                             const double* flux, const StageProgram& prog, cudaStream_t s);     \
   cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const double* P,     \

@@ -626,27 +626,39 @@ cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const d
   return cudaGetLastError();
 }
 
+// Boundary segments run on the side stream (when given) concurrently with
+// the interior faces; every face writes only its own flux row.
 template <int FLUX, bool FO, bool KH>
 static void flux_segments(const DevGeom& g, const double* P, const double* recon, double* flux,
-                          double gamma, cudaStream_t s) {
+                          double gamma, cudaStream_t s, const SideStream* side) {
   const double inv_gm1 = 1.0 / (gamma - 1.0);
-#define MCFD_SEG(SEGV)                                                              \
+  const bool fork = side && side->stream && g.seg_begin[SEG_COUNT] > g.seg_begin[SEG_INTERIOR + 1];
+  if (fork) {
+    cudaEventRecord(side->fork, s);
+    cudaStreamWaitEvent(side->stream, side->fork, 0);
+  }
+  const cudaStream_t b = fork ? side->stream : s;
+#define MCFD_SEG(SEGV, STREAM)                                                      \
   {                                                                                 \
     int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                              \
-    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<flux_blocks(g, n), flux_threads(g, n), 0, s>>>(g, P, recon, flux, gamma, inv_gm1); \
+    if (n > 0) count_launch(), k_flux<FLUX, SEGV, FO, KH><<<flux_blocks(g, n), flux_threads(g, n), 0, STREAM>>>(g, P, recon, flux, gamma, inv_gm1); \
   }
-  MCFD_SEG(SEG_INTERIOR)
-  MCFD_SEG(SEG_PERIODIC)
-  MCFD_SEG(SEG_WALL)
-  MCFD_SEG(SEG_VIN)
-  MCFD_SEG(SEG_POUT)
-  MCFD_SEG(SEG_FAR)
-  MCFD_SEG(SEG_BCX)
+  MCFD_SEG(SEG_PERIODIC, b)
+  MCFD_SEG(SEG_WALL, b)
+  MCFD_SEG(SEG_VIN, b)
+  MCFD_SEG(SEG_POUT, b)
+  MCFD_SEG(SEG_FAR, b)
+  MCFD_SEG(SEG_BCX, b)
+  MCFD_SEG(SEG_INTERIOR, s)
 #undef MCFD_SEG
+  if (fork) {
+    cudaEventRecord(side->join, side->stream);
+    cudaStreamWaitEvent(s, side->join, 0);
+  }
 }
 
 cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* P,
-                        const double* recon, double* flux, cudaStream_t s) {
+                        const double* recon, double* flux, cudaStream_t s, const SideStream* side) {
   const bool fo = cfg.reconstruction == MCFD_RECON_FIRST_ORDER;
   // The reference evaluates interior HLLC faces with its fused compiled kernel
   // when no curvature is present (solver.py:2479-2490); that kernel has its
@@ -654,17 +666,17 @@ cudaError_t launch_flux(const DevGeom& g, const mcfd_config& cfg, const double* 
   const bool kernel_hllc = cfg.reconstruction != MCFD_RECON_MUSCL_PARABOLIC;
   switch (cfg.flux) {
     case MCFD_FLUX_RUSANOV:
-      if (fo) flux_segments<0, true, false>(g, P, recon, flux, cfg.gamma, s);
-      else flux_segments<0, false, false>(g, P, recon, flux, cfg.gamma, s);
+      if (fo) flux_segments<0, true, false>(g, P, recon, flux, cfg.gamma, s, side);
+      else flux_segments<0, false, false>(g, P, recon, flux, cfg.gamma, s, side);
       break;
     case MCFD_FLUX_HLLC:
-      if (fo) flux_segments<1, true, true>(g, P, recon, flux, cfg.gamma, s);
-      else if (kernel_hllc) flux_segments<1, false, true>(g, P, recon, flux, cfg.gamma, s);
-      else flux_segments<1, false, false>(g, P, recon, flux, cfg.gamma, s);
+      if (fo) flux_segments<1, true, true>(g, P, recon, flux, cfg.gamma, s, side);
+      else if (kernel_hllc) flux_segments<1, false, true>(g, P, recon, flux, cfg.gamma, s, side);
+      else flux_segments<1, false, false>(g, P, recon, flux, cfg.gamma, s, side);
       break;
     default:
-      if (fo) flux_segments<2, true, false>(g, P, recon, flux, cfg.gamma, s);
-      else flux_segments<2, false, false>(g, P, recon, flux, cfg.gamma, s);
+      if (fo) flux_segments<2, true, false>(g, P, recon, flux, cfg.gamma, s, side);
+      else flux_segments<2, false, false>(g, P, recon, flux, cfg.gamma, s, side);
       break;
   }
   return cudaGetLastError();

@@ -61,18 +61,18 @@ struct Sound {
   double c, dp, dr;
 };
 __device__ __forceinline__ Sound sound_d(const St4& q, double gamma) {
-  const double inv_r = 1.0 / q.a;
-  const double c = sqrt(gamma * q.d * inv_r);
+  const double inv_r = div_rn(1.0, q.a);
+  const double c = sqrt_rn(gamma * q.d * inv_r);
   const double h = 0.5 * inv_r;
-  return Sound{c, gamma * h / c, -c * h};
+  return Sound{c, div_rn(gamma * h, c), -c * h};
 }
 
 __device__ __forceinline__ void rusanov_bar(const St4& L, const St4& R, double nx, double ny, double gamma,
                                             double inv_gm1, const double Fb[4], double Lb[4], double Rb[4]) {
   const double unl = L.b * nx + L.c * ny, unr = R.b * nx + R.c * ny;
   const Sound sl_ = sound_d(L, gamma), sr_ = sound_d(R, gamma);
-  const double sl = fabs(unl) + sl_.c, sr = fabs(unr) + sr_.c;
-  const bool left = sl >= sr;
+  const double sl = abs_of(unl) + sl_.c, sr = abs_of(unr) + sr_.c;
+  const bool left = !icmp::lt_nonneg(sl, sr);  // sl >= sr
   const double s = left ? sl : sr;
   const double UL[4] = {L.a, L.a * L.b, L.a * L.c, L.d * inv_gm1 + 0.5 * L.a * (L.b * L.b + L.c * L.c)};
   const double UR[4] = {R.a, R.a * R.b, R.a * R.c, R.d * inv_gm1 + 0.5 * R.a * (R.b * R.b + R.c * R.c)};
@@ -88,7 +88,7 @@ __device__ __forceinline__ void rusanov_bar(const St4& L, const St4& R, double n
   physical_bar(R, nx, ny, inv_gm1, FLb, URb, Rb);
   double* qb = left ? Lb : Rb;
   const Sound& sd = left ? sl_ : sr_;
-  const double unb = (left ? unl : unr) < 0.0 ? -sb : sb;
+  const double unb = icmp::neg_gt_pos(left ? unl : unr, 0.0) ? negate(sb) : sb;
   qb[0] += sb * sd.dr;
   qb[1] += unb * nx;
   qb[2] += unb * ny;
@@ -103,25 +103,25 @@ __device__ __forceinline__ void hllc_bar(const St4& L, const St4& R, double nx, 
   const Sound sl_ = sound_d(L, gamma), sr_ = sound_d(R, gamma);
   const double cl = sl_.c, cr = sr_.c;
   const double a1 = unl - cl, b1 = unr - cr;
-  const bool wl_right = b1 < a1;
+  const bool wl_right = icmp::lt(b1, a1);
   const double wl = wl_right ? b1 : a1;
   const double a2 = unl + cl, b2 = unr + cr;
-  const bool wr_right = b2 > a2;
+  const bool wr_right = icmp::lt(a2, b2);
   const double wr = wr_right ? b2 : a2;
   double den = L.a * (wl - unl) - R.a * (wr - unr);
-  const bool guarded = !(fabs(den) > 1e-14);
-  if (guarded) den = copysign(1e-14, den);
-  const double inv_den = 1.0 / den;
+  const bool guarded = !icmp::abs_gt(den, 1e-14);
+  if (guarded) den = with_sign_of(1e-14, den);
+  const double inv_den = div_rn(1.0, den);
   const double contact = ((R.d - L.d) + L.a * unl * (wl - unl) - R.a * unr * (wr - unr)) * inv_den;
   int branch;
   if (KERNEL_BRANCHES) {
-    if (wl >= 0.0) branch = 0;
-    else if (wr <= 0.0) branch = 3;
-    else branch = contact >= 0.0 ? 1 : 2;
+    if (icmp::ge0(wl)) branch = 0;
+    else if (icmp::le0(wr)) branch = 3;
+    else branch = icmp::ge0(contact) ? 1 : 2;
   } else {
-    if (wl >= 0.0) branch = 0;
-    else if (contact >= 0.0) branch = 1;
-    else if (wr > 0.0) branch = 2;
+    if (icmp::ge0(wl)) branch = 0;
+    else if (icmp::ge0(contact)) branch = 1;
+    else if (icmp::gt0(wr)) branch = 2;
     else branch = 3;
   }
   if (branch == 0) {
@@ -137,14 +137,14 @@ __device__ __forceinline__ void hllc_bar(const St4& L, const St4& R, double nx, 
   double* qb = left ? Lb : Rb;
   const double un = left ? unl : unr, w = left ? wl : wr;
   const double r = q.a, u = q.b, v = q.c, p = q.d;
-  const double inv_r = 1.0 / r;
+  const double inv_r = div_rn(1.0, r);
   const double E = p * inv_gm1 + 0.5 * r * (u * u + v * v);
   const double Uq[4] = {r, r * u, r * v, E};
   const double wu = w - un;
-  const double B = w - contact, inv_B = 1.0 / B, A = r * wu, factor = A * inv_B;
+  const double B = w - contact, inv_B = div_rn(1.0, B), A = r * wu, factor = A * inv_B;
   const double dc = contact - un;
   const double sux = u + dc * nx, suy = v + dc * ny;
-  const double inv_Z = inv_r / wu;  // 1 / (r (w - un))
+  const double inv_Z = div_rn(inv_r, wu);  // 1 / (r (w - un))
   const double pz = p * inv_Z;
   const double Y = contact + pz, Er = E * inv_r, X = Er + dc * Y;
   const double star[4] = {factor, factor * sux, factor * suy, factor * X};
@@ -228,11 +228,11 @@ __global__ void __launch_bounds__(kBlock) k_vjp_face_rev(DevGeom g, const double
   const double len = g.ff_len[f];
   const int lc = g.ff_lcell[f];
   const St4 la = ld4(lambda + 4 * (size_t)lc);
-  const double wl = -len / g.area[lc];
+  const double wl = div_rn(-len, g.area[lc]);
   double fb[4] = {wl * la.a, wl * la.b, wl * la.c, wl * la.d};
   if (SEG == SEG_INTERIOR || SEG == SEG_PERIODIC) {
     const St4 lb = ld4(lambda + 4 * (size_t)g.ff_rcell[f]);
-    const double wr = len / g.area[g.ff_rcell[f]];
+    const double wr = div_rn(len, g.area[g.ff_rcell[f]]);
     fb[0] += wr * lb.a; fb[1] += wr * lb.b; fb[2] += wr * lb.c; fb[3] += wr * lb.d;
   }
   const St4 L = FO ? ld4(P + 4 * (size_t)lc) : ld4(recon + 4 * (size_t)g.ff_lslot[f]);
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_face_rev(DevGeom g, const double
     R = St4{L.a, L.b, L.c, g.ff_pout_pressure[f - begin]};
   }
   double Lb[4] = {0.0, 0.0, 0.0, 0.0}, Rb[4] = {0.0, 0.0, 0.0, 0.0};
-  const double inv_gm1 = 1.0 / (gamma - 1.0);
+  const double inv_gm1 = div_rn(1.0, gamma - 1.0);
   if (FLUX == MCFD_FLUX_RUSANOV) rusanov_bar(L, R, n.x, n.y, gamma, inv_gm1, fb, Lb, Rb);
   else hllc_bar<(SEG == SEG_INTERIOR) && KH>(L, R, n.x, n.y, gamma, inv_gm1, fb, Lb, Rb);
   if (SEG == SEG_WALL) {  // R = mirror(L)
@@ -284,12 +284,12 @@ __global__ void __launch_bounds__(kBlock) k_vjp_face(DevGeom g, const double* __
   const int lc = g.ff_lcell[f];
   // face adjoint (solver.py:2164-2165 coefficients, boundary -(F L)/A)
   const St4 la = ld4(lambda + 4 * (size_t)lc);
-  const double wl = -len / g.area[lc];
+  const double wl = div_rn(-len, g.area[lc]);
   double fb[4] = {wl * la.a, wl * la.b, wl * la.c, wl * la.d};
   if (SEG == SEG_INTERIOR || SEG == SEG_PERIODIC) {
     const int rc = g.ff_rcell[f];
     const St4 lb = ld4(lambda + 4 * (size_t)rc);
-    const double wr = len / g.area[rc];
+    const double wr = div_rn(len, g.area[rc]);
     fb[0] += wr * lb.a; fb[1] += wr * lb.b; fb[2] += wr * lb.c; fb[3] += wr * lb.d;
   }
   const St4 qL = FO ? ld4(P + 4 * (size_t)lc) : ld4(recon + 4 * (size_t)g.ff_lslot[f]);
@@ -325,15 +325,15 @@ __global__ void __launch_bounds__(kBlock) k_vjp_face(DevGeom g, const double* __
 
 template <int LIMITER>
 __device__ __forceinline__ double limiter_slope(double r) {
-  if (LIMITER <= 1) return r < 1.0 ? 1.0 : 0.0;
+  if (LIMITER <= 1) return icmp::lt(r, 1.0) ? 1.0 : 0.0;
   if (LIMITER == 2) {
-    if (!(r > 0.0)) return 0.0;
-    return r < 1.0 ? 2.0 / ((1.0 + r) * (1.0 + r)) : 0.0;  // 2r / (1 + r) < 1 iff r < 1
+    if (!icmp::gt0(r)) return 0.0;
+    return icmp::lt(r, 1.0) ? div_rn(2.0, (1.0 + r) * (1.0 + r)) : 0.0;  // 2r / (1 + r) < 1 iff r < 1
   }
   const double eps = 1e-12;
   const double N = r * r + 2.0 * r + eps, D = r * r + r + 2.0 + eps;
   if (N > D) return 0.0;  // capped at 1
-  const double inv_D = 1.0 / D;
+  const double inv_D = div_rn(1.0, D);
   return ((2.0 * r + 2.0) * D - N * (2.0 * r + 1.0)) * (inv_D * inv_D);
 }
 
@@ -390,9 +390,9 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
         for (int v = 0; v < 4; ++v) {
           const double inc = gx[v] * dd.x + gy[v] * dd.y;
           if (icmp::gt_pos(inc, tol[v])) {
-            if (ps[v] < 0 || inc > pmax[v]) { pmax[v] = inc; ps[v] = s; }
+            if (ps[v] < 0 || icmp::lt(pmax[v], inc)) { pmax[v] = inc; ps[v] = s; }
           } else if (icmp::neg_gt_pos(inc, tol[v])) {
-            if (ns[v] < 0 || inc < nmin[v]) { nmin[v] = inc; ns[v] = s; }
+            if (ns[v] < 0 || icmp::lt(inc, nmin[v])) { nmin[v] = inc; ns[v] = s; }
           } else if (fs[v] < 0) {
             fs[v] = s;
           }
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
         for (int k = 0; k < 3; ++k) {
           if (cand[k] < 0) continue;
           const double f = limiter_face_factor<LIMITER>(pv[v], cinc[k], lo[v], hi[v], tol[v]);
-          if (icmp::lt_nonneg(f, phi[v]) || (f == phi[v] && arg[v] >= 0 && cand[k] < arg[v])) {
+          if (icmp::lt_nonneg(f, phi[v]) || (icmp::key(f) == icmp::key(phi[v]) && arg[v] >= 0 && cand[k] < arg[v])) {
             phi[v] = f;
             arg[v] = cand[k];
           }
@@ -434,9 +434,9 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
       const bool pos = icmp::gt_pos(inc, tol), neg = icmp::neg_gt_pos(inc, tol);
       if (!(pos || neg)) continue;
       const double num = pos ? hi[v] - pv[v] : lo[v] - pv[v];
-      const double inv_inc = 1.0 / inc;
+      const double inv_inc = div_rn(1.0, inc);
       const double r = num * inv_inc;
-      if (!(r > 0.0)) continue;
+      if (!icmp::gt0(r)) continue;
       const double rb = limiter_slope<LIMITER>(r) * phib[v];
       const double numb = rb * inv_inc;
       const double incb = -numb * r;
@@ -481,13 +481,16 @@ __global__ void __launch_bounds__(kBlock) k_vjp_collect(DevGeom g, const double*
       pb.a += x.a; pb.b += x.b; pb.c += x.c; pb.d += x.d;
     }
   }
-  // U_bar = (dP/dU)^T P_bar
-  using D4 = ad::Dual<4>;
+  // U_bar = (dP/dU)^T P_bar for P = (rho, m / rho, n / rho, (gamma - 1)(E - (m^2 + n^2) / (2 rho))):
+  //   rho_bar = rho_b - (u u_b + v v_b) / rho + (gamma - 1) (u^2 + v^2) / 2 p_b
+  //   m_bar = u_b / rho - (gamma - 1) u p_b,  n_bar = v_b / rho - (gamma - 1) v p_b
+  //   E_bar = (gamma - 1) p_b
   const St4 u = ld4(U + 4 * (size_t)c);
-  const ad::S4<D4> q = ad::prim(ad::S4<D4>{seed<4>(u.a, 0), seed<4>(u.b, 1), seed<4>(u.c, 2), seed<4>(u.d, 3)}, gamma);
-  double out[4];
-  for (int k = 0; k < 4; ++k) out[k] = pb.a * q.a.d[k] + pb.b * q.b.d[k] + pb.c * q.c.d[k] + pb.d * q.d.d[k];
-  st4(ubar + 4 * (size_t)c, St4{out[0], out[1], out[2], out[3]});
+  const double inv = div_rn(1.0, u.a), vx = u.b * inv, vy = u.c * inv;
+  const double gp = (gamma - 1.0) * pb.d;
+  const double ub = pb.b * inv, vb = pb.c * inv;
+  const St4 out{pb.a - (vx * ub + vy * vb) + 0.5 * gp * (vx * vx + vy * vy), ub - gp * vx, vb - gp * vy, gp};
+  st4(ubar + 4 * (size_t)c, out);
 }
 
 // wall pressure force: per cell, its wall faces' p_c (n . dir) L, and the
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(kBlock) k_wall_force(DevGeom g, const double* 
     w += (n.x * dx + n.y * dy) * g.ff_len[f];
   }
   const St4 u = ld4(U + 4 * (size_t)c);
-  const double inv = 1.0 / u.a, vx = u.b * inv, vy = u.c * inv;
+  const double inv = div_rn(1.0, u.a), vx = u.b * inv, vy = u.c * inv;
   const double p = (gamma - 1.0) * (u.d - 0.5 * (u.b * u.b + u.c * u.c) * inv);
   cell_force[c] = p * w;
   if (dJdU) {
@@ -535,29 +538,44 @@ __global__ void k_sum_final(int blocks, const double* __restrict__ partials, dou
   }
 }
 
+// The interior segment runs on s; the boundary segments (periodic, wall,
+// inlet, outlet, far field: few faces, some of them in dual numbers and
+// latency-bound) on w.side, forked from s after the slot adjoints are zeroed
+// and joined back before the cell reverse.  Faces write disjoint slots.
 template <int FLUX, bool FO, bool KH>
 void face_segments(const DevGeom& g, const double* P, const double* recon, const double* lambda, double gamma,
-                   double* slot_bar, double* far_bar, cudaStream_t s) {
-#define MCFD_SEG(SEGV)                                                                                          \
+                   double* slot_bar, double* far_bar, const VjpWork& w, cudaStream_t s) {
+  const int n_boundary = g.seg_begin[SEG_COUNT] - g.seg_begin[SEG_INTERIOR + 1];
+  const bool fork = n_boundary > 0 && w.side;
+  if (fork) {
+    cudaEventRecord(w.fork, s);
+    cudaStreamWaitEvent(w.side, w.fork, 0);
+  }
+#define MCFD_SEG(SEGV, STREAM)                                                                                  \
   {                                                                                                             \
     int n = g.seg_begin[SEGV + 1] - g.seg_begin[SEGV];                                                          \
     if (n > 0) {                                                                                                \
       count_launch();                                                                                           \
       if (FLUX != MCFD_FLUX_ROE && SEGV != SEG_FAR)                                                             \
         k_vjp_face_rev<(FLUX == MCFD_FLUX_ROE ? MCFD_FLUX_HLLC : FLUX), SEGV, FO, KH>                           \
-            <<<seg_blocks(n), seg_threads(n), 0, s>>>(g, P, recon, lambda, gamma, slot_bar);                    \
+            <<<seg_blocks(n), seg_threads(n), 0, STREAM>>>(g, P, recon, lambda, gamma, slot_bar);               \
       else                                                                                                      \
-        k_vjp_face<FLUX, SEGV, FO, KH><<<seg_blocks(n), seg_threads(n), 0, s>>>(g, P, recon, lambda, gamma,     \
-                                                                                slot_bar, far_bar);             \
+        k_vjp_face<FLUX, SEGV, FO, KH><<<seg_blocks(n), seg_threads(n), 0, STREAM>>>(g, P, recon, lambda,       \
+                                                                                     gamma, slot_bar, far_bar); \
     }                                                                                                           \
   }
-  MCFD_SEG(SEG_INTERIOR)
-  MCFD_SEG(SEG_PERIODIC)
-  MCFD_SEG(SEG_WALL)
-  MCFD_SEG(SEG_VIN)
-  MCFD_SEG(SEG_POUT)
-  MCFD_SEG(SEG_FAR)
+  const cudaStream_t b = fork ? w.side : s;
+  MCFD_SEG(SEG_FAR, b)
+  MCFD_SEG(SEG_WALL, b)
+  MCFD_SEG(SEG_PERIODIC, b)
+  MCFD_SEG(SEG_VIN, b)
+  MCFD_SEG(SEG_POUT, b)
+  MCFD_SEG(SEG_INTERIOR, s)
 #undef MCFD_SEG
+  if (fork) {
+    cudaEventRecord(w.join, w.side);
+    cudaStreamWaitEvent(s, w.join, 0);
+  }
 }
 
 }  // namespace
@@ -583,17 +601,17 @@ cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U
   const bool kh = cfg.reconstruction != MCFD_RECON_MUSCL_PARABOLIC;
   switch (cfg.flux) {
     case MCFD_FLUX_RUSANOV:
-      if (fo) face_segments<0, true, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else face_segments<0, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      if (fo) face_segments<0, true, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, w, s);
+      else face_segments<0, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, w, s);
       break;
     case MCFD_FLUX_HLLC:
-      if (fo) face_segments<1, true, true>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else if (kh) face_segments<1, false, true>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else face_segments<1, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      if (fo) face_segments<1, true, true>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, w, s);
+      else if (kh) face_segments<1, false, true>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, w, s);
+      else face_segments<1, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, w, s);
       break;
     default:
-      if (fo) face_segments<2, true, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
-      else face_segments<2, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, s);
+      if (fo) face_segments<2, true, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, w, s);
+      else face_segments<2, false, false>(g, P, recon, lambda, cfg.gamma, w.slot_bar, far_bar, w, s);
       break;
   }
   count_launch(2);

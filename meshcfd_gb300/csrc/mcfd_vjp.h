@@ -12,6 +12,10 @@ struct VjpWork {
   double* pbar = nullptr;      // primitive adjoints [C][4] (also per-cell scratch)
   double* ent_bar = nullptr;   // per gradient entry: share for the neighbour [E][4]
   double* partials = nullptr;  // reduction scratch [608 block sums + 8]
+  // the boundary face segments run on a second stream, concurrently with
+  // the interior faces (each face writes only its own two face-state slots)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 // P_in / recon_in: primitive and face states of U when the caller has them
