@@ -357,7 +357,8 @@ int mcfd_jvp(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const dou
 int mcfd_vjp(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* lambda, double* U_bar,
              double* far_bar, void* stream);
 /* mcfd_vjp at a state whose primitive P and (MUSCL) face states recon the
- * caller already has (from mcfd_explicit_step_record). */
+ * caller already has (from mcfd_explicit_step_record).  U may be NULL: the
+ * product needs only P and recon. */
 int mcfd_vjp_at(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* P, const double* recon,
                 const double* lambda, double* U_bar, double* far_bar, void* stream);
 /* Pressure force on the wall faces along (dir_x, dir_y): J = sum over wall

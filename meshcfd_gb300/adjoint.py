@@ -25,7 +25,7 @@ import ctypes as C
 import numpy as np
 import torch
 
-from .device import DeviceGeometry, _device_view, _stream_ptr, make_config
+from .device import DeviceGeometry, _stream_ptr, make_config
 
 
 class ResidualFunction(torch.autograd.Function):
@@ -117,11 +117,12 @@ class WallForceAdjoint:
         return float(J[0]), dJ
 
     # --------------------------------------------------------------- reverse
-    def _vjp(self, U, P, recon, lam, coef):
-        """W = R'(U)^T lam; the far-field-state gradient accumulates with
-        weight coef dt (dt of each far face's owner cell)."""
+    def _vjp(self, P, recon, lam, coef):
+        """W = R'(U)^T lam at the state with primitive P and face states
+        recon; the far-field-state gradient accumulates with weight coef dt
+        (dt of each far face's owner cell)."""
         lib = self.geom.lib
-        lib.check(lib.mcfd_vjp_at(self.geom.handle, C.byref(self.cfg_vjp), U.data_ptr(), P.data_ptr(),
+        lib.check(lib.mcfd_vjp_at(self.geom.handle, C.byref(self.cfg_vjp), None, P.data_ptr(),
                                   recon.data_ptr() if recon is not None else None, lam.data_ptr(),
                                   self.W.data_ptr(), self.far.data_ptr(), _stream_ptr()), "mcfd_vjp_at")
         if self.geom.n_far_field:
@@ -137,13 +138,11 @@ class WallForceAdjoint:
         return torch.addcmul(x, w, self.dt_col)
 
     def _replay(self, U):
-        """Advance U one step in place; returns the step's stage states
-        (U0, U1, U2) and, per stage, the primitive and face states the
-        residual was evaluated at (the reverse sweep's linearisation points,
-        copied during the step)."""
+        """Advance U one step in place; returns, per stage, the primitive and
+        face states the residual was evaluated at (the reverse sweep's
+        linearisation points, written during the step)."""
         g, lib, n = self.geom, self.geom.lib, self.geom.n_cells
         dev = g.device
-        U0 = U.clone()
         Ps = [torch.empty(n, 4, dtype=torch.float64, device=dev) for _ in range(3)]
         recons = ([torch.empty(int(g.info.n_limiter), 4, dtype=torch.float64, device=dev) for _ in range(3)]
                   if self.cfg.reconstruction != 0 else [None] * 3)
@@ -152,8 +151,7 @@ class WallForceAdjoint:
         lib.check(lib.mcfd_explicit_step_record(g.handle, C.byref(self.cfg), 2, U.data_ptr(), self.dt_dev.data_ptr(),
                                                 int(self.per_cell), p_ptrs, r_ptrs, 3, _stream_ptr()),
                   "mcfd_explicit_step_record")
-        U1, U2 = (_device_view(lib.mcfd_geom_stage_state(g.handle, k), (n, 4), dev).clone() for k in (0, 1))
-        return (U0, U1, U2), Ps, recons
+        return Ps, recons
 
     def backward(self, lam_final: torch.Tensor) -> torch.Tensor:
         """Adjoint of the initial state; the far-field-state gradient per
@@ -168,12 +166,12 @@ class WallForceAdjoint:
             end = min(start + self.k, self.steps)
             U = self.checkpoints[seg].clone()
             records = [self._replay(U) for _ in range(start, end)]
-            for (U0, U1, U2), Ps, recons in reversed(records):
-                w = self._vjp(U2, Ps[2], recons[2], lam, 2.0 / 3.0)
+            for Ps, recons in reversed(records):
+                w = self._vjp(Ps[2], recons[2], lam, 2.0 / 3.0)
                 lam2 = self._plus_dt(lam, w).mul_(2.0 / 3.0)
-                w = self._vjp(U1, Ps[1], recons[1], lam2, 0.25)
+                w = self._vjp(Ps[1], recons[1], lam2, 0.25)
                 lam1 = self._plus_dt(lam2, w).mul_(0.25)
-                w = self._vjp(U0, Ps[0], recons[0], lam1, 1.0)
+                w = self._vjp(Ps[0], recons[0], lam1, 1.0)
                 new = self._plus_dt(lam1, w)
                 new.add_(lam, alpha=1.0 / 3.0).add_(lam2, alpha=0.75)
                 lam = new

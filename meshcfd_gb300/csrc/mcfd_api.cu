@@ -1252,7 +1252,7 @@ int mcfd_vjp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
 
 int mcfd_vjp_at(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double* P, const double* recon,
                 const double* lambda, double* U_bar, double* far_bar, void* stream) {
-  if (!h || !U || !P || !lambda || !U_bar) return MCFD_E_ARG;
+  if (!h || !P || !lambda || !U_bar) return MCFD_E_ARG;  // U is not needed once P is given
   int c = check_cfg(cfg);
   if (c) return c;
   if (cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC || h->g.n_bc_patches > 0 ||

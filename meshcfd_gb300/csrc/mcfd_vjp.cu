@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
 }
 
 template <bool FO>
-__global__ void __launch_bounds__(kBlock) k_vjp_collect(DevGeom g, const double* __restrict__ U,
+__global__ void __launch_bounds__(kBlock) k_vjp_collect(DevGeom g, const double* __restrict__ P,
                                                         const double* __restrict__ pbar,
                                                         const double* __restrict__ ent_bar, double gamma,
                                                         double* __restrict__ ubar) {
@@ -485,8 +485,8 @@ __global__ void __launch_bounds__(kBlock) k_vjp_collect(DevGeom g, const double*
   //   rho_bar = rho_b - (u u_b + v v_b) / rho + (gamma - 1) (u^2 + v^2) / 2 p_b
   //   m_bar = u_b / rho - (gamma - 1) u p_b,  n_bar = v_b / rho - (gamma - 1) v p_b
   //   E_bar = (gamma - 1) p_b
-  const St4 u = ld4(U + 4 * (size_t)c);
-  const double inv = div_rn(1.0, u.a), vx = u.b * inv, vy = u.c * inv;
+  const St4 q = ld4(P + 4 * (size_t)c);  // the primitive of U: rho, u, v, p
+  const double inv = div_rn(1.0, q.a), vx = q.b, vy = q.c;
   const double gp = (gamma - 1.0) * pb.d;
   const double ub = pb.b * inv, vb = pb.c * inv;
   const St4 out{pb.a - (vx * ub + vy * vb) + 0.5 * gp * (vx * vx + vy * vy), ub - gp * vx, vb - gp * vy, gp};
@@ -618,7 +618,7 @@ cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U
   const double ax = cfg.acceleration_x, ay = cfg.acceleration_y;
   if (fo) {
     k_vjp_cell<0, true><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar);
-    k_vjp_collect<true><<<blocks_for(C), kBlock, 0, s>>>(g, U, w.pbar, w.ent_bar, cfg.gamma, ubar);
+    k_vjp_collect<true><<<blocks_for(C), kBlock, 0, s>>>(g, P, w.pbar, w.ent_bar, cfg.gamma, ubar);
   } else {
     switch (cfg.limiter) {
       case 0: k_vjp_cell<0, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
@@ -626,7 +626,7 @@ cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U
       case 2: k_vjp_cell<2, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
       default: k_vjp_cell<3, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
     }
-    k_vjp_collect<false><<<blocks_for(C), kBlock, 0, s>>>(g, U, w.pbar, w.ent_bar, cfg.gamma, ubar);
+    k_vjp_collect<false><<<blocks_for(C), kBlock, 0, s>>>(g, P, w.pbar, w.ent_bar, cfg.gamma, ubar);
   }
   return cudaGetLastError();
 }

@@ -236,3 +236,7 @@ def test_recorded_step_and_vjp_at_match_plain_calls(cuda_device):
                               lam.data_ptr(), b.data_ptr(), None, stream) == 0
     dg.check_status()
     assert torch.equal(a, b)
+    c = torch.empty_like(lam)  # the recorded primitive suffices: no conservative state
+    assert dg.lib.mcfd_vjp_at(dg.handle, C.byref(cfg), None, Ps[0].data_ptr(), Rs[0].data_ptr(),
+                              lam.data_ptr(), c.data_ptr(), None, stream) == 0
+    assert torch.equal(a, c)
