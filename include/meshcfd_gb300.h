@@ -448,6 +448,11 @@ int mcfd_residual_sumsq_noalloc(const double* R, int64_t n_cells, double* sums, 
  */
 int mcfd_ieee_div_sqrt(const double* a, const double* b, int64_t n, double* quotient, double* root,
                        void* stream);
+/* Element-wise IEEE binary64 product on the integer pipe, as the
+ * exact-arithmetic kernels evaluate part of their products:
+ * product[i] = a[i] * b[i], bit-identical to the FP64 unit.  Device arrays of
+ * n doubles.  No reference counterpart (verification). */
+int mcfd_ieee_mul(const double* a, const double* b, int64_t n, double* product, void* stream);
 
 /* ---- host helpers (no GPU needed) ---- */
 

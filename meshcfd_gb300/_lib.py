@@ -122,6 +122,7 @@ SIGNATURES = {
     "mcfd_batch_time_steps": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
     "mcfd_residual_sumsq_noalloc": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "mcfd_ieee_div_sqrt": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "mcfd_ieee_mul": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp]),
     "mcfd_host_cell_geometry": (c_i32, [c_i64, P_i64, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
     "mcfd_host_face_geometry": (c_i32, [c_i64, P_i64, P_dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
 }

@@ -1,5 +1,5 @@
 // Variant-independent kernels: the residual sum of squares, the launch
-// counter and the element-wise division / square root entry point.  Compiled
+// counter and the element-wise division / square root / product entry points.  Compiled
 // with -fmad=false (plain additions in a fixed tree).
 #include "mcfd_device.cuh"
 #include "mcfd_internal.h"
@@ -114,7 +114,24 @@ __global__ void __launch_bounds__(kBlock) k_ieee_div_sqrt(long long n, const dou
   }
 }
 
+__global__ void __launch_bounds__(kBlock) k_ieee_mul(long long n, const double* __restrict__ a,
+                                                     const double* __restrict__ b, double* __restrict__ product) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    product[i] = mul_rn(a[i], b[i]);
+}
+
 }  // namespace mcfd
+
+extern "C" int mcfd_ieee_mul(const double* a, const double* b, int64_t n, double* product, void* stream) {
+  if (n < 0 || (n > 0 && (!a || !b || !product))) return MCFD_E_ARG;
+  if (n == 0) return MCFD_OK;
+  const long long blocks = (n + mcfd::kBlock - 1) / mcfd::kBlock;
+  mcfd::count_launch(1);
+  mcfd::k_ieee_mul<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), mcfd::kBlock, 0,
+                     static_cast<cudaStream_t>(stream)>>>(n, a, b, product);
+  return cudaGetLastError() == cudaSuccess ? MCFD_OK : MCFD_E_CUDA;
+}
 
 extern "C" int mcfd_ieee_div_sqrt(const double* a, const double* b, int64_t n, double* quotient,
                                   double* root, void* stream) {

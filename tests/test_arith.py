@@ -1,7 +1,8 @@
-"""The integer-pipe IEEE division and square root that the residual kernels
-use in place of the FP64 unit's: bit-identical results on the host (the
-header compiled as plain C++ against the host's IEEE arithmetic) and on the
-GPU (through mcfd_ieee_div_sqrt against the FP64 unit's `/` and `sqrt`)."""
+"""The integer-pipe IEEE division, square root and product that the residual
+kernels use in place of the FP64 unit's: bit-identical results on the host
+(the header compiled as plain C++ against the host's IEEE arithmetic) and on
+the GPU (through mcfd_ieee_div_sqrt / mcfd_ieee_mul against the FP64 unit's
+`/`, `sqrt` and `*`)."""
 
 import shutil
 import subprocess
@@ -82,6 +83,28 @@ def test_gpu_division_and_root_match_the_fp64_unit(cuda_device):
         # and against numpy's (host IEEE) results, non-NaN entries
         with np.errstate(all="ignore"):
             assert _same_bits(qn, a_np / b_np).all()
+
+
+@pytest.mark.gpu
+def test_gpu_product_matches_the_fp64_unit(cuda_device):
+    import torch
+    from meshcfd_gb300 import _lib
+
+    lib = _lib.native()
+    stream = torch.cuda.current_stream().cuda_stream
+    for seed in (4, 5, 6):
+        a_np, b_np = _operands(1 << 20, seed)
+        a = torch.as_tensor(a_np, device=cuda_device)
+        b = torch.as_tensor(b_np, device=cuda_device)
+        p = torch.empty_like(a)
+        assert lib.mcfd_ieee_mul(a.data_ptr(), b.data_ptr(), a.numel(), p.data_ptr(), stream) == 0
+        ref = (a * b).cpu().numpy()
+        torch.cuda.synchronize()
+        ok = _same_bits(p.cpu().numpy(), ref)
+        assert ok.all(), (a_np[~ok][:3], b_np[~ok][:3])
+        with np.errstate(all="ignore"):
+            assert _same_bits(ref, a_np * b_np).all()
+    assert lib.mcfd_ieee_mul(None, None, 4, None, stream) == 1
 
 
 @pytest.mark.gpu
