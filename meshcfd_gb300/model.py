@@ -8,6 +8,8 @@ multi-million-cell meshes cheap to build.
 Reference interfaces mirrored:
   * ``FiniteVolumeMesh``      model.py:60-74
   * ``MeshPatch``             model.py:37-41
+  * ``BoundaryCurve``         model.py:44-49
+  * ``RefinementRecord``      model.py:52-57
   * ``BoundaryCondition``     model.py:77-84
   * ``PeriodicBoundaryPair``  model.py:87-92
   * ``NumericalSettings``     model.py:95-129
@@ -57,6 +59,22 @@ class MeshPatch:
     id: int
     name: str
     face_ids: Any
+
+
+@dataclass(frozen=True)
+class BoundaryCurve:
+    geometry: dict
+    start_parameter: float
+    end_parameter: float
+    patch_id: int
+
+
+@dataclass(frozen=True)
+class RefinementRecord:
+    parent_id: str
+    child_ids: tuple
+    vertices: tuple
+    level: int
 
 
 @dataclass

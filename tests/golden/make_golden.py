@@ -15,7 +15,10 @@ reference's outputs, so the tests can run without the reference:
 * parabolic_<case>.npz — ``_residual`` with MUSCL parabolic reconstruction for
   every flux x limiter (with and without a body force) and the outputs of
   ``_parabolic_reconstruction`` per limiter, on a geometry built with the
-  two-ring stencil.
+  two-ring stencil;
+* meshio.json          — the reference's MeshCAD JSON reader (io/mesh_io.py) on
+  valid inputs (its cell loops and re-serialisation) and its error message
+  for each mutation in ``MESH_MUTATIONS``  (mode ``meshio``).
 """
 
 from __future__ import annotations
@@ -438,7 +441,270 @@ def implicit_fixture(name, case, primitive, settings, steps, ref):
     print("implicit", name, n, "cells,", result.steps, "steps, t =", result.time)
 
 
+# ------------------------------------------------------------ MeshCAD JSON
+
+def meshio_square():
+    """The one-cell unit square of the reference's reader test
+    (tests/test_mesh_io.py:6-28)."""
+    return {
+        "format": "meshcad-mesh", "version": 1, "dimension": 2,
+        "nodes": {"coordinates": [[0, 0], [1, 0], [1, 1], [0, 1]]},
+        "faces": {"nodes": [[0, 1], [1, 2], [2, 3], [3, 0]], "owner": [0, 0, 0, 0], "patch": [0, 1, 2, 3],
+                  "neighbour": [-1, -1, -1, -1]},
+        "cells": {"faces": [[0, 1, 2, 3]], "face_signs": [[1, 1, 1, 1]]},
+        "patches": [{"id": 0, "name": "bottom", "faces": [0]}, {"id": 1, "name": "right", "faces": [1]},
+                    {"id": 2, "name": "top", "faces": [2]}, {"id": 3, "name": "left", "faces": [3]}],
+    }
+
+
+def meshio_pair():
+    """Two triangles of the unit square sharing the diagonal (face 2)."""
+    return {
+        "format": "meshcad-mesh", "version": 1, "dimension": 2,
+        "nodes": {"coordinates": [[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]]},
+        "faces": {"nodes": [[0, 1], [1, 2], [2, 0], [2, 3], [3, 0]], "owner": [0, 0, 0, 1, 1],
+                  "patch": [0, 1, -1, 2, 3], "neighbour": [-1, -1, 1, -1, -1]},
+        "cells": {"faces": [[0, 1, 2], [2, 3, 4]], "face_signs": [[1, 1, 1], [-1, 1, 1]]},
+        "patches": [{"id": 0, "name": "bottom", "faces": [0]}, {"id": 1, "name": "right", "faces": [1]},
+                    {"id": 2, "name": "top", "faces": [3]}, {"id": 3, "name": "left", "faces": [4]}],
+    }
+
+
+def meshio_pair_with_metadata():
+    """meshio_pair with line / spline / spline-segment boundary curves and
+    refinement metadata."""
+    d = meshio_pair()
+    d["boundary_curves"] = [
+        {"geometry": {"type": "line", "start": [0.0, 0.0], "end": [1.0, 0.0]}, "parameters": [0.0, 1.0],
+         "patch_id": 0},
+        {"geometry": {"type": "spline", "points": [[1.0, 0.0], [1.1, 0.5], [1.0, 1.0]]}, "parameters": [0.0, 1.0],
+         "patch_id": 1},
+        None,
+        {"geometry": {"type": "spline_segment", "points": [[2.0, 1.0], [1.0, 1.0], [0.0, 1.0], [-1.0, 1.0]],
+                      "start_t": 1.0 / 3.0, "end_t": 2.0 / 3.0}, "parameters": [0.0, 1.0], "patch_id": 2},
+        {"geometry": {"type": "line", "start": [0.0, 1.0], "end": [0.0, 0.0]}, "parameters": [0.0, 1.0],
+         "patch_id": 3},
+    ]
+    d["refinement"] = {"cell_ids": ["c0", "c1"], "cell_levels": [1, 1],
+                       "records": [{"parent_id": "p", "child_ids": ["c0", "c1"],
+                                    "vertices": [[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]], "level": 0}]}
+    return d
+
+
+def meshio_figure8(face_order=(0, 1, 2, 3, 4, 5)):
+    """One cell made of two triangles that share node 0 (node 0 starts two of
+    its edges, so the loop follows the reference's first-match rule)."""
+    coords = [[0.0, 0.0], [1.0, 0.0], [0.5, 1.0], [-1.0, 0.0], [-0.5, -1.0]]
+    nodes = [[0, 1], [1, 2], [2, 0], [0, 3], [3, 4], [4, 0]]
+    return {
+        "format": "meshcad-mesh", "version": 1, "dimension": 2,
+        "nodes": {"coordinates": coords},
+        "faces": {"nodes": nodes, "owner": [0] * 6, "patch": [0] * 6, "neighbour": [-1] * 6},
+        "cells": {"faces": [list(face_order)], "face_signs": [[1] * 6]},
+        "patches": [{"id": 0, "name": "outer", "faces": list(range(6))}],
+    }
+
+
+def _arc_curve():
+    return {"geometry": {"type": "arc", "center": [0.5, 0.5], "radius": 2 ** 0.5 / 2,
+                         "start_angle": -3 * 3.141592653589793 / 4, "end_angle": -3.141592653589793 / 4},
+            "parameters": [0.0, 1.0], "patch_id": 0}
+
+
+def _set(path, value):
+    def apply(d):
+        target = d
+        for key in path[:-1]:
+            target = target[key]
+        target[path[-1]] = value
+    return apply
+
+
+def _delete(path):
+    def apply(d):
+        target = d
+        for key in path[:-1]:
+            target = target[key]
+        del target[path[-1]]
+    return apply
+
+
+def _append(path, value):
+    def apply(d):
+        target = d
+        for key in path:
+            target = target[key]
+        target.append(value)
+    return apply
+
+
+def _curves(face, curve, n=4):
+    def apply(d):
+        curves = [None] * n
+        curves[face] = curve
+        d["boundary_curves"] = curves
+    return apply
+
+
+def _curve_geometry_set(key, value, base=None):
+    def apply(d):
+        curve = base() if base else _arc_curve()
+        if key in ("parameters", "patch_id"):
+            curve[key] = value
+        else:
+            curve["geometry"][key] = value
+        d["boundary_curves"] = [curve, None, None, None]
+    return apply
+
+
+def _line_curve():
+    return {"geometry": {"type": "line", "start": [0.0, 0.0], "end": [1.0, 0.0]}, "parameters": [0.0, 1.0],
+            "patch_id": 0}
+
+
+def _spline_segment_curve():
+    return {"geometry": {"type": "spline_segment", "points": [[-1.0, 0.0], [0.0, 0.0], [1.0, 0.0], [2.0, 0.0]],
+                         "start_t": 1.0 / 3.0, "end_t": 2.0 / 3.0}, "parameters": [0.0, 1.0], "patch_id": 0}
+
+
+_REC = {"parent_id": "p", "child_ids": ["a", "b"], "vertices": [[0, 0], [1, 0], [0, 1]], "level": 0}
+
+# (name, base mesh, mutation): every branch of the reader's validation
+MESH_MUTATIONS = [
+    ("format", "square", _set(["format"], "mesh")),
+    ("version", "square", _set(["version"], 2)),
+    ("dimension", "square", _set(["dimension"], 3)),
+    ("missing_nodes", "square", _delete(["nodes"])),
+    ("nodes_not_object", "square", _set(["nodes"], [])),
+    ("missing_patches", "square", _delete(["patches"])),
+    ("no_nodes", "square", _set(["nodes", "coordinates"], [])),
+    ("node_shape", "square", _set(["nodes", "coordinates", 1], [1])),
+    ("node_text", "square", _set(["nodes", "coordinates", 1], [1, "x"])),
+    ("node_nan", "square", _set(["nodes", "coordinates", 0, 0], float("nan"))),
+    ("node_inf", "square", _set(["nodes", "coordinates", 2, 1], float("inf"))),
+    ("no_faces", "square", _set(["faces", "nodes"], [])),
+    ("face_shape", "square", _set(["faces", "nodes", 1], [1, 2, 3])),
+    ("face_float", "square", _set(["faces", "nodes", 1], [1, 2.0])),
+    ("face_bool", "square", _set(["faces", "nodes", 1], [True, 2])),
+    ("face_same_nodes", "square", _set(["faces", "nodes", 1], [1, 1])),
+    ("face_node_range", "square", _set(["faces", "nodes", 1], [1, 9])),
+    ("face_node_negative", "square", _set(["faces", "nodes", 2], [-1, 2])),
+    ("owners_not_list", "square", _set(["faces", "owner"], 3)),
+    ("owner_float", "square", _set(["faces", "owner", 0], 0.0)),
+    ("neighbour_bool", "square", _set(["faces", "neighbour", 0], False)),
+    ("patch_id_text", "square", _set(["faces", "patch", 0], "0")),
+    ("face_lengths", "square", _append(["faces", "owner"], 0)),
+    ("patches_not_list", "square", _set(["patches"], {})),
+    ("patch_not_object", "square", _set(["patches", 0], 5)),
+    ("patch_id_missing", "square", _delete(["patches", 0, "id"])),
+    ("patch_name_blank", "square", _set(["patches", 0, "name"], " ")),
+    ("patch_duplicate_id", "square", _set(["patches", 1, "id"], 0)),
+    ("patch_duplicate_name", "square", _set(["patches", 1, "name"], "bottom")),
+    ("patch_faces_not_list", "square", _set(["patches", 0, "faces"], 0)),
+    ("patch_face_range", "square", _set(["patches", 0, "faces"], [9])),
+    ("cells_not_list", "square", _set(["cells", "faces"], {})),
+    ("cells_empty", "square", lambda d: d["cells"].update({"faces": [], "face_signs": []})),
+    ("cells_signs_length", "square", _append(["cells", "face_signs"], [1, 1, 1])),
+    ("unknown_patch", "square", _set(["faces", "patch", 0], 7)),
+    ("owner_range", "square", _set(["faces", "owner", 0], 5)),
+    ("neighbour_is_owner", "pair", _set(["faces", "neighbour", 2], 0)),
+    ("neighbour_range", "pair", _set(["faces", "neighbour", 2], 4)),
+    ("boundary_inconsistent", "pair", _set(["faces", "patch", 2], 0)),
+    ("cell_faces_not_list", "square", _set(["cells", "faces", 0], 5)),
+    ("cell_face_float", "square", _set(["cells", "faces", 0, 0], 0.0)),
+    ("cell_two_faces", "square", lambda d: d["cells"].update({"faces": [[0, 1]], "face_signs": [[1, 1]]})),
+    ("cell_face_range", "square", _set(["cells", "faces", 0, 0], 9)),
+    ("cell_sign", "square", _set(["cells", "face_signs", 0, 0], 2)),
+    ("open_cell", "square", _set(["cells", "face_signs", 0, 3], -1)),
+    ("second_cell_open", "pair", _set(["cells", "face_signs", 1, 0], 1)),
+    ("patch_unrelated_face", "square", _set(["patches", 0, "faces"], [1])),
+    ("patch_face_twice", "square", _set(["patches", 0, "faces"], [0, 0])),
+    ("patch_membership", "square", _set(["patches", 0, "faces"], [])),
+    ("refinement_not_object", "square", _set(["refinement"], [])),
+    ("refinement_ids_not_list", "square", _set(["refinement"], {"cell_ids": "a"})),
+    ("refinement_id_empty", "square", _set(["refinement"], {"cell_ids": [""]})),
+    ("refinement_level_float", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [0.5]})),
+    ("refinement_lengths", "square", _set(["refinement"], {"cell_ids": ["a", "b"], "cell_levels": [0, 0]})),
+    ("refinement_negative", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [-1]})),
+    ("records_not_list", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [0], "records": {}})),
+    ("records_need_ids", "square", _set(["refinement"], {"records": [{}]})),
+    ("record_not_object", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [0], "records": [5]})),
+    ("record_level_float", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [0],
+                                                           "records": [dict(_REC, level=0.5)]})),
+    ("record_one_child", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [0],
+                                                         "records": [dict(_REC, child_ids=["a"])]})),
+    ("record_vertex_shape", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [0],
+                                                            "records": [dict(_REC, vertices=[[0, 0], [1, 0], [0]])]})),
+    ("record_vertex_nan", "square", _set(["refinement"], {"cell_ids": ["a"], "cell_levels": [0],
+                                                          "records": [dict(_REC, vertices=[[0, 0], [1, 0], [float("nan"), 1]])]})),
+    ("curves_length", "square", _set(["boundary_curves"], [None])),
+    ("curve_not_object", "square", _set(["boundary_curves"], [5, None, None, None])),
+    ("curve_on_internal_face", "pair", _curves(2, _line_curve(), 5)),
+    ("curve_patch", "square", _curve_geometry_set("patch_id", 1)),
+    ("curve_one_parameter", "square", _curve_geometry_set("parameters", [0.0])),
+    ("curve_parameter_range", "square", _curve_geometry_set("parameters", [0.0, 2.0])),
+    ("curve_equal_parameters", "square", _curve_geometry_set("parameters", [0.5, 0.5])),
+    ("curve_type", "square", _curve_geometry_set("type", "circle")),
+    ("curve_arc_center", "square", _curve_geometry_set("center", [0])),
+    ("curve_arc_radius", "square", _curve_geometry_set("radius", -1.0)),
+    ("curve_arc_angle", "square", _curve_geometry_set("start_angle", "x")),
+    ("curve_line_start", "square", _curve_geometry_set("start", [0.0], _line_curve)),
+    ("curve_spline_points", "square", _curve_geometry_set("points", [[0.0, 0.0]], _spline_segment_curve)),
+    ("curve_spline_parameters", "square", _curve_geometry_set("end_t", 0.2, _spline_segment_curve)),
+    ("curve_spline_offset", "square", _curve_geometry_set("start_offset", [0.0], _spline_segment_curve)),
+    ("curve_mismatch", "square", _curve_geometry_set("parameters", [0.0, 0.5])),
+]
+
+MESHIO_BASES = {"square": meshio_square, "pair": meshio_pair}
+
+
+def meshio_valid_inputs():
+    from meshcfd_gb300 import mesh_io
+
+    square_arc = meshio_square()
+    square_arc["boundary_curves"] = [_arc_curve(), None, None, None]
+    vortex, _ = vortex_case(12, seed=0, jitter=0.15, split="half")
+    return {
+        "square": meshio_square(),
+        "square_arc": square_arc,
+        "pair": meshio_pair(),
+        "pair_metadata": meshio_pair_with_metadata(),
+        "figure8": meshio_figure8(),
+        "figure8_scrambled": meshio_figure8((3, 0, 4, 1, 5, 2)),
+        "vortex12": mesh_io.mesh_to_dict(vortex.mesh),
+    }
+
+
+def meshio_main():
+    """tests/golden/meshio.json: for each valid input the reference reader's
+    cell loops and re-serialisation; for each mutation of a valid input the
+    reference reader's error message."""
+    import copy
+    import json
+
+    from reference_shim import import_reference_mesh_io
+
+    ref = import_reference_mesh_io()
+    valid = {}
+    for name, data in meshio_valid_inputs().items():
+        mesh = ref.mesh_from_dict(copy.deepcopy(data))
+        valid[name] = {"data": data, "cells": [list(c) for c in mesh.cells], "to_dict": ref.mesh_to_dict(mesh)}
+    errors = {}
+    for name, base, mutate in MESH_MUTATIONS:
+        data = MESHIO_BASES[base]()
+        mutate(data)
+        try:
+            ref.mesh_from_dict(data)
+        except ref.MeshImportError as error:
+            errors[name] = str(error)
+        else:
+            raise RuntimeError(f"mutation {name} was accepted by the reference")
+    (HERE / "meshio.json").write_text(json.dumps({"valid": valid, "errors": errors}, allow_nan=True))
+
+
 def main(only=None):
+    if only == "meshio":
+        return meshio_main()
     ref = import_reference()
     if only == "parabolic":
         return parabolic_main(ref)

@@ -38,6 +38,14 @@ def import_reference():
     return types.SimpleNamespace(solver=solver, euler=euler, model=model, kernels=_kernels)
 
 
+def import_reference_mesh_io():
+    """Return the reference's ``meshcfd.io.mesh_io`` module."""
+    import_reference()
+    from meshcfd.io import mesh_io  # noqa: E402
+
+    return mesh_io
+
+
 def reference_case(case, ref):
     """Rebuild one of our cases with the reference's own dataclasses."""
     from meshcfd_gb300.meshes import to_reference_mesh
