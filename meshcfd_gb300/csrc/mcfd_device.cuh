@@ -102,20 +102,38 @@ __device__ __forceinline__ St4 cons_to_prim(const St4& U, double gamma, bool* ok
   return P;
 }
 
+// Products of the exact flux functions that a translation unit may evaluate
+// on the integer pipe (mul_rn, the same IEEE result): MCFD_FLUX_INT_MUL is a
+// mask of call sites -- 1 normal velocities, sound speeds and wave terms,
+// 2 the physical flux, 4 the HLLC star state -- set by a stage-kernel unit
+// before it includes this header; 0 (the FP64 unit) everywhere else.
+#ifndef MCFD_FLUX_INT_MUL
+#define MCFD_FLUX_INT_MUL 0
+#endif
+enum FluxMulSite { FMUL_WAVES = 1, FMUL_PHYSICAL = 2, FMUL_STAR = 4 };
+
+template <int SITE>
+__device__ __forceinline__ double fmul(double a, double b) {
+  if constexpr ((MCFD_FLUX_INT_MUL & SITE) != 0) return mul_rn(a, b);
+  else return a * b;
+}
+
 // euler.physical_flux (euler.py:43-57): flux and conservative state, with
 // the normal velocity un = ux nx + uy ny given (the callers compute it too).
 __device__ __forceinline__ void physical_flux_un(const St4& q, double un, double nx, double ny, double gamma,
                                                  double F[4], double U[4]) {
+  constexpr int S = FMUL_PHYSICAL;
   double rho = q.a, ux = q.b, uy = q.c, p = q.d;
-  double energy = div_rn(p, gamma - 1.0) + (0.5 * rho) * (ux * ux + uy * uy);
+  double energy = div_rn(p, gamma - 1.0) + fmul<S>(fmul<S>(0.5, rho), fmul<S>(ux, ux) + fmul<S>(uy, uy));
+  const double mx = fmul<S>(rho, ux), my = fmul<S>(rho, uy);
   U[0] = rho;
-  U[1] = rho * ux;
-  U[2] = rho * uy;
+  U[1] = mx;
+  U[2] = my;
   U[3] = energy;
-  F[0] = rho * un;
-  F[1] = (rho * ux) * un + p * nx;
-  F[2] = (rho * uy) * un + p * ny;
-  F[3] = (energy + p) * un;
+  F[0] = fmul<S>(rho, un);
+  F[1] = fmul<S>(mx, un) + fmul<S>(p, nx);
+  F[2] = fmul<S>(my, un) + fmul<S>(p, ny);
+  F[3] = fmul<S>(energy + p, un);
 }
 
 __device__ __forceinline__ void physical_flux(const St4& q, double nx, double ny, double gamma,
@@ -124,7 +142,7 @@ __device__ __forceinline__ void physical_flux(const St4& q, double nx, double ny
 }
 
 __device__ __forceinline__ double sound_speed(double rho, double p, double gamma) {
-  return sqrt_rn(div_rn(gamma * p, rho));
+  return sqrt_rn(div_rn(fmul<FMUL_WAVES>(gamma, p), rho));
 }
 
 // euler._rusanov_flux (euler.py:80-93).
@@ -155,16 +173,18 @@ __device__ __forceinline__ void rusanov_flux(const St4& L, const St4& R, double 
 template <bool KERNEL_BRANCHES>
 __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx, double ny,
                                           double gamma, double out[4]) {
+  constexpr int W = FMUL_WAVES, T = FMUL_STAR;
   double rl = L.a, pl = L.d, rr = R.a, pr = R.d;
-  double unl = L.b * nx + L.c * ny;
-  double unr = R.b * nx + R.c * ny;
+  double unl = fmul<W>(L.b, nx) + fmul<W>(L.c, ny);
+  double unr = fmul<W>(R.b, nx) + fmul<W>(R.c, ny);
   double cl = sound_speed(rl, pl, gamma);
   double cr = sound_speed(rr, pr, gamma);
   double wl = py_min(unl - cl, unr - cr);
   double wr = py_max(unl + cl, unr + cr);
-  double den = rl * (wl - unl) - rr * (wr - unr);
+  const double dl = wl - unl, dr = wr - unr;
+  double den = fmul<W>(rl, dl) - fmul<W>(rr, dr);
   if (!icmp::abs_gt(den, 1e-14)) den = with_sign_of(1e-14, den);
-  double contact = div_rn((pr - pl) + (rl * unl) * (wl - unl) - (rr * unr) * (wr - unr), den);
+  double contact = div_rn((pr - pl) + fmul<W>(fmul<W>(rl, unl), dl) - fmul<W>(fmul<W>(rr, unr), dr), den);
 
   int branch;  // 0: F_L, 1: F*_L, 2: F*_R, 3: F_R
   if (KERNEL_BRANCHES) {
@@ -188,13 +208,14 @@ __device__ __forceinline__ bool hllc_flux(const St4& L, const St4& R, double nx,
   } else {
     double wave = left ? wl : wr;
     double rho = q.a, pressure = q.d;
-    double factor = div_rn(rho * (wave - un), wave - contact);
-    double sux = q.b + (contact - un) * nx;
-    double suy = q.c + (contact - un) * ny;
-    double se = factor * (div_rn(U[3], rho) + (contact - un) * (contact + div_rn(pressure, rho * (wave - un))));
-    double star[4] = {factor, factor * sux, factor * suy, se};
+    const double m = fmul<T>(rho, wave - un), cu = contact - un;
+    double factor = div_rn(m, wave - contact);
+    double sux = q.b + fmul<T>(cu, nx);
+    double suy = q.c + fmul<T>(cu, ny);
+    double se = fmul<T>(factor, div_rn(U[3], rho) + fmul<T>(cu, contact + div_rn(pressure, m)));
+    double star[4] = {factor, fmul<T>(factor, sux), fmul<T>(factor, suy), se};
 #pragma unroll
-    for (int k = 0; k < 4; ++k) out[k] = F[k] + wave * (star[k] - U[k]);
+    for (int k = 0; k < 4; ++k) out[k] = F[k] + fmul<T>(wave, star[k] - U[k]);
   }
   if (!KERNEL_BRANCHES) {
     return icmp::finite(out[0]) && icmp::finite(out[1]) && icmp::finite(out[2]) && icmp::finite(out[3]);

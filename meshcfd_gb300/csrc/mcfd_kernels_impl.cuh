@@ -24,12 +24,19 @@
 // check, stage combination, primitive recovery of the new stage state).
 // There are no atomics on the data path: the face->cell scatter of the
 // reference is a deterministic CSR gather.
-#include "mcfd_device.cuh"
-#include "mcfd_internal.h"
-
 #ifndef MCFD_FAST
 #error "define MCFD_FAST (0 or 1) and MCFD_VARIANT before including this file"
 #endif
+
+// Flux products on the integer pipe (mcfd_device.cuh): the HLLC star state in
+// the exact-arithmetic variants (+1.8 % on the 1024^2 vortex step; adding a
+// second site group lost), none in the fma variant (its products contract).
+#if !defined(MCFD_FLUX_INT_MUL) && MCFD_FAST != 2
+#define MCFD_FLUX_INT_MUL 4
+#endif
+
+#include "mcfd_device.cuh"
+#include "mcfd_internal.h"
 
 namespace mcfd {
 namespace MCFD_VARIANT {
