@@ -63,8 +63,8 @@ __device__ __forceinline__ St4 interior_state(const DevGeom& g, const double* P,
 // outgoing invariant at Mach m: a0 / sqrt(1 + (gamma-1)/2 m^2) (dn m + 2/(gamma-1))
 __device__ __forceinline__ double invariant_at(double m, double dn, double a0, double gamma) {
   const double ratio = 1.0 + 0.5 * (gamma - 1.0) * (m * m);
-  const double sound = a0 / sqrt(ratio);
-  return sound * (dn * m + 2.0 / (gamma - 1.0));
+  const double sound = div_rn(a0, sqrt_rn(ratio));
+  return sound * (dn * m + div_rn(2.0, gamma - 1.0));
 }
 
 __device__ void pressure_inlet(const DevGeom& g, const double* P, const double* recon, double gamma, double R,
@@ -73,7 +73,7 @@ __device__ void pressure_inlet(const DevGeom& g, const double* P, const double* 
   const int j0 = g.bc_ptr[patch], j1 = g.bc_ptr[patch + 1];
   const double* v = g.bc_values + 4 * (size_t)patch;
   const double pt = v[0], tt = v[1], dx = v[2], dy = v[3];
-  const double a0 = sqrt(gamma * R * tt);
+  const double a0 = sqrt_rn(gamma * R * tt);
   for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     const int f = base + j;
     const St4 q = interior_state(g, P, recon, f);
@@ -81,12 +81,12 @@ __device__ void pressure_inlet(const DevGeom& g, const double* P, const double* 
     const double dn = g.bc_dn[j];
     int bits = 0;
     if (dn >= -1e-12) bits |= MCFD_S_PIN_DIRECTION;
-    const double c = sqrt(gamma * q.d / q.a);
+    const double c = sqrt_rn(div_rn(gamma * q.d, q.a));
     const double un = q.b * n.x + q.c * n.y;
-    const double mach_in = un / c;
+    const double mach_in = div_rn(un, c);
     if (mach_in >= 1.0) bits |= MCFD_S_PIN_SUPERSONIC_OUT;
     if (mach_in <= -1.0) bits |= MCFD_S_PIN_SUPERSONIC_IN;
-    const double outgoing = un + 2.0 * c / (gamma - 1.0);
+    const double outgoing = un + div_rn(2.0 * c, gamma - 1.0);
     if (!bits) {
       const double lo_v = invariant_at(0.0, dn, a0, gamma), hi_v = invariant_at(1.0, dn, a0, gamma);
       if (!(hi_v <= outgoing && outgoing <= lo_v)) bits |= MCFD_S_PIN_INCOMPATIBLE;
@@ -100,10 +100,10 @@ __device__ void pressure_inlet(const DevGeom& g, const double* P, const double* 
         else high = mid;
       }
       const double m = 0.5 * (low + high);
-      const double t = tt / (1.0 + 0.5 * (gamma - 1.0) * (m * m));
-      const double p = pt * pow(t / tt, gamma / (gamma - 1.0));
-      const double rho = p / (R * t);
-      const double speed = m * sqrt(gamma * R * t);
+      const double t = div_rn(tt, 1.0 + 0.5 * (gamma - 1.0) * (m * m));
+      const double p = pt * pow(div_rn(t, tt), div_rn(gamma, gamma - 1.0));
+      const double rho = div_rn(p, R * t);
+      const double speed = m * sqrt_rn(gamma * R * t);
       out = St4{rho, speed * dx, speed * dy, p};
       const bool finite = isfinite(out.a) && isfinite(out.b) && isfinite(out.c) && isfinite(out.d);
       if (!finite || !(rho > 0.0) || !(p > 0.0)) bits |= MCFD_S_PIN_STATE;
@@ -135,17 +135,17 @@ __device__ void mass_flow_inlet(const DevGeom& g, const double* P, const double*
     atomicOr(&s_bad, 1);
   }
   __syncthreads();
-  const double cp = gamma * R / (gamma - 1.0);
+  const double cp = div_rn(gamma * R, gamma - 1.0);
   double speed = 0.0;
   if (!s_bad) {
     double* terms = g.bc_terms + j0;
     // flow_at(s) > or < the configured rate, decided by thread 0 for the block
     auto below = [&](double s) -> bool {
-      const double rt = R * (tt - s * s / (2.0 * cp));
+      const double rt = R * (tt - div_rn(s * s, 2.0 * cp));
       for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
         const St4 q = interior_state(g, P, recon, base + j);
         const double proj = -g.bc_dn[j];
-        terms[j - j0] = q.d / rt * s * proj * g.ff_len[base + j];
+        terms[j - j0] = div_rn(q.d, rt) * s * proj * g.ff_len[base + j];
       }
       __syncthreads();
       if (threadIdx.x == 0) s_below = (0.0 + pairwise_sum(terms, n)) < mdot;
@@ -154,7 +154,7 @@ __device__ void mass_flow_inlet(const DevGeom& g, const double* P, const double*
       __syncthreads();
       return r;
     };
-    double low = 0.0, high = sqrt(2.0 * cp * tt) * (1.0 - 1e-12);
+    double low = 0.0, high = sqrt_rn(2.0 * cp * tt) * (1.0 - 1e-12);
     if (below(high)) {
       if (threadIdx.x == 0) flag_patch(g.status, MCFD_S_MFI_FLOW_RATE, patch);
     } else {
@@ -166,10 +166,10 @@ __device__ void mass_flow_inlet(const DevGeom& g, const double* P, const double*
     }
     speed = 0.5 * (low + high);
   }
-  const double rt = R * (tt - speed * speed / (2.0 * cp));
+  const double rt = R * (tt - div_rn(speed * speed, 2.0 * cp));
   for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     const St4 q = interior_state(g, P, recon, base + j);
-    st4(ext + 4 * (size_t)j, St4{q.d / rt, speed * dx, speed * dy, q.d});
+    st4(ext + 4 * (size_t)j, St4{div_rn(q.d, rt), speed * dx, speed * dy, q.d});
   }
 }
 
@@ -182,7 +182,7 @@ __device__ void mass_flow_outlet(const DevGeom& g, const double* P, const double
     const St4 q = interior_state(g, P, recon, f);
     if (q.a <= 0.0 || !isfinite(q.a)) flag_patch(g.status, MCFD_S_MFO_DENSITY, patch);
     const double2 n = g.ff_normal[f];
-    const double vn = mdot / (total_length * q.a);
+    const double vn = div_rn(mdot, total_length * q.a);
     const double tx = -n.y, ty = n.x;
     const double vt = q.b * tx + q.c * ty;
     st4(ext + 4 * (size_t)j, St4{q.a, vn * n.x + vt * tx, vn * n.y + vt * ty, q.d});

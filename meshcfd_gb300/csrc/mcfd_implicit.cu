@@ -65,7 +65,7 @@ __global__ void k_boundary_term(int n, const int* __restrict__ owner, const doub
   const double2 m = nrm[k];
   double radius = fabs(p.b * m.x + p.c * m.y) + sound_speed(p.a, p.d, gamma);
   const double d = dt_per_cell ? dt[o] : dt[0];
-  term[k] = d * radius * len[k] / area[o];
+  term[k] = div_rn(d * radius * len[k], area[o]);
 }
 
 // per cell: diagonal in the reference's np.add.at order and the row values
@@ -83,10 +83,10 @@ __global__ void k_lusgs_assemble(int C, const int* __restrict__ dptr, const int*
   double s = 1.0;
   for (int e = dptr[i]; e < dptr[i + 1]; ++e) {
     const int r = dref[e];
-    s = s + (r >= 0 ? (d * coef[r]) / A : bterm[-r - 1]);
+    s = s + (r >= 0 ? div_rn(d * coef[r], A) : bterm[-r - 1]);
   }
   for (int e = rptr[i]; e < rptr[i + 1]; ++e) {
-    const double v = -(d * coef[rref[e]]) / A;
+    const double v = div_rn(-(d * coef[rref[e]]), A);
     rval[e] = v;
     // a periodic pair whose two faces belong to one cell couples the cell to
     // itself: the reference's COO -> CSC conversion sums it into the diagonal
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kBlock) k_lusgs_sweep(SweepArgs a) {
         acc[3] = acc[3] - v * x.d;
       }
       const double dg = a.diag[i];
-      st4(a.out + 4 * (size_t)i, St4{acc[0] / dg, acc[1] / dg, acc[2] / dg, acc[3] / dg});
+      st4(a.out + 4 * (size_t)i, St4{div_rn(acc[0], dg), div_rn(acc[1], dg), div_rn(acc[2], dg), div_rn(acc[3], dg)});
     }
     grid.sync();
   }
@@ -191,10 +191,10 @@ __global__ void __launch_bounds__(kBlock) k_equation(int C, const double* __rest
     const double d = dt_per_cell ? dt[i >> 2] : dt[0];
     const double du = U[i] - U0[i];
     const double eq = du - d * R[i];
-    const double se = eq / s.v[i & 3];
+    const double se = div_rn(eq, s.v[i & 3]);
     if (b) b[i] = -se;
     e_abs = (unsigned long long)(icmp::bits(se) & 0x7fffffffffffffffLL);
-    u_abs = (unsigned long long)(icmp::bits(du / s.v[i & 3]) & 0x7fffffffffffffffLL);
+    u_abs = (unsigned long long)(icmp::bits(div_rn(du, s.v[i & 3])) & 0x7fffffffffffffffLL);
   }
   for (int off = 16; off > 0; off >>= 1) {
     unsigned long long a = __shfl_down_sync(0xffffffffu, e_abs, off);
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kBlock) k_scaled_sumsq_partial(long long n, co
   double acc = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const double q = x[i] / s.v[i & 3];
+    const double q = div_rn(x[i], s.v[i & 3]);
     acc += q * q;
   }
   sh[threadIdx.x] = acc;
@@ -311,9 +311,9 @@ __global__ void k_sub(long long n, const double* __restrict__ b, const double* _
 // eps = sqrt(machine eps) * max(1, |u/s|) / |v|  (solver.py:1546-1561)
 __global__ void k_fd_eps(const double* __restrict__ v_sumsq, double state_norm, double* eps_out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    const double dn = sqrt(v_sumsq[0]);
+    const double dn = sqrt_rn(v_sumsq[0]);
     const double fd = 1.4901161193847656e-08;  // math.sqrt(np.finfo(float).eps)
-    eps_out[0] = (dn == 0.0) ? 0.0 : fd * (state_norm > 1.0 ? state_norm : 1.0) / dn;
+    eps_out[0] = (dn == 0.0) ? 0.0 : div_rn(fd * (state_norm > 1.0 ? state_norm : 1.0), dn);
   }
 }
 
@@ -339,8 +339,8 @@ __global__ void k_fd_combine(int C, const double* __restrict__ v, const double* 
     return;
   }
   const double d = dt_per_cell ? dt[i >> 2] : dt[0];
-  const double jv = (rp[i] - rate[i]) / e;
-  out[i] = v[i] - (d * jv) / s.v[i & 3];
+  const double jv = div_rn(rp[i] - rate[i], e);
+  out[i] = v[i] - div_rn(d * jv, s.v[i & 3]);
 }
 
 }  // namespace

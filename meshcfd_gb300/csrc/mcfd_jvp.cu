@@ -51,13 +51,13 @@ __device__ __forceinline__ double limiter_slope(double r) {
   if (LIMITER <= 1) return r < 1.0 ? 1.0 : 0.0;
   if (LIMITER == 2) {
     if (!(r > 0.0)) return 0.0;
-    const double q = 2.0 * r / (1.0 + r);
-    return q < 1.0 ? 2.0 / ((1.0 + r) * (1.0 + r)) : 0.0;
+    const double q = div_rn(2.0 * r, 1.0 + r);
+    return q < 1.0 ? div_rn(2.0, (1.0 + r) * (1.0 + r)) : 0.0;
   }
   const double eps = 1e-12;
   const double N = r * r + 2.0 * r + eps, D = r * r + r + 2.0 + eps;
-  if (N / D > 1.0) return 0.0;
-  return ((2.0 * r + 2.0) * D - N * (2.0 * r + 1.0)) / (D * D);
+  if (div_rn(N, D) > 1.0) return 0.0;
+  return div_rn((2.0 * r + 2.0) * D - N * (2.0 * r + 1.0), D * D);
 }
 
 template <int LIMITER>
@@ -106,8 +106,8 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_tangent(DevGeom g, const
         if (pos || neg) {
           const double num = pos ? hi[v] - pv[v] : lo[v] - pv[v];
           const double dnum = pos ? dhi[v] - dpv[v] : dlo[v] - dpv[v];
-          const double r = num / inc;
-          if (r > 0.0) df = limiter_slope<LIMITER>(r) * (dnum - r * dinc) / inc;
+          const double r = div_rn(num, inc);
+          if (r > 0.0) df = div_rn(limiter_slope<LIMITER>(r) * (dnum - r * dinc), inc);
         }
         dphi[v] = df;
       }
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_tangent(DevGeom g, const doub
   }
   const int jb0 = g.gb_ptr[c], jb1 = g.gb_ptr[c + 1];
   if (jb0 < jb1) {
-    const double ia = 1.0 / g.area[c];
+    const double ia = div_rn(1.0, g.area[c]);
     for (int j = jb0; j < jb1; ++j) {
       const double w = g.gb_len[j] * ia;
       const St4 F = ld4(dflux + 4 * (size_t)g.gb_flux[j]);
@@ -262,7 +262,7 @@ __global__ void k_exact_combine(int n4, const double* __restrict__ v, const doub
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n4) return;
   const double d = dt_per_cell ? dt[i >> 2] : dt[0];
-  out[i] = v[i] - (d * dR[i]) / s.v[i & 3];
+  out[i] = v[i] - div_rn(d * dR[i], s.v[i & 3]);
 }
 
 }  // namespace

@@ -75,7 +75,7 @@ __device__ __forceinline__ bool lu5(double (&A)[5][5], int (&piv)[5]) {
     }
 #pragma unroll
     for (int i = k + 1; i < 5; ++i) {
-      const double l = A[i][k] / A[k][k];
+      const double l = div_rn(A[i][k], A[k][k]);
       A[i][k] = l;
 #pragma unroll
       for (int j = k + 1; j < 5; ++j) A[i][j] = A[i][j] - l * A[k][j];
@@ -103,7 +103,7 @@ __device__ __forceinline__ void lu5_solve(const double (&LU)[5][5], const int (&
 #pragma unroll
       for (int v = 0; v < M; ++v) b[i][v] = b[i][v] - LU[i][j] * b[j][v];
 #pragma unroll
-    for (int v = 0; v < M; ++v) b[i][v] = b[i][v] / LU[i][i];
+    for (int v = 0; v < M; ++v) b[i][v] = div_rn(b[i][v], LU[i][i]);
   }
 }
 
@@ -128,12 +128,12 @@ __device__ __noinline__ int jacobi_rank5(const double (&M)[5][5]) {
           beta += A[i][q] * A[i][q];
           gam += A[i][p] * A[i][q];
         }
-        if (!(fabs(gam) > 1e-15 * sqrt(alpha * beta))) continue;
+        if (!(fabs(gam) > 1e-15 * sqrt_rn(alpha * beta))) continue;
         rotated = true;
-        const double zeta = (beta - alpha) / (2.0 * gam);
-        const double t = fabs(zeta) > 1e150 ? 0.5 / zeta
-                                            : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+        const double zeta = div_rn(beta - alpha, 2.0 * gam);
+        const double t = fabs(zeta) > 1e150 ? div_rn(0.5, zeta)
+                                            : div_rn(copysign(1.0, zeta), fabs(zeta) + sqrt_rn(1.0 + zeta * zeta));
+        const double c = div_rn(1.0, sqrt_rn(1.0 + t * t)), sn = c * t;
 #pragma unroll
         for (int i = 0; i < 5; ++i) {
           const double ap = A[i][p], aq = A[i][q];
@@ -149,7 +149,7 @@ __device__ __noinline__ int jacobi_rank5(const double (&M)[5][5]) {
     double n2 = 0.0;
 #pragma unroll
     for (int i = 0; i < 5; ++i) n2 += A[i][j] * A[i][j];
-    sv[j] = sqrt(n2);
+    sv[j] = sqrt_rn(n2);
     if (sv[j] > smax) smax = sv[j];
   }
   int rank = 0;
@@ -176,7 +176,7 @@ __device__ __forceinline__ bool full_rank5(const double (&M)[5][5], const double
         na += M[i][j] * M[i][j];
         ni += X[i][j] * X[i][j];
       }
-    const double kappa = sqrt(na) * sqrt(ni);
+    const double kappa = sqrt_rn(na) * sqrt_rn(ni);
     if (isfinite(kappa) && kappa < 1e12) return true;
   }
   return jacobi_rank5(M) == 5;
@@ -255,18 +255,18 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_full(DevGeom g, const do
     for (int v = 0; v < 4; ++v) lo[v] = hi[v] = pv[v];
     for (int e = e0; e < e1; ++e) {
       const double2 d = g.par_d[e];
-      const double nx = d.x / scale, ny = d.y / scale;
+      const double nx = div_rn(d.x, scale), ny = div_rn(d.y, scale);
       const double dd[5] = {nx, ny, 0.5 * (nx * nx), nx * ny, 0.5 * (ny * ny)};
       const double r2 = nx * nx + ny * ny;
-      const double w = 1.0 / (r2 >= 1e-300 ? r2 : 1e-300);
+      const double w = div_rn(1.0, r2 >= 1e-300 ? r2 : 1e-300);
       const St4 q = ld4(P + 4 * (size_t)g.par_nb[e]);
       const double qv[4] = {q.a, q.b, q.c, q.d};
       double diff[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         diff[v] = qv[v] - pv[v];
-        if (qv[v] < lo[v]) lo[v] = qv[v];
-        if (qv[v] > hi[v]) hi[v] = qv[v];
+        if (icmp::lt(qv[v], lo[v])) lo[v] = qv[v];
+        if (icmp::lt(hi[v], qv[v])) hi[v] = qv[v];
       }
 #pragma unroll
       for (int i = 0; i < 5; ++i) {
@@ -290,11 +290,11 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_full(DevGeom g, const do
       const double sc = scale, sc2 = scale * scale;
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        gx[v] = B[0][v] / sc;
-        gy[v] = B[1][v] / sc;
-        kxx[v] = B[2][v] / sc2;
-        kxy[v] = B[3][v] / sc2;
-        kyy[v] = B[4][v] / sc2;
+        gx[v] = div_rn(B[0][v], sc);
+        gy[v] = div_rn(B[1][v], sc);
+        kxx[v] = div_rn(B[2][v], sc2);
+        kxy[v] = div_rn(B[3][v], sc2);
+        kyy[v] = div_rn(B[4][v], sc2);
         phi[v] = 1.0;
       }
       const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];

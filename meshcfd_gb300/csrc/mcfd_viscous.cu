@@ -49,13 +49,13 @@ struct Visc {
 // _dynamic_viscosity; *bad set when Sutherland's law gives an invalid value
 __device__ __forceinline__ double viscosity(const Visc& v, double T, bool* bad) {
   if (v.model == MCFD_VISC_CONSTANT) return v.mu0;
-  double mu = v.suth_mu * pow(T / v.suth_t, 1.5);
-  mu *= (v.suth_t + v.suth_s) / (T + v.suth_s);
+  double mu = v.suth_mu * pow(div_rn(T, v.suth_t), 1.5);
+  mu *= div_rn(v.suth_t + v.suth_s, T + v.suth_s);
   if (!isfinite(mu) || !(mu > 0.0)) *bad = true;
   return mu;
 }
 __device__ __forceinline__ double conductivity(const Visc& v, double mu) {
-  return mu * v.gamma * v.R / ((v.gamma - 1.0) * v.pr);
+  return div_rn(mu * v.gamma * v.R, (v.gamma - 1.0) * v.pr);
 }
 
 // _viscous_flux for one face: components 1..3 (the mass component is zero)
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_cells(DevGeom g, const double* 
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.n_cells) return;
   const St4 p = ld4(P + 4 * (size_t)c);
-  const double T = p.d / (p.a * vs.R);
+  const double T = div_rn(p.d, p.a * vs.R);
   bool bad = false;
   const double mu = viscosity(vs, T, &bad);
   int bits = 0;
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_cells(DevGeom g, const double* 
   if (bits) flag(g.status, bits, c);
   const double k = conductivity(vs, mu);
   const double prm = vs.pr < 0.9 ? vs.pr : 0.9;
-  const double e1 = (4.0 / 3.0) * mu / p.a, e2 = mu / (p.a * prm);
+  const double e1 = div_rn((4.0 / 3.0) * mu, p.a), e2 = div_rn(mu, p.a * prm);
   st4(cell + 4 * (size_t)c, St4{T, mu, k, e2 > e1 ? e2 : e1});
 }
 
@@ -106,7 +106,7 @@ __device__ __forceinline__ bool inlet_values(const DevGeom& g, const double* P, 
   else return false;
   out[0] = st.b;
   out[1] = st.c;
-  out[2] = st.d / (st.a * R);
+  out[2] = div_rn(st.d, st.a * R);
   return true;
 }
 
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_gradients(DevGeom g, const doub
   double xx = 0.0, xy = 0.0, yy = 0.0, bx[3] = {0.0, 0.0, 0.0}, by[3] = {0.0, 0.0, 0.0};
   auto add = [&](double dx, double dy, const double diff[3]) {
     const double r2 = dx * dx + dy * dy;
-    const double w = 1.0 / (r2 > 1e-300 ? r2 : 1e-300);
+    const double w = div_rn(1.0, r2 > 1e-300 ? r2 : 1e-300);
     const double wx = w * dx, wy = w * dy;
     xx += wx * dx;
     xy += wx * dy;
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_gradients(DevGeom g, const doub
         ghost[2] = 2.0 * g.diff_value[j] - cv[2];
       } else {
         const double k = cc.c;  // conductivity of the cell's own temperature
-        ghost[2] += 2.0 * g.diff_nd[j] * g.diff_value[j] / k;
+        ghost[2] += div_rn(2.0 * g.diff_nd[j] * g.diff_value[j], k);
       }
     } else if (kind == MCFD_DIFF_SYMMETRY) {
       const double t = 2.0 * dot2(cv[0], cv[1], nx, ny);
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_gradients(DevGeom g, const doub
   const double det = xx * yy - xy * xy;
   const double xxyy = xx * yy;
   if (det > 1e-14 * (xxyy > 1e-300 ? xxyy : 1e-300)) {
-    const double inv = 1.0 / det;
+    const double inv = div_rn(1.0, det);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       out[2 * k] = (bx[k] * yy - by[k] * xy) * inv;
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_boundary(DevGeom g, const doubl
       const double w[2] = {wv.x, wv.y};
 #pragma unroll
       for (int comp = 0; comp < 2; ++comp) {
-        const double dn = (w[comp] - bv[comp] - dot2(fg[2 * comp], fg[2 * comp + 1], tox, toy)) / nd;
+        const double dn = div_rn(w[comp] - bv[comp] - dot2(fg[2 * comp], fg[2 * comp + 1], tox, toy), nd);
         const double t = dn - dot2(fg[2 * comp], fg[2 * comp + 1], nx, ny);
         fg[2 * comp] += t * nx;
         fg[2 * comp + 1] += t * ny;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_boundary(DevGeom g, const doubl
       bv[0] -= t * nx;
       bv[1] -= t * ny;
       const double gnv0 = nx * fg[0] + ny * fg[2], gnv1 = nx * fg[1] + ny * fg[3];
-      const double dn = -(nvel + dot2(gnv0, gnv1, tox, toy)) / nd;
+      const double dn = div_rn(-(nvel + dot2(gnv0, gnv1, tox, toy)), nd);
       const double d0 = dn * nx, d1 = dn * ny;  // desired = outer(dn n, n)
       const double r0 = gemv_row(fg[0], fg[1], nx, ny), r1 = gemv_row(fg[2], fg[3], nx, ny);
       fg[0] += d0 * nx - r0 * nx;
@@ -268,10 +268,10 @@ __global__ void __launch_bounds__(kBlock) k_visc_boundary(DevGeom g, const doubl
     }
     double dn;
     if (g.diff_thermal[j] == 0) {
-      dn = (g.diff_value[j] - bv[2] - dot2(fg[4], fg[5], tox, toy)) / nd;
+      dn = div_rn(g.diff_value[j] - bv[2] - dot2(fg[4], fg[5], tox, toy), nd);
       bv[2] = g.diff_value[j];
     } else {
-      dn = g.diff_value[j] / cc.c;
+      dn = div_rn(g.diff_value[j], cc.c);
       bv[2] += dot2(fg[4], fg[5], off.x, off.y);
     }
     const double t = dn - dot2(fg[4], fg[5], nx, ny);
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_boundary(DevGeom g, const doubl
     fg[5] += t * ny;
   } else if (kind == MCFD_DIFF_SYMMETRY) {
     const double nvel = dot2(bv[0], bv[1], nx, ny);
-    const double s = -nvel / nd;
+    const double s = div_rn(-nvel, nd);
     const double dvel[2] = {s * nx, s * ny};
 #pragma unroll
     for (int comp = 0; comp < 2; ++comp) {
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_boundary(DevGeom g, const doubl
       bv[2] = iv[2];
 #pragma unroll
       for (int comp = 0; comp < 3; ++comp) {
-        const double dn = (bv[comp] - cv[comp] - dot2(fg[2 * comp], fg[2 * comp + 1], tox, toy)) / nd;
+        const double dn = div_rn(bv[comp] - cv[comp] - dot2(fg[2 * comp], fg[2 * comp + 1], tox, toy), nd);
         const double t = dn - dot2(fg[2 * comp], fg[2 * comp + 1], nx, ny);
         fg[2 * comp] += t * nx;
         fg[2 * comp + 1] += t * ny;
@@ -349,10 +349,10 @@ __global__ void __launch_bounds__(kBlock) k_visc_gather(DevGeom g, const double*
     if (kind == 2) {  // diffusive boundary face: flux L / A
       const double len = g.diff_len[idx];
       const St4 F = ld4(bflux + 4 * (size_t)idx);
-      d[0] = d[0] + F.a * len / area;
-      d[1] = d[1] + F.b * len / area;
-      d[2] = d[2] + F.c * len / area;
-      d[3] = d[3] + F.d * len / area;
+      d[0] = d[0] + div_rn(F.a * len, area);
+      d[1] = d[1] + div_rn(F.b * len, area);
+      d[2] = d[2] + div_rn(F.c * len, area);
+      d[3] = d[3] + div_rn(F.d * len, area);
     } else {  // periodic pair idx: (flux L) / A on side a, -(flux L) / A on side b
       const int fi = g.seg_begin[SEG_PERIODIC] + idx;
       const double len = g.ff_len[fi];
@@ -361,10 +361,10 @@ __global__ void __launch_bounds__(kBlock) k_visc_gather(DevGeom g, const double*
       if (kind == 1) {
         v[0] = -v[0]; v[1] = -v[1]; v[2] = -v[2]; v[3] = -v[3];
       }
-      d[0] = d[0] + v[0] / area;
-      d[1] = d[1] + v[1] / area;
-      d[2] = d[2] + v[2] / area;
-      d[3] = d[3] + v[3] / area;
+      d[0] = d[0] + div_rn(v[0], area);
+      d[1] = d[1] + div_rn(v[1], area);
+      d[2] = d[2] + div_rn(v[2], area);
+      d[3] = d[3] + div_rn(v[3], area);
     }
   }
   st4(r + 4 * (size_t)c, St4{d[0], d[1], d[2], d[3]});
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_diffusion(DevGeom g, const doub
       e = eo > ec ? eo : ec;  // np.maximum
     }
     const double dist = g.vd_dist[i];
-    sum += e * g.vd_len[i] / (dist > 1e-14 ? dist : 1e-14);
+    sum += div_rn(e * g.vd_len[i], dist > 1e-14 ? dist : 1e-14);
   }
   diff[c] = sum;
 }
