@@ -37,7 +37,7 @@ METRIC = "RK3 HLLC-MUSCL cell-updates/s"
 UNIT = "cell-updates/s"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -61,7 +61,7 @@ def parse():
                          "(outside the 1e-12 bar on fine meshes)")
     ap.add_argument("--parity-steps", type=int, default=10)
     ap.add_argument("--variant-steps", type=int, default=20)
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 WORKLOADS = {
@@ -218,6 +218,23 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def replica_throughput(ms_local, cells, steps, dist=None, device=None):
+    """The replica job's time and throughput: every rank steps its own copy
+    of the workload (no data-path collective), the job's time is the slowest
+    rank's (MAX over ranks), and the value counts every rank's cells:
+    world * cells * steps / time.  Returns (ms, cell-updates/s)."""
+    import torch
+
+    world = 1
+    ms = float(ms_local)
+    if dist is not None:
+        world = dist.get_world_size()
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    return ms, world * cells * steps / (ms * 1e-3)
+
+
 def run_gpu(args):
     import torch
 
@@ -282,14 +299,9 @@ def run_gpu(args):
         stop.record(stream)
         barrier()
     launches = native.mcfd_launch_count() - launches0
-    ms = start.elapsed_time(stop)
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t)
+    ms, value = replica_throughput(start.elapsed_time(stop), C, args.steps, dist, device)
     dg.check_status()
     ms_per_step = ms / args.steps
-    value = world * C * args.steps / (ms * 1e-3)
 
     # per-kernel breakdown (CUDA events on the launching stream)
     import ctypes as Cc
