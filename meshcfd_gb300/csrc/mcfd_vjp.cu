@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
       for (int s = s0; s < s1; ++s) {
         const double2 dd = g.lim_d[s];
         for (int v = 0; v < 4; ++v) {
-          const double inc = gx[v] * dd.x + gy[v] * dd.y;
+          const double inc = mul_rn(gx[v], dd.x) + gy[v] * dd.y;
           if (icmp::gt_pos(inc, tol[v])) {
             if (ps[v] < 0 || icmp::lt(pmax[v], inc)) { pmax[v] = inc; ps[v] = s; }
           } else if (icmp::neg_gt_pos(inc, tol[v])) {
@@ -411,16 +411,20 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
         }
       }
     }
-    // reverse of Q_s = P + phi (G . r_s)
+    // reverse of Q_s = P + phi (G . r_s).  Products that would stand alone
+    // (not contracted into an FMA) run on the integer pipe (mul_rn, the same
+    // IEEE product): this kernel keeps the FP64 pipe busy and the integer
+    // pipe nearly idle.
     double phib[4] = {0, 0, 0, 0}, gxb[4] = {0, 0, 0, 0}, gyb[4] = {0, 0, 0, 0};
     for (int s = s0; s < s1; ++s) {
       const double2 dd = g.lim_d[s];
       const St4 q = ld4(slot_bar + 4 * (size_t)g.lim_slot[s]);
       const double qb[4] = {q.a, q.b, q.c, q.d};
       for (int v = 0; v < 4; ++v) {
-        phib[v] += qb[v] * (gx[v] * dd.x + gy[v] * dd.y);
-        gxb[v] += qb[v] * phi[v] * dd.x;
-        gyb[v] += qb[v] * phi[v] * dd.y;
+        phib[v] += qb[v] * (mul_rn(gx[v], dd.x) + gy[v] * dd.y);
+        const double qphi = mul_rn(qb[v], phi[v]);
+        gxb[v] += qphi * dd.x;
+        gyb[v] += qphi * dd.y;
       }
     }
     // reverse of the limiter through its minimising entry
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
     for (int v = 0; v < 4; ++v) {
       if (arg[v] < 0) continue;
       const double2 dd = g.lim_d[arg[v]];
-      const double inc = gx[v] * dd.x + gy[v] * dd.y;
+      const double inc = mul_rn(gx[v], dd.x) + gy[v] * dd.y;
       const double tol = limiter_tolerance(pv[v]);
       const bool pos = icmp::gt_pos(inc, tol), neg = icmp::neg_gt_pos(inc, tol);
       if (!(pos || neg)) continue;
@@ -451,7 +455,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
     for (int e = e0; e < e1; ++e) {
       double out[4];
       for (int v = 0; v < 4; ++v) {
-        const double w = g.grad_cx[e] * gxb[v] + g.grad_cy[e] * gyb[v];
+        const double w = mul_rn(g.grad_cx[e], gxb[v]) + g.grad_cy[e] * gyb[v];
         pb[v] -= w;
         out[v] = w + (ext_e[v] == e ? extb[v] : 0.0);
       }
