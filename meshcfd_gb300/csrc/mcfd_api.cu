@@ -584,8 +584,11 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   }
 
   // ---- visiting order of the per-cell stage kernels: cells grouped by their
-  // entry counts (stable), so that each warp's loops share one trip count
+  // entry counts (stable), so that each warp's loops share one trip count;
+  // cells with 3 or 4 limiter entries first (the fast reconstruction has a
+  // kernel compiled for exactly those, and one for the rest)
   std::vector<int> cell_order(C);
+  int n_lim34 = 0;
   {
     auto count = [](const std::vector<int>& ptr, size_t c) { return ptr.empty() ? 0 : ptr[c + 1] - ptr[c]; };
     std::vector<long long> ckey(C);
@@ -593,7 +596,10 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
       const long long k0 = count(grad_ptr, c), k1 = count(lim_ptr, c), k2 = count(gi_ptr, c),
                       k3 = count(gb_ptr, c), k4 = count(dt_ptr, c);
       auto clamp = [](long long v) { return v < 0 ? 0 : (v > 4095 ? 4095 : v); };
-      ckey[c] = (((clamp(k0) * 4096 + clamp(k1)) * 4096 + clamp(k2)) * 4096 + clamp(k3)) * 64 + (k4 > 63 ? 63 : k4);
+      const long long other = (k1 == 3 || k1 == 4) ? 0 : 1;
+      n_lim34 += other ? 0 : 1;
+      ckey[c] = ((((other * 4096 + clamp(k0)) * 4096 + clamp(k1)) * 4096 + clamp(k2)) * 4096 + clamp(k3)) * 64 +
+                (k4 > 63 ? 63 : k4);
     }
     for (size_t c = 0; c < C; ++c) cell_order[c] = (int)c;
     std::stable_sort(cell_order.begin(), cell_order.end(), [&](int a, int b) { return ckey[a] < ckey[b]; });
@@ -736,6 +742,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
 #define AT(T, off) reinterpret_cast<T>(base + (off))
   g.area = AT(const double*, o_area);
   g.cell_order = AT(const int*, o_cell_order);
+  g.n_lim34 = n_lim34;
   g.grad_ptr = AT(const int*, o_grad_ptr);
   g.grad_nb = AT(const int*, o_grad_nb);
   g.grad_cx = AT(const double*, o_grad_cx);

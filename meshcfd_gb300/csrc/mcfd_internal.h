@@ -38,6 +38,7 @@ struct DevGeom {
   // cells grouped by (gradient, limiter, gather, time-step) entry counts,
   // stable in cell id: the visiting order of the per-cell stage kernels
   const int* cell_order;  // [C]
+  int n_lim34;            // cells cell_order[0 .. n_lim34) have 3 or 4 limiter entries
   // least-squares gradient entries grouped by source cell, reference order
   const int* grad_ptr;
   const int* grad_nb;

@@ -119,9 +119,14 @@ __global__ void __launch_bounds__(kBlock) k_primitive(int n, const double* __res
 // triangle lane idle through the fourth entry, which still costs FP64 issue
 // slots).  Each cell's arithmetic and outputs do not depend on the order.
 
+// Resident 256-thread blocks per SM the generic kernel is compiled for.
+#ifndef MCFD_RECON_GENERIC_MIN_BLOCKS
+#define MCFD_RECON_GENERIC_MIN_BLOCKS 2
+#endif
+
 template <int LIMITER>
-__global__ void __launch_bounds__(kBlock) k_reconstruct(DevGeom g, const double* __restrict__ P,
-                                                        double* __restrict__ recon) {
+__global__ void __launch_bounds__(kBlock, MCFD_RECON_GENERIC_MIN_BLOCKS) k_reconstruct(DevGeom g, const double* __restrict__ P,
+                                                                                       double* __restrict__ recon) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n_cells) return;
   const int c = g.cell_order[i];
@@ -338,17 +343,40 @@ __device__ __forceinline__ void reconstruct_cell_fast_by_variable(const DevGeom&
   }
 }
 
+// Register bound of the 3 / 4-entry kernel: MCFD_RECON_MAXNREG caps the
+// registers a thread directly; otherwise the bound is MCFD_RECON_MIN_BLOCKS
+// resident 256-thread blocks per SM.
+#ifndef MCFD_RECON_MIN_BLOCKS
+#define MCFD_RECON_MIN_BLOCKS 3
+#endif
+#ifdef MCFD_RECON_MAXNREG
+#define MCFD_RECON_BOUND __maxnreg__(MCFD_RECON_MAXNREG)
+#else
+#define MCFD_RECON_BOUND __launch_bounds__(kBlock, MCFD_RECON_MIN_BLOCKS)
+#endif
+
+// Cells with 3 or 4 limiter entries (cell_order[0 .. n_lim34)); the kernel
+// for any other count is separate, so that its register budget does not set
+// this one's occupancy.
 template <int LIMITER>
-__global__ void __launch_bounds__(kBlock, 2) k_reconstruct_fast(DevGeom g, const double* __restrict__ P,
-                                                                double* __restrict__ recon) {
+__global__ void MCFD_RECON_BOUND k_reconstruct_fast(DevGeom g, const double* __restrict__ P, double* __restrict__ recon) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n_lim34) return;
+  const int c = g.cell_order[i];
+  const St4 p = ld4(P + 4 * (size_t)c);
+  const int s0 = g.lim_ptr[c];
+  if (g.lim_ptr[c + 1] - s0 == 3) reconstruct_cell_fast_by_variable<LIMITER, 3>(g, P, recon, c, p, s0);
+  else reconstruct_cell_fast_by_variable<LIMITER, 4>(g, P, recon, c, p, s0);
+}
+
+template <int LIMITER>
+__global__ void __launch_bounds__(kBlock) k_reconstruct_fast_any(DevGeom g, const double* __restrict__ P,
+                                                                 double* __restrict__ recon) {
+  const int i = g.n_lim34 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n_cells) return;
   const int c = g.cell_order[i];
   const St4 p = ld4(P + 4 * (size_t)c);
-  const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
-  if (s1 - s0 == 3) reconstruct_cell_fast_by_variable<LIMITER, 3>(g, P, recon, c, p, s0);
-  else if (s1 - s0 == 4) reconstruct_cell_fast_by_variable<LIMITER, 4>(g, P, recon, c, p, s0);
-  else reconstruct_cell_fast<LIMITER, 0>(g, P, recon, c, p, s0, s1);
+  reconstruct_cell_fast<LIMITER, 0>(g, P, recon, c, p, g.lim_ptr[c], g.lim_ptr[c + 1]);
 }
 
 // -------------------------------------------------------------------- fluxes
@@ -614,15 +642,29 @@ cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const d
   if (g.n_cells == 0) return cudaSuccess;
   const int t = g.tune_recon_threads ? g.tune_recon_threads : kBlock;
   const int b = (g.n_cells + t - 1) / t;
-  count_launch();
   if constexpr (kFast || kMinRatio) {
-    switch (cfg.limiter) {
-      case 0: k_reconstruct_fast<0><<<b, t, 0, s>>>(g, P, recon); break;
-      case 1: k_reconstruct_fast<1><<<b, t, 0, s>>>(g, P, recon); break;
-      case 2: k_reconstruct_fast<2><<<b, t, 0, s>>>(g, P, recon); break;
-      default: k_reconstruct_fast<3><<<b, t, 0, s>>>(g, P, recon); break;
+    if (g.n_lim34 > 0) {
+      const int b34 = (g.n_lim34 + t - 1) / t;
+      count_launch();
+      switch (cfg.limiter) {
+        case 0: k_reconstruct_fast<0><<<b34, t, 0, s>>>(g, P, recon); break;
+        case 1: k_reconstruct_fast<1><<<b34, t, 0, s>>>(g, P, recon); break;
+        case 2: k_reconstruct_fast<2><<<b34, t, 0, s>>>(g, P, recon); break;
+        default: k_reconstruct_fast<3><<<b34, t, 0, s>>>(g, P, recon); break;
+      }
+    }
+    if (g.n_cells > g.n_lim34) {
+      const int ba = (g.n_cells - g.n_lim34 + kBlock - 1) / kBlock;
+      count_launch();
+      switch (cfg.limiter) {
+        case 0: k_reconstruct_fast_any<0><<<ba, kBlock, 0, s>>>(g, P, recon); break;
+        case 1: k_reconstruct_fast_any<1><<<ba, kBlock, 0, s>>>(g, P, recon); break;
+        case 2: k_reconstruct_fast_any<2><<<ba, kBlock, 0, s>>>(g, P, recon); break;
+        default: k_reconstruct_fast_any<3><<<ba, kBlock, 0, s>>>(g, P, recon); break;
+      }
     }
   } else {
+    count_launch();
     switch (cfg.limiter) {
       case 0: k_reconstruct<0><<<b, t, 0, s>>>(g, P, recon); break;
       case 1: k_reconstruct<1><<<b, t, 0, s>>>(g, P, recon); break;
