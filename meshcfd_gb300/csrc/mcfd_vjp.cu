@@ -341,8 +341,127 @@ __device__ __forceinline__ double limiter_slope(double r) {
   return ((2.0 * r + 2.0) * D - N * (2.0 * r + 1.0)) * (inv_D * inv_D);
 }
 
+// The cell reverse of one variable (the cell kernel's loop body): the
+// variable's gradient and extremes, limiter minimum and its first entry,
+// then the reverse of the face states, of the limiter and of the gradient.
+// One variable's state is live at a time (96 registers instead of 128 with
+// spills for all four at once), and its first four increments are kept for
+// the reverse instead of being recomputed.
+template <int LIMITER>
+__device__ __forceinline__ void vjp_cell_variable(const DevGeom& g, const double* __restrict__ P,
+                                                  const double* __restrict__ slot_bar, int v, double pv,
+                                                  int e0, int e1, int s0, int s1, double& pb,
+                                                  double* __restrict__ ent_bar) {
+  double gx = 0.0, gy = 0.0, lo = pv, hi = pv;
+  int lo_e = -1, hi_e = -1;
+  for (int e = e0; e < e1; ++e) {
+    const double q = P[4 * (size_t)g.grad_nb[e] + v];
+    const double d = q - pv;
+    gx = gx + g.grad_cx[e] * d;
+    gy = gy + g.grad_cy[e] * d;
+    if (icmp::lt(q, lo)) { lo = q; lo_e = e; }
+    if (icmp::lt(hi, q)) { hi = q; hi_e = e; }
+  }
+  // phi = min over entries of f(max(r, 0)) and its first entry, from the
+  // three candidates (largest positive increment, most negative, first
+  // entry in the tolerance band)
+  const double tol = limiter_tolerance(pv);
+  double pmax = 0.0, nmin = 0.0;
+  int ps = -1, ns = -1, fs = -1;
+  double inc4[4] = {0.0, 0.0, 0.0, 0.0};
+  auto classify = [&](int s, double inc) {
+    if (icmp::gt_pos(inc, tol)) {
+      if (ps < 0 || icmp::lt(pmax, inc)) { pmax = inc; ps = s; }
+    } else if (icmp::neg_gt_pos(inc, tol)) {
+      if (ns < 0 || icmp::lt(inc, nmin)) { nmin = inc; ns = s; }
+    } else if (fs < 0) {
+      fs = s;
+    }
+  };
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (s0 + k < s1) {
+      const double2 dd = g.lim_d[s0 + k];
+      inc4[k] = mul_rn(gx, dd.x) + gy * dd.y;
+      classify(s0 + k, inc4[k]);
+    }
+  }
+  for (int s = s0 + 4; s < s1; ++s) {
+    const double2 dd = g.lim_d[s];
+    classify(s, mul_rn(gx, dd.x) + gy * dd.y);
+  }
+  double phi = 1.0;
+  int arg = -1;
+  {
+    const int cand[3] = {ps, ns, fs};
+    const double cinc[3] = {pmax, nmin, 0.0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (cand[k] < 0) continue;
+      const double f = limiter_face_factor<LIMITER>(pv, cinc[k], lo, hi, tol);
+      if (icmp::lt_nonneg(f, phi) || (icmp::key(f) == icmp::key(phi) && arg >= 0 && cand[k] < arg)) {
+        phi = f;
+        arg = cand[k];
+      }
+    }
+  }
+  // reverse of Q_s = P + phi (G . r_s)
+  double phib = 0.0, gxb = 0.0, gyb = 0.0;
+  auto face_reverse = [&](int s, double inc, const double2& dd) {
+    const double qb = slot_bar[4 * (size_t)g.lim_slot[s] + v];
+    phib += qb * inc;
+    const double qphi = mul_rn(qb, phi);
+    gxb += qphi * dd.x;
+    gyb += qphi * dd.y;
+  };
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (s0 + k < s1) face_reverse(s0 + k, inc4[k], g.lim_d[s0 + k]);
+  for (int s = s0 + 4; s < s1; ++s) {
+    const double2 dd = g.lim_d[s];
+    face_reverse(s, mul_rn(gx, dd.x) + gy * dd.y, dd);
+  }
+  // reverse of the limiter through its minimising entry
+  double extb = 0.0;
+  int ext_e = -1;
+  if (arg >= 0) {
+    const double2 dd = g.lim_d[arg];
+    const int k = arg - s0;
+    const double inc = k == 0 ? inc4[0] : k == 1 ? inc4[1] : k == 2 ? inc4[2] : k == 3 ? inc4[3]
+                                                                                  : mul_rn(gx, dd.x) + gy * dd.y;
+    const bool pos = icmp::gt_pos(inc, tol), neg = icmp::neg_gt_pos(inc, tol);
+    if (pos || neg) {
+      const double num = pos ? hi - pv : lo - pv;
+      const double inv_inc = div_rn(1.0, inc);
+      const double r = num * inv_inc;
+      if (icmp::gt0(r)) {
+        const double rb = limiter_slope<LIMITER>(r) * phib;
+        const double numb = rb * inv_inc;
+        const double incb = -numb * r;
+        pb -= numb;
+        const int ee = pos ? hi_e : lo_e;
+        if (ee < 0) pb += numb;  // the extreme is the cell itself
+        else { extb = numb; ext_e = ee; }
+        gxb += incb * dd.x;
+        gyb += incb * dd.y;
+      }
+    }
+  }
+  // reverse of G = sum_e coef_e (P_nb - P_c): neighbour share per entry
+  for (int e = e0; e < e1; ++e) {
+    const double w = mul_rn(g.grad_cx[e], gxb) + g.grad_cy[e] * gyb;
+    pb -= w;
+    ent_bar[4 * (size_t)e + v] = w + (ext_e == e ? extb : 0.0);
+  }
+}
+
+// Resident 256-thread blocks per SM the cell reverse is compiled for.
+#ifndef MCFD_VJP_CELL_MIN_BLOCKS
+#define MCFD_VJP_CELL_MIN_BLOCKS 2
+#endif
+
 template <int LIMITER, bool FO>
-__global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __restrict__ P,
+__global__ void __launch_bounds__(kBlock, MCFD_VJP_CELL_MIN_BLOCKS) k_vjp_cell(DevGeom g, const double* __restrict__ P,
                                                      const double* __restrict__ lambda,
                                                      const double* __restrict__ slot_bar, double ax, double ay,
                                                      double* __restrict__ pbar, double* __restrict__ ent_bar) {
@@ -358,113 +477,8 @@ __global__ void __launch_bounds__(kBlock) k_vjp_cell(DevGeom g, const double* __
     pb[0] += q.a; pb[1] += q.b; pb[2] += q.c; pb[3] += q.d;
   }
   if (!FO) {
-    // forward values in the residual's exact order
-    double gx[4] = {0, 0, 0, 0}, gy[4] = {0, 0, 0, 0}, lo[4], hi[4];
-    int lo_e[4] = {-1, -1, -1, -1}, hi_e[4] = {-1, -1, -1, -1};
-    for (int v = 0; v < 4; ++v) lo[v] = hi[v] = pv[v];
-    for (int e = e0; e < e1; ++e) {
-      const St4 q = ld4(P + 4 * (size_t)g.grad_nb[e]);
-      const double qv[4] = {q.a, q.b, q.c, q.d};
-      for (int v = 0; v < 4; ++v) {
-        const double d = qv[v] - pv[v];
-        gx[v] = gx[v] + g.grad_cx[e] * d;
-        gy[v] = gy[v] + g.grad_cy[e] * d;
-        if (icmp::lt(qv[v], lo[v])) { lo[v] = qv[v]; lo_e[v] = e; }
-        if (icmp::lt(hi[v], qv[v])) { hi[v] = qv[v]; hi_e[v] = e; }
-      }
-    }
-    // phi = min over entries of f(max(r, 0)), arg = its first entry.  Every
-    // limiter f is nondecreasing in r and correctly rounded division is
-    // monotone, so among entries with a positive increment the smallest
-    // factor sits at the largest increment, among negative ones at the most
-    // negative; entries inside the tolerance band give f(1).  Three
-    // candidates per variable instead of a division per entry.
-    double phi[4] = {1.0, 1.0, 1.0, 1.0};
-    int arg[4] = {-1, -1, -1, -1};
-    {
-      double tol[4], pmax[4], nmin[4];
-      int ps[4] = {-1, -1, -1, -1}, ns[4] = {-1, -1, -1, -1}, fs[4] = {-1, -1, -1, -1};
-      for (int v = 0; v < 4; ++v) {
-        tol[v] = limiter_tolerance(pv[v]);
-        pmax[v] = 0.0;
-        nmin[v] = 0.0;
-      }
-      for (int s = s0; s < s1; ++s) {
-        const double2 dd = g.lim_d[s];
-        for (int v = 0; v < 4; ++v) {
-          const double inc = mul_rn(gx[v], dd.x) + gy[v] * dd.y;
-          if (icmp::gt_pos(inc, tol[v])) {
-            if (ps[v] < 0 || icmp::lt(pmax[v], inc)) { pmax[v] = inc; ps[v] = s; }
-          } else if (icmp::neg_gt_pos(inc, tol[v])) {
-            if (ns[v] < 0 || icmp::lt(inc, nmin[v])) { nmin[v] = inc; ns[v] = s; }
-          } else if (fs[v] < 0) {
-            fs[v] = s;
-          }
-        }
-      }
-      for (int v = 0; v < 4; ++v) {
-        const int cand[3] = {ps[v], ns[v], fs[v]};
-        const double cinc[3] = {pmax[v], nmin[v], 0.0};
-        for (int k = 0; k < 3; ++k) {
-          if (cand[k] < 0) continue;
-          const double f = limiter_face_factor<LIMITER>(pv[v], cinc[k], lo[v], hi[v], tol[v]);
-          if (icmp::lt_nonneg(f, phi[v]) || (icmp::key(f) == icmp::key(phi[v]) && arg[v] >= 0 && cand[k] < arg[v])) {
-            phi[v] = f;
-            arg[v] = cand[k];
-          }
-        }
-      }
-    }
-    // reverse of Q_s = P + phi (G . r_s).  Products that would stand alone
-    // (not contracted into an FMA) run on the integer pipe (mul_rn, the same
-    // IEEE product): this kernel keeps the FP64 pipe busy and the integer
-    // pipe nearly idle.
-    double phib[4] = {0, 0, 0, 0}, gxb[4] = {0, 0, 0, 0}, gyb[4] = {0, 0, 0, 0};
-    for (int s = s0; s < s1; ++s) {
-      const double2 dd = g.lim_d[s];
-      const St4 q = ld4(slot_bar + 4 * (size_t)g.lim_slot[s]);
-      const double qb[4] = {q.a, q.b, q.c, q.d};
-      for (int v = 0; v < 4; ++v) {
-        phib[v] += qb[v] * (mul_rn(gx[v], dd.x) + gy[v] * dd.y);
-        const double qphi = mul_rn(qb[v], phi[v]);
-        gxb[v] += qphi * dd.x;
-        gyb[v] += qphi * dd.y;
-      }
-    }
-    // reverse of the limiter through its minimising entry
-    double extb[4] = {0, 0, 0, 0};
-    int ext_e[4] = {-1, -1, -1, -1};
-    for (int v = 0; v < 4; ++v) {
-      if (arg[v] < 0) continue;
-      const double2 dd = g.lim_d[arg[v]];
-      const double inc = mul_rn(gx[v], dd.x) + gy[v] * dd.y;
-      const double tol = limiter_tolerance(pv[v]);
-      const bool pos = icmp::gt_pos(inc, tol), neg = icmp::neg_gt_pos(inc, tol);
-      if (!(pos || neg)) continue;
-      const double num = pos ? hi[v] - pv[v] : lo[v] - pv[v];
-      const double inv_inc = div_rn(1.0, inc);
-      const double r = num * inv_inc;
-      if (!icmp::gt0(r)) continue;
-      const double rb = limiter_slope<LIMITER>(r) * phib[v];
-      const double numb = rb * inv_inc;
-      const double incb = -numb * r;
-      pb[v] -= numb;
-      const int ee = pos ? hi_e[v] : lo_e[v];
-      if (ee < 0) pb[v] += numb;  // the extreme is the cell itself
-      else { extb[v] = numb; ext_e[v] = ee; }
-      gxb[v] += incb * dd.x;
-      gyb[v] += incb * dd.y;
-    }
-    // reverse of G = sum_e coef_e (P_nb - P_c): neighbour share per entry
-    for (int e = e0; e < e1; ++e) {
-      double out[4];
-      for (int v = 0; v < 4; ++v) {
-        const double w = mul_rn(g.grad_cx[e], gxb[v]) + g.grad_cy[e] * gyb[v];
-        pb[v] -= w;
-        out[v] = w + (ext_e[v] == e ? extb[v] : 0.0);
-      }
-      st4(ent_bar + 4 * (size_t)e, St4{out[0], out[1], out[2], out[3]});
-    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) vjp_cell_variable<LIMITER>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar);
   }
   if (ax != 0.0 || ay != 0.0) {  // body force (solver.py:2709-2715)
     const St4 l = ld4(lambda + 4 * (size_t)c);
