@@ -98,7 +98,6 @@ __device__ __forceinline__ void rusanov_bar(const St4& L, const St4& R, double n
 template <bool KERNEL_BRANCHES>
 __device__ __forceinline__ void hllc_bar(const St4& L, const St4& R, double nx, double ny, double gamma,
                                          double inv_gm1, const double Fb[4], double Lb[4], double Rb[4]) {
-  const double zero[4] = {0.0, 0.0, 0.0, 0.0};
   const double unl = L.b * nx + L.c * ny, unr = R.b * nx + R.c * ny;
   const Sound sl_ = sound_d(L, gamma), sr_ = sound_d(R, gamma);
   const double cl = sl_.c, cr = sr_.c;
@@ -124,56 +123,60 @@ __device__ __forceinline__ void hllc_bar(const St4& L, const St4& R, double nx, 
     else if (icmp::gt0(wr)) branch = 2;
     else branch = 3;
   }
-  if (branch == 0) {
-    physical_bar(L, nx, ny, inv_gm1, Fb, zero, Lb);
-    return;
-  }
-  if (branch == 3) {
-    physical_bar(R, nx, ny, inv_gm1, Fb, zero, Rb);
-    return;
-  }
-  const bool left = branch == 1;
+  // Branches 0 and 3 take one side's physical flux; the star branches add
+  // the star state's terms.  physical_bar runs once for every lane (with a
+  // zero state adjoint outside the star region), so a warp mixing
+  // supersonic and subsonic faces does not issue it twice.
+  const bool star = branch == 1 || branch == 2;
+  const bool left = branch <= 1;
   const St4& q = left ? L : R;
   double* qb = left ? Lb : Rb;
-  const double un = left ? unl : unr, w = left ? wl : wr;
-  const double r = q.a, u = q.b, v = q.c, p = q.d;
-  const double inv_r = left ? sl_.inv_r : sr_.inv_r;
-  const double E = p * inv_gm1 + 0.5 * r * (u * u + v * v);
-  const double Uq[4] = {r, r * u, r * v, E};
-  const double wu = w - un;
-  const double B = w - contact, inv_B = div_rn(1.0, B), A = r * wu, factor = A * inv_B;
-  const double dc = contact - un;
-  const double sux = u + dc * nx, suy = v + dc * ny;
-  const double inv_Z = div_rn(inv_r, wu);  // 1 / (r (w - un))
-  const double pz = p * inv_Z;
-  const double Y = contact + pz, Er = E * inv_r, X = Er + dc * Y;
-  const double star[4] = {factor, factor * sux, factor * suy, factor * X};
-  // Reverse sweep.  Products that share a factor are grouped (Uq_bar =
-  // -star_bar exactly; Z_bar and A_bar enter r, w and un only through their
-  // sum; the contact's numerator and denominator adjoints through
-  // numb * un + denb per side), which removes about a fifth of the FP64
-  // operations of the term-by-term transpose; the results agree to rounding.
-  double wb = 0.0, Uqb[4], starb[4];
+  double Uqb[4] = {0.0, 0.0, 0.0, 0.0};
+  double wb = 0.0, rb = 0.0, suxb = 0.0, suyb = 0.0, unb = 0.0, pb = 0.0, contactb = 0.0;
+  if (star) {
+    const double un = left ? unl : unr, w = left ? wl : wr;
+    const double r = q.a, u = q.b, v = q.c, p = q.d;
+    const double inv_r = left ? sl_.inv_r : sr_.inv_r;
+    const double E = p * inv_gm1 + 0.5 * r * (u * u + v * v);
+    const double Uq[4] = {r, r * u, r * v, E};
+    const double wu = w - un;
+    const double B = w - contact, inv_B = div_rn(1.0, B), A = r * wu, factor = A * inv_B;
+    const double dc = contact - un;
+    const double sux = u + dc * nx, suy = v + dc * ny;
+    const double inv_Z = div_rn(inv_r, wu);  // 1 / (r (w - un))
+    const double pz = p * inv_Z;
+    const double Y = contact + pz, Er = E * inv_r, X = Er + dc * Y;
+    const double star_state[4] = {factor, factor * sux, factor * suy, factor * X};
+    // Reverse sweep.  Products that share a factor are grouped (Uq_bar =
+    // -star_bar exactly; Z_bar and A_bar enter r, w and un only through their
+    // sum; the contact's numerator and denominator adjoints through
+    // numb * un + denb per side), which removes about a fifth of the FP64
+    // operations of the term-by-term transpose; the results agree to rounding.
+    double starb[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    wb += Fb[k] * (star[k] - Uq[k]);
-    starb[k] = w * Fb[k];
-    Uqb[k] = negate(starb[k]);
+    for (int k = 0; k < 4; ++k) {
+      wb += Fb[k] * (star_state[k] - Uq[k]);
+      starb[k] = w * Fb[k];
+      Uqb[k] = negate(starb[k]);
+    }
+    const double factorb = starb[0] + starb[1] * sux + starb[2] * suy + starb[3] * X;
+    suxb = starb[1] * factor;
+    suyb = starb[2] * factor;
+    const double Xb = starb[3] * factor;
+    const double Xr = Xb * inv_r;
+    Uqb[3] += Xr;
+    const double dcb = Xb * Y + suxb * nx + suyb * ny;
+    const double Yb = Xb * dc;
+    pb = Yb * inv_Z;
+    const double Ab = factorb * inv_B;
+    const double ZA = Ab - pb * pz;  // Z_bar + A_bar, Z_bar = -Yb pz / Z
+    rb = ZA * wu - Xr * Er;
+    unb = negate(dcb + ZA * r);
+    wb += ZA * r - Ab * factor;  // + B_bar = -A_bar factor
+    contactb = Yb + dcb + Ab * factor;
   }
-  const double factorb = starb[0] + starb[1] * sux + starb[2] * suy + starb[3] * X;
-  const double suxb = starb[1] * factor, suyb = starb[2] * factor, Xb = starb[3] * factor;
-  const double Xr = Xb * inv_r;
-  Uqb[3] += Xr;
-  const double dcb = Xb * Y + suxb * nx + suyb * ny;
-  const double Yb = Xb * dc;
-  const double pb = Yb * inv_Z;
-  const double Ab = factorb * inv_B;
-  const double ZA = Ab - pb * pz;  // Z_bar + A_bar, Z_bar = -Yb pz / Z
-  const double rb = ZA * wu - Xr * Er;
-  const double unb = negate(dcb + ZA * r);
-  wb += ZA * r - Ab * factor;  // + B_bar = -A_bar factor
-  const double contactb = Yb + dcb + Ab * factor;
   physical_bar(q, nx, ny, inv_gm1, Fb, Uqb, qb);
+  if (!star) return;
   qb[0] += rb;
   qb[1] += suxb + unb * nx;
   qb[2] += suyb + unb * ny;
@@ -214,13 +217,13 @@ __device__ __forceinline__ void hllc_bar(const St4& L, const St4& R, double nx, 
   Rb[2] += unrb * ny;
 }
 
-// Face VJP by the hand-written reverse (Rusanov / HLLC on every segment but
-// the far field, whose ghost state keeps the dual-number path).
 // Resident 256-thread blocks per SM the face reverse is compiled for.
 #ifndef MCFD_VJP_FACE_MIN_BLOCKS
 #define MCFD_VJP_FACE_MIN_BLOCKS 1
 #endif
 
+// Face VJP by the hand-written reverse (Rusanov / HLLC on every segment but
+// the far field, whose ghost state keeps the dual-number path).
 template <int FLUX, int SEG, bool FO, bool KH>
 __global__ void __launch_bounds__(kBlock, MCFD_VJP_FACE_MIN_BLOCKS) k_vjp_face_rev(DevGeom g, const double* __restrict__ P,
                                                          const double* __restrict__ recon,
@@ -345,9 +348,12 @@ __device__ __forceinline__ double limiter_slope(double r) {
 // variable's gradient and extremes, limiter minimum and its first entry,
 // then the reverse of the face states, of the limiter and of the gradient.
 // One variable's state is live at a time (96 registers instead of 128 with
-// spills for all four at once), and its first four increments are kept for
-// the reverse instead of being recomputed.
-template <int LIMITER>
+// spills for all four at once), and its increments are kept for the reverse
+// instead of being recomputed.  NS > 0 compiles the cell for exactly NS
+// limiter entries (the cell order makes the count warp-uniform, so a warp of
+// triangles issues no FP64 work for a fourth entry); NS = 0 handles any
+// count, keeping the first four increments.
+template <int LIMITER, int NS>
 __device__ __forceinline__ void vjp_cell_variable(const DevGeom& g, const double* __restrict__ P,
                                                   const double* __restrict__ slot_bar, int v, double pv,
                                                   int e0, int e1, int s0, int s1, double& pb,
@@ -368,7 +374,8 @@ __device__ __forceinline__ void vjp_cell_variable(const DevGeom& g, const double
   const double tol = limiter_tolerance(pv);
   double pmax = 0.0, nmin = 0.0;
   int ps = -1, ns = -1, fs = -1;
-  double inc4[4] = {0.0, 0.0, 0.0, 0.0};
+  constexpr int kCache = NS > 0 ? NS : 4;
+  double incs[kCache];
   auto classify = [&](int s, double inc) {
     if (icmp::gt_pos(inc, tol)) {
       if (ps < 0 || icmp::lt(pmax, inc)) { pmax = inc; ps = s; }
@@ -379,16 +386,19 @@ __device__ __forceinline__ void vjp_cell_variable(const DevGeom& g, const double
     }
   };
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (s0 + k < s1) {
+  for (int k = 0; k < kCache; ++k) {
+    incs[k] = 0.0;
+    if (NS > 0 || s0 + k < s1) {
       const double2 dd = g.lim_d[s0 + k];
-      inc4[k] = mul_rn(gx, dd.x) + gy * dd.y;
-      classify(s0 + k, inc4[k]);
+      incs[k] = mul_rn(gx, dd.x) + gy * dd.y;
+      classify(s0 + k, incs[k]);
     }
   }
-  for (int s = s0 + 4; s < s1; ++s) {
-    const double2 dd = g.lim_d[s];
-    classify(s, mul_rn(gx, dd.x) + gy * dd.y);
+  if (NS == 0) {
+    for (int s = s0 + kCache; s < s1; ++s) {
+      const double2 dd = g.lim_d[s];
+      classify(s, mul_rn(gx, dd.x) + gy * dd.y);
+    }
   }
   double phi = 1.0;
   int arg = -1;
@@ -415,11 +425,13 @@ __device__ __forceinline__ void vjp_cell_variable(const DevGeom& g, const double
     gyb += qphi * dd.y;
   };
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
-    if (s0 + k < s1) face_reverse(s0 + k, inc4[k], g.lim_d[s0 + k]);
-  for (int s = s0 + 4; s < s1; ++s) {
-    const double2 dd = g.lim_d[s];
-    face_reverse(s, mul_rn(gx, dd.x) + gy * dd.y, dd);
+  for (int k = 0; k < kCache; ++k)
+    if (NS > 0 || s0 + k < s1) face_reverse(s0 + k, incs[k], g.lim_d[s0 + k]);
+  if (NS == 0) {
+    for (int s = s0 + kCache; s < s1; ++s) {
+      const double2 dd = g.lim_d[s];
+      face_reverse(s, mul_rn(gx, dd.x) + gy * dd.y, dd);
+    }
   }
   // reverse of the limiter through its minimising entry
   double extb = 0.0;
@@ -427,8 +439,11 @@ __device__ __forceinline__ void vjp_cell_variable(const DevGeom& g, const double
   if (arg >= 0) {
     const double2 dd = g.lim_d[arg];
     const int k = arg - s0;
-    const double inc = k == 0 ? inc4[0] : k == 1 ? inc4[1] : k == 2 ? inc4[2] : k == 3 ? inc4[3]
-                                                                                  : mul_rn(gx, dd.x) + gy * dd.y;
+    double inc = incs[0];
+#pragma unroll
+    for (int m = 1; m < kCache; ++m)
+      if (k == m) inc = incs[m];
+    if (NS == 0 && k >= kCache) inc = mul_rn(gx, dd.x) + gy * dd.y;
     const bool pos = icmp::gt_pos(inc, tol), neg = icmp::neg_gt_pos(inc, tol);
     if (pos || neg) {
       const double num = pos ? hi - pv : lo - pv;
@@ -465,8 +480,9 @@ __global__ void __launch_bounds__(kBlock, MCFD_VJP_CELL_MIN_BLOCKS) k_vjp_cell(D
                                                      const double* __restrict__ lambda,
                                                      const double* __restrict__ slot_bar, double ax, double ay,
                                                      double* __restrict__ pbar, double* __restrict__ ent_bar) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.n_cells) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n_cells) return;
+  const int c = g.cell_order[i];  // groups equal stencil sizes; outputs do not depend on the order
   const St4 p = ld4(P + 4 * (size_t)c);
   const double pv[4] = {p.a, p.b, p.c, p.d};
   const int e0 = g.grad_ptr[c], e1 = g.grad_ptr[c + 1];
@@ -477,8 +493,16 @@ __global__ void __launch_bounds__(kBlock, MCFD_VJP_CELL_MIN_BLOCKS) k_vjp_cell(D
     pb[0] += q.a; pb[1] += q.b; pb[2] += q.c; pb[3] += q.d;
   }
   if (!FO) {
+    if (s1 - s0 == 3) {
 #pragma unroll
-    for (int v = 0; v < 4; ++v) vjp_cell_variable<LIMITER>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar);
+      for (int v = 0; v < 4; ++v) vjp_cell_variable<LIMITER, 3>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar);
+    } else if (s1 - s0 == 4) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) vjp_cell_variable<LIMITER, 4>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar);
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) vjp_cell_variable<LIMITER, 0>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar);
+    }
   }
   if (ax != 0.0 || ay != 0.0) {  // body force (solver.py:2709-2715)
     const St4 l = ld4(lambda + 4 * (size_t)c);
