@@ -20,6 +20,12 @@ def _case(kind, n):
     if kind == "riemann":
         case, _ = riemann_case(n)
         P = smooth_primitive(len(case.mesh.cells), seed=3, amplitude=1.0)
+    elif kind == "polygons":  # pentagons and hexagons: the any-count cell reverse
+        from test_gpu_polygons import _polygon_case
+
+        case = _polygon_case()
+        P = vortex_primitive(10.0 * cell_centroids(case.mesh), mach=0.3)
+        P *= 1.0 + 0.01 * np.random.default_rng(9).standard_normal(P.shape)
     else:
         case, _ = vortex_case(n, split="half")
         P = vortex_primitive(cell_centroids(case.mesh))
@@ -27,7 +33,7 @@ def _case(kind, n):
     return case, build_geometry(case.mesh, case), P
 
 
-@pytest.mark.parametrize("kind,n", (("riemann", 20), ("vortex", 16)))
+@pytest.mark.parametrize("kind,n", (("riemann", 20), ("vortex", 16), ("polygons", 0)))
 @pytest.mark.parametrize("flux", ("Rusanov", "HLLC", "Roe"))
 @pytest.mark.parametrize("recon,limiter", (("First order", "Barth-Jespersen"), ("MUSCL linear", "Venkatakrishnan"),
                                            ("MUSCL linear", "Barth-Jespersen"), ("MUSCL linear", "Van Leer")))
