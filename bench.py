@@ -324,7 +324,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     achieved = mbytes[dominant] / (kernels[dominant]["ms_per_group"] * 1e-3) / 1e9
     traffic = None
-    fp64_pipe = alu_pipe = issue = None
+    fp64_pipe = alu_pipe = issue = fp64 = None
     tpath = ROOT / "profiles" / "ncu_summary.json"
     if tpath.exists():
         summary = json.loads(tpath.read_text())
@@ -334,6 +334,17 @@ def run_gpu(args):
         fp64_pipe = summary.get("fp64_pipe_active_pct", {}).get(dominant)
         alu_pipe = summary.get("alu_pipe_active_pct", {}).get(dominant)
         issue = summary.get("issue_active_pct", {}).get(dominant)
+        # the FP64 side of the same kernel: its FP64 instructions per cell
+        # (ncu count on the same mesh recipe and mode) over the live launch time
+        ipc = summary.get("fp64_instructions_per_cell", {}).get(dominant)
+        fpeak = summary.get("fp64_peak_ginstr_s")
+        if ipc and fpeak and args.mode == summary.get("mode") and args.workload in ("vortex1024", "vortex512",
+                                                                                     "vortex256"):
+            got = ipc * C / (kernels[dominant]["ms_per_group"] * 1e-3) / 1e9
+            fp64 = {"achieved": got, "peak": fpeak, "unit": "G FP64 thread-instructions/s", "frac": got / fpeak,
+                    "instructions_per_cell": ipc,
+                    "source": "instructions per cell from the ncu capture of this kernel on the 512^2 mesh of this "
+                              "recipe; peak = measured DFMA issue rate (" + summary.get("fp64_peak_source", "") + ")"}
     step_bytes = 3 * (mbytes["reconstruct"] + mbytes["flux"] + mbytes["gather"]) - 32 * C + mbytes["time_step"]
     roofline = {
         "bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -345,9 +356,11 @@ def run_gpu(args):
         "fp64_pipe_active_pct_ncu": fp64_pipe,
         "alu_pipe_active_pct_ncu": alu_pipe,
         "issue_active_pct_ncu": issue,
+        "fp64": fp64,
         "note": ("compute bound, not HBM bound: GB300's FP64 pipe issues ~0.5 T instr/s; divisions, square roots "
                  "and part of the products run bit-identically on the integer pipe, and ncu shows the dominant "
-                 "kernel sharing the FP64 and ALU pipes (fp64 / alu / issue percentages above)"),
+                 "kernel sharing the FP64 and ALU pipes (fp64 / alu / issue percentages above); 'fp64' is the "
+                 "kernel's FP64 instruction rate against the measured FP64 issue rate"),
     }
 
     # end to end: state in pinned host memory, H2D + step + D2H every step
