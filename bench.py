@@ -344,7 +344,7 @@ def run_gpu(args):
             fp64 = {"achieved": got, "peak": fpeak, "unit": "G FP64 thread-instructions/s", "frac": got / fpeak,
                     "instructions_per_cell": ipc,
                     "source": "instructions per cell from the ncu capture of this kernel on the 512^2 mesh of this "
-                              "recipe; peak = measured DFMA issue rate (" + summary.get("fp64_peak_source", "") + ")"}
+                              "recipe; peak: " + summary.get("fp64_peak_source", "")}
     step_bytes = 3 * (mbytes["reconstruct"] + mbytes["flux"] + mbytes["gather"]) - 32 * C + mbytes["time_step"]
     roofline = {
         "bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
