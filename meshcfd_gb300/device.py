@@ -77,81 +77,90 @@ def _check_state(x: torch.Tensor, n_cells: int, name: str) -> None:
         raise ValueError(f"{name} must be a contiguous CUDA float64 tensor of shape ({n_cells}, 4)")
 
 
+def geometry_descriptor(geometry):
+    """The `mcfd_geom_desc` of a host geometry (the reference `_Geometry`
+    arrays, plus the boundary-patch and viscous tables when present), the
+    NumPy arrays it points into (keep them alive while the descriptor is in
+    use) and the boundary-patch names.  Needs no device."""
+    keep = {}
+
+    def a(name, dtype, shape=None, src=None):
+        v = getattr(geometry, name) if src is None else src
+        arr = np.ascontiguousarray(np.asarray(v, dtype=dtype))
+        if shape is not None:
+            arr = arr.reshape(shape)
+        keep[name] = arr
+        kind = _lib.P_i64 if dtype == np.int64 else _lib.P_dbl
+        return arr.ctypes.data_as(kind) if arr.size else None, len(arr)
+
+    d = _lib.GeomDesc()
+    d.areas, n_cells = a("areas", np.float64)
+    d.face_lengths, n_faces = a("face_lengths", np.float64)
+    d.n_cells, d.n_faces = n_cells, n_faces
+    d.face_normals, _ = a("face_normals", np.float64, (-1, 2))
+    d.owners, _ = a("owners", np.int64)
+    d.neighbours, _ = a("neighbours", np.int64)
+    d.interior_faces, d.n_interior = a("interior_faces", np.int64)
+    d.periodic_faces_a, d.n_periodic = a("periodic_faces_a", np.int64)
+    d.periodic_faces_b, _ = a("periodic_faces_b", np.int64)
+    d.wall_faces, d.n_wall = a("wall_faces", np.int64)
+    d.wall_velocities, _ = a("wall_velocities", np.float64, (-1, 2))
+    d.velocity_inlet_faces, d.n_velocity_inlet = a("velocity_inlet_faces", np.int64)
+    d.velocity_inlet_states, _ = a("velocity_inlet_states", np.float64, (-1, 4))
+    d.pressure_outlet_faces, d.n_pressure_outlet = a("pressure_outlet_faces", np.int64)
+    d.pressure_outlet_pressures, _ = a("pressure_outlet_pressures", np.float64)
+    d.far_field_faces, d.n_far_field = a("far_field_faces", np.int64)
+    d.far_field_states, _ = a("far_field_states", np.float64, (-1, 4))
+    d.gradient_sources, d.n_gradient = a("gradient_sources", np.int64)
+    d.gradient_neighbours, _ = a("gradient_neighbours", np.int64)
+    d.gradient_coefficients_x, _ = a("gradient_coefficients_x", np.float64)
+    d.gradient_coefficients_y, _ = a("gradient_coefficients_y", np.float64)
+    d.limiter_cells, d.n_limiter = a("limiter_cells", np.int64)
+    d.limiter_dx, _ = a("limiter_dx", np.float64)
+    d.limiter_dy, _ = a("limiter_dy", np.float64)
+    empty_i, empty_d = np.empty(0, dtype=np.int64), np.empty(0)
+    d.parabolic_sources, d.n_parabolic = a("parabolic_sources", np.int64,
+                                           src=getattr(geometry, "parabolic_sources", empty_i))
+    d.parabolic_neighbours, _ = a("parabolic_neighbours", np.int64,
+                                  src=getattr(geometry, "parabolic_neighbours", empty_i))
+    d.parabolic_dx, _ = a("parabolic_dx", np.float64, src=getattr(geometry, "parabolic_dx", empty_d))
+    d.parabolic_dy, _ = a("parabolic_dy", np.float64, src=getattr(geometry, "parabolic_dy", empty_d))
+    bc = boundary_patches(geometry)
+    d.n_bc_patches = len(bc["names"])
+    if d.n_bc_patches:
+        keep["bc_kind"] = bc["kind"]
+        d.bc_kind = bc["kind"].ctypes.data_as(C.POINTER(C.c_int32))
+        d.bc_values, _ = a("bc_values", np.float64, src=bc["values"])
+        d.bc_offsets, _ = a("bc_offsets", np.int64, src=bc["offsets"])
+        d.bc_faces, _ = a("bc_faces", np.int64, src=bc["faces"])
+        d.bc_direction_normal, _ = a("bc_direction_normal", np.float64, src=bc["direction_normal"])
+    vt = viscous_tables(geometry, bc) \
+        if hasattr(geometry, "diffusive_boundary_faces") and hasattr(geometry, "gradient_dx") else None
+    if vt is not None:
+        d.gradient_dx, _ = a("gradient_dx", np.float64)
+        d.gradient_dy, _ = a("gradient_dy", np.float64)
+        d.diffusive_faces, d.n_diffusive = a("diffusive_faces", np.int64, src=vt["faces"])
+        for name in ("kind", "thermal", "inlet"):
+            arr = vt[name]
+            keep["diffusive_" + name] = arr
+            setattr(d, "diffusive_" + name, arr.ctypes.data_as(C.POINTER(C.c_int32)) if arr.size else None)
+        d.diffusive_value, _ = a("diffusive_value", np.float64, src=vt["value"])
+        d.diffusive_normal_distance, _ = a("diffusive_nd", np.float64, src=vt["nd"])
+        d.diffusive_ghost_offset, _ = a("diffusive_ghost", np.float64, src=vt["ghost"])
+        d.diffusive_offset, _ = a("diffusive_offset", np.float64, src=vt["offset"])
+        d.interior_distance, _ = a("interior_distance", np.float64, src=vt["interior_distance"])
+        d.periodic_distance, _ = a("periodic_distance", np.float64, src=vt["periodic_distance"])
+    return d, keep, bc["names"]
+
+
 class DeviceGeometry:
     """Packed device geometry + workspace for one mesh (one CUDA device)."""
 
     def __init__(self, geometry, device=None):
         self.lib = _lib.native()
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else torch.device(device).index or 0)
-        keep = {}
-
-        def a(name, dtype, shape=None, src=None):
-            v = getattr(geometry, name) if src is None else src
-            arr = np.ascontiguousarray(np.asarray(v, dtype=dtype))
-            if shape is not None:
-                arr = arr.reshape(shape)
-            keep[name] = arr
-            kind = _lib.P_i64 if dtype == np.int64 else _lib.P_dbl
-            return arr.ctypes.data_as(kind) if arr.size else None, len(arr)
-
-        d = _lib.GeomDesc()
-        d.areas, n_cells = a("areas", np.float64)
-        d.face_lengths, n_faces = a("face_lengths", np.float64)
-        d.n_cells, d.n_faces = n_cells, n_faces
-        d.face_normals, _ = a("face_normals", np.float64, (-1, 2))
-        d.owners, _ = a("owners", np.int64)
-        d.neighbours, _ = a("neighbours", np.int64)
-        d.interior_faces, d.n_interior = a("interior_faces", np.int64)
-        d.periodic_faces_a, d.n_periodic = a("periodic_faces_a", np.int64)
-        d.periodic_faces_b, _ = a("periodic_faces_b", np.int64)
-        d.wall_faces, d.n_wall = a("wall_faces", np.int64)
-        d.wall_velocities, _ = a("wall_velocities", np.float64, (-1, 2))
-        d.velocity_inlet_faces, d.n_velocity_inlet = a("velocity_inlet_faces", np.int64)
-        d.velocity_inlet_states, _ = a("velocity_inlet_states", np.float64, (-1, 4))
-        d.pressure_outlet_faces, d.n_pressure_outlet = a("pressure_outlet_faces", np.int64)
-        d.pressure_outlet_pressures, _ = a("pressure_outlet_pressures", np.float64)
-        d.far_field_faces, d.n_far_field = a("far_field_faces", np.int64)
-        d.far_field_states, _ = a("far_field_states", np.float64, (-1, 4))
-        d.gradient_sources, d.n_gradient = a("gradient_sources", np.int64)
-        d.gradient_neighbours, _ = a("gradient_neighbours", np.int64)
-        d.gradient_coefficients_x, _ = a("gradient_coefficients_x", np.float64)
-        d.gradient_coefficients_y, _ = a("gradient_coefficients_y", np.float64)
-        d.limiter_cells, d.n_limiter = a("limiter_cells", np.int64)
-        d.limiter_dx, _ = a("limiter_dx", np.float64)
-        d.limiter_dy, _ = a("limiter_dy", np.float64)
-        empty_i, empty_d = np.empty(0, dtype=np.int64), np.empty(0)
-        d.parabolic_sources, d.n_parabolic = a("parabolic_sources", np.int64,
-                                               src=getattr(geometry, "parabolic_sources", empty_i))
-        d.parabolic_neighbours, _ = a("parabolic_neighbours", np.int64,
-                                      src=getattr(geometry, "parabolic_neighbours", empty_i))
-        d.parabolic_dx, _ = a("parabolic_dx", np.float64, src=getattr(geometry, "parabolic_dx", empty_d))
-        d.parabolic_dy, _ = a("parabolic_dy", np.float64, src=getattr(geometry, "parabolic_dy", empty_d))
-        bc = boundary_patches(geometry)
-        self.bc_patch_names = bc["names"]
-        d.n_bc_patches = len(bc["names"])
-        if d.n_bc_patches:
-            keep["bc_kind"] = bc["kind"]
-            d.bc_kind = bc["kind"].ctypes.data_as(C.POINTER(C.c_int32))
-            d.bc_values, _ = a("bc_values", np.float64, src=bc["values"])
-            d.bc_offsets, _ = a("bc_offsets", np.int64, src=bc["offsets"])
-            d.bc_faces, _ = a("bc_faces", np.int64, src=bc["faces"])
-            d.bc_direction_normal, _ = a("bc_direction_normal", np.float64, src=bc["direction_normal"])
-        vt = viscous_tables(geometry, bc) \
-            if hasattr(geometry, "diffusive_boundary_faces") and hasattr(geometry, "gradient_dx") else None
-        if vt is not None:
-            d.gradient_dx, _ = a("gradient_dx", np.float64)
-            d.gradient_dy, _ = a("gradient_dy", np.float64)
-            d.diffusive_faces, d.n_diffusive = a("diffusive_faces", np.int64, src=vt["faces"])
-            for name in ("kind", "thermal", "inlet"):
-                arr = vt[name]
-                keep["diffusive_" + name] = arr
-                setattr(d, "diffusive_" + name, arr.ctypes.data_as(C.POINTER(C.c_int32)) if arr.size else None)
-            d.diffusive_value, _ = a("diffusive_value", np.float64, src=vt["value"])
-            d.diffusive_normal_distance, _ = a("diffusive_nd", np.float64, src=vt["nd"])
-            d.diffusive_ghost_offset, _ = a("diffusive_ghost", np.float64, src=vt["ghost"])
-            d.diffusive_offset, _ = a("diffusive_offset", np.float64, src=vt["offset"])
-            d.interior_distance, _ = a("interior_distance", np.float64, src=vt["interior_distance"])
-            d.periodic_distance, _ = a("periodic_distance", np.float64, src=vt["periodic_distance"])
+        d, keep, self.bc_patch_names = geometry_descriptor(geometry)
+        n_cells = int(d.n_cells)
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             rc = self.lib.mcfd_geom_create(C.byref(d), C.byref(handle))

@@ -96,6 +96,43 @@ def test_host_geometry_helpers_reject_degenerate_cells():
         native.face_geometry(np.array([[0, 0]]), points, np.zeros((1, 2)), np.array([0]))
 
 
+MALFORMED = {
+    # name: (mutation of the descriptor's arrays / fields, expected return code)
+    "no cells": (lambda d, k: setattr(d, "n_cells", 0), 1),
+    "null areas": (lambda d, k: setattr(d, "areas", None), 1),
+    "owner out of range": (lambda d, k: k["owners"].__setitem__(0, d.n_cells), 4),
+    "neighbour out of range": (lambda d, k: k["neighbours"].__setitem__(k["interior_faces"][0], d.n_cells), 4),
+    "interior faces unsorted": (lambda d, k: k["interior_faces"].__setitem__(slice(0, 2), k["interior_faces"][1::-1]), 4),
+    "far-field face with a neighbour": (lambda d, k: k["far_field_faces"].__setitem__(0, k["interior_faces"][0]), 4),
+    "gradient neighbour negative": (lambda d, k: k["gradient_neighbours"].__setitem__(0, -1), 4),
+    "limiter cell out of range": (lambda d, k: k["limiter_cells"].__setitem__(0, d.n_cells), 4),
+    "limiter count": (lambda d, k: setattr(d, "n_limiter", d.n_limiter - 1), 4),
+    "zero area": (lambda d, k: k["areas"].__setitem__(3, 0.0), 4),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MALFORMED))
+def test_geometry_create_rejects_malformed_descriptors(name):
+    """mcfd_geom_create validates every index before it touches the device,
+    so no kernel can read out of bounds; malformed descriptors return
+    MCFD_E_ARG (1) or MCFD_E_GEOMETRY (4) without a GPU."""
+    import ctypes as C
+
+    from meshcfd_gb300 import _lib
+    from meshcfd_gb300.device import geometry_descriptor
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import riemann_case
+
+    case, _ = riemann_case(6)
+    desc, keep, _ = geometry_descriptor(build_geometry(case.mesh, case))
+    assert desc.n_far_field > 0 and desc.n_interior > 1
+    mutate, expected = MALFORMED[name]
+    mutate(desc, keep)
+    handle = C.c_void_p()
+    assert _lib.native().mcfd_geom_create(C.byref(desc), C.byref(handle)) == expected
+    assert handle.value is None
+
+
 def test_config_mapping_rejects_unsupported_models():
     from meshcfd_gb300.device import make_config
     from meshcfd_gb300.model import NumericalSettings
