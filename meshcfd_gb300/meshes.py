@@ -377,15 +377,12 @@ def ogrid_case(n_theta=1024, n_r=512, radius=0.5, half_width=10.0, growth=None, 
     ip = (i + 1) % n_theta
     quad = np.column_stack((j * n_theta + i, j * n_theta + ip, (j + 1) * n_theta + ip, (j + 1) * n_theta + i))
     cells = CellArray(np.arange(0, 4 * len(quad) + 1, 4, dtype=np.int64), quad.ravel().astype(np.int64))
-    inner_ids = set(range(n_theta))
-
     def classify(a, b):
         ra = np.linalg.norm(a, axis=1)
         ids = np.where(ra < 0.5 * (radius + half_width), 0, 1)
         return ids, ("cylinder", "farfield")
 
     mesh = build_faces(points, cells, classify)
-    del inner_ids
     case = Case(name=f"ogrid{n_theta}x{n_r}", mesh=mesh)
     gamma = case.numerics.gamma
     u = mach * math.sqrt(gamma)
@@ -402,3 +399,67 @@ def ogrid_case(n_theta=1024, n_r=512, radius=0.5, half_width=10.0, growth=None, 
     num.time_step_mode, num.end_time, num.residual_tolerance = "Global fixed", 1.0e30, 1e-300
     P = np.tile((1.0, u, 0.0, 1.0), (len(mesh.cells), 1))
     return case, P
+
+
+def bump_case(nx=512, ny=256, height=0.1, seed=1, stretch=1.05, jitter=0.1, mach=0.5, x0=-1.0, x1=2.0, top=1.0):
+    """Channel over a circular-arc bump: x in [x0, x1] with the arc of chord 1
+    (x from 0 to 1) and ``height`` on the lower wall, the upper boundary at
+    y = ``top``; nx x ny quads, rows spaced geometrically from the lower wall
+    (ratio ``stretch``), interior points jittered by up to ``jitter`` of the
+    local spacing (seeded).  Slip wall below, far field (free stream at Mach
+    ``mach`` along x, rho = 1, p = 1) at the inflow and on top, pressure
+    outlet (p = 1) at the outflow.  Settings: Roe, MUSCL linear with
+    Barth-Jespersen, implicit Euler with local time steps at CFL 200,
+    GMRES(30) to 1e-3 with LU-SGS."""
+    rng = np.random.default_rng(seed)
+    xs = x0 + (x1 - x0) * np.arange(nx + 1) / nx
+    xs[-1] = x1
+    radius = (0.25 + height * height) / (2.0 * height)
+    on_arc = (xs > 0.0) & (xs < 1.0)
+    yb = np.zeros(nx + 1)
+    yb[on_arc] = np.sqrt(radius * radius - (xs[on_arc] - 0.5) ** 2) - (radius - height)
+    t = (stretch ** np.arange(ny + 1) - 1.0) / (stretch**ny - 1.0)
+    t[-1] = 1.0
+    X = np.broadcast_to(xs, (ny + 1, nx + 1)).copy()
+    Y = yb[None, :] + t[:, None] * (top - yb)[None, :]
+    Y[-1, :] = top
+    if jitter:
+        dy = np.diff(Y, axis=0)
+        h = np.minimum(np.minimum(dy[:-1], dy[1:]), (x1 - x0) / nx)[:, 1:-1]
+        shift = rng.uniform(-jitter, jitter, size=(ny - 1, nx - 1, 2)) * h[:, :, None]
+        X[1:-1, 1:-1] += shift[:, :, 0]
+        Y[1:-1, 1:-1] += shift[:, :, 1]
+    points = np.column_stack((X.ravel(), Y.ravel()))
+    j, i = np.divmod(np.arange(nx * ny), nx)
+    bl = j * (nx + 1) + i
+    quad = np.column_stack((bl, bl + 1, bl + nx + 2, bl + nx + 1))
+    cells = CellArray(np.arange(0, 4 * len(quad) + 1, 4, dtype=np.int64), quad.ravel().astype(np.int64))
+
+    def classify(a, b):
+        ids = np.zeros(len(a), dtype=np.int64)  # the lower wall
+        ids[(a[:, 0] == x0) & (b[:, 0] == x0)] = 1
+        ids[(a[:, 1] == top) & (b[:, 1] == top)] = 2
+        ids[(a[:, 0] == x1) & (b[:, 0] == x1)] = 3
+        return ids, ("wall", "inflow", "top", "outflow")
+
+    mesh = build_faces(points, cells, classify)
+    case = Case(name=f"bump{nx}x{ny}", mesh=mesh)
+    u = mach * math.sqrt(case.numerics.gamma)
+    for cond in case.boundary_conditions:
+        if cond.patch_name == "wall":
+            cond.kind = "Wall"
+            cond.mechanical_condition = "Slip"
+        elif cond.patch_name == "outflow":
+            cond.kind = "Pressure Outlet"
+            cond.values = {"pressure": 1.0}
+        else:
+            cond.kind = "Far Field"
+            cond.values = {"density": 1.0, "velocity_x": u, "velocity_y": 0.0, "pressure": 1.0}
+    num = case.numerics
+    num.flux, num.reconstruction, num.limiter = "Roe", "MUSCL linear", "Barth-Jespersen"
+    num.time_integration, num.cfl, num.time_step_mode = "Implicit Euler", 200.0, "Local (steady)"
+    num.gmres_tolerance, num.gmres_krylov_dimension, num.implicit_preconditioner = 1e-3, 30, "LU-SGS"
+    num.end_time, num.residual_tolerance = 1.0e30, 1e-300
+    P = np.tile((1.0, u, 0.0, 1.0), (len(mesh.cells), 1))
+    return case, P
+

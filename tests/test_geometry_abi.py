@@ -54,6 +54,23 @@ def test_workload_mesh_sizes():
     assert len(v.mesh.cells) == 32 * 32 + 32 * 32 // 2
 
 
+def test_bump_channel_mesh():
+    """The bump-channel configuration at full size: 512 x 256 quads, the arc's
+    crest at 10 % of the chord, wall / far-field / outlet face counts, every
+    cell of positive area (the rows stretched by 1.05 toward the wall)."""
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import bump_case
+
+    case, P = bump_case()
+    g = build_geometry(case.mesh, case)
+    assert len(g.areas) == 131072 and P.shape == (131072, 4)
+    assert (len(g.wall_faces), len(g.far_field_faces), len(g.pressure_outlet_faces)) == (512, 768, 256)
+    assert float(np.min(g.areas)) > 0.0
+    points = np.asarray(case.mesh.points)
+    assert abs(points[:513, 1].max() - 0.1) < 1e-5  # the wall row; x = 0.5 is a grid line
+    assert case.numerics.flux == "Roe" and case.numerics.limiter == "Barth-Jespersen"
+
+
 def test_periodic_matching_rejects_mismatch():
     from meshcfd_gb300.errors import SolverError
     from meshcfd_gb300.geometry import build_geometry
