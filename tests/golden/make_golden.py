@@ -36,6 +36,7 @@ sys.path.insert(0, str(HERE.parents[1]))
 from reference_shim import import_reference, reference_case  # noqa: E402
 
 from meshcfd_gb300.meshes import (  # noqa: E402
+    bump_case,
     box_mesh,
     cell_centroids,
     periodic_case,
@@ -720,6 +721,9 @@ def main(only=None):
     if only == "bc":
         bc_fixture("pinlet", ref)
         bc_fixture("massflow", ref)
+        return None
+    if only == "bump":  # the implicit configuration's mesh recipe: slip wall, far field, pressure outlet
+        residual_fixture("bump", bump_case(16, 8)[0], ref)
         return None
     riemann, riemann_p = riemann_case(16)
     residual_fixture("riemann16", riemann, ref)
