@@ -39,6 +39,7 @@ from meshcfd_gb300.meshes import (  # noqa: E402
     bump_case,
     box_mesh,
     cell_centroids,
+    ogrid_case,
     periodic_case,
     riemann_case,
     smooth_primitive,
@@ -724,6 +725,9 @@ def main(only=None):
         return None
     if only == "bump":  # the implicit configuration's mesh recipe: slip wall, far field, pressure outlet
         residual_fixture("bump", bump_case(16, 8)[0], ref)
+        return None
+    if only == "ogrid":  # the adjoint configuration's mesh recipe: curved slip wall, far field
+        residual_fixture("ogrid", ogrid_case(32, 16)[0], ref)
         return None
     riemann, riemann_p = riemann_case(16)
     residual_fixture("riemann16", riemann, ref)

@@ -8,7 +8,7 @@ from conftest import load_fixture, residual_keys, settings_for, solve_settings
 from oracle.oracle import Oracle
 
 RESIDUAL_FIXTURES = ("residual_riemann16.npz", "residual_periodic_mixed.npz", "residual_channel.npz",
-                     "residual_bump.npz")
+                     "residual_bump.npz", "residual_ogrid.npz")
 SOLVE_FIXTURES = ("solve_riemann16_euler.npz", "solve_vortex12_rk3.npz", "solve_channel_rk4_local.npz",
                   "solve_channel_rk2_vanleer.npz")
 
