@@ -67,6 +67,66 @@ def test_uniform_periodic_flow_is_preserved(backend, request, cells, flux, integ
     np.testing.assert_allclose(P, np.tile(state, (len(P), 1)), rtol=1e-12, atol=1e-12)
 
 
+def _boundary_case(cells, kinds):
+    """The box of ``cells`` with its bottom / right / top / left patches set
+    to ``kinds`` (kind, values) and no periodic pairs."""
+    from meshcfd_gb300.meshes import box_mesh
+    from meshcfd_gb300.model import Case
+
+    case = Case(name="box", mesh=box_mesh(*cells))
+    for condition, (kind, values) in zip(case.boundary_conditions, kinds):
+        condition.kind, condition.values = kind, dict(values)
+    s = case.numerics
+    s.gas_constant, s.end_time, s.max_iterations, s.residual_tolerance = 1.0, 0.01, 10000, 1e-300
+    return case
+
+
+INLET = ("Velocity Inlet", {"density": 1.0, "velocity_x": 1.0, "velocity_y": 0.0, "temperature": 1.0})
+WALL = ("Wall", {})
+
+
+@pytest.mark.parametrize("backend,cells", UNIFORM_MESHES)
+@pytest.mark.parametrize("flux", FLUXES)
+def test_velocity_inlet_and_pressure_outlet_preserve_matching_uniform_flow(backend, request, cells, flux):
+    """test_solver.py:877-908: walls below and above, a pressure outlet
+    (p = 1) on the right and a velocity inlet (rho = 1, u = 1, R T = 1) on
+    the left keep the matching uniform state to 1e-12 up to t = 0.01."""
+    case = _boundary_case(cells, (WALL, ("Pressure Outlet", {"pressure": 1.0}), WALL, INLET))
+    case.numerics.flux = flux
+    state = (1.0, 1.0, 0.0, 1.0)
+    _, U, _, _ = _march(backend, request, case, case.numerics, np.tile(state, (cells[0] * cells[1], 1)))
+    np.testing.assert_allclose(_primitive(U, 1.4), np.tile(state, (len(U), 1)), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("backend,cells", UNIFORM_MESHES)
+def test_pressure_outlet_applies_configured_static_pressure(backend, request, cells):
+    """test_solver.py:911-931: a fluid at rest (p = 1) next to an outlet at
+    p = 0.8 starts to move towards it in the first step."""
+    case = _boundary_case(cells, (WALL, ("Pressure Outlet", {"pressure": 0.8}), WALL,
+                                  ("Velocity Inlet", {"density": 1.0, "velocity_x": 0.0, "velocity_y": 0.0,
+                                                      "temperature": 1.0})))
+    case.numerics.max_iterations = 1
+    _, U, _, steps = _march(backend, request, case, case.numerics, np.tile((1.0, 0.0, 0.0, 1.0),
+                                                                           (cells[0] * cells[1], 1)))
+    assert steps == 1
+    nx, ny = cells
+    outlet_column = _primitive(U, 1.4)[nx - 1::nx, 1]  # the cells along the right boundary
+    assert len(outlet_column) == ny and (outlet_column > 0.0).all()
+
+
+@pytest.mark.parametrize("backend,cells", UNIFORM_MESHES)
+@pytest.mark.parametrize("flux", FLUXES)
+def test_far_field_preserves_matching_uniform_flow(backend, request, cells, flux):
+    """test_solver.py:1119-1146: far field on every side with the interior's
+    uniform state keeps it to 1e-12 up to t = 0.01."""
+    far = ("Far Field", {"density": 1.0, "velocity_x": 0.2, "velocity_y": -0.1, "pressure": 1.0})
+    case = _boundary_case(cells, (far, far, far, far))
+    case.numerics.flux = flux
+    state = (1.0, 0.2, -0.1, 1.0)
+    _, U, _, _ = _march(backend, request, case, case.numerics, np.tile(state, (cells[0] * cells[1], 1)))
+    np.testing.assert_allclose(_primitive(U, 1.4), np.tile(state, (len(U), 1)), rtol=1e-12, atol=1e-12)
+
+
 @pytest.mark.parametrize("backend", BACKENDS)
 @pytest.mark.parametrize("flux", FLUXES)
 @pytest.mark.parametrize("integrator", INTEGRATORS)
