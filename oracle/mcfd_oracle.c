@@ -629,6 +629,16 @@ static int far_field(const double* in, const double* far, const double* n, doubl
   return 0;
 }
 
+/* _far_field_boundary_states (solver.py:4350-4409) for n rows of interior
+ * primitive states, far-field states and unit normals; OR of the rows'
+ * status bits. */
+int orc_far_field_states(int64_t n, const double* in, const double* far, const double* normals, double gamma,
+                         double* ext) {
+  int status = 0;
+  for (int64_t i = 0; i < n; ++i) status |= far_field(in + 4 * i, far + 4 * i, normals + 2 * i, gamma, ext + 4 * i);
+  return status;
+}
+
 /* NumPy's pairwise summation of a contiguous float64 array (np.sum). */
 static double pairwise(const double* a, int64_t n) {
   if (n < 8) {

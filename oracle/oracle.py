@@ -99,7 +99,21 @@ def lib():
         _lib.orc_linear_gradients_and_factors.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD]
         _lib.orc_parabolic_reconstruction.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD, PD]
         _lib.orc_bc_states.argtypes = [C.POINTER(OrcGeom), C.c_int64, PD, C.c_double, C.c_double, PD]
+        _lib.orc_far_field_states.argtypes = [C.c_int64, PD, PD, PD, C.c_double, PD]
     return _lib
+
+
+def far_field_states(interior, far_field, normals, gamma):
+    """_far_field_boundary_states (solver.py:4350-4409): exterior primitive
+    states of far-field faces from interior states, far-field states and
+    unit normals, each (n, 4) / (n, 2)."""
+    interior = np.ascontiguousarray(interior, dtype=np.float64)
+    far_field = np.ascontiguousarray(far_field, dtype=np.float64)
+    normals = np.ascontiguousarray(normals, dtype=np.float64)
+    ext = np.empty_like(interior)
+    _raise(lib().orc_far_field_states(len(interior), interior.ctypes.data_as(PD), far_field.ctypes.data_as(PD),
+                                      normals.ctypes.data_as(PD), gamma, ext.ctypes.data_as(PD)))
+    return ext
 
 
 class OracleError(ValueError):

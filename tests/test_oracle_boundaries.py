@@ -119,3 +119,21 @@ def test_inlets_reject_direction_pointing_out_of_domain(kind):
     orc = Oracle(build_geometry(case.mesh, case))
     with pytest.raises(OracleError, match="direction must point into the domain"):
         orc.boundary_states(0, np.array(((1.0, 0.0, 0.0, 1.0),)), 1.4, 1.0)
+
+
+def test_far_field_characteristics_select_incoming_and_outgoing_information():
+    """test_solver.py:1149-1166 on the oracle: supersonic outflow keeps the
+    interior state, supersonic inflow takes the far-field state, subsonic
+    outflow takes the normal velocity from the two Riemann invariants and the
+    tangential velocity and entropy from the interior."""
+    from oracle.oracle import far_field_states
+
+    interior = np.array(((1.0, 3.0, 0.0, 1.0), (1.0, 0.2, 0.0, 1.0), (1.0, -3.0, 0.0, 1.0)))
+    far = np.array(((2.0, 0.0, 0.0, 2.0), (2.0, 0.4, 0.0, 2.0), (2.0, 0.0, 0.0, 2.0)))
+    normals = np.array(((1.0, 0.0), (1.0, 0.0), (1.0, 0.0)))
+    ext = far_field_states(interior, far, normals, 1.4)
+    np.testing.assert_array_equal(ext[0], interior[0])
+    np.testing.assert_array_equal(ext[2], far[2])
+    assert ext[1, 1] == pytest.approx(0.3)
+    assert ext[1, 2] == pytest.approx(interior[1, 2])
+    assert ext[1, 3] / ext[1, 0] ** 1.4 == pytest.approx(interior[1, 3] / interior[1, 0] ** 1.4)
