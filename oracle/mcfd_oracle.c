@@ -629,6 +629,24 @@ static int far_field(const double* in, const double* far, const double* n, doubl
   return 0;
 }
 
+/* The face fluxes of n rows of left / right primitive states and unit
+ * normals: kind 0 Rusanov (euler.py:80-93), 1 HLLC (euler.py:96-166),
+ * 2 Roe (euler.py:169-262), 3 the compiled kernel's HLLC
+ * (_kernels.py:71-160); OR of the rows' status bits. */
+int orc_face_fluxes(int kind, int64_t n, const double* L, const double* R, const double* normals, double gamma,
+                    double* out) {
+  int status = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double *l = L + 4 * i, *r = R + 4 * i, *nrm = normals + 2 * i;
+    double* o = out + 4 * i;
+    if (kind == 0) status |= rusanov(l, r, nrm, gamma, o);
+    else if (kind == 1) status |= hllc_numpy(l, r, nrm, gamma, o);
+    else if (kind == 2) status |= roe(l, r, nrm, gamma, o);
+    else kernel_hllc(l, r, nrm, gamma, o);
+  }
+  return status;
+}
+
 /* _far_field_boundary_states (solver.py:4350-4409) for n rows of interior
  * primitive states, far-field states and unit normals; OR of the rows'
  * status bits. */

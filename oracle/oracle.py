@@ -100,7 +100,23 @@ def lib():
         _lib.orc_parabolic_reconstruction.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD, PD]
         _lib.orc_bc_states.argtypes = [C.POINTER(OrcGeom), C.c_int64, PD, C.c_double, C.c_double, PD]
         _lib.orc_far_field_states.argtypes = [C.c_int64, PD, PD, PD, C.c_double, PD]
+        _lib.orc_face_fluxes.argtypes = [C.c_int, C.c_int64, PD, PD, PD, C.c_double, PD]
     return _lib
+
+
+FACE_FLUXES = {"Rusanov": 0, "HLLC": 1, "Roe": 2, "HLLC kernel": 3}
+
+
+def face_fluxes(kind, left, right, normals, gamma):
+    """The numerical flux ``kind`` (a key of FACE_FLUXES) of rows of left /
+    right primitive states (n, 4) across unit normals (n, 2)."""
+    left = np.ascontiguousarray(left, dtype=np.float64)
+    right = np.ascontiguousarray(right, dtype=np.float64)
+    normals = np.ascontiguousarray(normals, dtype=np.float64)
+    out = np.empty_like(left)
+    _raise(lib().orc_face_fluxes(FACE_FLUXES[kind], len(left), left.ctypes.data_as(PD), right.ctypes.data_as(PD),
+                                 normals.ctypes.data_as(PD), gamma, out.ctypes.data_as(PD)))
+    return out
 
 
 def far_field_states(interior, far_field, normals, gamma):

@@ -729,6 +729,8 @@ def main(only=None):
     if only == "ogrid":  # the adjoint configuration's mesh recipe: curved slip wall, far field
         residual_fixture("ogrid", ogrid_case(32, 16)[0], ref)
         return None
+    if only == "fluxes":
+        return fluxes_fixture(ref)
     riemann, riemann_p = riemann_case(16)
     residual_fixture("riemann16", riemann, ref)
     residual_fixture("periodic_mixed", periodic_case(8, 6, split="half", jitter=0.25, seed=2), ref)
@@ -763,6 +765,26 @@ def main(only=None):
     solve_fixture("channel_rk2_vanleer", chan, cp,
                   {"flux": "HLLC", "reconstruction": "MUSCL linear", "limiter": "Van Leer",
                    "time_integration": "Explicit RK2", "cfl": 0.6, "acceleration_x": 0.2}, 8, ref)
+
+
+def fluxes_fixture(ref, n=1000, seed=11):
+    """The reference's numerical fluxes (euler.numerical_flux) of random
+    face states: subsonic and supersonic, both directions, random unit
+    normals."""
+    rng = np.random.default_rng(seed)
+
+    def states():
+        return np.column_stack((rng.uniform(0.3, 2.0, n), rng.uniform(-3.0, 3.0, n), rng.uniform(-3.0, 3.0, n),
+                                rng.uniform(0.3, 2.0, n)))
+
+    L, R = states(), states()
+    theta = rng.uniform(0.0, 2.0 * np.pi, n)
+    N = np.column_stack((np.cos(theta), np.sin(theta)))
+    out = {"L": L, "R": R, "normals": N}
+    for kind in ("Rusanov", "HLLC", "Roe"):
+        out[kind] = ref.euler.numerical_flux(L, R, N, 1.4, kind)
+    np.savez_compressed(HERE / "fluxes.npz", **out)
+    print("fluxes", n, "faces")
 
 
 def parabolic_main(ref):
