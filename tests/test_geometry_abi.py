@@ -116,6 +116,8 @@ def test_host_geometry_helpers_reject_degenerate_cells():
 MALFORMED = {
     # name: (mutation of the descriptor's arrays / fields, expected return code)
     "no cells": (lambda d, k: setattr(d, "n_cells", 0), 1),
+    "cells beyond the 2^30 index limit": (lambda d, k: setattr(d, "n_cells", (1 << 30) + 1), 1),
+    "faces beyond the 2^30 index limit": (lambda d, k: setattr(d, "n_faces", (1 << 30) + 1), 1),
     "null areas": (lambda d, k: setattr(d, "areas", None), 1),
     "owner out of range": (lambda d, k: k["owners"].__setitem__(0, d.n_cells), 4),
     "neighbour out of range": (lambda d, k: k["neighbours"].__setitem__(k["interior_faces"][0], d.n_cells), 4),
