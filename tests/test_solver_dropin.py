@@ -101,7 +101,7 @@ def test_patched_functions_match_the_oracle(cuda_device):
 
 @pytest.mark.gpu
 def test_patched_implicit_step_matches_the_oracle(cuda_device):
-    """One implicit-Euler step of the bump-channel recipe (16 x 8) through
+    """One implicit-Euler step of the bump-channel recipe (32 x 16) through
     the patched `_implicit_euler_step`, against the oracle's restatement with
     SciPy's GMRES."""
     from meshcfd_gb300 import dropin
@@ -110,7 +110,7 @@ def test_patched_implicit_step_matches_the_oracle(cuda_device):
     from oracle.implicit import ImplicitOracle
     from oracle.oracle import Oracle
 
-    case, P = bump_case(16, 8)
+    case, P = bump_case(32, 16)
     s = case.numerics
     g = build_geometry(case.mesh, case)
     orc = Oracle(g)
