@@ -71,6 +71,23 @@ def test_bump_channel_mesh():
     assert case.numerics.flux == "Roe" and case.numerics.limiter == "Barth-Jespersen"
 
 
+def test_ogrid_mesh():
+    """The adjoint configuration's O-grid at full size: 1024 x 512 quads
+    between the cylinder (radius 0.5) and the square [-10, 10]^2, 1,024 wall
+    and 1,024 far-field faces, every cell of positive area."""
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import ogrid_case
+
+    case, P = ogrid_case(1024, 512)
+    g = build_geometry(case.mesh, case)
+    assert len(g.areas) == 524288 and P.shape == (524288, 4)
+    assert (len(g.wall_faces), len(g.far_field_faces)) == (1024, 1024)
+    assert float(np.min(g.areas)) > 0.0
+    points = np.asarray(case.mesh.points)
+    np.testing.assert_allclose(np.linalg.norm(points[:1024], axis=1), 0.5, rtol=1e-15)
+    np.testing.assert_array_equal(np.abs(points[-1024:]).max(axis=1), 10.0)
+
+
 def test_periodic_matching_rejects_mismatch():
     from meshcfd_gb300.errors import SolverError
     from meshcfd_gb300.geometry import build_geometry
