@@ -53,7 +53,8 @@ def parse(argv=None):
     ap.add_argument("--graph-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-steps", type=int, default=5, help="RK3 steps of the CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=10,
+                    help="RK3 steps of the CPU baseline sample (about 12 s on one Grace core)")
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--mode", choices=("fast", "exact", "fma"), default="fast",
                     help="exact: reference operation order, bit-exact; fast: exact arithmetic with the "
