@@ -73,6 +73,18 @@ WORKLOADS = {
 }
 
 
+def _sample_case(name, n):
+    """(case, settings, geometry, initial primitive) of workload ``name``,
+    at ``n`` x ``n`` quads when given."""
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import cell_centroids, vortex_case, vortex_primitive
+
+    w = WORKLOADS[name]
+    case, _ = vortex_case(n or w["n"], split=w["split"])
+    g = build_geometry(case.mesh, case)
+    return case, case.numerics, g, vortex_primitive(cell_centroids(case.mesh))
+
+
 def make_workload(name):
     from meshcfd_gb300.geometry import build_geometry
     from meshcfd_gb300.meshes import cell_centroids, vortex_case, vortex_primitive
@@ -190,12 +202,35 @@ def cpu_oracle_rate(g, settings, P0, steps):
     return len(g.areas) * steps / dt, dt
 
 
+# CPU time the reference arm may spend on its timed and warm-up steps, at a
+# conservative one-core rate of the reference path (cell-updates/s)
+REFERENCE_BUDGET_S, REFERENCE_RATE = 180.0, 1.0e6
+
+
+def reference_sample(name, steps, warmup):
+    """The workload the reference arm times: the named one, or the same
+    recipe at the largest smaller size whose ``steps + warmup`` full RK3
+    steps fit the CPU budget (the per-cell rate does not depend on the size
+    once the mesh exceeds the caches)."""
+    w = WORKLOADS[name]
+    for n in (w["n"], 512, 256):
+        if n > w["n"]:
+            continue
+        cells = n * n * (3 if w["split"] == "half" else 4) // 2
+        if cells * (steps + warmup) / REFERENCE_RATE <= REFERENCE_BUDGET_S:
+            break
+    return n
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     case, settings, g, P0, config = make_workload(args.workload)
     steps, warm = args.steps, args.warmup
+    n = reference_sample(args.workload, steps, warm)
+    if n != WORKLOADS[args.workload]["n"]:
+        case, settings, g, P0 = _sample_case(args.workload, n)
     from oracle.oracle import Oracle
 
     orc = Oracle(g)
@@ -211,8 +246,9 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded vortex)",
         "config": config,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"{steps} RK3 steps of the full {len(g.areas)}-cell workload "
-                                   "(oracle: single-threaded C restatement of the reference path; "
+                         "sample": f"{steps} RK3 steps of the same recipe at {n}x{n} quads ({len(g.areas)} "
+                                   f"cells{'' if n == WORKLOADS[args.workload]['n'] else ', reduced to fit ~3 min of CPU time'})"
+                                   " (oracle: single-threaded C restatement of the reference path; "
                                    "the reference itself is single-threaded NumPy/Numba)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

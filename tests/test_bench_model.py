@@ -39,3 +39,16 @@ def test_mixed_vortex_mesh_moves_about_2142_bytes_per_cell_update():
     _, step, n = _step_bytes_per_cell(build_geometry(case.mesh, case))
     assert np.isclose(n["F"] / n["C"], 5.0 / 3.0)
     assert abs(step - 2142) <= 1.0
+
+
+def test_reference_arm_sample_fits_its_cpu_budget():
+    """The reference arm times the full mesh when its steps fit ~3 min of
+    one core, else the same recipe at 512^2 or 256^2 quads."""
+    import bench
+
+    assert bench.reference_sample("vortex1024", 100, 3) == 1024
+    assert bench.reference_sample("vortex1024", 300, 3) == 512
+    assert bench.reference_sample("vortex1024", 1000, 3) == 256
+    case, settings, g, P0 = bench._sample_case("vortex1024", 16)
+    assert len(g.areas) == 16 * 16 * 3 // 2 == len(P0)
+    assert settings.flux == "HLLC" and settings.limiter == "Venkatakrishnan"
