@@ -731,6 +731,8 @@ def main(only=None):
         return None
     if only == "fluxes":
         return fluxes_fixture(ref)
+    if only == "bump_implicit":
+        return bump_implicit_fixture(ref)
     riemann, riemann_p = riemann_case(16)
     residual_fixture("riemann16", riemann, ref)
     residual_fixture("periodic_mixed", periodic_case(8, 6, split="half", jitter=0.25, seed=2), ref)
@@ -765,6 +767,22 @@ def main(only=None):
     solve_fixture("channel_rk2_vanleer", chan, cp,
                   {"flux": "HLLC", "reconstruction": "MUSCL linear", "limiter": "Van Leer",
                    "time_integration": "Explicit RK2", "cfl": 0.6, "acceleration_x": 0.2}, 8, ref)
+
+
+def bump_implicit_fixture(ref, nx=16, ny=8):
+    """One implicit-Euler step of the reference (_implicit_euler_step) on the
+    bump-channel recipe from the free stream with its local time steps:
+    at CFL 200 its Newton solve fails until the step has been halved 9
+    times, which the fixture records with the new state."""
+    case, P = bump_case(nx, ny)
+    rc = reference_case(case, ref)
+    rg = ref.solver._build_geometry(rc.mesh, rc)
+    num = rc.numerics
+    U = ref.euler.primitive_to_conservative(P, num.gamma)
+    dt = ref.solver._stable_time_steps(ref.euler.conservative_to_primitive(U, num.gamma), rg, num)
+    out, used = ref.solver._implicit_euler_step(U, dt, rg, num)
+    np.savez_compressed(HERE / "implicit_bump.npz", U=U, dt=dt, U_next=out, used=np.asarray(used))
+    print("bump implicit", len(U), "cells, accepted / initial step", float(np.mean(used) / np.mean(dt)))
 
 
 def fluxes_fixture(ref, n=1000, seed=11):

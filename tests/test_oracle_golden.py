@@ -97,3 +97,23 @@ def test_oracle_implicit_matches_reference(name):
     P = imp.orc.primitive(Uc, s.gamma)
     assert np.abs(P - data["P_final"]).max() <= 1e-10 * np.abs(data["P_final"]).max()
     assert abs(time - float(data["time"])) <= 1e-12 * float(data["time"])
+
+
+def test_oracle_implicit_step_on_the_bump_recipe_matches_reference():
+    """tests/golden/implicit_bump.npz: the reference's implicit-Euler step on
+    a 16x8 bump channel (Roe, MUSCL linear, Barth-Jespersen, local CFL 200,
+    GMRES(30) to 1e-3, LU-SGS) halves its time step 9 times before its
+    Newton solve converges; the oracle takes the same steps to the same
+    state."""
+    from conftest import ROOT
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import bump_case
+    from oracle.implicit import ImplicitOracle
+
+    data = np.load(ROOT / "tests" / "golden" / "implicit_bump.npz")
+    case, _ = bump_case(16, 8)
+    g = build_geometry(case.mesh, case)
+    out, used = ImplicitOracle(g).step(data["U"], data["dt"], case.numerics)
+    np.testing.assert_array_equal(used, data["used"])
+    np.testing.assert_array_equal(used, data["dt"] * 0.5**9)
+    assert np.abs(out - data["U_next"]).max() <= 1e-12 * np.abs(data["U_next"]).max()
