@@ -434,7 +434,10 @@ int64_t mcfd_launch_count(void);
  * owned by another allocator).  Its scratch is a fixed 19,456-byte __device__
  * array shared by all calls: overlapping calls race.  The first call on each
  * device looks up that array's address (call it once before any stream
- * capture).  n_cells above 2^30 returns MCFD_E_TOO_LARGE.
+ * capture); the address stays cached for the process, so do not call it
+ * again on a device after cudaDeviceReset.  n_cells above 2^30 returns
+ * MCFD_E_TOO_LARGE.  The status reads the thread's CUDA error state without
+ * clearing it, so an earlier call's pending error is reported as MCFD_E_CUDA.
  */
 int mcfd_residual_sumsq_noalloc(const double* R, int64_t n_cells, double* sums, void* stream);
 

@@ -609,7 +609,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   Arena A;
   auto bytes_i = [](size_t n) { return n * sizeof(int); };
   auto bytes_d = [](size_t n) { return n * sizeof(double); };
-  const int partial_blocks = 152 * 4;
+  const int partial_blocks = kSumsqBlocks;
   size_t o_area = A.take(bytes_d(C)), o_cell_order = A.take(bytes_i(C));
   size_t o_grad_ptr = A.take(bytes_i(C + 1)), o_grad_nb = A.take(bytes_i(NG)),
          o_grad_cx = A.take(bytes_d(NG)), o_grad_cy = A.take(bytes_d(NG)), o_grad_twin = A.take(bytes_i(NG));

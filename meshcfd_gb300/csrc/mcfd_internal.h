@@ -232,7 +232,12 @@ cudaError_t launch_viscous_diffusion(const DevGeom& g, const mcfd_config& cfg, c
 // first order when recon is null) into ext
 cudaError_t launch_bc_states(const DevGeom& g, const mcfd_config& cfg, const double* P, const double* recon,
                              double* ext, cudaStream_t s);
-// reduction kernels of the sum of squares
+// reduction kernels of the sum of squares.  kSumsqBlocks is the grid of the
+// partial kernel for every entry point that reduces a residual (the handle's
+// mcfd_residual_sumsq and the allocation-free variant): the grid fixes the
+// summation order, so both give the same bits only while they share it.
+constexpr int kSumsqBlocks = 152 * 4;
+constexpr int kSumsqThreads = 256;
 __global__ void k_sumsq_partial(int n, const double* __restrict__ R, double* __restrict__ partials);
 __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums);
 cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,

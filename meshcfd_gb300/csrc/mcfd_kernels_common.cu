@@ -10,23 +10,28 @@ static constexpr int kBlock = 256;
 
 // ------------------------------------------------------------- sum of squares
 
-__global__ void __launch_bounds__(kBlock) k_sumsq_partial(int n, const double* __restrict__ R,
-                                                          double* __restrict__ partials) {
-  __shared__ double sh[4][kBlock];
+// Per thread a grid-stride sum, per warp a shuffle tree, per block the warps'
+// sums added in warp order by one thread: a fixed order for a fixed grid
+// (kSumsqBlocks x kSumsqThreads), so every call gives the same bits.
+__global__ void __launch_bounds__(kSumsqThreads) k_sumsq_partial(int n, const double* __restrict__ R,
+                                                                 double* __restrict__ partials) {
+  __shared__ double warp_sum[kSumsqThreads / 32][4];
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
     const St4 r = ld4(R + 4 * (size_t)c);
     acc[0] += r.a * r.a; acc[1] += r.b * r.b; acc[2] += r.c * r.c; acc[3] += r.d * r.d;
   }
-  for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] = acc[k];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 4; ++k) warp_sum[threadIdx.x >> 5][k] = acc[k];
   __syncthreads();
-  for (int width = kBlock / 2; width > 0; width >>= 1) {
-    if (threadIdx.x < width)
-      for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + width];
-    __syncthreads();
+  if (threadIdx.x < 4) {
+    double s = warp_sum[0][threadIdx.x];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) s += warp_sum[w][threadIdx.x];
+    partials[4 * blockIdx.x + threadIdx.x] = s;
   }
-  if (threadIdx.x == 0)
-    for (int k = 0; k < 4; ++k) partials[4 * blockIdx.x + k] = sh[k][0];
 }
 
 __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums) {
@@ -95,7 +100,7 @@ void count_launch(int n) { __atomic_fetch_add(&g_launches, (long long)n, __ATOMI
 cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,
                          double* sums, cudaStream_t s) {
   count_launch(2);
-  k_sumsq_partial<<<blocks, kBlock, 0, s>>>(g.n_cells, R, partials);
+  k_sumsq_partial<<<blocks, kSumsqThreads, 0, s>>>(g.n_cells, R, partials);
   k_sumsq_final<<<1, 32, 0, s>>>(blocks, partials, sums);
   return cudaGetLastError();
 }

@@ -13,9 +13,14 @@ GPU-backed versions taking and returning NumPy arrays:
 
 so ``solve_case`` runs unchanged on top of them.  :func:`solve_case` goes
 further: it keeps the state in HBM for the whole explicit loop and returns the
-reference's ``SolverResult``.  Cases outside the GPU path (viscous, SST,
-parabolic reconstruction, pressure-inlet / mass-flow boundaries) raise
-``NotImplementedError``; nothing falls back to the CPU.
+reference's ``SolverResult``.  Inviscid and laminar viscous (constant or
+Sutherland) cases, first-order, MUSCL-linear and MUSCL-parabolic
+reconstruction and every boundary kind of ``_residual`` run on the GPU.
+Refused with ``NotImplementedError`` (nothing falls back to the CPU): SST
+turbulence states, and in :func:`solve_case` the implicit integrator and
+adaptive refinement (use :func:`install` and the reference's own loop for
+those).  Walls with a prescribed velocity take their velocities from the
+geometry as the reference computed them.
 """
 
 from __future__ import annotations
@@ -33,10 +38,15 @@ _PATCHED = ("_residual", "_stable_time_steps", "_stable_time_step", "_explicit_r
 
 class _Cache:
     """DeviceGeometry per reference ``_Geometry`` object (rebuilt after
-    adaptation, solver.py:864, so keyed by identity)."""
+    adaptation, solver.py:864, so keyed by identity).  Entries go when their
+    geometry is collected; geometries that cannot be weakly referenced are
+    held strongly, at most ``STRONG_LIMIT`` of them (oldest dropped first)."""
+
+    STRONG_LIMIT = 4
 
     def __init__(self):
         self.items = {}
+        self.strong = []
 
     def get(self, geometry) -> DeviceGeometry:
         key = id(geometry)
@@ -47,7 +57,10 @@ class _Cache:
         try:
             ref = weakref.ref(geometry, lambda _r, k=key: self.items.pop(k, None))
         except TypeError:
-            ref = lambda g=geometry: g  # noqa: E731  (objects without weakref support stay cached)
+            ref = lambda g=geometry: g  # noqa: E731  (no weakref support: held strongly)
+            self.strong.append(key)
+            while len(self.strong) > self.STRONG_LIMIT:
+                self.items.pop(self.strong.pop(0), None)
         self.items[key] = (ref, dg)
         return dg
 

@@ -310,7 +310,7 @@ def match_periodic_faces(mesh, patch_a_id: int, patch_b_id: int):
 
 # ------------------------------------------------------------------- builder
 
-def build_geometry(mesh: FiniteVolumeMesh, case) -> Geometry:
+def build_geometry(mesh: FiniteVolumeMesh, case, host=None) -> Geometry:
     """Restatement of ``_build_geometry`` (solver.py:1654-2238) for the hot path.
 
     Covers cell/face geometry, periodic pairing, boundary classification and
@@ -318,10 +318,17 @@ def build_geometry(mesh: FiniteVolumeMesh, case) -> Geometry:
     entries.  Not covered (out of scope for the inviscid path): wall distances
     (SST/viscous only), prescribed-velocity walls (expression evaluation) and
     SST inlet data.
-    """
-    from . import _lib
 
-    lib = _lib.native()
+    ``host`` supplies the cell and face loops (``cell_geometry`` and
+    ``face_geometry``, solver.py:1654-1696); the default is this library's
+    compiled host helpers.  A CPU-only caller may pass its own
+    implementation of the same two functions.
+    """
+    if host is None:
+        from . import _lib
+
+        host = _lib.native()
+    lib = host
     offsets, nodes = _cells_csr(mesh)
     n_cells = len(offsets) - 1
     points = np.ascontiguousarray(np.asarray(mesh.points, dtype=np.float64))

@@ -1146,3 +1146,87 @@ out:
   free(Pchk);
   return st;
 }
+
+/* ------------------------------------------------------- mesh geometry
+ *
+ * _build_geometry's cell and face loops (solver.py:1654-1696), so that the
+ * CPU reference path builds its geometry without the product library.
+ *
+ * Cells: twice the signed area is Python's built-in sum() of the shoelace
+ * cross products; for floats CPython >= 3.12 sums with Neumaier's
+ * compensation (running sum t, compensation c, added once at the end when it
+ * is non-zero and finite).  The centroid sums are plain left-to-right.
+ *
+ * Faces: np.linalg.norm of a 2-vector and np.dot of two 2-vectors are BLAS
+ * dot products, which round as fma(a1, b1, a0 * b0) on the reference's
+ * platform; the normal is (ey, -ex) / length, flipped when it points into the
+ * owner.  Returns 4 and the offending id on a degenerate cell or face (the
+ * reference's "Cell {id} has zero or invalid area." / "Face {id} has zero or
+ * invalid length.").
+ */
+int orc_cell_geometry(int64_t n_cells, const int64_t* off, const int64_t* nodes, const double* pts,
+                      double* centers, double* areas, int64_t* bad) {
+  for (int64_t c = 0; c < n_cells; ++c) {
+    const int64_t b = off[c], k = off[c + 1] - off[c];
+    double total = 0.0, comp = 0.0;
+    for (int64_t i = 0; i < k; ++i) {
+      const double* p = pts + 2 * nodes[b + i];
+      const double* q = pts + 2 * nodes[b + (i + 1) % k];
+      const double x = p[0] * q[1] - q[0] * p[1];
+      if (i == 0) {
+        total = x;
+        continue;
+      }
+      const double t = total + x;
+      if (fabs(total) >= fabs(x))
+        comp += (total - t) + x;
+      else
+        comp += (x - t) + total;
+      total = t;
+    }
+    if (comp != 0.0 && isfinite(comp)) total += comp;
+    if (!isfinite(total) || fabs(total) <= 1e-15) {
+      *bad = c;
+      return 4;
+    }
+    double xs = 0.0, ys = 0.0;
+    for (int64_t i = 0; i < k; ++i) {
+      const double* p = pts + 2 * nodes[b + i];
+      const double* q = pts + 2 * nodes[b + (i + 1) % k];
+      const double cross = p[0] * q[1] - q[0] * p[1];
+      xs += (p[0] + q[0]) * cross;
+      ys += (p[1] + q[1]) * cross;
+    }
+    centers[2 * c] = xs / (3.0 * total);
+    centers[2 * c + 1] = ys / (3.0 * total);
+    areas[c] = 0.5 * fabs(total);
+  }
+  return 0;
+}
+
+int orc_face_geometry(int64_t n_faces, const int64_t* face_nodes, const double* pts, const double* centers,
+                      const int64_t* owners, double* face_centers, double* normals, double* lengths, int64_t* bad) {
+  for (int64_t f = 0; f < n_faces; ++f) {
+    const double* a = pts + 2 * face_nodes[2 * f];
+    const double* b = pts + 2 * face_nodes[2 * f + 1];
+    const double ex = b[0] - a[0], ey = b[1] - a[1];
+    const double len = sqrt(fma(ey, ey, ex * ex));
+    if (!isfinite(len) || len <= 1e-15) {
+      *bad = f;
+      return 4;
+    }
+    double nx = ey / len, ny = -ex / len;
+    const double cx = 0.5 * (a[0] + b[0]), cy = 0.5 * (a[1] + b[1]);
+    const double* o = centers + 2 * owners[f];
+    if (fma(ny, cy - o[1], nx * (cx - o[0])) < 0.0) {
+      nx = -nx;
+      ny = -ny;
+    }
+    face_centers[2 * f] = cx;
+    face_centers[2 * f + 1] = cy;
+    normals[2 * f] = nx;
+    normals[2 * f + 1] = ny;
+    lengths[f] = len;
+  }
+  return 0;
+}

@@ -101,7 +101,46 @@ def lib():
         _lib.orc_bc_states.argtypes = [C.POINTER(OrcGeom), C.c_int64, PD, C.c_double, C.c_double, PD]
         _lib.orc_far_field_states.argtypes = [C.c_int64, PD, PD, PD, C.c_double, PD]
         _lib.orc_face_fluxes.argtypes = [C.c_int, C.c_int64, PD, PD, PD, C.c_double, PD]
+        _lib.orc_cell_geometry.argtypes = [C.c_int64, P64, P64, PD, PD, PD, P64]
+        _lib.orc_face_geometry.argtypes = [C.c_int64, P64, PD, PD, P64, PD, PD, PD, P64]
     return _lib
+
+
+class GeometryHost:
+    """The cell and face loops of ``_build_geometry`` (solver.py:1654-1696)
+    in the oracle's C, with the interface ``build_geometry(..., host=)``
+    expects: the CPU reference path builds its mesh geometry with these, so
+    it never loads the product library."""
+
+    @staticmethod
+    def cell_geometry(offsets, nodes, points):
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        nodes = np.ascontiguousarray(nodes, dtype=np.int64)
+        points = np.ascontiguousarray(points, dtype=np.float64)
+        n = len(offsets) - 1
+        centers, areas, bad = np.empty((n, 2)), np.empty(n), C.c_int64(-1)
+        rc = lib().orc_cell_geometry(n, offsets.ctypes.data_as(P64), nodes.ctypes.data_as(P64),
+                                     points.ctypes.data_as(PD), centers.ctypes.data_as(PD),
+                                     areas.ctypes.data_as(PD), C.byref(bad))
+        if rc:
+            raise OracleError(f"Cell {bad.value} has zero or invalid area.")
+        return centers, areas
+
+    @staticmethod
+    def face_geometry(faces, points, centers, owners):
+        faces = np.ascontiguousarray(faces, dtype=np.int64)
+        points = np.ascontiguousarray(points, dtype=np.float64)
+        centers = np.ascontiguousarray(centers, dtype=np.float64)
+        owners = np.ascontiguousarray(owners, dtype=np.int64)
+        n = len(faces)
+        fc, normals, lengths, bad = np.empty((n, 2)), np.empty((n, 2)), np.empty(n), C.c_int64(-1)
+        rc = lib().orc_face_geometry(n, faces.ctypes.data_as(P64), points.ctypes.data_as(PD),
+                                     centers.ctypes.data_as(PD), owners.ctypes.data_as(P64),
+                                     fc.ctypes.data_as(PD), normals.ctypes.data_as(PD),
+                                     lengths.ctypes.data_as(PD), C.byref(bad))
+        if rc:
+            raise OracleError(f"Face {bad.value} has zero or invalid length.")
+        return fc, normals, lengths
 
 
 FACE_FLUXES = {"Rusanov": 0, "HLLC": 1, "Roe": 2, "HLLC kernel": 3}

@@ -15,22 +15,42 @@ import sys
 import types
 from pathlib import Path
 
-REFERENCE = Path(os.environ.get("MESHCFD_REFERENCE", "/root/reference"))
+# Where the reference package is looked for, first match wins: the directory
+# named by MESHCFD_REFERENCE (a checkout with src/meshcfd, or a directory
+# holding the meshcfd package), the offline install of the unmodified
+# package under baseline/_ref of this repository (which travels with the
+# repository to machines without a checkout), and the read-only checkout of
+# the build container.
+_REPO = Path(__file__).resolve().parents[2]
+_CANDIDATES = [Path(p) for p in (os.environ.get("MESHCFD_REFERENCE"),) if p] + [
+    _REPO / "baseline" / "_ref", Path("/root/reference")]
+
+
+def _package_root():
+    """The directory that holds the ``meshcfd`` package, or None."""
+    for base in _CANDIDATES:
+        for root in (base / "src", base):
+            if (root / "meshcfd" / "core" / "solver.py").exists():
+                return root
+    return None
+
+
+REFERENCE = _package_root()
 
 
 def available() -> bool:
-    return (REFERENCE / "src" / "meshcfd" / "core" / "solver.py").exists()
+    return REFERENCE is not None
 
 
 def import_reference():
     """Return the reference's ``meshcfd.core`` modules as a namespace."""
     if not available():
-        raise ImportError(f"reference checkout not found at {REFERENCE}")
+        raise ImportError("reference package not found (set MESHCFD_REFERENCE)")
     if "numba" not in sys.modules:
         stub = types.ModuleType("numba")
         stub.njit = lambda *a, **k: (a[0] if a and callable(a[0]) else (lambda f: f))
         sys.modules["numba"] = stub
-    for p in (str(REFERENCE / "src"), str(REFERENCE)):
+    for p in (str(REFERENCE),):
         if p not in sys.path:
             sys.path.insert(0, p)
     from meshcfd.core import _kernels, euler, model, solver  # noqa: E402

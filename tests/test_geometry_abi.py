@@ -42,6 +42,28 @@ def test_geometry_builder_is_bit_exact(name):
                                       getattr(ref, field), err_msg=field)
 
 
+@pytest.mark.parametrize("name", ("riemann16", "periodic_mixed", "channel"))
+def test_oracle_geometry_loops_are_bit_exact(name):
+    """The oracle's restatement of the cell / face loops (what the CPU
+    reference arm builds its geometry with, without the product library)
+    against the reference's own arrays, and refusing degenerate elements with
+    the reference's messages."""
+    from meshcfd_gb300.geometry import build_geometry
+    from oracle.oracle import GeometryHost, OracleError
+
+    data, ref = load_fixture(f"residual_{name}.npz")
+    case = _case_for(name)
+    g = build_geometry(case.mesh, case, host=GeometryHost())
+    for field in FIELDS:
+        np.testing.assert_array_equal(np.asarray(getattr(g, field)).reshape(np.shape(getattr(ref, field))),
+                                      getattr(ref, field), err_msg=field)
+    points = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0]])
+    with pytest.raises(OracleError, match="Cell 0 has zero or invalid area"):
+        GeometryHost.cell_geometry(np.array([0, 3]), np.array([0, 1, 2]), points)
+    with pytest.raises(OracleError, match="Face 0 has zero or invalid length"):
+        GeometryHost.face_geometry(np.array([[0, 0]]), points, np.zeros((1, 2)), np.array([0]))
+
+
 def test_workload_mesh_sizes():
     from meshcfd_gb300.meshes import riemann_case, vortex_case
 

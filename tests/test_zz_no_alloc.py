@@ -39,7 +39,9 @@ def test_noalloc_sumsq_matches_allocating_entry_point(cuda_device, n):
         expected = torch.empty(4, dtype=torch.float64, device=cuda_device)
         assert lib.mcfd_residual_sumsq(dg.handle, R.data_ptr(), expected.data_ptr(), stream) == 0
         got = torch.full((4,), float("nan"), dtype=torch.float64, device=cuda_device)
+        launches = lib.mcfd_launch_count()
         assert lib.mcfd_residual_sumsq_noalloc(R.data_ptr(), dg.n_cells, got.data_ptr(), stream) == 0
+        assert lib.mcfd_launch_count() - launches == 2  # its two kernels are counted like every other launch
         torch.cuda.synchronize()
         np.testing.assert_array_equal(got.cpu().numpy(), expected.cpu().numpy())
         np.testing.assert_allclose(got.cpu().numpy(), (R * R).sum(dim=0).cpu().numpy(), rtol=1e-12)
