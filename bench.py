@@ -77,6 +77,9 @@ def parse(argv=None):
     ap.add_argument("--bump-steps", type=int, default=1)
     ap.add_argument("--bump-oracle", action="store_true",
                     help="bump workload: also run the oracle's SciPy restatement of the same step and compare")
+    ap.add_argument("--numbering", choices=("generator", "random", "rcm"), default="generator",
+                    help="vortex workloads: cell and face ids as generated, randomly permuted (as a mesh file "
+                         "may number them), or renumbered by reverse Cuthill-McKee")
     return ap.parse_args(argv)
 
 
@@ -89,29 +92,37 @@ WORKLOADS = {
 }
 
 
-def _sample_case(name, n, host=None):
+def _sample_case(name, n, host=None, numbering="generator"):
     """(case, settings, geometry, initial primitive) of workload ``name``,
-    at ``n`` x ``n`` quads when given."""
+    at ``n`` x ``n`` quads when given, with the mesh's ids as generated,
+    randomly permuted (seed 7) or renumbered by reverse Cuthill-McKee."""
     from meshcfd_gb300.geometry import build_geometry
-    from meshcfd_gb300.meshes import cell_centroids, vortex_case, vortex_primitive
+    from meshcfd_gb300.meshes import cell_centroids, permute_mesh, reverse_cuthill_mckee, vortex_case, vortex_primitive
 
     w = WORKLOADS[name]
     case, _ = vortex_case(n or w["n"], split=w["split"])
+    if numbering == "random":
+        rng = np.random.default_rng(7)
+        case.mesh = permute_mesh(case.mesh, rng.permutation(len(case.mesh.cells)),
+                                 rng.permutation(len(case.mesh.faces)))
+    elif numbering == "rcm":
+        case.mesh = permute_mesh(case.mesh, *reverse_cuthill_mckee(case.mesh))
     g = build_geometry(case.mesh, case, host=host)
     return case, case.numerics, g, vortex_primitive(cell_centroids(case.mesh))
 
 
-def make_workload(name, host=None):
+def make_workload(name, host=None, numbering="generator"):
     """The workload's case, settings, geometry, initial primitive state and
     the ``config`` both arms print (identical keys and values; the kernel
     variant of the device arm is the line's separate ``mode`` key).  ``host``:
     the cell / face geometry loops to build with (the CPU reference arm passes
     the oracle's, so that it never loads the product library)."""
     w = WORKLOADS[name]
-    case, settings, g, P0 = _sample_case(name, w["n"], host=host)
+    case, settings, g, P0 = _sample_case(name, w["n"], host=host, numbering=numbering)
     config = {
         "workload": f"isentropic vortex, periodic [0,10]^2, {w['n']}x{w['n']} quads, "
-                    f"{'half' if w['split'] == 'half' else 'all'} split to triangles, jitter 0.15h, seed 0",
+                    f"{'half' if w['split'] == 'half' else 'all'} split to triangles, jitter 0.15h, seed 0"
+                    + ("" if numbering == "generator" else f", ids {numbering}"),
         "cells": int(len(g.areas)),
         "faces": int(len(g.face_lengths)),
         "interior_faces": int(len(g.interior_faces)),
@@ -381,7 +392,7 @@ class ExplicitRun:
         from meshcfd_gb300.device import DeviceGeometry, make_config, primitive_to_conservative
 
         self.name, self.args, self.device = name, args, device
-        self.case, self.settings, self.g, self.P0, self.config = make_workload(name)
+        self.case, self.settings, self.g, self.P0, self.config = make_workload(name, numbering=args.numbering)
         self.cfg = make_config(self.settings, mode=args.mode)
         self.dg = DeviceGeometry(self.g, device)
         self.C = self.dg.n_cells
@@ -866,6 +877,112 @@ def run_adjoint(args):
     print(json.dumps(line))
 
 
+def run_bump(args):
+    """Implicit configuration: the bump channel (circular arc of 10 % chord,
+    rows stretched by 1.05 toward the wall, seed 1; Roe, MUSCL linear with
+    Barth-Jespersen, implicit Euler with local time steps at CFL 200,
+    GMRES(30) to 1e-3 with LU-SGS) at ``--bump-size``, ``--bump-steps``
+    implicit steps of the reference's algorithm (time-step halving, Newton,
+    line search) on the device under a wall-clock budget.  Reports the
+    per-step counts, seconds per step and per GMRES iteration, the density
+    residual drop and the state's deviation from the oracle's restatement
+    (SciPy GMRES) after the first step when ``--bump-oracle`` is given."""
+    import torch
+
+    from meshcfd_gb300.device import DeviceGeometry, make_config, primitive_to_conservative
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.implicit import BudgetExceeded, ImplicitEuler
+    from meshcfd_gb300.meshes import bump_case
+
+    device = torch.device("cuda", 0)
+    nx, ny = (int(v) for v in args.bump_size.split("x"))
+    t0 = time.perf_counter()
+    case, P0 = bump_case(nx, ny)
+    s = case.numerics
+    g = build_geometry(case.mesh, case)
+    setup_s = time.perf_counter() - t0
+    dg = DeviceGeometry(g, device)
+    cfg = make_config(s, "exact")
+    U0 = primitive_to_conservative(P0, s.gamma)
+    U = torch.as_tensor(U0, device=device)
+    R = torch.empty_like(U)
+
+    def density_residual():
+        dg.residual(U, cfg, out=R)
+        dg.check_status()
+        return math.sqrt(float((R[:, 0] * R[:, 0]).mean()))
+
+    r0 = density_residual()
+    start = time.perf_counter()
+    stepper = ImplicitEuler(dg, s, "exact", deadline=start + args.budget_s)
+    steps, first_state, first_dt = [], None, None
+    status = "completed"
+    before = _launches()
+    with ClockSampler(device.index) as clocks:
+        for k in range(args.bump_steps):
+            P = dg.primitive(U, cfg, out=dg.primitive_buffer())
+            dt, _ = dg.time_steps(P, cfg, per_cell=True)
+            dg.check_status()
+            counts0 = (stepper.attempts, stepper.newton_iterations, stepper.gmres_iterations, stepper.gmres_calls,
+                       stepper.gmres_seconds)
+            ts = time.perf_counter()
+            try:
+                new, used = stepper.step(U, dt)
+            except BudgetExceeded:
+                status = f"stopped by the {args.budget_s:.0f} s budget during step {k + 1}"
+                break
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - ts
+            if k == 0:
+                first_dt = dt.cpu().numpy()
+            U.copy_(new)
+            if k == 0:
+                first_state = U.cpu().numpy()
+            r = density_residual()
+            gi = stepper.gmres_iterations - counts0[2]
+            steps.append({"step": k + 1, "seconds": wall, "halvings": stepper.attempts - counts0[0] - 1,
+                          "newton_iterations": stepper.newton_iterations - counts0[1], "gmres_iterations": gi,
+                          "gmres_solves": stepper.gmres_calls - counts0[3],
+                          "ms_per_gmres_iteration": 1e3 * (stepper.gmres_seconds - counts0[4]) / max(gi, 1),
+                          "mean_cfl_used": float(s.cfl * float(used.mean()) / float(dt.mean())),
+                          "density_residual": r, "drop": r / r0})
+    launches = _launches() - before
+    vs_oracle = None
+    if args.bump_oracle and first_state is not None:
+        from oracle.implicit import ImplicitOracle
+
+        to = time.perf_counter()
+        ref, _ = ImplicitOracle(g).step(U0, first_dt, s)
+        vs_oracle = {"steps": 1, "state_max_rel_err": max_rel(first_state, ref),
+                     "oracle_seconds": time.perf_counter() - to,
+                     "oracle": "oracle/implicit.py: the reference's implicit step over the C residual, SciPy gmres "
+                               "and spsolve_triangular, one host thread"}
+    n = len(steps)
+    per_step = sum(x["seconds"] for x in steps) / n if n else None
+    estimate = None
+    if n and steps[-1]["drop"] < 1.0:
+        rate = steps[-1]["drop"] ** (1.0 / n)  # geometric mean drop per step so far
+        need = math.log(1e-8) / math.log(rate)
+        estimate = {"drop_per_step": rate, "steps_to_8_orders": need, "hours_at_measured_rate": need * per_step / 3600,
+                    "basis": f"geometric mean of the first {n} steps"}
+    line = {
+        "metric": "implicit Euler step, bump channel (s per step)", "value": per_step, "unit": "s/step",
+        "n_gpus": 1, "steps": n, "warmup": 0, "higher_is_better": False, "dtype": "f64",
+        "data": "synthetic (seeded bump channel, free-stream start)",
+        "config": {"workload": f"bump channel {nx}x{ny} ({dg.n_cells} cells), Roe, MUSCL linear, Barth-Jespersen, "
+                               f"implicit Euler, local CFL {s.cfl:g}, GMRES({s.gmres_krylov_dimension}) to "
+                               f"{s.gmres_tolerance:g} with LU-SGS", "setup_s": setup_s,
+                   "budget_s": args.budget_s, "mode": "exact"},
+        "status": status, "per_step": steps, "initial_density_residual": r0,
+        "ms_per_gmres_iteration": (1e3 * stepper.gmres_seconds / stepper.gmres_iterations
+                                   if stepper.gmres_iterations else None),
+        "time_to_8_orders": estimate, "vs_oracle": vs_oracle,
+        "gpu_launches": launches, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    dg.close()
+
+
 def _launches():
     from meshcfd_gb300._lib import native
 
@@ -874,14 +991,14 @@ def _launches():
 
 def main():
     args = parse()
-    if args.workload == "batch256":
-        run_batch(args)
-        return
-    if args.workload == "adjoint":
-        run_adjoint(args)
-        return
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch256":
+        run_batch(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
+    elif args.workload == "bump":
+        run_bump(args)
     else:
         run_gpu(args)
 

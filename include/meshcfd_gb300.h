@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define MCFD_ABI_VERSION 4
+#define MCFD_ABI_VERSION 5
 
 /* ---- return codes (host-side failures) ---- */
 #define MCFD_OK 0
@@ -84,6 +84,12 @@ typedef struct mcfd_status {
 #define MCFD_LIMITER_MINMOD 1
 #define MCFD_LIMITER_VAN_LEER 2
 #define MCFD_LIMITER_VENKATAKRISHNAN 3
+/* Venkatakrishnan's limiter in its published form with the smoothing constant
+ * K (mcfd_config.venkat_k): per face (d1^2 + e2 + 2 d1 d2) / (d1^2 + 2 d2^2 +
+ * d1 d2 + e2), e2 = (K sqrt(A))^3, minimum over faces, no cap.  No
+ * counterpart in the reference (its Venkatakrishnan form has no K); MUSCL
+ * linear only. */
+#define MCFD_LIMITER_VENKATAKRISHNAN_K 4
 /* kernel variants */
 #define MCFD_MODE_EXACT 0 /* reference operation order, no FMA: bit-exact */
 #define MCFD_MODE_FAST 1  /* exact arithmetic, limiter minimum via the smallest ratio */
@@ -111,7 +117,8 @@ typedef struct mcfd_config {
   double sutherland_reference_temperature;
   double sutherland_temperature;
   double prandtl_number;
-  double reserved[2];
+  double venkat_k;        /* K of MCFD_LIMITER_VENKATAKRISHNAN_K (> 0) */
+  double reserved;
 } mcfd_config;
 
 /* viscosity models (model.py:24) */
@@ -297,10 +304,16 @@ const double* mcfd_geom_stage_state(const mcfd_geom* geom, int32_t k);
  * settings by timing candidates on the state U (device [n_cells][4]):
  * reconstruction and gather threads per block in {64, 128, 256}, flux
  * threads in {64, 128, 256} x faces per thread in {1, 2, 4}.  The choice
- * stays with the handle; chosen (host [4]) receives reconstruction threads,
- * flux threads, flux faces per thread, gather threads (0: default).
+ * stays with the handle; chosen (host [5]) receives reconstruction threads,
+ * flux threads, flux faces per thread, gather threads (0: default) and
+ * whether the fast variant's reconstruction runs one thread per (cell,
+ * variable) (1) or per cell (0).
  * Synchronises the stream.  No counterpart in the reference. */
 int mcfd_autotune(mcfd_geom* geom, const mcfd_config* cfg, const double* U, int32_t* chosen, void* stream);
+/* Set the launch shapes directly (host [5], the layout mcfd_autotune fills;
+ * 0 = default), e.g. to replay a tuning saved from an earlier run.  Results
+ * do not depend on them.  No counterpart in the reference. */
+int mcfd_set_launch_shapes(mcfd_geom* geom, const int32_t* shapes);
 /* mcfd_explicit_step that also copies, for every stage k, the primitive state
  * it evaluates the residual at into stage_P[k] ([n_cells][4]) and, for MUSCL,
  * its face states into stage_recon[k] ([n_limiter][4], may be NULL): the
@@ -330,8 +343,8 @@ int mcfd_status_fetch(mcfd_geom* geom, void* stream, mcfd_status* out);
  * solver.py:1185-1300, assembled from P(U) and the time step), the
  * first-order residual R1(U) (jacobian_rate, solver.py:1445) with cfg's flux,
  * and |U / scales| (solver.py:1543).  dt: device scalar or [n_cells]
- * (dt_per_cell); it must stay valid while the operator is used.  scales:
- * host [4], the per-variable scaling of the Newton iteration.
+ * (dt_per_cell), copied on the stream.  scales: host [4], the per-variable
+ * scaling of the Newton iteration.
  */
 int mcfd_implicit_prepare(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const double* dt,
                           int32_t dt_per_cell, const double* scales, void* stream);
@@ -367,13 +380,22 @@ int mcfd_vjp_at(mcfd_geom* geom, const mcfd_config* cfg, const double* U, const 
 int mcfd_wall_force(mcfd_geom* geom, const mcfd_config* cfg, const double* U, double dir_x, double dir_y,
                     double* J, double* dJdU, void* stream);
 /* x = (D+U)^-1 D (D+L)^-1 v with the prepared scalar matrix applied to each
- * of the four variables (LU-SGS, solver.py:1302-1323); level-scheduled sweeps
- * in natural cell order. */
+ * of the four variables (LU-SGS, solver.py:1302-1323, the two
+ * spsolve_triangular calls): level-scheduled sweeps over the dependency
+ * graph of the natural cell order, so the result is the sequential
+ * triangular solves' (rows summed in ascending column order). */
 int mcfd_lusgs_apply(mcfd_geom* geom, const double* v, double* x, void* stream);
+/* Launch schedule of the LU-SGS sweeps: runs of levels at most wide_level
+ * rows wide go to one block that steps through them (a barrier per level),
+ * wider levels get a grid launch each; 0 restores the default (16384).
+ * Results do not depend on it.  No counterpart in the reference. */
+int mcfd_implicit_set_sweep(mcfd_geom* geom, int32_t wide_level);
 /* Solve operator(x) = b with restarted GMRES(krylov_dim) preconditioned by
  * LU-SGS, as _solve_gmres drives SciPy's gmres (solver.py:1489-1529; left
  * preconditioning, modified Gram-Schmidt, Givens rotations).  b, x: device
- * [4 n_cells].  Returns MCFD_OK, MCFD_E_NOT_CONVERGED or MCFD_E_BREAKDOWN. */
+ * [4 n_cells].  Returns MCFD_OK, MCFD_E_NOT_CONVERGED or MCFD_E_BREAKDOWN.
+ * The Arnoldi steps of a restart cycle run without a host round trip: the
+ * cycle is a CUDA graph whose loop condition the device sets. */
 int mcfd_gmres(mcfd_geom* geom, const double* b, double* x, double tol, int32_t max_iter,
                int32_t krylov_dim, int32_t* iterations, void* stream);
 /* Newton equation e = U - U0 - dt R (solver.py:1415-1418): writes

@@ -44,7 +44,8 @@ class Config(C.Structure):
         ("sutherland_reference_temperature", c_dbl),
         ("sutherland_temperature", c_dbl),
         ("prandtl_number", c_dbl),
-        ("reserved", c_dbl * 2),
+        ("venkat_k", c_dbl),
+        ("reserved", c_dbl),
     ]
 
 
@@ -83,7 +84,7 @@ class GeomInfo(C.Structure):
     ]
 
 
-ABI_VERSION = 4  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
+ABI_VERSION = 5  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
 
 # name -> (restype, argtypes); every symbol include/meshcfd_gb300.h declares.
 SIGNATURES = {
@@ -103,11 +104,13 @@ SIGNATURES = {
                                           c_vp]),
     "mcfd_vjp_at": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "mcfd_autotune": (c_i32, [c_vp, C.POINTER(Config), c_vp, C.POINTER(c_i32), c_vp]),
+    "mcfd_set_launch_shapes": (c_i32, [c_vp, C.POINTER(c_i32)]),
     "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
     "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),
     "mcfd_implicit_matvec": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_implicit_set_jacobian": (c_i32, [c_vp, c_i32]),
+    "mcfd_implicit_set_sweep": (c_i32, [c_vp, c_i32]),
     "mcfd_jvp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp]),
     "mcfd_vjp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp]),
     "mcfd_wall_force": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_dbl, c_dbl, P_dbl, c_vp, c_vp]),

@@ -79,10 +79,16 @@ bool in_range(int64_t v, int64_t n) { return v >= 0 && v < n; }
 static int check_cfg(const mcfd_config* cfg) {
   if (!cfg) return MCFD_E_ARG;
   if (cfg->flux < 0 || cfg->flux > 2) return MCFD_E_ARG;
-  if (cfg->limiter < 0 || cfg->limiter > 3) return MCFD_E_ARG;
+  if (cfg->limiter < 0 || cfg->limiter > MCFD_LIMITER_VENKATAKRISHNAN_K) return MCFD_E_ARG;
+  if (cfg->limiter == MCFD_LIMITER_VENKATAKRISHNAN_K &&
+      (!(cfg->venkat_k > 0.0) || !std::isfinite(cfg->venkat_k)))
+    return MCFD_E_ARG;
   if (cfg->reconstruction < 0 || cfg->reconstruction > 2) return MCFD_E_ARG;
   if (!(cfg->gamma > 1.0)) return MCFD_E_ARG;
   if (cfg->mode < MCFD_MODE_EXACT || cfg->mode > MCFD_MODE_FMA) return MCFD_E_ARG;
+  // the smooth Venkatakrishnan form is built for MUSCL linear only
+  if (cfg->limiter == MCFD_LIMITER_VENKATAKRISHNAN_K && cfg->reconstruction == MCFD_RECON_MUSCL_PARABOLIC)
+    return MCFD_E_UNSUPPORTED;
   if (cfg->viscosity_model < MCFD_VISC_INVISCID || cfg->viscosity_model > MCFD_VISC_SUTHERLAND) return MCFD_E_ARG;
   if (cfg->viscosity_model != MCFD_VISC_INVISCID && (!(cfg->gas_constant > 0.0) || !(cfg->prandtl_number > 0.0)))
     return MCFD_E_ARG;
@@ -896,6 +902,7 @@ int mcfd_reconstruction(mcfd_geom* h, const mcfd_config* cfg, const double* P, d
   int c = check_cfg(cfg);
   if (c) return c;
   if (cfg->reconstruction == MCFD_RECON_FIRST_ORDER) return MCFD_E_ARG;
+  if (cfg->limiter == MCFD_LIMITER_VENKATAKRISHNAN_K) return MCFD_E_UNSUPPORTED;  // the reference's fields only
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_RECONSTRUCT, s,
                   [&] { return launch_reconstruction_fields(h->g, *cfg, P, gradients, curvature, factors, s); }));
@@ -949,15 +956,21 @@ int mcfd_autotune(mcfd_geom* h, const mcfd_config* cfg, const double* U, int32_t
     else if (muscl)
       MCFD_DISPATCH(*cfg, launch_reconstruct(g, *cfg, h->ws.P, h->ws.recon, s));
   };
-  int best_recon = 0, best_flux_t = 0, best_flux_f = 1, best_gather = 0;
+  int best_recon = 0, best_flux_t = 0, best_flux_f = 1, best_gather = 0, best_split = 0;
   if (muscl) {
+    // the fast variant's reconstruction also has a kernel with one thread per
+    // (cell, variable); both give the same bits
+    const int splits = cfg->mode == MCFD_MODE_FAST && cfg->limiter != MCFD_LIMITER_VENKATAKRISHNAN_K ? 2 : 1;
     float best = 1e30f;
-    for (int t : kThreads) {
-      g.tune_recon_threads = t;
-      const float ms = time_ms(recon);
-      if (ms < best) best = ms, best_recon = t;
-    }
+    for (int sp = 0; sp < splits; ++sp)
+      for (int t : kThreads) {
+        g.tune_recon_threads = t;
+        g.tune_recon_split = sp;
+        const float ms = time_ms(recon);
+        if (ms < best) best = ms, best_recon = t, best_split = sp;
+      }
     g.tune_recon_threads = best_recon;
+    g.tune_recon_split = best_split;
   }
   recon();
   {
@@ -989,7 +1002,27 @@ int mcfd_autotune(mcfd_geom* h, const mcfd_config* cfg, const double* U, int32_t
   chosen[1] = best_flux_t;
   chosen[2] = best_flux_f;
   chosen[3] = best_gather;
+  chosen[4] = best_split;
   return rc(cudaGetLastError());
+}
+
+int mcfd_set_launch_shapes(mcfd_geom* h, const int32_t* shapes) {
+  if (!h || !shapes) return MCFD_E_ARG;
+  static const int allowed[] = {0, 32, 64, 96, 128, 192, 256};
+  auto ok_threads = [&](int t) {
+    for (int a : allowed)
+      if (t == a) return true;
+    return false;
+  };
+  if (!ok_threads(shapes[0]) || !ok_threads(shapes[1]) || !ok_threads(shapes[3]) || shapes[2] < 0 ||
+      shapes[2] > 64 || shapes[4] < 0 || shapes[4] > 1)
+    return MCFD_E_ARG;
+  h->g.tune_recon_threads = shapes[0];
+  h->g.tune_flux_threads = shapes[1];
+  h->g.tune_flux_faces = shapes[2];
+  h->g.tune_gather_threads = shapes[3];
+  h->g.tune_recon_split = shapes[4];
+  return MCFD_OK;
 }
 
 const double* mcfd_geom_stage_state(const mcfd_geom* h, int32_t k) {
@@ -1160,26 +1193,25 @@ int mcfd_implicit_prepare(mcfd_geom* h, const mcfd_config* cfg, const double* U,
   if ((c = ensure_implicit(h))) return c;
   cudaStream_t s = (cudaStream_t)stream;
   ImplicitState& st = h->imp;
-  h->imp_cfg = *cfg;
-  h->imp_cfg.reconstruction = MCFD_RECON_FIRST_ORDER;  // replace(settings, reconstruction="First order")
-  st.scale = scale_of(scales);
-  st.dt = dt;
-  st.dt_per_cell = dt_per_cell;
+  mcfd_config first = *cfg;
+  first.reconstruction = MCFD_RECON_FIRST_ORDER;  // replace(settings, reconstruction="First order")
+  // the captured GMRES step holds this configuration's kernels: rebuild it
+  // when the configuration or the time-step layout changes
+  if (std::memcmp(&first, &h->imp_cfg, sizeof(first)) != 0 || st.dt_per_cell != (dt_per_cell != 0))
+    st.inner_key = -1;
+  h->imp_cfg = first;
+  cudaError_t e = implicit_set_operator(st, scale_of(scales), dt, dt_per_cell != 0, s);
   const size_t bytes = 4 * (size_t)h->g.n_cells * sizeof(double);
-  cudaError_t e = cudaMemcpyAsync(st.state, U, bytes, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(st.state, U, bytes, cudaMemcpyDeviceToDevice, s);
   // preconditioner from the state's primitive variables
   if (e == cudaSuccess)
     e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, h->ws.P, s)); });
   if (e == cudaSuccess)
-    e = timed(h, MCFD_PROF_OTHER, s, [&] { return implicit_assemble(st, h->ws.P, h->g.area, dt, dt_per_cell, cfg->gamma, s); });
+    e = timed(h, MCFD_PROF_OTHER, s, [&] { return implicit_assemble(st, h->ws.P, h->g.area, st.dt, st.dt_per_cell, cfg->gamma, s); });
   // jacobian_rate = R1(state)
   if (e == cudaSuccess) e = residual_first_order(h, U, st.rate, s);
-  // |state / scale|
+  // |state / scale|^2, read by the operator on the device
   if (e == cudaSuccess) e = implicit_scaled_sumsq(st, U, st.scale, st.scalars + 8, s);
-  double sumsq = 0.0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&sumsq, st.scalars + 8, sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  st.state_norm = std::sqrt(sumsq);
   st.prepared = e == cudaSuccess;
   return rc(e);
 }
@@ -1303,13 +1335,24 @@ int mcfd_lusgs_apply(mcfd_geom* h, const double* v, double* x, void* stream) {
   return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return lusgs_apply(h->imp, v, x, s); }));
 }
 
+int mcfd_implicit_set_sweep(mcfd_geom* h, int32_t wide_level) {
+  if (!h || wide_level < 0) return MCFD_E_ARG;
+  int c = ensure_implicit(h);
+  if (c) return c;
+  implicit_set_wide_level(h->imp, wide_level);
+  return MCFD_OK;
+}
+
 int mcfd_gmres(mcfd_geom* h, const double* b, double* x, double tol, int32_t max_iter, int32_t krylov_dim,
                int32_t* iterations, void* stream) {
   if (!h || !b || !x || !h->imp_built || !h->imp.prepared || max_iter <= 0 || krylov_dim <= 0) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   MatvecFn mv = implicit_operator(h);
   int it = 0;
-  int r = gmres_solve(h->imp, mv, b, x, tol, max_iter, krylov_dim, &it, s);
+  // the inner loop runs as a captured graph unless events are being recorded
+  // for profiling (a captured loop body holds kernels only)
+  const int key = h->profiling ? -1 : (h->imp_exact_jacobian ? 1 : 0);
+  int r = gmres_solve(h->imp, mv, key, b, x, tol, max_iter, krylov_dim, &it, s);
   if (iterations) *iterations = it;
   switch (r) {
     case GMRES_OK: return MCFD_OK;

@@ -393,6 +393,49 @@ __device__ __forceinline__ double limiter_factor_min_ratio(double value, double 
   return f;
 }
 
+// Venkatakrishnan's limiter in its published form with the smoothing
+// constant (V. Venkatakrishnan, "Convergence to steady state solutions of the
+// Euler equations on unstructured grids with limiters", J. Comput. Phys. 118,
+// 120-130, 1995), an extension beside the reference's form (which has no K):
+// for a face increment d2 = grad . r and d1 = max - v (d2 > 0) or min - v
+// (d2 <= 0),
+//   f = (d1^2 + e2 + 2 d1 d2) / (d1^2 + 2 d2^2 + d1 d2 + e2),
+//   e2 = (K sqrt(A))^3,
+// and the cell factor is the minimum over its faces, not capped at 1 (f
+// exceeds 1 slightly where d2 is small against d1, as in the paper).  f is a
+// rational function of (d1, d2) with e2 > 0, so away from ties between faces
+// and between extreme neighbours the factor is differentiable, which is what
+// a gradient check against finite differences needs.  f = 1 at d2 = 0.
+// Products and sums of the smooth form go through __dmul_rn / __dadd_rn,
+// which are never contracted into FMA: every kernel (forward in each
+// variant, tangent and reverse) evaluates the same bits, so the reverse
+// sweep's minimising face is the forward's.
+__device__ __forceinline__ double venkat_k_e2(double k, double area) {
+  const double t = __dmul_rn(k, sqrt_rn(area));
+  return __dmul_rn(__dmul_rn(t, t), t);
+}
+
+struct VenkatK {
+  double f, N, D, d1;
+};
+
+__device__ __forceinline__ VenkatK venkat_k_face(double value, double increment, double lo, double hi, double e2) {
+  VenkatK r;
+  r.d1 = icmp::gt0(increment) ? __dadd_rn(hi, -value) : __dadd_rn(lo, -value);
+  const double d1d1 = __dmul_rn(r.d1, r.d1), d12 = __dmul_rn(r.d1, increment);
+  r.N = __dadd_rn(__dadd_rn(d1d1, e2), __dadd_rn(d12, d12));
+  r.D = __dadd_rn(__dadd_rn(__dadd_rn(d1d1, __dmul_rn(2.0, __dmul_rn(increment, increment))), d12), e2);
+  r.f = div_rn(r.N, r.D);
+  return r;
+}
+
+// partial derivatives of f with respect to d1 and d2 (from N, D of the face)
+__device__ __forceinline__ void venkat_k_slopes(const VenkatK& v, double increment, double* df_dd1, double* df_dd2) {
+  const double inv = div_rn(1.0, v.D * v.D);
+  *df_dd1 = ((2.0 * v.d1 + 2.0 * increment) * v.D - v.N * (2.0 * v.d1 + increment)) * inv;
+  *df_dd2 = ((2.0 * v.d1) * v.D - v.N * (4.0 * increment + v.d1)) * inv;
+}
+
 __device__ __forceinline__ double limiter_tolerance(double value) {
   double m = abs_of(value);
   return 1e-14 * (icmp::lt_pos(m, 1.0) ? 1.0 : m);  // 1e-14 * max(|v|, 1.0)

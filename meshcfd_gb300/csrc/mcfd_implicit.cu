@@ -5,10 +5,11 @@
 //   1 + sum dt_i rho_f L / (2 A_i) over interior and periodic faces +
 //   dt_i rho L / A_i over boundary faces, off-diagonals -dt_i rho_f L/(2 A_i);
 //   the forward solve (D+L) y = v and backward solve (D+U) x = D y run over
-//   level sets of the natural-cell-order dependency graph, one cooperative
-//   persistent kernel per sweep with a grid barrier between levels, so the
+//   level sets of the natural-cell-order dependency graph, so the
 //   preconditioner is exactly the reference's (only independent rows run
-//   concurrently);
+//   concurrently): runs of narrow levels in one block that barriers between
+//   levels and keeps the latest solutions in a shared-memory ring, wide
+//   levels one grid launch each;
 // * the matrix-free operator v -> v - dt [R1(u + eps s v) - R1(u)] / (eps s)
 //   (_matrix_free_implicit_operator, solver.py:1532-1567);
 // * restarted GMRES(m) as the reference drives SciPy's gmres
@@ -96,50 +97,175 @@ __global__ void k_lusgs_assemble(int C, const int* __restrict__ dptr, const int*
   dclamp[i] = icmp::lt_pos(s, 1e-14) ? 1e-14 : s;  // np.maximum(diagonal, 1e-14)
 }
 
-struct SweepArgs {
-  int n_levels;
+// ------------------------------------------------------------ LU-SGS sweeps
+//
+// Row at sweep position p, cell i: x_i = (r_i - sum_j a_ij x_j) / d_i over
+// the off-diagonal entries in ascending column order, r = v (forward) or
+// D y (backward, D the clamped diagonal); the products and differences round
+// one at a time, the quotient is the correctly rounded one.
+
+struct SweepDev {
   const int* level_ptr;
-  const int* level_cells;
-  const int* row_ptr;   // this sweep's off-diagonal entries per cell
-  const int* row_col;
-  const int* row_val;   // index into rval
+  const int* pos_cell;
+  const int* ent_ptr;    // CSR of the rows (entries beyond the packed ones)
+  const int* ent_cell;
+  const int* ent_pos;
+  const int* ent_val;
   const double* rval;
-  const double* diag;
-  const double* dclamp;  // backward sweep: right-hand side D * y
+  const int* pk_cnt;
+  const int* pk_pos;
+  const int* pk_cell;
+  const double* pk_val;
+  const double* pk_diag;
+  const double* pk_dc;
   const double* in;
   double* out;
   int backward;
 };
 
-// Level-scheduled triangular sweep: rows of one level are independent; the
-// grid barrier orders the levels (cooperative launch: all blocks resident).
-__global__ void __launch_bounds__(kBlock) k_lusgs_sweep(SweepArgs a) {
-  cg::grid_group grid = cg::this_grid();
-  const int stride = gridDim.x * blockDim.x;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int l = 0; l < a.n_levels; ++l) {
-    const int b = a.level_ptr[l], e = a.level_ptr[l + 1];
-    for (int t = b + tid; t < e; t += stride) {
-      const int i = a.level_cells[t];
-      St4 r = ld4(a.in + 4 * (size_t)i);
-      double acc[4] = {r.a, r.b, r.c, r.d};
-      if (a.backward) {
-        const double dc = a.dclamp[i];
-        for (int k = 0; k < 4; ++k) acc[k] = dc * acc[k];
-      }
-      for (int j = a.row_ptr[i]; j < a.row_ptr[i + 1]; ++j) {
-        const double v = a.rval[a.row_val[j]];
-        const St4 x = ld4(a.out + 4 * (size_t)a.row_col[j]);
-        acc[0] = acc[0] - v * x.a;
-        acc[1] = acc[1] - v * x.b;
-        acc[2] = acc[2] - v * x.c;
-        acc[3] = acc[3] - v * x.d;
-      }
-      const double dg = a.diag[i];
-      st4(a.out + 4 * (size_t)i, St4{div_rn(acc[0], dg), div_rn(acc[1], dg), div_rn(acc[2], dg), div_rn(acc[3], dg)});
-    }
-    grid.sync();
+constexpr int kWaveThreads = 512;
+constexpr int kRing = 4096;        // latest solved rows kept in shared memory (128 KiB)
+constexpr int kWideLevel = 16384;  // wider levels get a grid launch each
+constexpr size_t kRingBytes = kRing * 4 * sizeof(double);
+
+// Everything of a row that does not depend on the solution: loaded for the
+// next level before the block barrier, so a level's critical path is the
+// reads of earlier solutions (shared memory) and the row's own arithmetic.
+struct SweepRow {
+  int i, n;
+  St4 r;
+  double dg;
+  double v[kSweepPack];
+  int cp[kSweepPack], cc[kSweepPack];
+};
+
+__device__ __forceinline__ void sweep_load(const SweepDev& a, int p, SweepRow& R) {
+  R.i = a.pos_cell[p];
+  R.n = a.pk_cnt[p];
+#pragma unroll
+  for (int k = 0; k < kSweepPack; ++k) {
+    R.v[k] = a.pk_val[(size_t)p * kSweepPack + k];
+    R.cp[k] = a.pk_pos[(size_t)p * kSweepPack + k];
+    R.cc[k] = a.pk_cell[(size_t)p * kSweepPack + k];
   }
+  R.dg = a.pk_diag[p];
+  const St4 r = ld4(a.in + 4 * (size_t)R.i);
+  if (a.backward) {
+    const double dc = a.pk_dc[p];
+    R.r = St4{dc * r.a, dc * r.b, dc * r.c, dc * r.d};
+  } else {
+    R.r = r;
+  }
+}
+
+__device__ __forceinline__ void sweep_sub(double acc[4], double v, const St4& x) {
+  acc[0] = acc[0] - v * x.a;
+  acc[1] = acc[1] - v * x.b;
+  acc[2] = acc[2] - v * x.c;
+  acc[3] = acc[3] - v * x.d;
+}
+
+// x_p = (r - sum_j a_j x_j) / d over the row's entries in ascending column
+// order; earlier solutions from the ring when their position is at least
+// ring_lo, else from global memory.  Writes the global solution and, when
+// ring is given, the ring slot of position p.
+__device__ __forceinline__ void sweep_solve(const SweepDev& a, const SweepRow& R, int p, const double* ring,
+                                            int ring_lo, double* ring_out) {
+  double acc[4] = {R.r.a, R.r.b, R.r.c, R.r.d};
+#pragma unroll
+  for (int k = 0; k < kSweepPack; ++k) {
+    if (k < R.n) {
+      St4 x;
+      if (ring && R.cp[k] >= ring_lo) {
+        const double* q = ring + 4 * (R.cp[k] & (kRing - 1));
+        x = St4{q[0], q[1], q[2], q[3]};
+      } else {
+        x = ld4(a.out + 4 * (size_t)R.cc[k]);
+      }
+      sweep_sub(acc, R.v[k], x);
+    }
+  }
+  if (R.n > kSweepPack) {  // the rest of a long row from the CSR
+    for (int j = a.ent_ptr[p] + kSweepPack, j1 = a.ent_ptr[p + 1]; j < j1; ++j) {
+      const int cp = a.ent_pos[j];
+      St4 x;
+      if (ring && cp >= ring_lo) {
+        const double* q = ring + 4 * (cp & (kRing - 1));
+        x = St4{q[0], q[1], q[2], q[3]};
+      } else {
+        x = ld4(a.out + 4 * (size_t)a.ent_cell[j]);
+      }
+      sweep_sub(acc, a.rval[a.ent_val[j]], x);
+    }
+  }
+  const St4 res{div_rn(acc[0], R.dg), div_rn(acc[1], R.dg), div_rn(acc[2], R.dg), div_rn(acc[3], R.dg)};
+  st4(a.out + 4 * (size_t)R.i, res);
+  if (ring_out) {
+    double* q = ring_out + 4 * (p & (kRing - 1));
+    q[0] = res.a;
+    q[1] = res.b;
+    q[2] = res.c;
+    q[3] = res.d;
+  }
+}
+
+// Levels [l0, l1) in one block: rows of a level in parallel, a block barrier
+// between levels, the next level's rows loaded before the barrier.  The
+// solutions of the last kRing positions stay in shared memory (slot =
+// position mod kRing); position p' is read from there when p' >= max(end of
+// the current level - kRing, first position of the launch), which no row of
+// the current level can overwrite.
+__global__ void __launch_bounds__(kWaveThreads, 1) k_lusgs_wavefront(SweepDev a, int l0, int l1) {
+  extern __shared__ double ring[];  // [kRing][4]
+  const int base = a.level_ptr[l0];
+  const int t = threadIdx.x;
+  SweepRow R;
+  int b = base, e = a.level_ptr[l0 + 1];
+  bool have = b + t < e;
+  if (have) sweep_load(a, b + t, R);
+  for (int l = l0; l < l1; ++l) {
+    const int lo = max(e - kRing, base);
+    if (have) sweep_solve(a, R, b + t, ring, lo, ring);
+    for (int p = b + t + (int)blockDim.x; p < e; p += blockDim.x) {  // levels wider than the block
+      SweepRow W;
+      sweep_load(a, p, W);
+      sweep_solve(a, W, p, ring, lo, ring);
+    }
+    // the next level's rows, independent of this level's solutions
+    if (l + 1 < l1) {
+      b = e;
+      e = a.level_ptr[l + 2];
+      have = b + t < e;
+      if (have) sweep_load(a, b + t, R);
+    }
+    __syncthreads();
+  }
+}
+
+// One wide level over the whole grid (earlier levels finished in earlier
+// launches on the same stream).
+__global__ void __launch_bounds__(kBlock) k_lusgs_level(SweepDev a, int b, int e) {
+  const int p = b + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= e) return;
+  SweepRow R;
+  sweep_load(a, p, R);
+  sweep_solve(a, R, p, nullptr, 0, nullptr);
+}
+
+// Values of the packed rows after an assembly: the entries' matrix values,
+// the diagonal and the clamped diagonal in sweep order.
+__global__ void k_pack_rows(int C, const int* __restrict__ pos_cell, const int* __restrict__ ent_ptr,
+                            const int* __restrict__ ent_val, const double* __restrict__ rval,
+                            const double* __restrict__ diag, const double* __restrict__ dclamp,
+                            double* __restrict__ pk_val, double* __restrict__ pk_diag, double* __restrict__ pk_dc) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= C) return;
+  const int i = pos_cell[p];
+  const int j0 = ent_ptr[p], n = ent_ptr[p + 1] - j0;
+#pragma unroll
+  for (int k = 0; k < kSweepPack; ++k) pk_val[(size_t)p * kSweepPack + k] = k < n ? rval[ent_val[j0 + k]] : 0.0;
+  pk_diag[p] = diag[i];
+  pk_dc[p] = dclamp[i];
 }
 
 // ------------------------------------------------------------------ vectors
@@ -167,13 +293,6 @@ __global__ void k_dot_final(int blocks, const double* __restrict__ partials, dou
     for (int b = 0; b < blocks; ++b) s += partials[b];
     out[0] = s;
   }
-}
-
-// y -= alpha[0] * x   (modified Gram-Schmidt update with a device scalar)
-__global__ void k_axmy_dev(long long n, const double* __restrict__ alpha, const double* __restrict__ x,
-                           double* __restrict__ y) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) y[i] = y[i] - alpha[0] * x[i];
 }
 
 // Newton equation of the implicit step (solver.py:1415-1426):
@@ -294,11 +413,6 @@ __global__ void k_axpy(long long n, double a, const double* __restrict__ x, doub
   if (i < n) y[i] = y[i] + a * x[i];
 }
 
-__global__ void k_scale(long long n, double a, double* __restrict__ x) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) x[i] = x[i] * a;
-}
-
 // r = b - x
 __global__ void k_sub(long long n, const double* __restrict__ b, const double* __restrict__ x,
                       double* __restrict__ r) {
@@ -308,10 +422,13 @@ __global__ void k_sub(long long n, const double* __restrict__ b, const double* _
 
 // ------------------------------------------------------------- FD operator
 
-// eps = sqrt(machine eps) * max(1, |u/s|) / |v|  (solver.py:1546-1561)
-__global__ void k_fd_eps(const double* __restrict__ v_sumsq, double state_norm, double* eps_out) {
+// eps = sqrt(machine eps) * max(1, |u/s|) / |v|  (solver.py:1546-1561);
+// |u/s| = sqrt of the prepared sum of squares
+__global__ void k_fd_eps(const double* __restrict__ v_sumsq, const double* __restrict__ state_sumsq,
+                         double* eps_out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     const double dn = sqrt_rn(v_sumsq[0]);
+    const double state_norm = sqrt_rn(state_sumsq[0]);
     const double fd = 1.4901161193847656e-08;  // math.sqrt(np.finfo(float).eps)
     eps_out[0] = (dn == 0.0) ? 0.0 : div_rn(fd * (state_norm > 1.0 ? state_norm : 1.0), dn);
   }
@@ -319,17 +436,18 @@ __global__ void k_fd_eps(const double* __restrict__ v_sumsq, double state_norm, 
 
 // U_p = u + (eps * s_k) * v
 __global__ void k_fd_perturb(int C, const double* __restrict__ u, const double* __restrict__ v,
-                             const double* __restrict__ eps, ScaleVec s, double* __restrict__ up) {
+                             const double* __restrict__ eps, const double* __restrict__ scale,
+                             double* __restrict__ up) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 4 * C) return;
   const double e = eps[0];
-  up[i] = u[i] + (e * s.v[i & 3]) * v[i];
+  up[i] = u[i] + (e * scale[i & 3]) * v[i];
 }
 
 // out = v - dt * ((R_p - R) / eps) / s_k ; out = v when |v| = 0
 __global__ void k_fd_combine(int C, const double* __restrict__ v, const double* __restrict__ rp,
                              const double* __restrict__ rate, const double* __restrict__ eps,
-                             ScaleVec s, const double* __restrict__ dt, int dt_per_cell,
+                             const double* __restrict__ scale, const double* __restrict__ dt, int dt_per_cell,
                              double* __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 4 * C) return;
@@ -340,7 +458,195 @@ __global__ void k_fd_combine(int C, const double* __restrict__ v, const double* 
   }
   const double d = dt_per_cell ? dt[i >> 2] : dt[0];
   const double jv = div_rn(rp[i] - rate[i], e);
-  out[i] = v[i] - div_rn(d * jv, s.v[i & 3]);
+  out[i] = v[i] - div_rn(d * jv, scale[i & 3]);
+}
+
+__global__ void k_set_scale(ScaleVec s, double* __restrict__ out) {
+  if (threadIdx.x < 4) out[threadIdx.x] = s.v[threadIdx.x];
+}
+
+// ------------------------------------------------------- GMRES on the device
+
+// Deterministic grid dot product inside a cooperative kernel: block partials
+// (grid-stride sums, shared-memory tree) into one of two buffers, a grid
+// barrier, then every block adds the partials in the same fixed order (32
+// strided lane sums and a shuffle tree).  Alternating buffers make one
+// barrier per product enough: a block reads buffer k only before it reaches
+// the barrier of product k + 1.
+__device__ double grid_dot(cg::grid_group& grid, const double* __restrict__ x, const double* __restrict__ y,
+                           long long n, double* __restrict__ partials, int& buf, double* sh) {
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += x[i] * y[i];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kBlock / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  double* part = partials + (size_t)buf * gridDim.x;
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+  buf ^= 1;
+  grid.sync();
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) t += part[b];
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+    if (threadIdx.x == 0) sh[kBlock] = t;
+  }
+  __syncthreads();
+  const double total = sh[kBlock];
+  __syncthreads();
+  return total;
+}
+
+// Modified Gram-Schmidt of w against basis vectors 0..col (col from the
+// cycle state): hcol[k] = <v_k, w> then w -= hcol[k] v_k, in order;
+// hcol[m + 1] = |w|^2 before, hcol[m + 2] = |w|^2 after.  Each thread
+// updates the entries its grid-stride dot products read, so only the
+// reductions need the grid barrier.
+struct MgsArgs {
+  const double* basis;
+  long long n;
+  double* w;
+  const GmresCycle* cycle;
+  double* hcol;
+  int m;
+  double* partials;  // [2][gridDim.x]
+};
+
+__global__ void __launch_bounds__(kBlock) k_mgs(MgsArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ double sh[kBlock + 1];
+  int buf = 0;
+  const int col = a.cycle->col;
+  const double before = grid_dot(grid, a.w, a.w, a.n, a.partials, buf, sh);
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.hcol[a.m + 1] = before;
+  for (int k = 0; k <= col; ++k) {
+    const double* v = a.basis + (size_t)k * a.n;
+    const double h = grid_dot(grid, v, a.w, a.n, a.partials, buf, sh);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.hcol[k] = h;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.n; i += (long long)gridDim.x * blockDim.x)
+      a.w[i] = a.w[i] - h * v[i];
+  }
+  const double after = grid_dot(grid, a.w, a.w, a.n, a.partials, buf, sh);
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.hcol[a.m + 2] = after;
+}
+
+// LAPACK dlartg for finite, well-scaled inputs (Anderson's 2017 algorithm
+// as in LAPACK 3.10+): c = |f| / d, r = sign(f) d, s = g / r.
+__device__ void lartg_dev(double f, double g, double* c, double* sn, double* r) {
+  if (g == 0.0) {
+    *c = 1.0;
+    *sn = 0.0;
+    *r = f;
+  } else if (f == 0.0) {
+    *c = 0.0;
+    *sn = g > 0.0 ? 1.0 : -1.0;
+    *r = fabs(g);
+  } else {
+    const double d = sqrt(f * f + g * g);
+    *c = fabs(f) / d;
+    *r = copysign(d, f);
+    *sn = g / *r;
+  }
+}
+
+// SciPy's inner-loop bookkeeping for column col (iterative.py, gmres):
+// Hessenberg column from the Gram-Schmidt products, breakdown test
+// h1 <= eps h0, the previous rotations applied, a new rotation, the
+// residual estimate |S[col + 1]|, and the stop decision; sets the while
+// condition of the captured inner loop when ``handle`` is given.
+__global__ void k_givens(GmresCycle* cyc, const double* __restrict__ hcol, double* __restrict__ hess,
+                         double* __restrict__ givens, int m, cudaGraphConditionalHandle handle, int use_handle) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int col = cyc->col;
+  double* H = hess + (size_t)col * (m + 1);
+  double* gc = givens;
+  double* gs = givens + m;
+  double* S = givens + 2 * m;
+  const double eps = 2.220446049250313e-16;
+  const double h0 = sqrt(hcol[m + 1]), h1 = sqrt(hcol[m + 2]);
+  for (int k = 0; k <= col; ++k) H[k] = hcol[k];
+  H[col + 1] = h1;
+  int breakdown = 0;
+  double inv = 1.0;
+  if (h1 <= eps * h0) {
+    H[col + 1] = 0.0;
+    breakdown = 1;
+  } else {
+    inv = 1.0 / h1;
+  }
+  for (int k = 0; k < col; ++k) {
+    const double c = gc[k], sn = gs[k];
+    const double n0 = H[k], n1 = H[k + 1];
+    H[k] = c * n0 + sn * n1;
+    H[k + 1] = -sn * n0 + c * n1;
+  }
+  double c, sn, mag;
+  lartg_dev(H[col], H[col + 1], &c, &sn, &mag);
+  gc[col] = c;
+  gs[col] = sn;
+  H[col] = mag;
+  H[col + 1] = 0.0;
+  const double t = -sn * S[col];
+  S[col] = c * S[col];
+  S[col + 1] = t;
+  const double presid = fabs(t);
+  cyc->presid = presid;
+  cyc->inv_h1 = inv;
+  cyc->breakdown = breakdown;
+  cyc->last = col;
+  cyc->inner = cyc->inner + 1;
+  cyc->col = col + 1;
+  const int done = (presid <= cyc->ptol) || breakdown || (col + 1 >= cyc->restart);
+  cyc->done = done;
+  if (use_handle) cudaGraphSetConditional(handle, done ? 0u : 1u);
+}
+
+// vcur = basis[col]
+__global__ void k_take_column(const double* __restrict__ basis, long long n, const GmresCycle* cyc,
+                              double* __restrict__ vcur) {
+  const double* v = basis + (size_t)cyc->col * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    vcur[i] = v[i];
+}
+
+// basis[last + 1] = w * inv_h1 (w unscaled at breakdown)
+__global__ void k_next_basis(double* __restrict__ basis, long long n, const GmresCycle* cyc,
+                             const double* __restrict__ w) {
+  double* v = basis + (size_t)(cyc->last + 1) * n;
+  const int scale = !cyc->breakdown;
+  const double inv = cyc->inv_h1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v[i] = scale ? w[i] * inv : w[i];
+}
+
+// start of a restart cycle: S = (|z|, 0, ...), basis[0] = z / |z|, cycle
+// counters reset; |z|^2 given on the device
+__global__ void k_cycle_start(GmresCycle* cyc, double* __restrict__ givens, int m, const double* __restrict__ zsq,
+                              int restart, double ptol, double* __restrict__ inv_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double z = sqrt(zsq[0]);
+  double* S = givens + 2 * m;
+  for (int k = 0; k <= m; ++k) S[k] = 0.0;
+  S[0] = z;
+  inv_out[0] = 1.0 / z;
+  cyc->col = 0;
+  cyc->last = -1;
+  cyc->restart = restart;
+  cyc->inner = 0;
+  cyc->breakdown = 0;
+  cyc->done = 0;
+  cyc->ptol = ptol;
+  cyc->presid = 0.0;
+  cyc->inv_h1 = 1.0;
+}
+
+// x = x * alpha[0]
+__global__ void k_scale_dev(long long n, const double* __restrict__ alpha, double* __restrict__ x) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) x[i] = x[i] * alpha[0];
 }
 
 }  // namespace
@@ -353,6 +659,33 @@ cudaError_t implicit_dot(ImplicitState& st, long long n, const double* x, const 
   k_dot_partial<<<kRedBlocks, kBlock, 0, s>>>(n, x, y, st.partials);
   k_dot_final<<<1, 32, 0, s>>>(kRedBlocks, st.partials, out);
   return cudaGetLastError();
+}
+
+// Launches of one sweep: runs of consecutive levels at most `wide` rows wide
+// in one wavefront launch, each wider level alone in a grid launch.
+static void sweep_schedule(SweepPlan& pl, int wide) {
+  const std::vector<int>& lp = pl.host_level_ptr;
+  const int nlev = (int)lp.size() - 1;
+  pl.schedule.clear();
+  int l = 0;
+  while (l < nlev) {
+    if (lp[l + 1] - lp[l] > wide) {
+      pl.schedule.push_back({0, l, l + 1});
+      ++l;
+      continue;
+    }
+    int l1 = l;
+    while (l1 < nlev && lp[l1 + 1] - lp[l1] <= wide) ++l1;
+    pl.schedule.push_back({1, l, l1});
+    l = l1;
+  }
+}
+
+void implicit_set_wide_level(ImplicitState& st, int wide) {
+  st.wide_level = wide > 0 ? wide : kWideLevel;
+  sweep_schedule(st.fwd, st.wide_level);
+  sweep_schedule(st.bwd, st.wide_level);
+  st.inner_key = -1;  // the captured loop holds the old launches
 }
 
 cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
@@ -405,9 +738,10 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
     std::sort(lower[i].begin(), lower[i].end());
     std::sort(upper[i].begin(), upper[i].end());
   }
-  // level sets
-  auto levels = [&](bool fwd, std::vector<int>& lptr, std::vector<int>& lcells) {
-    std::vector<int> lev(C, 0);
+  // level sets of the natural-order dependency graph: forward over the
+  // lower entries (col < i), backward over the upper ones (col > i)
+  auto levels = [&](bool fwd, std::vector<int>& lev) {
+    lev.assign(C, 0);
     int nlev = 0;
     if (fwd) {
       for (int i = 0; i < C; ++i) {
@@ -425,32 +759,61 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
         nlev = std::max(nlev, m + 1);
       }
     }
-    lptr.assign(nlev + 1, 0);
-    for (int i = 0; i < C; ++i) lptr[lev[i] + 1]++;
-    for (int l = 0; l < nlev; ++l) lptr[l + 1] += lptr[l];
-    lcells.resize(C);
-    std::vector<int> fill(lptr.begin(), lptr.end() - 1);
-    for (int i = 0; i < C; ++i) lcells[fill[lev[i]]++] = i;
     return nlev;
   };
-  std::vector<int> flp, flc, blp, blc;
-  st.n_levels_fwd = levels(true, flp, flc);
-  st.n_levels_bwd = levels(false, blp, blc);
-  auto csr = [&](std::vector<std::vector<std::pair<int, int>>>& rowsv, std::vector<int>& ptr,
-                 std::vector<int>& col, std::vector<int>& val, bool drop_diag) {
-    ptr.assign(C + 1, 0);
+  // sweep order: cells by level (stable in cell id); entries of each row in
+  // ascending column order with the column's own sweep position
+  struct HostPlan {
+    std::vector<int> level_ptr, pos_cell, ent_ptr, ent_cell, ent_pos, ent_val;
+  };
+  auto plan = [&](bool fwd, HostPlan& hp) {
+    std::vector<int> lev;
+    const int nlev = levels(fwd, lev);
+    hp.level_ptr.assign(nlev + 1, 0);
+    for (int i = 0; i < C; ++i) hp.level_ptr[lev[i] + 1]++;
+    for (int l = 0; l < nlev; ++l) hp.level_ptr[l + 1] += hp.level_ptr[l];
+    hp.pos_cell.resize(C);
+    std::vector<int> fill(hp.level_ptr.begin(), hp.level_ptr.end() - 1), pos_of(C);
     for (int i = 0; i < C; ++i) {
-      for (auto& e : rowsv[i]) {
-        if (drop_diag && e.first == i) continue;
-        col.push_back(e.first);
-        val.push_back(e.second);
+      pos_of[i] = fill[lev[i]]++;
+      hp.pos_cell[pos_of[i]] = i;
+    }
+    hp.ent_ptr.assign(C + 1, 0);
+    for (int p = 0; p < C; ++p) {
+      const int i = hp.pos_cell[p];
+      for (auto& e : (fwd ? lower : upper)[i]) {
+        if (e.first == i) continue;  // a self-coupled periodic pair: on the diagonal
+        hp.ent_cell.push_back(e.first);
+        hp.ent_pos.push_back(pos_of[e.first]);
+        hp.ent_val.push_back(e.second);
       }
-      ptr[i + 1] = (int)col.size();
+      hp.ent_ptr[p + 1] = (int)hp.ent_cell.size();
+    }
+    return nlev;
+  };
+  HostPlan hf, hb;
+  st.n_levels_fwd = plan(true, hf);
+  st.n_levels_bwd = plan(false, hb);
+  // packed topology: the first kSweepPack entries of every row
+  struct Packed {
+    std::vector<int> cnt, pos, cell;
+  };
+  auto pack = [&](const HostPlan& hp, Packed& pk) {
+    pk.cnt.resize(C);
+    pk.pos.assign((size_t)C * kSweepPack, 0);
+    pk.cell.assign((size_t)C * kSweepPack, 0);
+    for (int p = 0; p < C; ++p) {
+      const int j0 = hp.ent_ptr[p], n = hp.ent_ptr[p + 1] - j0;
+      pk.cnt[p] = n;
+      for (int k = 0; k < kSweepPack && k < n; ++k) {
+        pk.pos[(size_t)p * kSweepPack + k] = hp.ent_pos[j0 + k];
+        pk.cell[(size_t)p * kSweepPack + k] = hp.ent_cell[j0 + k];
+      }
     }
   };
-  std::vector<int> lptr, lcol, lval, uptr, ucol, uval;
-  csr(lower, lptr, lcol, lval, true);
-  csr(upper, uptr, ucol, uval, true);
+  Packed pf, pb;
+  pack(hf, pf);
+  pack(hb, pb);
 
   // device memory
   std::vector<std::pair<void**, size_t>> allocs;
@@ -477,17 +840,32 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   UP(rptr, rptr);
   UP(rref, rref);
   UP(rcol, rcol);
-  UP(flp, fwd_level_ptr);
-  UP(flc, fwd_level_cells);
-  UP(blp, bwd_level_ptr);
-  UP(blc, bwd_level_cells);
-  UP(lptr, lower_ptr);
-  UP(lcol, lower_col);
-  UP(lval, lower_val);
-  UP(uptr, upper_ptr);
-  UP(ucol, upper_col);
-  UP(uval, upper_val);
+  UP(hf.level_ptr, fwd.level_ptr);
+  UP(hf.pos_cell, fwd.pos_cell);
+  UP(hf.ent_ptr, fwd.ent_ptr);
+  UP(hf.ent_cell, fwd.ent_cell);
+  UP(hf.ent_pos, fwd.ent_pos);
+  UP(hf.ent_val, fwd.ent_val);
+  UP(hb.level_ptr, bwd.level_ptr);
+  UP(hb.pos_cell, bwd.pos_cell);
+  UP(hb.ent_ptr, bwd.ent_ptr);
+  UP(hb.ent_cell, bwd.ent_cell);
+  UP(hb.ent_pos, bwd.ent_pos);
+  UP(hb.ent_val, bwd.ent_val);
+  UP(pf.cnt, fwd.pk_cnt);
+  UP(pf.pos, fwd.pk_pos);
+  UP(pf.cell, fwd.pk_cell);
+  UP(pb.cnt, bwd.pk_cnt);
+  UP(pb.pos, bwd.pk_pos);
+  UP(pb.cell, bwd.pk_cell);
 #undef UP
+  st.fwd.n_levels = st.n_levels_fwd;
+  st.bwd.n_levels = st.n_levels_bwd;
+  st.fwd.host_level_ptr = hf.level_ptr;
+  st.bwd.host_level_ptr = hb.level_ptr;
+  st.wide_level = kWideLevel;
+  sweep_schedule(st.fwd, st.wide_level);
+  sweep_schedule(st.bwd, st.wide_level);
   auto zeros = [&](size_t n, double** dst) {
     if (e == cudaSuccess) e = cudaMalloc((void**)dst, std::max<size_t>(n, 1) * sizeof(double));
     if (e == cudaSuccess) st.owned.push_back(*dst);
@@ -505,26 +883,54 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   zeros(N4, &st.rp);
   zeros(N4, &st.w);
   zeros(N4, &st.av);
+  zeros(N4, &st.vcur);
+  for (SweepPlan* pl : {&st.fwd, &st.bwd}) {
+    zeros((size_t)C * kSweepPack, &pl->pk_val);
+    zeros(C, &pl->pk_diag);
+    zeros(C, &pl->pk_dc);
+  }
   zeros(kRedBlocks, &st.partials);
   zeros(64, &st.scalars);
+  zeros(4, &st.scale_dev);
+  zeros(C, &st.dt_buf);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&st.cycle, sizeof(GmresCycle));
+  if (e == cudaSuccess) st.owned.push_back(st.cycle);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&st.cycle_host, sizeof(GmresCycle));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_wavefront, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kRingBytes);
   if (e == cudaSuccess) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lusgs_sweep, kBlock, 0);
-    st.sweep_blocks = std::max(1, sms * std::min(per_sm, 2));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mgs, kBlock, 0);
+    st.mgs_blocks = std::max(1, sms * std::min(per_sm, 2));
+    zeros(2 * (size_t)st.mgs_blocks, &st.mgs_partials);
   }
+  st.dt = st.dt_buf;
   return e;
 }
 
+static void free_gmres_basis(ImplicitState& st) {
+  if (st.inner_exec) cudaGraphExecDestroy(st.inner_exec);
+  if (st.inner_graph) cudaGraphDestroy(st.inner_graph);
+  st.inner_exec = nullptr;
+  st.inner_graph = nullptr;
+  st.inner_key = -1;
+  for (double** p : {&st.basis, &st.hess, &st.givens, &st.hcol}) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  st.basis_m = 0;
+}
+
 void implicit_free(ImplicitState& st) {
+  free_gmres_basis(st);
+  if (st.cap_stream) cudaStreamDestroy(st.cap_stream);
+  st.cap_stream = nullptr;
   for (void* p : st.owned) cudaFree(p);
   st.owned.clear();
-  for (double* v : st.krylov) cudaFree(v);
-  st.krylov.clear();
-  if (st.hcol) cudaFree(st.hcol);
-  st.hcol = nullptr;
-  st.hcol_size = 0;
+  if (st.cycle_host) cudaFreeHost(st.cycle_host);
+  st.cycle_host = nullptr;
 }
 
 cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* area, const double* dt,
@@ -543,54 +949,63 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
   k_lusgs_assemble<<<blocks_for(st.n_cells), kBlock, 0, s>>>(st.n_cells, st.dptr, st.dref, st.coef, st.bterm,
                                                              st.rptr, st.rref, st.rcol, area, dt, dt_per_cell,
                                                              st.diag, st.dclamp, st.rval);
+  for (SweepPlan* pl : {&st.fwd, &st.bwd}) {
+    count_launch();
+    k_pack_rows<<<blocks_for(st.n_cells), kBlock, 0, s>>>(st.n_cells, pl->pos_cell, pl->ent_ptr, pl->ent_val,
+                                                          st.rval, st.diag, st.dclamp, pl->pk_val, pl->pk_diag,
+                                                          pl->pk_dc);
+  }
+  return cudaGetLastError();
+}
+
+static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const double* in, double* out, int backward,
+                         cudaStream_t s) {
+  SweepDev a{pl.level_ptr, pl.pos_cell, pl.ent_ptr, pl.ent_cell, pl.ent_pos, pl.ent_val, st.rval,
+             pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, in, out, backward};
+  for (const SweepPlan::Launch& l : pl.schedule) {
+    count_launch();
+    if (l.wavefront) {
+      k_lusgs_wavefront<<<1, kWaveThreads, kRingBytes, s>>>(a, l.l0, l.l1);
+    } else {
+      const int b = pl.host_level_ptr[l.l0], e = pl.host_level_ptr[l.l0 + 1];
+      k_lusgs_level<<<blocks_for(e - b), kBlock, 0, s>>>(a, b, e);
+    }
+  }
   return cudaGetLastError();
 }
 
 cudaError_t lusgs_apply(ImplicitState& st, const double* v, double* x, cudaStream_t s) {
-  SweepArgs f{};
-  f.n_levels = st.n_levels_fwd;
-  f.level_ptr = st.fwd_level_ptr;
-  f.level_cells = st.fwd_level_cells;
-  f.row_ptr = st.lower_ptr;
-  f.row_col = st.lower_col;
-  f.row_val = st.lower_val;
-  f.rval = st.rval;
-  f.diag = st.diag;
-  f.dclamp = st.dclamp;
-  f.in = v;
-  f.out = st.tmp;
-  f.backward = 0;
-  void* args_f[] = {&f};
-  count_launch(2);
-  cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_lusgs_sweep, st.sweep_blocks, kBlock, args_f, 0, s);
-  if (e != cudaSuccess) return e;
-  SweepArgs b = f;
-  b.n_levels = st.n_levels_bwd;
-  b.level_ptr = st.bwd_level_ptr;
-  b.level_cells = st.bwd_level_cells;
-  b.row_ptr = st.upper_ptr;
-  b.row_col = st.upper_col;
-  b.row_val = st.upper_val;
-  b.in = st.tmp;
-  b.out = x;
-  b.backward = 1;
-  void* args_b[] = {&b};
-  return cudaLaunchCooperativeKernel((const void*)k_lusgs_sweep, st.sweep_blocks, kBlock, args_b, 0, s);
+  cudaError_t e = sweep(st.fwd, st, v, st.tmp, 0, s);  // (D + L) y = v
+  if (e == cudaSuccess) e = sweep(st.bwd, st, st.tmp, x, 1, s);  // (D + U) x = D y
+  return e;
+}
+
+cudaError_t implicit_set_operator(ImplicitState& st, ScaleVec scale, const double* dt, int dt_per_cell,
+                                  cudaStream_t s) {
+  st.scale = scale;
+  st.dt_per_cell = dt_per_cell;
+  count_launch();
+  k_set_scale<<<1, 32, 0, s>>>(scale, st.scale_dev);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(st.dt_buf, dt, (dt_per_cell ? (size_t)st.n_cells : 1) * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s);
+  st.dt = st.dt_buf;
+  return e;
 }
 
 cudaError_t fd_operator(ImplicitState& st, const ResidualFn& residual1, const double* v, double* out,
                         cudaStream_t s) {
   const int C = st.n_cells;
   const long long N = 4LL * C;
-  const double* dt = st.dt;
-  const int dt_per_cell = st.dt_per_cell;
   cudaError_t e = implicit_dot(st, N, v, v, st.scalars + 0, s);
   count_launch(3);
-  k_fd_eps<<<1, 32, 0, s>>>(st.scalars + 0, st.state_norm, st.scalars + 1);
-  k_fd_perturb<<<blocks_for(N), kBlock, 0, s>>>(C, st.state, v, st.scalars + 1, st.scale, st.up);
+  k_fd_eps<<<1, 32, 0, s>>>(st.scalars + 0, st.scalars + 8, st.scalars + 1);
+  k_fd_perturb<<<blocks_for(N), kBlock, 0, s>>>(C, st.state, v, st.scalars + 1, st.scale_dev, st.up);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e == cudaSuccess) e = residual1(st.up, st.rp, s);
-  k_fd_combine<<<blocks_for(N), kBlock, 0, s>>>(C, v, st.rp, st.rate, st.scalars + 1, st.scale, dt, dt_per_cell, out);
+  k_fd_combine<<<blocks_for(N), kBlock, 0, s>>>(C, v, st.rp, st.rate, st.scalars + 1, st.scale_dev, st.dt,
+                                                st.dt_per_cell, out);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;
 }
@@ -602,52 +1017,125 @@ static double host_scalar(const double* d, cudaStream_t s, cudaError_t* e) {
   return h;
 }
 
-// LAPACK dlartg for finite, well-scaled inputs (Anderson's 2017 algorithm
-// as in LAPACK 3.10+): c = |f| / d, r = sign(f) d, s = g / r.
-static void lartg(double f, double g, double* c, double* sn, double* r) {
-  if (g == 0.0) {
-    *c = 1.0;
-    *sn = 0.0;
-    *r = f;
-  } else if (f == 0.0) {
-    *c = 0.0;
-    *sn = g > 0.0 ? 1.0 : -1.0;
-    *r = std::fabs(g);
-  } else {
-    double d = std::sqrt(f * f + g * g);
-    *c = std::fabs(f) / d;
-    *r = std::copysign(d, f);
-    *sn = g / *r;
-  }
+// Krylov basis, Hessenberg columns and rotations for restart length m.
+static cudaError_t ensure_gmres_basis(ImplicitState& st, int m) {
+  if (st.basis_m >= m) return cudaSuccess;
+  free_gmres_basis(st);
+  const size_t N = 4 * (size_t)st.n_cells;
+  cudaError_t e = cudaMalloc((void**)&st.basis, (size_t)(m + 1) * N * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&st.hess, (size_t)m * (m + 1) * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&st.givens, (size_t)(3 * m + 2) * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&st.hcol, (size_t)(m + 3) * sizeof(double));
+  if (e == cudaSuccess) st.basis_m = m;
+  return e;
 }
 
-int gmres_solve(ImplicitState& st, const MatvecFn& matvec, const double* b, double* x, double tol,
+// One Arnoldi step of SciPy's inner loop, all on the device: basis[col] ->
+// matvec -> preconditioner -> Gram-Schmidt -> Givens -> basis[col + 1].
+static cudaError_t arnoldi_step(ImplicitState& st, const MatvecFn& matvec, int m, cudaGraphConditionalHandle handle,
+                                int use_handle, cudaStream_t s) {
+  const long long N = 4LL * st.n_cells;
+  const int grid = (int)std::min<long long>(blocks_for(N), 152LL * 8);
+  count_launch();
+  k_take_column<<<grid, kBlock, 0, s>>>(st.basis, N, st.cycle, st.vcur);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = matvec(st.vcur, st.av, s);
+  if (e == cudaSuccess) e = lusgs_apply(st, st.av, st.w, s);
+  if (e == cudaSuccess) {
+    MgsArgs a{st.basis, N, st.w, st.cycle, st.hcol, m, st.mgs_partials};
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(st.mgs_blocks);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    count_launch();
+    e = cudaLaunchKernelEx(&cfg, k_mgs, a);
+  }
+  if (e == cudaSuccess) {
+    count_launch(2);
+    k_givens<<<1, 32, 0, s>>>(st.cycle, st.hcol, st.hess, st.givens, m, handle, use_handle);
+    k_next_basis<<<grid, kBlock, 0, s>>>(st.basis, N, st.cycle, st.w);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+// The inner loop as a graph: a while node whose body is one Arnoldi step;
+// the Givens kernel clears the condition when the cycle is done.  Built once
+// per (restart length, operator) and replayed for every cycle.  Returns false
+// (and the caller steps from the host) when the runtime refuses any part.
+static bool ensure_inner_graph(ImplicitState& st, const MatvecFn& matvec, int key, int m) {
+  if (st.graph_failed) return false;
+  if (st.inner_exec && st.inner_key == key) return true;
+  if (st.inner_exec) cudaGraphExecDestroy(st.inner_exec);
+  if (st.inner_graph) cudaGraphDestroy(st.inner_graph);
+  st.inner_exec = nullptr;
+  st.inner_graph = nullptr;
+  if (!st.cap_stream && cudaStreamCreateWithFlags(&st.cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    st.graph_failed = true;
+    return false;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaGraphConditionalHandle handle{};
+  bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess &&
+            cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  cudaGraphNodeParams params{};
+  cudaGraphNode_t node;
+  if (ok) {
+    params.type = cudaGraphNodeTypeConditional;
+    params.conditional.handle = handle;
+    params.conditional.type = cudaGraphCondTypeWhile;
+    params.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &params) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = params.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(st.cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      const long long before = launch_count();
+      const bool step_ok = arnoldi_step(st, matvec, m, handle, 1, st.cap_stream) == cudaSuccess;
+      count_launch(-(int)(launch_count() - before));  // captured, not launched
+      cudaGraph_t captured = nullptr;
+      ok = cudaStreamEndCapture(st.cap_stream, &captured) == cudaSuccess && step_ok;
+      size_t nodes = 0;
+      if (ok) ok = cudaGraphGetNodes(body, nullptr, &nodes) == cudaSuccess;
+      st.inner_nodes = (int)nodes;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&st.inner_exec, graph, 0) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();  // clear a refused call's error
+    if (st.inner_exec) cudaGraphExecDestroy(st.inner_exec);
+    st.inner_exec = nullptr;
+    if (graph) cudaGraphDestroy(graph);
+    st.graph_failed = true;
+    return false;
+  }
+  st.inner_graph = graph;
+  st.inner_key = key;
+  return true;
+}
+
+int gmres_solve(ImplicitState& st, const MatvecFn& matvec, int matvec_key, const double* b, double* x, double tol,
                 int max_iter, int m, int* iterations, cudaStream_t s) {
   const long long N = 4LL * st.n_cells;
   cudaError_t e = cudaSuccess;
   auto grid = [&](long long n) { return blocks_for(n); };
-  // Krylov basis (allocated once per size)
-  if ((int)st.krylov.size() < m + 1) {
-    for (int k = (int)st.krylov.size(); k < m + 1; ++k) {
-      double* p = nullptr;
-      e = cudaMalloc((void**)&p, N * sizeof(double));
-      if (e != cudaSuccess) return GMRES_CUDA;
-      st.krylov.push_back(p);
-    }
-  }
+  if (ensure_gmres_basis(st, m) != cudaSuccess) return GMRES_CUDA;
+  const bool graph = matvec_key >= 0 && ensure_inner_graph(st, matvec, matvec_key * 4096 + m, m);
   double* w = st.w;
   double* av = st.av;
-  if (st.hcol_size < m + 3) {
-    if (st.hcol) cudaFree(st.hcol);
-    st.hcol = nullptr;
-    if (cudaMalloc((void**)&st.hcol, (m + 3) * sizeof(double)) != cudaSuccess) return GMRES_CUDA;
-    st.hcol_size = m + 3;
-  }
-  const double eps = 2.220446049250313e-16;
   cudaMemsetAsync(x, 0, N * sizeof(double), s);
   int used = 0;
   *iterations = 0;
   bool x_nonzero = false;
+  std::vector<double> H, S;
+  GmresCycle& cyc = *st.cycle_host;
   while (used < max_iter) {
     const int restart = std::min(m, max_iter - used);
     // ---- one SciPy gmres call with maxiter=1 (iterative.py, gmres)
@@ -663,7 +1151,7 @@ int gmres_solve(ImplicitState& st, const MatvecFn& matvec, const double* b, doub
     e = implicit_dot(st, N, w, w, st.scalars + 3, s);
     const double mb = std::sqrt(host_scalar(st.scalars + 3, s, &e));
     double ptol = mb * std::min(1.0, atol / bnrm2);
-    double* r = st.krylov[0];
+    double* r = st.basis;
     if (x_nonzero) {
       if (matvec(x, av, s) != cudaSuccess) return GMRES_CUDA;
       count_launch();
@@ -673,87 +1161,59 @@ int gmres_solve(ImplicitState& st, const MatvecFn& matvec, const double* b, doub
     }
     e = implicit_dot(st, N, r, r, st.scalars + 4, s);
     if (std::sqrt(host_scalar(st.scalars + 4, s, &e)) < atol) return GMRES_OK;
-    // v0 = psolve(r) / |psolve(r)|
-    if (lusgs_apply(st, r, st.krylov[0], s) != cudaSuccess) return GMRES_CUDA;
-    e = implicit_dot(st, N, st.krylov[0], st.krylov[0], st.scalars + 5, s);
-    const double tmp0 = std::sqrt(host_scalar(st.scalars + 5, s, &e));
-    count_launch();
-    k_scale<<<grid(N), kBlock, 0, s>>>(N, 1.0 / tmp0, st.krylov[0]);
-    std::vector<double> S(restart + 1, 0.0), gc(restart, 0.0), gs(restart, 0.0);
-    std::vector<std::vector<double>> h(restart, std::vector<double>(restart + 1, 0.0));
-    S[0] = tmp0;
-    double presid = 0.0;
-    bool breakdown = false;
-    int col = 0;
-    int inner = 0;
-    double* hdev = st.hcol;  // h[col][0..col], then |w|^2 before and after at m+1, m+2
-    for (col = 0; col < restart; ++col) {
-      if (matvec(st.krylov[col], av, s) != cudaSuccess) return GMRES_CUDA;
-      if (lusgs_apply(st, av, w, s) != cudaSuccess) return GMRES_CUDA;
-      // modified Gram-Schmidt with device scalars (no host round trip)
-      e = implicit_dot(st, N, w, w, hdev + m + 1, s);
-      for (int k = 0; k <= col; ++k) {
-        implicit_dot(st, N, st.krylov[k], w, hdev + k, s);
-        count_launch();
-        k_axmy_dev<<<grid(N), kBlock, 0, s>>>(N, hdev + k, st.krylov[k], w);
-      }
-      e = implicit_dot(st, N, w, w, hdev + m + 2, s);
-      std::vector<double> hh(m + 3);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(hh.data(), hdev, (m + 3) * sizeof(double), cudaMemcpyDeviceToHost, s);
+    // v0 = psolve(r) / |psolve(r)|, S = (|psolve(r)|, 0, ...)
+    if (lusgs_apply(st, r, w, s) != cudaSuccess) return GMRES_CUDA;
+    cudaMemcpyAsync(st.basis, w, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    e = implicit_dot(st, N, st.basis, st.basis, st.scalars + 5, s);
+    count_launch(2);
+    k_cycle_start<<<1, 32, 0, s>>>(st.cycle, st.givens, m, st.scalars + 5, restart, ptol, st.scalars + 6);
+    k_scale_dev<<<grid(N), kBlock, 0, s>>>(N, st.scalars + 6, st.basis);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return GMRES_CUDA;
+    // ---- the inner loop: graph replay, or one step at a time from the host
+    if (graph) {
+      e = cudaGraphLaunch(st.inner_exec, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(st.cycle_host, st.cycle, sizeof(GmresCycle), cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) return GMRES_CUDA;
-      const double h0 = std::sqrt(hh[m + 1]), h1 = std::sqrt(hh[m + 2]);
-      for (int k = 0; k <= col; ++k) h[col][k] = hh[k];
-      h[col][col + 1] = h1;
-      cudaMemcpyAsync(st.krylov[col + 1], w, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
-      if (h1 <= eps * h0) {
-        h[col][col + 1] = 0.0;
-        breakdown = true;
-      } else {
-        count_launch();
-        k_scale<<<grid(N), kBlock, 0, s>>>(N, 1.0 / h1, st.krylov[col + 1]);
-      }
-      for (int k = 0; k < col; ++k) {
-        const double c = gc[k], sn = gs[k];
-        const double n0 = h[col][k], n1 = h[col][k + 1];
-        h[col][k] = c * n0 + sn * n1;
-        h[col][k + 1] = -sn * n0 + c * n1;
-      }
-      double c, sn, mag;
-      lartg(h[col][col], h[col][col + 1], &c, &sn, &mag);
-      gc[col] = c;
-      gs[col] = sn;
-      h[col][col] = mag;
-      h[col][col + 1] = 0.0;
-      const double t = -sn * S[col];
-      S[col] = c * S[col];
-      S[col + 1] = t;
-      presid = std::fabs(t);
-      ++inner;
-      if (presid <= ptol || breakdown) break;
+      count_launch(cyc.inner * st.inner_nodes);
+    } else {
+      do {
+        if (arnoldi_step(st, matvec, m, cudaGraphConditionalHandle{}, 0, s) != cudaSuccess) return GMRES_CUDA;
+        e = cudaMemcpyAsync(st.cycle_host, st.cycle, sizeof(GmresCycle), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return GMRES_CUDA;
+      } while (!cyc.done);
     }
-    if (col == restart) col = restart - 1;
-    // back substitution (upper triangular in h[k][k])
-    if (h[col][col] == 0.0) S[col] = 0.0;
-    std::vector<double> y(S.begin(), S.begin() + col + 1);
+    const int col = cyc.last;
+    const int inner = cyc.inner;
+    // back substitution (upper triangular in h[k][k]) on the host
+    H.resize((size_t)(col + 1) * (m + 1));
+    S.resize(3 * (size_t)m + 2);
+    e = cudaMemcpy(H.data(), st.hess, H.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(S.data(), st.givens, S.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return GMRES_CUDA;
+    auto h = [&](int c, int k) { return H[(size_t)c * (m + 1) + k]; };
+    std::vector<double> y(S.begin() + 2 * m, S.begin() + 2 * m + col + 1);
+    if (h(col, col) == 0.0) y[col] = 0.0;
     for (int k = col; k > 0; --k) {
       if (y[k] != 0.0) {
-        y[k] /= h[k][k];
+        y[k] /= h(k, k);
         const double tk = y[k];
-        for (int j = 0; j < k; ++j) y[j] -= tk * h[k][j];
+        for (int j = 0; j < k; ++j) y[j] -= tk * h(k, j);
       }
     }
-    if (y[0] != 0.0) y[0] /= h[0][0];
+    if (y[0] != 0.0) y[0] /= h(0, 0);
     for (int k = 0; k <= col; ++k) {
       count_launch();
-      k_axpy<<<grid(N), kBlock, 0, s>>>(N, y[k], st.krylov[k], x);
+      k_axpy<<<grid(N), kBlock, 0, s>>>(N, y[k], st.basis + (size_t)k * N, x);
     }
     x_nonzero = true;
     if (matvec(x, av, s) != cudaSuccess) return GMRES_CUDA;
     count_launch();
     k_sub<<<grid(N), kBlock, 0, s>>>(N, b, av, st.tmp);
-    e = implicit_dot(st, N, st.tmp, st.tmp, st.scalars + 6, s);
-    const double rnorm = std::sqrt(host_scalar(st.scalars + 6, s, &e));
+    e = implicit_dot(st, N, st.tmp, st.tmp, st.scalars + 7, s);
+    const double rnorm = std::sqrt(host_scalar(st.scalars + 7, s, &e));
     if (e != cudaSuccess) return GMRES_CUDA;
     used += inner;
     *iterations = used;

@@ -31,31 +31,94 @@ struct ImplicitTopology {
   std::vector<double> boundary_len;
 };
 
+// One triangular sweep of LU-SGS, laid out in sweep order: rows sorted by
+// their level in the dependency graph of the reference's natural cell order
+// (positions), each row's off-diagonal entries in ascending column order.
+// The schedule is a list of launches over consecutive levels: runs of narrow
+// levels in one single-block wavefront launch, each wide level in a grid
+// launch of its own.
+constexpr int kSweepPack = 4;
+
+struct SweepPlan {
+  int n_levels = 0;
+  int* level_ptr = nullptr;  // [n_levels + 1] positions
+  int* pos_cell = nullptr;   // [C] cell at each position
+  int* ent_ptr = nullptr;    // [C + 1] entries per position
+  int* ent_cell = nullptr;   // column cell of the entry
+  int* ent_pos = nullptr;    // column position of the entry (sweep order)
+  int* ent_val = nullptr;    // index into the row values
+  // rows packed in sweep order with a fixed stride of kSweepPack entries
+  // (longer rows continue in the CSR above): column position and cell
+  // (topology, built once) and the matrix values, diagonal and clamped
+  // diagonal (refreshed by every assembly)
+  int* pk_cnt = nullptr;     // [C] entries of the row
+  int* pk_pos = nullptr;     // [C][kSweepPack]
+  int* pk_cell = nullptr;    // [C][kSweepPack]
+  double* pk_val = nullptr;  // [C][kSweepPack]
+  double* pk_diag = nullptr; // [C]
+  double* pk_dc = nullptr;   // [C]
+  std::vector<int> host_level_ptr;
+  struct Launch {
+    int wavefront;  // 1: single-block run of levels [l0, l1); 0: grid launch of level l0
+    int l0, l1;
+  };
+  std::vector<Launch> schedule;
+};
+
+// Device-resident state of one GMRES restart cycle (SciPy's inner loop):
+// the Hessenberg columns, Givens rotations and the residual estimate, so
+// that an Arnoldi step needs no host round trip.
+struct GmresCycle {
+  int col;        // column of the next Arnoldi step
+  int last;       // last column processed
+  int restart;    // inner iterations allowed in this cycle
+  int inner;      // inner iterations done
+  int breakdown;
+  int done;       // presid <= ptol, breakdown, or restart reached
+  double ptol;
+  double presid;
+  double inv_h1;  // scale of the next basis vector (1 / h1, or 1 at breakdown)
+};
+
 struct ImplicitState {
   int n_cells = 0, n_coupling = 0, n_boundary = 0;
-  int n_levels_fwd = 0, n_levels_bwd = 0, sweep_blocks = 1;
+  int n_levels_fwd = 0, n_levels_bwd = 0;
   // topology (device)
   int *ca = nullptr, *cb = nullptr, *bowner = nullptr;
   double2 *na = nullptr, *nb = nullptr, *bnormal = nullptr;
   double *clen = nullptr, *blen = nullptr;
   int *dptr = nullptr, *dref = nullptr, *rptr = nullptr, *rref = nullptr, *rcol = nullptr;
-  int *fwd_level_ptr = nullptr, *fwd_level_cells = nullptr, *bwd_level_ptr = nullptr, *bwd_level_cells = nullptr;
-  int *lower_ptr = nullptr, *lower_col = nullptr, *lower_val = nullptr;
-  int *upper_ptr = nullptr, *upper_col = nullptr, *upper_val = nullptr;
+  SweepPlan fwd, bwd;
+  int wide_level = 0;  // levels wider than this get a grid launch each
   // values and vectors (device)
   double *coef = nullptr, *bterm = nullptr, *diag = nullptr, *dclamp = nullptr, *rval = nullptr;
   double *tmp = nullptr, *state = nullptr, *rate = nullptr, *up = nullptr, *rp = nullptr;
-  double *w = nullptr, *av = nullptr, *partials = nullptr, *scalars = nullptr;
-  // prepared operator
+  double *w = nullptr, *av = nullptr, *vcur = nullptr, *partials = nullptr, *scalars = nullptr;
+  // prepared operator: scales, |state / scale|^2 and the time steps live on
+  // the device, so a captured GMRES step reads the current values
   ScaleVec scale{{1.0, 1.0, 1.0, 1.0}};
-  double state_norm = 0.0;
-  const double* dt = nullptr;
+  double* scale_dev = nullptr;  // [4]
+  double* dt_buf = nullptr;     // [C] copy of the prepared time steps
+  const double* dt = nullptr;   // = dt_buf
   int dt_per_cell = 0;
   bool prepared = false;
-  // Krylov basis and Hessenberg column scratch, grown on demand
-  std::vector<double*> krylov;
-  double* hcol = nullptr;
-  int hcol_size = 0;
+  // Krylov basis ((m + 1) x 4C, one allocation) and the cycle state
+  double* basis = nullptr;
+  int basis_m = 0;
+  GmresCycle* cycle = nullptr;      // device
+  GmresCycle* cycle_host = nullptr;  // pinned mirror
+  double* hess = nullptr;            // device [m][m + 1] Hessenberg columns
+  double* givens = nullptr;          // device [3 m + 2]: c, s, S
+  double* hcol = nullptr;            // device [m + 3]: dots, |w|^2 before / after
+  double* mgs_partials = nullptr;    // device [2][mgs_blocks]
+  int mgs_blocks = 0;
+  cudaStream_t cap_stream = nullptr;  // stream the inner loop is captured on
+  int inner_nodes = 0;                // nodes of one captured Arnoldi step
+  // the inner loop as a graph with a device-evaluated while condition
+  cudaGraphExec_t inner_exec = nullptr;
+  cudaGraph_t inner_graph = nullptr;
+  int inner_key = -1;  // (m, operator) the graph was built for
+  bool graph_failed = false;
   std::vector<void*> owned;
 };
 
@@ -68,10 +131,17 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t);
 void implicit_free(ImplicitState& st);
 cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* area, const double* dt,
                               int dt_per_cell, double gamma, cudaStream_t s);
+// operator set-up of mcfd_implicit_prepare: scales, |state / scale|^2 and a
+// copy of the time steps into the state's device buffers
+cudaError_t implicit_set_operator(ImplicitState& st, ScaleVec scale, const double* dt, int dt_per_cell,
+                                  cudaStream_t s);
 cudaError_t lusgs_apply(ImplicitState& st, const double* v, double* x, cudaStream_t s);
+void implicit_set_wide_level(ImplicitState& st, int wide);
 cudaError_t fd_operator(ImplicitState& st, const ResidualFn& residual1, const double* v, double* out,
                         cudaStream_t s);
-int gmres_solve(ImplicitState& st, const MatvecFn& matvec, const double* b, double* x, double tol,
+// matvec_key: distinguishes operators for the captured inner loop (a graph is
+// rebuilt when it changes); count: kernels launched per captured step
+int gmres_solve(ImplicitState& st, const MatvecFn& matvec, int matvec_key, const double* b, double* x, double tol,
                 int max_iter, int m, int* iterations, cudaStream_t s);
 // scaled norms and reductions of the Newton iteration
 cudaError_t implicit_dot(ImplicitState& st, long long n, const double* x, const double* y, double* out,

@@ -120,6 +120,7 @@ struct DevGeom {
   const double* visc_diff;    // [C] diffusion sum of the last viscous time step (workspace)
   // launch shapes chosen by mcfd_autotune (0: the defaults)
   int tune_recon_threads, tune_flux_threads, tune_flux_faces, tune_gather_threads;
+  int tune_recon_split;  // fast variant: one thread per (cell, variable) for cells with 3 / 4 entries
 };
 
 // One term of an explicit stage combination, evaluated left to right.

@@ -63,7 +63,7 @@ __device__ __forceinline__ double limiter_slope(double r) {
 template <int LIMITER>
 __global__ void __launch_bounds__(kBlock) k_reconstruct_tangent(DevGeom g, const double* __restrict__ P,
                                                                 const double* __restrict__ dP,
-                                                                double* __restrict__ dQ) {
+                                                                double* __restrict__ dQ, double venkat_k) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.n_cells) return;
   const St4 p = ld4(P + 4 * (size_t)c), tp = ld4(dP + 4 * (size_t)c);
@@ -92,6 +92,26 @@ __global__ void __launch_bounds__(kBlock) k_reconstruct_tangent(DevGeom g, const
   }
   double phi[4] = {1.0, 1.0, 1.0, 1.0}, dphi[4] = {0.0, 0.0, 0.0, 0.0};
   const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
+  if constexpr (LIMITER == MCFD_LIMITER_VENKATAKRISHNAN_K) {
+    // the smooth form: the minimising face's factor and its total derivative
+    // through d1 (the extreme neighbour or the cell) and d2 (the gradient)
+    const double e2 = venkat_k_e2(venkat_k, g.area[c]);
+    for (int s = s0; s < s1; ++s) {
+      const double2 dd = g.lim_d[s];
+      for (int v = 0; v < 4; ++v) {
+        const double inc = gx[v] * dd.x + gy[v] * dd.y;
+        const double dinc = dgx[v] * dd.x + dgy[v] * dd.y;
+        const VenkatK f = venkat_k_face(pv[v], inc, lo[v], hi[v], e2);
+        if (s == s0 || icmp::lt(f.f, phi[v])) {
+          phi[v] = f.f;
+          double a, b;
+          venkat_k_slopes(f, inc, &a, &b);
+          const double dd1 = (icmp::gt0(inc) ? dhi[v] : dlo[v]) - dpv[v];
+          dphi[v] = a * dd1 + b * dinc;
+        }
+      }
+    }
+  } else
   for (int s = s0; s < s1; ++s) {
     const double2 dd = g.lim_d[s];
     for (int v = 0; v < 4; ++v) {
@@ -220,10 +240,14 @@ cudaError_t launch_jvp(const DevGeom& g, const mcfd_config& cfg, const double* U
     if (e != cudaSuccess) return e;
     count_launch();
     switch (cfg.limiter) {
-      case 0: k_reconstruct_tangent<0><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon); break;
-      case 1: k_reconstruct_tangent<1><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon); break;
-      case 2: k_reconstruct_tangent<2><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon); break;
-      default: k_reconstruct_tangent<3><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon); break;
+      case 0: k_reconstruct_tangent<0><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon, 0.0); break;
+      case 1: k_reconstruct_tangent<1><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon, 0.0); break;
+      case 2: k_reconstruct_tangent<2><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon, 0.0); break;
+      case 3: k_reconstruct_tangent<3><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon, 0.0); break;
+      default:
+        k_reconstruct_tangent<MCFD_LIMITER_VENKATAKRISHNAN_K><<<blocks_for(C), kBlock, 0, s>>>(g, w.P, w.dP, w.drecon,
+                                                                                              cfg.venkat_k);
+        break;
     }
   }
   const bool kh = cfg.reconstruction != MCFD_RECON_MUSCL_PARABOLIC;
@@ -252,17 +276,21 @@ cudaError_t launch_jvp(const DevGeom& g, const mcfd_config& cfg, const double* U
 namespace mcfd {
 namespace {
 
-__global__ void k_scale_dir(int n4, const double* __restrict__ v, ScaleVec s, double* __restrict__ out) {
+// the scales are read from the prepared operator's device copy, so a
+// captured GMRES step uses the current ones
+__global__ void k_scale_dir(int n4, const double* __restrict__ v, const double* __restrict__ scale,
+                            double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n4) out[i] = s.v[i & 3] * v[i];
+  if (i < n4) out[i] = scale[i & 3] * v[i];
 }
 
-__global__ void k_exact_combine(int n4, const double* __restrict__ v, const double* __restrict__ dR, ScaleVec s,
-                                const double* __restrict__ dt, int dt_per_cell, double* __restrict__ out) {
+__global__ void k_exact_combine(int n4, const double* __restrict__ v, const double* __restrict__ dR,
+                                const double* __restrict__ scale, const double* __restrict__ dt, int dt_per_cell,
+                                double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n4) return;
   const double d = dt_per_cell ? dt[i >> 2] : dt[0];
-  out[i] = v[i] - div_rn(d * dR[i], s.v[i & 3]);
+  out[i] = v[i] - div_rn(d * dR[i], scale[i & 3]);
 }
 
 }  // namespace
@@ -271,11 +299,11 @@ cudaError_t exact_operator(const DevGeom& g, const mcfd_config& cfg1, const Impl
                            const double* v, double* out, cudaStream_t s) {
   const int n4 = 4 * g.n_cells;
   count_launch();
-  k_scale_dir<<<blocks_for(n4), kBlock, 0, s>>>(n4, v, st.scale, w.sv);
+  k_scale_dir<<<blocks_for(n4), kBlock, 0, s>>>(n4, v, st.scale_dev, w.sv);
   cudaError_t e = launch_jvp(g, cfg1, st.state, w.sv, w, w.dR, s);
   if (e != cudaSuccess) return e;
   count_launch();
-  k_exact_combine<<<blocks_for(n4), kBlock, 0, s>>>(n4, v, w.dR, st.scale, st.dt, st.dt_per_cell, out);
+  k_exact_combine<<<blocks_for(n4), kBlock, 0, s>>>(n4, v, w.dR, st.scale_dev, st.dt, st.dt_per_cell, out);
   return cudaGetLastError();
 }
 

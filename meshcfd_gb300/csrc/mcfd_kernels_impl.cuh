@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(kBlock) k_primitive(int n, const double* __res
 
 template <int LIMITER>
 __global__ void __launch_bounds__(kBlock, MCFD_RECON_GENERIC_MIN_BLOCKS) k_reconstruct(DevGeom g, const double* __restrict__ P,
-                                                                                       double* __restrict__ recon) {
+                                                                                       double* __restrict__ recon,
+                                                                                       double venkat_k) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n_cells) return;
   const int c = g.cell_order[i];
@@ -153,18 +154,32 @@ __global__ void __launch_bounds__(kBlock, MCFD_RECON_GENERIC_MIN_BLOCKS) k_recon
       if (above) hi[v] = qv[v];
     }
   }
-  double tol[4];
-#pragma unroll
-  for (int v = 0; v < 4; ++v) tol[v] = limiter_tolerance(pv[v]);
   double phi[4] = {1.0, 1.0, 1.0, 1.0};
   const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
-  for (int s = s0; s < s1; ++s) {
-    const double2 d = g.lim_d[s];
+  if constexpr (LIMITER == MCFD_LIMITER_VENKATAKRISHNAN_K) {
+    // minimum over the faces of the smooth face function (no cap at 1)
+    const double e2 = venkat_k_e2(venkat_k, g.area[c]);
+    for (int s = s0; s < s1; ++s) {
+      const double2 d = g.lim_d[s];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      double inc = kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y);
-      double f = limiter_face_factor<LIMITER>(pv[v], inc, lo[v], hi[v], tol[v]);
-      if (icmp::lt_nonneg(f, phi[v])) phi[v] = f;
+      for (int v = 0; v < 4; ++v) {
+        const double inc = kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y);
+        const double f = venkat_k_face(pv[v], inc, lo[v], hi[v], e2).f;
+        if (s == s0 || icmp::lt(f, phi[v])) phi[v] = f;
+      }
+    }
+  } else {
+    double tol[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) tol[v] = limiter_tolerance(pv[v]);
+    for (int s = s0; s < s1; ++s) {
+      const double2 d = g.lim_d[s];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        double inc = kmul<MUL_INCREMENT>(gx[v], d.x) + kmul<MUL_INCREMENT>(gy[v], d.y);
+        double f = limiter_face_factor<LIMITER>(pv[v], inc, lo[v], hi[v], tol[v]);
+        if (icmp::lt_nonneg(f, phi[v])) phi[v] = f;
+      }
     }
   }
   for (int s = s0; s < s1; ++s) {
@@ -367,6 +382,73 @@ __global__ void MCFD_RECON_BOUND k_reconstruct_fast(DevGeom g, const double* __r
   const int s0 = g.lim_ptr[c];
   if (g.lim_ptr[c + 1] - s0 == 3) reconstruct_cell_fast_by_variable<LIMITER, 3>(g, P, recon, c, p, s0);
   else reconstruct_cell_fast_by_variable<LIMITER, 4>(g, P, recon, c, p, s0);
+}
+
+// The same reconstruction with one thread per (cell, variable): the four
+// variables of a cell are independent (gradient, extremes, limiter and face
+// values of variable v read only variable v), so four adjacent threads take
+// one cell's variables and run exactly the per-variable code above, with a
+// quarter of its registers: more warps per SM to hide the latency of the
+// integer-pipe divisions.  Cells with 3 or 4 limiter entries; results are
+// those of k_reconstruct_fast.
+template <int LIMITER, int NS>
+__device__ __forceinline__ void reconstruct_variable_fast(const DevGeom& g, const double* __restrict__ P,
+                                                          double* __restrict__ recon, int c, int v, double pv,
+                                                          int s0) {
+  double gx = 0.0, gy = 0.0, lo = pv, hi = pv;
+  const bool positive = (v == 0 || v == 3);  // density and pressure: the raw bits order them
+  for (int e = g.grad_ptr[c], e1 = g.grad_ptr[c + 1]; e < e1; ++e) {
+    const double q = P[4 * (size_t)g.grad_nb[e] + v];
+    const double d = q - pv;
+    gx += kmul<MUL_GRADIENT>(g.grad_cx[e], d);
+    gy += kmul<MUL_GRADIENT>(g.grad_cy[e], d);
+    const bool below = positive ? icmp::lt_pos(q, lo) : icmp::lt(q, lo);
+    const bool above = positive ? icmp::gt_pos(q, hi) : icmp::lt(hi, q);
+    if (below) lo = q;
+    if (above) hi = q;
+  }
+  const double tol = limiter_tolerance(pv);
+  double pos = 0.0, neg = 0.0, inc[NS];
+  bool has_pos = false, has_neg = false, flat = false;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    const double2 dk = g.lim_d[s0 + k];
+    inc[k] = kmul<MUL_INCREMENT>(gx, dk.x) + kmul<MUL_INCREMENT>(gy, dk.y);
+    if (icmp::gt_pos(inc[k], tol)) {
+      has_pos = true;
+      if (icmp::lt_nonneg(pos, inc[k])) pos = inc[k];
+    } else if (icmp::neg_gt_pos(inc[k], tol)) {
+      has_neg = true;
+      const double m = negate(inc[k]);
+      if (icmp::lt_nonneg(neg, m)) neg = m;
+    } else {
+      flat = true;
+    }
+  }
+  double phi;
+  if constexpr (kMinRatio)
+    phi = limiter_factor_min_ratio<LIMITER>(pv, lo, hi, pos, negate(neg), has_pos, has_neg, flat);
+  else
+    phi = limiter_factor_fast<LIMITER>(hi - pv, pos, pv - lo, neg, has_pos, has_neg, flat);
+#pragma unroll
+  for (int k = 0; k < NS; ++k) recon[4 * (size_t)g.lim_slot[s0 + k] + v] = pv + kmul<MUL_OUTPUT>(phi, inc[k]);
+}
+
+#ifndef MCFD_RECON_SPLIT_MIN_BLOCKS
+#define MCFD_RECON_SPLIT_MIN_BLOCKS 4
+#endif
+
+template <int LIMITER>
+__global__ void __launch_bounds__(kBlock, MCFD_RECON_SPLIT_MIN_BLOCKS) k_reconstruct_fast_split(
+    DevGeom g, const double* __restrict__ P, double* __restrict__ recon) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t >> 2, v = t & 3;
+  if (i >= g.n_lim34) return;
+  const int c = g.cell_order[i];
+  const double pv = P[4 * (size_t)c + v];
+  const int s0 = g.lim_ptr[c];
+  if (g.lim_ptr[c + 1] - s0 == 3) reconstruct_variable_fast<LIMITER, 3>(g, P, recon, c, v, pv, s0);
+  else reconstruct_variable_fast<LIMITER, 4>(g, P, recon, c, v, pv, s0);
 }
 
 template <int LIMITER>
@@ -642,8 +724,24 @@ cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const d
   if (g.n_cells == 0) return cudaSuccess;
   const int t = g.tune_recon_threads ? g.tune_recon_threads : kBlock;
   const int b = (g.n_cells + t - 1) / t;
+  if (cfg.limiter == MCFD_LIMITER_VENKATAKRISHNAN_K) {
+    // the smooth form has no smallest-ratio shortcut: per-face evaluation in
+    // every variant
+    count_launch();
+    k_reconstruct<MCFD_LIMITER_VENKATAKRISHNAN_K><<<b, t, 0, s>>>(g, P, recon, cfg.venkat_k);
+    return cudaGetLastError();
+  }
   if constexpr (kFast || kMinRatio) {
-    if (g.n_lim34 > 0) {
+    if (g.n_lim34 > 0 && g.tune_recon_split) {
+      const int bs = (int)((4LL * g.n_lim34 + t - 1) / t);
+      count_launch();
+      switch (cfg.limiter) {
+        case 0: k_reconstruct_fast_split<0><<<bs, t, 0, s>>>(g, P, recon); break;
+        case 1: k_reconstruct_fast_split<1><<<bs, t, 0, s>>>(g, P, recon); break;
+        case 2: k_reconstruct_fast_split<2><<<bs, t, 0, s>>>(g, P, recon); break;
+        default: k_reconstruct_fast_split<3><<<bs, t, 0, s>>>(g, P, recon); break;
+      }
+    } else if (g.n_lim34 > 0) {
       const int b34 = (g.n_lim34 + t - 1) / t;
       count_launch();
       switch (cfg.limiter) {
@@ -666,10 +764,10 @@ cudaError_t launch_reconstruct(const DevGeom& g, const mcfd_config& cfg, const d
   } else {
     count_launch();
     switch (cfg.limiter) {
-      case 0: k_reconstruct<0><<<b, t, 0, s>>>(g, P, recon); break;
-      case 1: k_reconstruct<1><<<b, t, 0, s>>>(g, P, recon); break;
-      case 2: k_reconstruct<2><<<b, t, 0, s>>>(g, P, recon); break;
-      default: k_reconstruct<3><<<b, t, 0, s>>>(g, P, recon); break;
+      case 0: k_reconstruct<0><<<b, t, 0, s>>>(g, P, recon, 0.0); break;
+      case 1: k_reconstruct<1><<<b, t, 0, s>>>(g, P, recon, 0.0); break;
+      case 2: k_reconstruct<2><<<b, t, 0, s>>>(g, P, recon, 0.0); break;
+      default: k_reconstruct<3><<<b, t, 0, s>>>(g, P, recon, 0.0); break;
     }
   }
   return cudaGetLastError();

@@ -353,6 +353,95 @@ __device__ __forceinline__ double limiter_slope(double r) {
 // limiter entries (the cell order makes the count warp-uniform, so a warp of
 // triangles issues no FP64 work for a fourth entry); NS = 0 handles any
 // count, keeping the first four increments.
+// The cell reverse of one variable for the smooth Venkatakrishnan form: the
+// forward's gradient, increments and face factors in the forward kernels'
+// rounding (separately rounded products), the first face of least factor,
+// then the reverse of the face states and of that face's factor through d1
+// (the extreme neighbour, or the cell) and d2 (the gradient).
+template <int NS>
+__device__ __forceinline__ void vjp_cell_variable_vk(const DevGeom& g, const double* __restrict__ P,
+                                                     const double* __restrict__ slot_bar, int v, double pv,
+                                                     int e0, int e1, int s0, int s1, double& pb,
+                                                     double* __restrict__ ent_bar, double e2) {
+  double gx = 0.0, gy = 0.0, lo = pv, hi = pv;
+  int lo_e = -1, hi_e = -1;
+  for (int e = e0; e < e1; ++e) {
+    const double q = P[4 * (size_t)g.grad_nb[e] + v];
+    const double d = q - pv;
+    gx = gx + mul_rn(g.grad_cx[e], d);
+    gy = gy + mul_rn(g.grad_cy[e], d);
+    if (icmp::lt(q, lo)) { lo = q; lo_e = e; }
+    if (icmp::lt(hi, q)) { hi = q; hi_e = e; }
+  }
+  constexpr int kCache = NS > 0 ? NS : 4;
+  double incs[kCache];
+  double phi = 1.0, arg_inc = 0.0;
+  int arg = -1;
+  auto consider = [&](int s, double inc) {
+    const double f = venkat_k_face(pv, inc, lo, hi, e2).f;
+    if (arg < 0 || icmp::lt(f, phi)) {
+      phi = f;
+      arg = s;
+      arg_inc = inc;
+    }
+  };
+#pragma unroll
+  for (int k = 0; k < kCache; ++k) {
+    incs[k] = 0.0;
+    if (NS > 0 || s0 + k < s1) {
+      const double2 dd = g.lim_d[s0 + k];
+      incs[k] = __dadd_rn(mul_rn(gx, dd.x), mul_rn(gy, dd.y));
+      consider(s0 + k, incs[k]);
+    }
+  }
+  if (NS == 0) {
+    for (int s = s0 + kCache; s < s1; ++s) {
+      const double2 dd = g.lim_d[s];
+      consider(s, __dadd_rn(mul_rn(gx, dd.x), mul_rn(gy, dd.y)));
+    }
+  }
+  // reverse of Q_s = P + phi (G . r_s)
+  double phib = 0.0, gxb = 0.0, gyb = 0.0;
+  auto face_reverse = [&](int s, double inc, const double2& dd) {
+    const double qb = slot_bar[4 * (size_t)g.lim_slot[s] + v];
+    phib += qb * inc;
+    const double qphi = qb * phi;
+    gxb += qphi * dd.x;
+    gyb += qphi * dd.y;
+  };
+#pragma unroll
+  for (int k = 0; k < kCache; ++k)
+    if (NS > 0 || s0 + k < s1) face_reverse(s0 + k, incs[k], g.lim_d[s0 + k]);
+  if (NS == 0) {
+    for (int s = s0 + kCache; s < s1; ++s) {
+      const double2 dd = g.lim_d[s];
+      face_reverse(s, __dadd_rn(mul_rn(gx, dd.x), mul_rn(gy, dd.y)), dd);
+    }
+  }
+  // reverse of phi = f(d1, d2) at the minimising face
+  double extb = 0.0;
+  int ext_e = -1;
+  if (arg >= 0) {
+    const VenkatK f = venkat_k_face(pv, arg_inc, lo, hi, e2);
+    double a, b;
+    venkat_k_slopes(f, arg_inc, &a, &b);
+    const double d1b = a * phib, incb = b * phib;
+    pb -= d1b;
+    const int ee = icmp::gt0(arg_inc) ? hi_e : lo_e;
+    if (ee < 0) pb += d1b;  // the extreme is the cell itself
+    else { extb = d1b; ext_e = ee; }
+    const double2 dd = g.lim_d[arg];
+    gxb += incb * dd.x;
+    gyb += incb * dd.y;
+  }
+  // reverse of G = sum_e coef_e (P_nb - P_c): neighbour share per entry
+  for (int e = e0; e < e1; ++e) {
+    const double w = g.grad_cx[e] * gxb + g.grad_cy[e] * gyb;
+    pb -= w;
+    ent_bar[4 * (size_t)e + v] = w + (ext_e == e ? extb : 0.0);
+  }
+}
+
 template <int LIMITER, int NS>
 __device__ __forceinline__ void vjp_cell_variable(const DevGeom& g, const double* __restrict__ P,
                                                   const double* __restrict__ slot_bar, int v, double pv,
@@ -479,7 +568,8 @@ template <int LIMITER, bool FO>
 __global__ void __launch_bounds__(kBlock, MCFD_VJP_CELL_MIN_BLOCKS) k_vjp_cell(DevGeom g, const double* __restrict__ P,
                                                      const double* __restrict__ lambda,
                                                      const double* __restrict__ slot_bar, double ax, double ay,
-                                                     double* __restrict__ pbar, double* __restrict__ ent_bar) {
+                                                     double* __restrict__ pbar, double* __restrict__ ent_bar,
+                                                     double venkat_k) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n_cells) return;
   const int c = g.cell_order[i];  // groups equal stencil sizes; outputs do not depend on the order
@@ -492,7 +582,19 @@ __global__ void __launch_bounds__(kBlock, MCFD_VJP_CELL_MIN_BLOCKS) k_vjp_cell(D
     const St4 q = ld4(slot_bar + 4 * (size_t)g.lim_slot[s]);
     pb[0] += q.a; pb[1] += q.b; pb[2] += q.c; pb[3] += q.d;
   }
-  if (!FO) {
+  if constexpr (!FO && LIMITER == MCFD_LIMITER_VENKATAKRISHNAN_K) {
+    const double e2 = venkat_k_e2(venkat_k, g.area[c]);
+    if (s1 - s0 == 3) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) vjp_cell_variable_vk<3>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar, e2);
+    } else if (s1 - s0 == 4) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) vjp_cell_variable_vk<4>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar, e2);
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) vjp_cell_variable_vk<0>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar, e2);
+    }
+  } else if (!FO) {
     if (s1 - s0 == 3) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) vjp_cell_variable<LIMITER, 3>(g, P, slot_bar, v, pv[v], e0, e1, s0, s1, pb[v], ent_bar);
@@ -664,14 +766,18 @@ cudaError_t launch_vjp(const DevGeom& g, const mcfd_config& cfg, const double* U
   count_launch(2);
   const double ax = cfg.acceleration_x, ay = cfg.acceleration_y;
   if (fo) {
-    k_vjp_cell<0, true><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar);
+    k_vjp_cell<0, true><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar, 0.0);
     k_vjp_collect<true><<<blocks_for(C), kBlock, 0, s>>>(g, P, w.pbar, w.ent_bar, cfg.gamma, ubar);
   } else {
     switch (cfg.limiter) {
-      case 0: k_vjp_cell<0, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
-      case 1: k_vjp_cell<1, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
-      case 2: k_vjp_cell<2, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
-      default: k_vjp_cell<3, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar); break;
+      case 0: k_vjp_cell<0, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar, 0.0); break;
+      case 1: k_vjp_cell<1, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar, 0.0); break;
+      case 2: k_vjp_cell<2, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar, 0.0); break;
+      case 3: k_vjp_cell<3, false><<<blocks_for(C), kBlock, 0, s>>>(g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar, 0.0); break;
+      default:
+        k_vjp_cell<MCFD_LIMITER_VENKATAKRISHNAN_K, false><<<blocks_for(C), kBlock, 0, s>>>(
+            g, P, lambda, w.slot_bar, ax, ay, w.pbar, w.ent_bar, cfg.venkat_k);
+        break;
     }
     k_vjp_collect<false><<<blocks_for(C), kBlock, 0, s>>>(g, P, w.pbar, w.ent_bar, cfg.gamma, ubar);
   }

@@ -16,7 +16,8 @@ import torch
 
 from . import _lib
 from .errors import SolverError, StatusCode, raise_for_status
-from .model import FLUX_CODES, LIMITER_CODES, RECONSTRUCTION_CODES
+from .model import (EXTENSION_LIMITER_CODES, FLUX_CODES, LIMITER_CODES, RECONSTRUCTION_CODES,
+                    VENKATAKRISHNAN_K_DEFAULT)
 
 TIME_SCHEME_CODES = {"Explicit Euler": 0, "Explicit RK2": 1, "Explicit RK3": 2, "Explicit RK4": 3}
 
@@ -30,7 +31,9 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
     ``mode``: "exact" (reference operation order, bit-exact), "fast" (exact
     arithmetic, limiter minimum through the smallest ratio) or "fma" (shared
     reciprocals and FMA; outside the 1e-12 bar on fine meshes).  MUSCL
-    parabolic reconstructs with exact arithmetic in every mode."""
+    parabolic reconstructs with exact arithmetic in every mode.  The limiter
+    "Venkatakrishnan K" (an extension, code 4) reads K from the settings
+    attribute ``venkatakrishnan_k``."""
     viscous = {"Inviscid": 0, "Constant": 1, "Sutherland": 2}
     if settings.viscosity_model not in viscous:
         raise SolverError(f"Unsupported viscosity model '{settings.viscosity_model}'.")
@@ -39,7 +42,7 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
     try:
         flux = FLUX_CODES[settings.flux]
         recon = RECONSTRUCTION_CODES[settings.reconstruction]
-        limiter = LIMITER_CODES[settings.limiter]
+        limiter = {**LIMITER_CODES, **EXTENSION_LIMITER_CODES}[settings.limiter]
     except KeyError as error:
         raise SolverError(f"Unsupported scheme {error}") from error
     cfg = _lib.Config()
@@ -55,6 +58,7 @@ def make_config(settings, mode: str = "exact") -> _lib.Config:
     cfg.sutherland_reference_temperature = float(settings.sutherland_reference_temperature)
     cfg.sutherland_temperature = float(settings.sutherland_temperature)
     cfg.prandtl_number = float(settings.prandtl_number)
+    cfg.venkat_k = float(getattr(settings, "venkatakrishnan_k", VENKATAKRISHNAN_K_DEFAULT))
     return cfg
 
 
@@ -245,11 +249,11 @@ class DeviceGeometry:
         """Time the stage kernels' launch shapes on state U and keep the
         fastest for this handle (mcfd_autotune)."""
         _check_state(U, self.n_cells, "U")
-        chosen = (C.c_int32 * 4)()
+        chosen = (C.c_int32 * 5)()
         self.lib.check(self.lib.mcfd_autotune(self.handle, C.byref(cfg), U.data_ptr(), chosen, _stream_ptr()),
                        "mcfd_autotune")
         return {"reconstruct_threads": chosen[0], "flux_threads": chosen[1], "flux_faces_per_thread": chosen[2],
-                "gather_threads": chosen[3]}
+                "gather_threads": chosen[3], "reconstruct_per_variable": chosen[4]}
 
     def primitive_buffer(self) -> torch.Tensor:
         """The handle's primitive buffer as a tensor view (valid after a

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import time
 
 import numpy as np
 import torch
@@ -24,10 +25,28 @@ def _host(values) -> C.Array:
     return (C.c_double * len(values))(*[float(v) for v in values])
 
 
+class BudgetExceeded(RuntimeError):
+    """The caller's wall-clock deadline passed (checked before each GMRES
+    solve); the state is left as it was at the start of the step."""
+
+
 class ImplicitEuler:
     """Device implicit-Euler stepper for one geometry and settings."""
 
-    def __init__(self, geom: DeviceGeometry, settings, mode: str = "exact", solver_error=SolverError):
+    # work counters (instance values once counting starts)
+    attempts = 0
+    newton_iterations = 0
+    gmres_iterations = 0
+    gmres_calls = 0
+    gmres_seconds = 0.0
+    deadline = None
+
+    def __init__(self, geom: DeviceGeometry, settings, mode: str = "exact", solver_error=SolverError,
+                 deadline: float | None = None):
+        """``deadline``: optional ``time.perf_counter()`` value after which the
+        next GMRES solve raises :class:`BudgetExceeded` instead of starting.
+        ``newton_iterations``, ``gmres_iterations``, ``gmres_calls``,
+        ``gmres_seconds`` and ``attempts`` count the work done so far."""
         if settings.implicit_preconditioner != "LU-SGS":
             raise NotImplementedError("the GPU implicit path implements the LU-SGS preconditioner")
         self.geom = geom
@@ -44,6 +63,10 @@ class ImplicitEuler:
         self.correction = torch.empty_like(self.rate)
         self.gmres_iterations = 0
         self.newton_iterations = 0
+        self.gmres_calls = 0
+        self.gmres_seconds = 0.0
+        self.attempts = 0
+        self.deadline = deadline
 
     # -------------------------------------------------------------- helpers
     def _check(self, rc, what):
@@ -95,10 +118,15 @@ class ImplicitEuler:
                                                        dt.data_ptr(), per_cell, scales, _stream_ptr()),
                         "mcfd_implicit_prepare")
             raise_for_status(self.geom.status_code(), err)
+            if self.deadline is not None and time.perf_counter() > self.deadline:
+                raise BudgetExceeded("wall-clock budget of the implicit step exceeded")
             iters = C.c_int32(0)
+            t0 = time.perf_counter()
             rc = self.lib.mcfd_gmres(self.geom.handle, self.rhs.data_ptr(), self.correction.data_ptr(),
                                      float(s.gmres_tolerance), int(s.gmres_max_iterations),
                                      int(s.gmres_krylov_dimension), C.byref(iters), _stream_ptr())
+            self.gmres_seconds += time.perf_counter() - t0
+            self.gmres_calls += 1
             self.gmres_iterations += iters.value
             if rc == 6:
                 raise err(f"Implicit Euler GMRES did not converge within {s.gmres_max_iterations} iterations "
@@ -135,6 +163,7 @@ class ImplicitEuler:
         last = None
         attempts = 12 if allow_time_step_reduction else 1
         for _ in range(attempts):
+            self.attempts += 1
             try:
                 return self.solve_once(initial, attempted), attempted
             except SolverError as error:

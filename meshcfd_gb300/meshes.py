@@ -102,6 +102,87 @@ def build_faces(points: np.ndarray, cells: CellArray, classify) -> FiniteVolumeM
     )
 
 
+def permute_mesh(mesh: FiniteVolumeMesh, cell_order=None, face_order=None) -> FiniteVolumeMesh:
+    """The same mesh with other cell and face ids: new cell k is old cell
+    ``cell_order[k]``, new face k is old face ``face_order[k]`` (None keeps
+    the ids).  Owners, neighbours, face orientation and the patches' face
+    order are carried over, so the geometry is the same up to the ids (a
+    mesh read from a file arrives in whatever order the file has)."""
+    offsets = np.asarray(mesh.cells.offsets, dtype=np.int64)
+    nodes = np.asarray(mesh.cells.nodes, dtype=np.int64)
+    n_cells, n_faces = len(offsets) - 1, len(mesh.faces)
+    co = np.arange(n_cells) if cell_order is None else np.asarray(cell_order, dtype=np.int64)
+    fo = np.arange(n_faces) if face_order is None else np.asarray(face_order, dtype=np.int64)
+    inv_c = np.empty(n_cells, dtype=np.int64)
+    inv_c[co] = np.arange(n_cells)
+    inv_f = np.empty(n_faces, dtype=np.int64)
+    inv_f[fo] = np.arange(n_faces)
+    counts = np.diff(offsets)[co]
+    new_offsets = np.concatenate(([0], np.cumsum(counts))).astype(np.int64)
+    take = np.concatenate([np.arange(offsets[c], offsets[c + 1]) for c in co]) if n_cells else np.empty(0, np.int64)
+    owners = inv_c[np.asarray(mesh.face_owners, dtype=np.int64)[fo]]
+    nb = np.asarray(mesh.face_neighbours, dtype=np.int64)[fo]
+    neighbours = np.where(nb >= 0, inv_c[np.maximum(nb, 0)], -1)
+    face_ids = np.asarray(mesh.cell_face_ids.nodes, dtype=np.int64)[take]
+    signs = np.asarray(mesh.cell_face_signs.nodes)[take]
+    return FiniteVolumeMesh(
+        points=mesh.points,
+        cells=CellArray(new_offsets, nodes[take]),
+        faces=np.asarray(mesh.faces)[fo],
+        face_owners=owners,
+        face_neighbours=neighbours,
+        face_patch_ids=np.asarray(mesh.face_patch_ids)[fo],
+        patches=tuple(MeshPatch(p.id, p.name, tuple(int(inv_f[f]) for f in p.face_ids)) for p in mesh.patches),
+        cell_face_ids=CellArray(new_offsets, inv_f[face_ids]),
+        cell_face_signs=CellArray(new_offsets, signs),
+    )
+
+
+def reverse_cuthill_mckee(mesh: FiniteVolumeMesh) -> tuple[np.ndarray, np.ndarray]:
+    """Cell and face orders that number the mesh by reverse Cuthill-McKee
+    (breadth-first from a minimum-degree cell, neighbours by increasing
+    degree, reversed), faces then by their smaller new cell id.  For
+    :func:`permute_mesh`."""
+    owners = np.asarray(mesh.face_owners, dtype=np.int64)
+    nbs = np.asarray(mesh.face_neighbours, dtype=np.int64)
+    n = len(mesh.cells.offsets) - 1
+    inner = nbs >= 0
+    a = np.concatenate((owners[inner], nbs[inner]))
+    b = np.concatenate((nbs[inner], owners[inner]))
+    order = np.lexsort((b, a))
+    a, b = a[order], b[order]
+    ptr = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(ptr, a + 1, 1)
+    ptr = np.cumsum(ptr)
+    degree = np.diff(ptr)
+    seen = np.zeros(n, dtype=bool)
+    out = np.empty(n, dtype=np.int64)
+    k = 0
+    for start in np.argsort(degree, kind="stable"):
+        if seen[start]:
+            continue
+        seen[start] = True
+        out[k] = start
+        head, k = k, k + 1
+        while head < k:
+            c = out[head]
+            head += 1
+            nb = b[ptr[c]:ptr[c + 1]]
+            nb = nb[~seen[nb]]
+            if len(nb):
+                nb = np.unique(nb)
+                nb = nb[np.argsort(degree[nb], kind="stable")]
+                seen[nb] = True
+                out[k:k + len(nb)] = nb
+                k += len(nb)
+    cell_order = out[::-1].copy()
+    new_id = np.empty(n, dtype=np.int64)
+    new_id[cell_order] = np.arange(n)
+    key = np.where(inner, np.minimum(new_id[owners], new_id[np.maximum(nbs, 0)]), new_id[owners])
+    face_order = np.lexsort((np.where(inner, np.maximum(new_id[owners], new_id[np.maximum(nbs, 0)]), -1), key))
+    return cell_order, face_order
+
+
 def to_reference_mesh(mesh: FiniteVolumeMesh, mesh_type):
     """Convert to the reference's tuple-based ``FiniteVolumeMesh`` (small meshes)."""
     patch_type = type(mesh.patches[0]) if mesh.patches else None

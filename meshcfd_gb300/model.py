@@ -52,6 +52,12 @@ TIME_STEP_MODES = ("Global adaptive", "Global fixed", "Local (steady)")
 FLUX_CODES = {"Rusanov": 0, "HLLC": 1, "Roe": 2}
 RECONSTRUCTION_CODES = {"First order": 0, "MUSCL linear": 1, "MUSCL parabolic": 2}
 LIMITER_CODES = {"Barth-Jespersen": 0, "Minmod": 1, "Van Leer": 2, "Venkatakrishnan": 3}
+# Extension with no counterpart in the reference: Venkatakrishnan's limiter in
+# its published form with the smoothing constant K (limiter code 4), chosen
+# with ``limiter = "Venkatakrishnan K"``; K is the settings attribute
+# ``venkatakrishnan_k`` (default VENKATAKRISHNAN_K_DEFAULT).
+EXTENSION_LIMITER_CODES = {"Venkatakrishnan K": 4}
+VENKATAKRISHNAN_K_DEFAULT = 5.0
 
 
 @dataclass

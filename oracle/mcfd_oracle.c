@@ -81,6 +81,7 @@ typedef struct {
 typedef struct {
   int32_t flux, reconstruction, limiter, pad;
   double gamma, acceleration_x, acceleration_y, cfl, gas_constant;
+  double venkat_k; /* K of limiter code 4 */
 } orc_settings;
 
 /* ------------------------------------------------------------ euler.py */
@@ -247,13 +248,27 @@ static int numerical_flux(int scheme, const double* L, const double* R, const do
 /* ------------------------------------------------------------ _kernels.py */
 
 /* limited_gradient_factors (_kernels.py:10-67) */
+/* code 4: Venkatakrishnan's limiter in its published form with the smoothing
+ * constant K (J. Comput. Phys. 118, 120-130, 1995), an extension with no
+ * counterpart in the reference: per face, d2 = grad . r, d1 = max - v
+ * (d2 > 0) or min - v (d2 <= 0), e2 = (K sqrt(A))^3,
+ * f = (d1^2 + e2 + 2 d1 d2) / (d1^2 + 2 d2^2 + d1 d2 + e2), and the cell
+ * factor is the least f over its faces (no cap at 1). */
+static double venkat_k_face(double v, double inc, double lo, double hi, double e2) {
+  const double d1 = inc > 0.0 ? hi - v : lo - v;
+  const double d1d1 = d1 * d1, d12 = d1 * inc;
+  const double num = (d1d1 + e2) + (d12 + d12);
+  const double den = ((d1d1 + 2.0 * (inc * inc)) + d12) + e2;
+  return num / den;
+}
+
 static void limited_gradient_factors(int64_t C, const double* P, const double* grad, const orc_geom* g,
-                                     int code, double* factors) {
+                                     int code, double venkat_k, double* factors) {
   double* lo = (double*)malloc(sizeof(double) * 4 * C);
   double* hi = (double*)malloc(sizeof(double) * 4 * C);
   memcpy(lo, P, sizeof(double) * 4 * C);
   memcpy(hi, P, sizeof(double) * 4 * C);
-  for (int64_t i = 0; i < 4 * C; ++i) factors[i] = 1.0;
+  for (int64_t i = 0; i < 4 * C; ++i) factors[i] = code == 4 ? INFINITY : 1.0;
   for (int64_t e = 0; e < g->n_gradient; ++e) {
     int64_t s = g->gradient_sources[e], nb = g->gradient_neighbours[e];
     for (int v = 0; v < 4; ++v) {
@@ -265,6 +280,17 @@ static void limited_gradient_factors(int64_t C, const double* P, const double* g
   for (int64_t e = 0; e < g->n_limiter; ++e) {
     int64_t c = g->limiter_cells[e];
     double dx = g->limiter_dx[e], dy = g->limiter_dy[e];
+    if (code == 4) {
+      const double t = venkat_k * sqrt(g->areas[c]);
+      const double e2 = (t * t) * t;
+      for (int v = 0; v < 4; ++v) {
+        const double cv = P[4 * c + v];
+        const double inc = grad[8 * c + 2 * v] * dx + grad[8 * c + 2 * v + 1] * dy;
+        const double f = venkat_k_face(cv, inc, lo[4 * c + v], hi[4 * c + v], e2);
+        if (f < factors[4 * c + v]) factors[4 * c + v] = f;
+      }
+      continue;
+    }
     for (int v = 0; v < 4; ++v) {
       double cv = P[4 * c + v];
       double inc = grad[8 * c + 2 * v] * dx + grad[8 * c + 2 * v + 1] * dy;
@@ -294,7 +320,7 @@ static void limited_gradient_factors(int64_t C, const double* P, const double* g
 }
 
 /* linear_gradients_and_factors (_kernels.py:240-273); grad is (C,4,2) */
-void orc_linear_gradients_and_factors(const orc_geom* g, const double* P, int code, double* grad,
+void orc_linear_gradients_and_factors(const orc_geom* g, const double* P, int code, double venkat_k, double* grad,
                                       double* factors) {
   int64_t C = g->n_cells;
   memset(grad, 0, sizeof(double) * 8 * C);
@@ -307,7 +333,7 @@ void orc_linear_gradients_and_factors(const orc_geom* g, const double* P, int co
       grad[8 * s + 2 * v + 1] += cy * d;
     }
   }
-  limited_gradient_factors(C, P, grad, g, code, factors);
+  limited_gradient_factors(C, P, grad, g, code, venkat_k, factors);
 }
 
 /* reconstruct_hllc_flux (_kernels.py:71-160), one face */
@@ -490,7 +516,7 @@ static int full_rank5(const double M[5][5], double LU[5][5], const int piv[5], i
 int orc_parabolic_reconstruction(const orc_geom* g, const double* P, int code, double* grad, double* curv,
                                  double* fac) {
   int64_t C = g->n_cells, NE = g->n_parabolic;
-  if (g->n_gradient) orc_linear_gradients_and_factors(g, P, code, grad, fac);
+  if (g->n_gradient) orc_linear_gradients_and_factors(g, P, code, 0.0, grad, fac);
   else {
     memset(grad, 0, sizeof(double) * 8 * C);
     for (int64_t i = 0; i < 4 * C; ++i) fac[i] = 1.0;
@@ -878,7 +904,7 @@ int orc_residual(const orc_geom* g, const orc_settings* s, const double* U, doub
     curv = (double*)calloc(12 * C, sizeof(double));
     orc_parabolic_reconstruction(g, P, s->limiter, grad, curv, fac);
   } else if (s->reconstruction == 1 && g->n_gradient) {
-    orc_linear_gradients_and_factors(g, P, s->limiter, grad, fac);
+    orc_linear_gradients_and_factors(g, P, s->limiter, s->venkat_k, grad, fac);
   } else {
     for (int64_t i = 0; i < 4 * C; ++i) fac[i] = 1.0;
   }

@@ -20,7 +20,7 @@ LIB = HERE / "_build" / "libmcfd_oracle.so"
 
 FLUX = {"Rusanov": 0, "HLLC": 1, "Roe": 2}
 RECON = {"First order": 0, "MUSCL linear": 1, "MUSCL parabolic": 2}
-LIMITER = {"Barth-Jespersen": 0, "Minmod": 1, "Van Leer": 2, "Venkatakrishnan": 3}
+LIMITER = {"Barth-Jespersen": 0, "Minmod": 1, "Van Leer": 2, "Venkatakrishnan": 3, "Venkatakrishnan K": 4}
 SCHEME = {"Explicit Euler": 0, "Explicit RK2": 1, "Explicit RK3": 2, "Explicit RK4": 3}
 
 STATUS_TEXT = {
@@ -72,7 +72,7 @@ class OrcGeom(C.Structure):
 class OrcSettings(C.Structure):
     _fields_ = [("flux", C.c_int32), ("reconstruction", C.c_int32), ("limiter", C.c_int32), ("pad", C.c_int32),
                 ("gamma", C.c_double), ("acceleration_x", C.c_double), ("acceleration_y", C.c_double),
-                ("cfl", C.c_double), ("gas_constant", C.c_double)]
+                ("cfl", C.c_double), ("gas_constant", C.c_double), ("venkat_k", C.c_double)]
 
 
 def build(force: bool = False) -> Path:
@@ -96,7 +96,7 @@ def lib():
         _lib.orc_explicit_step.argtypes = [C.POINTER(OrcGeom), C.POINTER(OrcSettings), C.c_int, PD, PD, C.c_int]
         _lib.orc_conservative_to_primitive.argtypes = [C.c_int64, PD, C.c_double, PD]
         _lib.orc_primitive_to_conservative.argtypes = [C.c_int64, PD, C.c_double, PD]
-        _lib.orc_linear_gradients_and_factors.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD]
+        _lib.orc_linear_gradients_and_factors.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, C.c_double, PD, PD]
         _lib.orc_parabolic_reconstruction.argtypes = [C.POINTER(OrcGeom), PD, C.c_int, PD, PD, PD]
         _lib.orc_bc_states.argtypes = [C.POINTER(OrcGeom), C.c_int64, PD, C.c_double, C.c_double, PD]
         _lib.orc_far_field_states.argtypes = [C.c_int64, PD, PD, PD, C.c_double, PD]
@@ -292,6 +292,7 @@ class Oracle:
         s.acceleration_y = num.acceleration_y
         s.cfl = num.cfl
         s.gas_constant = num.gas_constant
+        s.venkat_k = float(getattr(num, "venkatakrishnan_k", 5.0))
         return s
 
     def primitive(self, U, gamma):
@@ -348,12 +349,12 @@ class Oracle:
             _raise(0x02)
         return R
 
-    def gradients_and_factors(self, P, limiter):
+    def gradients_and_factors(self, P, limiter, venkat_k=5.0):
         P = np.ascontiguousarray(P, dtype=np.float64)
         grad = np.empty((len(P), 4, 2))
         fac = np.empty((len(P), 4))
         lib().orc_linear_gradients_and_factors(C.byref(self.struct), P.ctypes.data_as(PD), LIMITER[limiter],
-                                               grad.ctypes.data_as(PD), fac.ctypes.data_as(PD))
+                                               float(venkat_k), grad.ctypes.data_as(PD), fac.ctypes.data_as(PD))
         return grad, fac
 
     def parabolic_reconstruction(self, P, limiter):

@@ -15,11 +15,14 @@ agree with the oracle to rounding (~1e-13), not bit for bit.
 
 from __future__ import annotations
 
+import math
+
 import numpy as np
+
 import torch
 
 FLUX = {"Rusanov": 0, "HLLC": 1, "Roe": 2}
-LIMITER = {"Barth-Jespersen": 0, "Minmod": 1, "Van Leer": 2, "Venkatakrishnan": 3}
+LIMITER = {"Barth-Jespersen": 0, "Minmod": 1, "Van Leer": 2, "Venkatakrishnan": 3, "Venkatakrishnan K": 4}
 
 
 def _t(a, dtype=torch.float64, shape=None):
@@ -151,6 +154,7 @@ class TorchResidual:
         if settings.reconstruction not in ("First order", "MUSCL linear"):
             raise NotImplementedError(settings.reconstruction)
         self.limiter = LIMITER[settings.limiter]
+        self.venkat_k = float(getattr(settings, "venkatakrishnan_k", 5.0))
         self.ax, self.ay = float(settings.acceleration_x), float(settings.acceleration_y)
         i64 = torch.int64
         self.C = len(g.areas)
@@ -194,6 +198,14 @@ class TorchResidual:
         c = self.lcell
         cv = P.index_select(0, c)
         inc = gx.index_select(0, c) * self.ldx[:, None] + gy.index_select(0, c) * self.ldy[:, None]
+        if self.limiter == 4:  # Venkatakrishnan with K (extension): least face factor, no cap
+            t = self.venkat_k * torch.sqrt(self.areas.index_select(0, c))
+            e2 = ((t * t) * t)[:, None]
+            d1 = torch.where(inc > 0.0, hi.index_select(0, c) - cv, lo.index_select(0, c) - cv)
+            f = ((d1 * d1 + e2) + 2.0 * d1 * inc) / (((d1 * d1 + 2.0 * (inc * inc)) + d1 * inc) + e2)
+            phi = torch.full_like(P, math.inf).scatter_reduce(0, c[:, None].expand(-1, 4), f, "amin",
+                                                              include_self=True)
+            return gx, gy, phi
         tol = 1e-14 * torch.clamp(cv.abs(), min=1.0)
         one = torch.ones_like(cv)
         up = (hi.index_select(0, c) - cv) / torch.where(inc > tol, inc, one)

@@ -175,3 +175,113 @@ def test_bump_channel_implicit_steps_match_the_oracle(cuda_device):
     err = np.abs(U.cpu().numpy() - U_ref).max() / np.abs(U_ref).max()
     print(f"bump 32x16, 3 implicit steps: max relative difference {err:.2e}")
     assert err <= 1e-12, err  # measured 1.6e-16: the GMRES iterates track SciPy's
+
+
+def _prepare_on(g, s, P, cuda_device):
+    """An implicit operator prepared on geometry g at primitive state P with
+    the recipe's local time steps and the Newton scales of the state."""
+    import torch
+    from meshcfd_gb300.device import DeviceGeometry, make_config
+    from oracle.implicit import ImplicitOracle
+    from oracle.oracle import Oracle
+
+    orc = Oracle(g)
+    U0 = orc.conservative(P, s.gamma)
+    dt = orc.stable_time_steps(P, s)
+    scales = ImplicitOracle.scales(U0, P, s.gamma)[0]
+    dg = DeviceGeometry(g)
+    cfg = make_config(s)
+    U = torch.as_tensor(U0, device=cuda_device)
+    dtd = torch.as_tensor(dt, device=cuda_device)
+    assert dg.lib.mcfd_implicit_prepare(dg.handle, C.byref(cfg), U.data_ptr(), dtd.data_ptr(), 1,
+                                        (C.c_double * 4)(*scales), torch.cuda.current_stream().cuda_stream) == 0
+    dg.check_status()
+    return dg, U0, dt, scales
+
+
+def _permuted_periodic(n, seed):
+    """A periodic mesh whose cell and face ids are randomly permuted: its
+    LU-SGS levels are few and wide and rows depend on far-away positions."""
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import periodic_case, permute_mesh
+
+    case = periodic_case(n, n, split="half", jitter=0.2, seed=5)
+    rng = np.random.default_rng(seed)
+    case.mesh = permute_mesh(case.mesh, rng.permutation(len(case.mesh.cells)), rng.permutation(len(case.mesh.faces)))
+    s = case.numerics
+    s.flux, s.reconstruction, s.time_integration, s.cfl = "Roe", "MUSCL linear", "Implicit Euler", 50.0
+    s.time_step_mode = "Local (steady)"
+    return case, build_geometry(case.mesh, case)
+
+
+@pytest.mark.parametrize("mesh", ("bump", "permuted"))
+def test_lusgs_schedules_agree_and_match_spsolve(cuda_device, mesh):
+    """Every launch schedule of the level-scheduled sweeps (one block
+    stepping through narrow levels with its shared-memory ring, grid launches
+    per level, and mixtures) gives the same bits, and matches the reference's
+    two spsolve_triangular calls (within 1e-12)."""
+    import torch
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import bump_case, smooth_primitive
+    from oracle.implicit import ImplicitOracle
+    from dataclasses import replace
+
+    if mesh == "bump":
+        case, P = bump_case(96, 48)
+        P = P * (1.0 + 0.05 * np.random.default_rng(4).standard_normal(P.shape))
+        s = case.numerics
+        g = build_geometry(case.mesh, case)
+    else:
+        case, g = _permuted_periodic(64, 7)
+        s = case.numerics
+        P = smooth_primitive(len(g.areas), seed=3)
+    dg, U0, dt, _ = _prepare_on(g, s, P, cuda_device)
+    v = torch.as_tensor(np.random.default_rng(2).standard_normal(U0.shape), device=cuda_device)
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for wide in (0, 1, 7, 1 << 30):
+        assert dg.lib.mcfd_implicit_set_sweep(dg.handle, wide) == 0
+        x = torch.empty_like(v)
+        assert dg.lib.mcfd_lusgs_apply(dg.handle, v.data_ptr(), x.data_ptr(), stream) == 0
+        outs.append(x.cpu().numpy())
+    dg.check_status()
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
+    M = ImplicitOracle(g).preconditioner(P, replace(s, reconstruction="First order"), dt)
+    ref = M.matvec(v.cpu().numpy().ravel()).reshape(U0.shape)
+    assert np.abs(outs[0] - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("exact_jacobian", (0, 1))
+def test_gmres_captured_inner_loop_equals_host_stepping(cuda_device, exact_jacobian):
+    """The restart cycle as a CUDA graph with a device-set loop condition
+    against the same Arnoldi steps driven from the host one at a time (the
+    path taken while profiling events are recorded): equal iteration counts
+    and solutions bit for bit, twice in a row (graph reuse), with both
+    Jacobians."""
+    import torch
+    from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.meshes import bump_case
+
+    case, P = bump_case(48, 24)
+    P = P * (1.0 + 0.05 * np.random.default_rng(5).standard_normal(P.shape))
+    s = case.numerics
+    g = build_geometry(case.mesh, case)
+    dg, U0, dt, _ = _prepare_on(g, s, P, cuda_device)
+    assert dg.lib.mcfd_implicit_set_jacobian(dg.handle, exact_jacobian) == 0
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(9)
+    for _ in range(2):
+        b = torch.as_tensor(rng.standard_normal(U0.shape), device=cuda_device)
+        results = []
+        for profiling in (0, 1):
+            dg.lib.mcfd_profile_enable(dg.handle, profiling)
+            x = torch.empty_like(b)
+            it = C.c_int32(0)
+            rc = dg.lib.mcfd_gmres(dg.handle, b.data_ptr(), x.data_ptr(), 1e-3, 120, 30, C.byref(it), stream)
+            results.append((rc, it.value, x.cpu().numpy()))
+        dg.lib.mcfd_profile_enable(dg.handle, 0)
+        dg.check_status()
+        (rc0, it0, x0), (rc1, it1, x1) = results
+        assert rc0 == rc1 and rc0 in (0, 6) and it0 == it1 and it0 > 30  # more than one restart cycle
+        np.testing.assert_array_equal(x0, x1)
