@@ -825,6 +825,7 @@ def adjoint_measure(args, device, steps, clocks=True):
     fwd_ms, adj_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
     C = int(dg.n_cells)
     far = float(adj.far_acc.norm())
+    fd_check = adjoint_fd_check(dg, case, g, P0, steps, args) if steps >= 400 else None
     out = {
         "workload": f"O-grid 1024x512 around a cylinder ({C} cells), Mach 0.3, HLLC, MUSCL linear, "
                     f"Venkatakrishnan, RK3 fixed dt, {steps} steps, checkpoint every {args.checkpoint_every}",
@@ -835,9 +836,50 @@ def adjoint_measure(args, device, steps, clocks=True):
                     "work_per_step": "1 replayed RK3 step + 3 residual VJPs"},
         "J": J, "grad_norm": float(lam0.norm()), "far_grad_norm": far,
         "far_grad_note": far_note(P0, settings.gamma, steps * dt) if far == 0.0 else None,
+        "fd_check": fd_check,
         "gpu_launches": launches, "clocks": sampler.summary() if sampler else None,
     }
     dg.close()
+    return out
+
+
+def adjoint_fd_check(dg, case, g, P, steps, args):
+    """The configuration's gradient check: from the inflow state plus a
+    seeded 10 % perturbation, the adjoint gradient of the x wall force in a
+    smooth localised initial-state direction (a Gaussian blob upstream of
+    the cylinder) against central differences with step 1e-6, with the
+    reference's limiter and with the smooth form (K = 5)."""
+    import torch
+
+    from meshcfd_gb300.adjoint import WallForceAdjoint
+    from meshcfd_gb300.device import primitive_to_conservative
+
+    out = {"steps": steps, "checkpoint_every": args.checkpoint_every, "h": 1e-6,
+           "direction": "Gaussian blob (width 0.5) at (-1.5, 0.2) in every variable, scaled by |U|",
+           "initial_state": "inflow + seeded 10 % perturbation", "bar": 1e-6}
+    rng = np.random.default_rng(11)
+    P0 = P + 0.1 * np.array([1.0, 0.3, 0.3, 1.0]) * rng.standard_normal(P.shape)
+    U0 = primitive_to_conservative(P0, case.numerics.gamma)
+    centers = np.asarray(g.centers).reshape(-1, 2)
+    r2 = ((centers - np.array([-1.5, 0.2])) ** 2).sum(axis=1)
+    v = np.exp(-r2 / 0.25)[:, None] * np.abs(U0) * np.array([1.0, 0.5, -0.7, 0.8])
+    from meshcfd_gb300.device import make_config
+
+    for limiter in ("Venkatakrishnan", "Venkatakrishnan K"):
+        case.numerics.limiter = limiter
+        case.numerics.venkatakrishnan_k = 5.0
+        cfg = make_config(case.numerics, args.mode)
+        _, dt_min = dg.time_steps(dg.primitive(torch.as_tensor(U0, device=dg.device), cfg), cfg)
+        dt = 0.5 * float(dt_min)
+        adj = WallForceAdjoint(dg, case.numerics, dt, direction=(1.0, 0.0), checkpoint_every=args.checkpoint_every,
+                               mode=args.mode)
+        _, lam0, _ = adj.gradient(torch.as_tensor(U0, device=dg.device), steps)
+        vals = [adj.functional(adj.forward(torch.as_tensor(U0 + sg * 1e-6 * v, device=dg.device), steps))[0]
+                for sg in (1, -1)]
+        fd = (vals[0] - vals[1]) / 2e-6
+        an = float((lam0.cpu().numpy() * v).sum())
+        out[limiter] = {"adjoint": an, "fd": fd, "rel_err": abs(fd - an) / abs(fd)}
+    case.numerics.limiter = "Venkatakrishnan"
     return out
 
 
@@ -947,16 +989,18 @@ def run_bump(args):
                           "mean_cfl_used": float(s.cfl * float(used.mean()) / float(dt.mean())),
                           "density_residual": r, "drop": r / r0})
     launches = _launches() - before
-    vs_oracle = None
+    vs_oracle = cpu = None
     if args.bump_oracle and first_state is not None:
         from oracle.implicit import ImplicitOracle
 
         to = time.perf_counter()
         ref, _ = ImplicitOracle(g).step(U0, first_dt, s)
-        vs_oracle = {"steps": 1, "state_max_rel_err": max_rel(first_state, ref),
-                     "oracle_seconds": time.perf_counter() - to,
+        secs = time.perf_counter() - to
+        vs_oracle = {"steps": 1, "state_max_rel_err": max_rel(first_state, ref), "oracle_seconds": secs,
                      "oracle": "oracle/implicit.py: the reference's implicit step over the C residual, SciPy gmres "
                                "and spsolve_triangular, one host thread"}
+        cpu = {"value": secs, "unit": "s/step", "cores": 1, "kind": "port",
+               "sample": "the first implicit step of the same recipe (oracle restatement, SciPy, one thread)"}
     n = len(steps)
     per_step = sum(x["seconds"] for x in steps) / n if n else None
     estimate = None
@@ -976,7 +1020,7 @@ def run_bump(args):
         "status": status, "per_step": steps, "initial_density_residual": r0,
         "ms_per_gmres_iteration": (1e3 * stepper.gmres_seconds / stepper.gmres_iterations
                                    if stepper.gmres_iterations else None),
-        "time_to_8_orders": estimate, "vs_oracle": vs_oracle,
+        "time_to_8_orders": estimate, "vs_oracle": vs_oracle, "cpu_baseline": cpu,
         "gpu_launches": launches, "clocks": clocks.summary(),
     }
     print(json.dumps(line))

@@ -386,10 +386,14 @@ int mcfd_wall_force(mcfd_geom* geom, const mcfd_config* cfg, const double* U, do
  * triangular solves' (rows summed in ascending column order). */
 int mcfd_lusgs_apply(mcfd_geom* geom, const double* v, double* x, void* stream);
 /* Launch schedule of the LU-SGS sweeps: runs of levels at most wide_level
- * rows wide go to one block that steps through them (a barrier per level),
- * wider levels get a grid launch each; 0 restores the default (16384).
- * Results do not depend on it.  No counterpart in the reference. */
-int mcfd_implicit_set_sweep(mcfd_geom* geom, int32_t wide_level);
+ * rows wide go to one launch that steps through them with a barrier per
+ * level, swept by one block (cluster = 1) or a thread-block cluster of 8 or
+ * 16 blocks sharing their latest solutions in distributed shared memory;
+ * wider levels get a grid launch each.  0 restores the defaults (16384, one
+ * block); 8 or 16 returns MCFD_E_UNSUPPORTED where the device cannot run
+ * that cluster size.  Results do not depend on it.  No counterpart in the
+ * reference. */
+int mcfd_implicit_set_sweep(mcfd_geom* geom, int32_t wide_level, int32_t cluster);
 /* Solve operator(x) = b with restarted GMRES(krylov_dim) preconditioned by
  * LU-SGS, as _solve_gmres drives SciPy's gmres (solver.py:1489-1529; left
  * preconditioning, modified Gram-Schmidt, Givens rotations).  b, x: device

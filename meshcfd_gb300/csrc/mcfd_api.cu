@@ -1335,11 +1335,12 @@ int mcfd_lusgs_apply(mcfd_geom* h, const double* v, double* x, void* stream) {
   return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return lusgs_apply(h->imp, v, x, s); }));
 }
 
-int mcfd_implicit_set_sweep(mcfd_geom* h, int32_t wide_level) {
-  if (!h || wide_level < 0) return MCFD_E_ARG;
+int mcfd_implicit_set_sweep(mcfd_geom* h, int32_t wide_level, int32_t cluster) {
+  if (!h || wide_level < 0 || (cluster != 0 && cluster != 1 && cluster != 8 && cluster != 16)) return MCFD_E_ARG;
   int c = ensure_implicit(h);
   if (c) return c;
-  implicit_set_wide_level(h->imp, wide_level);
+  if ((cluster == 8 && !h->imp.cluster8_ok) || (cluster == 16 && !h->imp.cluster16_ok)) return MCFD_E_UNSUPPORTED;
+  implicit_set_wide_level(h->imp, wide_level, cluster ? cluster : 1);
   return MCFD_OK;
 }
 

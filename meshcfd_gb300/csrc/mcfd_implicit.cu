@@ -124,8 +124,10 @@ struct SweepDev {
 };
 
 constexpr int kWaveThreads = 512;
+constexpr int kClusterThreads = 256;
 constexpr int kRing = 4096;        // latest solved rows kept in shared memory (128 KiB)
 constexpr int kWideLevel = 16384;  // wider levels get a grid launch each
+constexpr int kPortableCluster = 8;  // the portable cluster size of the cluster sweep
 constexpr size_t kRingBytes = kRing * 4 * sizeof(double);
 
 // Everything of a row that does not depend on the solution: loaded for the
@@ -239,6 +241,95 @@ __global__ void __launch_bounds__(kWaveThreads, 1) k_lusgs_wavefront(SweepDev a,
       if (have) sweep_load(a, b + t, R);
     }
     __syncthreads();
+  }
+}
+
+// The same sweep over a thread-block cluster of NC blocks (one per SM): the
+// rows of a level are dealt out round robin (row b + rank + NC t in block
+// `rank`), every block stores each solution it computes into the rings of
+// all NC blocks (distributed shared memory), and a cluster barrier with
+// release / acquire semantics separates the levels.  Reads of earlier
+// solutions are local shared-memory loads, or, outside the ring, loads that
+// bypass L1 (another block of the cluster may have written the line).  A
+// level's FP64 work is split over NC SMs, which is what bounds the
+// single-block sweep on narrow levels of a few hundred rows.
+__device__ __forceinline__ St4 ld4_cg(const double* p) {
+  const double2 a = __ldcg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldcg(reinterpret_cast<const double2*>(p) + 1);
+  return St4{a.x, a.y, b.x, b.y};
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kClusterThreads, 1) k_lusgs_cluster(SweepDev a, int l0, int l1) {
+  extern __shared__ double ring[];  // [kRing][4], the same contents in every block of the cluster
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  double* rings[NC];
+#pragma unroll
+  for (int r = 0; r < NC; ++r) rings[r] = cluster.map_shared_rank(ring, r);
+  cluster.sync();  // every block is running before any remote store
+  const int base = a.level_ptr[l0];
+  const int stride = NC * (int)blockDim.x;
+  const int first = rank + NC * (int)threadIdx.x;
+  SweepRow R;
+  int b = base, e = a.level_ptr[l0 + 1];
+  bool have = b + first < e;
+  if (have) sweep_load(a, b + first, R);
+  auto solve = [&](const SweepRow& W, int p, int lo) {
+    double acc[4] = {W.r.a, W.r.b, W.r.c, W.r.d};
+#pragma unroll
+    for (int k = 0; k < kSweepPack; ++k) {
+      if (k < W.n) {
+        St4 x;
+        if (W.cp[k] >= lo) {
+          const double* q = ring + 4 * (W.cp[k] & (kRing - 1));
+          x = St4{q[0], q[1], q[2], q[3]};
+        } else {
+          x = ld4_cg(a.out + 4 * (size_t)W.cc[k]);
+        }
+        sweep_sub(acc, W.v[k], x);
+      }
+    }
+    if (W.n > kSweepPack) {
+      for (int j = a.ent_ptr[p] + kSweepPack, j1 = a.ent_ptr[p + 1]; j < j1; ++j) {
+        const int cp = a.ent_pos[j];
+        St4 x;
+        if (cp >= lo) {
+          const double* q = ring + 4 * (cp & (kRing - 1));
+          x = St4{q[0], q[1], q[2], q[3]};
+        } else {
+          x = ld4_cg(a.out + 4 * (size_t)a.ent_cell[j]);
+        }
+        sweep_sub(acc, a.rval[a.ent_val[j]], x);
+      }
+    }
+    const St4 res{div_rn(acc[0], W.dg), div_rn(acc[1], W.dg), div_rn(acc[2], W.dg), div_rn(acc[3], W.dg)};
+    st4(a.out + 4 * (size_t)W.i, res);
+    const int slot = 4 * (p & (kRing - 1));
+#pragma unroll
+    for (int r = 0; r < NC; ++r) {
+      double* q = rings[r] + slot;
+      q[0] = res.a;
+      q[1] = res.b;
+      q[2] = res.c;
+      q[3] = res.d;
+    }
+  };
+  for (int l = l0; l < l1; ++l) {
+    const int lo = max(e - kRing, base);
+    if (have) solve(R, b + first, lo);
+    for (int p = b + first + stride; p < e; p += stride) {
+      SweepRow W;
+      sweep_load(a, p, W);
+      solve(W, p, lo);
+    }
+    if (l + 1 < l1) {
+      b = e;
+      e = a.level_ptr[l + 2];
+      have = b + first < e;
+      if (have) sweep_load(a, b + first, R);
+    }
+    cluster.sync();
   }
 }
 
@@ -681,8 +772,9 @@ static void sweep_schedule(SweepPlan& pl, int wide) {
   }
 }
 
-void implicit_set_wide_level(ImplicitState& st, int wide) {
+void implicit_set_wide_level(ImplicitState& st, int wide, int cluster) {
   st.wide_level = wide > 0 ? wide : kWideLevel;
+  st.cluster = cluster;
   sweep_schedule(st.fwd, st.wide_level);
   sweep_schedule(st.bwd, st.wide_level);
   st.inner_key = -1;  // the captured loop holds the old launches
@@ -898,6 +990,36 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   if (e == cudaSuccess) e = cudaMallocHost((void**)&st.cycle_host, sizeof(GmresCycle));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_wavefront, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)kRingBytes);
+  // Sweeps of narrow levels run in one block by default: measured on the
+  // 512 x 256 bump (767 levels of at most 256 rows), one LU-SGS application
+  // takes 4.08 ms in one block, 4.68 ms in a cluster of 8 and 5.01 ms in a
+  // cluster of 16 (the cluster barrier and the remote ring stores cost more
+  // than the FP64 work they spread).  The cluster sweeps stay selectable
+  // where the device can run them (8: portable; 16: non-portable).
+  st.cluster = 1;
+  st.cluster8_ok = false;
+  if (e == cudaSuccess &&
+      cudaFuncSetAttribute(k_lusgs_cluster<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes) ==
+          cudaSuccess) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kPortableCluster);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = kRingBytes;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kPortableCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    st.cluster8_ok = cudaOccupancyMaxActiveClusters(&clusters, k_lusgs_cluster<8>, &cfg) == cudaSuccess && clusters > 0;
+  }
+  st.cluster16_ok =
+      cudaFuncSetAttribute(k_lusgs_cluster<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(k_lusgs_cluster<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  cudaGetLastError();
   if (e == cudaSuccess) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
@@ -964,7 +1086,23 @@ static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const dou
              pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, in, out, backward};
   for (const SweepPlan::Launch& l : pl.schedule) {
     count_launch();
-    if (l.wavefront) {
+    if (l.wavefront && st.cluster > 1) {
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3(st.cluster);
+      cfg.blockDim = dim3(kClusterThreads);
+      cfg.dynamicSmemBytes = kRingBytes;
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = st.cluster;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      const cudaError_t e = st.cluster == 16 ? cudaLaunchKernelEx(&cfg, k_lusgs_cluster<16>, a, l.l0, l.l1)
+                                             : cudaLaunchKernelEx(&cfg, k_lusgs_cluster<8>, a, l.l0, l.l1);
+      if (e != cudaSuccess) return e;
+    } else if (l.wavefront) {
       k_lusgs_wavefront<<<1, kWaveThreads, kRingBytes, s>>>(a, l.l0, l.l1);
     } else {
       const int b = pl.host_level_ptr[l.l0], e = pl.host_level_ptr[l.l0 + 1];

@@ -90,6 +90,8 @@ struct ImplicitState {
   int *dptr = nullptr, *dref = nullptr, *rptr = nullptr, *rref = nullptr, *rcol = nullptr;
   SweepPlan fwd, bwd;
   int wide_level = 0;  // levels wider than this get a grid launch each
+  int cluster = 1;     // blocks sweeping a run of narrow levels (1: one block; 8 or 16: a cluster)
+  bool cluster8_ok = false, cluster16_ok = false;
   // values and vectors (device)
   double *coef = nullptr, *bterm = nullptr, *diag = nullptr, *dclamp = nullptr, *rval = nullptr;
   double *tmp = nullptr, *state = nullptr, *rate = nullptr, *up = nullptr, *rp = nullptr;
@@ -136,7 +138,7 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
 cudaError_t implicit_set_operator(ImplicitState& st, ScaleVec scale, const double* dt, int dt_per_cell,
                                   cudaStream_t s);
 cudaError_t lusgs_apply(ImplicitState& st, const double* v, double* x, cudaStream_t s);
-void implicit_set_wide_level(ImplicitState& st, int wide);
+void implicit_set_wide_level(ImplicitState& st, int wide, int cluster);
 cudaError_t fd_operator(ImplicitState& st, const ResidualFn& residual1, const double* v, double* out,
                         cudaStream_t s);
 // matvec_key: distinguishes operators for the captured inner loop (a graph is

@@ -216,10 +216,11 @@ def _permuted_periodic(n, seed):
 
 @pytest.mark.parametrize("mesh", ("bump", "permuted"))
 def test_lusgs_schedules_agree_and_match_spsolve(cuda_device, mesh):
-    """Every launch schedule of the level-scheduled sweeps (one block
-    stepping through narrow levels with its shared-memory ring, grid launches
-    per level, and mixtures) gives the same bits, and matches the reference's
-    two spsolve_triangular calls (within 1e-12)."""
+    """Every launch schedule of the level-scheduled sweeps (one block or a
+    cluster of 8 or 16 stepping through narrow levels with their
+    shared-memory rings, grid launches per level, and mixtures) gives the
+    same bits, and matches the reference's two spsolve_triangular calls
+    (within 1e-12)."""
     import torch
     from meshcfd_gb300.geometry import build_geometry
     from meshcfd_gb300.meshes import bump_case, smooth_primitive
@@ -239,8 +240,11 @@ def test_lusgs_schedules_agree_and_match_spsolve(cuda_device, mesh):
     v = torch.as_tensor(np.random.default_rng(2).standard_normal(U0.shape), device=cuda_device)
     stream = torch.cuda.current_stream().cuda_stream
     outs = []
-    for wide in (0, 1, 7, 1 << 30):
-        assert dg.lib.mcfd_implicit_set_sweep(dg.handle, wide) == 0
+    for wide, cluster in ((0, 1), (0, 8), (0, 16), (1, 8), (7, 1), (7, 8), (1 << 30, 1), (1 << 30, 16)):
+        rc = dg.lib.mcfd_implicit_set_sweep(dg.handle, wide, cluster)
+        if cluster > 1 and rc == 3:
+            continue  # the device cannot run this cluster size
+        assert rc == 0
         x = torch.empty_like(v)
         assert dg.lib.mcfd_lusgs_apply(dg.handle, v.data_ptr(), x.data_ptr(), stream) == 0
         outs.append(x.cpu().numpy())
