@@ -687,6 +687,33 @@ def batch_measure(args, device, steps, clocks=True):
     dg.check_status()
     batched_ms = a.elapsed_time(b)
     done_steps = reps * gsteps
+    U_launches = U.clone()
+    # the same steps with each stage as one cooperative launch (grid barriers
+    # between reconstruction, fluxes and gather), captured the same way
+    dg.set_fused_stage(True)
+    fused_stepper = BatchStepper(dg, layout, settings, mode=args.mode)
+    U.copy_(torch.as_tensor(U0, device=device))
+    fused_stepper.capture(U, gsteps)
+    for _ in range(max(1, args.warmup // gsteps)):
+        fused_stepper.replay()
+    torch.cuda.synchronize()
+    U.copy_(torch.as_tensor(U0, device=device))
+    a.record()
+    for _ in range(reps):
+        fused_stepper.replay()
+    b.record()
+    torch.cuda.synchronize()
+    dg.check_status()
+    fused_ms = a.elapsed_time(b)
+    fused = {"ms": fused_ms, "cell_updates_per_s": int(dg.n_cells) * done_steps / (fused_ms * 1e-3),
+             "resident_blocks_per_sm": dg.fused_stage_blocks,
+             "bit_identical_to_launch_per_kernel": bool(torch.equal(U, U_launches))}
+    dg.set_fused_stage(False)
+    del fused_stepper
+    stage_launch = "one cooperative launch per stage" if fused_ms < batched_ms else "one launch per kernel"
+    per_kernel_ms = batched_ms
+    batched_ms = min(batched_ms, fused_ms)
+    U.copy_(U_launches)
     # one at a time: the plain path per case (its own geometry handle and loop)
     singles = [DeviceGeometry(g, device) for g in geoms]
     Us = [torch.as_tensor(U0[layout.cell_offsets[k]:layout.cell_offsets[k + 1]], device=device)
@@ -716,7 +743,11 @@ def batch_measure(args, device, steps, clocks=True):
                     f"Mach U[0.3,2.0], seed 3", "cells_total": n_cells, "mode": args.mode,
         "graph_steps": gsteps, "setup_s": setup_s, "steps": done_steps,
         "case_steps_per_s": layout.n_cases * done_steps / (batched_ms * 1e-3),
-        "batched": {"cell_updates_per_s": n_cells * done_steps / (batched_ms * 1e-3), "ms": batched_ms},
+        "batched": {"cell_updates_per_s": n_cells * done_steps / (batched_ms * 1e-3), "ms": batched_ms,
+                    "stage_launch": stage_launch},
+        "launch_per_kernel": {"cell_updates_per_s": n_cells * done_steps / (per_kernel_ms * 1e-3),
+                              "ms": per_kernel_ms},
+        "launch_per_stage": fused,
         "one_at_a_time": {"case_steps_per_s": layout.n_cases * done_steps / (single_ms * 1e-3), "ms": single_ms},
         "batched_over_one_at_a_time": single_ms / batched_ms,
         "bit_identical": bool(same), "clocks": sampler.summary() if sampler else None,
@@ -735,8 +766,8 @@ def run_batch(args):
         "ms_per_step": b["batched"]["ms"] / b["steps"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded channel/Riemann cases)",
         "config": {k: b[k] for k in ("workload", "cells_total", "mode", "graph_steps", "setup_s")},
-        **{k: b[k] for k in ("batched", "one_at_a_time", "batched_over_one_at_a_time", "bit_identical", "clocks",
-                             "batched_adjoint", "autotune")},
+        **{k: b[k] for k in ("batched", "launch_per_kernel", "launch_per_stage", "one_at_a_time",
+                             "batched_over_one_at_a_time", "bit_identical", "clocks", "batched_adjoint", "autotune")},
     }
     print(json.dumps(line))
 

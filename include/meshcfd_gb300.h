@@ -314,6 +314,17 @@ int mcfd_autotune(mcfd_geom* geom, const mcfd_config* cfg, const double* U, int3
  * 0 = default), e.g. to replay a tuning saved from an earlier run.  Results
  * do not depend on them.  No counterpart in the reference. */
 int mcfd_set_launch_shapes(mcfd_geom* geom, const int32_t* shapes);
+/* on = 1: run each explicit stage (mcfd_explicit_step, _record) as one
+ * cooperative launch of one resident grid — reconstruction, face fluxes and
+ * gather separated by grid barriers — where the settings allow it (fast
+ * mode, HLLC, MUSCL linear with a capped limiter, inviscid, no pressure-inlet or
+ * mass-flow patches, no body force); other settings keep the launch per
+ * kernel.  Results are identical either way.  on = 0 (the default) restores
+ * the launch per kernel.  No counterpart in the reference. */
+int mcfd_set_fused_stage(mcfd_geom* geom, int32_t on);
+/* Resident 256-thread blocks per SM of the last one-launch stage (0 before
+ * any).  No counterpart in the reference. */
+int mcfd_fused_stage_blocks(const mcfd_geom* geom);
 /* mcfd_explicit_step that also copies, for every stage k, the primitive state
  * it evaluates the residual at into stage_P[k] ([n_cells][4]) and, for MUSCL,
  * its face states into stage_recon[k] ([n_limiter][4], may be NULL): the

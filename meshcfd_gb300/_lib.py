@@ -110,6 +110,8 @@ SIGNATURES = {
     "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),
     "mcfd_implicit_matvec": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_implicit_set_jacobian": (c_i32, [c_vp, c_i32]),
+    "mcfd_set_fused_stage": (c_i32, [c_vp, c_i32]),
+    "mcfd_fused_stage_blocks": (c_i32, [c_vp]),
     "mcfd_implicit_set_sweep": (c_i32, [c_vp, c_i32, c_i32]),
     "mcfd_jvp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp]),
     "mcfd_vjp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp]),

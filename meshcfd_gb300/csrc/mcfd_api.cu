@@ -44,6 +44,9 @@ struct mcfd_geom {
   double* const* rec_P = nullptr;
   double* const* rec_recon = nullptr;
   int rec_n = 0, rec_k = 0;
+  // explicit stages as one cooperative launch where the settings allow it
+  bool fused_stage = false;
+  int fused_blocks = 0;  // resident blocks per SM of the last fused launch
 };
 
 namespace {
@@ -153,6 +156,19 @@ static cudaError_t stage(mcfd_geom* h, const mcfd_config& cfg, const StageProgra
   double* recon_out = h->ws.recon;
   if (record && h->rec_recon && h->rec_recon[h->rec_k] && cfg.reconstruction != MCFD_RECON_FIRST_ORDER)
     recon_out = h->rec_recon[h->rec_k];
+  if (h->fused_stage && MCFD_DISPATCH(cfg, stage_fused_supported(h->g, cfg, prog))) {
+    if (record) {
+      const int k = h->rec_k++;
+      e = cudaMemcpyAsync(h->rec_P[k], h->ws.P, 4 * sizeof(double) * (size_t)h->g.n_cells, cudaMemcpyDeviceToDevice,
+                          s);
+    }
+    if (e == cudaSuccess)
+      e = timed(h, MCFD_PROF_OTHER, s, [&] {
+        return MCFD_DISPATCH(cfg, launch_stage_fused(h->g, cfg, h->ws.P, recon_out, h->ws.flux, prog, s,
+                                                     &h->fused_blocks));
+      });
+    return e;
+  }
   if (cfg.reconstruction == MCFD_RECON_MUSCL_LINEAR)
     e = timed(h, MCFD_PROF_RECONSTRUCT, s, [&] { return MCFD_DISPATCH(cfg, launch_reconstruct(h->g, cfg, h->ws.P, recon_out, s)); });
   else if (cfg.reconstruction == MCFD_RECON_MUSCL_PARABOLIC)
@@ -1024,6 +1040,14 @@ int mcfd_set_launch_shapes(mcfd_geom* h, const int32_t* shapes) {
   h->g.tune_recon_split = shapes[4];
   return MCFD_OK;
 }
+
+int mcfd_set_fused_stage(mcfd_geom* h, int32_t on) {
+  if (!h || on < 0 || on > 1) return MCFD_E_ARG;
+  h->fused_stage = on != 0;
+  return MCFD_OK;
+}
+
+int mcfd_fused_stage_blocks(const mcfd_geom* h) { return h ? h->fused_blocks : 0; }
 
 const double* mcfd_geom_stage_state(const mcfd_geom* h, int32_t k) {
   return (h && k >= 0 && k < 4) ? h->ws.stage[k] : nullptr;

@@ -175,6 +175,10 @@ struct SideStream {
   cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const double* P,     \
                                 double* dt_cells, double* dt_min, double time_limit,           \
                                 cudaStream_t s);                                               \
+  bool stage_fused_supported(const DevGeom& g, const mcfd_config& cfg, const StageProgram& prog); \
+  cudaError_t launch_stage_fused(const DevGeom& g, const mcfd_config& cfg, const double* P,    \
+                                 double* recon, double* flux, const StageProgram& prog,        \
+                                 cudaStream_t s, int* blocks_per_sm);                          \
   }
 MCFD_DECLARE_LAUNCHERS(exact)
 MCFD_DECLARE_LAUNCHERS(fast)

@@ -35,11 +35,15 @@
 #define MCFD_FLUX_INT_MUL 4
 #endif
 
+#include <cooperative_groups.h>
+
 #include "mcfd_device.cuh"
 #include "mcfd_internal.h"
 
 namespace mcfd {
 namespace MCFD_VARIANT {
+
+namespace cg = cooperative_groups;
 
 static constexpr int kBlock = 256;
 static constexpr bool kFast = MCFD_FAST == 2;      // fast arithmetic (fluxes, primitive)
@@ -481,17 +485,13 @@ __device__ __forceinline__ int numerical_flux(const St4& L, const St4& R, double
   }
 }
 
-// One launch per segment keeps every warp on one code path.  FIRST_ORDER
-// reads cell states directly (the reference's reconstruction is the identity
-// there: zero gradients, unit factors).
+// One flux face of segment SEG (face f of the flux-face list, `begin` the
+// segment's first face).  FIRST_ORDER reads cell states directly (the
+// reference's reconstruction is the identity there: zero gradients, unit
+// factors).
 template <int FLUX, int SEG, bool FIRST_ORDER, bool KERNEL_HLLC>
-__global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __restrict__ P,
-                                                 const double* __restrict__ recon,
-                                                 double* __restrict__ flux, double gamma,
-                                                 double inv_gm1) {
-  const int begin = g.seg_begin[SEG], end = g.seg_begin[SEG + 1];
-  // grid-stride: the autotuner may give each thread several faces
-  for (int f = begin + blockIdx.x * blockDim.x + threadIdx.x; f < end; f += gridDim.x * blockDim.x) {
+__device__ __forceinline__ void flux_face(const DevGeom& g, const double* P, const double* recon, double* flux,
+                                          double gamma, double inv_gm1, int f, int begin) {
   const double2 n = g.ff_normal[f];
   const St4 L = FIRST_ORDER ? ld4(P + 4 * (size_t)g.ff_lcell[f]) : ld4(recon + 4 * (size_t)g.ff_lslot[f]);
   St4 R;
@@ -516,7 +516,18 @@ __global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __rest
   bits |= numerical_flux<FLUX, (SEG == SEG_INTERIOR) && KERNEL_HLLC>(L, R, n.x, n.y, gamma, inv_gm1, out);
   if (bits) flag_face(g.status, bits, f);
   st4(flux + 4 * (size_t)f, St4{out[0], out[1], out[2], out[3]});
-  }
+}
+
+// One launch per segment keeps every warp on one code path.
+template <int FLUX, int SEG, bool FIRST_ORDER, bool KERNEL_HLLC>
+__global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __restrict__ P,
+                                                 const double* __restrict__ recon,
+                                                 double* __restrict__ flux, double gamma,
+                                                 double inv_gm1) {
+  const int begin = g.seg_begin[SEG], end = g.seg_begin[SEG + 1];
+  // grid-stride: the autotuner may give each thread several faces
+  for (int f = begin + blockIdx.x * blockDim.x + threadIdx.x; f < end; f += gridDim.x * blockDim.x)
+    flux_face<FLUX, SEG, FIRST_ORDER, KERNEL_HLLC>(g, P, recon, flux, gamma, inv_gm1, f, begin);
 }
 
 // ------------------------------------------------------------ gather + stage
@@ -534,12 +545,11 @@ __device__ __forceinline__ double stage_dt(const StageProgram& prog, int c) {
 // EXTRAS compiles the viscous residual and body-force adds in.
 enum GatherShape { SHAPE_GENERIC = 0, SHAPE_EULER = 1, SHAPE_X_XDTR = 2 };
 
+// Cell at visiting position i: divergence, boundary adds, extras, finiteness
+// check, stage combination and primitive recovery of the new state.
 template <int SHAPE, bool EXTRAS>
-__global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
-                                                   const double* __restrict__ flux, double gamma,
-                                                   double ax, double ay, StageProgram prog) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g.n_cells) return;
+__device__ __forceinline__ void gather_cell(const DevGeom& g, const double* P, const double* flux, double gamma,
+                                            double ax, double ay, const StageProgram& prog, int i) {
   const int c = g.cell_order[i];
   // interior divergence: SciPy CSR product, ascending face order
   // (solver.py:2160-2174, 2501); derivative starts from zero.
@@ -637,6 +647,75 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __re
     if (!ok) flag_cell(g.status, MCFD_S_NONPHYSICAL_STATE, c);
     st4(prog.out_p + 4 * (size_t)c, q);
   }
+}
+
+template <int SHAPE, bool EXTRAS>
+__global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
+                                                   const double* __restrict__ flux, double gamma,
+                                                   double ax, double ay, StageProgram prog) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < g.n_cells) gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i);
+}
+
+// ------------------------------------------------------ one launch per stage
+//
+// The three phases of an explicit stage — reconstruction, face fluxes,
+// gather with the stage update — in one cooperative launch of one grid (as
+// many resident blocks as the SMs hold), separated by grid barriers.  Each
+// phase is a grid-stride loop over the items of its own kernel and runs the
+// same per-item code (reconstruct_variable_fast / reconstruct_cell_fast,
+// flux_face per segment, gather_cell), so the results are those of the
+// three-launch stage bit for bit.  Built for the smallest-ratio variant with
+// HLLC and MUSCL-linear reconstruction (one of the four capped limiters), inviscid,
+// without pressure-inlet / mass-flow patches or a body force, and the Euler
+// and x0 + (x1 + dt r) stage shapes; launch_stage_fused refuses the rest.
+// No restrict qualifiers: the gather phase writes the primitive array that
+// the first two phases read.
+#ifndef MCFD_FUSED_MIN_BLOCKS
+#define MCFD_FUSED_MIN_BLOCKS 3
+#endif
+
+template <int FLUX, int SEG>
+__device__ __forceinline__ void flux_phase(const DevGeom& g, const double* P, const double* recon, double* flux,
+                                           double gamma, double inv_gm1, int tid, int stride) {
+  const int begin = g.seg_begin[SEG], end = g.seg_begin[SEG + 1];
+  for (int f = begin + tid; f < end; f += stride)
+    flux_face<FLUX, SEG, false, true>(g, P, recon, flux, gamma, inv_gm1, f, begin);
+}
+
+// Cells with other than 3 or 4 limiter entries (polygons): out of line, so
+// that their larger register demand stays in this rarely taken call.
+template <int LIMITER>
+__device__ __noinline__ void reconstruct_cell_any(const DevGeom& g, const double* P, double* recon, int c) {
+  reconstruct_cell_fast<LIMITER, 0>(g, P, recon, c, ld4(P + 4 * (size_t)c), g.lim_ptr[c], g.lim_ptr[c + 1]);
+}
+
+template <int LIMITER, int FLUX, int SHAPE>
+__global__ void __launch_bounds__(kBlock, MCFD_FUSED_MIN_BLOCKS) k_stage_fused(DevGeom g, const double* P,
+                                                                               double* recon, double* flux,
+                                                                               double gamma, double inv_gm1,
+                                                                               StageProgram prog) {
+  cg::grid_group grid = cg::this_grid();
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;  // a multiple of 4: t & 3 is the variable
+  const int n4 = 4 * g.n_lim34;
+  for (int t = tid; t < n4; t += stride) {
+    const int c = g.cell_order[t >> 2], v = t & 3;
+    const double pv = P[4 * (size_t)c + v];
+    const int s0 = g.lim_ptr[c];
+    if (g.lim_ptr[c + 1] - s0 == 3) reconstruct_variable_fast<LIMITER, 3>(g, P, recon, c, v, pv, s0);
+    else reconstruct_variable_fast<LIMITER, 4>(g, P, recon, c, v, pv, s0);
+  }
+  for (int i = g.n_lim34 + tid; i < g.n_cells; i += stride) reconstruct_cell_any<LIMITER>(g, P, recon, g.cell_order[i]);
+  grid.sync();
+  flux_phase<FLUX, SEG_INTERIOR>(g, P, recon, flux, gamma, inv_gm1, tid, stride);
+  flux_phase<FLUX, SEG_PERIODIC>(g, P, recon, flux, gamma, inv_gm1, tid, stride);
+  flux_phase<FLUX, SEG_WALL>(g, P, recon, flux, gamma, inv_gm1, tid, stride);
+  flux_phase<FLUX, SEG_VIN>(g, P, recon, flux, gamma, inv_gm1, tid, stride);
+  flux_phase<FLUX, SEG_POUT>(g, P, recon, flux, gamma, inv_gm1, tid, stride);
+  flux_phase<FLUX, SEG_FAR>(g, P, recon, flux, gamma, inv_gm1, tid, stride);
+  grid.sync();
+  for (int i = tid; i < g.n_cells; i += stride) gather_cell<SHAPE, false>(g, P, flux, gamma, 0.0, 0.0, prog, i);
 }
 
 // --------------------------------------------------------------- time steps
@@ -867,6 +946,71 @@ cudaError_t launch_time_steps(const DevGeom& g, const mcfd_config& cfg, const do
   return cudaGetLastError();
 }
 
+
+// Stage shape of a program (SHAPE_GENERIC when neither special shape fits).
+static int stage_shape(const StageProgram& prog) {
+  if (prog.out_u && prog.n_terms == 2 && prog.t[0].kind == TERM_X) {
+    if (prog.t[1].kind == TERM_DTR && prog.t[0].coef == 1.0 && prog.t[1].coef == 1.0) return SHAPE_EULER;
+    if (prog.t[1].kind == TERM_X_PLUS_DTR) return SHAPE_X_XDTR;
+  }
+  return SHAPE_GENERIC;
+}
+
+bool stage_fused_supported(const DevGeom& g, const mcfd_config& cfg, const StageProgram& prog) {
+  if constexpr (!kMinRatio) return false;
+  return cfg.flux == MCFD_FLUX_HLLC && cfg.reconstruction == MCFD_RECON_MUSCL_LINEAR && cfg.limiter >= 0 &&
+         cfg.limiter <= 3 &&
+         cfg.viscosity_model == MCFD_VISC_INVISCID && g.n_bc_patches == 0 && g.n_cells > 0 &&
+         cfg.acceleration_x == 0.0 && cfg.acceleration_y == 0.0 && !prog.visc_r && prog.out_u &&
+         stage_shape(prog) != SHAPE_GENERIC;
+}
+
+template <int LIMITER, int FLUX, int SHAPE>
+static cudaError_t launch_fused_as(const DevGeom& g, const mcfd_config& cfg, const double* P, double* recon,
+                                   double* flux, const StageProgram& prog, cudaStream_t s, int* blocks_out) {
+  auto kernel = k_stage_fused<LIMITER, FLUX, SHAPE>;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
+  if (blocks_out) *blocks_out = per_sm;
+  cudaLaunchConfig_t lc{};
+  lc.gridDim = dim3(sms * per_sm);
+  lc.blockDim = dim3(kBlock);
+  lc.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  count_launch();
+  return cudaLaunchKernelEx(&lc, kernel, g, P, recon, flux, cfg.gamma, 1.0 / (cfg.gamma - 1.0), prog);
+}
+
+template <int LIMITER, int FLUX>
+static cudaError_t launch_fused_shape(const DevGeom& g, const mcfd_config& cfg, const double* P, double* recon,
+                                      double* flux, const StageProgram& prog, cudaStream_t s, int* blocks) {
+  if (stage_shape(prog) == SHAPE_EULER)
+    return launch_fused_as<LIMITER, FLUX, SHAPE_EULER>(g, cfg, P, recon, flux, prog, s, blocks);
+  return launch_fused_as<LIMITER, FLUX, SHAPE_X_XDTR>(g, cfg, P, recon, flux, prog, s, blocks);
+}
+
+
+cudaError_t launch_stage_fused(const DevGeom& g, const mcfd_config& cfg, const double* P, double* recon,
+                               double* flux, const StageProgram& prog, cudaStream_t s, int* blocks_per_sm) {
+  if (!stage_fused_supported(g, cfg, prog)) return cudaErrorNotSupported;
+  if constexpr (kMinRatio) {
+    switch (cfg.limiter) {
+      case 0: return launch_fused_shape<0, MCFD_FLUX_HLLC>(g, cfg, P, recon, flux, prog, s, blocks_per_sm);
+      case 1: return launch_fused_shape<1, MCFD_FLUX_HLLC>(g, cfg, P, recon, flux, prog, s, blocks_per_sm);
+      case 2: return launch_fused_shape<2, MCFD_FLUX_HLLC>(g, cfg, P, recon, flux, prog, s, blocks_per_sm);
+      default: return launch_fused_shape<3, MCFD_FLUX_HLLC>(g, cfg, P, recon, flux, prog, s, blocks_per_sm);
+    }
+  }
+  return cudaErrorNotSupported;
+}
 
 }  // namespace MCFD_VARIANT
 }  // namespace mcfd

@@ -255,6 +255,17 @@ class DeviceGeometry:
         return {"reconstruct_threads": chosen[0], "flux_threads": chosen[1], "flux_faces_per_thread": chosen[2],
                 "gather_threads": chosen[3], "reconstruct_per_variable": chosen[4]}
 
+    def set_fused_stage(self, on: bool) -> None:
+        """Run each explicit stage as one cooperative launch (reconstruction,
+        fluxes and gather separated by grid barriers) where the settings allow
+        it (mcfd_set_fused_stage); results are identical either way."""
+        self.lib.check(self.lib.mcfd_set_fused_stage(self.handle, 1 if on else 0), "mcfd_set_fused_stage")
+
+    @property
+    def fused_stage_blocks(self) -> int:
+        """Resident blocks per SM of the last one-launch stage (0 before any)."""
+        return int(self.lib.mcfd_fused_stage_blocks(self.handle))
+
     def primitive_buffer(self) -> torch.Tensor:
         """The handle's primitive buffer as a tensor view (valid after a
         residual / primitive / step call)."""
