@@ -75,6 +75,11 @@ def parse(argv=None):
                     help="bump workload: wall-clock budget of the implicit step (checked between GMRES calls)")
     ap.add_argument("--bump-size", default="512x256")
     ap.add_argument("--bump-steps", type=int, default=1)
+    ap.add_argument("--bump-until-drop", type=float, default=0.0,
+                    help="bump workload: stop once the density residual has fallen by this factor (1e-8 for the "
+                         "configuration's 8 orders); progress lines go to stderr and --bump-log")
+    ap.add_argument("--bump-log", default="",
+                    help="bump workload: file rewritten with the line so far after every step")
     ap.add_argument("--bump-oracle", action="store_true",
                     help="bump workload: also run the oracle's SciPy restatement of the same step and compare")
     ap.add_argument("--numbering", choices=("generator", "random", "rcm"), default="generator",
@@ -1019,6 +1024,13 @@ def run_bump(args):
                           "ms_per_gmres_iteration": 1e3 * (stepper.gmres_seconds - counts0[4]) / max(gi, 1),
                           "mean_cfl_used": float(s.cfl * float(used.mean()) / float(dt.mean())),
                           "density_residual": r, "drop": r / r0})
+            print(json.dumps(steps[-1]), file=sys.stderr, flush=True)
+            if args.bump_log:
+                Path(args.bump_log).write_text(json.dumps({"elapsed_s": time.perf_counter() - start,
+                                                           "per_step": steps}) + "\n")
+            if args.bump_until_drop > 0 and r / r0 <= args.bump_until_drop:
+                status = f"density residual fell by {args.bump_until_drop:g} after {k + 1} steps"
+                break
     launches = _launches() - before
     vs_oracle = cpu = None
     if args.bump_oracle and first_state is not None:

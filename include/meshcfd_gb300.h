@@ -64,6 +64,9 @@ extern "C" {
 #define MCFD_S_VISC_TEMPERATURE 0x20000   /* solver.py:3620-3621 */
 #define MCFD_S_VISC_SUTHERLAND 0x40000    /* solver.py:2734-2735 */
 #define MCFD_S_VISC_DISTANCE 0x80000      /* solver.py:3944-3945 */
+/* No counterpart in the reference: an LU-SGS sweep of the implicit path waited
+ * past its bound for a row it depends on and stopped (its output is invalid). */
+#define MCFD_S_SWEEP_TIMEOUT 0x100000
 
 typedef struct mcfd_status {
   int32_t code;       /* OR of MCFD_S_* bits since the last fetch */
@@ -397,14 +400,23 @@ int mcfd_wall_force(mcfd_geom* geom, const mcfd_config* cfg, const double* U, do
  * triangular solves' (rows summed in ascending column order). */
 int mcfd_lusgs_apply(mcfd_geom* geom, const double* v, double* x, void* stream);
 /* Launch schedule of the LU-SGS sweeps: runs of levels at most wide_level
- * rows wide go to one launch that steps through them with a barrier per
- * level, swept by one block (cluster = 1) or a thread-block cluster of 8 or
- * 16 blocks sharing their latest solutions in distributed shared memory;
- * wider levels get a grid launch each.  0 restores the defaults (16384, one
- * block); 8 or 16 returns MCFD_E_UNSUPPORTED where the device cannot run
- * that cluster size.  Results do not depend on it.  No counterpart in the
+ * rows wide go to one launch, wider levels get a grid launch each.  engine
+ * chooses how such a run is swept: 1 one block with a barrier per level;
+ * 2, 3, 4: one block of 512, 1024 or 256 threads whose rows wait only for
+ * the rows they read (no barrier per level, chunks of consecutive levels in
+ * flight together); 5: as 2 with the rows' products on the integer pipe
+ * (the same IEEE products); 8 or 16 a
+ * thread-block cluster of that many blocks sharing their latest solutions in
+ * distributed shared memory, a cluster barrier per level.  0 restores the
+ * defaults (wide_level 16384, engine 2); 8 or 16 returns MCFD_E_UNSUPPORTED
+ * where the device cannot run that cluster size.  Results do not depend on
+ * it.  No counterpart in the reference. */
+int mcfd_implicit_set_sweep(mcfd_geom* geom, int32_t wide_level, int32_t engine);
+/* Rows per chunk of the per-row-wait sweeps (engines 2-4): 1..32, 0 restores
+ * the default (32).  A chunk is a run of consecutive rows of one level taken
+ * by one warp.  Results do not depend on it.  No counterpart in the
  * reference. */
-int mcfd_implicit_set_sweep(mcfd_geom* geom, int32_t wide_level, int32_t cluster);
+int mcfd_implicit_set_chunk(mcfd_geom* geom, int32_t rows);
 /* Solve operator(x) = b with restarted GMRES(krylov_dim) preconditioned by
  * LU-SGS, as _solve_gmres drives SciPy's gmres (solver.py:1489-1529; left
  * preconditioning, modified Gram-Schmidt, Givens rotations).  b, x: device

@@ -113,6 +113,7 @@ SIGNATURES = {
     "mcfd_set_fused_stage": (c_i32, [c_vp, c_i32]),
     "mcfd_fused_stage_blocks": (c_i32, [c_vp]),
     "mcfd_implicit_set_sweep": (c_i32, [c_vp, c_i32, c_i32]),
+    "mcfd_implicit_set_chunk": (c_i32, [c_vp, c_i32]),
     "mcfd_jvp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp]),
     "mcfd_vjp": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp]),
     "mcfd_wall_force": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_dbl, c_dbl, P_dbl, c_vp, c_vp]),

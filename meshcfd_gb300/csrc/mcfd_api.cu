@@ -1188,6 +1188,7 @@ static int ensure_implicit(mcfd_geom* h) {
     implicit_free(h->imp);
     return MCFD_E_CUDA;
   }
+  h->imp.status = h->status;
   h->imp_built = true;
   return MCFD_OK;
 }
@@ -1353,18 +1354,26 @@ int mcfd_jvp(mcfd_geom* h, const mcfd_config* cfg, const double* U, const double
   return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return launch_jvp(h->g, *cfg, U, dU, h->jvp, dR, s); }));
 }
 
+int mcfd_implicit_set_chunk(mcfd_geom* h, int32_t rows) {
+  if (!h || rows < 0 || rows > 32) return MCFD_E_ARG;
+  int c = ensure_implicit(h);
+  if (c) return c;
+  return rc(implicit_set_chunk(h->imp, rows));
+}
+
 int mcfd_lusgs_apply(mcfd_geom* h, const double* v, double* x, void* stream) {
   if (!h || !v || !x || !h->imp_built || !h->imp.prepared) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   return rc(timed(h, MCFD_PROF_OTHER, s, [&] { return lusgs_apply(h->imp, v, x, s); }));
 }
 
-int mcfd_implicit_set_sweep(mcfd_geom* h, int32_t wide_level, int32_t cluster) {
-  if (!h || wide_level < 0 || (cluster != 0 && cluster != 1 && cluster != 8 && cluster != 16)) return MCFD_E_ARG;
+int mcfd_implicit_set_sweep(mcfd_geom* h, int32_t wide_level, int32_t engine) {
+  if (!h || wide_level < 0 || (engine < 0 || (engine > 5 && engine != 8 && engine != 16)))
+    return MCFD_E_ARG;
   int c = ensure_implicit(h);
   if (c) return c;
-  if ((cluster == 8 && !h->imp.cluster8_ok) || (cluster == 16 && !h->imp.cluster16_ok)) return MCFD_E_UNSUPPORTED;
-  implicit_set_wide_level(h->imp, wide_level, cluster ? cluster : 1);
+  if ((engine == 8 && !h->imp.cluster8_ok) || (engine == 16 && !h->imp.cluster16_ok)) return MCFD_E_UNSUPPORTED;
+  implicit_set_wide_level(h->imp, wide_level, engine);
   return MCFD_OK;
 }
 

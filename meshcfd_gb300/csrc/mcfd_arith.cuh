@@ -166,13 +166,13 @@ MCFD_IA_FN u64 round_q55(u64 q, bool inexact_tail, int& e) {
   return m >> carry;
 }
 
-MCFD_IA_FN double div_rn(double a, double b) {
-  const u64 ia = bits(a), ib = bits(b);
-  const unsigned ea = (unsigned)(ia >> 52) & 0x7ffu, eb = (unsigned)(ib >> 52) & 0x7ffu;
-  const u64 ma = (ia & kMant) | kImpl, mb = (ib & kMant) | kImpl;
-  const unsigned sh = ma < mb ? 1u : 0u;
-  const u64 A = ma << sh;  // A / mb in [1, 2)
-  int e = (int)ea - (int)eb + 1023 - (int)sh;
+// The fixed-point reciprocal X ~ 2^116 / mb of the divisor's 53-bit
+// significand mb that div_rn divides with: the fp32 seed refined by two
+// Newton steps.  It depends on b alone, so quotients by one divisor can share
+// it (div_rn_recip); for zero, subnormal or non-finite b it is unused (those
+// divisions take the FP64 unit).
+MCFD_IA_FN u64 recip_fixed(double b) {
+  const u64 mb = (bits(b) & kMant) | kImpl;
   // seed: x32 ~ 2^87 / (mb >> 29) ~ 2^84 / mb (the float conversion is exact)
   const unsigned x32 = to_u32(rcp_seed((float)(unsigned)(mb >> 29)) * 0x1p55f);
   // Newton step 1 on X = x32 2^32 (~2^116 / mb): D = 2^84 - mb x32 (mod 2^64,
@@ -190,6 +190,17 @@ MCFD_IA_FN double div_rn(double a, double b) {
     h = mulhi(X, ad) >> 20;
     X = D < 0 ? X - h : X + h;
   }
+  return X;
+}
+
+// a / b given X = recip_fixed(b): the same bits as div_rn(a, b).
+MCFD_IA_FN double div_rn_recip(double a, double b, u64 X) {
+  const u64 ia = bits(a), ib = bits(b);
+  const unsigned ea = (unsigned)(ia >> 52) & 0x7ffu, eb = (unsigned)(ib >> 52) & 0x7ffu;
+  const u64 ma = (ia & kMant) | kImpl, mb = (ib & kMant) | kImpl;
+  const unsigned sh = ma < mb ? 1u : 0u;
+  const u64 A = ma << sh;  // A / mb in [1, 2)
+  int e = (int)ea - (int)eb + 1023 - (int)sh;
   // Q = floor(A 2^54 / mb) in [2^54, 2^55), corrected by the exact remainder
   u64 Q = (mulhi(A, X) << 2) | ((A * X) >> 62);
   long long R = (long long)((A << 54) - Q * mb);
@@ -211,6 +222,8 @@ MCFD_IA_FN double div_rn(double a, double b) {
     return div_fp64(a, b);
   return from_bits(a_zero ? ((ia ^ ib) & kSign) : (((ia ^ ib) & kSign) | ((u64)e << 52) | (m & kMant)));
 }
+
+MCFD_IA_FN double div_rn(double a, double b) { return div_rn_recip(a, b, recip_fixed(b)); }
 
 // a * b, round to nearest even, in 32-bit words.  With the significands
 // split as a = a1 2^32 + a0 (a1 21 bits), the 106-bit product is summed by
@@ -324,6 +337,8 @@ MCFD_IA_FN double plus_zero(double x) { return bits(x) == kSign ? 0.0 : x; }
 
 using ia::abs_of;
 using ia::div_rn;
+using ia::div_rn_recip;
+using ia::recip_fixed;
 using ia::mul_rn;
 using ia::negate;
 using ia::plus_zero;

@@ -94,9 +94,10 @@ __device__ __forceinline__ bool finite4(const St4& s) {
 // euler.conservative_to_primitive (euler.py:20-40), one row.
 __device__ __forceinline__ St4 cons_to_prim(const St4& U, double gamma, bool* ok) {
   double rho = U.a;
-  double ux = div_rn(U.b, rho);
-  double uy = div_rn(U.c, rho);
-  double p = (gamma - 1.0) * (U.d - div_rn(0.5 * (U.b * U.b + U.c * U.c), rho));
+  const unsigned long long rx = recip_fixed(rho);  // the three quotients share the divisor
+  double ux = div_rn_recip(U.b, rho, rx);
+  double uy = div_rn_recip(U.c, rho, rx);
+  double p = (gamma - 1.0) * (U.d - div_rn_recip(0.5 * (U.b * U.b + U.c * U.c), rho, rx));
   St4 P{rho, ux, uy, p};
   *ok = finite4(P) && icmp::gt0(rho) && icmp::gt0(p);
   return P;

@@ -16,6 +16,7 @@
 //   (_solve_gmres, solver.py:1489-1529): left preconditioning, modified
 //   Gram-Schmidt, Givens rotations, SciPy's inner/outer tolerance control.
 // Vector reductions are deterministic two-level trees.
+#include <climits>
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -128,6 +129,7 @@ constexpr int kClusterThreads = 256;
 constexpr int kRing = 4096;        // latest solved rows kept in shared memory (128 KiB)
 constexpr int kWideLevel = 16384;  // wider levels get a grid launch each
 constexpr int kPortableCluster = 8;  // the portable cluster size of the cluster sweep
+constexpr int kDefaultEngine = kSweepDataflow;
 constexpr size_t kRingBytes = kRing * 4 * sizeof(double);
 
 // Everything of a row that does not depend on the solution: loaded for the
@@ -137,10 +139,14 @@ struct SweepRow {
   int i, n;
   St4 r;
   double dg;
+  unsigned long long rx;  // recip_fixed(dg): the four quotients share the divisor's reciprocal
   double v[kSweepPack];
   int cp[kSweepPack], cc[kSweepPack];
 };
 
+// IM (integer products): the products of the row run on the integer pipe
+// (mul_rn, the same IEEE result), which takes them off the FP64 pipe.
+template <bool IM = false>
 __device__ __forceinline__ void sweep_load(const SweepDev& a, int p, SweepRow& R) {
   R.i = a.pos_cell[p];
   R.n = a.pk_cnt[p];
@@ -151,26 +157,37 @@ __device__ __forceinline__ void sweep_load(const SweepDev& a, int p, SweepRow& R
     R.cc[k] = a.pk_cell[(size_t)p * kSweepPack + k];
   }
   R.dg = a.pk_diag[p];
+  R.rx = recip_fixed(R.dg);
   const St4 r = ld4(a.in + 4 * (size_t)R.i);
   if (a.backward) {
     const double dc = a.pk_dc[p];
-    R.r = St4{dc * r.a, dc * r.b, dc * r.c, dc * r.d};
+    if constexpr (IM) R.r = St4{mul_rn(dc, r.a), mul_rn(dc, r.b), mul_rn(dc, r.c), mul_rn(dc, r.d)};
+    else R.r = St4{dc * r.a, dc * r.b, dc * r.c, dc * r.d};
   } else {
     R.r = r;
   }
 }
 
+template <bool IM = false>
 __device__ __forceinline__ void sweep_sub(double acc[4], double v, const St4& x) {
-  acc[0] = acc[0] - v * x.a;
-  acc[1] = acc[1] - v * x.b;
-  acc[2] = acc[2] - v * x.c;
-  acc[3] = acc[3] - v * x.d;
+  if constexpr (IM) {
+    acc[0] = acc[0] - mul_rn(v, x.a);
+    acc[1] = acc[1] - mul_rn(v, x.b);
+    acc[2] = acc[2] - mul_rn(v, x.c);
+    acc[3] = acc[3] - mul_rn(v, x.d);
+  } else {
+    acc[0] = acc[0] - v * x.a;
+    acc[1] = acc[1] - v * x.b;
+    acc[2] = acc[2] - v * x.c;
+    acc[3] = acc[3] - v * x.d;
+  }
 }
 
 // x_p = (r - sum_j a_j x_j) / d over the row's entries in ascending column
 // order; earlier solutions from the ring when their position is at least
 // ring_lo, else from global memory.  Writes the global solution and, when
 // ring is given, the ring slot of position p.
+template <bool IM = false>
 __device__ __forceinline__ void sweep_solve(const SweepDev& a, const SweepRow& R, int p, const double* ring,
                                             int ring_lo, double* ring_out) {
   double acc[4] = {R.r.a, R.r.b, R.r.c, R.r.d};
@@ -184,7 +201,7 @@ __device__ __forceinline__ void sweep_solve(const SweepDev& a, const SweepRow& R
       } else {
         x = ld4(a.out + 4 * (size_t)R.cc[k]);
       }
-      sweep_sub(acc, R.v[k], x);
+      sweep_sub<IM>(acc, R.v[k], x);
     }
   }
   if (R.n > kSweepPack) {  // the rest of a long row from the CSR
@@ -197,10 +214,11 @@ __device__ __forceinline__ void sweep_solve(const SweepDev& a, const SweepRow& R
       } else {
         x = ld4(a.out + 4 * (size_t)a.ent_cell[j]);
       }
-      sweep_sub(acc, a.rval[a.ent_val[j]], x);
+      sweep_sub<IM>(acc, a.rval[a.ent_val[j]], x);
     }
   }
-  const St4 res{div_rn(acc[0], R.dg), div_rn(acc[1], R.dg), div_rn(acc[2], R.dg), div_rn(acc[3], R.dg)};
+  const St4 res{div_rn_recip(acc[0], R.dg, R.rx), div_rn_recip(acc[1], R.dg, R.rx),
+                div_rn_recip(acc[2], R.dg, R.rx), div_rn_recip(acc[3], R.dg, R.rx)};
   st4(a.out + 4 * (size_t)R.i, res);
   if (ring_out) {
     double* q = ring_out + 4 * (p & (kRing - 1));
@@ -303,7 +321,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_lusgs_cluster(SweepDev a
         sweep_sub(acc, a.rval[a.ent_val[j]], x);
       }
     }
-    const St4 res{div_rn(acc[0], W.dg), div_rn(acc[1], W.dg), div_rn(acc[2], W.dg), div_rn(acc[3], W.dg)};
+    const St4 res{div_rn_recip(acc[0], W.dg, W.rx), div_rn_recip(acc[1], W.dg, W.rx),
+                  div_rn_recip(acc[2], W.dg, W.rx), div_rn_recip(acc[3], W.dg, W.rx)};
     st4(a.out + 4 * (size_t)W.i, res);
     const int slot = 4 * (p & (kRing - 1));
 #pragma unroll
@@ -330,6 +349,113 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_lusgs_cluster(SweepDev a
       if (have) sweep_load(a, b + first, R);
     }
     cluster.sync();
+  }
+}
+
+// The same sweep in one block without a barrier per level: the rows are cut
+// into chunks of at most 32 (by default) consecutive positions inside one
+// level, chunk k
+// goes to warp k mod kFlowWarps, and each warp works through its chunks in
+// order.  A row waits only for the rows it reads: every solved row writes its
+// solution into a shared-memory ring of kFlowRing positions and then the
+// position into the slot's tag; a reader spins (bounded) until the tag of
+// each earlier position it needs equals that position.  A warp starts a
+// chunk only when every position more than kFlowAhead before its first row
+// is solved (each warp publishes the first position of its current chunk),
+// which (i) keeps a ring slot from being overwritten while a reader may still
+// need it (a position is read from the ring only within 2048 positions, and
+// the writer of that slot's next position waits for the reader's chunk) and
+// (ii) makes every older position readable from global memory.  So narrow
+// levels no longer wait for the whole previous level, and chunks of
+// consecutive levels are in flight at once.  The oldest unfinished chunk can
+// always proceed (its rows depend on earlier levels only, all solved), so
+// the waits end; each one is bounded anyway, after which the block flags
+// MCFD_S_SWEEP_TIMEOUT and every warp stops.  The arithmetic of each row is
+// sweep_solve's, so the results equal the other schedules' bit for bit.
+constexpr int kFlowRing = 4096;  // positions
+constexpr int kFlowAhead = 2016;  // positions below start - kFlowAhead are solved when a chunk starts
+constexpr int kFlowRingWindow = kFlowRing - kFlowAhead - 32;  // ring reads within this distance
+constexpr long long kFlowSpinLimit = 1LL << 22;
+constexpr int kFlowChunk = 32;  // default rows per chunk
+constexpr size_t kFlowSmemBytes = kFlowRing * (4 * sizeof(double) + sizeof(int));
+static_assert(kFlowRing >= 2 * kFlowAhead + 32, "ring reads must fall inside the guaranteed window");
+
+template <int NT, bool IM>
+__global__ void __launch_bounds__(NT, 1) k_lusgs_dataflow(SweepDev a, const int2* __restrict__ chunks, int k0, int k1,
+                                                          DevStatus* status) {
+  constexpr int kFlowWarps = NT / 32;
+  extern __shared__ double flow_smem[];
+  double* ring = flow_smem;                                      // [kFlowRing][4]
+  volatile int* tag = reinterpret_cast<volatile int*>(ring + 4 * kFlowRing);  // [kFlowRing]
+  __shared__ int prog[kFlowWarps];  // first position of each warp's current chunk (INT_MAX: none left)
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < kFlowRing; i += blockDim.x) tag[i] = -1;
+  if (lane == 0) prog[warp] = k0 + warp < k1 ? chunks[k0 + warp].x : INT_MAX;
+  if (threadIdx.x == 0) abort_flag = 0;
+  __syncthreads();
+  volatile int* vprog = prog;
+  volatile int* vabort = &abort_flag;
+  const int base = chunks[k0].x;  // positions below were solved by earlier launches
+  for (int k = k0 + warp; k < k1; k += kFlowWarps) {
+    const int2 ch = chunks[k];
+    const int start = ch.x;
+    const bool have = lane < ch.y;
+    const int p = start + lane;
+    SweepRow R;
+    if (have) sweep_load<IM>(a, p, R);
+    // throttle: every position below start - kFlowAhead solved
+    if (start - kFlowAhead > base) {  // warp-uniform loop: every exit is decided by the whole warp
+      long long spins = 0;
+      while (true) {
+        const int v = lane < kFlowWarps ? vprog[lane] : INT_MAX;
+        if (__reduce_min_sync(0xffffffffu, v) >= start - kFlowAhead) break;
+        if (__any_sync(0xffffffffu, ++spins > kFlowSpinLimit || *vabort)) {
+          if (lane == 0) *vabort = 1;
+          break;
+        }
+      }
+    }
+    if (__any_sync(0xffffffffu, *vabort)) break;
+    const int ring_lo = max(start - kFlowRingWindow, base);
+    bool ok = true;
+    if (have) {
+      // wait for the tags of the ring-resident positions this row reads
+      auto wait_tag = [&](int cp) {
+        if (cp < ring_lo) return;
+        long long spins = 0;
+        while (tag[cp & (kFlowRing - 1)] != cp) {
+          if (++spins > kFlowSpinLimit || *vabort) {
+            ok = false;
+            return;
+          }
+        }
+      };
+#pragma unroll
+      for (int q = 0; q < kSweepPack; ++q)
+        if (q < R.n && ok) wait_tag(R.cp[q]);
+      if (R.n > kSweepPack)
+        for (int j = a.ent_ptr[p] + kSweepPack, j1 = a.ent_ptr[p + 1]; j < j1 && ok; ++j) wait_tag(a.ent_pos[j]);
+    }
+    if (__any_sync(0xffffffffu, !ok)) {
+      if (lane == 0) *vabort = 1;
+      break;
+    }
+    __threadfence_block();  // the solutions behind the tags seen above
+    if (have) {
+      sweep_solve<IM>(a, R, p, ring, ring_lo, ring);
+      __threadfence_block();
+      tag[p & (kFlowRing - 1)] = p;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      vprog[warp] = k + kFlowWarps < k1 ? chunks[k + kFlowWarps].x : INT_MAX;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && abort_flag) {
+    atomicOr(&status->code, MCFD_S_SWEEP_TIMEOUT);
   }
 }
 
@@ -772,12 +898,34 @@ static void sweep_schedule(SweepPlan& pl, int wide) {
   }
 }
 
-void implicit_set_wide_level(ImplicitState& st, int wide, int cluster) {
+void implicit_set_wide_level(ImplicitState& st, int wide, int engine) {
   st.wide_level = wide > 0 ? wide : kWideLevel;
-  st.cluster = cluster;
+  st.engine = engine > 0 ? engine : kDefaultEngine;
   sweep_schedule(st.fwd, st.wide_level);
   sweep_schedule(st.bwd, st.wide_level);
   st.inner_key = -1;  // the captured loop holds the old launches
+}
+
+// The dataflow sweep's chunks: runs of at most `rows` consecutive positions
+// inside one level (rows <= 32, one warp).
+static cudaError_t sweep_chunks(SweepPlan& pl, int rows) {
+  const std::vector<int>& lp = pl.host_level_ptr;
+  std::vector<int2> ch;
+  pl.host_chunk_ptr.assign(lp.size(), 0);
+  for (size_t l = 0; l + 1 < lp.size(); ++l) {
+    pl.host_chunk_ptr[l] = (int)ch.size();
+    for (int p = lp[l]; p < lp[l + 1]; p += rows) ch.push_back(make_int2(p, std::min(rows, lp[l + 1] - p)));
+  }
+  pl.host_chunk_ptr.back() = (int)ch.size();
+  return ch.empty() ? cudaSuccess : cudaMemcpy(pl.chunks, ch.data(), ch.size() * sizeof(int2), cudaMemcpyHostToDevice);
+}
+
+cudaError_t implicit_set_chunk(ImplicitState& st, int rows) {
+  const int r = rows > 0 ? rows : kFlowChunk;
+  cudaError_t e = sweep_chunks(st.fwd, r);
+  if (e == cudaSuccess) e = sweep_chunks(st.bwd, r);
+  st.inner_key = -1;  // the captured loop holds the old chunk ranges
+  return e;
 }
 
 cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
@@ -955,6 +1103,11 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   st.bwd.n_levels = st.n_levels_bwd;
   st.fwd.host_level_ptr = hf.level_ptr;
   st.bwd.host_level_ptr = hb.level_ptr;
+  for (SweepPlan* pl : {&st.fwd, &st.bwd}) {  // room for chunks of one row
+    if (e == cudaSuccess) e = cudaMalloc((void**)&pl->chunks, (size_t)std::max(C, 1) * sizeof(int2));
+    if (e == cudaSuccess) st.owned.push_back(pl->chunks);
+    if (e == cudaSuccess) e = sweep_chunks(*pl, kFlowChunk);
+  }
   st.wide_level = kWideLevel;
   sweep_schedule(st.fwd, st.wide_level);
   sweep_schedule(st.bwd, st.wide_level);
@@ -996,7 +1149,15 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   // cluster of 16 (the cluster barrier and the remote ring stores cost more
   // than the FP64 work they spread).  The cluster sweeps stay selectable
   // where the device can run them (8: portable; 16: non-portable).
-  st.cluster = 1;
+  st.engine = kDefaultEngine;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kFlowSmemBytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kFlowSmemBytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kFlowSmemBytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kFlowSmemBytes);
   st.cluster8_ok = false;
   if (e == cudaSuccess &&
       cudaFuncSetAttribute(k_lusgs_cluster<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes) ==
@@ -1086,20 +1247,32 @@ static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const dou
              pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, in, out, backward};
   for (const SweepPlan::Launch& l : pl.schedule) {
     count_launch();
-    if (l.wavefront && st.cluster > 1) {
+    if (l.wavefront && st.engine == kSweepDataflow) {
+      const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
+      k_lusgs_dataflow<512, false><<<1, 512, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);
+    } else if (l.wavefront && st.engine == kSweepDataflowWide) {
+      const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
+      k_lusgs_dataflow<1024, false><<<1, 1024, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);
+    } else if (l.wavefront && st.engine == kSweepDataflowIntMul) {
+      const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
+      k_lusgs_dataflow<512, true><<<1, 512, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);
+    } else if (l.wavefront && st.engine == kSweepDataflowNarrow) {
+      const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
+      k_lusgs_dataflow<256, false><<<1, 256, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);
+    } else if (l.wavefront && (st.engine == kSweepCluster8 || st.engine == kSweepCluster16)) {
       cudaLaunchConfig_t cfg{};
-      cfg.gridDim = dim3(st.cluster);
+      cfg.gridDim = dim3(st.engine);
       cfg.blockDim = dim3(kClusterThreads);
       cfg.dynamicSmemBytes = kRingBytes;
       cfg.stream = s;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = st.cluster;
+      attr[0].val.clusterDim.x = st.engine;
       attr[0].val.clusterDim.y = 1;
       attr[0].val.clusterDim.z = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      const cudaError_t e = st.cluster == 16 ? cudaLaunchKernelEx(&cfg, k_lusgs_cluster<16>, a, l.l0, l.l1)
+      const cudaError_t e = st.engine == 16 ? cudaLaunchKernelEx(&cfg, k_lusgs_cluster<16>, a, l.l0, l.l1)
                                              : cudaLaunchKernelEx(&cfg, k_lusgs_cluster<8>, a, l.l0, l.l1);
       if (e != cudaSuccess) return e;
     } else if (l.wavefront) {

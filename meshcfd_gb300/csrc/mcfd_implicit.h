@@ -39,6 +39,21 @@ struct ImplicitTopology {
 // launch of its own.
 constexpr int kSweepPack = 4;
 
+// How a run of narrow levels is swept: one block with a barrier per level,
+// one block of 256, 512 or 1024 threads with per-row waits (no barrier per
+// level),
+// or a thread-block cluster of 8 / 16 blocks with a cluster barrier per
+// level.
+enum SweepEngine {
+  kSweepBlock = 1,
+  kSweepDataflow = 2,      // 512 threads
+  kSweepDataflowWide = 3,  // 1024 threads
+  kSweepDataflowNarrow = 4,  // 256 threads
+  kSweepDataflowIntMul = 5,  // 512 threads, the row's products on the integer pipe
+  kSweepCluster8 = 8,
+  kSweepCluster16 = 16
+};
+
 struct SweepPlan {
   int n_levels = 0;
   int* level_ptr = nullptr;  // [n_levels + 1] positions
@@ -58,6 +73,10 @@ struct SweepPlan {
   double* pk_diag = nullptr; // [C]
   double* pk_dc = nullptr;   // [C]
   std::vector<int> host_level_ptr;
+  // chunks of at most 32 consecutive positions inside one level (start,
+  // rows), for the dataflow sweep; chunk_ptr[l] = first chunk of level l
+  int2* chunks = nullptr;
+  std::vector<int> host_chunk_ptr;
   struct Launch {
     int wavefront;  // 1: single-block run of levels [l0, l1); 0: grid launch of level l0
     int l0, l1;
@@ -90,8 +109,9 @@ struct ImplicitState {
   int *dptr = nullptr, *dref = nullptr, *rptr = nullptr, *rref = nullptr, *rcol = nullptr;
   SweepPlan fwd, bwd;
   int wide_level = 0;  // levels wider than this get a grid launch each
-  int cluster = 1;     // blocks sweeping a run of narrow levels (1: one block; 8 or 16: a cluster)
+  int engine = 0;      // how a run of narrow levels is swept (SweepEngine)
   bool cluster8_ok = false, cluster16_ok = false;
+  DevStatus* status = nullptr;  // the geometry's status word (sweep time-outs)
   // values and vectors (device)
   double *coef = nullptr, *bterm = nullptr, *diag = nullptr, *dclamp = nullptr, *rval = nullptr;
   double *tmp = nullptr, *state = nullptr, *rate = nullptr, *up = nullptr, *rp = nullptr;
@@ -138,7 +158,8 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
 cudaError_t implicit_set_operator(ImplicitState& st, ScaleVec scale, const double* dt, int dt_per_cell,
                                   cudaStream_t s);
 cudaError_t lusgs_apply(ImplicitState& st, const double* v, double* x, cudaStream_t s);
-void implicit_set_wide_level(ImplicitState& st, int wide, int cluster);
+void implicit_set_wide_level(ImplicitState& st, int wide, int engine);
+cudaError_t implicit_set_chunk(ImplicitState& st, int rows);
 cudaError_t fd_operator(ImplicitState& st, const ResidualFn& residual1, const double* v, double* out,
                         cudaStream_t s);
 // matvec_key: distinguishes operators for the captured inner loop (a graph is

@@ -37,6 +37,8 @@
 
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "mcfd_device.cuh"
 #include "mcfd_internal.h"
 
@@ -123,6 +125,49 @@ __global__ void __launch_bounds__(kBlock) k_primitive(int n, const double* __res
 // triangle lane idle through the fourth entry, which still costs FP64 issue
 // slots).  Each cell's arithmetic and outputs do not depend on the order.
 
+// Least-squares gradient sums of one cell over its entries in the
+// reference's order (np.zeros, then += c (q - p) per entry) and the
+// neighbour extremes.  The first entry's sum is 0.0 + t, which is t itself
+// except that -0.0 becomes +0.0: plus_zero on the integer pipe gives those
+// bits without an FP64 addition.
+__device__ __forceinline__ void gradient_sums(const DevGeom& g, const double* __restrict__ P, int c,
+                                              const double pv[4], double gx[4], double gy[4], double lo[4],
+                                              double hi[4]) {
+  auto visit = [&](int e, auto first) {
+    const int nb = g.grad_nb[e];
+    const double cx = g.grad_cx[e], cy = g.grad_cy[e];
+    const St4 q = ld4(P + 4 * (size_t)nb);
+    const double qv[4] = {q.a, q.b, q.c, q.d};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const double d = qv[v] - pv[v];
+      const double tx = kmul<MUL_GRADIENT>(cx, d), ty = kmul<MUL_GRADIENT>(cy, d);
+      if constexpr (decltype(first)::value) {
+        gx[v] = plus_zero(tx);
+        gy[v] = plus_zero(ty);
+      } else {
+        gx[v] = gx[v] + tx;
+        gy[v] = gy[v] + ty;
+      }
+      // density and pressure are positive (checked at primitive recovery), so
+      // their order is the order of the raw bits; velocities need the key.
+      const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
+      const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
+      if (below) lo[v] = qv[v];
+      if (above) hi[v] = qv[v];
+    }
+  };
+  int e = g.grad_ptr[c];
+  const int e1 = g.grad_ptr[c + 1];
+  if (e < e1) {
+    visit(e++, std::true_type{});
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) gx[v] = gy[v] = 0.0;
+  }
+  for (; e < e1; ++e) visit(e, std::false_type{});
+}
+
 // Resident 256-thread blocks per SM the generic kernel is compiled for.
 #ifndef MCFD_RECON_GENERIC_MIN_BLOCKS
 #define MCFD_RECON_GENERIC_MIN_BLOCKS 2
@@ -136,28 +181,10 @@ __global__ void __launch_bounds__(kBlock, MCFD_RECON_GENERIC_MIN_BLOCKS) k_recon
   if (i >= g.n_cells) return;
   const int c = g.cell_order[i];
   const St4 p = ld4(P + 4 * (size_t)c);
-  double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+  double gx[4], gy[4];
   double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
   const double pv[4] = {p.a, p.b, p.c, p.d};
-  const int e0 = g.grad_ptr[c], e1 = g.grad_ptr[c + 1];
-  for (int e = e0; e < e1; ++e) {
-    const int nb = g.grad_nb[e];
-    const double cx = g.grad_cx[e], cy = g.grad_cy[e];
-    const St4 q = ld4(P + 4 * (size_t)nb);
-    const double qv[4] = {q.a, q.b, q.c, q.d};
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      double d = qv[v] - pv[v];
-      gx[v] = gx[v] + kmul<MUL_GRADIENT>(cx, d);
-      gy[v] = gy[v] + kmul<MUL_GRADIENT>(cy, d);
-      // density and pressure are positive (checked at primitive recovery), so
-      // their order is the order of the raw bits; velocities need the key.
-      const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
-      const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
-      if (below) lo[v] = qv[v];
-      if (above) hi[v] = qv[v];
-    }
-  }
+  gradient_sums(g, P, c, pv, gx, gy, lo, hi);
   double phi[4] = {1.0, 1.0, 1.0, 1.0};
   const int s0 = g.lim_ptr[c], s1 = g.lim_ptr[c + 1];
   if constexpr (LIMITER == MCFD_LIMITER_VENKATAKRISHNAN_K) {
@@ -208,25 +235,9 @@ __device__ __forceinline__ void reconstruct_cell_fast(const DevGeom& g, const do
                                                       double* __restrict__ recon, int c, const St4& p,
                                                       int s0, int s1) {
   const double pv[4] = {p.a, p.b, p.c, p.d};
-  double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+  double gx[4], gy[4];
   double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
-  const int e0 = g.grad_ptr[c], e1 = g.grad_ptr[c + 1];
-  for (int e = e0; e < e1; ++e) {
-    const int nb = g.grad_nb[e];
-    const double cx = g.grad_cx[e], cy = g.grad_cy[e];
-    const St4 q = ld4(P + 4 * (size_t)nb);
-    const double qv[4] = {q.a, q.b, q.c, q.d};
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      double d = qv[v] - pv[v];
-      gx[v] += kmul<MUL_GRADIENT>(cx, d);
-      gy[v] += kmul<MUL_GRADIENT>(cy, d);
-      const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
-      const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
-      if (below) lo[v] = qv[v];
-      if (above) hi[v] = qv[v];
-    }
-  }
+  gradient_sums(g, P, c, pv, gx, gy, lo, hi);
   double tol[4], pos[4], neg[4];
   bool has_pos[4], has_neg[4], flat[4];
 #pragma unroll
@@ -307,25 +318,9 @@ __device__ __forceinline__ void reconstruct_cell_fast_by_variable(const DevGeom&
                                                                   double* __restrict__ recon, int c,
                                                                   const St4& p, int s0) {
   const double pv[4] = {p.a, p.b, p.c, p.d};
-  double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+  double gx[4], gy[4];
   double lo[4] = {p.a, p.b, p.c, p.d}, hi[4] = {p.a, p.b, p.c, p.d};
-  const int e0 = g.grad_ptr[c], e1 = g.grad_ptr[c + 1];
-  for (int e = e0; e < e1; ++e) {
-    const int nb = g.grad_nb[e];
-    const double cx = g.grad_cx[e], cy = g.grad_cy[e];
-    const St4 q = ld4(P + 4 * (size_t)nb);
-    const double qv[4] = {q.a, q.b, q.c, q.d};
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      double d = qv[v] - pv[v];
-      gx[v] += kmul<MUL_GRADIENT>(cx, d);
-      gy[v] += kmul<MUL_GRADIENT>(cy, d);
-      const bool below = (v == 0 || v == 3) ? icmp::lt_pos(qv[v], lo[v]) : icmp::lt(qv[v], lo[v]);
-      const bool above = (v == 0 || v == 3) ? icmp::gt_pos(qv[v], hi[v]) : icmp::lt(hi[v], qv[v]);
-      if (below) lo[v] = qv[v];
-      if (above) hi[v] = qv[v];
-    }
-  }
+  gradient_sums(g, P, c, pv, gx, gy, lo, hi);
   double2 dk[NS];
   size_t out[NS];
 #pragma unroll
@@ -401,16 +396,26 @@ __device__ __forceinline__ void reconstruct_variable_fast(const DevGeom& g, cons
                                                           int s0) {
   double gx = 0.0, gy = 0.0, lo = pv, hi = pv;
   const bool positive = (v == 0 || v == 3);  // density and pressure: the raw bits order them
-  for (int e = g.grad_ptr[c], e1 = g.grad_ptr[c + 1]; e < e1; ++e) {
+  auto visit = [&](int e, auto first) {  // the first sum is 0.0 + t: plus_zero (gradient_sums)
     const double q = P[4 * (size_t)g.grad_nb[e] + v];
     const double d = q - pv;
-    gx += kmul<MUL_GRADIENT>(g.grad_cx[e], d);
-    gy += kmul<MUL_GRADIENT>(g.grad_cy[e], d);
+    const double tx = kmul<MUL_GRADIENT>(g.grad_cx[e], d), ty = kmul<MUL_GRADIENT>(g.grad_cy[e], d);
+    if constexpr (decltype(first)::value) {
+      gx = plus_zero(tx);
+      gy = plus_zero(ty);
+    } else {
+      gx = gx + tx;
+      gy = gy + ty;
+    }
     const bool below = positive ? icmp::lt_pos(q, lo) : icmp::lt(q, lo);
     const bool above = positive ? icmp::gt_pos(q, hi) : icmp::lt(hi, q);
     if (below) lo = q;
     if (above) hi = q;
-  }
+  };
+  int e = g.grad_ptr[c];
+  const int e1 = g.grad_ptr[c + 1];
+  if (e < e1) visit(e++, std::true_type{});
+  for (; e < e1; ++e) visit(e, std::false_type{});
   const double tol = limiter_tolerance(pv);
   double pos = 0.0, neg = 0.0, inc[NS];
   bool has_pos = false, has_neg = false, flat = false;
@@ -553,8 +558,20 @@ __device__ __forceinline__ void gather_cell(const DevGeom& g, const double* P, c
   const int c = g.cell_order[i];
   // interior divergence: SciPy CSR product, ascending face order
   // (solver.py:2160-2174, 2501); derivative starts from zero.
+  // the first term's sum 0.0 + t is plus_zero(t) (integer pipe, same bits)
   double s[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int j = g.gi_ptr[c], j1 = g.gi_ptr[c + 1]; j < j1; ++j) {
+  int j = g.gi_ptr[c];
+  const int j1 = g.gi_ptr[c + 1];
+  if (j < j1) {
+    const double a = g.gi_coef[j];
+    const St4 F = ld4(flux + 4 * (size_t)g.gi_flux[j]);
+    s[0] = plus_zero(kmul<MUL_GATHER>(a, F.a));
+    s[1] = plus_zero(kmul<MUL_GATHER>(a, F.b));
+    s[2] = plus_zero(kmul<MUL_GATHER>(a, F.c));
+    s[3] = plus_zero(kmul<MUL_GATHER>(a, F.d));
+    ++j;
+  }
+  for (; j < j1; ++j) {
     const double a = g.gi_coef[j];
     const St4 F = ld4(flux + 4 * (size_t)g.gi_flux[j]);
     s[0] = s[0] + kmul<MUL_GATHER>(a, F.a);

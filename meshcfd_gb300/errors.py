@@ -44,6 +44,8 @@ STATUS_MFO_DENSITY = 1 << 16
 STATUS_VISC_TEMPERATURE = 1 << 17
 STATUS_VISC_SUTHERLAND = 1 << 18
 STATUS_VISC_DISTANCE = 1 << 19
+# no counterpart in the reference: an LU-SGS sweep stopped after a bounded wait
+STATUS_SWEEP_TIMEOUT = 1 << 20
 
 
 class StatusCode(int):
@@ -83,6 +85,7 @@ STATUS_MESSAGES = (
     (STATUS_ROE_NONFINITE, ValueError, "Roe flux produced a non-finite value."),
     (STATUS_NONFINITE_RESIDUAL, SolverError, "Spatial residual contains non-finite values."),
     (STATUS_TIME_STEP, SolverError, "Local stable time steps must be positive and finite."),
+    (STATUS_SWEEP_TIMEOUT, RuntimeError, "LU-SGS sweep waited past its bound for a row it depends on."),
 )
 
 

@@ -214,11 +214,12 @@ def _permuted_periodic(n, seed):
     return case, build_geometry(case.mesh, case)
 
 
-@pytest.mark.parametrize("mesh", ("bump", "permuted"))
+@pytest.mark.parametrize("mesh", ("bump", "permuted", "bump512", "permuted192"))
 def test_lusgs_schedules_agree_and_match_spsolve(cuda_device, mesh):
-    """Every launch schedule of the level-scheduled sweeps (one block or a
-    cluster of 8 or 16 stepping through narrow levels with their
-    shared-memory rings, grid launches per level, and mixtures) gives the
+    """Every launch schedule of the level-scheduled sweeps (one block with a
+    barrier per level, one block whose rows wait only for the rows they read,
+    or a cluster of 8 or 16, stepping through narrow levels with their
+    shared-memory rings; grid launches per level; and mixtures) gives the
     same bits, and matches the reference's two spsolve_triangular calls
     (within 1e-12)."""
     import torch
@@ -227,22 +228,27 @@ def test_lusgs_schedules_agree_and_match_spsolve(cuda_device, mesh):
     from oracle.implicit import ImplicitOracle
     from dataclasses import replace
 
-    if mesh == "bump":
-        case, P = bump_case(96, 48)
+    if mesh.startswith("bump"):
+        case, P = bump_case(*((512, 256) if mesh == "bump512" else (96, 48)))
         P = P * (1.0 + 0.05 * np.random.default_rng(4).standard_normal(P.shape))
         s = case.numerics
         g = build_geometry(case.mesh, case)
     else:
-        case, g = _permuted_periodic(64, 7)
+        # randomly numbered cells: rows read solutions far back in sweep
+        # order (beyond the dataflow sweep's shared-memory window)
+        case, g = _permuted_periodic(192 if mesh == "permuted192" else 64, 7)
         s = case.numerics
         P = smooth_primitive(len(g.areas), seed=3)
     dg, U0, dt, _ = _prepare_on(g, s, P, cuda_device)
     v = torch.as_tensor(np.random.default_rng(2).standard_normal(U0.shape), device=cuda_device)
     stream = torch.cuda.current_stream().cuda_stream
     outs = []
-    for wide, cluster in ((0, 1), (0, 8), (0, 16), (1, 8), (7, 1), (7, 8), (1 << 30, 1), (1 << 30, 16)):
-        rc = dg.lib.mcfd_implicit_set_sweep(dg.handle, wide, cluster)
-        if cluster > 1 and rc == 3:
+    for wide, engine, chunk in ((0, 1, 0), (0, 2, 0), (0, 3, 0), (0, 4, 0), (0, 5, 0), (7, 5, 0), (0, 2, 1), (0, 4, 8), (0, 2, 17),
+                                (0, 8, 0), (0, 16, 0), (1, 8, 0), (7, 1, 0), (7, 2, 0), (7, 3, 5), (7, 8, 0),
+                                (1 << 30, 1, 0), (1 << 30, 2, 0), (1 << 30, 3, 0), (1 << 30, 16, 0)):
+        assert dg.lib.mcfd_implicit_set_chunk(dg.handle, chunk) == 0
+        rc = dg.lib.mcfd_implicit_set_sweep(dg.handle, wide, engine)
+        if engine > 2 and rc == 3:
             continue  # the device cannot run this cluster size
         assert rc == 0
         x = torch.empty_like(v)
