@@ -527,6 +527,22 @@ int mcfd_host_face_geometry(int64_t n_faces, const int64_t* face_nodes, const do
                             const double* centers, const int64_t* owners, double* face_centers,
                             double* normals, double* lengths, int64_t* bad_face);
 
+/*
+ * The two-ring stencil of the MUSCL-parabolic reconstruction
+ * (_parabolic_stencil, solver.py:2241-2291): per cell, a breadth-first search
+ * of depth two over the gradient entries (sources, neighbours, dx, dy in the
+ * reference's entry order), each (cell, offset) pair once with offsets keyed
+ * by Python's round(offset / domain_scale, 10), pairs with a non-zero offset
+ * kept in visiting order.  Host code (several threads).  Writes at most
+ * `capacity` entries and the count to *out_count; MCFD_E_ARG when the count
+ * exceeds capacity (*out_count then holds the count needed).
+ */
+int mcfd_host_parabolic_stencil(int64_t n_cells, int64_t n_entries, const int64_t* sources,
+                                const int64_t* neighbours, const double* dx, const double* dy,
+                                double domain_scale, int64_t capacity, int64_t* out_sources,
+                                int64_t* out_neighbours, double* out_dx, double* out_dy,
+                                int64_t* out_count);
+
 #ifdef __cplusplus
 }
 #endif

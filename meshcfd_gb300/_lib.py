@@ -131,6 +131,8 @@ SIGNATURES = {
     "mcfd_ieee_mul": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp]),
     "mcfd_host_cell_geometry": (c_i32, [c_i64, P_i64, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
     "mcfd_host_face_geometry": (c_i32, [c_i64, P_i64, P_dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
+    "mcfd_host_parabolic_stencil": (c_i32, [c_i64, c_i64, P_i64, P_i64, P_dbl, P_dbl, c_dbl, c_i64, P_i64, P_i64,
+                                            P_dbl, P_dbl, P_i64]),
 }
 
 
@@ -194,6 +196,30 @@ class Native:
             raise SolverError(f"Face {bad.value} has zero or invalid length.")
         self.check(rc, "face geometry")
         return fc, normals, lengths
+
+
+    def parabolic_stencil(self, cell_count, sources, neighbours, dx, dy, domain_scale):
+        """The two-ring stencil (solver.py:2241-2291) by the compiled search
+        (mcfd_host_parabolic_stencil); the same entries as
+        ``geometry.parabolic_stencil``."""
+        sources = np.ascontiguousarray(sources, dtype=np.int64)
+        neighbours = np.ascontiguousarray(neighbours, dtype=np.int64)
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        dy = np.ascontiguousarray(dy, dtype=np.float64)
+        degree = np.bincount(sources, minlength=cell_count) if len(sources) else np.zeros(cell_count, np.int64)
+        capacity = int(len(sources) + degree[neighbours].sum()) if len(sources) else 0
+        out_s = np.empty(max(capacity, 1), dtype=np.int64)
+        out_n = np.empty_like(out_s)
+        out_x = np.empty(max(capacity, 1))
+        out_y = np.empty_like(out_x)
+        count = C.c_int64(0)
+        rc = self.mcfd_host_parabolic_stencil(int(cell_count), len(sources), _ptr(sources, P_i64),
+                                              _ptr(neighbours, P_i64), _ptr(dx, P_dbl), _ptr(dy, P_dbl),
+                                              float(domain_scale), capacity, _ptr(out_s, P_i64), _ptr(out_n, P_i64),
+                                              _ptr(out_x, P_dbl), _ptr(out_y, P_dbl), C.byref(count))
+        self.check(rc, "parabolic stencil")
+        n = count.value
+        return out_s[:n].copy(), out_n[:n].copy(), out_x[:n].copy(), out_y[:n].copy()
 
 
 def library_path() -> Path:

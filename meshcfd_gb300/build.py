@@ -42,6 +42,7 @@ UNITS = [
     ("mcfd_viscous.cu", ["-fmad=false"]),
     ("mcfd_api.cu", []),
     ("mcfd_noalloc.cu", ["-fmad=false"]),
+    ("mcfd_stencil.cu", []),
 ]
 
 

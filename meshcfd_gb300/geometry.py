@@ -515,7 +515,8 @@ def build_geometry(mesh: FiniteVolumeMesh, case, host=None) -> Geometry:
     parabolic = (np.empty(0, dtype=np.int64), np.empty(0, dtype=np.int64), np.empty(0), np.empty(0))
     if case.numerics.reconstruction == "MUSCL parabolic":
         domain_scale = max(float(points[:, 0].max() - points[:, 0].min()), float(points[:, 1].max() - points[:, 1].min()), 1e-12)
-        parabolic = parabolic_stencil(n_cells, src, nbr, gdx, gdy, domain_scale)
+        search = getattr(lib, "parabolic_stencil", None) or parabolic_stencil
+        parabolic = search(n_cells, src, nbr, gdx, gdy, domain_scale)
 
     return Geometry(
         centers=centers,

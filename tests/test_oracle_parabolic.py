@@ -80,3 +80,39 @@ def test_parabolic_reconstruction_recovers_quadratic_field():
     np.testing.assert_allclose(grad[c, 0], (2.0 * x[c] + 2.0 * y[c], 2.0 * x[c] + 6.0 * y[c]), rtol=1e-10, atol=1e-10)
     np.testing.assert_allclose(curv[c, 0], (2.0, 2.0, 6.0), rtol=1e-10, atol=1e-10)
     assert fac[c, 0] == pytest.approx(1.0)
+
+
+@pytest.mark.parametrize("mesh", ("vortex_half", "bump", "periodic_permuted", "box_all"))
+def test_compiled_two_ring_stencil_equals_the_restated_search(mesh):
+    """The library's threaded two-ring search (mcfd_host_parabolic_stencil)
+    returns the entries of the Python restatement of _parabolic_stencil
+    (solver.py:2241-2291) in the same order, on periodic meshes (offsets
+    across the period, where the rounded-offset keys separate images of one
+    cell), a stretched wall-bounded mesh, randomly numbered cells and an
+    all-triangle box."""
+    from meshcfd_gb300 import _lib
+    from meshcfd_gb300.geometry import build_geometry, parabolic_stencil
+    from meshcfd_gb300.meshes import box_mesh, bump_case, periodic_case, permute_mesh, vortex_case
+    from meshcfd_gb300.model import Case
+
+    if mesh == "vortex_half":
+        case, _ = vortex_case(24, split="half")
+    elif mesh == "bump":
+        case, _ = bump_case(24, 12)
+    elif mesh == "periodic_permuted":
+        case = periodic_case(20, 20, split="half", jitter=0.2, seed=5)
+        rng = np.random.default_rng(3)
+        case.mesh = permute_mesh(case.mesh, rng.permutation(len(case.mesh.cells)),
+                                 rng.permutation(len(case.mesh.faces)))
+    else:
+        case = Case(name="box", mesh=box_mesh(14, 9, 2.0, 1.0, split="all", jitter=0.2, seed=2))
+    g = build_geometry(case.mesh, case)
+    points = np.asarray(case.mesh.points, dtype=float)
+    scale = max(float(np.ptp(points[:, 0])), float(np.ptp(points[:, 1])), 1e-12)
+    args = (len(g.areas), np.asarray(g.gradient_sources), np.asarray(g.gradient_neighbours),
+            np.asarray(g.gradient_dx), np.asarray(g.gradient_dy), scale)
+    ref = parabolic_stencil(*args)
+    got = _lib.native().parabolic_stencil(*args)
+    assert len(ref[0]) > 6 * len(g.areas)
+    for a, b in zip(got, ref):
+        np.testing.assert_array_equal(a, b)
