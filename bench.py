@@ -404,20 +404,40 @@ class ExplicitRun:
         self.U_init = primitive_to_conservative(self.P0, self.settings.gamma)
         self.U = torch.as_tensor(self.U_init, device=device)
         self.dt = torch.empty(1, dtype=torch.float64, device=device)
+        self.dt_next = torch.empty(1, dtype=torch.float64, device=device)
         self.P = self.dg.primitive_buffer()
+        self.primed = None  # the settings whose time step self.dt holds for the state in self.U
         self.tuned = None
 
-    def step(self, U=None, cfg=None):
-        U = self.U if U is None else U
+    def step(self, cfg=None):
+        """One step of the run's state: the stable time step, then the RK3
+        stages.  Once primed (``reset``), the time step of every step comes
+        from the previous step's last stage (mcfd_explicit_step_next, the
+        values mcfd_time_steps gives) and the step starts from the primitive
+        that stage left; ``self.last_dt`` is the step's time step."""
         cfg = self.cfg if cfg is None else cfg
-        self.dg.time_steps(self.P, cfg, out_min=self.dt)
-        self.dg.explicit_step(U, cfg, 2, self.dt)
+        if self.primed is not cfg:
+            self.dg.time_steps(self.P, cfg, out_min=self.dt)
+            self.primed = cfg
+        self.dg.explicit_step_next(self.U, cfg, 2, self.dt, next_dt_min=self.dt_next, primitive_current=True)
+        self.last_dt = self.dt
+        self.dt, self.dt_next = self.dt_next, self.dt
+
+    def step_plain(self):
+        """One drop-in step of the state in self.U: primitive, stable time
+        step and RK3 stages, each from the state (mcfd_primitive,
+        mcfd_time_steps, mcfd_explicit_step)."""
+        self.dg.primitive(self.U, self.cfg, out=self.P)
+        self.dg.time_steps(self.P, self.cfg, out_min=self.dt)
+        self.dg.explicit_step(self.U, self.cfg, 2, self.dt)
+        self.primed = None
 
     def reset(self, cfg=None):
         import torch
 
         self.U.copy_(torch.as_tensor(self.U_init, device=self.device))
         self.dg.primitive(self.U, cfg or self.cfg, out=self.P)
+        self.primed = None
 
     def march(self, steps, cfg=None):
         """``steps`` steps from the initial state; returns the physical time."""
@@ -425,7 +445,7 @@ class ExplicitRun:
         t = 0.0
         for _ in range(steps):
             self.step(cfg=cfg)
-            t += float(self.dt.item())
+            t += float(self.last_dt.item())
         self.dg.check_status()
         return t
 
@@ -545,8 +565,7 @@ def run_gpu(args):
 
         def e2e_step():
             run.U.copy_(host, non_blocking=True)
-            run.dg.primitive(run.U, cfg, out=run.P)
-            run.step()
+            run.step_plain()
             out.copy_(run.U, non_blocking=True)
 
         for _ in range(2):
@@ -969,6 +988,7 @@ def run_bump(args):
 
     from meshcfd_gb300.device import DeviceGeometry, make_config, primitive_to_conservative
     from meshcfd_gb300.geometry import build_geometry
+    from meshcfd_gb300.errors import SolverError
     from meshcfd_gb300.implicit import BudgetExceeded, ImplicitEuler
     from meshcfd_gb300.meshes import bump_case
 
@@ -1008,6 +1028,9 @@ def run_bump(args):
                 new, used = stepper.step(U, dt)
             except BudgetExceeded:
                 status = f"stopped by the {args.budget_s:.0f} s budget during step {k + 1}"
+                break
+            except SolverError as error:  # the reference's own stop (solver.py:1363-1368, 810-811)
+                status = f"Solver failed at step {k + 1}: {error}"
                 break
             torch.cuda.synchronize()
             wall = time.perf_counter() - ts

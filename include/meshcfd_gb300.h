@@ -284,6 +284,21 @@ int mcfd_time_steps(mcfd_geom* geom, const mcfd_config* cfg, const double* P,
  */
 int mcfd_explicit_step(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, double* U,
                        const double* dt, int32_t dt_per_cell, void* stream);
+/* mcfd_explicit_step followed by mcfd_time_steps on the new state: the time
+ * steps of the next step (per cell into next_dt_cells and / or their minimum
+ * with time_limit into next_dt_min, either may be NULL, neither may alias dt)
+ * — computed by the last stage from the primitive it recovers, where they
+ * depend on the cell state alone (inviscid, no pressure-inlet or mass-flow
+ * patches), else by the time-step pass; the same values either way.
+ * primitive_current = 1 skips the primitive recovery at the start of the
+ * step: the caller asserts that the handle's primitive buffer holds the
+ * primitive of U, as the previous explicit step on this handle left it.
+ * The reference computes the stable step at the top of each loop iteration
+ * (solver.py:437-461); this is the same sequence with the step boundary
+ * moved.  No counterpart in the reference. */
+int mcfd_explicit_step_next(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, double* U,
+                            const double* dt, int32_t dt_per_cell, int32_t primitive_current,
+                            double* next_dt_cells, double* next_dt_min, double time_limit, void* stream);
 
 /* The reconstruction fields of the reference for primitive P [n_cells][4]:
  * MUSCL linear -> _limited_gradients (solver.py:2294-2319): gradients

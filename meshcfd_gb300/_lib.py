@@ -97,6 +97,7 @@ SIGNATURES = {
     "mcfd_residual": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp]),
     "mcfd_time_steps": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_dbl, c_vp]),
     "mcfd_explicit_step": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp]),
+    "mcfd_explicit_step_next": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_dbl, c_vp]),
     "mcfd_geom_primitive": (c_vp, [c_vp]),
     "mcfd_geom_stage_state": (c_vp, [c_vp, C.c_int32]),
     "mcfd_reconstruction": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -1098,16 +1098,25 @@ int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, doubl
 }
 
 
-int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U,
-                       const double* dt, int32_t dt_per_cell, void* stream) {
-  if (!h || !U || !dt) return MCFD_E_ARG;
-  int c = check_cfg(cfg);
-  if (c) return c;
-  if ((c = ensure_viscous(h, cfg))) return c;
-  if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
+// One explicit step (solver.py:532-806, 1128-1182).  primitive_current: the
+// handle's primitive buffer already holds the primitive of U (as the final
+// stage of the previous step left it), so the step starts without
+// recomputing it.  next: the last stage also writes the stable time steps of
+// the new state (NextDt), where the settings allow; the caller completes
+// them otherwise.
+struct NextDt {
+  double* cells = nullptr;
+  int min = 0;
+  double cfl = 0.0;
+};
+
+static cudaError_t explicit_step_impl(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U,
+                                      const double* dt, int32_t dt_per_cell, bool primitive_current,
+                                      const NextDt& next, cudaStream_t s) {
   Workspace& w = h->ws;
-  cudaError_t e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, w.P, s)); });
+  cudaError_t e = cudaSuccess;
+  if (!primitive_current)
+    e = timed(h, MCFD_PROF_PRIMITIVE, s, [&] { return MCFD_DISPATCH(*cfg, launch_primitive(h->g, *cfg, U, w.P, s)); });
   auto run = [&](std::initializer_list<StageTerm> terms, double* out, double* save_r) {
     if (e != cudaSuccess) return;
     StageProgram p{};
@@ -1118,6 +1127,11 @@ int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, dou
     p.out_u = out;
     p.out_p = w.P;
     p.out_r = save_r;
+    if (out == U) {  // the last stage
+      p.next_dt_cells = next.cells;
+      p.next_dt_min = next.min;
+      p.cfl = next.cfl;
+    }
     e = stage(h, *cfg, p, s);
   };
   double *X1 = w.stage[0], *X2 = w.stage[1], *X3 = w.stage[2], *X4 = w.stage[3];
@@ -1147,6 +1161,48 @@ int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, dou
            term(TERM_DTR, 0.226007483236906, nullptr)}, U, nullptr);
       break;
   }
+  return e;
+}
+
+int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U,
+                       const double* dt, int32_t dt_per_cell, void* stream) {
+  if (!h || !U || !dt) return MCFD_E_ARG;
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if ((c = ensure_viscous(h, cfg))) return c;
+  if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
+  return rc(explicit_step_impl(h, cfg, scheme, U, dt, dt_per_cell, false, NextDt{}, (cudaStream_t)stream));
+}
+
+int mcfd_explicit_step_next(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U, const double* dt,
+                            int32_t dt_per_cell, int32_t primitive_current, double* next_dt_cells,
+                            double* next_dt_min, double time_limit, void* stream) {
+  if (!h || !U || !dt || (!next_dt_cells && !next_dt_min)) return MCFD_E_ARG;
+  if (next_dt_cells == dt || next_dt_min == dt) return MCFD_E_ARG;  // the stages read dt to the end
+  int c = check_cfg(cfg);
+  if (c) return c;
+  if ((c = ensure_viscous(h, cfg))) return c;
+  if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
+  if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the last stage computes the time steps where they depend on the cell
+  // state alone (inviscid, no pressure-inlet / mass-flow patches, whose
+  // exterior states come from a pass of their own)
+  const bool fused = cfg->viscosity_model == MCFD_VISC_INVISCID && h->g.n_bc_patches == 0;
+  NextDt next;
+  if (fused) {
+    next.cells = next_dt_cells;
+    next.min = next_dt_min != nullptr;
+    next.cfl = cfg->cfl;
+  }
+  cudaError_t e = explicit_step_impl(h, cfg, scheme, U, dt, dt_per_cell, primitive_current != 0, next, s);
+  if (e != cudaSuccess) return MCFD_E_CUDA;
+  if (!fused) return mcfd_time_steps(h, cfg, h->ws.P, next_dt_cells, next_dt_min, time_limit, stream);
+  if (next_dt_min)
+    e = timed(h, MCFD_PROF_TIME_STEP, s, [&] {
+      count_launch();
+      return finalize_time_step(h->g.status, next_dt_min, time_limit, s);
+    });
   return rc(e);
 }
 

@@ -139,6 +139,12 @@ struct StageProgram {
   double* out_p;     // primitive of out_u, may be null
   double* out_r;     // residual store, may be null
   const double* visc_r;  // laminar viscous residual added before the body force, may be null
+  // the stable time steps of the new state (out_u), computed by the gather
+  // from its primitive: per cell into next_dt_cells (may be null) and, when
+  // next_dt_min, their minimum into the status word (as k_time_steps)
+  double* next_dt_cells;
+  int next_dt_min;
+  double cfl;
 };
 
 struct Workspace {
@@ -245,6 +251,7 @@ constexpr int kSumsqBlocks = 152 * 4;
 constexpr int kSumsqThreads = 256;
 __global__ void k_sumsq_partial(int n, const double* __restrict__ R, double* __restrict__ partials);
 __global__ void k_sumsq_final(int blocks, const double* __restrict__ partials, double* sums);
+cudaError_t finalize_time_step(DevStatus* st, double* dt_min, double time_limit, cudaStream_t s);
 cudaError_t launch_sumsq(const DevGeom& g, const double* R, double* partials, int blocks,
                          double* sums, cudaStream_t s);
 

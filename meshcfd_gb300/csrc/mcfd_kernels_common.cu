@@ -126,6 +126,19 @@ __global__ void __launch_bounds__(kBlock) k_ieee_mul(long long n, const double* 
     product[i] = mul_rn(a[i], b[i]);
 }
 
+// The global time step from the block minima (min with the end-time limit,
+// Python's min semantics, solver.py:455-461); resets the minimum.
+__global__ void k_finalize_time_step(DevStatus* st, double* dt_min, double time_limit) {
+  const double stable = __longlong_as_double((long long)st->dt_min_bits);
+  dt_min[0] = icmp::lt(time_limit, stable) ? time_limit : stable;
+  st->dt_min_bits = 0x7ff0000000000000ULL;
+}
+
+cudaError_t finalize_time_step(DevStatus* st, double* dt_min, double time_limit, cudaStream_t s) {
+  k_finalize_time_step<<<1, 1, 0, s>>>(st, dt_min, time_limit);
+  return cudaGetLastError();
+}
+
 }  // namespace mcfd
 
 extern "C" int mcfd_ieee_mul(const double* a, const double* b, int64_t n, double* product, void* stream) {

@@ -535,6 +535,77 @@ __global__ void __launch_bounds__(kBlock) k_flux(DevGeom g, const double* __rest
     flux_face<FLUX, SEG, FIRST_ORDER, KERNEL_HLLC>(g, P, recon, flux, gamma, inv_gm1, f, begin);
 }
 
+// --------------------------------------------------------------- time steps
+//
+// _stable_time_steps (solver.py:4132-4343), inviscid: per cell, the sum over
+// its owner-side faces (face order) of (|u.n| + c) * L — with the exterior
+// radius max'ed in on inlet / outlet / far-field faces — then over its
+// neighbour-side interior faces; dt = CFL * A / sum; global = min.
+
+// One cell's stable time step from its primitive p (flags status bits).
+__device__ __forceinline__ double cell_time_step(const DevGeom& g, int c, const St4& p, double gamma, double cfl,
+                                                 const double* __restrict__ diffusion, int* bits) {
+  const double sound = sound_speed(p.a, p.d, gamma);
+  double sum = 0.0;
+  for (int e = g.dt_ptr[c], e1 = g.dt_ptr[c + 1]; e < e1; ++e) {
+    const double2 n = g.dt_normal[e];
+    const int info = g.dt_info[e];
+    double radius = abs_of(p.b * n.x + p.c * n.y) + sound;
+    const int kind = info >> 28;
+    if (kind != DT_PLAIN) {
+      const int idx = info & 0x0fffffff;
+      St4 ext;
+      if (kind == DT_VIN) ext = ld4(g.ff_vin_state + 4 * (size_t)idx);
+      else if (kind == DT_POUT) ext = St4{p.a, p.b, p.c, g.ff_pout_pressure[idx]};
+      else if (kind == DT_FAR) *bits |= far_field_state(p, ld4(g.ff_far_state + 4 * (size_t)idx), n.x, n.y, gamma, &ext);
+      else ext = ld4(g.bc_ext_dt + 4 * (size_t)idx);  // solver.py:4153-4188, states from k_bc_states
+      double er = abs_of(ext.b * n.x + ext.c * n.y) + sound_speed(ext.a, ext.d, gamma);
+      radius = icmp::lt_nonneg(radius, er) ? er : radius;  // np.maximum
+    }
+    sum = sum + radius * g.dt_len[e];
+  }
+  if (diffusion) sum += 2.0 * diffusion[c];  // viscous terms (solver.py:4331)
+  const double dt = div_rn(cfl * g.area[c], sum);
+  if (!icmp::finite(dt) || !icmp::gt0(dt)) *bits |= MCFD_S_TIME_STEP;
+  return dt;
+}
+
+// Block minimum of the positive time steps by warp shuffles, then one
+// atomicMin on the bit pattern (positive doubles order like their bits).
+// Every thread of the block calls it.
+__device__ __forceinline__ void block_min_time_step(DevStatus* st, double dt, bool active) {
+  long long m = (active && icmp::gt0(dt)) ? icmp::bits(dt) : 0x7ff0000000000000LL;
+  for (int off = 16; off > 0; off >>= 1) {
+    long long o = __shfl_down_sync(0xffffffffu, m, off);
+    m = (o < m) ? o : m;
+  }
+  __shared__ long long warp_min[32];
+  if ((threadIdx.x & 31) == 0) warp_min[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long b = warp_min[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = (warp_min[w] < b) ? warp_min[w] : b;
+    atomicMin(&st->dt_min_bits, (unsigned long long)b);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* __restrict__ P,
+                                                       double gamma, double cfl,
+                                                       double* __restrict__ dt_cells,
+                                                       int want_min, const double* __restrict__ diffusion) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < g.n_cells;
+  double dt = __longlong_as_double(0x7ff0000000000000LL);
+  if (active) {
+    const int c = g.cell_order[i];
+    int bits = 0;
+    dt = cell_time_step(g, c, ld4(P + 4 * (size_t)c), gamma, cfl, diffusion, &bits);
+    if (bits) flag_cell(g.status, bits, c);
+    if (dt_cells) dt_cells[c] = dt;
+  }
+  if (want_min) block_min_time_step(g.status, dt, active);
+}
+
 // ------------------------------------------------------------ gather + stage
 
 __device__ __forceinline__ double stage_dt(const StageProgram& prog, int c) {
@@ -554,7 +625,8 @@ enum GatherShape { SHAPE_GENERIC = 0, SHAPE_EULER = 1, SHAPE_X_XDTR = 2 };
 // check, stage combination and primitive recovery of the new state.
 template <int SHAPE, bool EXTRAS>
 __device__ __forceinline__ void gather_cell(const DevGeom& g, const double* P, const double* flux, double gamma,
-                                            double ax, double ay, const StageProgram& prog, int i) {
+                                            double ax, double ay, const StageProgram& prog, int i,
+                                            St4* q_out = nullptr) {
   const int c = g.cell_order[i];
   // interior divergence: SciPy CSR product, ascending face order
   // (solver.py:2160-2174, 2501); derivative starts from zero.
@@ -663,15 +735,35 @@ __device__ __forceinline__ void gather_cell(const DevGeom& g, const double* P, c
     const St4 q = to_prim(U, gamma, &ok);
     if (!ok) flag_cell(g.status, MCFD_S_NONPHYSICAL_STATE, c);
     st4(prog.out_p + 4 * (size_t)c, q);
+    if (q_out) *q_out = q;
   }
 }
 
-template <int SHAPE, bool EXTRAS>
+// DT: the stage also computes the stable time steps of its new state from
+// the primitive it has just recovered (cell_time_step, the same bits as
+// k_time_steps on that primitive), which saves the time-step pass over the
+// state of the next step.
+template <int SHAPE, bool EXTRAS, bool DT>
 __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
                                                    const double* __restrict__ flux, double gamma,
                                                    double ax, double ay, StageProgram prog) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < g.n_cells) gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i);
+  if constexpr (!DT) {
+    if (i < g.n_cells) gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i);
+  } else {
+    const bool active = i < g.n_cells;
+    double dt = __longlong_as_double(0x7ff0000000000000LL);
+    if (active) {
+      St4 q;
+      gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i, &q);
+      const int c = g.cell_order[i];
+      int bits = 0;
+      dt = cell_time_step(g, c, q, gamma, prog.cfl, nullptr, &bits);
+      if (bits) flag_cell(g.status, bits, c);
+      if (prog.next_dt_cells) prog.next_dt_cells[c] = dt;
+    }
+    if (prog.next_dt_min) block_min_time_step(g.status, dt, active);
+  }
 }
 
 // ------------------------------------------------------ one launch per stage
@@ -733,68 +825,6 @@ __global__ void __launch_bounds__(kBlock, MCFD_FUSED_MIN_BLOCKS) k_stage_fused(D
   flux_phase<FLUX, SEG_FAR>(g, P, recon, flux, gamma, inv_gm1, tid, stride);
   grid.sync();
   for (int i = tid; i < g.n_cells; i += stride) gather_cell<SHAPE, false>(g, P, flux, gamma, 0.0, 0.0, prog, i);
-}
-
-// --------------------------------------------------------------- time steps
-//
-// _stable_time_steps (solver.py:4132-4343), inviscid: per cell, the sum over
-// its owner-side faces (face order) of (|u.n| + c) * L — with the exterior
-// radius max'ed in on inlet / outlet / far-field faces — then over its
-// neighbour-side interior faces; dt = CFL * A / sum; global = min.
-
-__global__ void __launch_bounds__(kBlock) k_time_steps(DevGeom g, const double* __restrict__ P,
-                                                       double gamma, double cfl,
-                                                       double* __restrict__ dt_cells,
-                                                       int want_min, const double* __restrict__ diffusion) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = i < g.n_cells;
-  const int c = active ? g.cell_order[i] : 0;
-  double dt = __longlong_as_double(0x7ff0000000000000LL);
-  if (active) {
-    const St4 p = ld4(P + 4 * (size_t)c);
-    const double sound = sound_speed(p.a, p.d, gamma);
-    double sum = 0.0;
-    int bits = 0;
-    for (int e = g.dt_ptr[c], e1 = g.dt_ptr[c + 1]; e < e1; ++e) {
-      const double2 n = g.dt_normal[e];
-      const int info = g.dt_info[e];
-      double radius = abs_of(p.b * n.x + p.c * n.y) + sound;
-      const int kind = info >> 28;
-      if (kind != DT_PLAIN) {
-        const int idx = info & 0x0fffffff;
-        St4 ext;
-        if (kind == DT_VIN) ext = ld4(g.ff_vin_state + 4 * (size_t)idx);
-        else if (kind == DT_POUT) ext = St4{p.a, p.b, p.c, g.ff_pout_pressure[idx]};
-        else if (kind == DT_FAR) bits |= far_field_state(p, ld4(g.ff_far_state + 4 * (size_t)idx), n.x, n.y, gamma, &ext);
-        else ext = ld4(g.bc_ext_dt + 4 * (size_t)idx);  // solver.py:4153-4188, states from k_bc_states
-        double er = abs_of(ext.b * n.x + ext.c * n.y) + sound_speed(ext.a, ext.d, gamma);
-        radius = icmp::lt_nonneg(radius, er) ? er : radius;  // np.maximum
-      }
-      sum = sum + radius * g.dt_len[e];
-    }
-    if (diffusion) sum += 2.0 * diffusion[c];  // viscous terms (solver.py:4331)
-    dt = div_rn(cfl * g.area[c], sum);
-    if (!icmp::finite(dt) || !icmp::gt0(dt)) bits |= MCFD_S_TIME_STEP;
-    if (bits) flag_cell(g.status, bits, c);
-    if (dt_cells) dt_cells[c] = dt;
-  }
-  if (!want_min) return;
-  // block minimum by warp shuffles, then one atomicMin on the bit pattern
-  // (positive doubles order like their unsigned bits).
-  // positive doubles order like their bits: the minimum runs on integers
-  long long m = (active && icmp::gt0(dt)) ? icmp::bits(dt) : 0x7ff0000000000000LL;
-  for (int off = 16; off > 0; off >>= 1) {
-    long long o = __shfl_down_sync(0xffffffffu, m, off);
-    m = (o < m) ? o : m;
-  }
-  __shared__ long long warp_min[kBlock / 32];
-  if ((threadIdx.x & 31) == 0) warp_min[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    long long b = warp_min[0];
-    for (int w = 1; w < kBlock / 32; ++w) b = (warp_min[w] < b) ? warp_min[w] : b;
-    atomicMin(&g.status->dt_min_bits, (unsigned long long)b);
-  }
 }
 
 __global__ void k_time_step_finalize(DevStatus* st, double* dt_min, double time_limit) {
@@ -938,7 +968,21 @@ cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double
   const int b = (g.n_cells + t - 1) / t;
   const double ax = cfg.acceleration_x, ay = cfg.acceleration_y;
   count_launch();
-#define MCFD_GATHER(SH, EX) k_gather<SH, EX><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
+  if (prog.out_u && (prog.next_dt_cells || prog.next_dt_min) && !prog.visc_r) {
+#define MCFD_GATHER_DT(SH, EX) k_gather<SH, EX, true><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
+    if (extras) {
+      if (shape == SHAPE_EULER) MCFD_GATHER_DT(SHAPE_EULER, true);
+      else if (shape == SHAPE_X_XDTR) MCFD_GATHER_DT(SHAPE_X_XDTR, true);
+      else MCFD_GATHER_DT(SHAPE_GENERIC, true);
+    } else {
+      if (shape == SHAPE_EULER) MCFD_GATHER_DT(SHAPE_EULER, false);
+      else if (shape == SHAPE_X_XDTR) MCFD_GATHER_DT(SHAPE_X_XDTR, false);
+      else MCFD_GATHER_DT(SHAPE_GENERIC, false);
+    }
+#undef MCFD_GATHER_DT
+    return cudaGetLastError();
+  }
+#define MCFD_GATHER(SH, EX) k_gather<SH, EX, false><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
   if (extras) {
     if (shape == SHAPE_EULER) MCFD_GATHER(SHAPE_EULER, true);
     else if (shape == SHAPE_X_XDTR) MCFD_GATHER(SHAPE_X_XDTR, true);
@@ -979,7 +1023,7 @@ bool stage_fused_supported(const DevGeom& g, const mcfd_config& cfg, const Stage
          cfg.limiter <= 3 &&
          cfg.viscosity_model == MCFD_VISC_INVISCID && g.n_bc_patches == 0 && g.n_cells > 0 &&
          cfg.acceleration_x == 0.0 && cfg.acceleration_y == 0.0 && !prog.visc_r && prog.out_u &&
-         stage_shape(prog) != SHAPE_GENERIC;
+         !prog.next_dt_cells && !prog.next_dt_min && stage_shape(prog) != SHAPE_GENERIC;
 }
 
 template <int LIMITER, int FLUX, int SHAPE>

@@ -291,6 +291,27 @@ class DeviceGeometry:
         self.lib.check(self.lib.mcfd_explicit_step(self.handle, C.byref(cfg), int(scheme), U.data_ptr(), dt.data_ptr(),
                                                    per_cell, _stream_ptr()), "mcfd_explicit_step")
 
+    def explicit_step_next(self, U: torch.Tensor, cfg, scheme: int, dt: torch.Tensor, *,
+                           next_dt_min: torch.Tensor | None = None, next_dt_cells: torch.Tensor | None = None,
+                           time_limit: float = math.inf, primitive_current: bool = False) -> None:
+        """One explicit step that also leaves the next step's stable time
+        steps (mcfd_explicit_step_next): per cell into ``next_dt_cells``
+        and / or their minimum with ``time_limit`` into ``next_dt_min``.
+        ``primitive_current``: the handle's primitive buffer holds the
+        primitive of U (as the previous step left it)."""
+        _check_state(U, self.n_cells, "U")
+        if dt.dtype != torch.float64 or not dt.is_cuda or dt.numel() not in (1, self.n_cells):
+            raise ValueError("dt must be a CUDA float64 tensor with 1 or n_cells elements")
+        for name, t, n in (("next_dt_min", next_dt_min, 1), ("next_dt_cells", next_dt_cells, self.n_cells)):
+            if t is not None and (t.dtype != torch.float64 or not t.is_cuda or t.numel() != n):
+                raise ValueError(f"{name} must be a CUDA float64 tensor with {n} elements")
+        per_cell = int(dt.numel() == self.n_cells and self.n_cells != 1)
+        self.lib.check(self.lib.mcfd_explicit_step_next(
+            self.handle, C.byref(cfg), int(scheme), U.data_ptr(), dt.data_ptr(), per_cell, int(primitive_current),
+            next_dt_cells.data_ptr() if next_dt_cells is not None else None,
+            next_dt_min.data_ptr() if next_dt_min is not None else None, float(time_limit), _stream_ptr()),
+            "mcfd_explicit_step_next")
+
     def residual_sumsq(self, R: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         _check_state(R, self.n_cells, "R")
         sums = torch.empty(4, dtype=torch.float64, device=self.device) if out is None else out

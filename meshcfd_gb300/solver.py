@@ -51,10 +51,18 @@ class SolverResult:
 
 def run_explicit(geom: DeviceGeometry, settings, U: torch.Tensor, *, start_time: float = 0.0,
                  step_offset: int = 0, progress_callback=None, cancel_callback=None,
-                 solution_callback=None, solution_interval: int = 1, mode: str = "exact",
+                 solution_callback=None, solution_interval: int = 1, mode: str = "fast",
                  solver_error=SolverError, check_every: int = 1, final_residual: bool = True):
     """Advance ``U`` (device (C,4) float64, modified in place) like the
-    reference's explicit loop.  Returns a :class:`SolverResult`."""
+    reference's explicit loop.  Returns a :class:`SolverResult`.
+
+    ``mode``: "fast" (the default) keeps exact IEEE arithmetic in the
+    reference's operation order and takes each cell's limiter minimum through
+    its smallest ratio (three divisions per variable instead of one per
+    limiter entry; the same factor for Barth-Jespersen and Minmod, and for the
+    smooth limiters unless two candidates round to a last-place tie); "exact"
+    evaluates every limiter entry as the reference does; "fma" contracts
+    products (outside the 1e-12 bar on fine meshes)."""
     cpu_start = thread_time()
     if settings.time_integration not in TIME_SCHEME_CODES:
         raise NotImplementedError(f"{settings.time_integration} is not an explicit integrator")

@@ -144,12 +144,15 @@ def test_implicit_conserves_periodic_state(cuda_device):
     np.testing.assert_allclose(after, before, rtol=1e-10, atol=1e-10)
 
 
-def test_bump_channel_implicit_steps_match_the_oracle(cuda_device):
+@pytest.mark.parametrize("nx,ny,n_steps", ((32, 16, 3), (128, 64, 1)))
+def test_bump_channel_implicit_steps_match_the_oracle(cuda_device, nx, ny, n_steps):
     """The bump-channel recipe (circular-arc bump, rows stretched toward the
     wall, slip wall, far field and pressure outlet; Roe, MUSCL linear with
     Barth-Jespersen, implicit Euler with local steps at CFL 200, GMRES(30) to
-    1e-3 with LU-SGS) on a 32x16 mesh: three implicit steps on the device
-    against the oracle's restatement with SciPy's GMRES."""
+    1e-3 with LU-SGS) on a 32x16 mesh (three implicit steps) and a 128x64
+    mesh (one step: ten time-step halvings, ~80 Newton and ~2,000 GMRES
+    iterations, 191 sweep levels) on the device against the oracle's
+    restatement with SciPy's GMRES."""
     import torch
     from meshcfd_gb300.device import DeviceGeometry
     from meshcfd_gb300.geometry import build_geometry
@@ -158,23 +161,23 @@ def test_bump_channel_implicit_steps_match_the_oracle(cuda_device):
     from oracle.implicit import ImplicitOracle
     from oracle.oracle import Oracle
 
-    case, P = bump_case(32, 16)
+    case, P = bump_case(nx, ny)
     s = case.numerics
     g = build_geometry(case.mesh, case)
     assert len(g.wall_faces) and len(g.far_field_faces) and len(g.pressure_outlet_faces)
     orc, imp = Oracle(g), ImplicitOracle(g)
     U0 = orc.conservative(P, s.gamma)
     U_ref = U0.copy()
-    for _ in range(3):
+    for _ in range(n_steps):
         dt = orc.stable_time_steps(orc.primitive(U_ref, s.gamma), s)
         U_ref, _ = imp.step(U_ref, dt, s)
     dg = DeviceGeometry(g)
     U = torch.as_tensor(U0, device=cuda_device)
-    _, steps, _ = run_implicit(dg, s, U, max_steps=3)
-    assert steps == 3
+    _, steps, _ = run_implicit(dg, s, U, max_steps=n_steps)
+    assert steps == n_steps
     err = np.abs(U.cpu().numpy() - U_ref).max() / np.abs(U_ref).max()
-    print(f"bump 32x16, 3 implicit steps: max relative difference {err:.2e}")
-    assert err <= 1e-12, err  # measured 1.6e-16: the GMRES iterates track SciPy's
+    print(f"bump {nx}x{ny}, {n_steps} implicit steps: max relative difference {err:.2e}")
+    assert err <= 1e-12, err  # measured 1.6e-16 on 32x16: the GMRES iterates track SciPy's
 
 
 def _prepare_on(g, s, P, cuda_device):
