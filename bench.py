@@ -82,9 +82,11 @@ def parse(argv=None):
                     help="bump workload: file rewritten with the line so far after every step")
     ap.add_argument("--bump-oracle", action="store_true",
                     help="bump workload: also run the oracle's SciPy restatement of the same step and compare")
-    ap.add_argument("--numbering", choices=("generator", "random", "rcm"), default="generator",
+    ap.add_argument("--numbering", choices=("generator", "random", "rcm", "random-rcm-cells"), default="generator",
                     help="vortex workloads: cell and face ids as generated, randomly permuted (as a mesh file "
-                         "may number them), or renumbered by reverse Cuthill-McKee")
+                         "may number them), renumbered by reverse Cuthill-McKee, or randomly permuted and then "
+                         "its cells (not its faces) renumbered by reverse Cuthill-McKee (meshes.renumber_cells, "
+                         "which keeps every cell's results bit for bit)")
     return ap.parse_args(argv)
 
 
@@ -102,7 +104,8 @@ def _sample_case(name, n, host=None, numbering="generator"):
     at ``n`` x ``n`` quads when given, with the mesh's ids as generated,
     randomly permuted (seed 7) or renumbered by reverse Cuthill-McKee."""
     from meshcfd_gb300.geometry import build_geometry
-    from meshcfd_gb300.meshes import cell_centroids, permute_mesh, reverse_cuthill_mckee, vortex_case, vortex_primitive
+    from meshcfd_gb300.meshes import (cell_centroids, permute_mesh, renumber_cells, reverse_cuthill_mckee,
+                                      vortex_case, vortex_primitive)
 
     w = WORKLOADS[name]
     case, _ = vortex_case(n or w["n"], split=w["split"])
@@ -112,6 +115,13 @@ def _sample_case(name, n, host=None, numbering="generator"):
                                  rng.permutation(len(case.mesh.faces)))
     elif numbering == "rcm":
         case.mesh = permute_mesh(case.mesh, *reverse_cuthill_mckee(case.mesh))
+    elif numbering == "random-rcm-cells":
+        rng = np.random.default_rng(7)
+        case.mesh = permute_mesh(case.mesh, rng.permutation(len(case.mesh.cells)),
+                                 rng.permutation(len(case.mesh.faces)))
+        case.mesh, cell_order = renumber_cells(case.mesh)
+        g = build_geometry(case.mesh, case, host=host)
+        return case, case.numerics, g, vortex_primitive(cell_centroids(case.mesh))
     g = build_geometry(case.mesh, case, host=host)
     return case, case.numerics, g, vortex_primitive(cell_centroids(case.mesh))
 
