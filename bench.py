@@ -50,6 +50,10 @@ def parse(argv=None):
     ap.add_argument("--checkpoint-every", type=int, default=20)
     ap.add_argument("--batch-adjoint-steps", type=int, default=20)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--launch-shapes", default="",
+                    help="set the stage kernels' launch shapes instead of autotuning: reconstruction threads, flux "
+                         "threads, flux faces per thread, gather threads, per-variable reconstruction (0/1), "
+                         "e.g. 64,64,1,64,1 (mcfd_set_launch_shapes)")
     ap.add_argument("--batch-adjoint-checkpoint", type=int, default=5)
     ap.add_argument("--batch-cases", type=int, default=256)
     ap.add_argument("--graph-steps", type=int, default=10)
@@ -470,7 +474,14 @@ class ExplicitRun:
         native = _lib.native()
         stream = torch.cuda.current_stream()
         self.reset()
-        self.tuned = self.dg.autotune(self.U, self.cfg) if not self.args.no_autotune else None
+        if self.args.launch_shapes:
+            shapes = [int(v) for v in self.args.launch_shapes.split(",")]
+            self.dg.lib.check(self.dg.lib.mcfd_set_launch_shapes(self.dg.handle, (C.c_int32 * 5)(*shapes)),
+                              "mcfd_set_launch_shapes")
+            self.tuned = dict(zip(("reconstruct_threads", "flux_threads", "flux_faces_per_thread", "gather_threads",
+                                   "reconstruct_per_variable"), shapes))
+        else:
+            self.tuned = self.dg.autotune(self.U, self.cfg) if not self.args.no_autotune else None
         self.reset()
         for _ in range(warmup):
             self.step()
@@ -504,7 +515,7 @@ class ExplicitRun:
             v["share"] = v["ms_total"] / total_ms
         return {"value": value, "ms_per_step": ms_per_step, "launches": int(launches),
                 "clocks": sampler.summary() if clocks else None, "kernels": kernels,
-                "roofline": roofline_for(self.name, self.g, kernels, ms_per_step, self.args.mode),
+                "roofline": roofline_for(self.name, self.g, kernels, ms_per_step, self.args.mode) if kernels else None,
                 "autotune": self.tuned}
 
     def vs_oracle(self, steps):
