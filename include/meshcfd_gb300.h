@@ -558,6 +558,37 @@ int mcfd_host_parabolic_stencil(int64_t n_cells, int64_t n_entries, const int64_
                                 int64_t* out_neighbours, double* out_dx, double* out_dy,
                                 int64_t* out_count);
 
+/*
+ * The geometry build's numeric loops on the device (device pointers, int64
+ * indices; the same arrays as the host build bit for bit): cell centroids
+ * and areas (mcfd_host_cell_geometry's sums, solver.py:1655-1676); face
+ * centres, outward unit normals and lengths (mcfd_host_face_geometry,
+ * solver.py:1678-1695); the least-squares gradient offsets, coefficients
+ * (solver.py:2004-2078) of an entry list whose first n_interior_entries
+ * entries are the interior faces' (owner, neighbour) pairs and the rest the
+ * periodic pairs' (periodic_shifts [pairs][2]), with cell_entry_ptr /
+ * cell_entry_order the entries of each cell in entry order and scratch
+ * [2 n_entries + 3 n_cells] doubles; and the limiter-entry offsets (face
+ * centre minus cell centre, solver.py:2098-2105).  bad_cell / bad_face:
+ * device uint64 holding UINT64 / INT64 max on entry, left at the smallest
+ * invalid cell (zero / non-finite area) or face (zero / non-finite length).
+ * No counterpart as such in the reference (its loops run in Python).
+ */
+int mcfd_device_cell_geometry(int64_t n_cells, const int64_t* cell_offsets, const int64_t* cell_nodes,
+                              const double* points, double* centers, double* areas, uint64_t* bad_cell,
+                              void* stream);
+int mcfd_device_face_geometry(int64_t n_faces, const int64_t* face_nodes, const double* points,
+                              const double* centers, const int64_t* owners, double* face_centers, double* normals,
+                              double* lengths, uint64_t* bad_face, void* stream);
+int mcfd_device_gradient_coefficients(int64_t n_cells, int64_t n_entries, int64_t n_interior_entries,
+                                      const int64_t* sources, const int64_t* neighbours, const double* centers,
+                                      const double* periodic_shifts, const int64_t* cell_entry_ptr,
+                                      const int64_t* cell_entry_order, double* dx, double* dy, double* cx,
+                                      double* cy, double* scratch, void* stream);
+int mcfd_device_limiter_offsets(int64_t n_slots, const int64_t* slot_faces, const int64_t* slot_cells,
+                                const double* face_centers, const double* centers, double* dx, double* dy,
+                                void* stream);
+
 #ifdef __cplusplus
 }
 #endif

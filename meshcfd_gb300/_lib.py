@@ -132,6 +132,11 @@ SIGNATURES = {
     "mcfd_ieee_mul": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp]),
     "mcfd_host_cell_geometry": (c_i32, [c_i64, P_i64, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
     "mcfd_host_face_geometry": (c_i32, [c_i64, P_i64, P_dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
+    "mcfd_device_cell_geometry": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_device_face_geometry": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_device_gradient_coefficients": (c_i32, [c_i64, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                                  c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "mcfd_device_limiter_offsets": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "mcfd_host_parabolic_stencil": (c_i32, [c_i64, c_i64, P_i64, P_i64, P_dbl, P_dbl, c_dbl, c_i64, P_i64, P_i64,
                                             P_dbl, P_dbl, P_i64]),
 }

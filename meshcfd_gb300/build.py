@@ -43,6 +43,7 @@ UNITS = [
     ("mcfd_api.cu", []),
     ("mcfd_noalloc.cu", ["-fmad=false"]),
     ("mcfd_stencil.cu", []),
+    ("mcfd_geometry.cu", ["-fmad=false"]),
 ]
 
 

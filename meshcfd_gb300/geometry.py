@@ -473,44 +473,56 @@ def build_geometry(mesh: FiniteVolumeMesh, case, host=None) -> Geometry:
     # owner entry then the neighbour entry, then per periodic pair.
     io = owners[interior_faces]
     ineigh = neighbours[interior_faces]
-    delta = centers[ineigh] - centers[io]
     pa_own = owners[periodic_a]
     pb_own = owners[periodic_b]
-    pdelta = (centers[pb_own] - shifts) - centers[pa_own]
     src = np.concatenate((np.column_stack((io, ineigh)).ravel(), np.column_stack((pa_own, pb_own)).ravel()))
     nbr = np.concatenate((np.column_stack((ineigh, io)).ravel(), np.column_stack((pb_own, pa_own)).ravel()))
-    gdx = np.concatenate((np.column_stack((delta[:, 0], -delta[:, 0])).ravel(), np.column_stack((pdelta[:, 0], -pdelta[:, 0])).ravel()))
-    gdy = np.concatenate((np.column_stack((delta[:, 1], -delta[:, 1])).ravel(), np.column_stack((pdelta[:, 1], -pdelta[:, 1])).ravel()))
     src = src.astype(np.int64)
     nbr = nbr.astype(np.int64)
-
-    # Least-squares coefficients (solver.py:2050-2078).
-    dist2 = gdx * gdx + gdy * gdy
-    weights = 1.0 / np.maximum(dist2, 1e-300)
-    wdx = weights * gdx
-    wdy = weights * gdy
-    mxx = np.zeros(n_cells)
-    mxy = np.zeros(n_cells)
-    myy = np.zeros(n_cells)
-    np.add.at(mxx, src, wdx * gdx)
-    np.add.at(mxy, src, wdx * gdy)
-    np.add.at(myy, src, wdy * gdy)
-    det = mxx * myy - mxy * mxy
-    valid = det > 1e-14 * np.maximum(mxx * myy, 1e-300)
-    ixx = np.zeros(n_cells)
-    ixy = np.zeros(n_cells)
-    iyy = np.zeros(n_cells)
-    ixx[valid] = myy[valid] / det[valid]
-    ixy[valid] = -mxy[valid] / det[valid]
-    iyy[valid] = mxx[valid] / det[valid]
-    cx = ixx[src] * wdx + ixy[src] * wdy
-    cy = ixy[src] * wdx + iyy[src] * wdy
-
-    # Limiter entries (solver.py:2098-2105): every face's owner, then every
-    # interior face's neighbour.
     lim_cells = np.concatenate((owners, ineigh))
-    lim_dx = np.concatenate((face_centers[:, 0] - centers[owners, 0], face_centers[interior_faces, 0] - centers[ineigh, 0]))
-    lim_dy = np.concatenate((face_centers[:, 1] - centers[owners, 1], face_centers[interior_faces, 1] - centers[ineigh, 1]))
+    device_numeric = getattr(lib, "gradient_and_limiter_offsets", None)
+    if device_numeric is not None:
+        # the offsets, weights, moment sums, coefficients and limiter offsets
+        # below, computed by the library's kernels in the same order
+        gdx, gdy, cx, cy, lim_dx, lim_dy = device_numeric(
+            n_cells, src, nbr, 2 * len(interior_faces), shifts, centers, face_centers,
+            np.concatenate((np.arange(n_faces, dtype=np.int64), interior_faces)), lim_cells)
+    else:
+        delta = centers[ineigh] - centers[io]
+        pdelta = (centers[pb_own] - shifts) - centers[pa_own]
+        gdx = np.concatenate((np.column_stack((delta[:, 0], -delta[:, 0])).ravel(),
+                              np.column_stack((pdelta[:, 0], -pdelta[:, 0])).ravel()))
+        gdy = np.concatenate((np.column_stack((delta[:, 1], -delta[:, 1])).ravel(),
+                              np.column_stack((pdelta[:, 1], -pdelta[:, 1])).ravel()))
+
+        # Least-squares coefficients (solver.py:2050-2078).
+        dist2 = gdx * gdx + gdy * gdy
+        weights = 1.0 / np.maximum(dist2, 1e-300)
+        wdx = weights * gdx
+        wdy = weights * gdy
+        mxx = np.zeros(n_cells)
+        mxy = np.zeros(n_cells)
+        myy = np.zeros(n_cells)
+        np.add.at(mxx, src, wdx * gdx)
+        np.add.at(mxy, src, wdx * gdy)
+        np.add.at(myy, src, wdy * gdy)
+        det = mxx * myy - mxy * mxy
+        valid = det > 1e-14 * np.maximum(mxx * myy, 1e-300)
+        ixx = np.zeros(n_cells)
+        ixy = np.zeros(n_cells)
+        iyy = np.zeros(n_cells)
+        ixx[valid] = myy[valid] / det[valid]
+        ixy[valid] = -mxy[valid] / det[valid]
+        iyy[valid] = mxx[valid] / det[valid]
+        cx = ixx[src] * wdx + ixy[src] * wdy
+        cy = ixy[src] * wdx + iyy[src] * wdy
+
+        # Limiter entries (solver.py:2098-2105): every face's owner, then every
+        # interior face's neighbour.
+        lim_dx = np.concatenate((face_centers[:, 0] - centers[owners, 0],
+                                 face_centers[interior_faces, 0] - centers[ineigh, 0]))
+        lim_dy = np.concatenate((face_centers[:, 1] - centers[owners, 1],
+                                 face_centers[interior_faces, 1] - centers[ineigh, 1]))
 
     parabolic = (np.empty(0, dtype=np.int64), np.empty(0, dtype=np.int64), np.empty(0), np.empty(0))
     if case.numerics.reconstruction == "MUSCL parabolic":

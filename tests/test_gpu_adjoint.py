@@ -54,7 +54,8 @@ def test_vjp_matches_torch_autograd(cuda_device, kind, n, flux, recon, limiter):
     (ubar,) = torch.autograd.grad(R, U, torch.as_tensor(lam, device=cuda_device))
     fbar = torch.zeros(max(dg.n_far_field, 1), 4, dtype=torch.float64, device=cuda_device)
     ubar2 = torch.empty_like(ubar)
-    assert dg.lib.mcfd_vjp(dg.handle, C.byref(cfg), U.data_ptr(), torch.as_tensor(lam, device=cuda_device).data_ptr(),
+    lam_d = torch.as_tensor(lam, device=cuda_device)
+    assert dg.lib.mcfd_vjp(dg.handle, C.byref(cfg), U.data_ptr(), lam_d.data_ptr(),
                            ubar2.data_ptr(), fbar.data_ptr(), torch.cuda.current_stream().cuda_stream) == 0
     dg.check_status()
     assert torch.equal(ubar, ubar2)

@@ -89,8 +89,8 @@ def test_jvp_vjp_and_torch_autograd(cuda_device, flux):
     stream = torch.cuda.current_stream().cuda_stream
     U = torch.as_tensor(U0, device=cuda_device)
     jv = torch.empty_like(U)
-    assert dg.lib.mcfd_jvp(dg.handle, C.byref(cfg), U.data_ptr(), torch.as_tensor(v, device=cuda_device).data_ptr(),
-                           jv.data_ptr(), stream) == 0
+    v_d = torch.as_tensor(v, device=cuda_device)
+    assert dg.lib.mcfd_jvp(dg.handle, C.byref(cfg), U.data_ptr(), v_d.data_ptr(), jv.data_ptr(), stream) == 0
     Ug = U.clone().requires_grad_(True)
     (ResidualFunction.apply(Ug, dg, cfg) * torch.as_tensor(lam, device=cuda_device)).sum().backward()
     dg.check_status()
