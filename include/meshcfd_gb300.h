@@ -420,15 +420,16 @@ int mcfd_lusgs_apply(mcfd_geom* geom, const double* v, double* x, void* stream);
  * 2, 3, 4: one block of 512, 1024 or 256 threads whose rows wait only for
  * the rows they read (no barrier per level, chunks of consecutive levels in
  * flight together); 5: as 2 with the rows' products on the integer pipe
- * (the same IEEE products); 8 or 16 a
+ * (the same IEEE products); 6: as 2 with one thread per (row, component),
+ * chunks of at most 8 rows; 8 or 16 a
  * thread-block cluster of that many blocks sharing their latest solutions in
  * distributed shared memory, a cluster barrier per level.  0 restores the
  * defaults (wide_level 16384, engine 2); 8 or 16 returns MCFD_E_UNSUPPORTED
  * where the device cannot run that cluster size.  Results do not depend on
  * it.  No counterpart in the reference. */
 int mcfd_implicit_set_sweep(mcfd_geom* geom, int32_t wide_level, int32_t engine);
-/* Rows per chunk of the per-row-wait sweeps (engines 2-4): 1..32, 0 restores
- * the default (32).  A chunk is a run of consecutive rows of one level taken
+/* Rows per chunk of the per-row-wait sweeps (engines 2-6): 1..32 (at most 8
+ * for engine 6), 0 restores the default (32; 8 for engine 6).  A chunk is a run of consecutive rows of one level taken
  * by one warp.  Results do not depend on it.  No counterpart in the
  * reference. */
 int mcfd_implicit_set_chunk(mcfd_geom* geom, int32_t rows);

@@ -1424,7 +1424,7 @@ int mcfd_lusgs_apply(mcfd_geom* h, const double* v, double* x, void* stream) {
 }
 
 int mcfd_implicit_set_sweep(mcfd_geom* h, int32_t wide_level, int32_t engine) {
-  if (!h || wide_level < 0 || (engine < 0 || (engine > 5 && engine != 8 && engine != 16)))
+  if (!h || wide_level < 0 || (engine < 0 || (engine > 6 && engine != 8 && engine != 16)))
     return MCFD_E_ARG;
   int c = ensure_implicit(h);
   if (c) return c;

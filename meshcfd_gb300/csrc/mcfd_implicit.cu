@@ -459,6 +459,128 @@ __global__ void __launch_bounds__(NT, 1) k_lusgs_dataflow(SweepDev a, const int2
   }
 }
 
+// The same per-row-wait sweep with one lane per (row, component): a chunk of
+// at most 8 rows takes a warp, lane 4 r + v solving component v of the
+// chunk's row r.  The FP64 work of a level is the same number of warp
+// instructions as with one lane per row, but it is spread over four times as
+// many warps (all four SM sub-partitions take part on narrow levels), and a
+// row's dependent chain is its own component's products and differences
+// only, so the time from a row's last input to its solution is about a
+// quarter.  The ring, tags, throttle and bounds are k_lusgs_dataflow's; a
+// row's tag is written once all four of its components are stored.  The
+// component arithmetic is sweep_solve's, so the bits are the same.
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_lusgs_dataflow_comp(SweepDev a, const int2* __restrict__ chunks, int k0,
+                                                               int k1, DevStatus* status) {
+  constexpr int kFlowWarps = NT / 32;
+  extern __shared__ double flow_smem[];
+  double* ring = flow_smem;                                                   // [kFlowRing][4]
+  volatile int* tag = reinterpret_cast<volatile int*>(ring + 4 * kFlowRing);  // [kFlowRing]
+  __shared__ int prog[kFlowWarps];
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rl = lane >> 2, v = lane & 3;  // row of the chunk, component
+  for (int i = threadIdx.x; i < kFlowRing; i += blockDim.x) tag[i] = -1;
+  if (lane == 0) prog[warp] = k0 + warp < k1 ? chunks[k0 + warp].x : INT_MAX;
+  if (threadIdx.x == 0) abort_flag = 0;
+  __syncthreads();
+  volatile int* vprog = prog;
+  volatile int* vabort = &abort_flag;
+  const int base = chunks[k0].x;
+  for (int k = k0 + warp; k < k1; k += kFlowWarps) {
+    const int2 ch = chunks[k];
+    const int start = ch.x;
+    const bool have = rl < ch.y;
+    const int p = start + rl;
+    // the row's data (independent of the solutions)
+    int i = 0, n = 0;
+    double r = 0.0, dg = 1.0, vk[kSweepPack];
+    int cp[kSweepPack], cc[kSweepPack];
+    unsigned long long rx = 0;
+    if (have) {
+      i = a.pos_cell[p];
+      n = a.pk_cnt[p];
+#pragma unroll
+      for (int q = 0; q < kSweepPack; ++q) {
+        vk[q] = a.pk_val[(size_t)p * kSweepPack + q];
+        cp[q] = a.pk_pos[(size_t)p * kSweepPack + q];
+        cc[q] = a.pk_cell[(size_t)p * kSweepPack + q];
+      }
+      dg = a.pk_diag[p];
+      rx = recip_fixed(dg);
+      const double in = a.in[4 * (size_t)i + v];
+      r = a.backward ? a.pk_dc[p] * in : in;
+    }
+    if (start - kFlowAhead > base) {  // warp-uniform loop, as in k_lusgs_dataflow
+      long long spins = 0;
+      while (true) {
+        const int pv = lane < kFlowWarps ? vprog[lane] : INT_MAX;
+        if (__reduce_min_sync(0xffffffffu, pv) >= start - kFlowAhead) break;
+        if (__any_sync(0xffffffffu, ++spins > kFlowSpinLimit || *vabort)) {
+          if (lane == 0) *vabort = 1;
+          break;
+        }
+      }
+    }
+    if (__any_sync(0xffffffffu, *vabort)) break;
+    const int ring_lo = max(start - kFlowRingWindow, base);
+    bool ok = true;
+    if (have) {
+      auto wait_tag = [&](int dep) {
+        if (dep < ring_lo) return;
+        long long spins = 0;
+        while (tag[dep & (kFlowRing - 1)] != dep) {
+          if (++spins > kFlowSpinLimit || *vabort) {
+            ok = false;
+            return;
+          }
+        }
+      };
+#pragma unroll
+      for (int q = 0; q < kSweepPack; ++q)
+        if (q < n && ok) wait_tag(cp[q]);
+      if (n > kSweepPack)
+        for (int j = a.ent_ptr[p] + kSweepPack, j1 = a.ent_ptr[p + 1]; j < j1 && ok; ++j) wait_tag(a.ent_pos[j]);
+    }
+    if (__any_sync(0xffffffffu, !ok)) {
+      if (lane == 0) *vabort = 1;
+      break;
+    }
+    __threadfence_block();
+    if (have) {
+      double acc = r;
+#pragma unroll
+      for (int q = 0; q < kSweepPack; ++q) {
+        if (q < n) {
+          const double x = cp[q] >= ring_lo ? ring[4 * (cp[q] & (kFlowRing - 1)) + v] : a.out[4 * (size_t)cc[q] + v];
+          acc = acc - vk[q] * x;
+        }
+      }
+      if (n > kSweepPack) {
+        for (int j = a.ent_ptr[p] + kSweepPack, j1 = a.ent_ptr[p + 1]; j < j1; ++j) {
+          const int dep = a.ent_pos[j];
+          const double x = dep >= ring_lo ? ring[4 * (dep & (kFlowRing - 1)) + v] : a.out[4 * (size_t)a.ent_cell[j] + v];
+          acc = acc - a.rval[a.ent_val[j]] * x;
+        }
+      }
+      const double res = div_rn_recip(acc, dg, rx);
+      a.out[4 * (size_t)i + v] = res;
+      ring[4 * (p & (kFlowRing - 1)) + v] = res;
+    }
+    __threadfence_block();  // each lane's component before the row's tag
+    __syncwarp();
+    __threadfence_block();
+    if (have && v == 0) tag[p & (kFlowRing - 1)] = p;
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      vprog[warp] = k + kFlowWarps < k1 ? chunks[k + kFlowWarps].x : INT_MAX;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && abort_flag) atomicOr(&status->code, MCFD_S_SWEEP_TIMEOUT);
+}
+
 // One wide level over the whole grid (earlier levels finished in earlier
 // launches on the same stream).
 __global__ void __launch_bounds__(kBlock) k_lusgs_level(SweepDev a, int b, int e) {
@@ -901,6 +1023,8 @@ static void sweep_schedule(SweepPlan& pl, int wide) {
 void implicit_set_wide_level(ImplicitState& st, int wide, int engine) {
   st.wide_level = wide > 0 ? wide : kWideLevel;
   st.engine = engine > 0 ? engine : kDefaultEngine;
+  // the per-component sweep takes chunks of at most 8 rows
+  if (st.engine == kSweepDataflowComponents && st.chunk_rows > 8) implicit_set_chunk(st, 8);
   sweep_schedule(st.fwd, st.wide_level);
   sweep_schedule(st.bwd, st.wide_level);
   st.inner_key = -1;  // the captured loop holds the old launches
@@ -921,7 +1045,9 @@ static cudaError_t sweep_chunks(SweepPlan& pl, int rows) {
 }
 
 cudaError_t implicit_set_chunk(ImplicitState& st, int rows) {
-  const int r = rows > 0 ? rows : kFlowChunk;
+  int r = rows > 0 ? rows : kFlowChunk;
+  if (st.engine == kSweepDataflowComponents && r > 8) r = 8;  // a warp holds 8 rows of 4 components
+  st.chunk_rows = r;
   cudaError_t e = sweep_chunks(st.fwd, r);
   if (e == cudaSuccess) e = sweep_chunks(st.bwd, r);
   st.inner_key = -1;  // the captured loop holds the old chunk ranges
@@ -1106,7 +1232,7 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   for (SweepPlan* pl : {&st.fwd, &st.bwd}) {  // room for chunks of one row
     if (e == cudaSuccess) e = cudaMalloc((void**)&pl->chunks, (size_t)std::max(C, 1) * sizeof(int2));
     if (e == cudaSuccess) st.owned.push_back(pl->chunks);
-    if (e == cudaSuccess) e = sweep_chunks(*pl, kFlowChunk);
+    if (e == cudaSuccess) e = sweep_chunks(*pl, kDefaultEngine == kSweepDataflowComponents ? 8 : kFlowChunk);
   }
   st.wide_level = kWideLevel;
   sweep_schedule(st.fwd, st.wide_level);
@@ -1150,6 +1276,7 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   // than the FP64 work they spread).  The cluster sweeps stay selectable
   // where the device can run them (8: portable; 16: non-portable).
   st.engine = kDefaultEngine;
+  st.chunk_rows = kDefaultEngine == kSweepDataflowComponents ? 8 : kFlowChunk;
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)kFlowSmemBytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1157,6 +1284,8 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)kFlowSmemBytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kFlowSmemBytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow_comp<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)kFlowSmemBytes);
   st.cluster8_ok = false;
   if (e == cudaSuccess &&
@@ -1256,6 +1385,9 @@ static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const dou
     } else if (l.wavefront && st.engine == kSweepDataflowIntMul) {
       const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
       k_lusgs_dataflow<512, true><<<1, 512, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);
+    } else if (l.wavefront && st.engine == kSweepDataflowComponents) {
+      const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
+      k_lusgs_dataflow_comp<512><<<1, 512, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);
     } else if (l.wavefront && st.engine == kSweepDataflowNarrow) {
       const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
       k_lusgs_dataflow<256, false><<<1, 256, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);

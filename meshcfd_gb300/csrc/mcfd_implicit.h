@@ -50,6 +50,7 @@ enum SweepEngine {
   kSweepDataflowWide = 3,  // 1024 threads
   kSweepDataflowNarrow = 4,  // 256 threads
   kSweepDataflowIntMul = 5,  // 512 threads, the row's products on the integer pipe
+  kSweepDataflowComponents = 6,  // 512 threads, one lane per (row, component), chunks of 8 rows
   kSweepCluster8 = 8,
   kSweepCluster16 = 16
 };
@@ -110,6 +111,7 @@ struct ImplicitState {
   SweepPlan fwd, bwd;
   int wide_level = 0;  // levels wider than this get a grid launch each
   int engine = 0;      // how a run of narrow levels is swept (SweepEngine)
+  int chunk_rows = 32;  // rows per chunk of the per-row-wait sweeps
   bool cluster8_ok = false, cluster16_ok = false;
   DevStatus* status = nullptr;  // the geometry's status word (sweep time-outs)
   // values and vectors (device)
