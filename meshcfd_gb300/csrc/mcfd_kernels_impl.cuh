@@ -739,31 +739,49 @@ __device__ __forceinline__ void gather_cell(const DevGeom& g, const double* P, c
   }
 }
 
-// DT: the stage also computes the stable time steps of its new state from
-// the primitive it has just recovered (cell_time_step, the same bits as
-// k_time_steps on that primitive), which saves the time-step pass over the
-// state of the next step.
-template <int SHAPE, bool EXTRAS, bool DT>
+template <int SHAPE, bool EXTRAS>
 __global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
                                                    const double* __restrict__ flux, double gamma,
                                                    double ax, double ay, StageProgram prog) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if constexpr (!DT) {
-    if (i < g.n_cells) gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i);
-  } else {
-    const bool active = i < g.n_cells;
-    double dt = __longlong_as_double(0x7ff0000000000000LL);
-    if (active) {
-      St4 q;
-      gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i, &q);
-      const int c = g.cell_order[i];
-      int bits = 0;
-      dt = cell_time_step(g, c, q, gamma, prog.cfl, nullptr, &bits);
-      if (bits) flag_cell(g.status, bits, c);
-      if (prog.next_dt_cells) prog.next_dt_cells[c] = dt;
-    }
-    if (prog.next_dt_min) block_min_time_step(g.status, dt, active);
+  if (i < g.n_cells) gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i);
+}
+
+// The gather of a step's last stage that also computes the stable time steps
+// of its new state from the primitive it has just recovered (cell_time_step,
+// the same bits as k_time_steps on that primitive), which saves the
+// time-step pass over the state of the next step.
+// Resident 256-thread blocks per SM of the time-step gather: 4 (64
+// registers, a 24-byte spill) measured 0.162 against 0.171 ms per stage on
+// the 1024^2 vortex step (78 registers unbounded, 80 for 3 blocks); 0 leaves
+// the kernel unbounded.
+#ifndef MCFD_GATHER_DT_MIN_BLOCKS
+#define MCFD_GATHER_DT_MIN_BLOCKS 4
+#endif
+#if MCFD_GATHER_DT_MIN_BLOCKS > 0
+#define MCFD_GATHER_DT_BOUND __launch_bounds__(kBlock, MCFD_GATHER_DT_MIN_BLOCKS)
+#else
+#define MCFD_GATHER_DT_BOUND __launch_bounds__(kBlock)
+#endif
+
+template <int SHAPE, bool EXTRAS>
+__global__ void MCFD_GATHER_DT_BOUND k_gather_dt(DevGeom g, const double* __restrict__ P,
+                                                                              const double* __restrict__ flux,
+                                                                              double gamma, double ax, double ay,
+                                                                              StageProgram prog) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < g.n_cells;
+  double dt = __longlong_as_double(0x7ff0000000000000LL);
+  if (active) {
+    St4 q;
+    gather_cell<SHAPE, EXTRAS>(g, P, flux, gamma, ax, ay, prog, i, &q);
+    const int c = g.cell_order[i];
+    int bits = 0;
+    dt = cell_time_step(g, c, q, gamma, prog.cfl, nullptr, &bits);
+    if (bits) flag_cell(g.status, bits, c);
+    if (prog.next_dt_cells) prog.next_dt_cells[c] = dt;
   }
+  if (prog.next_dt_min) block_min_time_step(g.status, dt, active);
 }
 
 // ------------------------------------------------------ one launch per stage
@@ -969,7 +987,7 @@ cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double
   const double ax = cfg.acceleration_x, ay = cfg.acceleration_y;
   count_launch();
   if (prog.out_u && (prog.next_dt_cells || prog.next_dt_min) && !prog.visc_r) {
-#define MCFD_GATHER_DT(SH, EX) k_gather<SH, EX, true><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
+#define MCFD_GATHER_DT(SH, EX) k_gather_dt<SH, EX><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
     if (extras) {
       if (shape == SHAPE_EULER) MCFD_GATHER_DT(SHAPE_EULER, true);
       else if (shape == SHAPE_X_XDTR) MCFD_GATHER_DT(SHAPE_X_XDTR, true);
@@ -982,7 +1000,7 @@ cudaError_t launch_gather(const DevGeom& g, const mcfd_config& cfg, const double
 #undef MCFD_GATHER_DT
     return cudaGetLastError();
   }
-#define MCFD_GATHER(SH, EX) k_gather<SH, EX, false><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
+#define MCFD_GATHER(SH, EX) k_gather<SH, EX><<<b, t, 0, s>>>(g, P, flux, cfg.gamma, ax, ay, prog)
   if (extras) {
     if (shape == SHAPE_EULER) MCFD_GATHER(SHAPE_EULER, true);
     else if (shape == SHAPE_X_XDTR) MCFD_GATHER(SHAPE_X_XDTR, true);
