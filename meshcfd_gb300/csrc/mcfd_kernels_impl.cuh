@@ -443,8 +443,11 @@ __device__ __forceinline__ void reconstruct_variable_fast(const DevGeom& g, cons
   for (int k = 0; k < NS; ++k) recon[4 * (size_t)g.lim_slot[s0 + k] + v] = pv + kmul<MUL_OUTPUT>(phi, inc[k]);
 }
 
+// 6 resident 256-thread blocks per SM (40 registers, a 4-byte spill) for the
+// per-variable reconstruction: 0.394 against 0.406 ms per launch on the
+// 1024^2 vortex (47 registers at 4 blocks); 5 blocks (46 registers) 0.410.
 #ifndef MCFD_RECON_SPLIT_MIN_BLOCKS
-#define MCFD_RECON_SPLIT_MIN_BLOCKS 4
+#define MCFD_RECON_SPLIT_MIN_BLOCKS 6
 #endif
 
 template <int LIMITER>
@@ -739,8 +742,20 @@ __device__ __forceinline__ void gather_cell(const DevGeom& g, const double* P, c
   }
 }
 
+// Resident 256-thread blocks per SM of the gather (0: unbounded): 5 (48
+// registers instead of 54) measured 0.159 against 0.161 ms per stage on the
+// 1024^2 vortex; 6 spills.
+#ifndef MCFD_GATHER_MIN_BLOCKS
+#define MCFD_GATHER_MIN_BLOCKS 5
+#endif
+#if MCFD_GATHER_MIN_BLOCKS > 0
+#define MCFD_GATHER_BOUND __launch_bounds__(kBlock, MCFD_GATHER_MIN_BLOCKS)
+#else
+#define MCFD_GATHER_BOUND __launch_bounds__(kBlock)
+#endif
+
 template <int SHAPE, bool EXTRAS>
-__global__ void __launch_bounds__(kBlock) k_gather(DevGeom g, const double* __restrict__ P,
+__global__ void MCFD_GATHER_BOUND k_gather(DevGeom g, const double* __restrict__ P,
                                                    const double* __restrict__ flux, double gamma,
                                                    double ax, double ay, StageProgram prog) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
