@@ -345,6 +345,36 @@ def _ncu_summary():
     return json.loads(tpath.read_text()) if tpath.exists() else {}
 
 
+def reconstruction_fp64_model(g, issued_per_cell=None):
+    """FP64 operations per cell that the reference's reconstruction takes in
+    its own expression order (_kernels.py:10-67, 71-98, 240-273), counted
+    from the mesh's entry counts, against the FP64-pipe instructions the
+    device kernel issues (ncu).  Per gradient entry and variable: the
+    difference, two products and two sums (5); per limiter entry and
+    variable: the increment grad . r (3), the numerator of the ratio (1), the
+    ratio and the smooth limiter's quotient (2 divisions) and the rest of its
+    rational function (7); per variable the tolerance (1); per face state
+    and variable the increment again, the factor's product and the sum (5).
+    A division issued by the FP64 unit takes ~8.6 FP64-pipe slots on GB300
+    (measured by tests/arith_throughput.cu)."""
+    C = len(g.areas)
+    e = len(g.gradient_sources) / C
+    l = len(g.limiter_cells) / C
+    arithmetic = 4 * (5 * e + (3 + 1 + 7) * l + 1 + 5 * l)
+    divisions = 4 * 2 * l
+    out = {"reference_operations_per_cell": arithmetic + divisions, "of_which_divisions": divisions,
+           "fp64_pipe_slots_per_cell_if_native": arithmetic + 8.6 * divisions,
+           "gradient_entries_per_cell": e, "limiter_entries_per_cell": l,
+           "issued_fp64_instructions_per_cell": issued_per_cell,
+           "how": "divisions and square roots on the integer pipe (the same IEEE results), gradient and face "
+                  "products on the integer pipe, the limiter minimum through each variable's smallest ratio "
+                  "(3 divisions per variable instead of 2 per entry), increments kept for the face states, the "
+                  "first sum term without an FP64 addition"}
+    if issued_per_cell:
+        out["issued_over_reference_operations"] = issued_per_cell / (arithmetic + divisions)
+    return out
+
+
 def roofline_for(name, g, kernels, ms_per_step, mode):
     """The HBM roofline of the dominant kernel (algorithmic bytes of the
     reference 3-pass model per launch over its live launch time), the step's
@@ -385,6 +415,7 @@ def roofline_for(name, g, kernels, ms_per_step, mode):
         "alu_pipe_active_pct_ncu": alu_pipe,
         "issue_active_pct_ncu": issue,
         "fp64": fp64,
+        "fp64_model": reconstruction_fp64_model(g, ipc) if dominant == "reconstruct" else None,
         "note": ("compute bound, not HBM bound: GB300's FP64 pipe issues ~0.5 T instr/s; divisions, square roots "
                  "and part of the products run bit-identically on the integer pipe, and ncu shows the dominant "
                  "kernel sharing the FP64 and ALU pipes (fp64 / alu / issue percentages above); 'fp64' is the "

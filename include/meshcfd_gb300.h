@@ -17,7 +17,7 @@
  *
  * The reference is a Python package whose hot path is the set of module
  * functions cited below; a Python caller binds these entry points with
- * ctypes.
+ * ctypes (meshcfd_gb300/_lib.py holds one binding per entry point).
  */
 #ifndef MESHCFD_GB300_H
 #define MESHCFD_GB300_H
