@@ -471,10 +471,11 @@ class ExplicitRun:
     def step_plain(self):
         """One drop-in step of the state in self.U: primitive, stable time
         step and RK3 stages, each from the state (mcfd_primitive,
-        mcfd_time_steps, mcfd_explicit_step)."""
+        mcfd_time_steps, then mcfd_explicit_step_next starting from that
+        primitive, without a look-ahead)."""
         self.dg.primitive(self.U, self.cfg, out=self.P)
         self.dg.time_steps(self.P, self.cfg, out_min=self.dt)
-        self.dg.explicit_step(self.U, self.cfg, 2, self.dt)
+        self.dg.explicit_step_next(self.U, self.cfg, 2, self.dt, primitive_current=True)
         self.primed = None
 
     def reset(self, cfg=None):

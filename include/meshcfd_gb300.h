@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define MCFD_ABI_VERSION 5
+#define MCFD_ABI_VERSION 6
 
 /* ---- return codes (host-side failures) ---- */
 #define MCFD_OK 0
@@ -286,7 +286,8 @@ int mcfd_explicit_step(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, 
                        const double* dt, int32_t dt_per_cell, void* stream);
 /* mcfd_explicit_step followed by mcfd_time_steps on the new state: the time
  * steps of the next step (per cell into next_dt_cells and / or their minimum
- * with time_limit into next_dt_min, either may be NULL, neither may alias dt)
+ * with time_limit into next_dt_min; either or both may be NULL, neither may
+ * alias dt or U)
  * — computed by the last stage from the primitive it recovers, where they
  * depend on the cell state alone (inviscid, no pressure-inlet or mass-flow
  * patches), else by the time-step pass; the same values either way.
@@ -295,10 +296,20 @@ int mcfd_explicit_step(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, 
  * primitive of U, as the previous explicit step on this handle left it.
  * The reference computes the stable step at the top of each loop iteration
  * (solver.py:437-461); this is the same sequence with the step boundary
- * moved.  No counterpart in the reference. */
+ * moved.  The status bits of these time steps (MCFD_S_TIME_STEP and the
+ * boundary-state bits of the time-step pass) go to a second status word,
+ * read by mcfd_status_fetch_next, so that a caller raises them with the step
+ * that uses the time steps, as the reference does; the bits of the stages,
+ * the new state's primitive recovery included (solver.py:808-810), stay in
+ * the word mcfd_status_fetch reads.  start_residual (NULL or [n_cells][4]):
+ * the first stage also stores the residual of U that it computes, the
+ * reference's `derivative` (solver.py:466-468) on which its progress report
+ * takes the per-component RMS (solver.py:943-950).  No counterpart in the
+ * reference. */
 int mcfd_explicit_step_next(mcfd_geom* geom, const mcfd_config* cfg, int32_t scheme, double* U,
                             const double* dt, int32_t dt_per_cell, int32_t primitive_current,
-                            double* next_dt_cells, double* next_dt_min, double time_limit, void* stream);
+                            double* next_dt_cells, double* next_dt_min, double time_limit,
+                            double* start_residual, void* stream);
 
 /* The reconstruction fields of the reference for primitive P [n_cells][4]:
  * MUSCL linear -> _limited_gradients (solver.py:2294-2319): gradients
@@ -363,6 +374,9 @@ int mcfd_residual_sumsq(mcfd_geom* geom, const double* R, double* sums, void* st
  * Wait for `stream`, then return and clear the accumulated device status.
  */
 int mcfd_status_fetch(mcfd_geom* geom, void* stream, mcfd_status* out);
+/* The same for the status word of the look-ahead time steps that
+ * mcfd_explicit_step_next computes. */
+int mcfd_status_fetch_next(mcfd_geom* geom, void* stream, mcfd_status* out);
 
 /* ---- implicit Euler (solver.py:1185-1567) ---- */
 

@@ -84,7 +84,7 @@ class GeomInfo(C.Structure):
     ]
 
 
-ABI_VERSION = 5  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
+ABI_VERSION = 6  # MCFD_ABI_VERSION of include/meshcfd_gb300.h
 
 # name -> (restype, argtypes); every symbol include/meshcfd_gb300.h declares.
 SIGNATURES = {
@@ -97,7 +97,8 @@ SIGNATURES = {
     "mcfd_residual": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp]),
     "mcfd_time_steps": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_dbl, c_vp]),
     "mcfd_explicit_step": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_vp]),
-    "mcfd_explicit_step_next": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_dbl, c_vp]),
+    "mcfd_explicit_step_next": (c_i32, [c_vp, C.POINTER(Config), c_i32, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_dbl, c_vp,
+                                        c_vp]),
     "mcfd_geom_primitive": (c_vp, [c_vp]),
     "mcfd_geom_stage_state": (c_vp, [c_vp, C.c_int32]),
     "mcfd_reconstruction": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -108,6 +109,7 @@ SIGNATURES = {
     "mcfd_set_launch_shapes": (c_i32, [c_vp, C.POINTER(c_i32)]),
     "mcfd_residual_sumsq": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_status_fetch": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
+    "mcfd_status_fetch_next": (c_i32, [c_vp, c_vp, C.POINTER(Status)]),
     "mcfd_implicit_prepare": (c_i32, [c_vp, C.POINTER(Config), c_vp, c_vp, c_i32, P_dbl, c_vp]),
     "mcfd_implicit_matvec": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
     "mcfd_implicit_set_jacobian": (c_i32, [c_vp, c_i32]),

@@ -28,6 +28,7 @@ struct mcfd_geom {
   void* arena = nullptr;       // one device allocation for geometry + workspace
   size_t arena_bytes = 0;
   DevStatus* status = nullptr;  // inside the arena
+  DevStatus* status_next = nullptr;  // the look-ahead time steps' word (mcfd_explicit_step_next), inside the arena
   DevStatus* host_status = nullptr;  // pinned
   mcfd_geom_info info{};
   ImplicitTopology topo;       // host copy for the implicit path (built lazily)
@@ -659,7 +660,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
          o_gb_len = A.take(bytes_d(gb_len.size()));
   size_t o_dt_ptr = A.take(bytes_i(C + 1)), o_dt_n = A.take(bytes_d(dt_n.size())),
          o_dt_len = A.take(bytes_d(dt_len.size())), o_dt_info = A.take(bytes_i(dt_info.size()));
-  size_t o_status = A.take(sizeof(DevStatus));
+  size_t o_status = A.take(sizeof(DevStatus)), o_status_next = A.take(sizeof(DevStatus));
   size_t o_P = A.take(bytes_d(4 * C)), o_recon = A.take(bytes_d(4 * NL)),
          o_flux = A.take(bytes_d(4 * n_flux));
   size_t o_stage[4];
@@ -740,6 +741,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   DevStatus st0{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(), std::numeric_limits<int>::max(),
                 0x7ff0000000000000ULL};
   put(o_status, &st0, sizeof(st0));
+  put(o_status_next, &st0, sizeof(st0));
   // geometry part only (workspace stays uninitialised)
   err = cudaMemcpy(base, host.data(), o_P, cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMallocHost(&h->host_status, sizeof(DevStatus));
@@ -831,6 +833,7 @@ int mcfd_geom_create(const mcfd_geom_desc* d, mcfd_geom** out) {
   g.dt_info = AT(const int*, o_dt_info);
   g.status = AT(DevStatus*, o_status);
   h->status = g.status;
+  h->status_next = AT(DevStatus*, o_status_next);
   Workspace& w = h->ws;
   w.P = AT(double*, o_P);
   w.recon = AT(double*, o_recon);
@@ -1077,6 +1080,23 @@ int mcfd_residual(mcfd_geom* h, const mcfd_config* cfg, const double* U, double*
   return rc(e);
 }
 
+// The stable time steps of P with their status bits and minimum in *st.
+static int time_steps_into(mcfd_geom* h, DevStatus* st, const mcfd_config* cfg, const double* P, double* dt_cells,
+                           double* dt_min, double time_limit, cudaStream_t s) {
+  DevGeom g = h->g;
+  g.status = st;
+  return rc(timed(h, MCFD_PROF_TIME_STEP, s,
+                  [&] {
+                    cudaError_t r = cudaSuccess;
+                    if (g.n_bc_patches > 0) r = launch_bc_states(g, *cfg, P, nullptr, g.bc_ext_dt, s);
+                    if (r == cudaSuccess && cfg->viscosity_model != MCFD_VISC_INVISCID)
+                      r = launch_viscous_diffusion(g, *cfg, P, h->visc, s);
+                    if (r == cudaSuccess)
+                      r = MCFD_DISPATCH(*cfg, launch_time_steps(g, *cfg, P, dt_cells, dt_min, time_limit, s));
+                    return r;
+                  }));
+}
+
 int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, double* dt_cells,
                     double* dt_min, double time_limit, void* stream) {
   if (!h || !P) return MCFD_E_ARG;
@@ -1084,17 +1104,7 @@ int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, doubl
   if (c) return c;
   if ((c = ensure_viscous(h, cfg))) return c;
   if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  return rc(timed(h, MCFD_PROF_TIME_STEP, s,
-                  [&] {
-                    cudaError_t r = cudaSuccess;
-                    if (h->g.n_bc_patches > 0) r = launch_bc_states(h->g, *cfg, P, nullptr, h->g.bc_ext_dt, s);
-                    if (r == cudaSuccess && cfg->viscosity_model != MCFD_VISC_INVISCID)
-                      r = launch_viscous_diffusion(h->g, *cfg, P, h->visc, s);
-                    if (r == cudaSuccess)
-                      r = MCFD_DISPATCH(*cfg, launch_time_steps(h->g, *cfg, P, dt_cells, dt_min, time_limit, s));
-                    return r;
-                  }));
+  return time_steps_into(h, h->status, cfg, P, dt_cells, dt_min, time_limit, (cudaStream_t)stream);
 }
 
 
@@ -1103,16 +1113,19 @@ int mcfd_time_steps(mcfd_geom* h, const mcfd_config* cfg, const double* P, doubl
 // stage of the previous step left it), so the step starts without
 // recomputing it.  next: the last stage also writes the stable time steps of
 // the new state (NextDt), where the settings allow; the caller completes
-// them otherwise.
+// them otherwise.  start_residual (may be null): the first stage also stores
+// the residual of U it computes (the reference's `derivative`,
+// solver.py:466-468, which its progress report uses).
 struct NextDt {
   double* cells = nullptr;
   int min = 0;
   double cfl = 0.0;
+  DevStatus* status = nullptr;
 };
 
 static cudaError_t explicit_step_impl(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U,
                                       const double* dt, int32_t dt_per_cell, bool primitive_current,
-                                      const NextDt& next, cudaStream_t s) {
+                                      const NextDt& next, double* start_residual, cudaStream_t s) {
   Workspace& w = h->ws;
   cudaError_t e = cudaSuccess;
   if (!primitive_current)
@@ -1131,25 +1144,26 @@ static cudaError_t explicit_step_impl(mcfd_geom* h, const mcfd_config* cfg, int3
       p.next_dt_cells = next.cells;
       p.next_dt_min = next.min;
       p.cfl = next.cfl;
+      p.next_dt_status = next.status;
     }
     e = stage(h, *cfg, p, s);
   };
   double *X1 = w.stage[0], *X2 = w.stage[1], *X3 = w.stage[2], *X4 = w.stage[3];
   switch (scheme) {
     case MCFD_TIME_EULER:  // solver.py:532-533
-      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, U, nullptr);
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, U, start_residual);
       break;
     case MCFD_TIME_RK2:  // solver.py:566-627
-      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, X1, nullptr);
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, X1, start_residual);
       run({term(TERM_X, 0.5, U), term(TERM_X_PLUS_DTR, 0.5, X1)}, U, nullptr);
       break;
     case MCFD_TIME_RK3:  // solver.py:566-567, 676-678, 754-756
-      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, X1, nullptr);
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 1.0, nullptr)}, X1, start_residual);
       run({term(TERM_X, 0.75, U), term(TERM_X_PLUS_DTR, 0.25, X1)}, X2, nullptr);
       run({term(TERM_X, 1.0 / 3.0, U), term(TERM_X_PLUS_DTR, 2.0 / 3.0, X2)}, U, nullptr);
       break;
     default:  // SSPRK(5,4), solver.py:1128-1182
-      run({term(TERM_X, 1.0, U), term(TERM_DTR, 0.391752226571890, nullptr)}, X1, nullptr);
+      run({term(TERM_X, 1.0, U), term(TERM_DTR, 0.391752226571890, nullptr)}, X1, start_residual);
       run({term(TERM_X, 0.444370493651235, U), term(TERM_X, 0.555629506348765, X1),
            term(TERM_DTR, 0.368410593050371, nullptr)}, X2, nullptr);
       run({term(TERM_X, 0.620101851488403, U), term(TERM_X, 0.379898148511597, X2),
@@ -1171,37 +1185,45 @@ int mcfd_explicit_step(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, dou
   if (c) return c;
   if ((c = ensure_viscous(h, cfg))) return c;
   if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
-  return rc(explicit_step_impl(h, cfg, scheme, U, dt, dt_per_cell, false, NextDt{}, (cudaStream_t)stream));
+  return rc(explicit_step_impl(h, cfg, scheme, U, dt, dt_per_cell, false, NextDt{}, nullptr, (cudaStream_t)stream));
 }
 
 int mcfd_explicit_step_next(mcfd_geom* h, const mcfd_config* cfg, int32_t scheme, double* U, const double* dt,
                             int32_t dt_per_cell, int32_t primitive_current, double* next_dt_cells,
-                            double* next_dt_min, double time_limit, void* stream) {
-  if (!h || !U || !dt || (!next_dt_cells && !next_dt_min)) return MCFD_E_ARG;
-  if (next_dt_cells == dt || next_dt_min == dt) return MCFD_E_ARG;  // the stages read dt to the end
+                            double* next_dt_min, double time_limit, double* start_residual, void* stream) {
+  if (!h || !U || !dt) return MCFD_E_ARG;
+  // the stages read dt and U to the end
+  if ((next_dt_cells && (next_dt_cells == dt || next_dt_cells == U)) ||
+      (next_dt_min && (next_dt_min == dt || next_dt_min == U)) ||
+      (start_residual && (start_residual == U || start_residual == dt)))
+    return MCFD_E_ARG;
   int c = check_cfg(cfg);
   if (c) return c;
   if ((c = ensure_viscous(h, cfg))) return c;
   if (scheme < MCFD_TIME_EULER || scheme > MCFD_TIME_RK4) return MCFD_E_ARG;
-  if (!(cfg->cfl > 0.0)) return MCFD_E_ARG;
+  if ((next_dt_cells || next_dt_min) && !(cfg->cfl > 0.0)) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   // the last stage computes the time steps where they depend on the cell
   // state alone (inviscid, no pressure-inlet / mass-flow patches, whose
   // exterior states come from a pass of their own)
+  const bool want = next_dt_cells || next_dt_min;
   const bool fused = cfg->viscosity_model == MCFD_VISC_INVISCID && h->g.n_bc_patches == 0;
   NextDt next;
-  if (fused) {
+  if (want && fused) {
     next.cells = next_dt_cells;
     next.min = next_dt_min != nullptr;
     next.cfl = cfg->cfl;
+    next.status = h->status_next;
   }
-  cudaError_t e = explicit_step_impl(h, cfg, scheme, U, dt, dt_per_cell, primitive_current != 0, next, s);
+  cudaError_t e =
+      explicit_step_impl(h, cfg, scheme, U, dt, dt_per_cell, primitive_current != 0, next, start_residual, s);
   if (e != cudaSuccess) return MCFD_E_CUDA;
-  if (!fused) return mcfd_time_steps(h, cfg, h->ws.P, next_dt_cells, next_dt_min, time_limit, stream);
+  if (!want) return MCFD_OK;
+  if (!fused) return time_steps_into(h, h->status_next, cfg, h->ws.P, next_dt_cells, next_dt_min, time_limit, s);
   if (next_dt_min)
     e = timed(h, MCFD_PROF_TIME_STEP, s, [&] {
       count_launch();
-      return finalize_time_step(h->g.status, next_dt_min, time_limit, s);
+      return finalize_time_step(h->status_next, next_dt_min, time_limit, s);
     });
   return rc(e);
 }
@@ -1213,10 +1235,11 @@ int mcfd_residual_sumsq(mcfd_geom* h, const double* R, double* sums, void* strea
                   [&] { return launch_sumsq(h->g, R, h->ws.partials, h->ws.partial_blocks, sums, s); }));
 }
 
-int mcfd_status_fetch(mcfd_geom* h, void* stream, mcfd_status* out) {
+// Reads and clears one status word (keeping its time-step minimum).
+static int fetch_status(mcfd_geom* h, DevStatus* dev, void* stream, mcfd_status* out) {
   if (!h || !out) return MCFD_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemcpyAsync(h->host_status, h->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaMemcpyAsync(h->host_status, dev, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return MCFD_E_CUDA;
   DevStatus st = *h->host_status;
@@ -1228,11 +1251,19 @@ int mcfd_status_fetch(mcfd_geom* h, void* stream, mcfd_status* out) {
     DevStatus clear{0, std::numeric_limits<int>::max(), std::numeric_limits<int>::max(),
                     std::numeric_limits<int>::max(), st.dt_min_bits};
     *h->host_status = clear;
-    e = cudaMemcpyAsync(h->status, h->host_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s);
+    e = cudaMemcpyAsync(dev, h->host_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return MCFD_E_CUDA;
   }
   return MCFD_OK;
+}
+
+int mcfd_status_fetch(mcfd_geom* h, void* stream, mcfd_status* out) {
+  return fetch_status(h, h ? h->status : nullptr, stream, out);
+}
+
+int mcfd_status_fetch_next(mcfd_geom* h, void* stream, mcfd_status* out) {
+  return fetch_status(h, h ? h->status_next : nullptr, stream, out);
 }
 
 

@@ -141,10 +141,13 @@ struct StageProgram {
   const double* visc_r;  // laminar viscous residual added before the body force, may be null
   // the stable time steps of the new state (out_u), computed by the gather
   // from its primitive: per cell into next_dt_cells (may be null) and, when
-  // next_dt_min, their minimum into the status word (as k_time_steps)
+  // next_dt_min, their minimum into next_dt_status (as k_time_steps).  The
+  // time-step bits go to next_dt_status as well: they belong to the step
+  // that uses these time steps, not to the one that computed them.
   double* next_dt_cells;
   int next_dt_min;
   double cfl;
+  DevStatus* next_dt_status;
 };
 
 struct Workspace {

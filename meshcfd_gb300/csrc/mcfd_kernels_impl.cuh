@@ -793,10 +793,10 @@ __global__ void MCFD_GATHER_DT_BOUND k_gather_dt(DevGeom g, const double* __rest
     const int c = g.cell_order[i];
     int bits = 0;
     dt = cell_time_step(g, c, q, gamma, prog.cfl, nullptr, &bits);
-    if (bits) flag_cell(g.status, bits, c);
+    if (bits) flag_cell(prog.next_dt_status, bits, c);
     if (prog.next_dt_cells) prog.next_dt_cells[c] = dt;
   }
-  if (prog.next_dt_min) block_min_time_step(g.status, dt, active);
+  if (prog.next_dt_min) block_min_time_step(prog.next_dt_status, dt, active);
 }
 
 // ------------------------------------------------------ one launch per stage

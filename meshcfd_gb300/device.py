@@ -208,11 +208,14 @@ class DeviceGeometry:
     def check_status(self, solver_error=SolverError, stream=None) -> None:
         raise_for_status(self.status_code(stream), solver_error)
 
-    def status_code(self, stream=None) -> StatusCode:
+    def status_code(self, stream=None, *, look_ahead: bool = False) -> StatusCode:
         """The device status bits since the last fetch (an int), carrying the
-        name of the lowest failing boundary patch as ``.patch``."""
+        name of the lowest failing boundary patch as ``.patch``.
+        ``look_ahead``: the word of the next step's time steps that
+        :meth:`explicit_step_next` computes (mcfd_status_fetch_next)."""
         st = _lib.Status()
-        self.lib.check(self.lib.mcfd_status_fetch(self.handle, _stream_ptr(stream), C.byref(st)), "mcfd_status_fetch")
+        fetch = self.lib.mcfd_status_fetch_next if look_ahead else self.lib.mcfd_status_fetch
+        self.lib.check(fetch(self.handle, _stream_ptr(stream), C.byref(st)), "mcfd_status_fetch")
         code = StatusCode(st.code)
         if 0 <= st.first_patch < len(self.bc_patch_names):
             code.patch = self.bc_patch_names[st.first_patch]
@@ -293,13 +296,19 @@ class DeviceGeometry:
 
     def explicit_step_next(self, U: torch.Tensor, cfg, scheme: int, dt: torch.Tensor, *,
                            next_dt_min: torch.Tensor | None = None, next_dt_cells: torch.Tensor | None = None,
-                           time_limit: float = math.inf, primitive_current: bool = False) -> None:
+                           time_limit: float = math.inf, primitive_current: bool = False,
+                           start_residual: torch.Tensor | None = None) -> None:
         """One explicit step that also leaves the next step's stable time
         steps (mcfd_explicit_step_next): per cell into ``next_dt_cells``
         and / or their minimum with ``time_limit`` into ``next_dt_min``.
         ``primitive_current``: the handle's primitive buffer holds the
-        primitive of U (as the previous step left it)."""
+        primitive of U (as the previous step left it).  The time steps'
+        status bits are read by ``status_code(look_ahead=True)``.
+        ``start_residual``: (C,4) float64, receives the residual of U that
+        the first stage computes."""
         _check_state(U, self.n_cells, "U")
+        if start_residual is not None:
+            _check_state(start_residual, self.n_cells, "start_residual")
         if dt.dtype != torch.float64 or not dt.is_cuda or dt.numel() not in (1, self.n_cells):
             raise ValueError("dt must be a CUDA float64 tensor with 1 or n_cells elements")
         for name, t, n in (("next_dt_min", next_dt_min, 1), ("next_dt_cells", next_dt_cells, self.n_cells)):
@@ -309,7 +318,8 @@ class DeviceGeometry:
         self.lib.check(self.lib.mcfd_explicit_step_next(
             self.handle, C.byref(cfg), int(scheme), U.data_ptr(), dt.data_ptr(), per_cell, int(primitive_current),
             next_dt_cells.data_ptr() if next_dt_cells is not None else None,
-            next_dt_min.data_ptr() if next_dt_min is not None else None, float(time_limit), _stream_ptr()),
+            next_dt_min.data_ptr() if next_dt_min is not None else None, float(time_limit),
+            start_residual.data_ptr() if start_residual is not None else None, _stream_ptr()),
             "mcfd_explicit_step_next")
 
     def residual_sumsq(self, R: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:

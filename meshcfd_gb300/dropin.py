@@ -12,8 +12,8 @@ GPU-backed versions taking and returning NumPy arrays:
 * ``_implicit_euler_step(initial, time_step, geometry, settings, ...)``  solver.py:1337
 
 so ``solve_case`` runs unchanged on top of them.  :func:`solve_case` goes
-further: it keeps the state in HBM for the whole explicit loop and returns the
-reference's ``SolverResult``.  Inviscid and laminar viscous (constant or
+further: after the reference's own checks of the case, it keeps the state in
+HBM for the whole explicit loop and returns the reference's ``SolverResult``.  Inviscid and laminar viscous (constant or
 Sutherland) cases, first-order, MUSCL-linear and MUSCL-parabolic
 reconstruction and every boundary kind of ``_residual`` run on the GPU.
 Refused with ``NotImplementedError`` (nothing falls back to the CPU): SST
@@ -174,22 +174,56 @@ def uninstall(module, originals) -> None:
         setattr(module, name, fn)
 
 
+class _ChecksPassed(Exception):
+    """Raised by the stand-in geometry builder of :func:`_reference_checks`."""
+
+
+def _reference_checks(module, case, start_time, step_offset, solution_interval) -> None:
+    """Run the reference's own checks of the case and settings: the prologue
+    of ``solve_case`` (solver.py:193-377), which ends in the geometry build
+    (solver.py:379).  For the call, the module's ``_build_geometry`` is a
+    stand-in that stops the run there, so each failing check raises the
+    reference's own ``SolverError`` with its own message, in its own order."""
+    build = module._build_geometry
+
+    def stop(mesh, c):
+        raise _ChecksPassed
+
+    module._build_geometry = stop
+    try:
+        module.solve_case(case, start_time=start_time, step_offset=step_offset,
+                          solution_interval=solution_interval)
+    except _ChecksPassed:
+        pass
+    else:
+        raise RuntimeError("the reference's solve_case returned before its geometry build")
+    finally:
+        module._build_geometry = build
+
+
 def solve_case(module, case, initial_states=None, progress_callback=None, cancel_callback=None,
                start_time: float = 0.0, step_offset: int = 0, solution_callback=None, solution_interval: int = 1):
-    """The reference's ``solve_case`` for explicit inviscid cases with the
-    state resident in HBM for the whole loop.  ``module`` is the reference's
-    ``meshcfd.core.solver`` (its geometry builder, initial conditions and
-    result types are used as they are)."""
+    """The reference's ``solve_case`` (solver.py:179-1008) for the explicit
+    integrators with the state resident in HBM for the whole loop.
+    ``module`` is the reference's ``meshcfd.core.solver``: its checks of the
+    case and settings, geometry builder, initial conditions and result types
+    are used as they are."""
     from .solver import run_explicit
 
     settings = case.numerics
+    _reference_checks(module, case, start_time, step_offset, solution_interval)
     if settings.time_integration not in TIME_SCHEME_CODES:
         raise NotImplementedError("the HBM-resident loop covers the explicit integrators")
     if settings.adaptive_mesh:
         raise NotImplementedError("adaptive refinement is outside the GPU path")
+    if settings.turbulence_model != "None":
+        raise NotImplementedError("SST turbulence is outside the GPU path")
     geometry = module._build_geometry(case.mesh, case)
     if initial_states is None:
-        initial_states = module.evaluate_initial_conditions(case.mesh, case.initial_conditions)
+        try:
+            initial_states = module.evaluate_initial_conditions(case.mesh, case.initial_conditions)
+        except ValueError as error:
+            raise module.SolverError(f"Could not evaluate initial conditions: {error}") from error
     if len(initial_states) != len(case.mesh.cells):
         raise module.SolverError("Initial state count must match the mesh cell count.")
     primitive = np.array([(s.density, s.velocity_x, s.velocity_y, s.pressure) for s in initial_states], dtype=float)

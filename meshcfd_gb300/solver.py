@@ -1,11 +1,13 @@
 """GPU time loop for the explicit integrators, mirroring the reference's
 ``solve_case`` step loop (solver.py:437-1008) with the state kept in HBM.
 
-Per step: time step on the device (global adaptive: min over cells and
-``end_time - time``; global fixed; local steady: per-cell array and its mean),
-one fused explicit step, the status word checked, callbacks and convergence
-history as the reference emits them.  Adaptation and SST are outside this
-path.
+Per step: the time step (global adaptive: min over cells and
+``end_time - time``; global fixed; local steady: per-cell array and its
+mean), one explicit step whose last stage already computes the next step's
+time steps from the primitive it recovers, the status words checked
+(the stages' with this step, the look-ahead time steps' with the next),
+callbacks and convergence history as the reference emits them.  Adaptation
+and SST are outside this path.
 """
 
 from __future__ import annotations
@@ -18,7 +20,7 @@ import numpy as np
 import torch
 
 from .device import TIME_SCHEME_CODES, DeviceGeometry, make_config
-from .errors import SolverError, raise_for_status
+from .errors import SolverError, StatusCode, raise_for_status
 
 
 @dataclass(frozen=True)
@@ -71,7 +73,16 @@ def run_explicit(geom: DeviceGeometry, settings, U: torch.Tensor, *, start_time:
     local = settings.time_step_mode == "Local (steady)"
     fixed = settings.time_step_mode == "Global fixed"
     dev = geom.device
-    dt_dev = torch.empty(1, dtype=torch.float64, device=dev)
+    # each step's last stage also computes the next step's stable time steps
+    # (mcfd_explicit_step_next) into the other buffer of dt_a / dt_b; their
+    # status bits are a word of their own, raised by the step that uses them,
+    # where the reference computes them (at the top of its loop)
+    dt_a = torch.empty(geom.n_cells if local else 1, dtype=torch.float64, device=dev)
+    dt_b = torch.empty_like(dt_a)
+    ahead = False  # dt_a holds U's time steps and the handle's primitive buffer U's primitive
+    # the first stage leaves R(U) in R: the reference's progress report takes
+    # the RMS of the residual at the start of the step (solver.py:466, 943-950)
+    start_residual = progress_callback is not None and not local
     R = torch.empty_like(U)
     sums = torch.empty(4, dtype=torch.float64, device=dev)
     time = start_time
@@ -82,27 +93,35 @@ def run_explicit(geom: DeviceGeometry, settings, U: torch.Tensor, *, start_time:
         step = step_offset + local_step
         if cancel_callback is not None and cancel_callback():
             break
+        check = local_step % check_every == 0 or local
         try:
-            P = geom.primitive(U, cfg, out=geom.primitive_buffer())
-            if local:
-                dt_cells, _ = geom.time_steps(P, cfg, per_cell=True)
-                time_step = float(dt_cells.mean())
-                dt_arg = dt_cells
-            elif fixed:
-                time_step = min(settings.fixed_time_step, settings.end_time - time)
-                dt_dev.fill_(time_step)
-                dt_arg = dt_dev
+            if ahead:
+                code = geom.status_code(look_ahead=True) if check and not fixed else StatusCode(0)
             else:
-                geom.time_steps(P, cfg, time_limit=settings.end_time - time, out_min=dt_dev)
-                time_step = float(dt_dev.item())
-                dt_arg = dt_dev
-            code = geom.status_code() if (local_step % check_every == 0 or local) else 0
+                P = geom.primitive(U, cfg, out=geom.primitive_buffer())
+                if local:
+                    cells, _ = geom.time_steps(P, cfg, per_cell=True)
+                    dt_a.copy_(cells)
+                elif not fixed:
+                    geom.time_steps(P, cfg, time_limit=settings.end_time - time, out_min=dt_a)
+                code = geom.status_code() if check else StatusCode(0)
             raise_for_status(code, solver_error)
+            if fixed:
+                time_step = min(settings.fixed_time_step, settings.end_time - time)
+                dt_a.fill_(time_step)
+            else:
+                time_step = float(dt_a.mean()) if local else float(dt_a.item())
             if not math.isfinite(time_step) or time_step <= 0.0:
                 raise solver_error("The stable time step is non-positive or non-finite.")
-            geom.explicit_step(U, cfg, scheme, dt_arg)
-            derivative_valid = False
-            if local_step % check_every == 0:
+            geom.explicit_step_next(U, cfg, scheme, dt_a, next_dt_cells=dt_b if local else None,
+                                    next_dt_min=None if (local or fixed) else dt_b,
+                                    time_limit=settings.end_time - (time + time_step), primitive_current=ahead,
+                                    start_residual=R if start_residual else None)
+            if not fixed:
+                dt_a, dt_b = dt_b, dt_a
+            ahead = True
+            derivative_valid = start_residual
+            if check:
                 raise_for_status(geom.status_code(), solver_error)
         except (FloatingPointError, ValueError, ZeroDivisionError) as error:
             raise solver_error(f"Solver failed at step {step}: {error}") from error
@@ -134,6 +153,9 @@ def run_explicit(geom: DeviceGeometry, settings, U: torch.Tensor, *, start_time:
         if steady_converged:
             completed = True
             break
+    # the time steps the last step looked ahead to belong to a step not taken:
+    # the reference never computes them, so their bits raise nothing
+    geom.status_code(look_ahead=True)
     raise_for_status(geom.status_code(), solver_error)
     residual = float("nan")
     if final_residual:

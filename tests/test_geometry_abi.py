@@ -136,7 +136,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(native.lib, name), name
     assert set(declared) == set(_lib.SIGNATURES), "ctypes signatures out of sync with the header"
-    assert native.mcfd_abi_version() == _lib.ABI_VERSION == 5
+    assert native.mcfd_abi_version() == _lib.ABI_VERSION == 6
     assert native.mcfd_error_string(3) == b"option not supported by the GPU path"
 
 

@@ -144,3 +144,31 @@ def test_step_next_with_a_separate_time_step_pass(cuda_device, extra):
         np.testing.assert_array_equal(b[0], a[0])
         np.testing.assert_array_equal(b[1], a[1])
     dg.close()
+
+
+@pytest.mark.parametrize("recipe", ("riemann", "bump"))
+@pytest.mark.parametrize("scheme", (0, 1, 2, 3))
+def test_step_next_start_residual(cuda_device, recipe, scheme):
+    """``start_residual`` receives the residual of the state the step starts
+    from, the same bits as mcfd_residual on it, with and without the
+    look-ahead time steps; the look-ahead's status word stays clear."""
+    from meshcfd_gb300.device import DeviceGeometry, make_config, primitive_to_conservative
+    from meshcfd_gb300.geometry import build_geometry
+
+    case, P = {"riemann": _riemann, "bump": _bump}[recipe]()
+    s = case.numerics
+    dg = DeviceGeometry(build_geometry(case.mesh, case))
+    U = torch.as_tensor(primitive_to_conservative(P, s.gamma), device=cuda_device)
+    cfg = make_config(s, "fast")
+    _, dt = dg.time_steps(dg.primitive(U, cfg), cfg)
+    dt = dt.clone()
+    R = torch.empty_like(U)
+    nxt = torch.empty(1, dtype=torch.float64, device=cuda_device)
+    for look_ahead in (True, False, True):
+        R0 = dg.residual(U, cfg).clone()
+        dg.explicit_step_next(U, cfg, scheme, dt, next_dt_min=nxt if look_ahead else None, start_residual=R,
+                              primitive_current=True)
+        assert torch.equal(R, R0)
+    dg.check_status()
+    assert dg.status_code(look_ahead=True) == 0
+    dg.close()
