@@ -437,10 +437,15 @@ int mcfd_lusgs_apply(mcfd_geom* geom, const double* v, double* x, void* stream);
  * (the same IEEE products); 6: as 2 with one thread per (row, component),
  * chunks of at most 8 rows; 8 or 16 a
  * thread-block cluster of that many blocks sharing their latest solutions in
- * distributed shared memory, a cluster barrier per level.  0 restores the
- * defaults (wide_level 16384, engine 2); 8 or 16 returns MCFD_E_UNSUPPORTED
- * where the device cannot run that cluster size.  Results do not depend on
- * it.  No counterpart in the reference. */
+ * distributed shared memory, a cluster barrier per level; 7 or 9 a cluster
+ * of 8 or 16 blocks, each owning a band of consecutive cell ids, sweeping
+ * windows of up to 32 levels with a block barrier per level and a cluster
+ * barrier per window (each block recomputes the rows of other bands its own
+ * rows depend on inside the window; a plan that does not fit shared memory
+ * takes engine 2).  0 restores the defaults (wide_level 16384, engine 9
+ * where the device runs clusters of 16, else 7, else 2); 7, 8, 9 or 16
+ * returns MCFD_E_UNSUPPORTED where the device cannot run that cluster size.
+ * Results do not depend on it.  No counterpart in the reference. */
 int mcfd_implicit_set_sweep(mcfd_geom* geom, int32_t wide_level, int32_t engine);
 /* Rows per chunk of the per-row-wait sweeps (engines 2-6): 1..32 (at most 8
  * for engine 6), 0 restores the default (32; 8 for engine 6).  A chunk is a run of consecutive rows of one level taken
@@ -535,6 +540,12 @@ int mcfd_ieee_div_sqrt(const double* a, const double* b, int64_t n, double* quot
  * product[i] = a[i] * b[i], bit-identical to the FP64 unit.  Device arrays of
  * n doubles.  No reference counterpart (verification). */
 int mcfd_ieee_mul(const double* a, const double* b, int64_t n, double* product, void* stream);
+/* Element-wise IEEE binary64 division as the LU-SGS sweeps evaluate it:
+ * quotient[i] = a[i] / b[i] from the divisor's correctly rounded reciprocal
+ * (a Markstein-corrected candidate accepted by an exact remainder test, the
+ * integer-pipe division otherwise), bit-identical to the FP64 unit.  Device
+ * arrays of n doubles.  No reference counterpart (verification). */
+int mcfd_ieee_div_fma(const double* a, const double* b, int64_t n, double* quotient, void* stream);
 
 /* ---- host helpers (no GPU needed) ---- */
 

@@ -132,6 +132,7 @@ SIGNATURES = {
     "mcfd_residual_sumsq_noalloc": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "mcfd_ieee_div_sqrt": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "mcfd_ieee_mul": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "mcfd_ieee_div_fma": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp]),
     "mcfd_host_cell_geometry": (c_i32, [c_i64, P_i64, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
     "mcfd_host_face_geometry": (c_i32, [c_i64, P_i64, P_dbl, P_dbl, P_i64, P_dbl, P_dbl, P_dbl, P_i64]),
     "mcfd_device_cell_geometry": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

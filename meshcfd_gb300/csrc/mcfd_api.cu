@@ -1455,13 +1455,14 @@ int mcfd_lusgs_apply(mcfd_geom* h, const double* v, double* x, void* stream) {
 }
 
 int mcfd_implicit_set_sweep(mcfd_geom* h, int32_t wide_level, int32_t engine) {
-  if (!h || wide_level < 0 || (engine < 0 || (engine > 6 && engine != 8 && engine != 16)))
+  if (!h || wide_level < 0 || (engine < 0 || (engine > 9 && engine != 16)))
     return MCFD_E_ARG;
   int c = ensure_implicit(h);
   if (c) return c;
-  if ((engine == 8 && !h->imp.cluster8_ok) || (engine == 16 && !h->imp.cluster16_ok)) return MCFD_E_UNSUPPORTED;
-  implicit_set_wide_level(h->imp, wide_level, engine);
-  return MCFD_OK;
+  if ((engine == 8 && !h->imp.cluster8_ok) || (engine == 16 && !h->imp.cluster16_ok) ||
+      (engine == 7 && !h->imp.window8_ok) || (engine == 9 && !h->imp.window16_ok))
+    return MCFD_E_UNSUPPORTED;
+  return implicit_set_wide_level(h->imp, wide_level, engine) == cudaSuccess ? MCFD_OK : MCFD_E_CUDA;
 }
 
 int mcfd_gmres(mcfd_geom* h, const double* b, double* x, double tol, int32_t max_iter, int32_t krylov_dim,

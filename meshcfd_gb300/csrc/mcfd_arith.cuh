@@ -225,6 +225,54 @@ MCFD_IA_FN double div_rn_recip(double a, double b, u64 X) {
 
 MCFD_IA_FN double div_rn(double a, double b) { return div_rn_recip(a, b, recip_fixed(b)); }
 
+// a / b, the same bits as div_rn, in fewer dependent steps, from y =
+// RN(1/b) (div_rn_recip(1.0, b, X)) and X = recip_fixed(b), both of which
+// depend on b alone.  A candidate from one Markstein correction of the
+// product a y (q0 = RN(a y), q = RN(q0 + RN(a - b q0) y); P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990) is accepted only when the
+// remainder r = a - b q, an FMA that is exact for q within an ulp of a/b
+// (and is large otherwise), lies strictly inside (-|b| u / 2, |b| u / 2),
+// u the spacing of the doubles next to q on the side of a/b: then q is the
+// double nearest a/b, which is never a midpoint of two doubles (a rounding
+// test in the manner of Tuckerman's for square roots).  The bounds |b| u / 2
+// are powers-of-two multiples of |b|, formed exactly in the exponent field
+// and compared as bit patterns.  Zero, subnormal or non-finite operands,
+// quotients near either end of the normal range, and a rejected candidate
+// take div_rn_recip.  Four dependent FP64 operations and integer tests
+// instead of div_rn_recip's chain of 64-bit integer products.
+MCFD_IA_FN double fma_rn(double x, double y, double z) {
+#if defined(__CUDA_ARCH__)
+  return __fma_rn(x, y, z);
+#else
+  return fma(x, y, z);
+#endif
+}
+MCFD_IA_FN double mul_rn_fp64(double x, double y) {
+#if defined(__CUDA_ARCH__)
+  return __dmul_rn(x, y);
+#else
+  return x * y;
+#endif
+}
+
+MCFD_IA_FN double div_rn_fma(double a, double b, double y, u64 X) {
+  const double q0 = mul_rn_fp64(a, y);
+  const double q = fma_rn(fma_rn(-b, q0, a), y, q0);
+  const double r = fma_rn(-b, q, a);
+  const u64 ia = bits(a), ib = bits(b), iq = bits(q), ir = bits(r);
+  const unsigned ea = (unsigned)(ia >> 52) & 0x7ffu, eb = (unsigned)(ib >> 52) & 0x7ffu;
+  const unsigned eq = (unsigned)(iq >> 52) & 0x7ffu;
+  // |b| u / 2 with u = 2^(eq - 1075) away from zero; toward zero the same,
+  // or half of it when |q| is a power of two
+  const bool away = ((ir ^ ib ^ iq) >> 63) == 0ull;  // sign(r / b) == sign(q)
+  const int eh = (int)eb + (int)eq - 1076 - ((!away && (iq & kMant) == 0ull) ? 1 : 0);
+  const bool in_range = ea - 1u < 0x7feu && eb - 1u < 0x7feu && eq - 2u < 0x7fcu && eh >= 1 && eh <= 2046;
+  const u64 half = ((u64)(eh < 1 ? 1 : (eh > 2046 ? 2046 : eh)) << 52) | (ib & kMant);
+  if (in_range && (ir << 1) < (half << 1)) return q;  // |r| < |b| u / 2 (or r = 0)
+  return div_rn_recip(a, b, X);
+}
+
 // a * b, round to nearest even, in 32-bit words.  With the significands
 // split as a = a1 2^32 + a0 (a1 21 bits), the 106-bit product is summed by
 // columns with 32 x 32 + 64 -> 64-bit multiply-adds; its top 53 bits (from
@@ -338,6 +386,7 @@ MCFD_IA_FN double plus_zero(double x) { return bits(x) == kSign ? 0.0 : x; }
 using ia::abs_of;
 using ia::div_rn;
 using ia::div_rn_recip;
+using ia::div_rn_fma;
 using ia::recip_fixed;
 using ia::mul_rn;
 using ia::negate;

@@ -119,6 +119,8 @@ struct SweepDev {
   const double* pk_val;
   const double* pk_diag;
   const double* pk_dc;
+  const double* pk_rcp;                 // RN(1 / diagonal)
+  const unsigned long long* pk_rx;      // recip_fixed(diagonal)
   const double* in;
   double* out;
   int backward;
@@ -349,6 +351,152 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_lusgs_cluster(SweepDev a
       if (have) sweep_load(a, b + first, R);
     }
     cluster.sync();
+  }
+}
+
+// The windowed band sweep (SweepWindows): block k of a thread-block
+// cluster owns a band of consecutive cell ids.  Per window of levels it
+// loads the solutions it needs from before the window into shared-memory
+// slots, then solves, level by level with a block barrier between levels,
+// its own rows and the rows of other bands they depend on inside the window
+// (the same arithmetic on the same inputs: the same bits as their owners').
+// Only the rows a block owns go to global memory; a cluster barrier
+// (release / acquire) at each window's start makes the previous window's
+// rows visible to every block.  Each row is solved by four lanes, one per
+// component (warp w of four holds component w of 32 rows), so a level's
+// critical path holds a row's products and differences per entry once, not
+// four times over in one warp's instruction stream.  The next level's rows
+// (independent of the solutions) are loaded before the block barrier.  The
+// arithmetic is sweep_solve's, component by component: the same bits.  No
+// thread waits on a flag; every thread of every block passes the same
+// barriers.
+constexpr int kWinThreads = 256;                 // 8 warps: 64 rows of 4 components per pass
+constexpr int kWinRowsPerPass = kWinThreads / 4;
+constexpr int kWinMaxLevels = 32;                // levels per window at most
+constexpr int kWinMaxSlots = 6144;               // shared-memory slots of 4 doubles (192 KiB)
+
+struct WinDev {
+  const int *l0, *l1, *gbase, *grp, *ext_ptr, *ext_slot, *ext_cell, *pos, *cell, *slot, *eptr, *eslot;
+};
+
+// A row record (the plan's, fixed) and a row's values (the matrix's and the
+// right-hand side's, per sweep).
+struct WinRec {
+  int p0, i, slot, eb;
+};
+
+struct WinRow {
+  int p, i, n, slot, eb;
+  bool own;
+  double r, dc, dg, y;  // y: RN(1 / dg)
+  unsigned long long rx;
+  double v[kSweepPack];
+  int es[kSweepPack];
+};
+
+__device__ __forceinline__ void win_rec(const WinDev& w, int rec, WinRec& Q) {
+  Q.p0 = w.pos[rec];
+  Q.i = w.cell[rec];
+  Q.slot = w.slot[rec];
+  Q.eb = w.eptr[rec];
+}
+
+// loads only (the entry slots are padded, so none depends on the count)
+__device__ __forceinline__ void win_vals(const SweepDev& a, const WinDev& w, const WinRec& Q, int comp, WinRow& R) {
+  R.own = Q.p0 >= 0;
+  R.p = R.own ? Q.p0 : ~Q.p0;
+  R.i = Q.i;
+  R.slot = Q.slot;
+  R.eb = Q.eb;
+  R.n = a.pk_cnt[R.p];
+  R.dg = a.pk_diag[R.p];
+  R.y = a.pk_rcp[R.p];
+  R.rx = a.pk_rx[R.p];
+  R.r = a.in[4 * (size_t)R.i + comp];
+  R.dc = a.backward ? a.pk_dc[R.p] : 1.0;
+#pragma unroll
+  for (int k = 0; k < kSweepPack; ++k) {
+    R.v[k] = a.pk_val[(size_t)R.p * kSweepPack + k];
+    R.es[k] = w.eslot[R.eb + k];
+  }
+}
+
+__device__ __forceinline__ void win_solve(const SweepDev& a, const WinDev& w, double* sl, const WinRow& R,
+                                          int comp) {
+  double acc = a.backward ? R.dc * R.r : R.r;
+#pragma unroll
+  for (int k = 0; k < kSweepPack; ++k)
+    if (k < R.n) acc = acc - R.v[k] * sl[4 * R.es[k] + comp];
+  if (R.n > kSweepPack) {  // the rest of a long row: values from the CSR, slots from the record
+    const int j0 = a.ent_ptr[R.p];
+    for (int k = kSweepPack; k < R.n; ++k) acc = acc - a.rval[a.ent_val[j0 + k]] * sl[4 * w.eslot[R.eb + k] + comp];
+  }
+  // the quotient from the row's reciprocal: the same bits as div_rn in
+  // fewer dependent steps (div_rn_fma), the level's critical path
+  const double res = div_rn_fma(acc, R.dg, R.y, R.rx);
+  sl[4 * R.slot + comp] = res;
+  if (R.own) a.out[4 * (size_t)R.i + comp] = res;
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kWinThreads, 1) k_lusgs_window(SweepDev a, WinDev w, int w0, int w1) {
+  extern __shared__ double sl[];  // [slots][4]
+  __shared__ int grp[kWinMaxLevels + 1];  // this block's level ranges in the window
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int comp = ((int)threadIdx.x >> 5) & 3;
+  const int rl = (((int)threadIdx.x >> 7) << 5) | ((int)threadIdx.x & 31);  // row of the pass
+  for (int win = w0; win < w1; ++win) {
+    const int nl = w.l1[win] - w.l0[win];
+    const int g0 = w.gbase[win] + rank * (nl + 1);
+    if ((int)threadIdx.x <= nl) grp[threadIdx.x] = w.grp[g0 + threadIdx.x];
+    __syncthreads();
+    // a software pipeline over the window's levels: while level m is solved,
+    // the values of level m + 2 and the records of level m + 3 are loaded
+    // (a load uses only registers filled at least a level earlier, so no
+    // load waits on another in flight; the empty asm statements keep the
+    // compiler from sinking the loads to their uses)
+    auto in_level = [&](int m) { return m < nl && grp[m] + rl < grp[m + 1]; };
+    WinRec Q2, Q3;
+    WinRow cur, v1, v2;
+    bool h0 = in_level(0), h1 = in_level(1), q2 = in_level(2), q3 = false;
+    {
+      WinRec Q;
+      if (h0) {
+        win_rec(w, grp[0] + rl, Q);
+        win_vals(a, w, Q, comp, cur);
+      }
+      if (h1) {
+        win_rec(w, grp[1] + rl, Q);
+        win_vals(a, w, Q, comp, v1);
+      }
+      if (q2) win_rec(w, grp[2] + rl, Q2);
+    }
+    cluster.sync();  // the rows every block solved before this window are in global memory
+    for (int x = w.ext_ptr[win * NC + rank] + rl, x1 = w.ext_ptr[win * NC + rank + 1]; x < x1; x += kWinRowsPerPass)
+      sl[4 * w.ext_slot[x] + comp] = __ldcg(a.out + 4 * (size_t)w.ext_cell[x] + comp);
+    __syncthreads();
+    for (int m = 0; m < nl; ++m) {
+      q3 = in_level(m + 3);
+      if (q3) win_rec(w, grp[m + 3] + rl, Q3);
+      if (q2) win_vals(a, w, Q2, comp, v2);
+      asm volatile("" ::: "memory");
+      if (h0) win_solve(a, w, sl, cur, comp);
+      for (int r = grp[m] + rl + kWinRowsPerPass; r < grp[m + 1]; r += kWinRowsPerPass) {  // more rows than one pass
+        WinRec Qx;
+        WinRow X;
+        win_rec(w, r, Qx);
+        win_vals(a, w, Qx, comp, X);
+        win_solve(a, w, sl, X, comp);
+      }
+      __syncthreads();
+      cur = v1;
+      h0 = h1;
+      v1 = v2;
+      h1 = q2;
+      Q2 = Q3;
+      q2 = q3;
+    }
   }
 }
 
@@ -596,15 +744,21 @@ __global__ void __launch_bounds__(kBlock) k_lusgs_level(SweepDev a, int b, int e
 __global__ void k_pack_rows(int C, const int* __restrict__ pos_cell, const int* __restrict__ ent_ptr,
                             const int* __restrict__ ent_val, const double* __restrict__ rval,
                             const double* __restrict__ diag, const double* __restrict__ dclamp,
-                            double* __restrict__ pk_val, double* __restrict__ pk_diag, double* __restrict__ pk_dc) {
+                            double* __restrict__ pk_val, double* __restrict__ pk_diag, double* __restrict__ pk_dc,
+                            double* __restrict__ pk_rcp, unsigned long long* __restrict__ pk_rx) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= C) return;
   const int i = pos_cell[p];
   const int j0 = ent_ptr[p], n = ent_ptr[p + 1] - j0;
 #pragma unroll
   for (int k = 0; k < kSweepPack; ++k) pk_val[(size_t)p * kSweepPack + k] = k < n ? rval[ent_val[j0 + k]] : 0.0;
-  pk_diag[p] = diag[i];
+  const double d = diag[i];
+  pk_diag[p] = d;
   pk_dc[p] = dclamp[i];
+  // the divisor's reciprocals for the windowed sweep's quotients (div_rn_fma)
+  const unsigned long long X = recip_fixed(d);
+  pk_rx[p] = X;
+  pk_rcp[p] = div_rn_recip(1.0, d, X);
 }
 
 // ------------------------------------------------------------------ vectors
@@ -1020,14 +1174,26 @@ static void sweep_schedule(SweepPlan& pl, int wide) {
   }
 }
 
-void implicit_set_wide_level(ImplicitState& st, int wide, int engine) {
+static void free_windows(SweepWindows& W);
+static cudaError_t plan_windows(SweepPlan& pl, int C, int nc);
+
+cudaError_t implicit_set_wide_level(ImplicitState& st, int wide, int engine) {
   st.wide_level = wide > 0 ? wide : kWideLevel;
-  st.engine = engine > 0 ? engine : kDefaultEngine;
+  st.engine = engine > 0 ? engine : st.default_engine;
   // the per-component sweep takes chunks of at most 8 rows
-  if (st.engine == kSweepDataflowComponents && st.chunk_rows > 8) implicit_set_chunk(st, 8);
+  cudaError_t e = cudaSuccess;
+  if (st.engine == kSweepDataflowComponents && st.chunk_rows > 8) e = implicit_set_chunk(st, 8);
   sweep_schedule(st.fwd, st.wide_level);
   sweep_schedule(st.bwd, st.wide_level);
+  free_windows(st.fwd.win);
+  free_windows(st.bwd.win);
+  if (st.engine == kSweepWindow8 || st.engine == kSweepWindow16) {
+    const int nc = st.engine == kSweepWindow16 ? 16 : 8;
+    if (e == cudaSuccess) e = plan_windows(st.fwd, st.n_cells, nc);
+    if (e == cudaSuccess) e = plan_windows(st.bwd, st.n_cells, nc);
+  }
   st.inner_key = -1;  // the captured loop holds the old launches
+  return e;
 }
 
 // The dataflow sweep's chunks: runs of at most `rows` consecutive positions
@@ -1051,6 +1217,149 @@ cudaError_t implicit_set_chunk(ImplicitState& st, int rows) {
   cudaError_t e = sweep_chunks(st.fwd, r);
   if (e == cudaSuccess) e = sweep_chunks(st.bwd, r);
   st.inner_key = -1;  // the captured loop holds the old chunk ranges
+  return e;
+}
+
+// Plans the windowed band sweep of pl's current schedule for a cluster of nc
+// blocks (SweepWindows).  Each single-block run of the schedule is cut into
+// windows of at most kWinMaxLevels levels, fewer where a block's rows,
+// the rows they depend on inside the window and the rows read from before
+// it would not fit kWinMaxSlots; ok stays false when one level alone does
+// not fit (the sweep then takes the default engine).
+static void free_windows(SweepWindows& W) {
+  for (void* q : W.owned) cudaFree(q);
+  W = SweepWindows{};
+}
+
+static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
+  free_windows(pl.win);
+  SweepWindows& W = pl.win;
+  W.nc = nc;
+  W.band_rows = std::max(1, (C + nc - 1) / nc);
+  const std::vector<int>& lp = pl.host_level_ptr;
+  const std::vector<int>& pos_cell = pl.host_pos_cell;
+  const std::vector<int>& ent_ptr = pl.host_ent_ptr;
+  const std::vector<int>& ent_pos = pl.host_ent_pos;
+  const int nlev = (int)lp.size() - 1;
+  std::vector<int> lev_of(C);
+  for (int l = 0; l < nlev; ++l)
+    for (int p = lp[l]; p < lp[l + 1]; ++p) lev_of[p] = l;
+  std::vector<int> l0v, l1v, gbase, grp, ext_ptr{0}, ext_slot, ext_cell, posv, cellv, slotv, eptr, eslot;
+  std::vector<int> mark(C, -1), slot_of(C, -1);
+  std::vector<std::vector<int>> by_level(kWinMaxLevels);
+  std::vector<int> ext;
+  int stamp = 0;
+  // the closure of block k's rows in window [L0, L1): its rows and the rows
+  // they depend on inside the window (by_level), the positions before the
+  // window they read (ext); returns the slots it needs
+  auto closure = [&](int L0, int L1, int k) {
+    ++stamp;
+    const int base = lp[L0], nl = L1 - L0;
+    for (int m = 0; m < nl; ++m) by_level[m].clear();
+    ext.clear();
+    for (int m = 0; m < nl; ++m)
+      for (int p = lp[L0 + m]; p < lp[L0 + m + 1]; ++p)
+        if (pos_cell[p] / W.band_rows == k) {
+          mark[p] = stamp;
+          by_level[m].push_back(p);
+        }
+    for (int m = nl - 1; m >= 0; --m)  // dependencies lie on lower levels
+      for (size_t x = 0; x < by_level[m].size(); ++x) {
+        const int p = by_level[m][x];
+        for (int j = ent_ptr[p]; j < ent_ptr[p + 1]; ++j) {
+          const int q = ent_pos[j];
+          if (mark[q] == stamp) continue;
+          mark[q] = stamp;
+          if (q >= base) by_level[lev_of[q] - L0].push_back(q);
+          else ext.push_back(q);
+        }
+      }
+    size_t n = ext.size();
+    for (int m = 0; m < nl; ++m) n += by_level[m].size();
+    return n;
+  };
+  auto emit = [&](int L0, int L1, int k) {
+    const int nl = L1 - L0;
+    closure(L0, L1, k);
+    std::sort(ext.begin(), ext.end());
+    int sl = 0;
+    for (int q : ext) {
+      slot_of[q] = sl;
+      ext_slot.push_back(sl++);
+      ext_cell.push_back(pos_cell[q]);
+    }
+    ext_ptr.push_back((int)ext_slot.size());
+    for (int m = 0; m < nl; ++m) {
+      grp.push_back((int)posv.size());
+      std::vector<int>& rows = by_level[m];
+      std::sort(rows.begin(), rows.end());
+      for (int p : rows) {
+        slot_of[p] = sl++;
+        posv.push_back(pos_cell[p] / W.band_rows == k ? p : ~p);
+        cellv.push_back(pos_cell[p]);
+        slotv.push_back(slot_of[p]);
+        eptr.push_back((int)eslot.size());
+        for (int j = ent_ptr[p]; j < ent_ptr[p + 1]; ++j) eslot.push_back(slot_of[ent_pos[j]]);
+      }
+    }
+    grp.push_back((int)posv.size());
+    W.slots = std::max(W.slots, sl);
+  };
+  W.run_w0.assign(pl.schedule.size() + 1, 0);
+  bool ok = true;
+  for (size_t si = 0; si < pl.schedule.size() && ok; ++si) {
+    W.run_w0[si] = (int)l0v.size();
+    const SweepPlan::Launch& run = pl.schedule[si];
+    if (!run.wavefront) continue;
+    for (int L = run.l0; L < run.l1 && ok;) {
+      int H = std::min(kWinMaxLevels, run.l1 - L);
+      for (;;) {
+        size_t need = 0;
+        for (int k = 0; k < nc; ++k) need = std::max(need, closure(L, L + H, k));
+        if (need <= (size_t)kWinMaxSlots) break;
+        if (H == 1) {
+          ok = false;
+          break;
+        }
+        H = std::max(1, H / 2);
+      }
+      if (!ok) break;
+      l0v.push_back(L);
+      l1v.push_back(L + H);
+      gbase.push_back((int)grp.size());
+      for (int k = 0; k < nc; ++k) emit(L, L + H, k);
+      L += H;
+    }
+  }
+  W.run_w0.back() = (int)l0v.size();
+  eslot.insert(eslot.end(), kSweepPack, 0);  // a row's first kSweepPack slots load unconditionally
+  for (size_t si = pl.schedule.size(); si-- > 0;)  // entries without windows: empty ranges
+    if (!pl.schedule[si].wavefront) W.run_w0[si] = W.run_w0[si + 1];
+  if (!ok) {
+    free_windows(pl.win);
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaSuccess;
+  auto put = [&](const std::vector<int>& v, int** dst) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc((void**)dst, std::max<size_t>(v.size(), 1) * sizeof(int));
+    if (e != cudaSuccess) return;
+    W.owned.push_back(*dst);
+    if (!v.empty()) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice);
+  };
+  put(l0v, &W.l0);
+  put(l1v, &W.l1);
+  put(gbase, &W.gbase);
+  put(grp, &W.grp);
+  put(ext_ptr, &W.ext_ptr);
+  put(ext_slot, &W.ext_slot);
+  put(ext_cell, &W.ext_cell);
+  put(posv, &W.pos);
+  put(cellv, &W.cell);
+  put(slotv, &W.slot);
+  put(eptr, &W.eptr);
+  put(eslot, &W.eslot);
+  W.ok = e == cudaSuccess;
   return e;
 }
 
@@ -1225,6 +1534,13 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   UP(pb.pos, bwd.pk_pos);
   UP(pb.cell, bwd.pk_cell);
 #undef UP
+  for (int f = 0; f < 2; ++f) {
+    SweepPlan& pl = f == 0 ? st.fwd : st.bwd;
+    const HostPlan& hp = f == 0 ? hf : hb;
+    pl.host_pos_cell = hp.pos_cell;
+    pl.host_ent_ptr = hp.ent_ptr;
+    pl.host_ent_pos = hp.ent_pos;
+  }
   st.fwd.n_levels = st.n_levels_fwd;
   st.bwd.n_levels = st.n_levels_bwd;
   st.fwd.host_level_ptr = hf.level_ptr;
@@ -1259,6 +1575,8 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
     zeros((size_t)C * kSweepPack, &pl->pk_val);
     zeros(C, &pl->pk_diag);
     zeros(C, &pl->pk_dc);
+    zeros(C, &pl->pk_rcp);
+    zeros(C, (double**)&pl->pk_rx);
   }
   zeros(kRedBlocks, &st.partials);
   zeros(64, &st.scalars);
@@ -1269,12 +1587,11 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
   if (e == cudaSuccess) e = cudaMallocHost((void**)&st.cycle_host, sizeof(GmresCycle));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_wavefront, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)kRingBytes);
-  // Sweeps of narrow levels run in one block by default: measured on the
-  // 512 x 256 bump (767 levels of at most 256 rows), one LU-SGS application
-  // takes 4.08 ms in one block, 4.68 ms in a cluster of 8 and 5.01 ms in a
-  // cluster of 16 (the cluster barrier and the remote ring stores cost more
-  // than the FP64 work they spread).  The cluster sweeps stay selectable
-  // where the device can run them (8: portable; 16: non-portable).
+  // Measured on the 512 x 256 bump (767 levels of at most 256 rows), one
+  // LU-SGS application takes 3.20 ms in one block with per-row waits, 4.46 /
+  // 4.82 ms in a cluster of 8 / 16 sharing every solution, and 1.68 / 1.52 ms
+  // in the windowed band sweep on a cluster of 8 / 16, the default where the
+  // device runs it (set after the cluster checks below).
   st.engine = kDefaultEngine;
   st.chunk_rows = kDefaultEngine == kSweepDataflowComponents ? 8 : kFlowChunk;
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lusgs_dataflow<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1309,7 +1626,33 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
       cudaFuncSetAttribute(k_lusgs_cluster<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes) ==
           cudaSuccess &&
       cudaFuncSetAttribute(k_lusgs_cluster<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  // the windowed band sweeps: whether a cluster of 8 / 16 such blocks fits the device
+  auto window_fits = [](auto kernel, int nc) {
+    const int smem = kWinMaxSlots * 4 * (int)sizeof(double);
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return false;
+    if (nc > kPortableCluster &&
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+      return false;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(nc);
+    cfg.blockDim = dim3(kWinThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = nc;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    return cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) == cudaSuccess && clusters > 0;
+  };
+  st.window8_ok = e == cudaSuccess && window_fits(k_lusgs_window<8>, 8);
+  st.window16_ok = e == cudaSuccess && window_fits(k_lusgs_window<16>, 16);
   cudaGetLastError();
+  st.default_engine = st.window16_ok ? kSweepWindow16 : (st.window8_ok ? kSweepWindow8 : kDefaultEngine);
+  if (e == cudaSuccess) e = implicit_set_wide_level(st, 0, 0);
   if (e == cudaSuccess) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
@@ -1341,6 +1684,8 @@ void implicit_free(ImplicitState& st) {
   st.cap_stream = nullptr;
   for (void* p : st.owned) cudaFree(p);
   st.owned.clear();
+  free_windows(st.fwd.win);
+  free_windows(st.bwd.win);
   if (st.cycle_host) cudaFreeHost(st.cycle_host);
   st.cycle_host = nullptr;
 }
@@ -1365,7 +1710,7 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
     count_launch();
     k_pack_rows<<<blocks_for(st.n_cells), kBlock, 0, s>>>(st.n_cells, pl->pos_cell, pl->ent_ptr, pl->ent_val,
                                                           st.rval, st.diag, st.dclamp, pl->pk_val, pl->pk_diag,
-                                                          pl->pk_dc);
+                                                          pl->pk_dc, pl->pk_rcp, pl->pk_rx);
   }
   return cudaGetLastError();
 }
@@ -1373,10 +1718,14 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
 static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const double* in, double* out, int backward,
                          cudaStream_t s) {
   SweepDev a{pl.level_ptr, pl.pos_cell, pl.ent_ptr, pl.ent_cell, pl.ent_pos, pl.ent_val, st.rval,
-             pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, in, out, backward};
-  for (const SweepPlan::Launch& l : pl.schedule) {
+             pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, pl.pk_rcp, pl.pk_rx,
+             in, out, backward};
+  const bool window = st.engine == kSweepWindow8 || st.engine == kSweepWindow16;
+  for (size_t si = 0; si < pl.schedule.size(); ++si) {
+    const SweepPlan::Launch& l = pl.schedule[si];
     count_launch();
-    if (l.wavefront && st.engine == kSweepDataflow) {
+    // the windowed sweep falls back to the default where it has no plan
+    if (l.wavefront && (st.engine == kSweepDataflow || (window && !pl.win.ok))) {
       const int k0 = pl.host_chunk_ptr[l.l0], k1 = pl.host_chunk_ptr[l.l1];
       k_lusgs_dataflow<512, false><<<1, 512, kFlowSmemBytes, s>>>(a, pl.chunks, k0, k1, st.status);
     } else if (l.wavefront && st.engine == kSweepDataflowWide) {
@@ -1406,6 +1755,26 @@ static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const dou
       cfg.numAttrs = 1;
       const cudaError_t e = st.engine == 16 ? cudaLaunchKernelEx(&cfg, k_lusgs_cluster<16>, a, l.l0, l.l1)
                                              : cudaLaunchKernelEx(&cfg, k_lusgs_cluster<8>, a, l.l0, l.l1);
+      if (e != cudaSuccess) return e;
+    } else if (l.wavefront && window) {
+      const SweepWindows& W = pl.win;
+      const WinDev wd{W.l0,  W.l1,   W.gbase, W.grp,  W.ext_ptr, W.ext_slot,
+                      W.ext_cell, W.pos, W.cell, W.slot, W.eptr,    W.eslot};
+      const int w0 = W.run_w0[si], w1 = W.run_w0[si + 1];
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3(W.nc);
+      cfg.blockDim = dim3(kWinThreads);
+      cfg.dynamicSmemBytes = (size_t)std::max(W.slots, 1) * 4 * sizeof(double);
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = W.nc;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      const cudaError_t e = W.nc == 16 ? cudaLaunchKernelEx(&cfg, k_lusgs_window<16>, a, wd, w0, w1)
+                                       : cudaLaunchKernelEx(&cfg, k_lusgs_window<8>, a, wd, w0, w1);
       if (e != cudaSuccess) return e;
     } else if (l.wavefront) {
       k_lusgs_wavefront<<<1, kWaveThreads, kRingBytes, s>>>(a, l.l0, l.l1);

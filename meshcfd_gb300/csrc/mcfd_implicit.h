@@ -51,8 +51,33 @@ enum SweepEngine {
   kSweepDataflowNarrow = 4,  // 256 threads
   kSweepDataflowIntMul = 5,  // 512 threads, the row's products on the integer pipe
   kSweepDataflowComponents = 6,  // 512 threads, one lane per (row, component), chunks of 8 rows
+  kSweepWindow8 = 7,   // cluster of 8 blocks owning bands of cells, windows of levels (SweepWindows)
   kSweepCluster8 = 8,
+  kSweepWindow16 = 9,  // the same with 16 blocks
   kSweepCluster16 = 16
+};
+
+// The windowed band sweep of one plan for a cluster of nc blocks.  Block k
+// owns the cells [k * band_rows, (k + 1) * band_rows).  The levels of each
+// single-block run are cut into windows of consecutive levels; in a window,
+// block k solves its own rows and every row of another band they depend on
+// inside the window (recomputed, the same bits), reading the rows solved
+// before the window ("externals") from global memory once, at the window's
+// start, into shared-memory slots.
+//   windows w: levels [l0[w], l1[w]); rows of block k at window level m:
+//     row records [grp[gbase[w] + k * (nl + 1) + m], ... + 1), nl = l1 - l0;
+//   externals of (w, k): ext[ext_ptr[w * nc + k] .. ext_ptr[w * nc + k + 1])
+//     as (slot, cell);
+//   row record r: position pos[r] (~position for a row of another band,
+//     which is not stored to global memory), its cell, its slot, and the
+//     slots of its entries eslot[eptr[r] ..] in the entry order of the row.
+struct SweepWindows {
+  int nc = 0, band_rows = 0, slots = 0;  // slots: the most any (window, block) needs
+  bool ok = false;                       // planned for the current schedule
+  int *l0 = nullptr, *l1 = nullptr, *gbase = nullptr, *grp = nullptr, *ext_ptr = nullptr, *ext_slot = nullptr,
+      *ext_cell = nullptr, *pos = nullptr, *cell = nullptr, *slot = nullptr, *eptr = nullptr, *eslot = nullptr;
+  std::vector<int> run_w0;  // first window of each schedule entry (one more entry: the end)
+  std::vector<void*> owned;
 };
 
 struct SweepPlan {
@@ -73,7 +98,12 @@ struct SweepPlan {
   double* pk_val = nullptr;  // [C][kSweepPack]
   double* pk_diag = nullptr; // [C]
   double* pk_dc = nullptr;   // [C]
+  double* pk_rcp = nullptr;  // [C] RN(1 / diagonal)
+  unsigned long long* pk_rx = nullptr;  // [C] recip_fixed(diagonal)
   std::vector<int> host_level_ptr;
+  // host copies of the topology for planning the windowed sweep
+  std::vector<int> host_pos_cell, host_ent_ptr, host_ent_pos;
+  SweepWindows win;
   // chunks of at most 32 consecutive positions inside one level (start,
   // rows), for the dataflow sweep; chunk_ptr[l] = first chunk of level l
   int2* chunks = nullptr;
@@ -111,8 +141,9 @@ struct ImplicitState {
   SweepPlan fwd, bwd;
   int wide_level = 0;  // levels wider than this get a grid launch each
   int engine = 0;      // how a run of narrow levels is swept (SweepEngine)
+  int default_engine = kSweepDataflow;  // the fastest engine the device runs
   int chunk_rows = 32;  // rows per chunk of the per-row-wait sweeps
-  bool cluster8_ok = false, cluster16_ok = false;
+  bool cluster8_ok = false, cluster16_ok = false, window8_ok = false, window16_ok = false;
   DevStatus* status = nullptr;  // the geometry's status word (sweep time-outs)
   // values and vectors (device)
   double *coef = nullptr, *bterm = nullptr, *diag = nullptr, *dclamp = nullptr, *rval = nullptr;
@@ -160,7 +191,7 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
 cudaError_t implicit_set_operator(ImplicitState& st, ScaleVec scale, const double* dt, int dt_per_cell,
                                   cudaStream_t s);
 cudaError_t lusgs_apply(ImplicitState& st, const double* v, double* x, cudaStream_t s);
-void implicit_set_wide_level(ImplicitState& st, int wide, int engine);
+cudaError_t implicit_set_wide_level(ImplicitState& st, int wide, int engine);
 cudaError_t implicit_set_chunk(ImplicitState& st, int rows);
 cudaError_t fd_operator(ImplicitState& st, const ResidualFn& residual1, const double* v, double* out,
                         cudaStream_t s);

@@ -119,6 +119,16 @@ __global__ void __launch_bounds__(kBlock) k_ieee_div_sqrt(long long n, const dou
   }
 }
 
+__global__ void __launch_bounds__(kBlock) k_ieee_div_fma(long long n, const double* __restrict__ a,
+                                                         const double* __restrict__ b, double* __restrict__ quotient) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double d = b[i];
+    const unsigned long long X = recip_fixed(d);
+    quotient[i] = div_rn_fma(a[i], d, div_rn_recip(1.0, d, X), X);
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) k_ieee_mul(long long n, const double* __restrict__ a,
                                                      const double* __restrict__ b, double* __restrict__ product) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -148,6 +158,16 @@ extern "C" int mcfd_ieee_mul(const double* a, const double* b, int64_t n, double
   mcfd::count_launch(1);
   mcfd::k_ieee_mul<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), mcfd::kBlock, 0,
                      static_cast<cudaStream_t>(stream)>>>(n, a, b, product);
+  return cudaGetLastError() == cudaSuccess ? MCFD_OK : MCFD_E_CUDA;
+}
+
+extern "C" int mcfd_ieee_div_fma(const double* a, const double* b, int64_t n, double* quotient, void* stream) {
+  if (n < 0 || (n > 0 && (!a || !b || !quotient))) return MCFD_E_ARG;
+  if (n == 0) return MCFD_OK;
+  const long long blocks = (n + mcfd::kBlock - 1) / mcfd::kBlock;
+  mcfd::count_launch(1);
+  mcfd::k_ieee_div_fma<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), mcfd::kBlock, 0,
+                         static_cast<cudaStream_t>(stream)>>>(n, a, b, quotient);
   return cudaGetLastError() == cudaSuccess ? MCFD_OK : MCFD_E_CUDA;
 }
 

@@ -1,4 +1,4 @@
-// Host check of the integer-pipe division, multiplication, square root, doubling, negation, absolute value and 0 + x
+// Host check of the integer-pipe division (and its reciprocal-candidate form), multiplication, square root, doubling, negation, absolute value and 0 + x
 // (meshcfd_gb300/csrc/mcfd_arith.cuh compiled as plain C++) against the
 // host's IEEE binary64 division and square root, bit for bit.
 //
@@ -60,6 +60,12 @@ static void check(double a, double b) {
   const double q = mcfd::div_rn(a, b), qr = a / b;
   if (!same(q, qr)) {
     if (!g_bad) printf("div %a / %a: got %a expected %a\n", a, b, q, qr);
+    ++g_bad;
+  }
+  const unsigned long long X = mcfd::recip_fixed(b);
+  const double qf = mcfd::div_rn_fma(a, b, mcfd::div_rn_recip(1.0, b, X), X);
+  if (!same(qf, qr)) {
+    if (!g_bad) printf("div (reciprocal candidate) %a / %a: got %a expected %a\n", a, b, qf, qr);
     ++g_bad;
   }
   const double p = mcfd::mul_rn(a, b), pr = a * b;

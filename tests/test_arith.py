@@ -86,6 +86,35 @@ def test_gpu_division_and_root_match_the_fp64_unit(cuda_device):
 
 
 @pytest.mark.gpu
+def test_gpu_reciprocal_candidate_division_matches_the_fp64_unit(cuda_device):
+    """The sweeps' division (reciprocal candidate, exact remainder test,
+    integer-pipe fallback) on the random operands, and on quotients planted
+    next to midpoints of two doubles, where a candidate is most often
+    rejected."""
+    import torch
+    from meshcfd_gb300 import _lib
+
+    lib = _lib.native()
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(11)
+    b_mid = np.ldexp(1.0 + rng.random(1 << 18), rng.integers(-30, 30, 1 << 18))
+    m = np.ldexp(1.0 + rng.random(1 << 18), rng.integers(-8, 8, 1 << 18))
+    a_mid = b_mid * (m + np.ldexp(1.0, np.frexp(m)[1] - 54))  # a / b next to the midpoint above m
+    for seed in (7, 8, None):
+        a_np, b_np = _operands(1 << 20, seed) if seed is not None else (
+            np.concatenate([a_mid, np.nextafter(a_mid, 0.0), np.nextafter(a_mid, np.inf)]), np.tile(b_mid, 3))
+        a = torch.as_tensor(a_np, device=cuda_device)
+        b = torch.as_tensor(b_np, device=cuda_device)
+        q = torch.empty_like(a)
+        assert lib.mcfd_ieee_div_fma(a.data_ptr(), b.data_ptr(), a.numel(), q.data_ptr(), stream) == 0
+        ref = (a / b).cpu().numpy()
+        torch.cuda.synchronize()
+        ok = _same_bits(q.cpu().numpy(), ref)
+        assert ok.all(), (a_np[~ok][:3], b_np[~ok][:3])
+    assert lib.mcfd_ieee_div_fma(None, None, 4, None, stream) == 1
+
+
+@pytest.mark.gpu
 def test_gpu_product_matches_the_fp64_unit(cuda_device):
     import torch
     from meshcfd_gb300 import _lib

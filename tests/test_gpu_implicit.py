@@ -248,7 +248,8 @@ def test_lusgs_schedules_agree_and_match_spsolve(cuda_device, mesh):
     """Every launch schedule of the level-scheduled sweeps (one block with a
     barrier per level, one block whose rows wait only for the rows they read,
     or a cluster of 8 or 16, stepping through narrow levels with their
-    shared-memory rings; grid launches per level; and mixtures) gives the
+    shared-memory rings, either sharing every solution or each block owning
+    a band of cells; grid launches per level; and mixtures) gives the
     same bits, and matches the reference's two spsolve_triangular calls
     (within 1e-12)."""
     import torch
@@ -275,7 +276,8 @@ def test_lusgs_schedules_agree_and_match_spsolve(cuda_device, mesh):
     for wide, engine, chunk in ((0, 1, 0), (0, 2, 0), (0, 3, 0), (0, 4, 0), (0, 5, 0), (7, 5, 0), (0, 6, 0), (0, 6, 3), (7, 6, 0),
                                 (1 << 30, 6, 0), (0, 2, 1), (0, 4, 8), (0, 2, 17),
                                 (0, 8, 0), (0, 16, 0), (1, 8, 0), (7, 1, 0), (7, 2, 0), (7, 3, 5), (7, 8, 0),
-                                (1 << 30, 1, 0), (1 << 30, 2, 0), (1 << 30, 3, 0), (1 << 30, 16, 0)):
+                                (1 << 30, 1, 0), (1 << 30, 2, 0), (1 << 30, 3, 0), (1 << 30, 16, 0),
+                                (0, 7, 0), (0, 9, 0), (7, 7, 0), (1, 9, 0), (1 << 30, 7, 0), (1 << 30, 9, 0)):
         assert dg.lib.mcfd_implicit_set_chunk(dg.handle, chunk) == 0
         rc = dg.lib.mcfd_implicit_set_sweep(dg.handle, wide, engine)
         if engine > 2 and rc == 3:
