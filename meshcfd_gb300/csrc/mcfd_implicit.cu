@@ -119,8 +119,7 @@ struct SweepDev {
   const double* pk_val;
   const double* pk_diag;
   const double* pk_dc;
-  const double* pk_rcp;                 // RN(1 / diagonal)
-  const unsigned long long* pk_rx;      // recip_fixed(diagonal)
+  const double2* pk_row;  // [C][4]: (diagonal, RN(1 / diagonal)), (recip_fixed bits, clamped diagonal), values
   const double* in;
   double* out;
   int backward;
@@ -376,13 +375,14 @@ constexpr int kWinMaxLevels = 32;                // levels per window at most
 constexpr int kWinMaxSlots = 6144;               // shared-memory slots of 4 doubles (192 KiB)
 
 struct WinDev {
-  const int *l0, *l1, *gbase, *grp, *ext_ptr, *ext_slot, *ext_cell, *pos, *cell, *slot, *eptr, *eslot;
+  const int *l0, *l1, *gbase, *grp, *ext_ptr, *ext_slot, *ext_cell, *eslot;
+  const int4* rec;  // [2 per record]: (position, cell, slot | entries << 16, first entry slot), four entry slots
 };
 
 // A row record (the plan's, fixed) and a row's values (the matrix's and the
 // right-hand side's, per sweep).
 struct WinRec {
-  int p0, i, slot, eb;
+  int4 a, b;
 };
 
 struct WinRow {
@@ -395,30 +395,33 @@ struct WinRow {
 };
 
 __device__ __forceinline__ void win_rec(const WinDev& w, int rec, WinRec& Q) {
-  Q.p0 = w.pos[rec];
-  Q.i = w.cell[rec];
-  Q.slot = w.slot[rec];
-  Q.eb = w.eptr[rec];
+  Q.a = w.rec[2 * (size_t)rec];
+  Q.b = w.rec[2 * (size_t)rec + 1];
 }
 
 // loads only (the entry slots are padded, so none depends on the count)
 __device__ __forceinline__ void win_vals(const SweepDev& a, const WinDev& w, const WinRec& Q, int comp, WinRow& R) {
-  R.own = Q.p0 >= 0;
-  R.p = R.own ? Q.p0 : ~Q.p0;
-  R.i = Q.i;
-  R.slot = Q.slot;
-  R.eb = Q.eb;
-  R.n = a.pk_cnt[R.p];
-  R.dg = a.pk_diag[R.p];
-  R.y = a.pk_rcp[R.p];
-  R.rx = a.pk_rx[R.p];
+  R.own = Q.a.x >= 0;
+  R.p = R.own ? Q.a.x : ~Q.a.x;
+  R.i = Q.a.y;
+  R.slot = Q.a.z & 0xffff;
+  R.n = Q.a.z >> 16;
+  R.eb = Q.a.w;
+  R.es[0] = Q.b.x;
+  R.es[1] = Q.b.y;
+  R.es[2] = Q.b.z;
+  R.es[3] = Q.b.w;
+  const double2* row = a.pk_row + 4 * (size_t)R.p;
+  const double2 d0 = row[0], d1 = row[1], d2 = row[2], d3 = row[3];
+  R.dg = d0.x;
+  R.y = d0.y;
+  R.rx = (unsigned long long)__double_as_longlong(d1.x);
+  R.dc = d1.y;
+  R.v[0] = d2.x;
+  R.v[1] = d2.y;
+  R.v[2] = d3.x;
+  R.v[3] = d3.y;
   R.r = a.in[4 * (size_t)R.i + comp];
-  R.dc = a.backward ? a.pk_dc[R.p] : 1.0;
-#pragma unroll
-  for (int k = 0; k < kSweepPack; ++k) {
-    R.v[k] = a.pk_val[(size_t)R.p * kSweepPack + k];
-    R.es[k] = w.eslot[R.eb + k];
-  }
 }
 
 __device__ __forceinline__ void win_solve(const SweepDev& a, const WinDev& w, double* sl, const WinRow& R,
@@ -745,20 +748,28 @@ __global__ void k_pack_rows(int C, const int* __restrict__ pos_cell, const int* 
                             const int* __restrict__ ent_val, const double* __restrict__ rval,
                             const double* __restrict__ diag, const double* __restrict__ dclamp,
                             double* __restrict__ pk_val, double* __restrict__ pk_diag, double* __restrict__ pk_dc,
-                            double* __restrict__ pk_rcp, unsigned long long* __restrict__ pk_rx) {
+                            double2* __restrict__ pk_row) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= C) return;
   const int i = pos_cell[p];
   const int j0 = ent_ptr[p], n = ent_ptr[p + 1] - j0;
+  double v[kSweepPack];
 #pragma unroll
-  for (int k = 0; k < kSweepPack; ++k) pk_val[(size_t)p * kSweepPack + k] = k < n ? rval[ent_val[j0 + k]] : 0.0;
-  const double d = diag[i];
+  for (int k = 0; k < kSweepPack; ++k) {
+    v[k] = k < n ? rval[ent_val[j0 + k]] : 0.0;
+    pk_val[(size_t)p * kSweepPack + k] = v[k];
+  }
+  const double d = diag[i], dc = dclamp[i];
   pk_diag[p] = d;
-  pk_dc[p] = dclamp[i];
-  // the divisor's reciprocals for the windowed sweep's quotients (div_rn_fma)
+  pk_dc[p] = dc;
+  // one 64-byte row for the windowed sweep, with the divisor's reciprocals
+  // for its quotients (div_rn_fma)
   const unsigned long long X = recip_fixed(d);
-  pk_rx[p] = X;
-  pk_rcp[p] = div_rn_recip(1.0, d, X);
+  static_assert(kSweepPack == 4, "the windowed sweep's row holds four values");
+  pk_row[4 * (size_t)p] = make_double2(d, div_rn_recip(1.0, d, X));
+  pk_row[4 * (size_t)p + 1] = make_double2(__longlong_as_double((long long)X), dc);
+  pk_row[4 * (size_t)p + 2] = make_double2(v[0], v[1]);
+  pk_row[4 * (size_t)p + 3] = make_double2(v[2], v[3]);
 }
 
 // ------------------------------------------------------------------ vectors
@@ -1244,7 +1255,7 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
   std::vector<int> lev_of(C);
   for (int l = 0; l < nlev; ++l)
     for (int p = lp[l]; p < lp[l + 1]; ++p) lev_of[p] = l;
-  std::vector<int> l0v, l1v, gbase, grp, ext_ptr{0}, ext_slot, ext_cell, posv, cellv, slotv, eptr, eslot;
+  std::vector<int> l0v, l1v, gbase, grp, ext_ptr{0}, ext_slot, ext_cell, recv, eslot;
   std::vector<int> mark(C, -1), slot_of(C, -1);
   std::vector<std::vector<int>> by_level(kWinMaxLevels);
   std::vector<int> ext;
@@ -1290,23 +1301,26 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
     }
     ext_ptr.push_back((int)ext_slot.size());
     for (int m = 0; m < nl; ++m) {
-      grp.push_back((int)posv.size());
+      grp.push_back((int)(recv.size() / 8));
       std::vector<int>& rows = by_level[m];
       std::sort(rows.begin(), rows.end());
       for (int p : rows) {
         slot_of[p] = sl++;
-        posv.push_back(pos_cell[p] / W.band_rows == k ? p : ~p);
-        cellv.push_back(pos_cell[p]);
-        slotv.push_back(slot_of[p]);
-        eptr.push_back((int)eslot.size());
+        const int n = ent_ptr[p + 1] - ent_ptr[p];
+        recv.push_back(pos_cell[p] / W.band_rows == k ? p : ~p);
+        recv.push_back(pos_cell[p]);
+        recv.push_back(slot_of[p] | (n << 16));
+        recv.push_back((int)eslot.size());
+        for (int q = 0; q < kSweepPack; ++q) recv.push_back(q < n ? slot_of[ent_pos[ent_ptr[p] + q]] : 0);
         for (int j = ent_ptr[p]; j < ent_ptr[p + 1]; ++j) eslot.push_back(slot_of[ent_pos[j]]);
       }
     }
-    grp.push_back((int)posv.size());
+    grp.push_back((int)(recv.size() / 8));
     W.slots = std::max(W.slots, sl);
   };
   W.run_w0.assign(pl.schedule.size() + 1, 0);
   bool ok = true;
+  for (int p = 0; p < C && ok; ++p) ok = ent_ptr[p + 1] - ent_ptr[p] < (1 << 15);  // the record's 16-bit count
   for (size_t si = 0; si < pl.schedule.size() && ok; ++si) {
     W.run_w0[si] = (int)l0v.size();
     const SweepPlan::Launch& run = pl.schedule[si];
@@ -1316,7 +1330,7 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
       for (;;) {
         size_t need = 0;
         for (int k = 0; k < nc; ++k) need = std::max(need, closure(L, L + H, k));
-        if (need <= (size_t)kWinMaxSlots) break;
+        if (need <= (size_t)kWinMaxSlots) break;  // (slots and entry counts also fit 16 bits each)
         if (H == 1) {
           ok = false;
           break;
@@ -1332,7 +1346,6 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
     }
   }
   W.run_w0.back() = (int)l0v.size();
-  eslot.insert(eslot.end(), kSweepPack, 0);  // a row's first kSweepPack slots load unconditionally
   for (size_t si = pl.schedule.size(); si-- > 0;)  // entries without windows: empty ranges
     if (!pl.schedule[si].wavefront) W.run_w0[si] = W.run_w0[si + 1];
   if (!ok) {
@@ -1354,10 +1367,7 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
   put(ext_ptr, &W.ext_ptr);
   put(ext_slot, &W.ext_slot);
   put(ext_cell, &W.ext_cell);
-  put(posv, &W.pos);
-  put(cellv, &W.cell);
-  put(slotv, &W.slot);
-  put(eptr, &W.eptr);
+  put(recv, &W.rec);
   put(eslot, &W.eslot);
   W.ok = e == cudaSuccess;
   return e;
@@ -1575,8 +1585,7 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
     zeros((size_t)C * kSweepPack, &pl->pk_val);
     zeros(C, &pl->pk_diag);
     zeros(C, &pl->pk_dc);
-    zeros(C, &pl->pk_rcp);
-    zeros(C, (double**)&pl->pk_rx);
+    zeros(8 * (size_t)C, (double**)&pl->pk_row);
   }
   zeros(kRedBlocks, &st.partials);
   zeros(64, &st.scalars);
@@ -1710,7 +1719,7 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
     count_launch();
     k_pack_rows<<<blocks_for(st.n_cells), kBlock, 0, s>>>(st.n_cells, pl->pos_cell, pl->ent_ptr, pl->ent_val,
                                                           st.rval, st.diag, st.dclamp, pl->pk_val, pl->pk_diag,
-                                                          pl->pk_dc, pl->pk_rcp, pl->pk_rx);
+                                                          pl->pk_dc, pl->pk_row);
   }
   return cudaGetLastError();
 }
@@ -1718,7 +1727,7 @@ cudaError_t implicit_assemble(ImplicitState& st, const double* P, const double* 
 static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const double* in, double* out, int backward,
                          cudaStream_t s) {
   SweepDev a{pl.level_ptr, pl.pos_cell, pl.ent_ptr, pl.ent_cell, pl.ent_pos, pl.ent_val, st.rval,
-             pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, pl.pk_rcp, pl.pk_rx,
+             pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, pl.pk_row,
              in, out, backward};
   const bool window = st.engine == kSweepWindow8 || st.engine == kSweepWindow16;
   for (size_t si = 0; si < pl.schedule.size(); ++si) {
@@ -1758,8 +1767,8 @@ static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const dou
       if (e != cudaSuccess) return e;
     } else if (l.wavefront && window) {
       const SweepWindows& W = pl.win;
-      const WinDev wd{W.l0,  W.l1,   W.gbase, W.grp,  W.ext_ptr, W.ext_slot,
-                      W.ext_cell, W.pos, W.cell, W.slot, W.eptr,    W.eslot};
+      const WinDev wd{W.l0, W.l1, W.gbase, W.grp, W.ext_ptr, W.ext_slot, W.ext_cell, W.eslot,
+                      reinterpret_cast<const int4*>(W.rec)};
       const int w0 = W.run_w0[si], w1 = W.run_w0[si + 1];
       cudaLaunchConfig_t cfg{};
       cfg.gridDim = dim3(W.nc);

@@ -68,14 +68,15 @@ enum SweepEngine {
 //     row records [grp[gbase[w] + k * (nl + 1) + m], ... + 1), nl = l1 - l0;
 //   externals of (w, k): ext[ext_ptr[w * nc + k] .. ext_ptr[w * nc + k + 1])
 //     as (slot, cell);
-//   row record r: position pos[r] (~position for a row of another band,
-//     which is not stored to global memory), its cell, its slot, and the
-//     slots of its entries eslot[eptr[r] ..] in the entry order of the row.
+//   row record r: rec[8 r ..] = position (~position for a row of another
+//     band, which is not stored to global memory), cell, slot | entries << 16,
+//     the start of its entries' slots in eslot (entry order of the row), and
+//     its first kSweepPack entry slots.
 struct SweepWindows {
   int nc = 0, band_rows = 0, slots = 0;  // slots: the most any (window, block) needs
   bool ok = false;                       // planned for the current schedule
   int *l0 = nullptr, *l1 = nullptr, *gbase = nullptr, *grp = nullptr, *ext_ptr = nullptr, *ext_slot = nullptr,
-      *ext_cell = nullptr, *pos = nullptr, *cell = nullptr, *slot = nullptr, *eptr = nullptr, *eslot = nullptr;
+      *ext_cell = nullptr, *rec = nullptr, *eslot = nullptr;
   std::vector<int> run_w0;  // first window of each schedule entry (one more entry: the end)
   std::vector<void*> owned;
 };
@@ -98,8 +99,7 @@ struct SweepPlan {
   double* pk_val = nullptr;  // [C][kSweepPack]
   double* pk_diag = nullptr; // [C]
   double* pk_dc = nullptr;   // [C]
-  double* pk_rcp = nullptr;  // [C] RN(1 / diagonal)
-  unsigned long long* pk_rx = nullptr;  // [C] recip_fixed(diagonal)
+  double2* pk_row = nullptr; // [C][4] the windowed sweep's row: diagonal, RN(1 / diagonal), recip_fixed(diagonal), clamped diagonal, values
   std::vector<int> host_level_ptr;
   // host copies of the topology for planning the windowed sweep
   std::vector<int> host_pos_cell, host_ent_ptr, host_ent_pos;
