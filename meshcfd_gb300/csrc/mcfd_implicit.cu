@@ -371,7 +371,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_lusgs_cluster(SweepDev a
 // barriers.
 constexpr int kWinThreads = 256;                 // 8 warps: 64 rows of 4 components per pass
 constexpr int kWinRowsPerPass = kWinThreads / 4;
-constexpr int kWinMaxLevels = 32;                // levels per window at most
+#ifndef MCFD_WIN_LEVELS
+#define MCFD_WIN_LEVELS 32
+#endif
+constexpr int kWinMaxLevels = MCFD_WIN_LEVELS;   // levels per window at most (a build option)
 constexpr int kWinMaxSlots = 6144;               // shared-memory slots of 4 doubles (192 KiB)
 
 struct WinDev {
