@@ -355,155 +355,186 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_lusgs_cluster(SweepDev a
 
 // The windowed band sweep (SweepWindows): block k of a thread-block
 // cluster owns a band of consecutive cell ids.  Per window of levels it
-// loads the solutions it needs from before the window into shared-memory
-// slots, then solves, level by level with a block barrier between levels,
-// its own rows and the rows of other bands they depend on inside the window
-// (the same arithmetic on the same inputs: the same bits as their owners').
-// Only the rows a block owns go to global memory; a cluster barrier
-// (release / acquire) at each window's start makes the previous window's
-// rows visible to every block.  Each row is solved by four lanes, one per
-// component (warp w of four holds component w of 32 rows), so a level's
-// critical path holds a row's products and differences per entry once, not
-// four times over in one warp's instruction stream.  The next level's rows
-// (independent of the solutions) are loaded before the block barrier.  The
+// solves, level by level with a block barrier between levels, its own rows
+// and the rows of other bands they depend on inside the window (the same
+// arithmetic on the same inputs: the same bits as their owners'), reading
+// the solutions from before the window ("externals") from global memory
+// once, at the window's start, into shared-memory slots.  Only the rows a
+// block owns go to global memory; a cluster barrier (release / acquire) at
+// each window's start makes the previous window's rows visible to every
+// block.  Everything else a window reads is staged into shared memory by
+// asynchronous copies issued one window ahead: the window's row records
+// (32 bytes: position, cell, slot, entry count, entry slots), its rows'
+// values (64 bytes, k_pack_window_rows after each assembly), its rows'
+// right-hand sides (32 bytes, k_pack_window_rhs before each sweep, times
+// the clamped diagonal in the backward sweep), its externals (slot, cell)
+// and level ranges, each contiguous per (window, block) in the plan.  So a
+// level reads shared memory only.  Each row is solved by four lanes, one
+// per component (warp w of four holds component w of 32 rows), so a level's
+// critical path holds a row's products and differences per entry once.  The
 // arithmetic is sweep_solve's, component by component: the same bits.  No
 // thread waits on a flag; every thread of every block passes the same
 // barriers.
 constexpr int kWinThreads = 256;                 // 8 warps: 64 rows of 4 components per pass
 constexpr int kWinRowsPerPass = kWinThreads / 4;
-#ifndef MCFD_WIN_LEVELS
-#define MCFD_WIN_LEVELS 32
-#endif
-constexpr int kWinMaxLevels = MCFD_WIN_LEVELS;   // levels per window at most (a build option)
-constexpr int kWinMaxSlots = 6144;               // shared-memory slots of 4 doubles (192 KiB)
+constexpr int kWinMaxLevels = 32;                // levels per window at most
+constexpr int kWinMaxSlots = 2048;               // shared-memory solution slots of 4 doubles (64 KiB)
+constexpr int kWinMaxRows = 560;                 // row records per (window, block)
+constexpr int kWinMaxExt = 512;                  // externals per (window, block)
+constexpr int kWinRecBytes = 32, kWinRowBytes = 64, kWinRhsBytes = 32;
+constexpr int kWinStageBytes = kWinMaxRows * (kWinRecBytes + kWinRowBytes + kWinRhsBytes) + kWinMaxExt * 8;
+constexpr int kWinSmemBytes = kWinMaxSlots * 32 + 2 * kWinStageBytes;
+static_assert(kWinSmemBytes + 2 * (kWinMaxLevels + 1) * 4 <= 227 * 1024, "the windowed sweep's shared memory");
 
 struct WinDev {
-  const int *l0, *l1, *gbase, *grp, *ext_ptr, *ext_slot, *ext_cell, *eslot;
-  const int4* rec;  // [2 per record]: (position, cell, slot | entries << 16, first entry slot), four entry slots
+  const int *l0, *l1, *gbase, *grp, *eslot;
+  const int4* stage;    // [window * nc + block]: first record, records, first external, externals
+  const int4* rec;      // [2 per record]
+  const double2* row;   // [4 per record]
+  const double* rhs;    // [4 per record]
+  const int2* ext;      // (slot, cell) per external
 };
 
-// A row record (the plan's, fixed) and a row's values (the matrix's and the
-// right-hand side's, per sweep).
-struct WinRec {
-  int4 a, b;
-};
-
-struct WinRow {
-  int p, i, n, slot, eb;
-  bool own;
-  double r, dc, dg, y;  // y: RN(1 / dg)
-  unsigned long long rx;
-  double v[kSweepPack];
-  int es[kSweepPack];
-};
-
-__device__ __forceinline__ void win_rec(const WinDev& w, int rec, WinRec& Q) {
-  Q.a = w.rec[2 * (size_t)rec];
-  Q.b = w.rec[2 * (size_t)rec + 1];
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// loads only (the entry slots are padded, so none depends on the count)
-__device__ __forceinline__ void win_vals(const SweepDev& a, const WinDev& w, const WinRec& Q, int comp, WinRow& R) {
-  R.own = Q.a.x >= 0;
-  R.p = R.own ? Q.a.x : ~Q.a.x;
-  R.i = Q.a.y;
-  R.slot = Q.a.z & 0xffff;
-  R.n = Q.a.z >> 16;
-  R.eb = Q.a.w;
-  R.es[0] = Q.b.x;
-  R.es[1] = Q.b.y;
-  R.es[2] = Q.b.z;
-  R.es[3] = Q.b.w;
-  const double2* row = a.pk_row + 4 * (size_t)R.p;
-  const double2 d0 = row[0], d1 = row[1], d2 = row[2], d3 = row[3];
-  R.dg = d0.x;
-  R.y = d0.y;
-  R.rx = (unsigned long long)__double_as_longlong(d1.x);
-  R.dc = d1.y;
-  R.v[0] = d2.x;
-  R.v[1] = d2.y;
-  R.v[2] = d3.x;
-  R.v[3] = d3.y;
-  R.r = a.in[4 * (size_t)R.i + comp];
+// One window's staging for this block: row records, values, right-hand
+// sides, externals (buffer at st) and level ranges (gr).
+struct WinStage {
+  int nl, g0;  // levels; index of the first level range in w.grp
+  int4 info;   // first record, records, first external, externals
+};
+
+__device__ __forceinline__ void win_stage_info(const WinDev& w, int win, int rank, int nc, WinStage& S) {
+  const int nl = w.l1[win] - w.l0[win];
+  S.nl = nl;
+  S.g0 = w.gbase[win] + rank * (nl + 1);
+  S.info = w.stage[win * nc + rank];
 }
 
-__device__ __forceinline__ void win_solve(const SweepDev& a, const WinDev& w, double* sl, const WinRow& R,
-                                          int comp) {
-  double acc = a.backward ? R.dc * R.r : R.r;
+__device__ __forceinline__ void win_stage_copy(const WinDev& w, const WinStage& S, unsigned char* st, int* gr) {
+  const int t = (int)threadIdx.x;
+  const int r0 = S.info.x, nr = S.info.y, e0 = S.info.z, ne = S.info.w;
+  for (int c = t; c < 2 * nr; c += kWinThreads)
+    cp_async16(st + 16 * c, reinterpret_cast<const unsigned char*>(w.rec + 2 * (size_t)r0) + 16 * c);
+  unsigned char* row = st + kWinMaxRows * kWinRecBytes;
+  for (int c = t; c < 4 * nr; c += kWinThreads)
+    cp_async16(row + 16 * c, reinterpret_cast<const unsigned char*>(w.row + 4 * (size_t)r0) + 16 * c);
+  unsigned char* rhs = row + kWinMaxRows * kWinRowBytes;
+  for (int c = t; c < 2 * nr; c += kWinThreads)
+    cp_async16(rhs + 16 * c, reinterpret_cast<const unsigned char*>(w.rhs + 4 * (size_t)r0) + 16 * c);
+  unsigned char* ext = rhs + kWinMaxRows * kWinRhsBytes;
+  for (int c = t; c < ne; c += kWinThreads) cp_async8(ext + 8 * c, w.ext + e0 + c);
+  if (t <= S.nl) cp_async4(gr + t, w.grp + S.g0 + t);
+}
+
+__device__ __forceinline__ void win_solve(const SweepDev& a, const WinDev& w, double* sl, const unsigned char* st,
+                                          int r, int comp) {
+  const int4* rec = reinterpret_cast<const int4*>(st);
+  const double2* row = reinterpret_cast<const double2*>(st + kWinMaxRows * kWinRecBytes);
+  const double* rhs = reinterpret_cast<const double*>(st + kWinMaxRows * (kWinRecBytes + kWinRowBytes));
+  const int4 A = rec[2 * r], B = rec[2 * r + 1];
+  const double2 d0 = row[4 * r], d2 = row[4 * r + 2], d3 = row[4 * r + 3];
+  const double rx_bits = row[4 * r + 1].x;
+  const int n = A.z >> 16, slot = A.z & 0xffff;
+  double acc = rhs[4 * r + comp];
+  const int es[kSweepPack] = {B.x, B.y, B.z, B.w};
+  const double v[kSweepPack] = {d2.x, d2.y, d3.x, d3.y};
 #pragma unroll
   for (int k = 0; k < kSweepPack; ++k)
-    if (k < R.n) acc = acc - R.v[k] * sl[4 * R.es[k] + comp];
-  if (R.n > kSweepPack) {  // the rest of a long row: values from the CSR, slots from the record
-    const int j0 = a.ent_ptr[R.p];
-    for (int k = kSweepPack; k < R.n; ++k) acc = acc - a.rval[a.ent_val[j0 + k]] * sl[4 * w.eslot[R.eb + k] + comp];
+    if (k < n) acc = acc - v[k] * sl[4 * es[k] + comp];
+  if (n > kSweepPack) {  // the rest of a long row: values from the CSR, slots from the plan
+    const int p = A.x >= 0 ? A.x : ~A.x;
+    const int j0 = a.ent_ptr[p];
+    for (int k = kSweepPack; k < n; ++k) acc = acc - a.rval[a.ent_val[j0 + k]] * sl[4 * w.eslot[A.w + k] + comp];
   }
   // the quotient from the row's reciprocal: the same bits as div_rn in
   // fewer dependent steps (div_rn_fma), the level's critical path
-  const double res = div_rn_fma(acc, R.dg, R.y, R.rx);
-  sl[4 * R.slot + comp] = res;
-  if (R.own) a.out[4 * (size_t)R.i + comp] = res;
+  const double res = div_rn_fma(acc, d0.x, d0.y, (unsigned long long)__double_as_longlong(rx_bits));
+  sl[4 * slot + comp] = res;
+  if (A.x >= 0) a.out[4 * (size_t)A.y + comp] = res;
 }
 
 template <int NC>
 __global__ void __launch_bounds__(kWinThreads, 1) k_lusgs_window(SweepDev a, WinDev w, int w0, int w1) {
-  extern __shared__ double sl[];  // [slots][4]
-  __shared__ int grp[kWinMaxLevels + 1];  // this block's level ranges in the window
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* sl = reinterpret_cast<double*>(smem);  // [kWinMaxSlots][4]
+  unsigned char* stg = smem + kWinMaxSlots * 32;  // two staging buffers
+  __shared__ int grp[2][kWinMaxLevels + 1];      // level ranges (record indices) of the staged windows
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int comp = ((int)threadIdx.x >> 5) & 3;
   const int rl = (((int)threadIdx.x >> 7) << 5) | ((int)threadIdx.x & 31);  // row of the pass
+  WinStage cur, nxt;
+  win_stage_info(w, w0, rank, NC, cur);
+  win_stage_copy(w, cur, stg, grp[0]);
+  cp_async_commit();
+  if (w0 + 1 < w1) win_stage_info(w, w0 + 1, rank, NC, nxt);
   for (int win = w0; win < w1; ++win) {
-    const int nl = w.l1[win] - w.l0[win];
-    const int g0 = w.gbase[win] + rank * (nl + 1);
-    if ((int)threadIdx.x <= nl) grp[threadIdx.x] = w.grp[g0 + threadIdx.x];
-    __syncthreads();
-    // a software pipeline over the window's levels: while level m is solved,
-    // the values of level m + 2 and the records of level m + 3 are loaded
-    // (a load uses only registers filled at least a level earlier, so no
-    // load waits on another in flight; the empty asm statements keep the
-    // compiler from sinking the loads to their uses)
-    auto in_level = [&](int m) { return m < nl && grp[m] + rl < grp[m + 1]; };
-    WinRec Q2, Q3;
-    WinRow cur, v1, v2;
-    bool h0 = in_level(0), h1 = in_level(1), q2 = in_level(2), q3 = false;
-    {
-      WinRec Q;
-      if (h0) {
-        win_rec(w, grp[0] + rl, Q);
-        win_vals(a, w, Q, comp, cur);
-      }
-      if (h1) {
-        win_rec(w, grp[1] + rl, Q);
-        win_vals(a, w, Q, comp, v1);
-      }
-      if (q2) win_rec(w, grp[2] + rl, Q2);
+    const int buf = (win - w0) & 1;
+    const unsigned char* st = stg + buf * kWinStageBytes;
+    cp_async_wait<0>();  // this window's copies have landed
+    cluster.sync();      // every thread's copies are visible; the rows solved before this window are in global memory
+    const int2* ext = reinterpret_cast<const int2*>(st + kWinMaxRows * (kWinRecBytes + kWinRowBytes + kWinRhsBytes));
+    for (int x = rl; x < cur.info.w; x += kWinRowsPerPass) {
+      const int2 e = ext[x];
+      sl[4 * e.x + comp] = __ldcg(a.out + 4 * (size_t)e.y + comp);
     }
-    cluster.sync();  // the rows every block solved before this window are in global memory
-    for (int x = w.ext_ptr[win * NC + rank] + rl, x1 = w.ext_ptr[win * NC + rank + 1]; x < x1; x += kWinRowsPerPass)
-      sl[4 * w.ext_slot[x] + comp] = __ldcg(a.out + 4 * (size_t)w.ext_cell[x] + comp);
+    // the next window's staging, into the buffer the previous window read
+    // (every thread passed that window's last barrier), in flight while this
+    // window is solved
+    WinStage after;
+    if (win + 1 < w1) {
+      win_stage_copy(w, nxt, stg + (buf ^ 1) * kWinStageBytes, grp[buf ^ 1]);
+      cp_async_commit();
+      if (win + 2 < w1) win_stage_info(w, win + 2, rank, NC, after);
+    }
     __syncthreads();
-    for (int m = 0; m < nl; ++m) {
-      q3 = in_level(m + 3);
-      if (q3) win_rec(w, grp[m + 3] + rl, Q3);
-      if (q2) win_vals(a, w, Q2, comp, v2);
-      asm volatile("" ::: "memory");
-      if (h0) win_solve(a, w, sl, cur, comp);
-      for (int r = grp[m] + rl + kWinRowsPerPass; r < grp[m + 1]; r += kWinRowsPerPass) {  // more rows than one pass
-        WinRec Qx;
-        WinRow X;
-        win_rec(w, r, Qx);
-        win_vals(a, w, Qx, comp, X);
-        win_solve(a, w, sl, X, comp);
-      }
+    const int r0 = cur.info.x;
+    for (int m = 0; m < cur.nl; ++m) {
+      for (int r = grp[buf][m] - r0 + rl, r1 = grp[buf][m + 1] - r0; r < r1; r += kWinRowsPerPass)
+        win_solve(a, w, sl, st, r, comp);
       __syncthreads();
-      cur = v1;
-      h0 = h1;
-      v1 = v2;
-      h1 = q2;
-      Q2 = Q3;
-      q2 = q3;
     }
+    cur = nxt;
+    nxt = after;
   }
+}
+
+// Before a windowed sweep: each window record's 64-byte row (its
+// position's, as the last assembly left it) and its right-hand side, times
+// the clamped diagonal in the backward sweep (sweep_load's r).
+__global__ void k_pack_window(int n, const int4* __restrict__ rec, const double2* __restrict__ pk_row,
+                              const double* __restrict__ in, int backward, double2* __restrict__ row,
+                              double* __restrict__ rhs) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int4 A = rec[2 * (size_t)r];
+  const int p = A.x >= 0 ? A.x : ~A.x;
+  double2 q[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    q[k] = pk_row[4 * (size_t)p + k];
+    row[4 * (size_t)r + k] = q[k];
+  }
+  const St4 v = ld4(in + 4 * (size_t)A.y);
+  const double dc = q[1].y;
+  st4(rhs + 4 * (size_t)r, backward ? St4{dc * v.a, dc * v.b, dc * v.c, dc * v.d} : v);
 }
 
 // The same sweep in one block without a barrier per level: the rows are cut
@@ -1236,10 +1267,11 @@ cudaError_t implicit_set_chunk(ImplicitState& st, int rows) {
 
 // Plans the windowed band sweep of pl's current schedule for a cluster of nc
 // blocks (SweepWindows).  Each single-block run of the schedule is cut into
-// windows of at most kWinMaxLevels levels, fewer where a block's rows,
-// the rows they depend on inside the window and the rows read from before
-// it would not fit kWinMaxSlots; ok stays false when one level alone does
-// not fit (the sweep then takes the default engine).
+// windows of at most kWinMaxLevels levels, fewer where a block's rows, the
+// rows they depend on inside the window and the rows read from before it
+// would not fit the shared-memory slots or staging buffers; ok stays false
+// when one level alone does not fit (the sweep then takes the per-row-wait
+// engine).
 static void free_windows(SweepWindows& W) {
   for (void* q : W.owned) cudaFree(q);
   W = SweepWindows{};
@@ -1258,14 +1290,14 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
   std::vector<int> lev_of(C);
   for (int l = 0; l < nlev; ++l)
     for (int p = lp[l]; p < lp[l + 1]; ++p) lev_of[p] = l;
-  std::vector<int> l0v, l1v, gbase, grp, ext_ptr{0}, ext_slot, ext_cell, recv, eslot;
+  std::vector<int> l0v, l1v, gbase, grp, stage, recv, eslot, extv;
   std::vector<int> mark(C, -1), slot_of(C, -1);
   std::vector<std::vector<int>> by_level(kWinMaxLevels);
   std::vector<int> ext;
   int stamp = 0;
   // the closure of block k's rows in window [L0, L1): its rows and the rows
   // they depend on inside the window (by_level), the positions before the
-  // window they read (ext); returns the slots it needs
+  // window they read (ext); whether it fits the slots and staging buffers
   auto closure = [&](int L0, int L1, int k) {
     ++stamp;
     const int base = lp[L0], nl = L1 - L0;
@@ -1288,21 +1320,22 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
           else ext.push_back(q);
         }
       }
-    size_t n = ext.size();
-    for (int m = 0; m < nl; ++m) n += by_level[m].size();
-    return n;
+    size_t rows = 0;
+    for (int m = 0; m < nl; ++m) rows += by_level[m].size();
+    return rows + ext.size() <= (size_t)kWinMaxSlots && rows <= (size_t)kWinMaxRows &&
+           ext.size() <= (size_t)kWinMaxExt;
   };
   auto emit = [&](int L0, int L1, int k) {
     const int nl = L1 - L0;
     closure(L0, L1, k);
     std::sort(ext.begin(), ext.end());
     int sl = 0;
+    const int r0 = (int)(recv.size() / 8), e0 = (int)(extv.size() / 2);
     for (int q : ext) {
-      slot_of[q] = sl;
-      ext_slot.push_back(sl++);
-      ext_cell.push_back(pos_cell[q]);
+      slot_of[q] = sl++;
+      extv.push_back(slot_of[q]);
+      extv.push_back(pos_cell[q]);
     }
-    ext_ptr.push_back((int)ext_slot.size());
     for (int m = 0; m < nl; ++m) {
       grp.push_back((int)(recv.size() / 8));
       std::vector<int>& rows = by_level[m];
@@ -1319,7 +1352,10 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
       }
     }
     grp.push_back((int)(recv.size() / 8));
-    W.slots = std::max(W.slots, sl);
+    stage.push_back(r0);
+    stage.push_back((int)(recv.size() / 8) - r0);
+    stage.push_back(e0);
+    stage.push_back((int)(extv.size() / 2) - e0);
   };
   W.run_w0.assign(pl.schedule.size() + 1, 0);
   bool ok = true;
@@ -1331,14 +1367,14 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
     for (int L = run.l0; L < run.l1 && ok;) {
       int H = std::min(kWinMaxLevels, run.l1 - L);
       for (;;) {
-        size_t need = 0;
-        for (int k = 0; k < nc; ++k) need = std::max(need, closure(L, L + H, k));
-        if (need <= (size_t)kWinMaxSlots) break;  // (slots and entry counts also fit 16 bits each)
+        bool fits = true;
+        for (int k = 0; k < nc && fits; ++k) fits = closure(L, L + H, k);
+        if (fits) break;
         if (H == 1) {
           ok = false;
           break;
         }
-        H = std::max(1, H / 2);
+        H = std::max(1, H * 3 / 4);
       }
       if (!ok) break;
       l0v.push_back(L);
@@ -1355,10 +1391,11 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
     free_windows(pl.win);
     return cudaSuccess;
   }
+  W.n_records = (int)(recv.size() / 8);
   cudaError_t e = cudaSuccess;
   auto put = [&](const std::vector<int>& v, int** dst) {
     if (e != cudaSuccess) return;
-    e = cudaMalloc((void**)dst, std::max<size_t>(v.size(), 1) * sizeof(int));
+    e = cudaMalloc((void**)dst, std::max<size_t>(v.size(), 4) * sizeof(int));
     if (e != cudaSuccess) return;
     W.owned.push_back(*dst);
     if (!v.empty()) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice);
@@ -1367,11 +1404,16 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
   put(l1v, &W.l1);
   put(gbase, &W.gbase);
   put(grp, &W.grp);
-  put(ext_ptr, &W.ext_ptr);
-  put(ext_slot, &W.ext_slot);
-  put(ext_cell, &W.ext_cell);
+  put(stage, &W.stage);
   put(recv, &W.rec);
   put(eslot, &W.eslot);
+  put(extv, &W.ext);
+  for (double** dst : {&W.row, &W.rhs}) {
+    if (e != cudaSuccess) break;
+    const size_t per = dst == &W.row ? 8 : 4;  // doubles per record
+    e = cudaMalloc((void**)dst, std::max<size_t>((size_t)W.n_records * per, 4) * sizeof(double));
+    if (e == cudaSuccess) W.owned.push_back(*dst);
+  }
   W.ok = e == cudaSuccess;
   return e;
 }
@@ -1640,7 +1682,7 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
       cudaFuncSetAttribute(k_lusgs_cluster<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
   // the windowed band sweeps: whether a cluster of 8 / 16 such blocks fits the device
   auto window_fits = [](auto kernel, int nc) {
-    const int smem = kWinMaxSlots * 4 * (int)sizeof(double);
+    const int smem = kWinSmemBytes;
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
       return false;
     if (nc > kPortableCluster &&
@@ -1733,6 +1775,12 @@ static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const dou
              pl.pk_cnt, pl.pk_pos, pl.pk_cell, pl.pk_val, pl.pk_diag, pl.pk_dc, pl.pk_row,
              in, out, backward};
   const bool window = st.engine == kSweepWindow8 || st.engine == kSweepWindow16;
+  if (window && pl.win.ok && pl.win.n_records > 0) {
+    count_launch();
+    k_pack_window<<<blocks_for(pl.win.n_records), kBlock, 0, s>>>(
+        pl.win.n_records, reinterpret_cast<const int4*>(pl.win.rec), pl.pk_row, in, backward,
+        reinterpret_cast<double2*>(pl.win.row), pl.win.rhs);
+  }
   for (size_t si = 0; si < pl.schedule.size(); ++si) {
     const SweepPlan::Launch& l = pl.schedule[si];
     count_launch();
@@ -1770,13 +1818,21 @@ static cudaError_t sweep(const SweepPlan& pl, const ImplicitState& st, const dou
       if (e != cudaSuccess) return e;
     } else if (l.wavefront && window) {
       const SweepWindows& W = pl.win;
-      const WinDev wd{W.l0, W.l1, W.gbase, W.grp, W.ext_ptr, W.ext_slot, W.ext_cell, W.eslot,
-                      reinterpret_cast<const int4*>(W.rec)};
+      const WinDev wd{W.l0,
+                      W.l1,
+                      W.gbase,
+                      W.grp,
+                      W.eslot,
+                      reinterpret_cast<const int4*>(W.stage),
+                      reinterpret_cast<const int4*>(W.rec),
+                      reinterpret_cast<const double2*>(W.row),
+                      W.rhs,
+                      reinterpret_cast<const int2*>(W.ext)};
       const int w0 = W.run_w0[si], w1 = W.run_w0[si + 1];
       cudaLaunchConfig_t cfg{};
       cfg.gridDim = dim3(W.nc);
       cfg.blockDim = dim3(kWinThreads);
-      cfg.dynamicSmemBytes = (size_t)std::max(W.slots, 1) * 4 * sizeof(double);
+      cfg.dynamicSmemBytes = kWinSmemBytes;
       cfg.stream = s;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;

@@ -63,20 +63,26 @@ enum SweepEngine {
 // block k solves its own rows and every row of another band they depend on
 // inside the window (recomputed, the same bits), reading the rows solved
 // before the window ("externals") from global memory once, at the window's
-// start, into shared-memory slots.
-//   windows w: levels [l0[w], l1[w]); rows of block k at window level m:
-//     row records [grp[gbase[w] + k * (nl + 1) + m], ... + 1), nl = l1 - l0;
-//   externals of (w, k): ext[ext_ptr[w * nc + k] .. ext_ptr[w * nc + k + 1])
-//     as (slot, cell);
+// start, into shared-memory slots.  All of a (window, block)'s data is
+// contiguous, so that it can be staged into shared memory in a few copies:
+//   windows w: levels [l0[w], l1[w]); stage[w * nc + k] = (first record,
+//     records, first external, externals) of block k;
+//   level ranges: grp[gbase[w] + k * (nl + 1) + m], m = 0..nl, record
+//     indices, nl = l1 - l0;
 //   row record r: rec[8 r ..] = position (~position for a row of another
 //     band, which is not stored to global memory), cell, slot | entries << 16,
 //     the start of its entries' slots in eslot (entry order of the row), and
-//     its first kSweepPack entry slots.
+//     its first kSweepPack entry slots;
+//   row[r] (64 bytes, refreshed after each assembly) and rhs[r] (32 bytes,
+//     refreshed before each sweep): the record's position's values and its
+//     right-hand side;
+//   ext[e] = (slot, cell) of an external.
 struct SweepWindows {
-  int nc = 0, band_rows = 0, slots = 0;  // slots: the most any (window, block) needs
-  bool ok = false;                       // planned for the current schedule
-  int *l0 = nullptr, *l1 = nullptr, *gbase = nullptr, *grp = nullptr, *ext_ptr = nullptr, *ext_slot = nullptr,
-      *ext_cell = nullptr, *rec = nullptr, *eslot = nullptr;
+  int nc = 0, band_rows = 0, n_records = 0;
+  bool ok = false;  // planned for the current schedule
+  int *l0 = nullptr, *l1 = nullptr, *gbase = nullptr, *grp = nullptr, *stage = nullptr, *rec = nullptr,
+      *eslot = nullptr, *ext = nullptr;
+  double *row = nullptr, *rhs = nullptr;
   std::vector<int> run_w0;  // first window of each schedule entry (one more entry: the end)
   std::vector<void*> owned;
 };
