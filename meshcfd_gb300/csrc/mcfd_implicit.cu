@@ -1643,7 +1643,7 @@ cudaError_t implicit_build(ImplicitState& st, const ImplicitTopology& t) {
                                                  (int)kRingBytes);
   // Measured on the 512 x 256 bump (767 levels of at most 256 rows), one
   // LU-SGS application takes 3.20 ms in one block with per-row waits, 4.46 /
-  // 4.82 ms in a cluster of 8 / 16 sharing every solution, and 1.68 / 1.52 ms
+  // 4.82 ms in a cluster of 8 / 16 sharing every solution, and 1.82 / 1.25 ms
   // in the windowed band sweep on a cluster of 8 / 16, the default where the
   // device runs it (set after the cluster checks below).
   st.engine = kDefaultEngine;
