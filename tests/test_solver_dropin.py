@@ -125,3 +125,52 @@ def test_patched_implicit_step_matches_the_oracle(cuda_device):
         dropin.uninstall(module, originals)
     np.testing.assert_array_equal(used, used_ref)
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def _checking_module(check):
+    """A stand-in whose ``solve_case`` runs ``check`` (the reference's
+    prologue) and then builds the geometry, as solver.py:193-379 does."""
+    calls = []
+
+    def build(mesh, case):
+        calls.append("build")
+        return "geometry"
+
+    def solve_case(case, start_time=0.0, step_offset=0, solution_interval=1):
+        check(case, start_time, step_offset, solution_interval)
+        module._build_geometry(case.mesh, case)
+        raise AssertionError("the reference loop ran past its geometry build")
+
+    module = types.SimpleNamespace(SolverError=_SolverError, _build_geometry=build, solve_case=solve_case)
+    return module, build, calls
+
+
+def test_the_hbm_loop_runs_the_reference_checks_and_restores_the_builder():
+    """dropin.solve_case's prologue: the reference's own checks raise its
+    SolverError with its message; a case that passes them stops at the
+    geometry build, which does not run; the module's builder is the
+    reference's again either way."""
+    from meshcfd_gb300 import dropin
+
+    def check(case, start_time, step_offset, solution_interval):
+        if solution_interval <= 0:
+            raise _SolverError("Solution output interval must be a positive integer.")
+
+    module, build, calls = _checking_module(check)
+    case = types.SimpleNamespace(mesh="mesh")
+    with pytest.raises(_SolverError, match="Solution output interval"):
+        dropin._reference_checks(module, case, 0.0, 0, 0)
+    assert module._build_geometry is build and calls == []
+    assert dropin._reference_checks(module, case, 0.0, 0, 1) is None
+    assert module._build_geometry is build and calls == []
+
+
+def test_the_hbm_loop_refuses_a_reference_that_skips_its_geometry_build():
+    from meshcfd_gb300 import dropin
+
+    module = types.SimpleNamespace(SolverError=_SolverError, _build_geometry=lambda mesh, case: None,
+                                   solve_case=lambda case, **kw: None)
+    before = module._build_geometry
+    with pytest.raises(RuntimeError, match="returned before its geometry build"):
+        dropin._reference_checks(module, types.SimpleNamespace(mesh="mesh"), 0.0, 0, 1)
+    assert module._build_geometry is before
