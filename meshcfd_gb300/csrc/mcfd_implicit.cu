@@ -25,6 +25,7 @@
 
 #include "mcfd_device.cuh"
 #include "mcfd_implicit.h"
+#include "mcfd_window_plan.h"
 
 namespace cg = cooperative_groups;
 
@@ -1280,118 +1281,16 @@ static void free_windows(SweepWindows& W) {
 static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
   free_windows(pl.win);
   SweepWindows& W = pl.win;
-  W.nc = nc;
-  W.band_rows = std::max(1, (C + nc - 1) / nc);
-  const std::vector<int>& lp = pl.host_level_ptr;
-  const std::vector<int>& pos_cell = pl.host_pos_cell;
-  const std::vector<int>& ent_ptr = pl.host_ent_ptr;
-  const std::vector<int>& ent_pos = pl.host_ent_pos;
-  const int nlev = (int)lp.size() - 1;
-  std::vector<int> lev_of(C);
-  for (int l = 0; l < nlev; ++l)
-    for (int p = lp[l]; p < lp[l + 1]; ++p) lev_of[p] = l;
-  std::vector<int> l0v, l1v, gbase, grp, stage, recv, eslot, extv;
-  std::vector<int> mark(C, -1), slot_of(C, -1);
-  std::vector<std::vector<int>> by_level(kWinMaxLevels);
-  std::vector<int> ext;
-  int stamp = 0;
-  // the closure of block k's rows in window [L0, L1): its rows and the rows
-  // they depend on inside the window (by_level), the positions before the
-  // window they read (ext); whether it fits the slots and staging buffers
-  auto closure = [&](int L0, int L1, int k) {
-    ++stamp;
-    const int base = lp[L0], nl = L1 - L0;
-    for (int m = 0; m < nl; ++m) by_level[m].clear();
-    ext.clear();
-    for (int m = 0; m < nl; ++m)
-      for (int p = lp[L0 + m]; p < lp[L0 + m + 1]; ++p)
-        if (pos_cell[p] / W.band_rows == k) {
-          mark[p] = stamp;
-          by_level[m].push_back(p);
-        }
-    for (int m = nl - 1; m >= 0; --m)  // dependencies lie on lower levels
-      for (size_t x = 0; x < by_level[m].size(); ++x) {
-        const int p = by_level[m][x];
-        for (int j = ent_ptr[p]; j < ent_ptr[p + 1]; ++j) {
-          const int q = ent_pos[j];
-          if (mark[q] == stamp) continue;
-          mark[q] = stamp;
-          if (q >= base) by_level[lev_of[q] - L0].push_back(q);
-          else ext.push_back(q);
-        }
-      }
-    size_t rows = 0;
-    for (int m = 0; m < nl; ++m) rows += by_level[m].size();
-    return rows + ext.size() <= (size_t)kWinMaxSlots && rows <= (size_t)kWinMaxRows &&
-           ext.size() <= (size_t)kWinMaxExt;
-  };
-  auto emit = [&](int L0, int L1, int k) {
-    const int nl = L1 - L0;
-    closure(L0, L1, k);
-    std::sort(ext.begin(), ext.end());
-    int sl = 0;
-    const int r0 = (int)(recv.size() / 8), e0 = (int)(extv.size() / 2);
-    for (int q : ext) {
-      slot_of[q] = sl++;
-      extv.push_back(slot_of[q]);
-      extv.push_back(pos_cell[q]);
-    }
-    for (int m = 0; m < nl; ++m) {
-      grp.push_back((int)(recv.size() / 8));
-      std::vector<int>& rows = by_level[m];
-      std::sort(rows.begin(), rows.end());
-      for (int p : rows) {
-        slot_of[p] = sl++;
-        const int n = ent_ptr[p + 1] - ent_ptr[p];
-        recv.push_back(pos_cell[p] / W.band_rows == k ? p : ~p);
-        recv.push_back(pos_cell[p]);
-        recv.push_back(slot_of[p] | (n << 16));
-        recv.push_back((int)eslot.size());
-        for (int q = 0; q < kSweepPack; ++q) recv.push_back(q < n ? slot_of[ent_pos[ent_ptr[p] + q]] : 0);
-        for (int j = ent_ptr[p]; j < ent_ptr[p + 1]; ++j) eslot.push_back(slot_of[ent_pos[j]]);
-      }
-    }
-    grp.push_back((int)(recv.size() / 8));
-    stage.push_back(r0);
-    stage.push_back((int)(recv.size() / 8) - r0);
-    stage.push_back(e0);
-    stage.push_back((int)(extv.size() / 2) - e0);
-  };
-  W.run_w0.assign(pl.schedule.size() + 1, 0);
-  bool ok = true;
-  for (int p = 0; p < C && ok; ++p) ok = ent_ptr[p + 1] - ent_ptr[p] < (1 << 15);  // the record's 16-bit count
-  for (size_t si = 0; si < pl.schedule.size() && ok; ++si) {
-    W.run_w0[si] = (int)l0v.size();
-    const SweepPlan::Launch& run = pl.schedule[si];
-    if (!run.wavefront) continue;
-    for (int L = run.l0; L < run.l1 && ok;) {
-      int H = std::min(kWinMaxLevels, run.l1 - L);
-      for (;;) {
-        bool fits = true;
-        for (int k = 0; k < nc && fits; ++k) fits = closure(L, L + H, k);
-        if (fits) break;
-        if (H == 1) {
-          ok = false;
-          break;
-        }
-        H = std::max(1, H * 3 / 4);
-      }
-      if (!ok) break;
-      l0v.push_back(L);
-      l1v.push_back(L + H);
-      gbase.push_back((int)grp.size());
-      for (int k = 0; k < nc; ++k) emit(L, L + H, k);
-      L += H;
-    }
-  }
-  W.run_w0.back() = (int)l0v.size();
-  for (size_t si = pl.schedule.size(); si-- > 0;)  // entries without windows: empty ranges
-    if (!pl.schedule[si].wavefront) W.run_w0[si] = W.run_w0[si + 1];
-  if (!ok) {
-    free_windows(pl.win);
-    return cudaSuccess;
-  }
-  W.n_records = (int)(recv.size() / 8);
+  std::vector<int> runs;
+  for (const SweepPlan::Launch& l : pl.schedule) runs.insert(runs.end(), {l.wavefront, l.l0, l.l1});
+  WindowPlanHost H;
+  const WindowLimits lim{kWinMaxLevels, kWinMaxSlots, kWinMaxRows, kWinMaxExt};
+  if (!plan_windows_host(pl.host_level_ptr, pl.host_pos_cell, pl.host_ent_ptr, pl.host_ent_pos, runs, C, nc, lim, H))
+    return cudaSuccess;  // no plan: the sweep takes the per-row-wait engine
+  W.nc = H.nc;
+  W.band_rows = H.band_rows;
+  W.n_records = H.n_records;
+  W.run_w0 = H.run_w0;
   cudaError_t e = cudaSuccess;
   auto put = [&](const std::vector<int>& v, int** dst) {
     if (e != cudaSuccess) return;
@@ -1400,14 +1299,14 @@ static cudaError_t plan_windows(SweepPlan& pl, int C, int nc) {
     W.owned.push_back(*dst);
     if (!v.empty()) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice);
   };
-  put(l0v, &W.l0);
-  put(l1v, &W.l1);
-  put(gbase, &W.gbase);
-  put(grp, &W.grp);
-  put(stage, &W.stage);
-  put(recv, &W.rec);
-  put(eslot, &W.eslot);
-  put(extv, &W.ext);
+  put(H.l0, &W.l0);
+  put(H.l1, &W.l1);
+  put(H.gbase, &W.gbase);
+  put(H.grp, &W.grp);
+  put(H.stage, &W.stage);
+  put(H.rec, &W.rec);
+  put(H.eslot, &W.eslot);
+  put(H.ext, &W.ext);
   for (double** dst : {&W.row, &W.rhs}) {
     if (e != cudaSuccess) break;
     const size_t per = dst == &W.row ? 8 : 4;  // doubles per record
