@@ -366,12 +366,12 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_lusgs_cluster(SweepDev a
 // block.  Everything else a window reads is staged into shared memory by
 // asynchronous copies issued one window ahead: the window's row records
 // (32 bytes: position, cell, slot, entry count, entry slots), its rows'
-// values (64 bytes, k_pack_window_rows after each assembly), its rows'
-// right-hand sides (32 bytes, k_pack_window_rhs before each sweep, times
-// the clamped diagonal in the backward sweep), its externals (slot, cell)
-// and level ranges, each contiguous per (window, block) in the plan.  So a
-// level reads shared memory only.  Each row is solved by four lanes, one
-// per component (warp w of four holds component w of 32 rows), so a level's
+// values (64 bytes) and right-hand sides (32 bytes, times the clamped
+// diagonal in the backward sweep), both copied per record by k_pack_window
+// before each sweep, its externals (slot, cell) and level ranges, each
+// contiguous per (window, block) in the plan.  So a level reads shared
+// memory only.  Each row is solved by four lanes, one per component (warps
+// 4 h + c hold component c of rows 32 h .. 32 h + 31), so a level's
 // critical path holds a row's products and differences per entry once.  The
 // arithmetic is sweep_solve's, component by component: the same bits.  No
 // thread waits on a flag; every thread of every block passes the same
